@@ -1,0 +1,264 @@
+/*
+ * pierce_capi.h — C ABI of the GB300 (sm_103a) mesh spatial-join library.
+ *
+ * The reference has no shared library: its GPU seam is a set of launch
+ * parameter structs copied to the device before each optixLaunch plus a few
+ * extern "C" helpers.  Each entry point below replaces one of them (paths
+ * relative to the reference project root):
+ *
+ *   pierce_dataset_create / pierce_dataset_build
+ *       <- GeometryUploader::upload  pierce/query/src/geometry/GeometryUploader.cpp:12-34
+ *          PrecomputedEdgeData::uploadFromGeometry
+ *                                    pierce/query/src/geometry/PrecomputedEdgeData.cpp:5-29
+ *          OptixAccelerationStructure::build
+ *                                    pierce/query/src/optix/OptixAccelerationStructure.cpp:14-68
+ *   pierce_launch_edge_rays
+ *       <- MeshOverlapEdgesLauncher::launchMesh1ToMesh2 / launchMesh2ToMesh1
+ *                                    pierce/query/src/raytracing/MeshOverlapEdgesLauncher.cpp:140-154
+ *          (device program __raygen__mesh_overlap_edges,
+ *                                    pierce/query/src/cuda/mesh_overlap_edges.cu:105-208;
+ *           params MeshOverlapEdgesLaunchParams :12-42)
+ *   pierce_launch_parity
+ *       <- MeshIntersectionLauncher::launchContainmentMesh1ToMesh2/2To1
+ *                                    pierce/query/src/raytracing/MeshIntersectionLauncher.cpp:242-283
+ *          MeshContainmentLauncher::launchPointInMesh
+ *                                    pierce/query/src/raytracing/MeshContainmentLauncher.cpp:195-213
+ *   pierce_exclusive_scan
+ *       <- exclusive_scan_gpu        pierce/query/src/cuda/scan_utils.h:6-9, scan_utils.cu:11-28
+ *   pierce_merge_and_deduplicate_pairs
+ *       <- merge_and_deduplicate_pairs_gpu
+ *                                    pierce/query/src/cuda/mesh_query_deduplication.h:6-18,
+ *                                    mesh_query_deduplication.cu:94-120
+ *   pierce_compact_hash_table_pairs
+ *       <- compact_hash_table_pairs  pierce/query/src/cuda/mesh_query_deduplication.cu:123-144
+ *   pierce_join
+ *       <- executeTwoPassQueryEdgesOptimized
+ *                                    pierce/query/src/applications/pierce_overlap_two_pass_main.cpp:39-156
+ *          executeHashQuery (overlap)
+ *                                    pierce/query/src/applications/pierce_overlap_main.cpp:74-187
+ *          executeHashQuery (intersection)
+ *                                    pierce/query/src/applications/pierce_intersection_main.cpp:78-177
+ *          runOnce (containment)     pierce/query/src/applications/pierce_containment_main.cpp:385-550
+ *   pierce_estimate_pairs
+ *       <- estimateOverlapSelectivity / estimateIntersectionSelectivity
+ *                                    pierce/query/src/cuda/estimated_overlap.cu:43-77,
+ *                                    estimated_intersection.cu:43-79
+ *
+ * Conventions: plain C types only; every call returns a pierce_status and
+ * never exits the process; a failed call leaves a message for
+ * pierce_last_error() (per host thread).  All device work of a context runs
+ * on that context's own CUDA stream; one context per host thread.
+ * Out-of-capacity conditions inside kernels (hash table full, traversal
+ * stack overflow, output buffer overflow) come back as status codes.
+ * A pair is (object id in dataset A, object id in dataset B), 8 bytes,
+ * laid out like MeshQueryResult (pierce/common/include/common.h:34-37).
+ */
+#ifndef PIERCE_CAPI_H
+#define PIERCE_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pierce_status {
+    PIERCE_OK = 0,
+    PIERCE_ERR_INVALID_ARGUMENT = 1,
+    PIERCE_ERR_CUDA = 2,
+    PIERCE_ERR_OUT_OF_MEMORY = 3,
+    PIERCE_ERR_NO_DEVICE = 4,
+    PIERCE_ERR_HASH_FULL = 5,        /* a hash insert exceeded its probe bound */
+    PIERCE_ERR_STACK_OVERFLOW = 6,   /* BVH traversal stack exhausted */
+    PIERCE_ERR_OUTPUT_OVERFLOW = 7,  /* result buffer smaller than the pair count */
+    PIERCE_ERR_QUEUE_TIMEOUT = 8,    /* bounded wait in a persistent kernel expired */
+    PIERCE_ERR_NOT_BUILT = 9         /* dataset has no acceleration structure yet */
+} pierce_status;
+
+typedef struct pierce_ctx pierce_ctx;
+typedef struct pierce_dataset pierce_dataset;
+typedef struct pierce_result pierce_result;
+
+typedef struct pierce_pair {
+    int32_t a;  /* object id in dataset A (mesh1) */
+    int32_t b;  /* object id in dataset B (mesh2) */
+} pierce_pair;
+
+/* Arrays of one preprocessed dataset, as stored in a `.pre` file. */
+typedef struct pierce_mesh_view {
+    const float* vertices;        /* 3 * num_vertices (xyz) */
+    uint64_t num_vertices;
+    const uint32_t* indices;      /* 3 * num_triangles */
+    uint64_t num_triangles;
+    const int32_t* tri_to_object; /* num_triangles */
+    const float* edge_starts;     /* 3 * num_edges */
+    const float* edge_ends;       /* 3 * num_edges */
+    const int32_t* edge_src;      /* num_edges source object ids */
+    uint64_t num_edges;
+    int32_t num_objects;          /* max object id + 1; < 0: computed by the library */
+} pierce_mesh_view;
+
+enum pierce_memory { PIERCE_HOST_MEMORY = 0, PIERCE_DEVICE_MEMORY = 1 };
+
+typedef enum pierce_predicate {
+    PIERCE_OVERLAP = 0,       /* surfaces meet: edge rays both ways */
+    PIERCE_INTERSECTION = 1,  /* overlap U first-vertex parity both ways */
+    PIERCE_CONTAINMENT = 2    /* B's first vertex inside A by parity, minus overlap */
+} pierce_predicate;
+
+typedef enum pierce_direction {
+    PIERCE_BOTH = 0,
+    PIERCE_MESH1_TO_MESH2 = 1,
+    PIERCE_MESH2_TO_MESH1 = 2
+} pierce_direction;
+
+typedef enum pierce_sizing {
+    PIERCE_SIZING_TWO_PASS = 0,   /* count, scan, write, sort + unique */
+    PIERCE_SIZING_HASH = 1,       /* hash set sized from expected_pairs */
+    PIERCE_SIZING_FIXED = 2       /* hash set of hash_table_slots slots */
+} pierce_sizing;
+
+typedef enum pierce_precision {
+    PIERCE_EXACT = 0,   /* FP32 filter, FP64 then exact expansion fallback */
+    PIERCE_FP32 = 1     /* plain float32 Moller-Trumbore, no fallback */
+} pierce_precision;
+
+typedef struct pierce_tuning {
+    int32_t leaf_size;        /* max triangles per BVH leaf (1..8) */
+    int32_t block_size;       /* threads per block for traversal kernels */
+    int32_t sort_rays;        /* 1: trace edge rays in Morton order of their midpoints */
+    int32_t cull_objects;     /* 1: skip source objects whose box meets no target object */
+} pierce_tuning;
+
+typedef struct pierce_join_opts {
+    int32_t predicate;            /* pierce_predicate */
+    int32_t direction;            /* pierce_direction */
+    int32_t sizing;               /* pierce_sizing */
+    int32_t precision;            /* pierce_precision */
+    uint64_t expected_pairs;      /* HASH sizing input (0: default table) */
+    uint64_t hash_table_slots;    /* FIXED sizing */
+    double hash_load_factor;      /* (0,1], default 0.5 */
+    double output_safety;         /* result capacity = expected * safety (>= 1) */
+    int32_t include_overlap_pairs;/* containment: also report overlap pairs */
+    int32_t max_retries;          /* table/output enlargements before failing */
+} pierce_join_opts;
+
+typedef struct pierce_stats {
+    double ms_total;              /* GPU time of the whole join (CUDA events) */
+    double ms_edge_rays[2];       /* A->B, B->A edge-ray kernels (all passes) */
+    double ms_parity[2];          /* A->B, B->A parity kernels */
+    double ms_dedup;              /* scan, sort/unique or compaction */
+    uint64_t rays;                /* edge rays traced (per pass) */
+    uint64_t node_visits;         /* BVH nodes fetched */
+    uint64_t tri_tests;           /* ray-triangle tests */
+    uint64_t raw_hits;            /* pair emissions before deduplication */
+    uint64_t fp32_ambiguous;      /* predicates the FP32 filter could not decide */
+    uint64_t fp64_ambiguous;      /* ... and the FP64 filter could not decide */
+    uint64_t parity_rays;
+    uint64_t hash_slots;          /* hash table slots used by the join */
+    uint64_t result_capacity;     /* pairs the result buffer could hold */
+    uint64_t num_pairs;           /* pairs in the result */
+    uint64_t overlap_pairs;       /* containment: overlap pairs found */
+    uint64_t containment_pairs;   /* containment: strict containment pairs */
+    int32_t retries;              /* enlargements performed */
+    int32_t launches;             /* kernels launched by the join */
+} pierce_stats;
+
+typedef struct pierce_dataset_info {
+    uint64_t num_vertices, num_triangles, num_edges;
+    int32_t num_objects;
+    int32_t built;
+    uint64_t num_nodes;
+    uint64_t device_bytes;
+    double ms_build;              /* GPU time of the last build */
+    float bounds_lo[3], bounds_hi[3];
+} pierce_dataset_info;
+
+/* ---- context ------------------------------------------------------------ */
+const char* pierce_last_error(void);
+const char* pierce_status_string(int status);
+int pierce_ctx_create(int device, pierce_ctx** out);
+void pierce_ctx_destroy(pierce_ctx* ctx);
+int pierce_ctx_synchronize(pierce_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t), for callers that time or order
+ * their own work against the library's. */
+void* pierce_ctx_stream(pierce_ctx* ctx);
+void pierce_default_tuning(pierce_tuning* t);
+void pierce_default_join_opts(pierce_join_opts* o);
+/* Kernels launched by this context since its creation. */
+uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx);
+
+/* ---- datasets ----------------------------------------------------------- */
+/* Copy a dataset to the device (from host or device memory) and build its
+ * bounding-volume hierarchy (tuning may be NULL for defaults). */
+int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* view, int memory,
+                          const pierce_tuning* tuning, pierce_dataset** out);
+/* Rebuild the hierarchy (e.g. with another leaf size). */
+int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
+int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out);
+void pierce_dataset_destroy(pierce_dataset* ds);
+
+/* ---- joins -------------------------------------------------------------- */
+/* Full join of A (mesh1) and B (mesh2); the result holds the unique pairs
+ * sorted by (a, b), resident on the device. stats may be NULL. */
+int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                pierce_result** out, pierce_stats* stats);
+int pierce_result_count(const pierce_result* r, uint64_t* count);
+/* Device pointer to the result's pierce_pair array. */
+const pierce_pair* pierce_result_device_pairs(const pierce_result* r);
+/* Copy up to `capacity` pairs to host memory (synchronous). */
+int pierce_result_copy(pierce_ctx* ctx, const pierce_result* r, pierce_pair* host_out, uint64_t capacity);
+/* Containment with include_overlap_pairs: number of leading result entries
+ * that are strict containment pairs (the rest are overlap pairs). */
+int pierce_result_containment_count(const pierce_result* r, uint64_t* count);
+void pierce_result_destroy(pierce_result* r);
+
+/* ---- launch-level entry points (the reference's launcher seam) ---------- */
+enum pierce_ray_mode { PIERCE_RAYS_COUNT = 0, PIERCE_RAYS_WRITE = 1, PIERCE_RAYS_HASH = 2 };
+
+/* Edge rays of `src` against `tgt`'s triangles.  COUNT writes d_counts[e]
+ * (hits per edge after per-edge de-duplication of target objects); WRITE
+ * stores pair keys ((a << 32) | b, uint64) at d_keys[d_offsets[e] ...];
+ * HASH inserts the keys into the open-addressing set d_table of
+ * table_slots slots (a power of two; empty slot = all ones).  swap != 0
+ * stores (target, source) instead of (source, target). */
+int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode,
+                            int precision, int swap, int32_t* d_counts, const int64_t* d_offsets,
+                            uint64_t* d_keys, uint64_t* d_table, uint64_t table_slots, pierce_stats* stats);
+/* First-vertex +Z parity rays of `src` objects against `tgt`: toggles the
+ * parity of key (src, tgt) (or (tgt, src) when swap) in the set d_table /
+ * d_parity (table_slots slots). */
+int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int precision,
+                         int swap, uint64_t* d_table, uint32_t* d_parity, uint64_t table_slots,
+                         pierce_stats* stats);
+
+/* ---- helpers replacing the reference's extern "C" device helpers -------- */
+/* Exclusive scan of n int32 counts into int64 offsets; *total = sum. */
+int pierce_exclusive_scan(pierce_ctx* ctx, const int32_t* d_counts, int64_t* d_offsets, int64_t n,
+                          int64_t* total);
+/* Sort + unique of the concatenation of two device pair arrays written to
+ * d_out (which may alias d_pairs1); pairs end sorted by (a, b). */
+int pierce_merge_and_deduplicate_pairs(pierce_ctx* ctx, const pierce_pair* d_pairs1, int64_t n1,
+                                       const pierce_pair* d_pairs2, int64_t n2, pierce_pair* d_out,
+                                       int64_t* num_unique);
+/* Compact the occupied slots of a pair-key hash set into d_out (at most
+ * max_output pairs, unsorted); *count = number of occupied slots, which may
+ * exceed max_output (then PIERCE_ERR_OUTPUT_OVERFLOW is returned). */
+int pierce_compact_hash_table_pairs(pierce_ctx* ctx, const uint64_t* d_table, uint64_t table_slots,
+                                    pierce_pair* d_out, uint64_t max_output, uint64_t* count);
+
+/* ---- output sizing ------------------------------------------------------ */
+/* Grid selectivity estimate (GridCell statistics of both datasets); the
+ * cells arrays are host memory of 28-byte records {int3 index; u32 center;
+ * u32 touch; f32 avg_size; f32 vol_ratio}. Returns the raw sum over matched
+ * cells in *raw and the alpha-corrected estimate in *estimate. */
+int pierce_estimate_pairs(pierce_ctx* ctx, const void* cells_a, uint32_t num_a, const void* cells_b,
+                          uint32_t num_b, float cell_size, float epsilon, float gamma, int alpha_correction,
+                          double* raw, int64_t* estimate, int32_t* matched_cells);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PIERCE_CAPI_H */

@@ -1,0 +1,144 @@
+"""Python access to the CPU oracle (oracle/oracle.cpp) — test infrastructure.
+
+Only the test-suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module; it is the checker, never the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+_lib = None
+
+V = C.c_void_p
+U64 = C.c_uint64
+
+
+def build() -> Path:
+    """Compile the oracle (g++, OpenMP, no FMA contraction)."""
+    BUILD.mkdir(exist_ok=True)
+    src = HERE / "oracle.cpp"
+    if LIB.exists() and LIB.stat().st_mtime >= src.stat().st_mtime:
+        return LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           str(src), "-o", str(LIB)]
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + proc.stdout)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        L.oracle_overlap_pairs.restype = C.POINTER(C.c_uint64)
+        L.oracle_overlap_pairs.argtypes = [V, V, V, U64, V, V, V, U64, V, V, V, U64, V, V, V, U64,
+                                           C.c_int, C.c_int, C.POINTER(U64), C.POINTER(U64)]
+        L.oracle_parity_pairs.restype = C.POINTER(C.c_uint64)
+        L.oracle_parity_pairs.argtypes = [V, C.c_int32, V, V, V, U64, C.c_int, C.POINTER(U64)]
+        L.oracle_face_pairs.restype = C.POINTER(C.c_uint64)
+        L.oracle_face_pairs.argtypes = [V, V, V, U64, V, V, V, U64, U64, U64, C.POINTER(U64)]
+        L.oracle_free.argtypes = [V]
+        L.oracle_free.restype = None
+        for name in ("oracle_orient3d", "oracle_orient3d_exact"):
+            getattr(L, name).argtypes = [V, V, V, V]
+            getattr(L, name).restype = C.c_int
+        L.oracle_orient2d_xy.argtypes = [V, V, V]
+        L.oracle_seg_tri.argtypes = [V, V, V, V, V, C.c_int]
+        L.oracle_zray_crosses.argtypes = [V, V, V, V]
+        L.oracle_exact_calls.restype = C.c_uint64
+        L.oracle_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _take(ptr, n) -> np.ndarray:
+    out = np.ctypeslib.as_array(ptr, shape=(max(int(n), 1),))[: int(n)].copy()
+    lib().oracle_free(C.cast(ptr, V))
+    return out
+
+
+def keys_to_pairs(keys: np.ndarray) -> np.ndarray:
+    """(a << 32 | b) uint64 keys -> (n, 2) uint32 array of (a, b)."""
+    keys = np.asarray(keys, dtype=np.uint64)
+    return np.stack([(keys >> np.uint64(32)).astype(np.uint32),
+                     (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)], axis=1)
+
+
+def pairs_to_keys(pairs: np.ndarray) -> np.ndarray:
+    pairs = np.asarray(pairs).reshape(-1, 2)
+    return (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint64)
+
+
+def _geom_args(g):
+    v = g.vertices
+    i = g.indices
+    o = g.tri_to_object
+    return (v.ctypes.data, i.ctypes.data, o.ctypes.data, i.shape[0]), (v, i, o)
+
+
+def _edge_args(g):
+    s, e, o = g.edge_starts, g.edge_ends, g.edge_src
+    return (s.ctypes.data, e.ctypes.data, o.ctypes.data, o.shape[0]), (s, e, o)
+
+
+def overlap_keys(A, B, direction: int = 0, mode: int = 0):
+    """Sorted unique (a<<32|b) keys of the overlap join and the number of
+    triangle tests performed.  mode 0 exact, 1 float32 Moller-Trumbore."""
+    (ga, ka), (gb, kb) = _geom_args(A), _geom_args(B)
+    (ea, kea), (eb, keb) = _edge_args(A), _edge_args(B)
+    n, tests = U64(), U64()
+    ptr = lib().oracle_overlap_pairs(*ga, *ea, *gb, *eb, direction, mode, C.byref(n), C.byref(tests))
+    return _take(ptr, n.value), tests.value
+
+
+def parity_keys(first_vertices: np.ndarray, T, swap: int = 0) -> np.ndarray:
+    fv = _f32(first_vertices).reshape(-1, 3)
+    gt, keep = _geom_args(T)
+    n = U64()
+    ptr = lib().oracle_parity_pairs(fv.ctypes.data, fv.shape[0], *gt, swap, C.byref(n))
+    return _take(ptr, n.value)
+
+
+def face_keys(A, B, tri_begin: int = 0, tri_end: int | None = None) -> np.ndarray:
+    (ga, ka), (gb, kb) = _geom_args(A), _geom_args(B)
+    if tri_end is None:
+        tri_end = A.num_triangles
+    n = U64()
+    ptr = lib().oracle_face_pairs(*ga, *gb, tri_begin, tri_end, C.byref(n))
+    return _take(ptr, n.value)
+
+
+def intersection_keys(A, B) -> np.ndarray:
+    """S_surf U parity(A first vertex in B) U parity(B first vertex in A)."""
+    surf, _ = overlap_keys(A, B)
+    pa = parity_keys(A.first_vertices(), B, swap=0)
+    pb = parity_keys(B.first_vertices(), A, swap=1)
+    return np.unique(np.concatenate([surf, pa, pb]))
+
+
+def containment_keys(A, B) -> np.ndarray:
+    """(a, b) with B's first vertex inside A by parity and (a, b) not in S_surf."""
+    surf, _ = overlap_keys(A, B)
+    pb = parity_keys(B.first_vertices(), A, swap=1)
+    return np.setdiff1d(pb, surf, assume_unique=True)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())

@@ -1,0 +1,139 @@
+"""ctypes binding of ``include/pierce_capi.h`` (the CUDA join library).
+
+The structures below mirror the header field for field; the functions are
+declared with exact argument types so that a wrong call fails in Python
+instead of corrupting memory.  This module is the only place that talks to
+``libpierce_gb300.so`` directly; :mod:`pierce_gb300.join` builds the user API
+on top of it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import native
+
+V = C.c_void_p
+I32 = C.c_int32
+I64 = C.c_int64
+U64 = C.c_uint64
+D = C.c_double
+F = C.c_float
+
+# status codes
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_NO_DEVICE = 4
+ERR_HASH_FULL = 5
+ERR_STACK_OVERFLOW = 6
+ERR_OUTPUT_OVERFLOW = 7
+ERR_QUEUE_TIMEOUT = 8
+ERR_NOT_BUILT = 9
+
+HOST_MEMORY = 0
+DEVICE_MEMORY = 1
+
+OVERLAP, INTERSECTION, CONTAINMENT = 0, 1, 2
+BOTH, MESH1_TO_MESH2, MESH2_TO_MESH1 = 0, 1, 2
+SIZING_TWO_PASS, SIZING_HASH, SIZING_FIXED = 0, 1, 2
+EXACT, FP32 = 0, 1
+RAYS_COUNT, RAYS_WRITE, RAYS_HASH = 0, 1, 2
+
+
+class MeshView(C.Structure):
+    _fields_ = [("vertices", V), ("num_vertices", U64), ("indices", V), ("num_triangles", U64),
+                ("tri_to_object", V), ("edge_starts", V), ("edge_ends", V), ("edge_src", V),
+                ("num_edges", U64), ("num_objects", I32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("leaf_size", I32), ("block_size", I32), ("sort_rays", I32), ("cull_objects", I32)]
+
+
+class JoinOpts(C.Structure):
+    _fields_ = [("predicate", I32), ("direction", I32), ("sizing", I32), ("precision", I32),
+                ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
+                ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("ms_total", D), ("ms_edge_rays", D * 2), ("ms_parity", D * 2), ("ms_dedup", D),
+                ("rays", U64), ("node_visits", U64), ("tri_tests", U64), ("raw_hits", U64),
+                ("fp32_ambiguous", U64), ("fp64_ambiguous", U64), ("parity_rays", U64),
+                ("hash_slots", U64), ("result_capacity", U64), ("num_pairs", U64),
+                ("overlap_pairs", U64), ("containment_pairs", U64), ("retries", I32),
+                ("launches", I32)]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+class DatasetInfo(C.Structure):
+    _fields_ = [("num_vertices", U64), ("num_triangles", U64), ("num_edges", U64),
+                ("num_objects", I32), ("built", I32), ("num_nodes", U64), ("device_bytes", U64),
+                ("ms_build", D), ("bounds_lo", F * 3), ("bounds_hi", F * 3)]
+
+
+# Every symbol the header declares, with its signature.
+SIGNATURES = {
+    "pierce_last_error": (C.c_char_p, []),
+    "pierce_status_string": (C.c_char_p, [C.c_int]),
+    "pierce_ctx_create": (C.c_int, [C.c_int, C.POINTER(V)]),
+    "pierce_ctx_destroy": (None, [V]),
+    "pierce_ctx_synchronize": (C.c_int, [V]),
+    "pierce_ctx_stream": (V, [V]),
+    "pierce_default_tuning": (None, [C.POINTER(Tuning)]),
+    "pierce_default_join_opts": (None, [C.POINTER(JoinOpts)]),
+    "pierce_ctx_kernel_launches": (U64, [V]),
+    "pierce_dataset_create": (C.c_int, [V, C.POINTER(MeshView), C.c_int, C.POINTER(Tuning), C.POINTER(V)]),
+    "pierce_dataset_build": (C.c_int, [V, V, C.POINTER(Tuning)]),
+    "pierce_dataset_info_get": (C.c_int, [V, C.POINTER(DatasetInfo)]),
+    "pierce_dataset_destroy": (None, [V]),
+    "pierce_join": (C.c_int, [V, V, V, C.POINTER(JoinOpts), C.POINTER(V), C.POINTER(Stats)]),
+    "pierce_result_count": (C.c_int, [V, C.POINTER(U64)]),
+    "pierce_result_device_pairs": (V, [V]),
+    "pierce_result_copy": (C.c_int, [V, V, V, U64]),
+    "pierce_result_containment_count": (C.c_int, [V, C.POINTER(U64)]),
+    "pierce_result_destroy": (None, [V]),
+    "pierce_launch_edge_rays": (C.c_int, [V, V, V, C.c_int, C.c_int, C.c_int, V, V, V, V, U64,
+                                          C.POINTER(Stats)]),
+    "pierce_launch_parity": (C.c_int, [V, V, V, C.c_int, C.c_int, V, V, U64, C.POINTER(Stats)]),
+    "pierce_exclusive_scan": (C.c_int, [V, V, V, I64, C.POINTER(I64)]),
+    "pierce_merge_and_deduplicate_pairs": (C.c_int, [V, V, I64, V, I64, V, C.POINTER(I64)]),
+    "pierce_compact_hash_table_pairs": (C.c_int, [V, V, U64, V, U64, C.POINTER(U64)]),
+    "pierce_estimate_pairs": (C.c_int, [V, V, C.c_uint32, V, C.c_uint32, F, F, F, C.c_int,
+                                        C.POINTER(D), C.POINTER(I64), C.POINTER(I32)]),
+}
+
+_bound = None
+
+
+def lib() -> C.CDLL:
+    """The CUDA library with all signatures declared (raises if unbuilt)."""
+    global _bound
+    if _bound is None:
+        L = native.gpu()
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _bound = L
+    return _bound
+
+
+class PierceError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        L = lib()
+        self.status = status
+        msg = L.pierce_last_error().decode(errors="replace")
+        super().__init__(f"{what}: {L.pierce_status_string(status).decode()} ({status}): {msg}")
+
+
+def check(status: int, what: str) -> None:
+    if status != OK:
+        raise PierceError(status, what)

@@ -1,0 +1,1031 @@
+// C ABI of the GB300 join library (include/pierce_capi.h): contexts,
+// datasets, joins, results, the launch-level seam and the dedup/scan helpers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pgpu {
+// join.cu
+int launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode, int precision,
+                     int swap, int32_t* counts, const int64_t* offsets, uint64_t* keys, uint64_t* table,
+                     uint64_t slots);
+int launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int swap, uint64_t* table,
+                  uint32_t* parity, uint64_t slots);
+int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
+                  unsigned long long* d_count);
+int keys_to_pairs(pierce_ctx* ctx, uint64_t* keys, int64_t n);
+int pairs_to_keys(pierce_ctx* ctx, const uint64_t* pairs, uint64_t* keys, int64_t n);
+int parity_emit(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots, int mode,
+                const uint64_t* lookup_table, uint64_t lookup_slots, const uint64_t* lookup_sorted, int64_t lookup_n,
+                uint64_t* out_table, uint64_t out_slots, uint64_t* out_keys, unsigned long long* out_count,
+                uint64_t out_cap);
+uint64_t table_slots_for(uint64_t expected, double load_factor);
+int estimate_cells(pierce_ctx* ctx, const void* a, const void* b, int n, float cell_volume, float eps, float gamma,
+                   double* total);
+}  // namespace pgpu
+
+using namespace pgpu;
+
+namespace {
+thread_local std::string g_err;
+
+// scratch slot assignment
+enum : int {
+    SLOT_CUB = 0,
+    SLOT_BUILD_A = 1,
+    SLOT_BUILD_B = 2,
+    SLOT_BUILD_C = 3,
+    SLOT_BUILD_D = 4,
+    SLOT_TABLE = 5,
+    SLOT_KEYS = 6,
+    SLOT_AUX = 7,
+};
+}  // namespace
+
+namespace pgpu {
+
+int set_error(int status, const std::string& msg) {
+    g_err = msg;
+    return status;
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PIERCE_OK;
+    const int st = (e == cudaErrorMemoryAllocation) ? PIERCE_ERR_OUT_OF_MEMORY : PIERCE_ERR_CUDA;
+    return set_error(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int device_alloc(void** p, size_t bytes, const char* what) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(PIERCE_ERR_OUT_OF_MEMORY,
+                         std::string("cudaMalloc(") + std::to_string(bytes) + ") for " + what + ": " +
+                             cudaGetErrorString(e));
+    }
+    return PIERCE_OK;
+}
+
+int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
+    if (bytes == 0) bytes = 16;
+    if (ctx->scratch_bytes[slot] < bytes) {
+        if (ctx->scratch[slot]) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->scratch[slot]);
+            ctx->scratch[slot] = nullptr;
+            ctx->scratch_bytes[slot] = 0;
+        }
+        size_t want = bytes + bytes / 8;  // headroom against repeated growth
+        if (int s = device_alloc(&ctx->scratch[slot], want, "scratch")) return s;
+        ctx->scratch_bytes[slot] = want;
+    }
+    *out = ctx->scratch[slot];
+    return PIERCE_OK;
+}
+
+}  // namespace pgpu
+
+// ---------------------------------------------------------------- kernels --
+
+__global__ void k_pack_edges(const float* __restrict__ s, const float* __restrict__ e, const int32_t* __restrict__ src,
+                             int64_t n, float4* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        out[2 * i] = make_float4(s[3 * i], s[3 * i + 1], s[3 * i + 2], __int_as_float(src[i]));
+        out[2 * i + 1] = make_float4(e[3 * i], e[3 * i + 1], e[3 * i + 2], 0.0f);
+    }
+}
+
+__global__ void k_max_i32(const int32_t* __restrict__ v, int64_t n, int32_t* out) {
+    int32_t m = -1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, v[i]);
+    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ------------------------------------------------------------ host helpers --
+
+static int grid_for(pierce_ctx* ctx, int64_t n, int block) {
+    int64_t b = (n + block - 1) / block;
+    const int64_t cap = (int64_t)ctx->sm_count * 16;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
+static int sync_ctx(pierce_ctx* ctx, const char* what) {
+    return check_cuda(cudaStreamSynchronize(ctx->stream), what);
+}
+
+// Translate device error bits into a status (the bits are cleared).
+static int read_device_error(pierce_ctx* ctx, uint32_t* bits_out) {
+    cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (int s = sync_ctx(ctx, "error readback")) return s;
+    *bits_out = *ctx->h_err;
+    cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
+    return PIERCE_OK;
+}
+
+struct EventTimer {
+    std::vector<cudaEvent_t> ev;
+    std::vector<std::pair<int, int>> spans;  // (begin idx, end idx) per label
+    std::vector<double*> targets;
+    cudaStream_t st;
+    explicit EventTimer(cudaStream_t s) : st(s) {}
+    int record() {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        ev.push_back(e);
+        return (int)ev.size() - 1;
+    }
+    void span(int b, int e, double* target) {
+        spans.emplace_back(b, e);
+        targets.push_back(target);
+    }
+    void resolve() {
+        for (size_t i = 0; i < spans.size(); ++i) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[spans[i].first], ev[spans[i].second]);
+            *targets[i] += ms;
+        }
+    }
+    ~EventTimer() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
+// ------------------------------------------------------------------ C ABI --
+extern "C" {
+
+const char* pierce_last_error(void) { return g_err.c_str(); }
+
+const char* pierce_status_string(int status) {
+    switch (status) {
+        case PIERCE_OK: return "ok";
+        case PIERCE_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PIERCE_ERR_CUDA: return "CUDA error";
+        case PIERCE_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case PIERCE_ERR_NO_DEVICE: return "no CUDA device";
+        case PIERCE_ERR_HASH_FULL: return "hash table full";
+        case PIERCE_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+        case PIERCE_ERR_OUTPUT_OVERFLOW: return "output buffer overflow";
+        case PIERCE_ERR_QUEUE_TIMEOUT: return "work queue wait timed out";
+        case PIERCE_ERR_NOT_BUILT: return "dataset not built";
+        default: return "unknown status";
+    }
+}
+
+void pierce_default_tuning(pierce_tuning* t) {
+    if (!t) return;
+    t->leaf_size = 1;
+    t->block_size = 128;
+    t->sort_rays = 0;
+    t->cull_objects = 0;
+}
+
+void pierce_default_join_opts(pierce_join_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->predicate = PIERCE_OVERLAP;
+    o->direction = PIERCE_BOTH;
+    o->sizing = PIERCE_SIZING_HASH;
+    o->precision = PIERCE_EXACT;
+    o->expected_pairs = 0;
+    o->hash_table_slots = 0;
+    o->hash_load_factor = 0.5;
+    o->output_safety = 1.2;
+    o->include_overlap_pairs = 0;
+    o->max_retries = 4;
+}
+
+int pierce_ctx_create(int device, pierce_ctx** out) {
+    if (!out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "ctx_create: null out");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return set_error(PIERCE_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "ctx_create: bad device index");
+    if (int s = check_cuda(cudaSetDevice(device), "cudaSetDevice")) return s;
+    pierce_ctx* ctx = new pierce_ctx();
+    ctx->device = device;
+    int st = check_cuda(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream create");
+    if (!st) st = device_alloc((void**)&ctx->d_err, sizeof(uint32_t), "error word");
+    if (!st) st = device_alloc((void**)&ctx->d_counters, sizeof(DevCounters), "counters");
+    if (!st) st = check_cuda(cudaMallocHost((void**)&ctx->h_err, sizeof(uint32_t)), "pinned");
+    if (!st) st = check_cuda(cudaMallocHost((void**)&ctx->h_counters, sizeof(DevCounters)), "pinned");
+    if (!st) st = check_cuda(cudaMallocHost((void**)&ctx->h_small, 8 * sizeof(int64_t)), "pinned");
+    if (!st) st = check_cuda(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
+    if (!st) st = check_cuda(cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream), "memset");
+    if (!st) st = sync_ctx(ctx, "ctx init");
+    if (st) {
+        pierce_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return PIERCE_OK;
+}
+
+void pierce_ctx_destroy(pierce_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < 8; ++i)
+        if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int pierce_ctx_synchronize(pierce_ctx* ctx) {
+    if (!ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "null ctx");
+    return sync_ctx(ctx, "synchronize");
+}
+
+void* pierce_ctx_stream(pierce_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---- datasets ---------------------------------------------------------------
+
+void pierce_dataset_destroy(pierce_dataset* ds) {
+    if (!ds) return;
+    if (ds->ctx) {
+        cudaSetDevice(ds->ctx->device);
+        cudaStreamSynchronize(ds->ctx->stream);
+    }
+    void* ptrs[] = {ds->d_vertices, ds->d_indices, ds->d_tri_to_object, ds->d_edges,
+                    ds->d_soup,     ds->d_nodes,   ds->d_first_vertex,  ds->d_obj_box};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete ds;
+}
+
+int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning) {
+    if (!ctx || !ds) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_build: null argument");
+    pierce_tuning t;
+    pierce_default_tuning(&t);
+    if (tuning) t = *tuning;
+    return build_bvh(ctx, ds, t.leaf_size);
+}
+
+int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory, const pierce_tuning* tuning,
+                          pierce_dataset** out) {
+    if (!ctx || !v || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: null argument");
+    *out = nullptr;
+    if ((v->num_vertices && !v->vertices) || (v->num_triangles && (!v->indices || !v->tri_to_object)) ||
+        (v->num_edges && (!v->edge_starts || !v->edge_ends || !v->edge_src)))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: missing array");
+    if (v->num_triangles >= (1ull << 31) || v->num_edges >= (1ull << 40) || v->num_vertices >= (1ull << 32))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: dataset too large for 32-bit ids");
+    cudaSetDevice(ctx->device);
+    const cudaMemcpyKind kind = memory == PIERCE_DEVICE_MEMORY ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    pierce_dataset* ds = new pierce_dataset();
+    ds->ctx = ctx;
+    ds->nv = v->num_vertices;
+    ds->nt = v->num_triangles;
+    ds->ne = v->num_edges;
+    cudaStream_t st = ctx->stream;
+    int s = PIERCE_OK;
+    do {
+        // object count
+        int32_t nobj = v->num_objects;
+        if (nobj < 0) {
+            if (memory == PIERCE_HOST_MEMORY) {
+                nobj = 0;
+                for (uint64_t i = 0; i < ds->nt; ++i) nobj = std::max(nobj, v->tri_to_object[i] + 1);
+            } else if (ds->nt > 0) {
+                void* p = nullptr;
+                if ((s = scratch(ctx, SLOT_AUX, sizeof(int32_t), &p))) break;
+                cudaMemsetAsync(p, 0xFF, sizeof(int32_t), st);
+                k_max_i32<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(v->tri_to_object, (int64_t)ds->nt,
+                                                                                 (int32_t*)p);
+                ctx->launches += 1;
+                cudaMemcpyAsync(ctx->h_small, p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+                if ((s = sync_ctx(ctx, "object count"))) break;
+                nobj = *reinterpret_cast<int32_t*>(ctx->h_small) + 1;
+            } else {
+                nobj = 0;
+            }
+        }
+        ds->num_objects = nobj;
+        const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
+        if ((s = device_alloc((void**)&ds->d_vertices, vb, "vertices"))) break;
+        if ((s = device_alloc((void**)&ds->d_indices, ib, "indices"))) break;
+        if ((s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object"))) break;
+        if ((s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges"))) break;
+        if ((s = device_alloc((void**)&ds->d_soup, 48 * ds->nt, "triangle soup"))) break;
+        if ((s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))) break;
+        if ((s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices"))) break;
+        if ((s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes"))) break;
+        ds->device_bytes = vb + ib + ob + 32 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
+        if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, st), "copy vertices"))) break;
+        if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, st), "copy indices"))) break;
+        if (ob && (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, st), "copy t2o")))
+            break;
+        if (ds->ne) {
+            void *ps = nullptr, *pe = nullptr, *po = nullptr;
+            if ((s = scratch(ctx, SLOT_BUILD_A, 12 * ds->ne, &ps))) break;
+            if ((s = scratch(ctx, SLOT_BUILD_B, 12 * ds->ne, &pe))) break;
+            if ((s = scratch(ctx, SLOT_BUILD_C, 4 * ds->ne, &po))) break;
+            if ((s = check_cuda(cudaMemcpyAsync(ps, v->edge_starts, 12 * ds->ne, kind, st), "copy edge starts"))) break;
+            if ((s = check_cuda(cudaMemcpyAsync(pe, v->edge_ends, 12 * ds->ne, kind, st), "copy edge ends"))) break;
+            if ((s = check_cuda(cudaMemcpyAsync(po, v->edge_src, 4 * ds->ne, kind, st), "copy edge src"))) break;
+            k_pack_edges<<<grid_for(ctx, (int64_t)ds->ne, 256), 256, 0, st>>>((const float*)ps, (const float*)pe,
+                                                                               (const int32_t*)po, (int64_t)ds->ne,
+                                                                               ds->d_edges);
+            ctx->launches += 1;
+            if ((s = check_cuda(cudaGetLastError(), "pack edges"))) break;
+        }
+        if ((s = prepare_objects(ctx, ds))) break;
+        pierce_tuning t;
+        pierce_default_tuning(&t);
+        if (tuning) t = *tuning;
+        if ((s = build_bvh(ctx, ds, t.leaf_size))) break;
+    } while (0);
+    if (s) {
+        pierce_dataset_destroy(ds);
+        return s;
+    }
+    *out = ds;
+    return PIERCE_OK;
+}
+
+int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out) {
+    if (!ds || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_info: null argument");
+    std::memset(out, 0, sizeof(*out));
+    out->num_vertices = ds->nv;
+    out->num_triangles = ds->nt;
+    out->num_edges = ds->ne;
+    out->num_objects = ds->num_objects;
+    out->built = ds->built;
+    out->num_nodes = ds->num_nodes;
+    out->device_bytes = ds->device_bytes;
+    out->ms_build = ds->ms_build;
+    for (int k = 0; k < 3; ++k) {
+        out->bounds_lo[k] = ds->lo[k];
+        out->bounds_hi[k] = ds->hi[k];
+    }
+    return PIERCE_OK;
+}
+
+// ---- results ----------------------------------------------------------------
+
+int pierce_result_count(const pierce_result* r, uint64_t* count) {
+    if (!r || !count) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "result_count: null argument");
+    *count = r->count;
+    return PIERCE_OK;
+}
+
+int pierce_result_containment_count(const pierce_result* r, uint64_t* count) {
+    if (!r || !count) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "result_containment_count: null argument");
+    *count = r->containment_count;
+    return PIERCE_OK;
+}
+
+const pierce_pair* pierce_result_device_pairs(const pierce_result* r) { return r ? r->d_pairs : nullptr; }
+
+int pierce_result_copy(pierce_ctx* ctx, const pierce_result* r, pierce_pair* host_out, uint64_t capacity) {
+    if (!ctx || !r || (!host_out && capacity)) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "result_copy: null");
+    const uint64_t n = std::min(capacity, r->count);
+    if (n == 0) return PIERCE_OK;
+    if (int s = check_cuda(cudaMemcpyAsync(host_out, r->d_pairs, n * sizeof(pierce_pair), cudaMemcpyDeviceToHost,
+                                           ctx->stream),
+                           "result copy"))
+        return s;
+    if (int s = sync_ctx(ctx, "result copy")) return s;
+    return r->count > capacity ? set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "result_copy: capacity below pair count")
+                               : PIERCE_OK;
+}
+
+void pierce_result_destroy(pierce_result* r) {
+    if (!r) return;
+    if (r->d_pairs) cudaFree(r->d_pairs);
+    delete r;
+}
+
+}  // extern "C"
+
+// ---- join orchestration ------------------------------------------------------
+
+namespace {
+
+struct Join {
+    pierce_ctx* ctx;
+    pierce_dataset* A;
+    pierce_dataset* B;
+    pierce_join_opts o;
+    pierce_stats st;
+    EventTimer timer;
+    bool ab, ba;
+    Join(pierce_ctx* c, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts& opts)
+        : ctx(c), A(a), B(b), o(opts), timer(c->stream) {
+        std::memset(&st, 0, sizeof(st));
+        ab = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH1_TO_MESH2;
+        ba = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH2_TO_MESH1;
+    }
+
+    int edge_rays(int mode, int32_t* counts_ab, int32_t* counts_ba, const int64_t* off_ab, const int64_t* off_ba,
+                  uint64_t* keys, int64_t keys_ba_base, uint64_t* table, uint64_t slots) {
+        if (ab) {
+            int b = timer.record();
+            if (int s = launch_edge_rays(ctx, A, B, mode, o.precision, 0, counts_ab, off_ab, keys, table, slots))
+                return s;
+            timer.span(b, timer.record(), &st.ms_edge_rays[0]);
+        }
+        if (ba) {
+            int b = timer.record();
+            if (int s = launch_edge_rays(ctx, B, A, mode, o.precision, 1, counts_ba, off_ba,
+                                         keys ? keys + keys_ba_base : nullptr, table, slots))
+                return s;
+            timer.span(b, timer.record(), &st.ms_edge_rays[1]);
+        }
+        return PIERCE_OK;
+    }
+
+    // Overlap set in a hash table (scratch SLOT_TABLE); returns slots used.
+    int overlap_hash(uint64_t** table_out, uint64_t* slots_out) {
+        uint64_t slots;
+        if (o.sizing == PIERCE_SIZING_FIXED && o.hash_table_slots > 0) {
+            slots = 1;
+            while (slots < o.hash_table_slots) slots <<= 1;
+        } else {
+            const uint64_t expected = o.expected_pairs ? o.expected_pairs : (8u << 20);
+            slots = table_slots_for(expected, o.hash_load_factor);
+        }
+        for (int attempt = 0;; ++attempt) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_TABLE, slots * 8, &p)) return s;
+            uint64_t* table = static_cast<uint64_t*>(p);
+            cudaMemsetAsync(table, 0xFF, slots * 8, ctx->stream);
+            if (int s = edge_rays(2, nullptr, nullptr, nullptr, nullptr, nullptr, 0, table, slots)) return s;
+            uint32_t bits = 0;
+            if (int s = read_device_error(ctx, &bits)) return s;
+            if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+            if (bits & ERR_HASH_FULL) {
+                if (attempt >= o.max_retries)
+                    return set_error(PIERCE_ERR_HASH_FULL, "pair hash table full after retries");
+                slots *= 4;
+                st.retries++;
+                continue;
+            }
+            *table_out = table;
+            *slots_out = slots;
+            st.hash_slots = slots;
+            return PIERCE_OK;
+        }
+    }
+
+    // Occupied slots of a table -> keys in SLOT_KEYS (at offset `base` keys);
+    // the capacity is sized from the expected count and grown on overflow.
+    int compact(const uint64_t* table, uint64_t slots, uint64_t base, uint64_t* n_out, uint64_t** keys_out) {
+        uint64_t cap = o.expected_pairs ? (uint64_t)std::ceil((double)o.expected_pairs * std::max(1.0, o.output_safety))
+                                        : (1u << 20);
+        cap = std::max<uint64_t>(std::min<uint64_t>(cap, slots), 1024);
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_KEYS, (base + cap) * 8, &p)) return s;
+            void* pc = nullptr;
+            if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+            unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+            cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), ctx->stream);
+            uint64_t* keys = static_cast<uint64_t*>(p);
+            if (int s = compact_table(ctx, table, slots, keys + base, cap, d_count)) return s;
+            cudaMemcpyAsync(ctx->h_small, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+            if (int s = sync_ctx(ctx, "compact count")) return s;
+            const uint64_t n = (uint64_t)ctx->h_small[0];
+            st.result_capacity = cap;
+            if (n <= cap) {
+                *n_out = n;
+                *keys_out = keys;
+                return PIERCE_OK;
+            }
+            cap = n;  // output overflow: resize to the exact count and compact again
+            st.retries++;
+        }
+        return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "compaction output overflow");
+    }
+
+    // Two-pass overlap: count, scan, write, sort + unique into SLOT_KEYS.
+    int overlap_two_pass(uint64_t** keys_out, uint64_t* n_out) {
+        const uint64_t na = ab ? A->ne : 0, nb = ba ? B->ne : 0;
+        void* pc = nullptr;
+        // counts (int32) and offsets (int64) for both directions
+        const size_t cbytes = 4 * (na + nb) + 64, obytes = 8 * (na + nb) + 64;
+        if (int s = scratch(ctx, SLOT_BUILD_A, cbytes, &pc)) return s;
+        void* po = nullptr;
+        if (int s = scratch(ctx, SLOT_BUILD_B, obytes, &po)) return s;
+        int32_t* counts = static_cast<int32_t*>(pc);
+        int64_t* offs = static_cast<int64_t*>(po);
+        if (int s = edge_rays(0, counts, counts + na, nullptr, nullptr, nullptr, 0, nullptr, 0)) return s;
+        const int64_t n_all = (int64_t)(na + nb);
+        int tb = timer.record();
+        if (n_all > 0)
+            if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all)) return s;
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        // total = last offset + last count; B->A offsets are shifted by the A total
+        int64_t total = 0;
+        if (n_all > 0) {
+            cudaMemcpyAsync(ctx->h_small, offs + n_all - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
+            cudaMemcpyAsync(ctx->h_small + 1, counts + n_all - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        }
+        uint32_t bits = 0;
+        if (int s = read_device_error(ctx, &bits)) return s;
+        if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+        if (n_all > 0) total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
+        // raw keys then sorted keys
+        void* praw = nullptr;
+        if (int s = scratch(ctx, SLOT_TABLE, 8 * (size_t)std::max<int64_t>(total, 1), &praw)) return s;
+        uint64_t* raw = static_cast<uint64_t*>(praw);
+        if (int s = edge_rays(1, nullptr, nullptr, offs, offs + na, raw, 0, nullptr, 0)) return s;
+        void* pk = nullptr;
+        if (int s = scratch(ctx, SLOT_KEYS, 8 * (size_t)std::max<int64_t>(total, 1), &pk)) return s;
+        uint64_t* sorted = static_cast<uint64_t*>(pk);
+        tb = timer.record();
+        int64_t nu = 0;
+        if (total > 0) {
+            if (int s = sort_u64_keys(ctx, raw, sorted, total)) return s;
+            if (int s = unique_u64(ctx, sorted, raw, total, &nu)) return s;
+            cudaMemcpyAsync(sorted, raw, 8 * (size_t)nu, cudaMemcpyDeviceToDevice, ctx->stream);
+        }
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        st.result_capacity = (uint64_t)total;
+        *keys_out = sorted;
+        *n_out = (uint64_t)nu;
+        return PIERCE_OK;
+    }
+
+    // Parity of src first vertices against tgt into the parity table, then
+    // emit odd keys (mode 0: into out_table, mode 1: filtered append).
+    int parity(pierce_dataset* src, pierce_dataset* tgt, int swap, double* ms, int emit_mode, uint64_t* out_table,
+               uint64_t out_slots, const uint64_t* lookup_table, uint64_t lookup_slots, const uint64_t* lookup_sorted,
+               int64_t lookup_n, uint64_t* out_keys, unsigned long long* out_count, uint64_t out_cap) {
+        uint64_t pslots = table_slots_for(8 * (uint64_t)std::max(src->num_objects, 1), 0.5);
+        for (int attempt = 0;; ++attempt) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_BUILD_C, pslots * 12, &p)) return s;
+            uint64_t* ptable = static_cast<uint64_t*>(p);
+            uint32_t* par = reinterpret_cast<uint32_t*>(ptable + pslots);
+            cudaMemsetAsync(ptable, 0xFF, pslots * 8, ctx->stream);
+            cudaMemsetAsync(par, 0, pslots * 4, ctx->stream);
+            int b = timer.record();
+            if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots)) return s;
+            timer.span(b, timer.record(), ms);
+            uint32_t bits = 0;
+            if (int s = read_device_error(ctx, &bits)) return s;
+            if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+            if (bits & ERR_HASH_FULL) {
+                if (attempt >= o.max_retries) return set_error(PIERCE_ERR_HASH_FULL, "parity table full");
+                pslots *= 4;
+                st.retries++;
+                continue;
+            }
+            if (int s = parity_emit(ctx, ptable, par, pslots, emit_mode, lookup_table, lookup_slots, lookup_sorted,
+                                    lookup_n, out_table, out_slots, out_keys, out_count, out_cap))
+                return s;
+            return PIERCE_OK;
+        }
+    }
+
+    int make_result(const uint64_t* keys_sorted, uint64_t n, pierce_result** out) {
+        pierce_result* r = new pierce_result();
+        r->count = n;
+        r->capacity = n;
+        if (int s = device_alloc((void**)&r->d_pairs, std::max<uint64_t>(n, 1) * sizeof(pierce_pair), "result")) {
+            delete r;
+            return s;
+        }
+        if (n) {
+            cudaMemcpyAsync(r->d_pairs, keys_sorted, n * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (int s = keys_to_pairs(ctx, reinterpret_cast<uint64_t*>(r->d_pairs), (int64_t)n)) {
+                pierce_result_destroy(r);
+                return s;
+            }
+        }
+        *out = r;
+        return PIERCE_OK;
+    }
+
+    // Sort the keys in SLOT_KEYS[0..n) (unsorted, unique) into a result.
+    int sort_into_result(uint64_t* keys, uint64_t n, pierce_result** out) {
+        if (n == 0) return make_result(nullptr, 0, out);
+        void* p = nullptr;
+        if (int s = scratch(ctx, SLOT_BUILD_D, n * 8, &p)) return s;
+        int tb = timer.record();
+        if (int s = sort_u64_keys(ctx, keys, static_cast<uint64_t*>(p), (int64_t)n)) return s;
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        return make_result(static_cast<uint64_t*>(p), n, out);
+    }
+
+    // Sort + unique keys[0..n) (may contain duplicates) into a result.
+    int sort_unique_into_result(uint64_t* keys, uint64_t n, pierce_result** out) {
+        if (n == 0) return make_result(nullptr, 0, out);
+        void* p = nullptr;
+        if (int s = scratch(ctx, SLOT_BUILD_D, n * 8, &p)) return s;
+        int tb = timer.record();
+        if (int s = sort_u64_keys(ctx, keys, static_cast<uint64_t*>(p), (int64_t)n)) return s;
+        int64_t nu = 0;
+        if (int s = unique_u64(ctx, static_cast<uint64_t*>(p), keys, (int64_t)n, &nu)) return s;
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        return make_result(keys, (uint64_t)nu, out);
+    }
+
+    int run(pierce_result** out) {
+        cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
+        cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
+        const int t0 = timer.record();
+        int s = PIERCE_OK;
+        if (o.predicate == PIERCE_OVERLAP) s = run_overlap(out);
+        else if (o.predicate == PIERCE_INTERSECTION) s = run_intersection(out);
+        else s = run_containment(out);
+        const int t1 = timer.record();
+        timer.span(t0, t1, &st.ms_total);
+        if (s) return s;
+        cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream);
+        if ((s = sync_ctx(ctx, "join"))) return s;
+        timer.resolve();
+        const DevCounters& c = *ctx->h_counters;
+        st.rays = c.rays;
+        st.node_visits = c.node_visits;
+        st.tri_tests = c.tri_tests;
+        st.raw_hits = c.raw_hits;
+        st.fp32_ambiguous = c.fp32_ambiguous;
+        st.fp64_ambiguous = c.fp64_ambiguous;
+        st.parity_rays = c.parity_rays;
+        st.num_pairs = (*out)->count;
+        return PIERCE_OK;
+    }
+
+    int run_overlap(pierce_result** out) {
+        if (o.sizing == PIERCE_SIZING_TWO_PASS) {
+            uint64_t* keys = nullptr;
+            uint64_t n = 0;
+            if (int s = overlap_two_pass(&keys, &n)) return s;
+            return make_result(keys, n, out);
+        }
+        uint64_t* table = nullptr;
+        uint64_t slots = 0, n = 0;
+        if (int s = overlap_hash(&table, &slots)) return s;
+        uint64_t* keys = nullptr;
+        int tb = timer.record();
+        if (int s = compact(table, slots, 0, &n, &keys)) return s;
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        return sort_into_result(keys, n, out);
+    }
+
+    int run_intersection(pierce_result** out) {
+        if (o.sizing == PIERCE_SIZING_TWO_PASS) {
+            uint64_t* okeys = nullptr;
+            uint64_t n_over = 0;
+            if (int s = overlap_two_pass(&okeys, &n_over)) return s;
+            // parity keys are appended after the overlap keys, then sort + unique
+            const uint64_t extra = (uint64_t)A->num_objects + (uint64_t)B->num_objects;
+            void* p = nullptr;
+            // move overlap keys to a buffer with room for the parity keys
+            if (int s = scratch(ctx, SLOT_TABLE, (n_over + 8 * extra + 16) * 8, &p)) return s;
+            uint64_t* all = static_cast<uint64_t*>(p);
+            if (n_over) cudaMemcpyAsync(all, okeys, n_over * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+            void* pc = nullptr;
+            if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+            unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+            cudaMemsetAsync(d_count, 0, 8, ctx->stream);
+            const uint64_t cap = 8 * extra + 16;
+            if (ab)
+                if (int s = parity(A, B, 0, &st.ms_parity[0], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
+                                   d_count, cap))
+                    return s;
+            if (ba)
+                if (int s = parity(B, A, 1, &st.ms_parity[1], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
+                                   d_count, cap))
+                    return s;
+            cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
+            if (int s = sync_ctx(ctx, "parity count")) return s;
+            const uint64_t n_par = (uint64_t)ctx->h_small[0];
+            if (n_par > cap) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "parity output overflow");
+            return sort_unique_into_result(all, n_over + n_par, out);
+        }
+        uint64_t* table = nullptr;
+        uint64_t slots = 0, n = 0;
+        if (int s = overlap_hash(&table, &slots)) return s;
+        if (ab)
+            if (int s = parity(A, B, 0, &st.ms_parity[0], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
+                return s;
+        if (ba)
+            if (int s = parity(B, A, 1, &st.ms_parity[1], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
+                return s;
+        uint32_t bits = 0;
+        if (int s = read_device_error(ctx, &bits)) return s;
+        if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "pair table full while adding parity pairs");
+        uint64_t* keys = nullptr;
+        int tb = timer.record();
+        if (int s = compact(table, slots, 0, &n, &keys)) return s;
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        return sort_into_result(keys, n, out);
+    }
+
+    int run_containment(pierce_result** out) {
+        // Overlap set of A vs B (both directions as in the reference), then
+        // parity of B's first vertices against A, filtered by the overlap set.
+        const bool save_ab = ab, save_ba = ba;
+        ab = ba = true;
+        uint64_t* table = nullptr;
+        uint64_t slots = 0;
+        uint64_t* okeys = nullptr;
+        uint64_t n_over = 0;
+        const bool two_pass = o.sizing == PIERCE_SIZING_TWO_PASS;
+        if (two_pass) {
+            if (int s = overlap_two_pass(&okeys, &n_over)) return s;
+        } else {
+            if (int s = overlap_hash(&table, &slots)) return s;
+        }
+        ab = save_ab;
+        ba = save_ba;
+        // containment keys buffer (SLOT_TABLE is the hash table or raw keys; use SLOT_BUILD_D)
+        const uint64_t cap = 8 * (uint64_t)std::max(B->num_objects, 1) + 16;
+        void* p = nullptr;
+        if (int s = scratch(ctx, SLOT_BUILD_D, cap * 8, &p)) return s;
+        uint64_t* ckeys = static_cast<uint64_t*>(p);
+        void* pc = nullptr;
+        if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+        unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+        cudaMemsetAsync(d_count, 0, 8, ctx->stream);
+        if (int s = parity(B, A, 1, &st.ms_parity[1], 1, nullptr, 0, table, slots, okeys, (int64_t)n_over, ckeys,
+                           d_count, cap))
+            return s;
+        cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
+        if (int s = sync_ctx(ctx, "containment count")) return s;
+        const uint64_t n_cont = (uint64_t)ctx->h_small[0];
+        if (n_cont > cap) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "containment output overflow");
+        if (!two_pass && o.include_overlap_pairs) {
+            // overlap keys of the table after the containment keys
+            uint64_t* keys = nullptr;
+            if (int s = compact(table, slots, 0, &n_over, &keys)) return s;
+            okeys = keys;
+        }
+        st.containment_pairs = n_cont;
+        st.overlap_pairs = n_over;
+        // sort containment keys (into the front of a combined buffer)
+        const uint64_t n_total = n_cont + (o.include_overlap_pairs ? n_over : 0);
+        pierce_result* r = new pierce_result();
+        r->count = n_total;
+        r->capacity = n_total;
+        r->containment_count = n_cont;
+        if (int s = device_alloc((void**)&r->d_pairs, std::max<uint64_t>(n_total, 1) * 8, "result")) {
+            delete r;
+            return s;
+        }
+        uint64_t* rk = reinterpret_cast<uint64_t*>(r->d_pairs);
+        int tb = timer.record();
+        if (n_cont)
+            if (int s = sort_u64_keys(ctx, ckeys, rk, (int64_t)n_cont)) {
+                pierce_result_destroy(r);
+                return s;
+            }
+        if (o.include_overlap_pairs && n_over) {
+            if (two_pass) {
+                cudaMemcpyAsync(rk + n_cont, okeys, n_over * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+            } else if (int s = sort_u64_keys(ctx, okeys, rk + n_cont, (int64_t)n_over)) {
+                pierce_result_destroy(r);
+                return s;
+            }
+        }
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        if (int s = keys_to_pairs(ctx, rk, (int64_t)n_total)) {
+            pierce_result_destroy(r);
+            return s;
+        }
+        *out = r;
+        return PIERCE_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                pierce_result** out, pierce_stats* stats) {
+    if (!ctx || !a || !b || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: null argument");
+    *out = nullptr;
+    if (!a->built || !b->built) return set_error(PIERCE_ERR_NOT_BUILT, "join: dataset not built");
+    if (a->ctx != ctx || b->ctx != ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: dataset of other ctx");
+    pierce_join_opts o;
+    pierce_default_join_opts(&o);
+    if (opts) o = *opts;
+    if (o.predicate < 0 || o.predicate > 2 || o.direction < 0 || o.direction > 2 || o.sizing < 0 || o.sizing > 2 ||
+        o.precision < 0 || o.precision > 1)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: option out of range");
+    if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
+    cudaSetDevice(ctx->device);
+    const uint64_t l0 = ctx->launches;
+    Join j(ctx, a, b, o);
+    int s = j.run(out);
+    j.st.launches = (int32_t)(ctx->launches - l0);
+    if (stats) *stats = j.st;
+    return s;
+}
+
+int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode,
+                            int precision, int swap, int32_t* d_counts, const int64_t* d_offsets, uint64_t* d_keys,
+                            uint64_t* d_table, uint64_t table_slots, pierce_stats* stats) {
+    if (!ctx || !src || !tgt) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_edge_rays: null argument");
+    if (!tgt->built) return set_error(PIERCE_ERR_NOT_BUILT, "launch_edge_rays: target not built");
+    if (mode == PIERCE_RAYS_COUNT && !d_counts) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "COUNT needs d_counts");
+    if (mode == PIERCE_RAYS_WRITE && (!d_offsets || !d_keys))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "WRITE needs d_offsets and d_keys");
+    if (mode == PIERCE_RAYS_HASH && (!d_table || table_slots == 0 || (table_slots & (table_slots - 1))))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "HASH needs a power-of-two table");
+    cudaSetDevice(ctx->device);
+    cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
+    if (int s = launch_edge_rays(ctx, src, tgt, mode, precision, swap, d_counts, d_offsets, d_keys, d_table,
+                                 table_slots))
+        return s;
+    uint32_t bits = 0;
+    if (int s = read_device_error(ctx, &bits)) return s;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream);
+        if (int s = sync_ctx(ctx, "counters")) return s;
+        stats->rays = ctx->h_counters->rays;
+        stats->node_visits = ctx->h_counters->node_visits;
+        stats->tri_tests = ctx->h_counters->tri_tests;
+        stats->raw_hits = ctx->h_counters->raw_hits;
+        stats->fp32_ambiguous = ctx->h_counters->fp32_ambiguous;
+        stats->fp64_ambiguous = ctx->h_counters->fp64_ambiguous;
+    }
+    if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+    if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "hash table full");
+    return PIERCE_OK;
+}
+
+int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int precision,
+                         int swap, uint64_t* d_table, uint32_t* d_parity, uint64_t table_slots, pierce_stats* stats) {
+    (void)precision;
+    if (!ctx || !src || !tgt || !d_table || !d_parity || table_slots == 0 || (table_slots & (table_slots - 1)))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_parity: bad argument");
+    if (!tgt->built) return set_error(PIERCE_ERR_NOT_BUILT, "launch_parity: target not built");
+    cudaSetDevice(ctx->device);
+    cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
+    if (int s = launch_parity(ctx, src, tgt, swap, d_table, d_parity, table_slots)) return s;
+    uint32_t bits = 0;
+    if (int s = read_device_error(ctx, &bits)) return s;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream);
+        if (int s = sync_ctx(ctx, "counters")) return s;
+        stats->parity_rays = ctx->h_counters->parity_rays;
+        stats->node_visits = ctx->h_counters->node_visits;
+        stats->tri_tests = ctx->h_counters->tri_tests;
+    }
+    if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+    if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "parity table full");
+    return PIERCE_OK;
+}
+
+int pierce_exclusive_scan(pierce_ctx* ctx, const int32_t* d_counts, int64_t* d_offsets, int64_t n, int64_t* total) {
+    if (!ctx || (n > 0 && (!d_counts || !d_offsets)) || !total)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "exclusive_scan: bad argument");
+    cudaSetDevice(ctx->device);
+    *total = 0;
+    if (n <= 0) return PIERCE_OK;
+    if (int s = exclusive_scan_i32_to_i64(ctx, d_counts, d_offsets, n)) return s;
+    cudaMemcpyAsync(ctx->h_small, d_offsets + n - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(ctx->h_small + 1, d_counts + n - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (int s = sync_ctx(ctx, "scan total")) return s;
+    *total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
+    return PIERCE_OK;
+}
+
+int pierce_merge_and_deduplicate_pairs(pierce_ctx* ctx, const pierce_pair* d1, int64_t n1, const pierce_pair* d2,
+                                       int64_t n2, pierce_pair* d_out, int64_t* num_unique) {
+    if (!ctx || !num_unique || n1 < 0 || n2 < 0 || (n1 && !d1) || (n2 && !d2) || ((n1 + n2) && !d_out))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "merge_and_deduplicate: bad argument");
+    cudaSetDevice(ctx->device);
+    *num_unique = 0;
+    const int64_t n = n1 + n2;
+    if (n == 0) return PIERCE_OK;
+    void *pa = nullptr, *pb = nullptr;
+    if (int s = scratch(ctx, SLOT_KEYS, 8 * (size_t)n, &pa)) return s;
+    if (int s = scratch(ctx, SLOT_BUILD_D, 8 * (size_t)n, &pb)) return s;
+    uint64_t* keys = static_cast<uint64_t*>(pa);
+    uint64_t* sorted = static_cast<uint64_t*>(pb);
+    if (n1) pairs_to_keys(ctx, reinterpret_cast<const uint64_t*>(d1), keys, n1);
+    if (n2) pairs_to_keys(ctx, reinterpret_cast<const uint64_t*>(d2), keys + n1, n2);
+    if (int s = sort_u64_keys(ctx, keys, sorted, n)) return s;
+    int64_t nu = 0;
+    if (int s = unique_u64(ctx, sorted, keys, n, &nu)) return s;
+    if (int s = keys_to_pairs(ctx, keys, nu)) return s;
+    cudaMemcpyAsync(d_out, keys, 8 * (size_t)nu, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (int s = sync_ctx(ctx, "merge_and_deduplicate")) return s;
+    *num_unique = nu;
+    return PIERCE_OK;
+}
+
+int pierce_compact_hash_table_pairs(pierce_ctx* ctx, const uint64_t* d_table, uint64_t table_slots, pierce_pair* d_out,
+                                    uint64_t max_output, uint64_t* count) {
+    if (!ctx || !d_table || !count || (max_output && !d_out))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "compact_hash_table_pairs: bad argument");
+    cudaSetDevice(ctx->device);
+    void* pc = nullptr;
+    if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+    unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+    cudaMemsetAsync(d_count, 0, 8, ctx->stream);
+    uint64_t* out = reinterpret_cast<uint64_t*>(d_out);
+    if (int s = compact_table(ctx, d_table, table_slots, out, max_output, d_count)) return s;
+    cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (int s = sync_ctx(ctx, "compact")) return s;
+    *count = (uint64_t)ctx->h_small[0];
+    const uint64_t n = std::min(*count, max_output);
+    if (int s = keys_to_pairs(ctx, out, (int64_t)n)) return s;
+    if (int s = sync_ctx(ctx, "compact")) return s;
+    if (*count > max_output)
+        return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "compact_hash_table_pairs: more pairs than max_output");
+    return PIERCE_OK;
+}
+
+int pierce_estimate_pairs(pierce_ctx* ctx, const void* cells_a, uint32_t num_a, const void* cells_b, uint32_t num_b,
+                          float cell_size, float epsilon, float gamma, int alpha_correction, double* raw,
+                          int64_t* estimate, int32_t* matched_cells) {
+    if (!ctx || (num_a && !cells_a) || (num_b && !cells_b) || !raw || !estimate)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "estimate_pairs: bad argument");
+    struct Cell {
+        int32_t ix, iy, iz;
+        uint32_t center, touch;
+        float size, ratio;
+    };
+    static_assert(sizeof(Cell) == 28, "cell layout");
+    const Cell* A = static_cast<const Cell*>(cells_a);
+    const Cell* B = static_cast<const Cell*>(cells_b);
+    // match cells of B against A by index
+    struct H {
+        size_t operator()(uint64_t k) const { return std::hash<uint64_t>()(k * 0x9E3779B97F4A7C15ULL); }
+    };
+    auto key = [](const Cell& c) {
+        return ((uint64_t)(uint32_t)c.ix * 0x100000001B3ULL) ^ ((uint64_t)(uint32_t)c.iy << 21) ^
+               ((uint64_t)(uint32_t)c.iz << 42);
+    };
+    std::unordered_multimap<uint64_t, uint32_t, H> map;
+    map.reserve(num_a * 2 + 1);
+    for (uint32_t i = 0; i < num_a; ++i) map.emplace(key(A[i]), i);
+    std::vector<Cell> ma, mb;
+    for (uint32_t i = 0; i < num_b; ++i) {
+        auto range = map.equal_range(key(B[i]));
+        for (auto it = range.first; it != range.second; ++it) {
+            const Cell& a = A[it->second];
+            if (a.ix == B[i].ix && a.iy == B[i].iy && a.iz == B[i].iz) {
+                ma.push_back(a);
+                mb.push_back(B[i]);
+                break;
+            }
+        }
+    }
+    float cell_volume = cell_size * cell_size * cell_size;
+    double total = 0.0;
+    if (!ma.empty())
+        if (int s = estimate_cells(ctx, ma.data(), mb.data(), (int)ma.size(), cell_volume, epsilon, gamma, &total))
+            return s;
+    // global average size / volume ratio weighted by touch counts
+    auto avg = [](const Cell* c, uint32_t n, bool ratio) {
+        double sum = 0.0;
+        long long cnt = 0;
+        for (uint32_t i = 0; i < n; ++i)
+            if (c[i].touch > 0) {
+                sum += (double)(ratio ? c[i].ratio : c[i].size) * (double)c[i].touch;
+                cnt += c[i].touch;
+            }
+        if (cnt == 0) return ratio ? 1.0f : 0.0f;
+        return (float)(sum / cnt);
+    };
+    const float eff_a = avg(A, num_a, false) * std::cbrt(avg(A, num_a, true));
+    const float eff_b = avg(B, num_b, false) * std::cbrt(avg(B, num_b, true));
+    const float comb = eff_a + eff_b;
+    const float mink = comb * comb * comb;
+    if (cell_volume < 1e-9f) cell_volume = 1e-9f;
+    float alpha = 1.0f;
+    if (alpha_correction) {
+        alpha = mink / cell_volume;
+        if (alpha < 1.0f) alpha = 1.0f;
+    }
+    *raw = total;
+    *estimate = (int64_t)((float)total / alpha);
+    if (matched_cells) *matched_cells = (int32_t)ma.size();
+    return PIERCE_OK;
+}
+
+}  // extern "C"

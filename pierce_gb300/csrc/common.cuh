@@ -1,0 +1,147 @@
+// Shared device/host definitions of the GB300 join library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/pierce_capi.h"
+
+namespace pgpu {
+
+// Device-side error bits, OR-ed into one word per context and translated to
+// pierce_status codes by the host after each join phase.
+enum ErrBits : uint32_t {
+    ERR_HASH_FULL = 1u,
+    ERR_STACK_OVERFLOW = 2u,
+    ERR_OUTPUT_OVERFLOW = 4u,
+    ERR_QUEUE_TIMEOUT = 8u,
+};
+
+constexpr uint64_t kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kStackSize = 64;  // >= depth of any LBVH over 30-bit Morton + index keys
+
+// Counters accumulated by traversal kernels (one atomicAdd per warp).
+struct DevCounters {
+    unsigned long long rays;
+    unsigned long long node_visits;
+    unsigned long long tri_tests;
+    unsigned long long raw_hits;
+    unsigned long long fp32_ambiguous;
+    unsigned long long fp64_ambiguous;
+    unsigned long long parity_rays;
+    unsigned long long pad;
+};
+
+// Binary BVH node holding the boxes of its two children (64 bytes, four
+// 16-byte vector loads).  Child encoding: c >= 0 internal node index,
+// c < 0 leaf whose triangles are soup[~c .. ~c + count).
+struct __align__(16) Node {
+    float4 bx;   // c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x
+    float4 by;   // c0.lo.y, c0.hi.y, c1.lo.y, c1.hi.y
+    float4 bz;   // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
+    int4 ch;     // child0, child1, leaf count of child0, leaf count of child1
+};
+
+// Device view of one dataset (all pointers into its own allocations).
+struct DevDataset {
+    // triangle soup in BVH leaf order: per triangle 3 float4:
+    //   (v0.xyz, object id bits), (v1.xyz, original triangle index bits), (v2.xyz, 0)
+    const float4* soup;
+    const Node* nodes;
+    int64_t num_tris;
+    int root_is_leaf;       // 1 when the whole dataset is a single leaf
+    int root_leaf_count;
+    // edge rays, 2 float4 per edge: (start.xyz, src object bits), (end.xyz, 0)
+    const float4* edges;
+    int64_t num_edges;
+    // objects
+    const float4* first_vertex;  // per object (xyz, 0)
+    const float* obj_box;        // per object 6 floats lo.xyz hi.xyz
+    int32_t num_objects;
+};
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace pgpu
+
+// ---- host-side internal objects ------------------------------------------
+
+struct pierce_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_err = nullptr;
+    pgpu::DevCounters* d_counters = nullptr;
+    uint32_t* h_err = nullptr;                 // pinned
+    pgpu::DevCounters* h_counters = nullptr;   // pinned
+    int64_t* h_small = nullptr;                // pinned scratch for scalar readbacks (8 values)
+    // grow-only scratch buffers reused across joins
+    void* scratch[8] = {nullptr};
+    size_t scratch_bytes[8] = {0};
+    uint64_t launches = 0;
+    int sm_count = 0;
+};
+
+struct pierce_dataset {
+    pierce_ctx* ctx = nullptr;
+    uint64_t nv = 0, nt = 0, ne = 0;
+    int32_t num_objects = 0;
+    float* d_vertices = nullptr;
+    uint32_t* d_indices = nullptr;
+    int32_t* d_tri_to_object = nullptr;
+    float4* d_edges = nullptr;
+    float4* d_soup = nullptr;
+    pgpu::Node* d_nodes = nullptr;
+    float4* d_first_vertex = nullptr;
+    float* d_obj_box = nullptr;
+    uint64_t num_nodes = 0;
+    int built = 0;
+    int root_is_leaf = 0, root_leaf_count = 0;
+    int leaf_size = 1;
+    double ms_build = 0.0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    uint64_t device_bytes = 0;
+
+    pgpu::DevDataset view() const {
+        pgpu::DevDataset v;
+        v.soup = d_soup;
+        v.nodes = d_nodes;
+        v.num_tris = (int64_t)nt;
+        v.root_is_leaf = root_is_leaf;
+        v.root_leaf_count = root_leaf_count;
+        v.edges = d_edges;
+        v.num_edges = (int64_t)ne;
+        v.first_vertex = d_first_vertex;
+        v.obj_box = d_obj_box;
+        v.num_objects = num_objects;
+        return v;
+    }
+};
+
+struct pierce_result {
+    pierce_pair* d_pairs = nullptr;
+    uint64_t count = 0;
+    uint64_t capacity = 0;
+    uint64_t containment_count = 0;
+};
+
+namespace pgpu {
+// error reporting (capi.cu)
+int set_error(int status, const std::string& msg);
+int check_cuda(cudaError_t e, const char* what);
+// grow-only scratch buffer `slot` of at least `bytes`
+int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out);
+int device_alloc(void** p, size_t bytes, const char* what);
+
+// lbvh.cu
+int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);
+int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds);
+
+// sortscan.cu (CUB library calls)
+int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,
+                   int64_t n, int end_bit);
+int sort_u64_keys(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, int64_t n);
+int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
+int unique_u64(pierce_ctx* ctx, const uint64_t* in, uint64_t* out, int64_t n, int64_t* num_unique);
+}  // namespace pgpu

@@ -1,0 +1,529 @@
+// Join kernels: edge-ray traversal, +Z parity rays, pair hash set,
+// compaction, and the host orchestration of the overlap, intersection and
+// containment joins.
+//
+// Edge rays (pierce/query/src/cuda/mesh_overlap_edges.cu:105-208): every
+// unique edge of the source dataset is a closed segment; one thread per edge
+// walks the target BVH with an exact box-overlap test (segment box vs child
+// box, comparisons only) and tests the triangles of every reached leaf.  All
+// hits are collected in a single traversal (the reference re-traces up to
+// overlap_max_iterations times, advancing tmin past each hit).  Consecutive
+// hits on one target object are emitted once.  Output modes: COUNT (hits per
+// edge, pass 1 of the two-pass method), WRITE (keys at scanned offsets,
+// pass 2), HASH (insert into the pair set, the reference's hash mode).
+//
+// Parity rays (mesh_intersection_anyhit.cu:46-240, mesh_containment.cu:
+// 224-293): one thread per source object casts +Z from its first vertex and
+// toggles the parity of (source, target-object) in a per-join parity table;
+// odd entries are the "inside" pairs.
+//
+// Hash set (mesh_overlap_edges.cu:61-103): 64-bit keys (a << 32 | b), empty
+// slot all ones, MurmurHash3 fmix64 finaliser, linear probing in a
+// power-of-two table.  A probe sequence that exhausts its bound sets
+// ERR_HASH_FULL instead of silently dropping the pair; the host then
+// enlarges the table and reruns.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "predicates.cuh"
+
+namespace pgpu {
+
+enum RayMode { MODE_COUNT = 0, MODE_WRITE = 1, MODE_HASH = 2 };
+enum Precision { PREC_EXACT = 0, PREC_FP32 = 1 };
+
+constexpr int kShortStack = 32;  // stack entries kept in shared memory per thread
+
+__device__ __forceinline__ uint64_t fmix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return k;
+}
+
+__device__ __forceinline__ uint64_t pack_key(int32_t a, int32_t b) {
+    return ((uint64_t)(uint32_t)a << 32) | (uint64_t)(uint32_t)b;
+}
+
+// Insert; returns slot index or -1 when the probe bound is exhausted.
+__device__ __forceinline__ int64_t hash_insert(uint64_t* table, uint64_t mask, uint64_t key, uint32_t* err) {
+    uint64_t h = fmix64(key) & mask;
+    for (uint64_t i = 0; i <= mask; ++i) {
+        const uint64_t cur = __ldcg(table + h);
+        if (cur == key) return (int64_t)h;
+        if (cur == kEmptyKey) {
+            const unsigned long long old =
+                atomicCAS(reinterpret_cast<unsigned long long*>(table + h), (unsigned long long)kEmptyKey,
+                          (unsigned long long)key);
+            if (old == kEmptyKey || old == key) return (int64_t)h;
+        }
+        h = (h + 1) & mask;
+    }
+    atomicOr(err, ERR_HASH_FULL);
+    return -1;
+}
+
+__device__ __forceinline__ bool hash_contains(const uint64_t* table, uint64_t mask, uint64_t key) {
+    uint64_t h = fmix64(key) & mask;
+    for (uint64_t i = 0; i <= mask; ++i) {
+        const uint64_t cur = __ldcg(table + h);
+        if (cur == key) return true;
+        if (cur == kEmptyKey) return false;
+        h = (h + 1) & mask;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool sorted_contains(const uint64_t* keys, int64_t n, uint64_t key) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        const uint64_t v = keys[mid];
+        if (v < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < n && keys[lo] == key;
+}
+
+// Warp-aggregated counter flush: one atomicAdd per warp.
+__device__ __forceinline__ void flush_counter(unsigned long long* dst, unsigned long long v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+struct EdgeRayParams {
+    DevDataset src, tgt;
+    int swap;
+    int32_t* counts;
+    const int64_t* offsets;
+    uint64_t* keys;
+    uint64_t* table;
+    uint64_t mask;
+    uint32_t* err;
+    DevCounters* ctr;
+};
+
+__device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float hy, float lz, float hz,
+                                            const float3& lo, const float3& hi) {
+    return lx <= hi.x && lo.x <= hx && ly <= hi.y && lo.y <= hy && lz <= hi.z && lo.z <= hz;
+}
+
+template <int MODE, int PREC>
+__global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
+    __shared__ int sstack[kShortStack][128];
+    int lstack[kStackSize - kShortStack];
+    const int tid = threadIdx.x;
+    uint32_t n_nodes = 0, n_tests = 0, n_hits = 0;
+    PredCounters pc{0, 0};
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
+    const bool active = e < P.src.num_edges;
+    if (active) {
+        const float4 s4 = __ldg(P.src.edges + 2 * e);
+        const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
+        const int32_t src_obj = __float_as_int(s4.w);
+        const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
+        const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
+        const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
+        int64_t out = (MODE == MODE_WRITE) ? P.offsets[e] : 0;
+        int32_t last_obj = -1;
+        int nhit = 0;
+        auto leaf = [&](int first, int count) {
+            for (int k = 0; k < count; ++k) {
+                const int64_t t = (int64_t)first + k;
+                const float4 a4 = __ldg(P.tgt.soup + 3 * t);
+                const int32_t obj = __float_as_int(a4.w);
+                if (obj == last_obj) continue;
+                const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
+                const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
+                if (count > 1) {
+                    const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
+                    const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
+                    const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
+                    if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
+                }
+                ++n_tests;
+                const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
+                             c = make_float3(c4.x, c4.y, c4.z);
+                const bool hit = (PREC == PREC_EXACT) ? seg_tri_exact(p, q, a, b, c, pc) : seg_tri_mt_fp32(p, q, a, b, c);
+                if (!hit) continue;
+                last_obj = obj;
+                ++nhit;
+                if (MODE == MODE_COUNT) continue;
+                const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
+                if (MODE == MODE_WRITE) P.keys[out++] = key;
+                else hash_insert(P.table, P.mask, key, P.err);
+            }
+        };
+        if (P.tgt.root_is_leaf) {
+            if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+        } else {
+            int sp = 0;
+            int node = 0;
+            for (;;) {
+                ++n_nodes;
+                const Node* nd = P.tgt.nodes + node;
+                const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+                const int4 ch = __ldg(&nd->ch);
+                bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
+                bool h1 = box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
+                if (h0 && ch.x < 0) {
+                    leaf(~ch.x, ch.z);
+                    h0 = false;
+                }
+                if (h1 && ch.y < 0) {
+                    leaf(~ch.y, ch.w);
+                    h1 = false;
+                }
+                if (h0 && h1) {
+                    if (sp >= kStackSize) {
+                        atomicOr(P.err, ERR_STACK_OVERFLOW);
+                        break;
+                    }
+                    if (sp < kShortStack) sstack[sp][tid] = ch.y;
+                    else lstack[sp - kShortStack] = ch.y;
+                    ++sp;
+                    node = ch.x;
+                } else if (h0) {
+                    node = ch.x;
+                } else if (h1) {
+                    node = ch.y;
+                } else {
+                    if (sp == 0) break;
+                    --sp;
+                    node = sp < kShortStack ? sstack[sp][tid] : lstack[sp - kShortStack];
+                }
+            }
+        }
+        if (MODE == MODE_COUNT) P.counts[e] = nhit;
+        n_hits = (uint32_t)nhit;
+    }
+    flush_counter(&P.ctr->rays, active ? 1ull : 0ull);
+    flush_counter(&P.ctr->node_visits, n_nodes);
+    flush_counter(&P.ctr->tri_tests, n_tests);
+    flush_counter(&P.ctr->raw_hits, n_hits);
+    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+}
+
+struct ParityParams {
+    DevDataset src, tgt;
+    int swap;
+    uint64_t* table;
+    uint32_t* parity;
+    uint64_t mask;
+    uint32_t* err;
+    DevCounters* ctr;
+};
+
+__global__ void __launch_bounds__(128) k_parity(ParityParams P) {
+    __shared__ int sstack[kShortStack][128];
+    int lstack[kStackSize - kShortStack];
+    const int tid = threadIdx.x;
+    uint32_t n_nodes = 0, n_tests = 0, n_cross = 0;
+    PredCounters pc{0, 0};
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + tid;
+    bool active = o < P.src.num_objects;
+    if (active) {
+        const float4 fv = __ldg(P.src.first_vertex + o);
+        active = fv.w == 0.0f;
+        const float3 p = make_float3(fv.x, fv.y, fv.z);
+        auto leaf = [&](int first, int count) {
+            for (int k = 0; k < count; ++k) {
+                const int64_t t = (int64_t)first + k;
+                const float4 a4 = __ldg(P.tgt.soup + 3 * t), b4 = __ldg(P.tgt.soup + 3 * t + 1),
+                             c4 = __ldg(P.tgt.soup + 3 * t + 2);
+                if (count > 1) {
+                    if (fminf(a4.x, fminf(b4.x, c4.x)) > p.x || fmaxf(a4.x, fmaxf(b4.x, c4.x)) < p.x ||
+                        fminf(a4.y, fminf(b4.y, c4.y)) > p.y || fmaxf(a4.y, fmaxf(b4.y, c4.y)) < p.y ||
+                        fmaxf(a4.z, fmaxf(b4.z, c4.z)) < p.z)
+                        continue;
+                }
+                ++n_tests;
+                if (!zray_cross(p, make_float3(a4.x, a4.y, a4.z), make_float3(b4.x, b4.y, b4.z),
+                                make_float3(c4.x, c4.y, c4.z), pc))
+                    continue;
+                ++n_cross;
+                const int32_t obj = __float_as_int(a4.w);
+                const uint64_t key = P.swap ? pack_key(obj, (int32_t)o) : pack_key((int32_t)o, obj);
+                const int64_t slot = hash_insert(P.table, P.mask, key, P.err);
+                if (slot >= 0) P.parity[slot] ^= 1u;  // keys of one source are owned by one thread
+            }
+        };
+        if (active) {
+            if (P.tgt.root_is_leaf) {
+                if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+            } else {
+                int sp = 0, node = 0;
+                for (;;) {
+                    ++n_nodes;
+                    const Node* nd = P.tgt.nodes + node;
+                    const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+                    const int4 ch = __ldg(&nd->ch);
+                    bool h0 = bx.x <= p.x && p.x <= bx.y && by.x <= p.y && p.y <= by.y && bz.y >= p.z;
+                    bool h1 = bx.z <= p.x && p.x <= bx.w && by.z <= p.y && p.y <= by.w && bz.w >= p.z;
+                    if (h0 && ch.x < 0) {
+                        leaf(~ch.x, ch.z);
+                        h0 = false;
+                    }
+                    if (h1 && ch.y < 0) {
+                        leaf(~ch.y, ch.w);
+                        h1 = false;
+                    }
+                    if (h0 && h1) {
+                        if (sp >= kStackSize) {
+                            atomicOr(P.err, ERR_STACK_OVERFLOW);
+                            break;
+                        }
+                        if (sp < kShortStack) sstack[sp][tid] = ch.y;
+                        else lstack[sp - kShortStack] = ch.y;
+                        ++sp;
+                        node = ch.x;
+                    } else if (h0) {
+                        node = ch.x;
+                    } else if (h1) {
+                        node = ch.y;
+                    } else {
+                        if (sp == 0) break;
+                        --sp;
+                        node = sp < kShortStack ? sstack[sp][tid] : lstack[sp - kShortStack];
+                    }
+                }
+            }
+        }
+    }
+    flush_counter(&P.ctr->parity_rays, active ? 1ull : 0ull);
+    flush_counter(&P.ctr->node_visits, n_nodes);
+    flush_counter(&P.ctr->tri_tests, n_tests);
+    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+    (void)n_cross;
+}
+
+// Odd-parity entries of a parity table.  mode 0: insert into out_table;
+// mode 1 (containment): keep only keys absent from the overlap set (hash
+// table or sorted array) and append them to out_keys.
+__global__ void k_parity_emit(const uint64_t* __restrict__ ptable, const uint32_t* __restrict__ parity, uint64_t pslots,
+                              int mode, const uint64_t* lookup_table, uint64_t lookup_mask,
+                              const uint64_t* lookup_sorted, int64_t lookup_n, uint64_t* out_table, uint64_t out_mask,
+                              uint64_t* out_keys, unsigned long long* out_count, uint64_t out_cap, uint32_t* err) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < pslots; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = ptable[i];
+        if (key == kEmptyKey || !(parity[i] & 1u)) continue;
+        if (mode == 1) {
+            const bool in = lookup_table ? hash_contains(lookup_table, lookup_mask, key)
+                                         : sorted_contains(lookup_sorted, lookup_n, key);
+            if (in) continue;
+        }
+        if (out_table) {
+            hash_insert(out_table, out_mask, key, err);
+        } else {
+            const unsigned long long pos = atomicAdd(out_count, 1ull);
+            if (pos < out_cap) out_keys[pos] = key;
+        }
+    }
+}
+
+// Occupied slots -> dense key array (warp-aggregated cursor).  The counter
+// counts every occupied slot, so an undersized output is detected.
+__global__ void k_compact(const uint64_t* __restrict__ table, uint64_t slots, uint64_t* __restrict__ out,
+                          unsigned long long* count, uint64_t cap) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < slots; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const uint64_t key = i < slots ? __ldcs(table + i) : kEmptyKey;
+        const bool valid = key != kEmptyKey;
+        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, valid);
+        if (!ballot) continue;
+        const int lane = threadIdx.x & 31;
+        unsigned long long wbase = 0;
+        if (lane == 0) wbase = atomicAdd(count, (unsigned long long)__popc(ballot));
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+        if (valid) {
+            const unsigned long long pos = wbase + __popc(ballot & ((1u << lane) - 1u));
+            if (pos < cap) out[pos] = key;
+        }
+    }
+}
+
+// sorted keys (a << 32 | b) -> pierce_pair {a, b}, in place
+__global__ void k_keys_to_pairs(uint64_t* keys, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        keys[i] = (k >> 32) | (k << 32);
+    }
+}
+
+// pierce_pair {a, b} -> key (a << 32 | b)
+__global__ void k_pairs_to_keys(const uint64_t* __restrict__ pairs, uint64_t* __restrict__ keys, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = pairs[i];
+        keys[i] = (v >> 32) | (v << 32);
+    }
+}
+
+// =====================================================================
+// host side
+// =====================================================================
+
+static inline int grid_cap(pierce_ctx* ctx, int64_t n, int block) {
+    int64_t blocks = (n + block - 1) / block;
+    const int64_t cap = (int64_t)ctx->sm_count * 32;
+    if (blocks > cap) blocks = cap;
+    return (int)(blocks < 1 ? 1 : blocks);
+}
+
+static uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+int launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode, int precision,
+                     int swap, int32_t* counts, const int64_t* offsets, uint64_t* keys, uint64_t* table,
+                     uint64_t slots) {
+    if (src->ne == 0) return PIERCE_OK;
+    EdgeRayParams P;
+    P.src = src->view();
+    P.tgt = tgt->view();
+    P.swap = swap;
+    P.counts = counts;
+    P.offsets = offsets;
+    P.keys = keys;
+    P.table = table;
+    P.mask = slots ? slots - 1 : 0;
+    P.err = ctx->d_err;
+    P.ctr = ctx->d_counters;
+    const int B = 128;
+    const int64_t blocks = ((int64_t)src->ne + B - 1) / B;
+    if (blocks > 0x7FFFFFFF) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "too many edges for one launch");
+    dim3 g((unsigned)blocks);
+    cudaStream_t st = ctx->stream;
+#define PG_LAUNCH(M, PR) k_edge_rays<M, PR><<<g, B, 0, st>>>(P)
+    if (precision == PREC_EXACT) {
+        if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PREC_EXACT);
+        else if (mode == MODE_WRITE) PG_LAUNCH(MODE_WRITE, PREC_EXACT);
+        else PG_LAUNCH(MODE_HASH, PREC_EXACT);
+    } else {
+        if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PREC_FP32);
+        else if (mode == MODE_WRITE) PG_LAUNCH(MODE_WRITE, PREC_FP32);
+        else PG_LAUNCH(MODE_HASH, PREC_FP32);
+    }
+#undef PG_LAUNCH
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "edge ray kernel");
+}
+
+int launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int swap, uint64_t* table,
+                  uint32_t* parity, uint64_t slots) {
+    if (src->num_objects <= 0) return PIERCE_OK;
+    ParityParams P;
+    P.src = src->view();
+    P.tgt = tgt->view();
+    P.swap = swap;
+    P.table = table;
+    P.parity = parity;
+    P.mask = slots - 1;
+    P.err = ctx->d_err;
+    P.ctr = ctx->d_counters;
+    const int B = 128;
+    k_parity<<<(unsigned)((src->num_objects + B - 1) / B), B, 0, ctx->stream>>>(P);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "parity kernel");
+}
+
+int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
+                  unsigned long long* d_count) {
+    k_compact<<<grid_cap(ctx, (int64_t)slots, 256), 256, 0, ctx->stream>>>(table, slots, out, d_count, cap);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "compact kernel");
+}
+
+int keys_to_pairs(pierce_ctx* ctx, uint64_t* keys, int64_t n) {
+    if (n <= 0) return PIERCE_OK;
+    k_keys_to_pairs<<<grid_cap(ctx, n, 256), 256, 0, ctx->stream>>>(keys, n);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "keys_to_pairs");
+}
+
+int pairs_to_keys(pierce_ctx* ctx, const uint64_t* pairs, uint64_t* keys, int64_t n) {
+    if (n <= 0) return PIERCE_OK;
+    k_pairs_to_keys<<<grid_cap(ctx, n, 256), 256, 0, ctx->stream>>>(pairs, keys, n);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "pairs_to_keys");
+}
+
+int parity_emit(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots, int mode,
+                const uint64_t* lookup_table, uint64_t lookup_slots, const uint64_t* lookup_sorted, int64_t lookup_n,
+                uint64_t* out_table, uint64_t out_slots, uint64_t* out_keys, unsigned long long* out_count,
+                uint64_t out_cap) {
+    k_parity_emit<<<grid_cap(ctx, (int64_t)pslots, 256), 256, 0, ctx->stream>>>(
+        ptable, parity, pslots, mode, lookup_table, lookup_slots ? lookup_slots - 1 : 0, lookup_sorted, lookup_n,
+        out_table, out_slots ? out_slots - 1 : 0, out_keys, out_count, out_cap, ctx->d_err);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "parity emit");
+}
+
+// Grid selectivity estimate per matched cell (estimateSelectivityKernel,
+// pierce/query/src/cuda/estimated_overlap.cu:8-41): TouchA * TouchB *
+// min(1, (sizeA + sizeB + eps)^3 / Vcell * sqrt(ratioA * ratioB)^gamma),
+// summed in double.
+struct GridCellRec {
+    int32_t ix, iy, iz;
+    uint32_t center, touch;
+    float size, ratio;
+};
+
+__global__ void k_estimate(const GridCellRec* __restrict__ a, const GridCellRec* __restrict__ b, int n,
+                           float cell_volume, float eps, float gamma, double* total) {
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const GridCellRec A = a[i], B = b[i];
+        if (A.touch == 0 || B.touch == 0) continue;
+        const float comb = A.size + B.size + eps;
+        float prob = comb * comb * comb / cell_volume;
+        prob *= powf(sqrtf(A.ratio * B.ratio), gamma);
+        prob = fminf(prob, 1.0f);
+        acc += (double)((float)A.touch * (float)B.touch * prob);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, off);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(total, acc);
+}
+
+int estimate_cells(pierce_ctx* ctx, const void* a, const void* b, int n, float cell_volume, float eps, float gamma,
+                   double* total) {
+    void* p = nullptr;
+    const size_t bytes = sizeof(GridCellRec) * (size_t)n;
+    if (int s = scratch(ctx, 7, 2 * bytes + 64, &p)) return s;
+    GridCellRec* da = static_cast<GridCellRec*>(p);
+    GridCellRec* db = da + n;
+    double* dt = reinterpret_cast<double*>(db + n);
+    cudaMemcpyAsync(da, a, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(dt, 0, sizeof(double), ctx->stream);
+    if (cell_volume < 1e-9f) cell_volume = 1e-9f;
+    k_estimate<<<grid_cap(ctx, n, 256), 256, 0, ctx->stream>>>(da, db, n, cell_volume, eps, gamma, dt);
+    ctx->launches += 1;
+    cudaMemcpyAsync(ctx->h_small, dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "estimate")) return s;
+    std::memcpy(total, ctx->h_small, sizeof(double));
+    return PIERCE_OK;
+}
+
+uint64_t table_slots_for(uint64_t expected, double load_factor) {
+    if (load_factor <= 0.0 || load_factor > 1.0) load_factor = 0.5;
+    double want = (double)std::max<uint64_t>(expected, 1) / load_factor;
+    uint64_t s = next_pow2((uint64_t)std::ceil(want));
+    if (s < 1024) s = 1024;
+    const uint64_t cap = 1ull << 34;
+    if (s > cap) s = cap;
+    return s;
+}
+
+}  // namespace pgpu

@@ -1,0 +1,423 @@
+// Linear BVH construction over a dataset's triangles (replaces the OptiX
+// GAS build of pierce/query/src/optix/OptixAccelerationStructure.cpp:22-68).
+//
+// Steps, all on the context stream:
+//   1. centroids + centroid bounds (block reduction, ordered-integer atomics);
+//   2. 30-bit Morton codes of the centroids in the centroid bounds;
+//   3. radix sort of (code, triangle) pairs (CUB, sortscan.cu);
+//   4. triangle soup in sorted order: 3 float4 per triangle, object id and
+//      original index carried in the w lanes;
+//   5. hierarchy: Karras 2012 ("Maximizing Parallelism in the Construction
+//      of BVHs, Octrees, and k-d Trees"), restated; equal codes are split by
+//      index so every node has a unique split and the depth is bounded by
+//      30 + 32 levels;
+//   6. bottom-up refit: each leaf walks to the root, the second thread to
+//      reach a node (atomic arrival counter) merges the two child boxes.
+//      Child boxes are stored in the parent (Node::bx/by/bz), which is the
+//      layout the traversal reads;
+//   7. optional leaf collapse: children covering <= leaf_size triangles
+//      become leaves over their contiguous soup range.
+// All box arithmetic is min/max of input floats, so boxes are exact.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace pgpu {
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__device__ __forceinline__ float3 load_vertex(const float* v, uint32_t i) {
+    return make_float3(__ldg(v + 3 * (size_t)i), __ldg(v + 3 * (size_t)i + 1), __ldg(v + 3 * (size_t)i + 2));
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint32_t value, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+// 1. centroids and their bounds (bounds[0..2] ordered min, [3..5] ordered max)
+__global__ void k_centroids(const float* __restrict__ verts, const uint32_t* __restrict__ idx, int64_t nt,
+                            float4* __restrict__ cen, uint32_t* __restrict__ bounds) {
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
+        const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
+        const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
+        const float3 m = make_float3((a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
+                                     (a.z + b.z + c.z) * (1.0f / 3.0f));
+        cen[t] = make_float4(m.x, m.y, m.z, 0.0f);
+        mn[0] = fminf(mn[0], m.x); mn[1] = fminf(mn[1], m.y); mn[2] = fminf(mn[2], m.z);
+        mx[0] = fmaxf(mx[0], m.x); mx[1] = fmaxf(mx[1], m.y); mx[2] = fmaxf(mx[2], m.z);
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(bounds + k, f2o(mn[k]));
+            atomicMax(bounds + 3 + k, f2o(mx[k]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// 2. Morton codes
+__global__ void k_morton(const float4* __restrict__ cen, int64_t nt, const uint32_t* __restrict__ bounds,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const float lo[3] = {o2f(bounds[0]), o2f(bounds[1]), o2f(bounds[2])};
+    const float hi[3] = {o2f(bounds[3]), o2f(bounds[4]), o2f(bounds[5])};
+    float inv[3];
+    for (int k = 0; k < 3; ++k) inv[k] = hi[k] > lo[k] ? 1.0f / (hi[k] - lo[k]) : 0.0f;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const float4 c = cen[t];
+        const float cc[3] = {c.x, c.y, c.z};
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            float u = (cc[k] - lo[k]) * inv[k];
+            u = fminf(fmaxf(u, 0.0f), 1.0f);
+            q[k] = min((uint32_t)(u * 1024.0f), 1023u);
+        }
+        keys[t] = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+        vals[t] = (uint32_t)t;
+    }
+}
+
+// 4. triangle soup in sorted order
+__global__ void k_soup(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                       const int32_t* __restrict__ t2o, const uint32_t* __restrict__ order, int64_t nt,
+                       float4* __restrict__ soup) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nt; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t t = order[j];
+        const float3 a = load_vertex(verts, __ldg(idx + 3 * (size_t)t));
+        const float3 b = load_vertex(verts, __ldg(idx + 3 * (size_t)t + 1));
+        const float3 c = load_vertex(verts, __ldg(idx + 3 * (size_t)t + 2));
+        soup[3 * j + 0] = make_float4(a.x, a.y, a.z, __int_as_float(__ldg(t2o + t)));
+        soup[3 * j + 1] = make_float4(b.x, b.y, b.z, __int_as_float((int)t));
+        soup[3 * j + 2] = make_float4(c.x, c.y, c.z, 0.0f);
+    }
+}
+
+// longest common prefix of sorted keys i and j (index tie-break), -1 outside
+__device__ __forceinline__ int lcp(const uint32_t* keys, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t ki = keys[i], kj = keys[j];
+    if (ki == kj) return 32 + __clzll((unsigned long long)(i ^ j)) - 32;  // 32 + clz over 32-bit index
+    return __clz(ki ^ kj);
+}
+
+// 5. Karras hierarchy: internal node i covers sorted range [first, last]
+__global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, Node* __restrict__ nodes,
+                         int32_t* __restrict__ parent_int, int32_t* __restrict__ parent_leaf,
+                         int2* __restrict__ range) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n - 1; i += (int64_t)gridDim.x * blockDim.x) {
+        const int d = (lcp(keys, n, i, i + 1) - lcp(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = lcp(keys, n, i, i - d);
+        int64_t lmax = 2;
+        while (lcp(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int64_t l = 0;
+        for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+            if (lcp(keys, n, i, i + (l + t) * d) > dmin) l += t;
+        const int64_t j = i + l * d;
+        const int dnode = lcp(keys, n, i, j);
+        int64_t s = 0, t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (lcp(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+        const int64_t first = i < j ? i : j, last = i < j ? j : i;
+        int c0, c1;
+        if (first == gamma) {
+            c0 = ~(int)gamma;
+            parent_leaf[gamma] = (int)i;
+        } else {
+            c0 = (int)gamma;
+            parent_int[gamma] = (int)i;
+        }
+        if (last == gamma + 1) {
+            c1 = ~(int)(gamma + 1);
+            parent_leaf[gamma + 1] = (int)i;
+        } else {
+            c1 = (int)(gamma + 1);
+            parent_int[gamma + 1] = (int)i;
+        }
+        nodes[i].ch = make_int4(c0, c1, 1, 1);
+        range[i] = make_int2((int)first, (int)last);
+        if (i == 0) parent_int[0] = -1;
+    }
+}
+
+__device__ __forceinline__ void store_child_box(Node* nd, int slot, const float lo[3], const float hi[3]) {
+    float* bx = reinterpret_cast<float*>(&nd->bx);
+    float* by = reinterpret_cast<float*>(&nd->by);
+    float* bz = reinterpret_cast<float*>(&nd->bz);
+    __stcg(bx + 2 * slot, lo[0]);
+    __stcg(bx + 2 * slot + 1, hi[0]);
+    __stcg(by + 2 * slot, lo[1]);
+    __stcg(by + 2 * slot + 1, hi[1]);
+    __stcg(bz + 2 * slot, lo[2]);
+    __stcg(bz + 2 * slot + 1, hi[2]);
+}
+__device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], float hi[3]) {
+    const float* bx = reinterpret_cast<const float*>(&nd->bx);
+    const float* by = reinterpret_cast<const float*>(&nd->by);
+    const float* bz = reinterpret_cast<const float*>(&nd->bz);
+    lo[0] = __ldcg(bx + 2 * slot);
+    hi[0] = __ldcg(bx + 2 * slot + 1);
+    lo[1] = __ldcg(by + 2 * slot);
+    hi[1] = __ldcg(by + 2 * slot + 1);
+    lo[2] = __ldcg(bz + 2 * slot);
+    hi[2] = __ldcg(bz + 2 * slot + 1);
+}
+
+// 6. refit; root box is written to root_box[0..5]
+__global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes, const int32_t* __restrict__ parent_int,
+                        const int32_t* __restrict__ parent_leaf, uint32_t* arrivals, float* root_box) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = soup[3 * j], b = soup[3 * j + 1], c = soup[3 * j + 2];
+        float lo[3] = {fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z))};
+        float hi[3] = {fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z))};
+        int code = ~(int)j;
+        int node = parent_leaf[j];
+        while (node >= 0) {
+            Node* nd = nodes + node;
+            const int slot = (__ldcg(&nd->ch.x) == code) ? 0 : 1;
+            store_child_box(nd, slot, lo, hi);
+            __threadfence();
+            const uint32_t old = atomicAdd(arrivals + node, 1u);
+            if (old == 0) break;  // sibling not done yet; it will continue upward
+            __threadfence();
+            float olo[3], ohi[3];
+            load_child_box(nd, 1 - slot, olo, ohi);
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], olo[k]);
+                hi[k] = fmaxf(hi[k], ohi[k]);
+            }
+            code = node;
+            node = __ldcg(parent_int + node);
+            if (node < 0) {
+                for (int k = 0; k < 3; ++k) {
+                    root_box[k] = lo[k];
+                    root_box[3 + k] = hi[k];
+                }
+            }
+        }
+    }
+}
+
+// single-triangle dataset: the root box is the triangle's box
+__global__ void k_single_box(const float4* __restrict__ soup, float* root_box) {
+    const float4 a = soup[0], b = soup[1], c = soup[2];
+    root_box[0] = fminf(a.x, fminf(b.x, c.x));
+    root_box[1] = fminf(a.y, fminf(b.y, c.y));
+    root_box[2] = fminf(a.z, fminf(b.z, c.z));
+    root_box[3] = fmaxf(a.x, fmaxf(b.x, c.x));
+    root_box[4] = fmaxf(a.y, fmaxf(b.y, c.y));
+    root_box[5] = fmaxf(a.z, fmaxf(b.z, c.z));
+}
+
+// 7. collapse small subtrees into leaves
+__global__ void k_collapse(Node* nodes, const int2* __restrict__ range, int64_t n, int leaf_size) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n - 1; i += (int64_t)gridDim.x * blockDim.x) {
+        int4 ch = nodes[i].ch;
+        if (ch.x >= 0) {
+            const int2 r = range[ch.x];
+            if (r.y - r.x + 1 <= leaf_size) {
+                ch.x = ~r.x;
+                ch.z = r.y - r.x + 1;
+            }
+        }
+        if (ch.y >= 0) {
+            const int2 r = range[ch.y];
+            if (r.y - r.x + 1 <= leaf_size) {
+                ch.y = ~r.x;
+                ch.w = r.y - r.x + 1;
+            }
+        }
+        nodes[i].ch = ch;
+    }
+}
+
+// ---- per-object data: first vertex, bounding box ------------------------
+
+__global__ void k_first_tri(const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj, int32_t* first_tri,
+                            uint32_t* obj_box_o, const float* __restrict__ verts, const uint32_t* __restrict__ idx) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t o = t2o[t];
+        if (o < 0 || o >= nobj) continue;
+        atomicMin(first_tri + o, (int32_t)t);
+        const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
+        const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
+        const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
+        uint32_t* bx = obj_box_o + 6 * (size_t)o;
+        atomicMin(bx + 0, f2o(fminf(a.x, fminf(b.x, c.x))));
+        atomicMin(bx + 1, f2o(fminf(a.y, fminf(b.y, c.y))));
+        atomicMin(bx + 2, f2o(fminf(a.z, fminf(b.z, c.z))));
+        atomicMax(bx + 3, f2o(fmaxf(a.x, fmaxf(b.x, c.x))));
+        atomicMax(bx + 4, f2o(fmaxf(a.y, fmaxf(b.y, c.y))));
+        atomicMax(bx + 5, f2o(fmaxf(a.z, fmaxf(b.z, c.z))));
+    }
+}
+
+__global__ void k_obj_finish(const int32_t* __restrict__ first_tri, int32_t nobj, int64_t nv,
+                             const float* __restrict__ verts, const uint32_t* __restrict__ idx, float4* first_vertex,
+                             uint32_t* obj_box_o) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nobj; o += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t t = first_tri[o];
+        float4 fv = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // w = 1: object has no triangle
+        if (t != 0x7FFFFFFF) {
+            const uint32_t vi = idx[3 * (size_t)t];
+            if (vi < nv) {
+                const float3 v = load_vertex(verts, vi);
+                fv = make_float4(v.x, v.y, v.z, 0.0f);
+            }
+        }
+        first_vertex[o] = fv;
+        float* out = reinterpret_cast<float*>(obj_box_o + 6 * (size_t)o);
+        for (int k = 0; k < 6; ++k) out[k] = o2f(obj_box_o[6 * (size_t)o + k]);
+    }
+}
+
+__global__ void k_obj_box_init(uint32_t* box_o, int32_t nobj) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 6 * (int64_t)nobj;
+         i += (int64_t)gridDim.x * blockDim.x)
+        box_o[i] = (i % 6) < 3 ? f2o(__int_as_float(0x7F800000)) : f2o(__int_as_float((int)0xFF800000u));
+}
+
+static inline int grid_for(pierce_ctx* ctx, int64_t n, int block) {
+    int64_t blocks = (n + block - 1) / block;
+    int64_t cap = (int64_t)ctx->sm_count * 16;
+    if (blocks > cap) blocks = cap;
+    return (int)(blocks < 1 ? 1 : blocks);
+}
+
+int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
+    const int32_t nobj = ds->num_objects;
+    if (nobj <= 0) return PIERCE_OK;
+    void* p = nullptr;
+    if (int s = scratch(ctx, 1, sizeof(int32_t) * (size_t)nobj, &p)) return s;
+    int32_t* first_tri = static_cast<int32_t*>(p);
+    uint32_t* box_o = reinterpret_cast<uint32_t*>(ds->d_obj_box);
+    cudaStream_t st = ctx->stream;
+    k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(first_tri), 0x7FFFFFFFu, nobj);
+    k_obj_box_init<<<grid_for(ctx, 6 * (int64_t)nobj, 256), 256, 0, st>>>(box_o, nobj);
+    if (ds->nt > 0)
+        k_first_tri<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt, nobj,
+                                                                          first_tri, box_o, ds->d_vertices,
+                                                                          ds->d_indices);
+    k_obj_finish<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(first_tri, nobj, (int64_t)ds->nv, ds->d_vertices,
+                                                            ds->d_indices, ds->d_first_vertex, box_o);
+    ctx->launches += 3 + (ds->nt > 0 ? 1 : 0);
+    return check_cuda(cudaGetLastError(), "prepare_objects");
+}
+
+int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
+    const int64_t n = (int64_t)ds->nt;
+    cudaStream_t st = ctx->stream;
+    if (leaf_size < 1) leaf_size = 1;
+    if (leaf_size > 16) leaf_size = 16;
+    ds->leaf_size = leaf_size;
+    ds->built = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    int status = PIERCE_OK;
+    float root_box[6] = {0, 0, 0, 0, 0, 0};
+    do {
+        if (n == 0) {
+            ds->root_is_leaf = 1;
+            ds->root_leaf_count = 0;
+            ds->num_nodes = 0;
+            break;
+        }
+        // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 parents/range/arrivals/bounds
+        void *pc = nullptr, *pk = nullptr, *pv = nullptr, *pm = nullptr;
+        if ((status = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc))) break;
+        if ((status = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk))) break;
+        if ((status = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv))) break;
+        const size_t misc_bytes = sizeof(int32_t) * (size_t)(n + n) + sizeof(int2) * (size_t)n +
+                                  sizeof(uint32_t) * (size_t)n + 64;
+        if ((status = scratch(ctx, 4, misc_bytes, &pm))) break;
+        float4* cen = static_cast<float4*>(pc);
+        uint32_t* keys = static_cast<uint32_t*>(pk);
+        uint32_t* vals = static_cast<uint32_t*>(pv);
+        int32_t* parent_int = static_cast<int32_t*>(pm);
+        int32_t* parent_leaf = parent_int + n;
+        int2* range = reinterpret_cast<int2*>(parent_leaf + n);
+        uint32_t* arrivals = reinterpret_cast<uint32_t*>(range + n);
+        uint32_t* bounds = arrivals + n;        // 6 words
+        float* d_root_box = reinterpret_cast<float*>(bounds + 6);  // 6 floats
+
+        const uint32_t init_b[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+        cudaMemcpyAsync(bounds, init_b, sizeof(init_b), cudaMemcpyHostToDevice, st);
+        const int B = 256;
+        k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_vertices, ds->d_indices, n, cen, bounds);
+        k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
+        ctx->launches += 2;
+        if ((status = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30))) break;
+        const uint32_t* skeys = keys + n;
+        const uint32_t* order = vals + n;
+        k_soup<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_vertices, ds->d_indices, ds->d_tri_to_object, order, n,
+                                                  ds->d_soup);
+        ctx->launches += 1;
+        if (n == 1) {
+            k_single_box<<<1, 1, 0, st>>>(ds->d_soup, d_root_box);
+            ctx->launches += 1;
+            ds->root_is_leaf = 1;
+            ds->root_leaf_count = 1;
+            ds->num_nodes = 0;
+        } else {
+            cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * (size_t)n, st);
+            k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, ds->d_nodes, parent_int, parent_leaf, range);
+            k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_soup, n, ds->d_nodes, parent_int, parent_leaf, arrivals,
+                                                       d_root_box);
+            ctx->launches += 2;
+            if (leaf_size > 1) {
+                k_collapse<<<grid_for(ctx, n - 1, B), B, 0, st>>>(ds->d_nodes, range, n, leaf_size);
+                ctx->launches += 1;
+            }
+            ds->num_nodes = (uint64_t)(n - 1);
+            ds->root_is_leaf = (n <= leaf_size) ? 1 : 0;
+            ds->root_leaf_count = (n <= leaf_size) ? (int)n : 0;
+        }
+        if ((status = check_cuda(cudaMemcpyAsync(root_box, d_root_box, sizeof(root_box), cudaMemcpyDeviceToHost, st),
+                                 "bvh root box")))
+            break;
+    } while (0);
+    cudaEventRecord(e1, st);
+    if (status == PIERCE_OK) status = check_cuda(cudaStreamSynchronize(st), "bvh build");
+    if (status == PIERCE_OK) status = check_cuda(cudaGetLastError(), "bvh build kernels");
+    float ms = 0.0f;
+    if (status == PIERCE_OK) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != PIERCE_OK) return status;
+    for (int k = 0; k < 3; ++k) {
+        ds->lo[k] = root_box[k];
+        ds->hi[k] = root_box[3 + k];
+    }
+    ds->ms_build = ms;
+    ds->built = 1;
+    return PIERCE_OK;
+}
+
+}  // namespace pgpu

@@ -1,0 +1,331 @@
+// Unique-edge extraction and grid statistics for the `.pre` producer.
+//
+// Edge semantics follow EdgePreprocessor::extractEdges
+// (pierce/preprocess/src/EdgePreprocessor.cpp:44-111):
+//  * every triangle (in index order) contributes its three directed edges
+//    v0->v1, v1->v2, v2->v0; triangles with an out-of-range vertex index are
+//    skipped, and nothing is produced when triangleToObject and the index
+//    array differ in length;
+//  * endpoints are quantised to int64 with llround(double(x) * 1e5);
+//  * the key is (min(q0,q1), max(q0,q1), objectId) with points compared
+//    lexicographically; the first triangle edge that produces a key wins and
+//    keeps its own (unswapped) float endpoints;
+//  * output order is ascending key order (the std::map iteration order).
+// Here the map is replaced by a sort of (key, arrival index) records, done
+// per object in parallel: equal keys always share an object, so "first
+// arrival per key" is decided inside one object.  order == 0 then merges all
+// objects into global key order (byte-identical to the reference output);
+// order == 1 keeps objects in id order (same edge set, cheaper for large
+// datasets whose edge order does not matter to the join).
+//
+// Grid statistics follow generateGridStats
+// (pierce/preprocess/src/pierce_preprocess.cpp:49-167).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#include <parallel/algorithm>
+#endif
+
+#include "geometry.h"
+
+namespace {
+
+struct EdgeRec {
+    int64_t a[3];
+    int64_t b[3];
+    int32_t obj;
+    uint32_t corner;  // 0..2: which edge of the triangle
+    uint64_t tri;     // triangle index (arrival order = tri*3 + corner)
+};
+
+inline bool key_less(const EdgeRec& x, const EdgeRec& y) {
+    for (int i = 0; i < 3; ++i)
+        if (x.a[i] != y.a[i]) return x.a[i] < y.a[i];
+    for (int i = 0; i < 3; ++i)
+        if (x.b[i] != y.b[i]) return x.b[i] < y.b[i];
+    return x.obj < y.obj;
+}
+inline bool key_equal(const EdgeRec& x, const EdgeRec& y) {
+    return x.obj == y.obj && std::memcmp(x.a, y.a, sizeof(x.a)) == 0 &&
+           std::memcmp(x.b, y.b, sizeof(x.b)) == 0;
+}
+inline bool rec_less(const EdgeRec& x, const EdgeRec& y) {
+    if (key_less(x, y)) return true;
+    if (key_less(y, x)) return false;
+    if (x.tri != y.tri) return x.tri < y.tri;
+    return x.corner < y.corner;
+}
+
+// llround(double(x) * 1e5) without the libm call: truncate, then round half
+// away from zero on the exact remainder (x - trunc(x) is exact below 2^52).
+inline int64_t round_half_away(double x) {
+    if (!(std::fabs(x) < 4.0e18)) return (int64_t)std::llround(x);
+    int64_t i = (int64_t)x;
+    double frac = x - (double)i;
+    if (frac >= 0.5) ++i;
+    else if (frac <= -0.5) --i;
+    return i;
+}
+
+inline void quantise(const float* p, int64_t q[3]) {
+    for (int i = 0; i < 3; ++i) q[i] = round_half_away((double)p[i] * 1e5);
+}
+
+inline bool point_less(const int64_t* x, const int64_t* y) {
+    if (x[0] != y[0]) return x[0] < y[0];
+    if (x[1] != y[1]) return x[1] < y[1];
+    return x[2] < y[2];
+}
+
+}  // namespace
+
+namespace pierce {
+
+void extract_edges(pierce_geom& g, int order, int num_threads) {
+    g.edge_starts.clear();
+    g.edge_ends.clear();
+    g.edge_src.clear();
+    const uint64_t nt = g.num_triangles();
+    const uint64_t nv = g.num_vertices();
+    if (nt == 0 || nv == 0 || g.tri_to_object.size() != nt) return;
+
+#ifdef _OPENMP
+    if (num_threads > 0) omp_set_num_threads(num_threads);
+#else
+    (void)num_threads;
+#endif
+
+    // Group triangles by object id with a counting sort (objects may have
+    // negative ids in hostile inputs; those are grouped separately at the end).
+    int32_t max_obj = -1;
+    for (int32_t o : g.tri_to_object) max_obj = std::max(max_obj, o);
+    const int64_t nobj = (int64_t)max_obj + 2;  // last bucket: negative ids
+    std::vector<uint64_t> start(nobj + 1, 0);
+    auto bucket = [&](int32_t o) -> int64_t { return o < 0 ? nobj - 1 : (int64_t)o; };
+    for (uint64_t t = 0; t < nt; ++t) start[bucket(g.tri_to_object[t]) + 1]++;
+    for (int64_t i = 0; i < nobj; ++i) start[i + 1] += start[i];
+    std::vector<uint64_t> tris(nt);
+    {
+        std::vector<uint64_t> cur(start.begin(), start.end() - 1);
+        for (uint64_t t = 0; t < nt; ++t) tris[cur[bucket(g.tri_to_object[t])]++] = t;
+    }
+
+    // Per-object unique edges, each object's list in key order.  Each thread
+    // sorts one object's records in a reused buffer and appends the survivors
+    // (triangle, corner) to its own arena; objects are then laid out in id
+    // order.  Memory stays O(largest object) per thread plus the output.
+    struct Ref {
+        uint64_t tri;
+        uint32_t corner;
+        int32_t obj;
+    };
+    struct Slot {
+        int arena;
+        uint64_t offset, count;
+    };
+    int nthreads = 1;
+#ifdef _OPENMP
+    nthreads = omp_get_max_threads();
+#endif
+    std::vector<std::vector<Ref>> arenas(nthreads);
+    std::vector<Slot> slots(nobj);
+#pragma omp parallel
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        std::vector<EdgeRec> buf;
+        std::vector<Ref>& arena = arenas[tid];
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t o = 0; o < nobj; ++o) {
+            buf.clear();
+            for (uint64_t k = start[o]; k < start[o + 1]; ++k) {
+                const uint64_t t = tris[k];
+                const uint32_t* tri = &g.indices[3 * t];
+                if (tri[0] >= nv || tri[1] >= nv || tri[2] >= nv) continue;
+                int64_t q[3][3];
+                for (int c = 0; c < 3; ++c) quantise(&g.vertices[3 * (uint64_t)tri[c]], q[c]);
+                for (uint32_t e = 0; e < 3; ++e) {
+                    EdgeRec r;
+                    const int64_t* q0 = q[e];
+                    const int64_t* q1 = q[(e + 1) % 3];
+                    if (point_less(q1, q0)) std::swap(q0, q1);
+                    std::memcpy(r.a, q0, sizeof(r.a));
+                    std::memcpy(r.b, q1, sizeof(r.b));
+                    r.obj = g.tri_to_object[t];
+                    r.corner = e;
+                    r.tri = t;
+                    buf.push_back(r);
+                }
+            }
+            std::sort(buf.begin(), buf.end(), rec_less);
+            Slot s{tid, arena.size(), 0};
+            for (size_t i = 0; i < buf.size(); ++i) {
+                if (i > 0 && key_equal(buf[i], buf[i - 1])) continue;
+                arena.push_back(Ref{buf[i].tri, buf[i].corner, buf[i].obj});
+                s.count++;
+            }
+            slots[o] = s;
+        }
+    }
+    std::vector<uint64_t> off(nobj + 1, 0);
+    for (int64_t o = 0; o < nobj; ++o) off[o + 1] = off[o] + slots[o].count;
+    const uint64_t ne = off[nobj];
+    std::vector<Ref> all(ne);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t o = 0; o < nobj; ++o) {
+        const Slot& s = slots[o];
+        if (s.count)
+            std::memcpy(&all[off[o]], &arenas[s.arena][s.offset], s.count * sizeof(Ref));
+    }
+    arenas.clear();
+
+    if (order == 0) {
+        // Global key order: rebuild keys for the unique edges and sort them.
+        std::vector<EdgeRec> keyed(ne);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)ne; ++i) {
+            const Ref& r = all[i];
+            const uint32_t* tri = &g.indices[3 * r.tri];
+            int64_t q0[3], q1[3];
+            quantise(&g.vertices[3 * (uint64_t)tri[r.corner]], q0);
+            quantise(&g.vertices[3 * (uint64_t)tri[(r.corner + 1) % 3]], q1);
+            const int64_t* lo = q0;
+            const int64_t* hi = q1;
+            if (point_less(q1, q0)) std::swap(lo, hi);
+            EdgeRec& k = keyed[i];
+            std::memcpy(k.a, lo, sizeof(k.a));
+            std::memcpy(k.b, hi, sizeof(k.b));
+            k.obj = r.obj;
+            k.corner = r.corner;
+            k.tri = r.tri;
+        }
+#ifdef _OPENMP
+        __gnu_parallel::sort(keyed.begin(), keyed.end(), key_less);
+#else
+        std::sort(keyed.begin(), keyed.end(), key_less);
+#endif
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)ne; ++i) all[i] = Ref{keyed[i].tri, keyed[i].corner, keyed[i].obj};
+    }
+
+    g.edge_starts.resize(3 * ne);
+    g.edge_ends.resize(3 * ne);
+    g.edge_src.resize(ne);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)ne; ++i) {
+        const Ref& r = all[i];
+        const uint32_t* tri = &g.indices[3 * r.tri];
+        const float* p0 = &g.vertices[3 * (uint64_t)tri[r.corner]];
+        const float* p1 = &g.vertices[3 * (uint64_t)tri[(r.corner + 1) % 3]];
+        std::memcpy(&g.edge_starts[3 * i], p0, 3 * sizeof(float));
+        std::memcpy(&g.edge_ends[3 * i], p1, 3 * sizeof(float));
+        g.edge_src[i] = r.obj;
+    }
+}
+
+void grid_stats(pierce_geom& g, float cell_size) {
+    struct ObjStats {
+        float mn[3] = {1e30f, 1e30f, 1e30f};
+        float mx[3] = {-1e30f, -1e30f, -1e30f};
+        double volume = 0.0;
+        bool seen = false;
+    };
+    const uint64_t nt = g.num_triangles(), nv = g.num_vertices();
+    int32_t max_obj = -1;
+    for (int32_t o : g.tri_to_object) max_obj = std::max(max_obj, o);
+    std::vector<ObjStats> objs((size_t)(max_obj + 1));
+    const uint64_t nmap = std::min<uint64_t>(nt, g.tri_to_object.size());
+    for (uint64_t t = 0; t < nmap; ++t) {
+        const int32_t o = g.tri_to_object[t];
+        const uint32_t* tri = &g.indices[3 * t];
+        if (o < 0 || tri[0] >= nv || tri[1] >= nv || tri[2] >= nv) continue;
+        ObjStats& s = objs[o];
+        s.seen = true;
+        for (int k = 0; k < 3; ++k) {
+            const float* v = &g.vertices[3 * (uint64_t)tri[k]];
+            for (int d = 0; d < 3; ++d) {
+                s.mn[d] = std::min(s.mn[d], v[d]);
+                s.mx[d] = std::max(s.mx[d], v[d]);
+            }
+        }
+    }
+    // Signed volume relative to the AABB centre, float products summed in
+    // double as in the reference.
+    for (uint64_t t = 0; t < nmap; ++t) {
+        const int32_t o = g.tri_to_object[t];
+        const uint32_t* tri = &g.indices[3 * t];
+        if (o < 0 || tri[0] >= nv || tri[1] >= nv || tri[2] >= nv) continue;
+        ObjStats& s = objs[o];
+        float c[3], p[3][3];
+        for (int d = 0; d < 3; ++d) c[d] = (s.mn[d] + s.mx[d]) * 0.5f;
+        for (int k = 0; k < 3; ++k)
+            for (int d = 0; d < 3; ++d) p[k][d] = g.vertices[3 * (uint64_t)tri[k] + d] - c[d];
+        float cx = p[0][1] * p[1][2] - p[0][2] * p[1][1];
+        float cy = p[0][2] * p[1][0] - p[0][0] * p[1][2];
+        float cz = p[0][0] * p[1][1] - p[0][1] * p[1][0];
+        s.volume += (cx * p[2][0] + cy * p[2][1] + cz * p[2][2]);
+    }
+    struct Acc {
+        uint32_t center = 0, touch = 0;
+        float size = 0.0f, ratio = 0.0f;
+    };
+    std::map<std::tuple<int, int, int>, Acc> cells;
+    for (const ObjStats& s : objs) {
+        if (!s.seen) continue;
+        float mesh_vol = std::fabs((float)s.volume) / 6.0f;
+        float w = s.mx[0] - s.mn[0], h = s.mx[1] - s.mn[1], dpt = s.mx[2] - s.mn[2];
+        float aabb_vol = w * h * dpt;
+        if (aabb_vol < 1e-9f) aabb_vol = 1e-9f;
+        float ratio = mesh_vol / aabb_vol;
+        if (ratio > 1.0f) ratio = 1.0f;
+        float c[3];
+        for (int d = 0; d < 3; ++d) c[d] = (s.mn[d] + s.mx[d]) * 0.5f;
+        float avg = (w + h + dpt) / 3.0f;
+        cells[std::make_tuple((int)std::floor(c[0] / cell_size), (int)std::floor(c[1] / cell_size),
+                              (int)std::floor(c[2] / cell_size))]
+            .center++;
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = (int)std::floor(s.mn[d] / cell_size);
+            hi[d] = (int)std::floor((s.mx[d] - 1e-5f) / cell_size);
+        }
+        for (int z = lo[2]; z <= hi[2]; ++z)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int x = lo[0]; x <= hi[0]; ++x) {
+                    Acc& a = cells[std::make_tuple(x, y, z)];
+                    a.touch++;
+                    a.size += avg;
+                    a.ratio += ratio;
+                }
+    }
+    g.grid_cells.clear();
+    g.grid_cells.reserve(cells.size());
+    for (auto& kv : cells) {
+        pierce_grid_entry e;
+        e.ix = std::get<0>(kv.first);
+        e.iy = std::get<1>(kv.first);
+        e.iz = std::get<2>(kv.first);
+        e.center_count = kv.second.center;
+        e.touch_count = kv.second.touch;
+        e.avg_size_mean = kv.second.size;
+        e.vol_ratio = kv.second.ratio;
+        if (e.touch_count > 0) {
+            e.avg_size_mean /= (float)e.touch_count;
+            e.vol_ratio /= (float)e.touch_count;
+        }
+        g.grid_cells.push_back(e);
+    }
+    g.has_grid = true;
+    g.grid_cell_size = cell_size;
+}
+
+}  // namespace pierce

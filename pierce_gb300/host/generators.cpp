@@ -1,0 +1,406 @@
+// Seeded synthetic dataset generators.
+//
+// The reference ships no datasets (its benchmarks download MICrONS meshes or
+// instance template OBJ files), so the join workloads are generated here from
+// a seed.  All arithmetic is IEEE basic operations in double precision with
+// the deterministic series of detmath.h, rounded once to float32 per vertex
+// coordinate, so a given seed yields bit-identical files on every host.
+//
+// Mesh families:
+//  * icospheres: icosahedron subdivided `level` times, vertices projected to
+//    the unit sphere (F = 20*4^level, V = 10*4^level + 2), scaled by a
+//    lognormal radius and translated to a uniform centre;
+//  * ellipsoids: the same template scaled per axis, rotated by a uniform
+//    random rotation (Shoemake's quaternion method) and displaced radially by
+//    smooth 3-D value noise;
+//  * tubes: branching random-walk skeletons swept with an n-gon cross section
+//    and closed with centre-fan caps.
+// Every mesh is one object; object ids are dense 0..n-1 in generation order.
+// Edges are extracted in per-object order (pierce::extract_edges order 1).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <utility>
+#include <vector>
+
+#include "detmath.h"
+#include "geometry.h"
+
+namespace {
+
+using pierce::detm::Rng;
+
+struct V3 {
+    double x, y, z;
+};
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 mul(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline V3 normalize(V3 a) {
+    double l = std::sqrt(dot(a, a));
+    return l > 0 ? mul(a, 1.0 / l) : V3{0, 0, 1};
+}
+
+struct Template {
+    std::vector<V3> verts;          // unit vectors
+    std::vector<uint32_t> tris;     // 3 per triangle, outward CCW
+};
+
+// Icosahedron vertices (+-1, +-phi, 0) and cyclic permutations, with the
+// usual 20 outward-oriented faces, then midpoint subdivision.
+Template make_icosphere(int level) {
+    const double phi = (1.0 + std::sqrt(5.0)) / 2.0;
+    Template t;
+    const double raw[12][3] = {{-1, phi, 0}, {1, phi, 0},  {-1, -phi, 0}, {1, -phi, 0},
+                               {0, -1, phi}, {0, 1, phi},  {0, -1, -phi}, {0, 1, -phi},
+                               {phi, 0, -1}, {phi, 0, 1},  {-phi, 0, -1}, {-phi, 0, 1}};
+    for (auto& r : raw) t.verts.push_back(normalize({r[0], r[1], r[2]}));
+    const uint32_t faces[20][3] = {{0, 11, 5}, {0, 5, 1},  {0, 1, 7},   {0, 7, 10}, {0, 10, 11},
+                                   {1, 5, 9},  {5, 11, 4}, {11, 10, 2}, {10, 7, 6}, {7, 1, 8},
+                                   {3, 9, 4},  {3, 4, 2},  {3, 2, 6},   {3, 6, 8},  {3, 8, 9},
+                                   {4, 9, 5},  {2, 4, 11}, {6, 2, 10},  {8, 6, 7},  {9, 8, 1}};
+    for (auto& f : faces) t.tris.insert(t.tris.end(), f, f + 3);
+    for (int l = 0; l < level; ++l) {
+        std::map<std::pair<uint32_t, uint32_t>, uint32_t> mid;
+        auto midpoint = [&](uint32_t a, uint32_t b) -> uint32_t {
+            auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = mid.find(key);
+            if (it != mid.end()) return it->second;
+            V3 m = normalize(mul(add(t.verts[a], t.verts[b]), 0.5));
+            uint32_t id = (uint32_t)t.verts.size();
+            t.verts.push_back(m);
+            mid.emplace(key, id);
+            return id;
+        };
+        std::vector<uint32_t> nt;
+        nt.reserve(t.tris.size() * 4);
+        for (size_t i = 0; i < t.tris.size(); i += 3) {
+            uint32_t a = t.tris[i], b = t.tris[i + 1], c = t.tris[i + 2];
+            uint32_t ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+            const uint32_t add4[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
+            nt.insert(nt.end(), add4, add4 + 12);
+        }
+        t.tris.swap(nt);
+    }
+    return t;
+}
+
+// Smooth value noise in [-1, 1]: hashed lattice values, trilinear
+// interpolation with smoothstep weights.
+struct ValueNoise {
+    uint64_t seed;
+    double lattice(int64_t i, int64_t j, int64_t k) const {
+        uint64_t h = seed ^ ((uint64_t)i * 0x9E3779B97F4A7C15ULL) ^ ((uint64_t)j * 0xC2B2AE3D27D4EB4FULL) ^
+                     ((uint64_t)k * 0x165667B19E3779F9ULL);
+        h = Rng::splitmix(h);
+        return (double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    }
+    static double smooth(double t) { return t * t * (3.0 - 2.0 * t); }
+    double operator()(V3 p) const {
+        double fx = std::floor(p.x), fy = std::floor(p.y), fz = std::floor(p.z);
+        int64_t i = (int64_t)fx, j = (int64_t)fy, k = (int64_t)fz;
+        double u = smooth(p.x - fx), v = smooth(p.y - fy), w = smooth(p.z - fz);
+        double c000 = lattice(i, j, k), c100 = lattice(i + 1, j, k);
+        double c010 = lattice(i, j + 1, k), c110 = lattice(i + 1, j + 1, k);
+        double c001 = lattice(i, j, k + 1), c101 = lattice(i + 1, j, k + 1);
+        double c011 = lattice(i, j + 1, k + 1), c111 = lattice(i + 1, j + 1, k + 1);
+        double x00 = c000 + (c100 - c000) * u, x10 = c010 + (c110 - c010) * u;
+        double x01 = c001 + (c101 - c001) * u, x11 = c011 + (c111 - c011) * u;
+        double y0 = x00 + (x10 - x00) * v, y1 = x01 + (x11 - x01) * v;
+        return y0 + (y1 - y0) * w;
+    }
+};
+
+struct Rot {
+    double m[9];
+    V3 apply(V3 p) const {
+        return {m[0] * p.x + m[1] * p.y + m[2] * p.z, m[3] * p.x + m[4] * p.y + m[5] * p.z,
+                m[6] * p.x + m[7] * p.y + m[8] * p.z};
+    }
+};
+
+// Uniform random rotation from three uniforms (Shoemake 1992).
+Rot random_rotation(Rng& rng) {
+    double u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform();
+    double s1 = std::sqrt(1.0 - u1), s2 = std::sqrt(u1);
+    const double tp = pierce::detm::kTwoPi;
+    double x = s1 * pierce::detm::sin(tp * u2), y = s1 * pierce::detm::cos(tp * u2);
+    double z = s2 * pierce::detm::sin(tp * u3), w = s2 * pierce::detm::cos(tp * u3);
+    Rot r;
+    r.m[0] = 1 - 2 * (y * y + z * z);
+    r.m[1] = 2 * (x * y - z * w);
+    r.m[2] = 2 * (x * z + y * w);
+    r.m[3] = 2 * (x * y + z * w);
+    r.m[4] = 1 - 2 * (x * x + z * z);
+    r.m[5] = 2 * (y * z - x * w);
+    r.m[6] = 2 * (x * z - y * w);
+    r.m[7] = 2 * (y * z + x * w);
+    r.m[8] = 1 - 2 * (x * x + y * y);
+    return r;
+}
+
+struct EllipsoidParams {
+    V3 center;
+    double ax, ay, az;
+    Rot rot;
+    uint64_t noise_seed;
+    V3 noise_offset;
+};
+
+EllipsoidParams random_ellipsoid(Rng& rng, double lo, double hi, double axis_lo, double axis_hi) {
+    EllipsoidParams p;
+    p.center.x = rng.uniform(lo, hi);
+    p.center.y = rng.uniform(lo, hi);
+    p.center.z = rng.uniform(lo, hi);
+    p.ax = rng.uniform(axis_lo, axis_hi);
+    p.ay = rng.uniform(axis_lo, axis_hi);
+    p.az = rng.uniform(axis_lo, axis_hi);
+    p.rot = random_rotation(rng);
+    p.noise_seed = rng.next();
+    p.noise_offset = {rng.uniform(0, 64), rng.uniform(0, 64), rng.uniform(0, 64)};
+    return p;
+}
+
+// Append one mesh (template topology, given vertex positions) as object `obj`.
+void append_mesh(pierce_geom& g, const Template& t, const std::vector<float>& pos, int32_t obj) {
+    const uint32_t base = (uint32_t)g.num_vertices();
+    g.vertices.insert(g.vertices.end(), pos.begin(), pos.end());
+    for (size_t i = 0; i < t.tris.size(); ++i) g.indices.push_back(base + t.tris[i]);
+    g.tri_to_object.insert(g.tri_to_object.end(), t.tris.size() / 3, obj);
+}
+
+void ellipsoid_positions(const Template& t, const EllipsoidParams& p, double noise_amp, std::vector<float>& out) {
+    const double freq = 1.5;
+    ValueNoise vn{p.noise_seed};
+    out.resize(3 * t.verts.size());
+    for (size_t i = 0; i < t.verts.size(); ++i) {
+        V3 d = t.verts[i];
+        double n = vn(add(mul(d, freq), p.noise_offset));
+        double f = 1.0 + noise_amp * n;
+        V3 local = {p.ax * d.x * f, p.ay * d.y * f, p.az * d.z * f};
+        V3 w = add(p.center, p.rot.apply(local));
+        out[3 * i + 0] = (float)w.x;
+        out[3 * i + 1] = (float)w.y;
+        out[3 * i + 2] = (float)w.z;
+    }
+}
+
+void finish(pierce_geom& g) {
+    g.total_triangles = g.num_triangles();
+    pierce::extract_edges(g, 1, 0);
+}
+
+// ---- tubes ---------------------------------------------------------------
+
+V3 random_unit(Rng& rng) {
+    // Uniform direction from a normal triple.
+    for (;;) {
+        V3 v{rng.normal(), rng.normal(), rng.normal()};
+        double l2 = dot(v, v);
+        if (l2 > 1e-12) return mul(v, 1.0 / std::sqrt(l2));
+    }
+}
+
+// Sweep an n-gon along a polyline and cap both ends with centre fans.
+void sweep_branch(pierce_geom& g, const std::vector<V3>& pts, double radius, int n, int32_t obj) {
+    if (pts.size() < 2) return;
+    const uint32_t base = (uint32_t)g.num_vertices();
+    // Frames by parallel transport of an initial perpendicular.
+    V3 t0 = normalize(sub(pts[1], pts[0]));
+    V3 helper = std::fabs(t0.z) < 0.9 ? V3{0, 0, 1} : V3{1, 0, 0};
+    V3 u = normalize(cross(t0, helper));
+    const size_t m = pts.size();
+    for (size_t i = 0; i < m; ++i) {
+        V3 ti = (i + 1 < m) ? sub(pts[i + 1], pts[i]) : sub(pts[i], pts[i - 1]);
+        if (i > 0 && i + 1 < m) ti = add(normalize(sub(pts[i + 1], pts[i])), normalize(sub(pts[i], pts[i - 1])));
+        ti = normalize(ti);
+        u = normalize(sub(u, mul(ti, dot(u, ti))));
+        V3 v = cross(ti, u);
+        for (int k = 0; k < n; ++k) {
+            double ang = pierce::detm::kTwoPi * (double)k / (double)n;
+            V3 q = add(pts[i], add(mul(u, radius * pierce::detm::cos(ang)), mul(v, radius * pierce::detm::sin(ang))));
+            g.vertices.push_back((float)q.x);
+            g.vertices.push_back((float)q.y);
+            g.vertices.push_back((float)q.z);
+        }
+    }
+    const uint32_t c0 = (uint32_t)g.num_vertices();
+    g.vertices.push_back((float)pts[0].x);
+    g.vertices.push_back((float)pts[0].y);
+    g.vertices.push_back((float)pts[0].z);
+    const uint32_t c1 = c0 + 1;
+    g.vertices.push_back((float)pts[m - 1].x);
+    g.vertices.push_back((float)pts[m - 1].y);
+    g.vertices.push_back((float)pts[m - 1].z);
+    uint64_t added = 0;
+    for (size_t i = 0; i + 1 < m; ++i) {
+        for (int k = 0; k < n; ++k) {
+            uint32_t a = base + (uint32_t)(i * n + k), b = base + (uint32_t)(i * n + (k + 1) % n);
+            uint32_t c = a + (uint32_t)n, d = b + (uint32_t)n;
+            const uint32_t q[6] = {a, b, d, a, d, c};
+            g.indices.insert(g.indices.end(), q, q + 6);
+            added += 2;
+        }
+    }
+    for (int k = 0; k < n; ++k) {
+        uint32_t a = base + (uint32_t)k, b = base + (uint32_t)((k + 1) % n);
+        const uint32_t f0[3] = {c0, b, a};
+        g.indices.insert(g.indices.end(), f0, f0 + 3);
+        uint32_t la = base + (uint32_t)((m - 1) * n + k), lb = base + (uint32_t)((m - 1) * n + (k + 1) % n);
+        const uint32_t f1[3] = {c1, la, lb};
+        g.indices.insert(g.indices.end(), f1, f1 + 3);
+        added += 2;
+    }
+    g.tri_to_object.insert(g.tri_to_object.end(), added, obj);
+}
+
+}  // namespace
+
+extern "C" int pierce_gen_icospheres(uint64_t seed, int32_t num_meshes, int32_t level, double ln_mu, double sigma,
+                                     double lo, double hi, pierce_geom** out) {
+    if (!out || num_meshes < 0 || level < 0 || level > 8) {
+        pierce::set_last_error("gen_icospheres: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    Template t = make_icosphere(level);
+    std::unique_ptr<pierce_geom> g(new pierce_geom());
+    g->vertices.reserve((size_t)num_meshes * 3 * t.verts.size());
+    g->indices.reserve((size_t)num_meshes * t.tris.size());
+    Rng rng(seed);
+    std::vector<float> pos(3 * t.verts.size());
+    for (int32_t m = 0; m < num_meshes; ++m) {
+        V3 c{rng.uniform(lo, hi), rng.uniform(lo, hi), rng.uniform(lo, hi)};
+        double r = pierce::detm::exp(ln_mu + sigma * rng.normal());
+        for (size_t i = 0; i < t.verts.size(); ++i) {
+            pos[3 * i + 0] = (float)(c.x + r * t.verts[i].x);
+            pos[3 * i + 1] = (float)(c.y + r * t.verts[i].y);
+            pos[3 * i + 2] = (float)(c.z + r * t.verts[i].z);
+        }
+        append_mesh(*g, t, pos, m);
+    }
+    finish(*g);
+    *out = g.release();
+    return PIERCE_HOST_OK;
+}
+
+extern "C" int pierce_gen_ellipsoid_pair(uint64_t seed_a, uint64_t seed_b, int32_t num_a, int32_t num_b,
+                                         int32_t level, double axis_lo, double axis_hi, double noise_amp, double lo,
+                                         double hi, double frac_inside, double inside_scale, double frac_contact,
+                                         pierce_geom** out_a, pierce_geom** out_b) {
+    if (!out_a || !out_b || num_a < 0 || num_b < 0 || level < 0 || level > 8 ||
+        ((frac_inside > 0 || frac_contact > 0) && num_a == 0)) {
+        pierce::set_last_error("gen_ellipsoid_pair: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    Template t = make_icosphere(level);
+    std::unique_ptr<pierce_geom> A(new pierce_geom()), B(new pierce_geom());
+    const size_t nvm = t.verts.size();
+    A->vertices.reserve((size_t)num_a * 3 * nvm);
+    B->vertices.reserve((size_t)num_b * 3 * nvm);
+    std::vector<EllipsoidParams> params_a((size_t)num_a);
+    Rng ra(seed_a);
+    std::vector<float> pos;
+    for (int32_t m = 0; m < num_a; ++m) {
+        params_a[m] = random_ellipsoid(ra, lo, hi, axis_lo, axis_hi);
+        ellipsoid_positions(t, params_a[m], noise_amp, pos);
+        append_mesh(*A, t, pos, m);
+    }
+    Rng rb(seed_b);
+    for (int32_t m = 0; m < num_b; ++m) {
+        const double u = rb.uniform();
+        EllipsoidParams own = random_ellipsoid(rb, lo, hi, axis_lo, axis_hi);
+        if (u < frac_inside) {
+            // Scaled copy of a random A mesh about its generation centre: the
+            // meshes are star-shaped about that centre, so the copy is inside.
+            const int32_t j = (int32_t)rb.below((uint64_t)num_a);
+            const EllipsoidParams& pa = params_a[j];
+            pos.resize(3 * nvm);
+            const float* va = &A->vertices[(size_t)j * 3 * nvm];
+            for (size_t i = 0; i < nvm; ++i) {
+                pos[3 * i + 0] = (float)(pa.center.x + inside_scale * ((double)va[3 * i + 0] - pa.center.x));
+                pos[3 * i + 1] = (float)(pa.center.y + inside_scale * ((double)va[3 * i + 1] - pa.center.y));
+                pos[3 * i + 2] = (float)(pa.center.z + inside_scale * ((double)va[3 * i + 2] - pa.center.z));
+            }
+        } else if (u < frac_inside + frac_contact) {
+            const int32_t j = (int32_t)rb.below((uint64_t)num_a);
+            const float* va = &A->vertices[(size_t)j * 3 * nvm];
+            if (rb.uniform() < 0.5) {
+                // Exact duplicate of A_j: every face coplanar with a face of A_j.
+                pos.assign(va, va + 3 * nvm);
+            } else {
+                // Own ellipsoid resting on A_j: its lowest vertex is moved onto
+                // A_j's highest vertex exactly (a single-point contact).
+                ellipsoid_positions(t, own, noise_amp, pos);
+                size_t kb = 0, ka = 0;
+                for (size_t i = 1; i < nvm; ++i) {
+                    if (pos[3 * i + 2] < pos[3 * kb + 2]) kb = i;
+                    if (va[3 * i + 2] > va[3 * ka + 2]) ka = i;
+                }
+                const double tx = (double)va[3 * ka + 0] - (double)pos[3 * kb + 0];
+                const double ty = (double)va[3 * ka + 1] - (double)pos[3 * kb + 1];
+                const double tz = (double)va[3 * ka + 2] - (double)pos[3 * kb + 2];
+                for (size_t i = 0; i < nvm; ++i) {
+                    pos[3 * i + 0] = (float)((double)pos[3 * i + 0] + tx);
+                    pos[3 * i + 1] = (float)((double)pos[3 * i + 1] + ty);
+                    pos[3 * i + 2] = (float)((double)pos[3 * i + 2] + tz);
+                }
+                pos[3 * kb + 0] = va[3 * ka + 0];
+                pos[3 * kb + 1] = va[3 * ka + 1];
+                pos[3 * kb + 2] = va[3 * ka + 2];
+            }
+        } else {
+            ellipsoid_positions(t, own, noise_amp, pos);
+        }
+        append_mesh(*B, t, pos, m);
+    }
+    finish(*A);
+    finish(*B);
+    *out_a = A.release();
+    *out_b = B.release();
+    return PIERCE_HOST_OK;
+}
+
+extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris, double step,
+                                double branch_prob, double r_lo, double r_hi, int32_t n_sides, double lo, double hi,
+                                pierce_geom** out) {
+    if (!out || num_meshes < 0 || target_tris <= 0 || n_sides < 3 || step <= 0) {
+        pierce::set_last_error("gen_tubes: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    std::unique_ptr<pierce_geom> g(new pierce_geom());
+    Rng rng(seed);
+    const int64_t tris_per_segment = 2 * (int64_t)n_sides;
+    for (int32_t m = 0; m < num_meshes; ++m) {
+        const double radius = rng.uniform(r_lo, r_hi);
+        struct Start {
+            V3 p, d;
+        };
+        std::vector<Start> pending;
+        pending.push_back({{rng.uniform(lo, hi), rng.uniform(lo, hi), rng.uniform(lo, hi)}, random_unit(rng)});
+        int64_t budget = target_tris;
+        while (!pending.empty() && budget > 2 * n_sides + tris_per_segment) {
+            Start s = pending.back();
+            pending.pop_back();
+            std::vector<V3> pts{s.p};
+            V3 p = s.p, d = s.d;
+            budget -= 2 * n_sides;  // caps
+            while (budget >= tris_per_segment) {
+                d = normalize(add(d, mul(random_unit(rng), 0.35)));
+                p = add(p, mul(d, step));
+                pts.push_back(p);
+                budget -= tris_per_segment;
+                if (rng.uniform() < branch_prob) pending.push_back({p, normalize(add(d, random_unit(rng)))});
+                // Branches end with probability 1/400 per segment once a
+                // branch is queued, so the budget spreads over several arms.
+                if (!pending.empty() && rng.uniform() < 1.0 / 400.0) break;
+            }
+            sweep_branch(*g, pts, radius, n_sides, m);
+        }
+    }
+    finish(*g);
+    *out = g.release();
+    return PIERCE_HOST_OK;
+}

@@ -1,0 +1,204 @@
+"""User-facing join API over the CUDA library.
+
+Mirrors the reference's query operations (pierce/query/src/applications/):
+
+* :func:`overlap_join` – ``pierce_overlap`` (hash mode, executeHashQuery)
+* :func:`overlap_join_two_pass` – ``pierce_overlap_two_pass``
+  (executeTwoPassQueryEdgesOptimized)
+* :func:`intersection_join` – ``pierce_intersection``
+* :func:`containment_join` – ``pierce_containment``
+
+Each returns the unique (mesh1 object id, mesh2 object id) pairs as an
+``(n, 2)`` int32 array sorted by (a, b), plus the join statistics.  All
+computation happens in ``libpierce_gb300.so``; there is no other path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .capi import check
+
+PREDICATES = {"overlap": capi.OVERLAP, "intersection": capi.INTERSECTION, "containment": capi.CONTAINMENT}
+DIRECTIONS = {"both": capi.BOTH, "mesh1_to_mesh2": capi.MESH1_TO_MESH2, "mesh2_to_mesh1": capi.MESH2_TO_MESH1}
+SIZINGS = {"two_pass": capi.SIZING_TWO_PASS, "hash": capi.SIZING_HASH, "fixed": capi.SIZING_FIXED}
+PRECISIONS = {"exact": capi.EXACT, "fp32": capi.FP32}
+
+
+class Context:
+    """One CUDA device + stream; all datasets and joins of a context run on it."""
+
+    def __init__(self, device: int = 0):
+        self._lib = capi.lib()
+        h = C.c_void_p()
+        check(self._lib.pierce_ctx_create(device, C.byref(h)), "ctx_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.pierce_ctx_stream(self._h) or 0)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._lib.pierce_ctx_kernel_launches(self._h))
+
+    def synchronize(self) -> None:
+        check(self._lib.pierce_ctx_synchronize(self._h), "synchronize")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.pierce_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def default_tuning(**kw) -> capi.Tuning:
+    t = capi.Tuning()
+    capi.lib().pierce_default_tuning(C.byref(t))
+    for k, v in kw.items():
+        setattr(t, k, v)
+    return t
+
+
+class Dataset:
+    """A dataset resident on the device with its BVH."""
+
+    def __init__(self, ctx: Context, handle, keep=None):
+        self.ctx = ctx
+        self._h = handle
+        self._keep = keep
+        self._lib = capi.lib()
+
+    @classmethod
+    def from_arrays(cls, ctx: Context, vertices, indices, tri_to_object, edge_starts, edge_ends, edge_src,
+                    num_objects: int = -1, tuning: capi.Tuning | None = None) -> "Dataset":
+        arrs = [np.ascontiguousarray(vertices, np.float32), np.ascontiguousarray(indices, np.uint32),
+                np.ascontiguousarray(tri_to_object, np.int32), np.ascontiguousarray(edge_starts, np.float32),
+                np.ascontiguousarray(edge_ends, np.float32), np.ascontiguousarray(edge_src, np.int32)]
+        v = capi.MeshView()
+        v.vertices, v.num_vertices = arrs[0].ctypes.data, arrs[0].size // 3
+        v.indices, v.num_triangles = arrs[1].ctypes.data, arrs[1].size // 3
+        v.tri_to_object = arrs[2].ctypes.data
+        v.edge_starts, v.edge_ends, v.edge_src = arrs[3].ctypes.data, arrs[4].ctypes.data, arrs[5].ctypes.data
+        v.num_edges = arrs[5].size
+        v.num_objects = num_objects
+        h = C.c_void_p()
+        t = tuning if tuning is not None else default_tuning()
+        check(capi.lib().pierce_dataset_create(ctx.handle, C.byref(v), capi.HOST_MEMORY, C.byref(t), C.byref(h)),
+              "dataset_create")
+        return cls(ctx, h)
+
+    @classmethod
+    def from_geometry(cls, ctx: Context, geom, tuning: capi.Tuning | None = None) -> "Dataset":
+        if not geom.has_edges:
+            raise ValueError("geometry carries no precomputed edges; run extract_edges() first")
+        return cls.from_arrays(ctx, geom.vertices, geom.indices, geom.tri_to_object, geom.edge_starts,
+                               geom.edge_ends, geom.edge_src, geom.num_objects, tuning)
+
+    @classmethod
+    def from_device(cls, ctx: Context, view: capi.MeshView, tuning: capi.Tuning | None = None) -> "Dataset":
+        h = C.c_void_p()
+        t = tuning if tuning is not None else default_tuning()
+        check(capi.lib().pierce_dataset_create(ctx.handle, C.byref(view), capi.DEVICE_MEMORY, C.byref(t),
+                                               C.byref(h)), "dataset_create(device)")
+        return cls(ctx, h)
+
+    def build(self, tuning: capi.Tuning | None = None) -> None:
+        t = tuning if tuning is not None else default_tuning()
+        check(self._lib.pierce_dataset_build(self.ctx.handle, self._h, C.byref(t)), "dataset_build")
+
+    def info(self) -> capi.DatasetInfo:
+        i = capi.DatasetInfo()
+        check(self._lib.pierce_dataset_info_get(self._h, C.byref(i)), "dataset_info")
+        return i
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.pierce_dataset_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+@dataclass
+class JoinResult:
+    pairs: np.ndarray          # (n, 2) int32, sorted by (a, b)
+    stats: dict
+    containment_count: int = 0
+
+
+def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,
+              hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
+              max_retries=4) -> capi.JoinOpts:
+    o = capi.JoinOpts()
+    capi.lib().pierce_default_join_opts(C.byref(o))
+    o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
+    o.direction = DIRECTIONS[direction] if isinstance(direction, str) else int(direction)
+    o.sizing = SIZINGS[sizing] if isinstance(sizing, str) else int(sizing)
+    o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    o.expected_pairs = int(expected_pairs)
+    o.hash_table_slots = int(hash_table_slots)
+    o.hash_load_factor = float(hash_load_factor)
+    o.output_safety = float(output_safety)
+    o.include_overlap_pairs = 1 if include_overlap_pairs else 0
+    o.max_retries = int(max_retries)
+    return o
+
+
+def run_join(ctx: Context, a: Dataset, b: Dataset, opts: capi.JoinOpts, download: bool = True):
+    """Run one join; returns (JoinResult, result handle or None)."""
+    L = capi.lib()
+    r = C.c_void_p()
+    st = capi.Stats()
+    check(L.pierce_join(ctx.handle, a.handle, b.handle, C.byref(opts), C.byref(r), C.byref(st)), "join")
+    try:
+        n = C.c_uint64()
+        check(L.pierce_result_count(r, C.byref(n)), "result_count")
+        nc = C.c_uint64()
+        check(L.pierce_result_containment_count(r, C.byref(nc)), "result_containment_count")
+        pairs = np.zeros((n.value, 2), dtype=np.int32)
+        if download and n.value:
+            check(L.pierce_result_copy(ctx.handle, r, pairs.ctypes.data, n.value), "result_copy")
+        return JoinResult(pairs, st.as_dict(), int(nc.value))
+    finally:
+        L.pierce_result_destroy(r)
+
+
+def join(ctx: Context, a: Dataset, b: Dataset, **kw) -> JoinResult:
+    return run_join(ctx, a, b, make_opts(**kw))
+
+
+def overlap_join(ctx, a, b, **kw) -> JoinResult:
+    kw.setdefault("sizing", "hash")
+    return join(ctx, a, b, predicate="overlap", **kw)
+
+
+def overlap_join_two_pass(ctx, a, b, **kw) -> JoinResult:
+    return join(ctx, a, b, predicate="overlap", sizing="two_pass", **kw)
+
+
+def intersection_join(ctx, a, b, **kw) -> JoinResult:
+    return join(ctx, a, b, predicate="intersection", **kw)
+
+
+def containment_join(ctx, a, b, **kw) -> JoinResult:
+    return join(ctx, a, b, predicate="containment", **kw)
+
+
+def pairs_to_keys(pairs: np.ndarray) -> np.ndarray:
+    p = np.asarray(pairs).reshape(-1, 2)
+    return (p[:, 0].astype(np.uint32).astype(np.uint64) << np.uint64(32)) | p[:, 1].astype(np.uint32).astype(np.uint64)

@@ -1,0 +1,128 @@
+"""GPU parity tests: the CUDA join path against the CPU oracle.
+
+Every case compares the sorted (a, b) pair set bit-for-bit.  Inputs are the
+seeded generators at sizes the oracle finishes in seconds.
+"""
+import numpy as np
+import pytest
+
+import pierce_gb300 as pg
+from pierce_gb300 import join as J
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def keys(res):
+    return J.pairs_to_keys(res.pairs)
+
+
+def ds(ctx, geom, leaf=1):
+    return J.Dataset.from_geometry(ctx, geom, J.default_tuning(leaf_size=leaf))
+
+
+CASES = {
+    "icospheres": lambda: (pg.icospheres(101, 300, 3, hi=60.0), pg.icospheres(202, 300, 3, hi=60.0)),
+    "ellipsoids_contacts": lambda: pg.ellipsoid_pair(1, 2, 300, 300, 2, lo=0, hi=70, frac_contact=0.1),
+    "tubes_vs_ellipsoids": lambda: (pg.tubes(5, 4, 6000, hi=40.0),
+                                    pg.ellipsoid_pair(3, 4, 10, 400, 2, lo=0, hi=40)[1]),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    A, B = CASES[request.param]()
+    return request.param, A, B
+
+
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+@pytest.mark.parametrize("leaf", [1, 4])
+def test_overlap_exact_matches_oracle(ctx, case, sizing, leaf):
+    name, A, B = case
+    want, _ = O.overlap_keys(A, B)
+    got = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing)
+    assert np.array_equal(keys(got), want), name
+    passes = 2 if sizing == "two_pass" else 1
+    assert got.stats["rays"] == passes * (A.num_edges + B.num_edges)
+
+
+def test_overlap_fp32_plain_matches_oracle_fp32(ctx, case):
+    name, A, B = case
+    want, _ = O.overlap_keys(A, B, mode=1)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B), precision="fp32", sizing="two_pass")
+    assert np.array_equal(keys(got), want), name
+
+
+@pytest.mark.parametrize("direction", ["mesh1_to_mesh2", "mesh2_to_mesh1"])
+def test_overlap_direction(ctx, case, direction):
+    name, A, B = case
+    want, _ = O.overlap_keys(A, B, direction=1 if direction == "mesh1_to_mesh2" else 2)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B), direction=direction)
+    assert np.array_equal(keys(got), want), name
+
+
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+def test_intersection_matches_oracle(ctx, case, sizing):
+    name, A, B = case
+    want = O.intersection_keys(A, B)
+    got = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
+    assert np.array_equal(keys(got), want), name
+
+
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+def test_containment_matches_oracle(ctx, case, sizing):
+    name, A, B = case
+    want = O.containment_keys(A, B)
+    got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
+    assert np.array_equal(keys(got), want), name
+    assert got.containment_count == len(want)
+
+
+def test_containment_include_overlap(ctx, case):
+    name, A, B = case
+    cont = O.containment_keys(A, B)
+    over, _ = O.overlap_keys(A, B)
+    got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), include_overlap_pairs=True)
+    k = keys(got)
+    assert got.containment_count == len(cont)
+    assert np.array_equal(k[: len(cont)], cont)
+    assert np.array_equal(k[len(cont):], over)
+
+
+def test_tiny_hash_table_recovers(ctx, case):
+    """A deliberately undersized table is enlarged and the join rerun."""
+    name, A, B = case
+    want, _ = O.overlap_keys(A, B)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B), sizing="fixed", hash_table_slots=16, max_retries=12)
+    assert np.array_equal(keys(got), want)
+    if len(want) > 8:
+        assert got.stats["retries"] > 0
+
+
+def test_empty_and_single(ctx):
+    A = pg.icospheres(1, 1, 0, hi=0.0)          # one icosahedron at the origin
+    z = np.zeros((0, 3), np.float32)
+    empty = J.Dataset.from_arrays(ctx, z, np.zeros((0, 3), np.uint32), np.zeros(0, np.int32), z, z,
+                                  np.zeros(0, np.int32))
+    got = J.intersection_join(ctx, ds(ctx, A), empty)
+    assert got.pairs.shape == (0, 2)
+    # single triangle target
+    v = np.array([[-5, -5, 0], [5, -5, 0], [0, 5, 0]], np.float32)
+    T = pg.Geometry.from_arrays(v, np.array([[0, 1, 2]], np.uint32), np.array([0], np.int32)).extract_edges()
+    want, _ = O.overlap_keys(A, T)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, T))
+    assert np.array_equal(keys(got), want)
+    assert len(want) == 1
+
+
+def test_identical_datasets_coplanar(ctx):
+    """B == A: every face coplanar with a face of the other side."""
+    A = pg.icospheres(7, 50, 2, hi=30.0)
+    B = pg.Geometry.from_arrays(A.vertices, A.indices, A.tri_to_object).extract_edges()
+    want, _ = O.overlap_keys(A, B)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B))
+    assert np.array_equal(keys(got), want)
+    assert all((want >> np.uint64(32)) >= 0)
+    diag = (want >> np.uint64(32)) == (want & np.uint64(0xFFFFFFFF))
+    assert diag.sum() == 50
+    assert got.stats["fp32_ambiguous"] > 0
