@@ -1,0 +1,380 @@
+"""Benchmark of the mesh spatial-join path on one GB300.
+
+Workload (default): two datasets of 50,000 perturbed ellipsoids each
+(subdivision-3 icospheres, semi-axes U[2,5], random rotation, 5 % radial
+smooth value noise, in [0,1000]^3; 20 % of B scaled 0.3 inside a random A
+mesh, 1 % of B sharing exact vertices or faces with an A mesh), float32,
+seeded synthetic data.  One step = the join work a user of the executables
+runs per query pair: rebuild both BVHs from the resident geometry, then an
+intersection join and a containment join (2 join queries), from resident
+device geometry to the sorted device pair sets.
+
+Printed JSON line (rank 0):
+  value      – join queries/s with inputs resident in HBM (CUDA events on the
+               library's stream);
+  e2e        – the same metric through the C ABI from pinned host buffers:
+               H2D of both datasets, BVH builds, both joins, D2H of the pairs;
+  roofline   – the edge-ray traversal kernel against measured HBM bandwidth,
+               with algorithmic bytes per launch
+               28*E_src + 16*F_tgt + 12*V_tgt + 32*(2*F_tgt - 1) + 8*P_raw;
+  cpu_baseline – the CPU oracle (exact Face-style restatement, OpenMP) on a
+               spatial sample of the same workload, extrapolated.
+
+``--impl reference`` times the CPU restatement of the reference path instead
+(the reference's GPU path needs OptiX and cannot run here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "join queries/s & ray-tri tests/s, 1 GB300, exact pair set, tuned vs plain"
+UNIT = "join queries/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(scale: float = 1.0, seed_a: int = 2024, seed_b: int = 2025):
+    import pierce_gb300 as pg
+    n = max(10, int(round(50_000 * scale)))
+    hi = 1000.0 * scale ** (1.0 / 3.0)
+    A, B = pg.ellipsoid_pair(seed_a, seed_b, n, n, 3, 2.0, 5.0, 0.05, 0.0, hi, 0.2, 0.3, 0.01)
+    return A, B, {"workload": "ellipsoids-intersection+containment", "meshes_per_side": n,
+                  "subdivision": 3, "box": [0.0, round(hi, 3)], "triangles_per_side": A.num_triangles,
+                  "edges_per_side": A.num_edges, "seeds": [seed_a, seed_b]}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path: Path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, device: int = 0):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def edge_ray_bytes(src, tgt, raw_hits):
+    """Algorithmic bytes of one edge-ray launch (src edges vs tgt BVH)."""
+    E, F, V = src.num_edges, tgt.num_triangles, tgt.vertices.shape[0]
+    return 28 * E + 16 * F + 12 * V + 32 * (2 * F - 1) + 8 * raw_hits
+
+
+def cpu_sample(A_full, B_full, target_objects: int, seed: int = 7):
+    """Spatial sample: objects whose first vertex lies in a sub-cube holding
+    about target_objects objects of A; returns (A_sub, B_sub, fraction)."""
+    import pierce_gb300 as pg
+    nA = A_full.num_objects
+    frac = min(1.0, target_objects / max(nA, 1))
+    fa = A_full.first_vertices()
+    fb = B_full.first_vertices()
+    lo = np.minimum(fa.min(0), fb.min(0))
+    hi = np.maximum(fa.max(0), fb.max(0))
+    side = (hi - lo) * frac ** (1.0 / 3.0)
+    sel_hi = lo + side
+
+    def subset(G, fv):
+        keep = np.all((fv >= lo) & (fv <= sel_hi), axis=1)
+        objs = np.nonzero(keep)[0]
+        remap = -np.ones(G.num_objects, np.int64)
+        remap[objs] = np.arange(len(objs))
+        t2o = G.tri_to_object
+        tmask = keep[t2o]
+        idx = G.indices[tmask]
+        sub = pg.Geometry.from_arrays(G.vertices, idx, remap[t2o[tmask]].astype(np.int32))
+        es, ee, src = G.edge_starts, G.edge_ends, G.edge_src
+        em = keep[src]
+        sub.set_edges(es[em], ee[em], remap[src[em]].astype(np.int32))
+        return sub, len(objs)
+
+    As, na = subset(A_full, fa)
+    Bs, nb = subset(B_full, fb)
+    return As, Bs, na / max(nA, 1)
+
+
+def cpu_join_seconds(As, Bs) -> float:
+    """Exact CPU restatement of the intersection + containment joins."""
+    from oracle import pyoracle as O
+    t0 = time.perf_counter()
+    O.intersection_keys(As, Bs)
+    O.containment_keys(As, Bs)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    """CPU restatement of the reference path (the oracle port), all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as O
+    O.build()
+    A, B, cfg = workload(args.scale)
+    As, Bs, frac = cpu_sample(A, B, args.cpu_sample_objects)
+    threads = O.max_threads()
+    for _ in range(max(args.warmup, 0)):
+        cpu_join_seconds(As, Bs)
+    times = [cpu_join_seconds(As, Bs) for _ in range(args.steps)]
+    step_s = statistics.mean(times)
+    full_s = step_s / max(frac, 1e-12)   # seconds for the full workload's 2 joins
+    value = 2.0 / full_s
+    sample = (f"spatial sub-cube holding {As.num_objects}+{Bs.num_objects} of "
+              f"{A.num_objects}+{B.num_objects} objects (fraction {frac:.4f}); time scaled by 1/fraction")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * full_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/exact",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="pierce", choices=["pierce", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full workload (debug only)")
+    ap.add_argument("--cpu-sample-objects", type=int, default=3000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--leaf-size", type=int, default=1)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    import torch
+    from pierce_gb300 import capi
+    from pierce_gb300 import join as J
+    import ctypes as C
+
+    A, B, cfg = workload(args.scale)
+    ctx = J.Context(local_rank)
+    tuning = J.default_tuning(leaf_size=args.leaf_size)
+    da = J.Dataset.from_geometry(ctx, A, tuning)
+    db = J.Dataset.from_geometry(ctx, B, tuning)
+    opts_i = J.make_opts(predicate="intersection", sizing="hash", expected_pairs=4 * A.num_objects)
+    opts_c = J.make_opts(predicate="containment", sizing="hash", expected_pairs=4 * A.num_objects)
+    L = capi.lib()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local_rank))
+
+    def device_step(collect=None):
+        da.build(tuning)
+        db.build(tuning)
+        ri = J.run_join(ctx, da, db, opts_i, download=False)
+        rc = J.run_join(ctx, da, db, opts_c, download=False)
+        if collect is not None:
+            collect.append((ri, rc))
+        return ri, rc
+
+    for _ in range(args.warmup):
+        device_step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv" if (ROOT / "gpurun_out").exists()
+                    else Path(tempfile.gettempdir()) / f"pierce_clocks_{rank}.csv")
+    collected = []
+    l0 = ctx.kernel_launches
+    with clocks:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            device_step(collected)
+        e1.record(stream)
+        e1.synchronize()
+    launches = ctx.kernel_launches - l0
+    ms_total = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    queries = 2 * args.steps * world
+    value = queries / (ms_total / 1000.0)
+
+    # roofline of the dominant kernel: edge rays (both directions, both joins)
+    ri, rc = collected[-1]
+    edge_ms = ri.stats["ms_edge_rays"][0] + ri.stats["ms_edge_rays"][1]
+    raw_hits = ri.stats["raw_hits"]
+    bytes_ab = edge_ray_bytes(A, B, raw_hits / 2)
+    bytes_ba = edge_ray_bytes(B, A, raw_hits / 2)
+    achieved = (bytes_ab + bytes_ba) / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else 0.0
+    peak, peak_kind = peaks()
+    tri_tests = ri.stats["tri_tests"] + rc.stats["tri_tests"]
+    join_ms = ri.stats["ms_total"] + rc.stats["ms_total"]
+
+    # e2e through the C ABI from pinned host buffers
+    e2e = None
+    if rank == 0:
+        arrs = {}
+        for name, G in (("A", A), ("B", B)):
+            for field in ("vertices", "indices", "tri_to_object", "edge_starts", "edge_ends", "edge_src"):
+                src = np.ascontiguousarray(getattr(G, field))
+                pin = torch.empty(src.nbytes, dtype=torch.uint8, pin_memory=True)
+                pin.numpy()[:] = src.view(np.uint8).reshape(-1)
+                arrs[(name, field)] = (pin, src.shape)
+        h2d = sum(p.numel() for p, _ in arrs.values())
+
+        def view_of(name, G):
+            v = capi.MeshView()
+            v.vertices = arrs[(name, "vertices")][0].data_ptr()
+            v.num_vertices = G.vertices.shape[0]
+            v.indices = arrs[(name, "indices")][0].data_ptr()
+            v.num_triangles = G.num_triangles
+            v.tri_to_object = arrs[(name, "tri_to_object")][0].data_ptr()
+            v.edge_starts = arrs[(name, "edge_starts")][0].data_ptr()
+            v.edge_ends = arrs[(name, "edge_ends")][0].data_ptr()
+            v.edge_src = arrs[(name, "edge_src")][0].data_ptr()
+            v.num_edges = G.num_edges
+            v.num_objects = G.num_objects
+            return v
+
+        va, vb = view_of("A", A), view_of("B", B)
+        out_pairs = torch.empty(8 * (1 << 22), dtype=torch.uint8, pin_memory=True)
+
+        def e2e_step():
+            ha, hb = C.c_void_p(), C.c_void_p()
+            capi.check(L.pierce_dataset_create(ctx.handle, C.byref(va), capi.HOST_MEMORY, C.byref(tuning),
+                                               C.byref(ha)), "e2e dataset A")
+            capi.check(L.pierce_dataset_create(ctx.handle, C.byref(vb), capi.HOST_MEMORY, C.byref(tuning),
+                                               C.byref(hb)), "e2e dataset B")
+            d2h = 0
+            for o in (opts_i, opts_c):
+                r = C.c_void_p()
+                capi.check(L.pierce_join(ctx.handle, ha, hb, C.byref(o), C.byref(r), None), "e2e join")
+                n = C.c_uint64()
+                L.pierce_result_count(r, C.byref(n))
+                cap = out_pairs.numel() // 8
+                capi.check(L.pierce_result_copy(ctx.handle, r, out_pairs.data_ptr(), min(n.value, cap)),
+                           "e2e copy")
+                d2h += 8 * min(n.value, cap)
+                L.pierce_result_destroy(r)
+            L.pierce_dataset_destroy(ha)
+            L.pierce_dataset_destroy(hb)
+            return d2h
+
+        e2e_step()
+        t0 = time.perf_counter()
+        d2h_total = 0
+        e2e_steps = max(1, min(args.steps, 3))
+        for _ in range(e2e_steps):
+            d2h_total += e2e_step()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e = {"value": 2.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h_total // e2e_steps), "ms_per_step": 1000.0 * e2e_s}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+        As, Bs, frac = cpu_sample(A, B, args.cpu_sample_objects)
+        secs = cpu_join_seconds(As, Bs)
+        full = secs / max(frac, 1e-12)
+        cpu = {"value": 2.0 / full, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+               "sample": (f"intersection+containment joins of the objects in a spatial sub-cube "
+                          f"({As.num_objects}+{Bs.num_objects} of {A.num_objects}+{B.num_objects} objects, "
+                          f"fraction {frac:.4f}) took {secs:.2f} s; scaled by 1/fraction")}
+
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        return 0
+    clk = clocks.summary(local_rank)
+    cfg.update({"l2": "inputs larger than L2 (about 9 GB of geometry and BVH per side, 129 MB L2)",
+                "leaf_size": args.leaf_size, "sizing": "hash", "precision": "exact (fp32 filter, fp64, expansions)",
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU"})
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic", "config": cfg,
+        "ray_tri_tests_per_s": tri_tests / (join_ms / 1000.0) if join_ms > 0 else None,
+        "rays_per_s": (ri.stats["rays"]) / (edge_ms / 1000.0) if edge_ms > 0 else None,
+        "pairs": {"intersection": ri.stats["num_pairs"], "containment": rc.stats["num_pairs"]},
+        "ambiguous": {"fp32": ri.stats["fp32_ambiguous"], "fp64": ri.stats["fp64_ambiguous"],
+                      "tests": ri.stats["tri_tests"]},
+        "phase_ms": {"intersection": ri.stats["ms_total"], "containment": rc.stats["ms_total"],
+                     "edge_rays": edge_ms, "parity": sum(ri.stats["ms_parity"]), "dedup": ri.stats["ms_dedup"],
+                     "bvh_build": da.info().ms_build + db.info().ms_build},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "kernel": "k_edge_rays (exact, hash mode)", "peak_kind": peak_kind},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
