@@ -35,7 +35,9 @@ int estimate_cells(pierce_ctx* ctx, const void* a, const void* b, int n, float c
 using namespace pgpu;
 
 namespace {
-thread_local std::string g_err;
+// Last error message of the calling host thread.  A fixed buffer, so that
+// reporting an error never allocates.
+thread_local char g_err[512];
 
 // scratch slot assignment
 enum : int {
@@ -52,10 +54,12 @@ enum : int {
 
 namespace pgpu {
 
-int set_error(int status, const std::string& msg) {
-    g_err = msg;
+int set_error_cstr(int status, const char* msg) {
+    std::snprintf(g_err, sizeof(g_err), "%s", msg ? msg : "");
     return status;
 }
+
+int set_error(int status, const std::string& msg) { return set_error_cstr(status, msg.c_str()); }
 
 int check_cuda(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return PIERCE_OK;
@@ -167,7 +171,7 @@ struct EventTimer {
 // ------------------------------------------------------------------ C ABI --
 extern "C" {
 
-const char* pierce_last_error(void) { return g_err.c_str(); }
+const char* pierce_last_error(void) { return g_err; }
 
 const char* pierce_status_string(int status) {
     switch (status) {

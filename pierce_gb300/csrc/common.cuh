@@ -129,6 +129,7 @@ struct pierce_result {
 namespace pgpu {
 // error reporting (capi.cu)
 int set_error(int status, const std::string& msg);
+int set_error_cstr(int status, const char* msg);  // never allocates
 int check_cuda(cudaError_t e, const char* what);
 // grow-only scratch buffer `slot` of at least `bytes`
 int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out);
