@@ -248,6 +248,27 @@ int pierce_merge_and_deduplicate_pairs(pierce_ctx* ctx, const pierce_pair* d_pai
 int pierce_compact_hash_table_pairs(pierce_ctx* ctx, const uint64_t* d_table, uint64_t table_slots,
                                     pierce_pair* d_out, uint64_t max_output, uint64_t* count);
 
+/* ---- de-duplication without allocation ---------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they need unique pairs: code that runs between stream-ordered
+ * steps and must not let cudaMalloc/cudaFree synchronise the device, and
+ * plug-ins whose host application owns the memory budget.  The caller passes
+ * the input pairs, an output array of at least n pairs and a device word for
+ * the unique count; the scratch is a hash set in a fixed device array of
+ * PIERCE_NOALLOC_TABLE_SLOTS 64-bit slots (32 MiB) that every GPU loading
+ * this library holds until the process exits.  Inputs larger than
+ * PIERCE_NOALLOC_MAX_PAIRS pairs are rejected with
+ * PIERCE_ERR_INVALID_ARGUMENT.  The call enqueues its work on `stream` (a
+ * cudaStream_t of the current device) and returns without waiting; the
+ * unique pairs land in d_out[0 .. *d_num_unique) in no particular order.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls whose work overlaps on the GPU race: order them on one stream. */
+#define PIERCE_NOALLOC_TABLE_SLOTS (1u << 22)
+#define PIERCE_NOALLOC_MAX_PAIRS (1u << 21)
+int pierce_deduplicate_pairs_noalloc(const pierce_pair* d_pairs, int64_t n, pierce_pair* d_out,
+                                     uint64_t* d_num_unique, void* stream);
+
 /* ---- output sizing ------------------------------------------------------ */
 /* Grid selectivity estimate (GridCell statistics of both datasets); the
  * cells arrays are host memory of 28-byte records {int3 index; u32 center;

@@ -39,6 +39,8 @@ BOTH, MESH1_TO_MESH2, MESH2_TO_MESH1 = 0, 1, 2
 SIZING_TWO_PASS, SIZING_HASH, SIZING_FIXED = 0, 1, 2
 EXACT, FP32 = 0, 1
 RAYS_COUNT, RAYS_WRITE, RAYS_HASH = 0, 1, 2
+NOALLOC_TABLE_SLOTS = 1 << 22
+NOALLOC_MAX_PAIRS = 1 << 21
 
 
 class MeshView(C.Structure):
@@ -106,6 +108,7 @@ SIGNATURES = {
     "pierce_exclusive_scan": (C.c_int, [V, V, V, I64, C.POINTER(I64)]),
     "pierce_merge_and_deduplicate_pairs": (C.c_int, [V, V, I64, V, I64, V, C.POINTER(I64)]),
     "pierce_compact_hash_table_pairs": (C.c_int, [V, V, U64, V, U64, C.POINTER(U64)]),
+    "pierce_deduplicate_pairs_noalloc": (C.c_int, [V, I64, V, V, V]),
     "pierce_estimate_pairs": (C.c_int, [V, V, C.c_uint32, V, C.c_uint32, F, F, F, C.c_int,
                                         C.POINTER(D), C.POINTER(I64), C.POINTER(I32)]),
 }
