@@ -114,6 +114,17 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(value: float, dist) -> float:
+    """Largest per-rank time: the job is as slow as its slowest replica."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def edge_ray_bytes(src, tgt, raw_hits):
     """Algorithmic bytes of one edge-ray launch (src edges vs tgt BVH)."""
     E, F, V = src.num_edges, tgt.num_triangles, tgt.vertices.shape[0]
@@ -255,10 +266,7 @@ def main():
         e1.synchronize()
     launches = ctx.kernel_launches - l0
     ms_total = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, dist)
     ms_step = ms_total / args.steps
     queries = 2 * args.steps * world
     value = queries / (ms_total / 1000.0)

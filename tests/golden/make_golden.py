@@ -1,0 +1,89 @@
+"""Generate the committed golden fixtures (run in the development container,
+where the reference sources are present).
+
+* ``ref_*.pre`` / ``ref_digests.json`` — outputs of the reference's own
+  `.pre` tool (``oracle/_ref/ref_pre_tool``: the reference's BinaryIO.h and
+  EdgePreprocessor.cpp compiled from their sources) for seeded meshes written
+  without edges by this repository.  They pin this repository's writer and
+  edge extractor byte for byte (header padding bytes 50..55 excluded: the
+  reference leaves them uninitialised).
+* ``pairs_*.npz`` — oracle pair sets for small joins (overlap, intersection,
+  containment, FP32 plain overlap), so the GPU tests also compare against
+  stored answers.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+import pierce_gb300 as pg  # noqa: E402
+from oracle import pyoracle as O  # noqa: E402
+
+REF_TOOL = ROOT / "oracle" / "_ref" / "ref_pre_tool"
+
+# Datasets whose reference `.pre` output is pinned.  (name, builder)
+FORMAT_CASES = {
+    "icospheres_l1": lambda: pg.icospheres(7, 20, 1, hi=20.0),
+    "icospheres_l3": lambda: pg.icospheres(8, 40, 3, hi=40.0),
+    "ellipsoids_l2": lambda: pg.ellipsoid_pair(1, 2, 30, 30, 2, lo=0, hi=30, frac_contact=0.2)[1],
+    "tubes": lambda: pg.tubes(3, 2, 3000),
+}
+STORE_FULL = {"icospheres_l1"}   # small enough to commit the reference file itself
+
+JOIN_CASES = {
+    "icospheres": lambda: (pg.icospheres(101, 200, 2, hi=45.0), pg.icospheres(202, 200, 2, hi=45.0)),
+    "ellipsoid_contacts": lambda: pg.ellipsoid_pair(5, 6, 150, 150, 2, lo=0, hi=50, frac_contact=0.1),
+}
+
+
+def zero_padding(b: bytes) -> bytes:
+    return b[:50] + b"\x00" * 6 + b[56:]
+
+
+def raw_without_edges(geom) -> "pg.Geometry":
+    return pg.Geometry.from_arrays(geom.vertices, geom.indices, geom.tri_to_object)
+
+
+def main() -> None:
+    if not REF_TOOL.exists():
+        raise SystemExit("oracle/_ref/ref_pre_tool missing: run oracle/build_ref.sh first")
+    digests = {}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for name, make in FORMAT_CASES.items():
+            raw = raw_without_edges(make())
+            raw.write_pre(td / "in.pre")
+            subprocess.run([str(REF_TOOL), str(td / "in.pre"), str(td / "out.pre")], check=True,
+                           stdout=subprocess.DEVNULL)
+            ref = zero_padding((td / "out.pre").read_bytes())
+            digests[name] = {"sha256": hashlib.sha256(ref).hexdigest(), "bytes": len(ref),
+                             "input_sha256": hashlib.sha256(zero_padding((td / "in.pre").read_bytes())).hexdigest()}
+            if name in STORE_FULL:
+                (HERE / f"ref_{name}.pre").write_bytes(ref)
+    (HERE / "ref_digests.json").write_text(json.dumps(digests, indent=1, sort_keys=True) + "\n")
+
+    for name, make in JOIN_CASES.items():
+        A, B = make()
+        over, _ = O.overlap_keys(A, B)
+        fp32, _ = O.overlap_keys(A, B, mode=1)
+        inter = O.intersection_keys(A, B)
+        cont = O.containment_keys(A, B)
+        np.savez_compressed(HERE / f"pairs_{name}.npz", overlap=over, overlap_fp32=fp32,
+                            intersection=inter, containment=cont)
+        print(name, len(over), len(fp32), len(inter), len(cont))
+
+
+if __name__ == "__main__":
+    main()

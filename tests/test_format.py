@@ -1,0 +1,145 @@
+"""`.pre` format, edge extraction and generators (CPU only).
+
+The committed fixtures in tests/golden were produced by the reference's own
+`.pre` reader/writer and edge extractor (compiled from its sources by
+oracle/build_ref.sh); see tests/golden/make_golden.py.
+"""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import pierce_gb300 as pg
+from pierce_gb300.geometry import HostError
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+sys_path_ok = True
+
+
+def zero_padding(b: bytes) -> bytes:
+    return b[:50] + b"\x00" * 6 + b[56:]
+
+
+def _make(name):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.FORMAT_CASES[name]()
+
+
+DIGESTS = json.loads((GOLDEN / "ref_digests.json").read_text())
+
+
+@pytest.mark.parametrize("name", sorted(DIGESTS))
+def test_edges_and_writer_match_reference(tmp_path, name):
+    geom = _make(name)
+    raw = pg.Geometry.from_arrays(geom.vertices, geom.indices, geom.tri_to_object)
+    raw.write_pre(tmp_path / "in.pre")
+    inp = zero_padding((tmp_path / "in.pre").read_bytes())
+    # the generator is bit-identical on every host
+    assert hashlib.sha256(inp).hexdigest() == DIGESTS[name]["input_sha256"]
+    raw.extract_edges(0)
+    raw.write_pre(tmp_path / "out.pre")
+    out = zero_padding((tmp_path / "out.pre").read_bytes())
+    assert len(out) == DIGESTS[name]["bytes"]
+    assert hashlib.sha256(out).hexdigest() == DIGESTS[name]["sha256"]
+
+
+def test_reference_file_reads_and_rewrites_identically(tmp_path):
+    ref = (GOLDEN / "ref_icospheres_l1.pre").read_bytes()
+    g = pg.Geometry.read_pre(GOLDEN / "ref_icospheres_l1.pre")
+    assert g.has_edges and g.num_objects == 20 and g.num_triangles == 20 * 80
+    g.write_pre(tmp_path / "again.pre")
+    assert zero_padding((tmp_path / "again.pre").read_bytes()) == ref
+
+
+def test_object_order_has_the_same_edge_set():
+    geom = _make("tubes")
+    raw = pg.Geometry.from_arrays(geom.vertices, geom.indices, geom.tri_to_object)
+    raw.extract_edges(0)
+    a = np.concatenate([raw.edge_starts, raw.edge_ends, raw.edge_src[:, None].view(np.float32)], 1)
+    raw.extract_edges(1)
+    b = np.concatenate([raw.edge_starts, raw.edge_ends, raw.edge_src[:, None].view(np.float32)], 1)
+    sa = np.sort(a.view(np.uint32).view([("", np.uint32)] * 7).ravel())
+    sb = np.sort(b.view(np.uint32).view([("", np.uint32)] * 7).ravel())
+    assert np.array_equal(sa, sb)
+    # object order: source ids non-decreasing
+    assert np.all(np.diff(raw.edge_src) >= 0)
+
+
+def test_unique_edges_of_closed_icospheres():
+    g = pg.icospheres(3, 7, 2)
+    assert g.num_edges == 7 * 30 * 4 ** 2          # E = 1.5 F for closed 2-manifolds
+    assert g.num_triangles == 7 * 20 * 4 ** 2
+    assert g.vertices.shape[0] == 7 * (10 * 4 ** 2 + 2)
+
+
+def test_edge_rules_out_of_range_and_mismatch():
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    # a triangle with an out-of-range index is skipped
+    g = pg.Geometry.from_arrays(v, np.array([[0, 1, 2], [0, 1, 9]], np.uint32), np.array([0, 0], np.int32))
+    g.extract_edges(0)
+    assert g.num_edges == 3
+    # duplicate vertices closer than the 1e-5 quantum collapse into one key
+    v2 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1.000001, 0, 0]], np.float32)
+    g2 = pg.Geometry.from_arrays(v2, np.array([[0, 1, 2], [0, 3, 2]], np.uint32), np.array([0, 0], np.int32))
+    g2.extract_edges(0)
+    assert g2.num_edges == 3
+    # first-seen orientation is kept: edge 1->0 comes from triangle (0,1,2) as 0->1
+    assert any(np.array_equal(s, [0, 0, 0]) and np.array_equal(e, [1, 0, 0])
+               for s, e in zip(g2.edge_starts, g2.edge_ends))
+
+
+def test_grid_stats_roundtrip(tmp_path):
+    g = pg.icospheres(9, 30, 1, hi=30.0).grid_stats(5.0)
+    cells = g.grid_cells
+    assert len(cells) > 0 and cells["touch_count"].sum() >= 30 and cells["center_count"].sum() == 30
+    assert np.all(cells["vol_ratio"] <= 1.0) and np.all(cells["vol_ratio"] > 0.2)
+    g.write_pre(tmp_path / "g.pre")
+    h = pg.Geometry.read_pre(tmp_path / "g.pre")
+    assert np.array_equal(h.grid_cells, cells)
+    assert h.view().grid_cell_size == 5.0
+
+
+@pytest.mark.parametrize("damage,status", [("magic", 2), ("version", 3), ("truncate", 1), ("header", 1)])
+def test_corrupt_files_are_rejected(tmp_path, damage, status):
+    g = pg.icospheres(4, 3, 1)
+    p = tmp_path / "x.pre"
+    g.write_pre(p)
+    b = bytearray(p.read_bytes())
+    if damage == "magic":
+        b[0] ^= 0xFF
+    elif damage == "version":
+        b[4] = 3
+    elif damage == "truncate":
+        b = b[: len(b) - 17]
+    else:
+        b = b[:20]
+    p.write_bytes(bytes(b))
+    with pytest.raises(HostError) as e:
+        pg.Geometry.read_pre(p)
+    assert f"status {status}" in str(e.value)
+
+
+def test_missing_file():
+    with pytest.raises(HostError):
+        pg.Geometry.read_pre("/nonexistent/dir/none.pre")
+
+
+def test_generators_are_deterministic():
+    a = pg.ellipsoid_pair(3, 4, 20, 20, 1, frac_contact=0.3)
+    b = pg.ellipsoid_pair(3, 4, 20, 20, 1, frac_contact=0.3)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.vertices, y.vertices) and np.array_equal(x.edge_starts, y.edge_starts)
+    c = pg.ellipsoid_pair(3, 5, 20, 20, 1)
+    assert not np.array_equal(a[1].vertices, c[1].vertices)
+
+
+def test_inside_copies_are_inside():
+    A, B = pg.ellipsoid_pair(11, 12, 40, 200, 1, frac_inside=1.0, frac_contact=0.0, lo=0, hi=100)
+    from oracle import pyoracle as O
+    cont = O.containment_keys(A, B)
+    assert len(cont) == 200     # every B is a scaled copy strictly inside some A

@@ -1,0 +1,223 @@
+"""Pins of the CPU oracle's exact predicates against rational arithmetic,
+and self-consistency checks of its join definitions (CPU only)."""
+from fractions import Fraction as Fr
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import pierce_gb300 as pg
+from oracle import pyoracle as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+rng = np.random.default_rng(1234)
+
+
+def f32(*v):
+    return np.array(v, dtype=np.float32)
+
+
+def frac(p):
+    return [Fr(float(x)) for x in p]
+
+
+def det3(u, v, w):
+    return (u[0] * (v[1] * w[2] - v[2] * w[1]) + u[1] * (v[2] * w[0] - v[0] * w[2])
+            + u[2] * (v[0] * w[1] - v[1] * w[0]))
+
+
+def sub(a, b):
+    return [x - y for x, y in zip(a, b)]
+
+
+def sgn(x):
+    return (x > 0) - (x < 0)
+
+
+def exact_orient3d(a, b, c, d):
+    A, B, Cc, D = map(frac, (a, b, c, d))
+    return sgn(det3(sub(B, A), sub(Cc, A), sub(D, A)))
+
+
+def random_points(n, degenerate):
+    pts = rng.uniform(-50, 50, size=(n, 4, 3)).astype(np.float32)
+    if degenerate:
+        # d in the plane of a, b, c up to float rounding, plus exact coplanar lattice cases
+        for k in range(n):
+            a, b, c = pts[k, 0], pts[k, 1], pts[k, 2]
+            s, t = rng.uniform(-1, 2, 2)
+            pts[k, 3] = (a + s * (b - a) + t * (c - a)).astype(np.float32)
+            if k % 3 == 0:
+                pts[k] = rng.integers(-4, 5, size=(4, 3)).astype(np.float32)
+                pts[k, 3] = pts[k, 0] + (pts[k, 1] - pts[k, 0]) + 2 * (pts[k, 2] - pts[k, 0])
+    return pts
+
+
+@pytest.mark.parametrize("degenerate", [False, True])
+def test_orient3d_matches_rationals(degenerate):
+    L = O.lib()
+    pts = random_points(400, degenerate)
+    zero = 0
+    for a, b, c, d in pts:
+        want = exact_orient3d(a, b, c, d)
+        got = L.oracle_orient3d(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data)
+        got_exact = L.oracle_orient3d_exact(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data)
+        assert got == want and got_exact == want
+        zero += want == 0
+    if degenerate:
+        assert zero > 50  # the lattice cases are exactly coplanar
+
+
+def test_orient3d_extreme_exponents():
+    L = O.lib()
+    tiny = np.float32(1e-40)   # subnormal
+    cases = [(f32(0, 0, 0), f32(tiny, 0, 0), f32(0, tiny, 0), f32(0, 0, tiny)),
+             (f32(1e30, 0, 0), f32(0, 1e30, 0), f32(0, 0, 1e30), f32(1e-30, 1e-30, 1e-30)),
+             (f32(1, 1, 1), f32(1, 1, 1), f32(2, 3, 4), f32(5, 6, 7))]
+    for a, b, c, d in cases:
+        assert L.oracle_orient3d(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data) == \
+            exact_orient3d(a, b, c, d)
+
+
+def exact_seg_tri(p, q, a, b, c):
+    """Closed segment vs closed triangle with rational arithmetic, by a
+    formulation independent of the oracle: solve p + t (q - p) = a + u e1 + v e2
+    when not parallel, else test in the plane by barycentric/segment logic."""
+    P, Q, A, B, Cc = map(frac, (p, q, a, b, c))
+    e1, e2, d = sub(B, A), sub(Cc, A), sub(Q, P)
+    n = [e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]]
+    if n == [0, 0, 0]:
+        return False
+    den = sum(x * y for x, y in zip(n, d))
+    s = sub(P, A)
+    if den != 0:
+        t = -sum(x * y for x, y in zip(n, s)) / den
+        if t < 0 or t > 1:
+            return False
+        X = [P[i] + t * d[i] for i in range(3)]
+        return point_in_tri(X, A, B, Cc, n)
+    if sum(x * y for x, y in zip(n, s)) != 0:
+        return False
+    # coplanar: endpoints inside, or crossing an edge (sampled exactly on the segment)
+    if point_in_tri(P, A, B, Cc, n) or point_in_tri(Q, A, B, Cc, n):
+        return True
+    for U, W in ((A, B), (B, Cc), (Cc, A)):
+        if seg_seg_coplanar(P, Q, U, W, n):
+            return True
+    return False
+
+
+def point_in_tri(X, A, B, Cc, n):
+    def side(U, W):
+        e = sub(W, U)
+        r = sub(X, U)
+        cr = [e[1] * r[2] - e[2] * r[1], e[2] * r[0] - e[0] * r[2], e[0] * r[1] - e[1] * r[0]]
+        return sgn(sum(x * y for x, y in zip(cr, n)))
+    s = [side(A, B), side(B, Cc), side(Cc, A)]
+    return not (1 in s and -1 in s)
+
+
+def seg_seg_coplanar(P, Q, U, W, n):
+    def o(a, b, c):
+        e, r = sub(b, a), sub(c, a)
+        cr = [e[1] * r[2] - e[2] * r[1], e[2] * r[0] - e[0] * r[2], e[0] * r[1] - e[1] * r[0]]
+        return sgn(sum(x * y for x, y in zip(cr, n)))
+
+    def on(a, b, c):
+        return all(min(a[i], b[i]) <= c[i] <= max(a[i], b[i]) for i in range(3))
+    d1, d2, d3, d4 = o(P, Q, U), o(P, Q, W), o(U, W, P), o(U, W, Q)
+    if d1 * d2 < 0 and d3 * d4 < 0:
+        return True
+    return ((d1 == 0 and on(P, Q, U)) or (d2 == 0 and on(P, Q, W)) or (d3 == 0 and on(U, W, P))
+            or (d4 == 0 and on(U, W, Q)))
+
+
+def seg_tri_cases(n):
+    out = []
+    for k in range(n):
+        tri = rng.integers(-3, 4, size=(3, 3)).astype(np.float32)
+        kind = k % 4
+        if kind == 0:      # generic
+            p, q = rng.uniform(-3, 3, size=(2, 3)).astype(np.float32)
+        elif kind == 1:    # endpoint on a vertex / edge point of the triangle
+            p = tri[rng.integers(3)] if k % 8 == 1 else ((tri[0] + tri[1]) / 2).astype(np.float32)
+            q = rng.integers(-3, 4, size=3).astype(np.float32)
+        elif kind == 2:    # coplanar segment
+            s, t, u, w = rng.integers(-2, 3, 4)
+            p = (tri[0] + s * (tri[1] - tri[0]) + t * (tri[2] - tri[0])).astype(np.float32)
+            q = (tri[0] + u * (tri[1] - tri[0]) + w * (tri[2] - tri[0])).astype(np.float32)
+        else:              # lattice segment
+            p, q = rng.integers(-3, 4, size=(2, 3)).astype(np.float32)
+        out.append((p, q, tri[0], tri[1], tri[2]))
+    return out
+
+
+def test_segment_triangle_matches_rationals():
+    L = O.lib()
+    hits = 0
+    for p, q, a, b, c in seg_tri_cases(1500):
+        want = exact_seg_tri(p, q, a, b, c)
+        got = L.oracle_seg_tri(p.ctypes.data, q.ctypes.data, a.ctypes.data, b.ctypes.data, c.ctypes.data, 0)
+        assert bool(got) == want, (p, q, a, b, c)
+        hits += want
+    assert 200 < hits < 1400
+
+
+def test_zray_crossing_counts_each_crossing_once():
+    """A +Z ray through shared edges and vertices of a closed lattice cube
+    crosses it exactly twice (once in, once out) from below and once from
+    inside; the symbolic perturbation resolves every tie."""
+    L = O.lib()
+    cube_v = np.array([[x, y, z] for x in (0, 2) for y in (0, 2) for z in (0, 2)], np.float32)
+    # 12 triangles of the cube surface (two per face)
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    tris = []
+    for a, b, c, d in faces:
+        tris += [(a, b, c), (a, c, d)]
+    for px, py in [(1, 1), (0, 0), (1, 0), (2, 2), (0.5, 1.5), (2, 1), (0, 2)]:
+        for pz, want in [(-1, 2), (1, 1), (3, 0)]:
+            p = np.array([px, py, pz], np.float32)
+            n = 0
+            for t in tris:
+                a, b, c = (cube_v[i] for i in t)
+                n += L.oracle_zray_crosses(p.ctypes.data, a.ctypes.data, b.ctypes.data, c.ctypes.data)
+            if px in (0, 2) or py in (0, 2):
+                # on the boundary in x or y: perturbation moves the point to +x/+y
+                inside_xy = (px < 2) and (py < 2)
+                assert n == (want if inside_xy else 0), (px, py, pz, n)
+            else:
+                assert n == want, (px, py, pz, n)
+
+
+def test_face_restatement_equals_edge_definition():
+    A, B = pg.ellipsoid_pair(21, 22, 120, 120, 2, lo=0, hi=40, frac_contact=0.1)
+    edge, _ = O.overlap_keys(A, B)
+    face = O.face_keys(A, B)
+    assert np.array_equal(edge, face)
+    assert len(edge) > 50
+
+
+@pytest.mark.parametrize("name", ["icospheres", "ellipsoid_contacts"])
+def test_golden_pair_sets_reproduce(name):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    A, B = mod.JOIN_CASES[name]()
+    g = np.load(GOLDEN / f"pairs_{name}.npz")
+    assert np.array_equal(O.overlap_keys(A, B)[0], g["overlap"])
+    assert np.array_equal(O.overlap_keys(A, B, mode=1)[0], g["overlap_fp32"])
+    assert np.array_equal(O.intersection_keys(A, B), g["intersection"])
+    assert np.array_equal(O.containment_keys(A, B), g["containment"])
+
+
+def test_direction_split_and_swap():
+    A, B = pg.icospheres(31, 100, 2, hi=30.0), pg.icospheres(32, 100, 2, hi=30.0)
+    both, _ = O.overlap_keys(A, B)
+    ab, _ = O.overlap_keys(A, B, direction=1)
+    ba, _ = O.overlap_keys(A, B, direction=2)
+    assert np.array_equal(both, np.union1d(ab, ba))
+    # swapping the datasets swaps every pair
+    rev, _ = O.overlap_keys(B, A)
+    swapped = np.sort((rev << np.uint64(32)) | (rev >> np.uint64(32)))
+    assert np.array_equal(both, swapped)
