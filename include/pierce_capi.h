@@ -129,6 +129,7 @@ typedef struct pierce_tuning {
     int32_t block_size;       /* threads per block for traversal kernels */
     int32_t sort_rays;        /* 1: trace edge rays in Morton order of their midpoints */
     int32_t cull_objects;     /* 1: skip source objects whose box meets no target object */
+    int32_t defer_build;      /* 1: pierce_dataset_create uploads only; call pierce_dataset_build */
 } pierce_tuning;
 
 typedef struct pierce_join_opts {
@@ -163,6 +164,10 @@ typedef struct pierce_stats {
     uint64_t containment_pairs;   /* containment: strict containment pairs */
     int32_t retries;              /* enlargements performed */
     int32_t launches;             /* kernels launched by the join */
+    double ms_count_pass[2];      /* two-pass: pass-1 (count) share of ms_edge_rays */
+    uint64_t raw_pairs[2];        /* raw pair emissions A->B, B->A (two-pass pass 1) */
+    uint64_t hash_accesses;       /* hash slot inspections */
+    uint64_t hash_contentions;    /* inspections past the first slot of a probe */
 } pierce_stats;
 
 typedef struct pierce_dataset_info {
@@ -188,6 +193,8 @@ void pierce_default_tuning(pierce_tuning* t);
 void pierce_default_join_opts(pierce_join_opts* o);
 /* Kernels launched by this context since its creation. */
 uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx);
+/* Free and total memory of the context's device (cudaMemGetInfo). */
+int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 
 /* ---- datasets ----------------------------------------------------------- */
 /* Copy a dataset to the device (from host or device memory) and build its

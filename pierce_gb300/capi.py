@@ -50,7 +50,8 @@ class MeshView(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("leaf_size", I32), ("block_size", I32), ("sort_rays", I32), ("cull_objects", I32)]
+    _fields_ = [("leaf_size", I32), ("block_size", I32), ("sort_rays", I32), ("cull_objects", I32),
+                ("defer_build", I32)]
 
 
 class JoinOpts(C.Structure):
@@ -65,7 +66,8 @@ class Stats(C.Structure):
                 ("fp32_ambiguous", U64), ("fp64_ambiguous", U64), ("parity_rays", U64),
                 ("hash_slots", U64), ("result_capacity", U64), ("num_pairs", U64),
                 ("overlap_pairs", U64), ("containment_pairs", U64), ("retries", I32),
-                ("launches", I32)]
+                ("launches", I32), ("ms_count_pass", D * 2), ("raw_pairs", U64 * 2),
+                ("hash_accesses", U64), ("hash_contentions", U64)]
 
     def as_dict(self) -> dict:
         out = {}
@@ -92,6 +94,7 @@ SIGNATURES = {
     "pierce_default_tuning": (None, [C.POINTER(Tuning)]),
     "pierce_default_join_opts": (None, [C.POINTER(JoinOpts)]),
     "pierce_ctx_kernel_launches": (U64, [V]),
+    "pierce_device_memory": (C.c_int, [V, C.POINTER(U64), C.POINTER(U64)]),
     "pierce_dataset_create": (C.c_int, [V, C.POINTER(MeshView), C.c_int, C.POINTER(Tuning), C.POINTER(V)]),
     "pierce_dataset_build": (C.c_int, [V, V, C.POINTER(Tuning)]),
     "pierce_dataset_info_get": (C.c_int, [V, C.POINTER(DatasetInfo)]),

@@ -195,6 +195,7 @@ void pierce_default_tuning(pierce_tuning* t) {
     t->block_size = 128;
     t->sort_rays = 0;
     t->cull_objects = 0;
+    t->defer_build = 0;
 }
 
 void pierce_default_join_opts(pierce_join_opts* o) {
@@ -264,6 +265,16 @@ int pierce_ctx_synchronize(pierce_ctx* ctx) {
 void* pierce_ctx_stream(pierce_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes) {
+    if (!ctx || !free_bytes || !total_bytes) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "device_memory: null");
+    cudaSetDevice(ctx->device);
+    size_t f = 0, t = 0;
+    if (int s = check_cuda(cudaMemGetInfo(&f, &t), "cudaMemGetInfo")) return s;
+    *free_bytes = f;
+    *total_bytes = t;
+    return PIERCE_OK;
+}
 
 // ---- datasets ---------------------------------------------------------------
 
@@ -360,7 +371,11 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
         pierce_tuning t;
         pierce_default_tuning(&t);
         if (tuning) t = *tuning;
-        if ((s = build_bvh(ctx, ds, t.leaf_size))) break;
+        if (t.defer_build) {
+            if ((s = sync_ctx(ctx, "dataset upload"))) break;
+        } else if ((s = build_bvh(ctx, ds, t.leaf_size))) {
+            break;
+        }
     } while (0);
     if (s) {
         pierce_dataset_destroy(ds);
@@ -536,7 +551,14 @@ struct Join {
         if (int s = scratch(ctx, SLOT_BUILD_B, obytes, &po)) return s;
         int32_t* counts = static_cast<int32_t*>(pc);
         int64_t* offs = static_cast<int64_t*>(po);
+        const size_t span0 = timer.spans.size();
         if (int s = edge_rays(0, counts, counts + na, nullptr, nullptr, nullptr, 0, nullptr, 0)) return s;
+        // the pass-1 (count) spans also feed ms_count_pass
+        const size_t span1 = timer.spans.size();
+        for (size_t i = span0; i < span1; ++i) {
+            double* target = timer.targets[i] == &st.ms_edge_rays[0] ? &st.ms_count_pass[0] : &st.ms_count_pass[1];
+            timer.span(timer.spans[i].first, timer.spans[i].second, target);
+        }
         const int64_t n_all = (int64_t)(na + nb);
         int tb = timer.record();
         if (n_all > 0)
@@ -547,11 +569,15 @@ struct Join {
         if (n_all > 0) {
             cudaMemcpyAsync(ctx->h_small, offs + n_all - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
             cudaMemcpyAsync(ctx->h_small + 1, counts + n_all - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
+            if (na > 0 && nb > 0) cudaMemcpyAsync(ctx->h_small + 2, offs + na, 8, cudaMemcpyDeviceToHost, ctx->stream);
         }
         uint32_t bits = 0;
         if (int s = read_device_error(ctx, &bits)) return s;
         if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
         if (n_all > 0) total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
+        const int64_t total_ab = (na > 0 && nb > 0) ? ctx->h_small[2] : (na > 0 ? total : 0);
+        st.raw_pairs[0] = (uint64_t)total_ab;
+        st.raw_pairs[1] = (uint64_t)(total - total_ab);
         // raw keys then sorted keys
         void* praw = nullptr;
         if (int s = scratch(ctx, SLOT_TABLE, 8 * (size_t)std::max<int64_t>(total, 1), &praw)) return s;
@@ -671,6 +697,8 @@ struct Join {
         st.fp32_ambiguous = c.fp32_ambiguous;
         st.fp64_ambiguous = c.fp64_ambiguous;
         st.parity_rays = c.parity_rays;
+        st.hash_accesses = c.hash_accesses;
+        st.hash_contentions = c.hash_contentions;
         st.num_pairs = (*out)->count;
         return PIERCE_OK;
     }

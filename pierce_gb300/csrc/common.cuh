@@ -31,6 +31,8 @@ struct DevCounters {
     unsigned long long fp32_ambiguous;
     unsigned long long fp64_ambiguous;
     unsigned long long parity_rays;
+    unsigned long long hash_accesses;
+    unsigned long long hash_contentions;
     unsigned long long pad;
 };
 

@@ -53,9 +53,12 @@ __device__ __forceinline__ uint64_t pack_key(int32_t a, int32_t b) {
 }
 
 // Insert; returns slot index or -1 when the probe bound is exhausted.
-__device__ __forceinline__ int64_t hash_insert(uint64_t* table, uint64_t mask, uint64_t key, uint32_t* err) {
+// `probes` accumulates the slots inspected (for contention statistics).
+__device__ __forceinline__ int64_t hash_insert(uint64_t* table, uint64_t mask, uint64_t key, uint32_t* err,
+                                               uint32_t& probes) {
     uint64_t h = fmix64(key) & mask;
     for (uint64_t i = 0; i <= mask; ++i) {
+        ++probes;
         const uint64_t cur = __ldcg(table + h);
         if (cur == key) return (int64_t)h;
         if (cur == kEmptyKey) {
@@ -120,7 +123,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     __shared__ int sstack[kShortStack][128];
     int lstack[kStackSize - kShortStack];
     const int tid = threadIdx.x;
-    uint32_t n_nodes = 0, n_tests = 0, n_hits = 0;
+    uint32_t n_nodes = 0, n_tests = 0, n_hits = 0, n_inserts = 0, n_probes = 0;
     PredCounters pc{0, 0};
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
     const bool active = e < P.src.num_edges;
@@ -157,8 +160,12 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
                 ++nhit;
                 if (MODE == MODE_COUNT) continue;
                 const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
-                if (MODE == MODE_WRITE) P.keys[out++] = key;
-                else hash_insert(P.table, P.mask, key, P.err);
+                if (MODE == MODE_WRITE) {
+                    P.keys[out++] = key;
+                } else {
+                    ++n_inserts;
+                    hash_insert(P.table, P.mask, key, P.err, n_probes);
+                }
             }
         };
         if (P.tgt.root_is_leaf) {
@@ -210,6 +217,10 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     flush_counter(&P.ctr->raw_hits, n_hits);
     flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
     flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+    if (MODE == MODE_HASH) {
+        flush_counter(&P.ctr->hash_accesses, n_probes);
+        flush_counter(&P.ctr->hash_contentions, n_probes - n_inserts);
+    }
 }
 
 struct ParityParams {
@@ -252,7 +263,8 @@ __global__ void __launch_bounds__(128) k_parity(ParityParams P) {
                 ++n_cross;
                 const int32_t obj = __float_as_int(a4.w);
                 const uint64_t key = P.swap ? pack_key(obj, (int32_t)o) : pack_key((int32_t)o, obj);
-                const int64_t slot = hash_insert(P.table, P.mask, key, P.err);
+                uint32_t probes = 0;
+                const int64_t slot = hash_insert(P.table, P.mask, key, P.err, probes);
                 if (slot >= 0) P.parity[slot] ^= 1u;  // keys of one source are owned by one thread
             }
         };
@@ -322,7 +334,8 @@ __global__ void k_parity_emit(const uint64_t* __restrict__ ptable, const uint32_
             if (in) continue;
         }
         if (out_table) {
-            hash_insert(out_table, out_mask, key, err);
+            uint32_t probes = 0;
+            hash_insert(out_table, out_mask, key, err, probes);
         } else {
             const unsigned long long pos = atomicAdd(out_count, 1ull);
             if (pos < out_cap) out_keys[pos] = key;
