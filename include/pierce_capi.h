@@ -143,6 +143,10 @@ typedef struct pierce_join_opts {
     double output_safety;         /* result capacity = expected * safety (>= 1) */
     int32_t include_overlap_pairs;/* containment: also report overlap pairs */
     int32_t max_retries;          /* table/output enlargements before failing */
+    int32_t cull_objects;         /* 1 (default): skip edges of source objects whose box meets no target triangle box */
+    int32_t defer_exact;          /* 1 (default): queue FP32-undecided tests for a separate exact pass */
+    int32_t active_bvh;           /* 1 (default): build per-join BVHs over the triangles of objects whose box
+                                     meets an object box of the other side (datasets need no BVH of their own) */
 } pierce_join_opts;
 
 typedef struct pierce_stats {
@@ -168,6 +172,8 @@ typedef struct pierce_stats {
     uint64_t raw_pairs[2];        /* raw pair emissions A->B, B->A (two-pass pass 1) */
     uint64_t hash_accesses;       /* hash slot inspections */
     uint64_t hash_contentions;    /* inspections past the first slot of a probe */
+    double ms_build;              /* per-join BVH builds (active_bvh) */
+    uint64_t active_triangles[2]; /* triangles in the per-join BVHs of A and B */
 } pierce_stats;
 
 typedef struct pierce_dataset_info {

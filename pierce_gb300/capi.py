@@ -57,7 +57,8 @@ class Tuning(C.Structure):
 class JoinOpts(C.Structure):
     _fields_ = [("predicate", I32), ("direction", I32), ("sizing", I32), ("precision", I32),
                 ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
-                ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32)]
+                ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
+                ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32)]
 
 
 class Stats(C.Structure):
@@ -67,7 +68,8 @@ class Stats(C.Structure):
                 ("hash_slots", U64), ("result_capacity", U64), ("num_pairs", U64),
                 ("overlap_pairs", U64), ("containment_pairs", U64), ("retries", I32),
                 ("launches", I32), ("ms_count_pass", D * 2), ("raw_pairs", U64 * 2),
-                ("hash_accesses", U64), ("hash_contentions", U64)]
+                ("hash_accesses", U64), ("hash_contentions", U64), ("ms_build", D),
+                ("active_triangles", U64 * 2)]
 
     def as_dict(self) -> dict:
         out = {}

@@ -14,10 +14,21 @@
 
 namespace pgpu {
 // join.cu
-int launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode, int precision,
+int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int mode, int precision,
                      int swap, int32_t* counts, const int64_t* offsets, uint64_t* keys, uint64_t* table,
-                     uint64_t slots);
-int launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int swap, uint64_t* table,
+                     uint64_t slots, const RayOpts* ro);
+int launch_resolve(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
+                   uint64_t slots, const RayOpts* ro, uint64_t* keys_out, unsigned long long* keys_count,
+                   uint64_t keys_cap);
+int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, uint8_t* active, uint32_t* list,
+                unsigned long long* count);
+int launch_object_active(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, uint8_t* active);
+int launch_collect_rays(pierce_ctx* ctx, const DevDataset& src, const uint8_t* active, uint32_t* list,
+                        unsigned long long* count);
+int launch_collect_tris(pierce_ctx* ctx, const int32_t* t2o, int64_t nt, const uint8_t* active, uint32_t* list,
+                        unsigned long long* count);
+int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
+int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots);
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
                   unsigned long long* d_count);
@@ -49,6 +60,19 @@ enum : int {
     SLOT_TABLE = 5,
     SLOT_KEYS = 6,
     SLOT_AUX = 7,
+    SLOT_LIST_AB = 8,    // culled ray list A->B
+    SLOT_LIST_BA = 9,    // culled ray list B->A
+    SLOT_CULL = 10,      // active flags + counters
+    SLOT_AMB = 11,       // deferred exact tests
+    SLOT_EXTRA = 12,     // exactly resolved keys (two-pass)
+    SLOT_RED_SOUP_A = 13,  // per-join BVH over active triangles of A
+    SLOT_RED_NODES_A = 14,
+    SLOT_RED_SOUP_B = 15,
+    SLOT_RED_NODES_B = 16,
+    SLOT_OBJ_A = 17,     // object pseudo-triangles of A (indices, ids) + their BVH
+    SLOT_OBJ_B = 18,
+    SLOT_TRIS_A = 19,    // active triangle lists
+    SLOT_TRIS_B = 20,
 };
 }  // namespace
 
@@ -211,6 +235,9 @@ void pierce_default_join_opts(pierce_join_opts* o) {
     o->output_safety = 1.2;
     o->include_overlap_pairs = 0;
     o->max_retries = 4;
+    o->cull_objects = 1;
+    o->defer_exact = 1;
+    o->active_bvh = 1;
 }
 
 int pierce_ctx_create(int device, pierce_ctx** out) {
@@ -246,7 +273,7 @@ void pierce_ctx_destroy(pierce_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < kScratchSlots; ++i)
         if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
@@ -459,20 +486,167 @@ struct Join {
         ba = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH2_TO_MESH1;
     }
 
-    int edge_rays(int mode, int32_t* counts_ab, int32_t* counts_ba, const int64_t* off_ab, const int64_t* off_ba,
-                  uint64_t* keys, int64_t keys_ba_base, uint64_t* table, uint64_t slots) {
-        if (ab) {
-            int b = timer.record();
-            if (int s = launch_edge_rays(ctx, A, B, mode, o.precision, 0, counts_ab, off_ab, keys, table, slots))
-                return s;
-            timer.span(b, timer.record(), &st.ms_edge_rays[0]);
+    // Per-join state of the tuned edge-ray path: culled ray lists per
+    // direction and the queue of deferred exact tests.
+    bool listed[2] = {false, false};
+    uint32_t* list[2] = {nullptr, nullptr};
+    uint8_t* active = nullptr;
+    // words: [0] list count A->B, [1] list count B->A, [2] warp cursor,
+    //        [3] deferred-test count, [4] exactly resolved key count,
+    //        [5] active triangles of A, [6] active triangles of B
+    unsigned long long* words = nullptr;
+    // device views of A and B the kernels traverse (their own BVH, or the
+    // per-join BVH over active triangles)
+    DevDataset va{}, vb{};
+    unsigned long long* amb_queue = nullptr;
+    uint64_t amb_cap = 0;
+    bool defer = true;
+
+    int prepare() {
+        defer = o.defer_exact != 0;
+        va = A->view();
+        vb = B->view();
+        void* p = nullptr;
+        const size_t nobj_a = (size_t)std::max(A->num_objects, 1), nobj_b = (size_t)std::max(B->num_objects, 1);
+        if (int s = scratch(ctx, SLOT_CULL, 128 + nobj_a + nobj_b, &p)) return s;
+        words = static_cast<unsigned long long*>(p);
+        active = static_cast<uint8_t*>(p) + 128;
+        if (o.cull_objects || o.active_bvh) {
+            if (int s = scratch(ctx, SLOT_LIST_AB, 4 * std::max<uint64_t>(A->ne, 1), &p)) return s;
+            list[0] = static_cast<uint32_t*>(p);
+            if (int s = scratch(ctx, SLOT_LIST_BA, 4 * std::max<uint64_t>(B->ne, 1), &p)) return s;
+            list[1] = static_cast<uint32_t*>(p);
         }
-        if (ba) {
-            int b = timer.record();
-            if (int s = launch_edge_rays(ctx, B, A, mode, o.precision, 1, counts_ba, off_ba,
-                                         keys ? keys + keys_ba_base : nullptr, table, slots))
+        amb_cap = std::min<uint64_t>(std::max<uint64_t>(A->ne + B->ne, 1024), 1ull << 24);
+        if (int s = scratch(ctx, SLOT_AMB, 8 * amb_cap, &p)) return s;
+        amb_queue = static_cast<unsigned long long*>(p);
+        if (o.active_bvh) return prepare_active_bvh();
+        return PIERCE_OK;
+    }
+
+    // BVH of one dataset's object boxes (degenerate triangles lo, hi, hi).
+    int object_bvh(pierce_dataset* ds, int slot, DevDataset* out) {
+        const int64_t n = ds->num_objects;
+        void* p = nullptr;
+        const size_t bytes = 16 * (size_t)std::max<int64_t>(n, 1) + (48 + 64) * (size_t)std::max<int64_t>(n, 1) + 256;
+        if (int s = scratch(ctx, slot, bytes, &p)) return s;
+        uint32_t* idx = static_cast<uint32_t*>(p);
+        int32_t* t2o = reinterpret_cast<int32_t*>(idx + 3 * std::max<int64_t>(n, 1));
+        char* q = reinterpret_cast<char*>(t2o + std::max<int64_t>(n, 1));
+        q += (256 - ((uintptr_t)q & 255)) & 255;
+        float4* soup = reinterpret_cast<float4*>(q);
+        Node* nodes = reinterpret_cast<Node*>(soup + 3 * std::max<int64_t>(n, 1));
+        if (int s = launch_object_pseudo_tris(ctx, (int32_t)n, idx, t2o)) return s;
+        BvhShape shape;
+        if (int s = build_lbvh(ctx, ds->d_obj_box, idx, t2o, nullptr, n, 1, soup, nodes, &shape, nullptr)) return s;
+        *out = DevDataset{};
+        out->soup = soup;
+        out->nodes = nodes;
+        out->num_tris = n;
+        out->root_is_leaf = shape.root_is_leaf;
+        out->root_leaf_count = shape.root_leaf_count;
+        return PIERCE_OK;
+    }
+
+    // Per-join BVHs over the triangles of objects whose box meets an object
+    // box of the other side.  Exact: a segment lies in its object's box, and
+    // a first vertex with odd parity lies inside the target object's box, so
+    // no pair involves a triangle left out.
+    int prepare_active_bvh() {
+        const int b0 = timer.record();
+        DevDataset objA, objB;
+        if (int s = object_bvh(A, SLOT_OBJ_A, &objA)) return s;
+        if (int s = object_bvh(B, SLOT_OBJ_B, &objB)) return s;
+        uint8_t* act_a = active;
+        uint8_t* act_b = active + std::max(A->num_objects, 1);
+        if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
+        if (int s = launch_object_active(ctx, vb, objA, act_b)) return s;
+        void *ta = nullptr, *tb = nullptr;
+        if (int s = scratch(ctx, SLOT_TRIS_A, 4 * std::max<uint64_t>(A->nt, 1), &ta)) return s;
+        if (int s = scratch(ctx, SLOT_TRIS_B, 4 * std::max<uint64_t>(B->nt, 1), &tb)) return s;
+        if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
+            return s;
+        if (int s = launch_collect_tris(ctx, B->d_tri_to_object, (int64_t)B->nt, act_b, (uint32_t*)tb, words + 6))
+            return s;
+        if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
+        if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
+        listed[0] = listed[1] = true;
+        cudaMemcpyAsync(ctx->h_small, words + 5, 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (int s = sync_ctx(ctx, "active triangle counts")) return s;
+        const int64_t na = ctx->h_small[0], nb = ctx->h_small[1];
+        void *sa = nullptr, *sb = nullptr, *na_p = nullptr, *nb_p = nullptr;
+        if (int s = scratch(ctx, SLOT_RED_SOUP_A, 48 * (size_t)std::max<int64_t>(na, 1), &sa)) return s;
+        if (int s = scratch(ctx, SLOT_RED_NODES_A, 64 * (size_t)std::max<int64_t>(na, 1), &na_p)) return s;
+        if (int s = scratch(ctx, SLOT_RED_SOUP_B, 48 * (size_t)std::max<int64_t>(nb, 1), &sb)) return s;
+        if (int s = scratch(ctx, SLOT_RED_NODES_B, 64 * (size_t)std::max<int64_t>(nb, 1), &nb_p)) return s;
+        BvhShape shA, shB;
+        if (int s = build_lbvh(ctx, A->d_vertices, A->d_indices, A->d_tri_to_object, (const uint32_t*)ta, na,
+                               A->leaf_size, (float4*)sa, (Node*)na_p, &shA, nullptr))
+            return s;
+        if (int s = build_lbvh(ctx, B->d_vertices, B->d_indices, B->d_tri_to_object, (const uint32_t*)tb, nb,
+                               B->leaf_size, (float4*)sb, (Node*)nb_p, &shB, nullptr))
+            return s;
+        va.soup = (const float4*)sa;
+        va.nodes = (const Node*)na_p;
+        va.num_tris = na;
+        va.root_is_leaf = shA.root_is_leaf;
+        va.root_leaf_count = shA.root_leaf_count;
+        vb.soup = (const float4*)sb;
+        vb.nodes = (const Node*)nb_p;
+        vb.num_tris = nb;
+        vb.root_is_leaf = shB.root_is_leaf;
+        vb.root_leaf_count = shB.root_leaf_count;
+        st.active_triangles[0] = (uint64_t)na;
+        st.active_triangles[1] = (uint64_t)nb;
+        timer.span(b0, timer.record(), &st.ms_build);
+        return PIERCE_OK;
+    }
+
+    int precision_mode() const {
+        if (o.precision == PIERCE_FP32) return 1;  // plain float32
+        return defer ? 2 : 0;                      // deferred or inline exact
+    }
+
+    // Edge rays of the enabled directions.  COUNT and HASH queue undecided
+    // tests and resolve them right away: into the table (HASH) or into
+    // extra_keys (COUNT); WRITE skips them (already resolved by COUNT).
+    int edge_rays(int mode, int32_t* counts_ab, int32_t* counts_ba, const int64_t* off_ab, const int64_t* off_ba,
+                  uint64_t* keys, uint64_t* table, uint64_t slots, uint64_t* extra_keys = nullptr,
+                  uint64_t extra_cap = 0) {
+        const bool dirs[2] = {ab, ba};
+        for (int d = 0; d < 2; ++d) {
+            if (!dirs[d]) continue;
+            const DevDataset& src = d ? vb : va;
+            const DevDataset& tgt = d ? va : vb;
+            int32_t* counts = d ? counts_ba : counts_ab;
+            const int64_t* offs = d ? off_ba : off_ab;
+            const int b = timer.record();
+            RayOpts ro;
+            if ((o.cull_objects || o.active_bvh) && src.num_edges > 0) {
+                if (!listed[d]) {
+                    if (int s = launch_cull(ctx, src, tgt, active, list[d], words + d)) return s;
+                    listed[d] = true;
+                }
+                ro.list = list[d];
+                ro.count = words + d;
+                ro.cursor = words + 2;
+                if (mode == 0) cudaMemsetAsync(counts, 0, 4 * (size_t)src.num_edges, ctx->stream);
+            }
+            const int prec = precision_mode();
+            if (prec == 2) {
+                ro.amb_queue = amb_queue;
+                ro.amb_count = words + 3;
+                ro.amb_cap = amb_cap;
+                if (mode != 1) cudaMemsetAsync(words + 3, 0, 8, ctx->stream);
+            }
+            if (int s = launch_edge_rays(ctx, src, tgt, mode, prec, d, counts, offs, keys, table, slots,
+                                         (ro.list || ro.amb_queue) ? &ro : nullptr))
                 return s;
-            timer.span(b, timer.record(), &st.ms_edge_rays[1]);
+            if (prec == 2 && mode != 1)
+                if (int s = launch_resolve(ctx, src, tgt, d, mode == 2 ? table : nullptr, slots, &ro, extra_keys,
+                                           words + 4, extra_cap))
+                    return s;
+            timer.span(b, timer.record(), &st.ms_edge_rays[d]);
         }
         return PIERCE_OK;
     }
@@ -492,10 +666,14 @@ struct Join {
             if (int s = scratch(ctx, SLOT_TABLE, slots * 8, &p)) return s;
             uint64_t* table = static_cast<uint64_t*>(p);
             cudaMemsetAsync(table, 0xFF, slots * 8, ctx->stream);
-            if (int s = edge_rays(2, nullptr, nullptr, nullptr, nullptr, nullptr, 0, table, slots)) return s;
+            if (int s = edge_rays(2, nullptr, nullptr, nullptr, nullptr, nullptr, table, slots)) return s;
             uint32_t bits = 0;
             if (int s = read_device_error(ctx, &bits)) return s;
             if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+            if (bits & ERR_AMBIGUOUS_OVERFLOW) {
+                defer = false;  // too many undecided tests to queue: resolve them inline
+                continue;
+            }
             if (bits & ERR_HASH_FULL) {
                 if (attempt >= o.max_retries)
                     return set_error(PIERCE_ERR_HASH_FULL, "pair hash table full after retries");
@@ -551,50 +729,70 @@ struct Join {
         if (int s = scratch(ctx, SLOT_BUILD_B, obytes, &po)) return s;
         int32_t* counts = static_cast<int32_t*>(pc);
         int64_t* offs = static_cast<int64_t*>(po);
-        const size_t span0 = timer.spans.size();
-        if (int s = edge_rays(0, counts, counts + na, nullptr, nullptr, nullptr, 0, nullptr, 0)) return s;
-        // the pass-1 (count) spans also feed ms_count_pass
-        const size_t span1 = timer.spans.size();
-        for (size_t i = span0; i < span1; ++i) {
-            double* target = timer.targets[i] == &st.ms_edge_rays[0] ? &st.ms_count_pass[0] : &st.ms_count_pass[1];
-            timer.span(timer.spans[i].first, timer.spans[i].second, target);
-        }
+        void* pe = nullptr;
+        if (int s = scratch(ctx, SLOT_EXTRA, 8 * amb_cap, &pe)) return s;
+        uint64_t* extra = static_cast<uint64_t*>(pe);
         const int64_t n_all = (int64_t)(na + nb);
-        int tb = timer.record();
-        if (n_all > 0)
-            if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all)) return s;
-        timer.span(tb, timer.record(), &st.ms_dedup);
-        // total = last offset + last count; B->A offsets are shifted by the A total
-        int64_t total = 0;
-        if (n_all > 0) {
-            cudaMemcpyAsync(ctx->h_small, offs + n_all - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
-            cudaMemcpyAsync(ctx->h_small + 1, counts + n_all - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
-            if (na > 0 && nb > 0) cudaMemcpyAsync(ctx->h_small + 2, offs + na, 8, cudaMemcpyDeviceToHost, ctx->stream);
+        int64_t total = 0, total_ab = 0;
+        uint64_t n_extra = 0;
+        for (;;) {
+            cudaMemsetAsync(words + 4, 0, 8, ctx->stream);
+            const size_t span0 = timer.spans.size();
+            if (int s = edge_rays(0, counts, counts + na, nullptr, nullptr, nullptr, nullptr, 0, extra, amb_cap))
+                return s;
+            // the pass-1 (count) spans also feed ms_count_pass
+            const size_t span1 = timer.spans.size();
+            for (size_t i = span0; i < span1; ++i) {
+                double* target = timer.targets[i] == &st.ms_edge_rays[0] ? &st.ms_count_pass[0] : &st.ms_count_pass[1];
+                timer.span(timer.spans[i].first, timer.spans[i].second, target);
+            }
+            int tb = timer.record();
+            if (n_all > 0)
+                if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all)) return s;
+            timer.span(tb, timer.record(), &st.ms_dedup);
+            // total = last offset + last count; B->A offsets continue after the A total
+            if (n_all > 0) {
+                cudaMemcpyAsync(ctx->h_small, offs + n_all - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
+                cudaMemcpyAsync(ctx->h_small + 1, counts + n_all - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
+                if (na > 0 && nb > 0)
+                    cudaMemcpyAsync(ctx->h_small + 2, offs + na, 8, cudaMemcpyDeviceToHost, ctx->stream);
+            }
+            cudaMemcpyAsync(ctx->h_small + 3, words + 4, 8, cudaMemcpyDeviceToHost, ctx->stream);
+            uint32_t bits = 0;
+            if (int s = read_device_error(ctx, &bits)) return s;
+            if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+            if (bits & (ERR_AMBIGUOUS_OVERFLOW | ERR_OUTPUT_OVERFLOW)) {
+                if (!defer) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "resolved-test output overflow");
+                defer = false;
+                continue;
+            }
+            total = 0;
+            if (n_all > 0) total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
+            total_ab = (na > 0 && nb > 0) ? ctx->h_small[2] : (na > 0 ? total : 0);
+            n_extra = (uint64_t)ctx->h_small[3];
+            break;
         }
-        uint32_t bits = 0;
-        if (int s = read_device_error(ctx, &bits)) return s;
-        if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
-        if (n_all > 0) total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
-        const int64_t total_ab = (na > 0 && nb > 0) ? ctx->h_small[2] : (na > 0 ? total : 0);
         st.raw_pairs[0] = (uint64_t)total_ab;
         st.raw_pairs[1] = (uint64_t)(total - total_ab);
+        const int64_t n_raw = total + (int64_t)n_extra;
         // raw keys then sorted keys
         void* praw = nullptr;
-        if (int s = scratch(ctx, SLOT_TABLE, 8 * (size_t)std::max<int64_t>(total, 1), &praw)) return s;
+        if (int s = scratch(ctx, SLOT_TABLE, 8 * (size_t)std::max<int64_t>(n_raw, 1), &praw)) return s;
         uint64_t* raw = static_cast<uint64_t*>(praw);
-        if (int s = edge_rays(1, nullptr, nullptr, offs, offs + na, raw, 0, nullptr, 0)) return s;
+        if (int s = edge_rays(1, nullptr, nullptr, offs, offs + na, raw, nullptr, 0)) return s;
+        if (n_extra) cudaMemcpyAsync(raw + total, extra, 8 * n_extra, cudaMemcpyDeviceToDevice, ctx->stream);
         void* pk = nullptr;
-        if (int s = scratch(ctx, SLOT_KEYS, 8 * (size_t)std::max<int64_t>(total, 1), &pk)) return s;
+        if (int s = scratch(ctx, SLOT_KEYS, 8 * (size_t)std::max<int64_t>(n_raw, 1), &pk)) return s;
         uint64_t* sorted = static_cast<uint64_t*>(pk);
-        tb = timer.record();
+        int tb = timer.record();
         int64_t nu = 0;
-        if (total > 0) {
-            if (int s = sort_u64_keys(ctx, raw, sorted, total)) return s;
-            if (int s = unique_u64(ctx, sorted, raw, total, &nu)) return s;
+        if (n_raw > 0) {
+            if (int s = sort_u64_keys(ctx, raw, sorted, n_raw)) return s;
+            if (int s = unique_u64(ctx, sorted, raw, n_raw, &nu)) return s;
             cudaMemcpyAsync(sorted, raw, 8 * (size_t)nu, cudaMemcpyDeviceToDevice, ctx->stream);
         }
         timer.span(tb, timer.record(), &st.ms_dedup);
-        st.result_capacity = (uint64_t)total;
+        st.result_capacity = (uint64_t)n_raw;
         *keys_out = sorted;
         *n_out = (uint64_t)nu;
         return PIERCE_OK;
@@ -602,10 +800,10 @@ struct Join {
 
     // Parity of src first vertices against tgt into the parity table, then
     // emit odd keys (mode 0: into out_table, mode 1: filtered append).
-    int parity(pierce_dataset* src, pierce_dataset* tgt, int swap, double* ms, int emit_mode, uint64_t* out_table,
+    int parity(const DevDataset& src, const DevDataset& tgt, int swap, double* ms, int emit_mode, uint64_t* out_table,
                uint64_t out_slots, const uint64_t* lookup_table, uint64_t lookup_slots, const uint64_t* lookup_sorted,
                int64_t lookup_n, uint64_t* out_keys, unsigned long long* out_count, uint64_t out_cap) {
-        uint64_t pslots = table_slots_for(8 * (uint64_t)std::max(src->num_objects, 1), 0.5);
+        uint64_t pslots = table_slots_for(8 * (uint64_t)std::max(src.num_objects, 1), 0.5);
         for (int attempt = 0;; ++attempt) {
             void* p = nullptr;
             if (int s = scratch(ctx, SLOT_BUILD_C, pslots * 12, &p)) return s;
@@ -679,7 +877,8 @@ struct Join {
         cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
         cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
         const int t0 = timer.record();
-        int s = PIERCE_OK;
+        int s = prepare();
+        if (s) return s;
         if (o.predicate == PIERCE_OVERLAP) s = run_overlap(out);
         else if (o.predicate == PIERCE_INTERSECTION) s = run_intersection(out);
         else s = run_containment(out);
@@ -738,11 +937,11 @@ struct Join {
             cudaMemsetAsync(d_count, 0, 8, ctx->stream);
             const uint64_t cap = 8 * extra + 16;
             if (ab)
-                if (int s = parity(A, B, 0, &st.ms_parity[0], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
+                if (int s = parity(va, vb, 0, &st.ms_parity[0], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
                                    d_count, cap))
                     return s;
             if (ba)
-                if (int s = parity(B, A, 1, &st.ms_parity[1], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
+                if (int s = parity(vb, va, 1, &st.ms_parity[1], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
                                    d_count, cap))
                     return s;
             cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
@@ -755,10 +954,10 @@ struct Join {
         uint64_t slots = 0, n = 0;
         if (int s = overlap_hash(&table, &slots)) return s;
         if (ab)
-            if (int s = parity(A, B, 0, &st.ms_parity[0], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
+            if (int s = parity(va, vb, 0, &st.ms_parity[0], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
                 return s;
         if (ba)
-            if (int s = parity(B, A, 1, &st.ms_parity[1], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
+            if (int s = parity(vb, va, 1, &st.ms_parity[1], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
                 return s;
         uint32_t bits = 0;
         if (int s = read_device_error(ctx, &bits)) return s;
@@ -796,7 +995,7 @@ struct Join {
         if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
         unsigned long long* d_count = static_cast<unsigned long long*>(pc);
         cudaMemsetAsync(d_count, 0, 8, ctx->stream);
-        if (int s = parity(B, A, 1, &st.ms_parity[1], 1, nullptr, 0, table, slots, okeys, (int64_t)n_over, ckeys,
+        if (int s = parity(vb, va, 1, &st.ms_parity[1], 1, nullptr, 0, table, slots, okeys, (int64_t)n_over, ckeys,
                            d_count, cap))
             return s;
         cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
@@ -854,7 +1053,8 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
                 pierce_result** out, pierce_stats* stats) {
     if (!ctx || !a || !b || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: null argument");
     *out = nullptr;
-    if (!a->built || !b->built) return set_error(PIERCE_ERR_NOT_BUILT, "join: dataset not built");
+    if ((!opts || !opts->active_bvh) && (!a->built || !b->built))
+        return set_error(PIERCE_ERR_NOT_BUILT, "join: dataset not built (or use active_bvh)");
     if (a->ctx != ctx || b->ctx != ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: dataset of other ctx");
     pierce_join_opts o;
     pierce_default_join_opts(&o);
@@ -885,8 +1085,8 @@ int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pi
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "HASH needs a power-of-two table");
     cudaSetDevice(ctx->device);
     cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
-    if (int s = launch_edge_rays(ctx, src, tgt, mode, precision, swap, d_counts, d_offsets, d_keys, d_table,
-                                 table_slots))
+    if (int s = launch_edge_rays(ctx, src->view(), tgt->view(), mode, precision, swap, d_counts, d_offsets, d_keys,
+                                 d_table, table_slots, nullptr))
         return s;
     uint32_t bits = 0;
     if (int s = read_device_error(ctx, &bits)) return s;
@@ -914,7 +1114,7 @@ int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierc
     if (!tgt->built) return set_error(PIERCE_ERR_NOT_BUILT, "launch_parity: target not built");
     cudaSetDevice(ctx->device);
     cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
-    if (int s = launch_parity(ctx, src, tgt, swap, d_table, d_parity, table_slots)) return s;
+    if (int s = launch_parity(ctx, src->view(), tgt->view(), swap, d_table, d_parity, table_slots)) return s;
     uint32_t bits = 0;
     if (int s = read_device_error(ctx, &bits)) return s;
     if (stats) {

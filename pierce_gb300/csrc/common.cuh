@@ -17,6 +17,7 @@ enum ErrBits : uint32_t {
     ERR_STACK_OVERFLOW = 2u,
     ERR_OUTPUT_OVERFLOW = 4u,
     ERR_QUEUE_TIMEOUT = 8u,
+    ERR_AMBIGUOUS_OVERFLOW = 16u,  // deferred-test queue full: rerun with inline exact tests
 };
 
 constexpr uint64_t kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
@@ -66,6 +67,26 @@ struct DevDataset {
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// Optional inputs of an edge-ray launch: a compacted ray list (object
+// culling) and the queue of deferred exact tests.
+struct RayOpts {
+    const uint32_t* list = nullptr;
+    const unsigned long long* count = nullptr;
+    unsigned long long* cursor = nullptr;
+    unsigned long long* amb_queue = nullptr;
+    unsigned long long* amb_count = nullptr;
+    uint64_t amb_cap = 0;
+};
+
+constexpr int kScratchSlots = 24;
+
+struct BvhShape {
+    int leaf_size = 1;
+    int root_is_leaf = 1;
+    int root_leaf_count = 0;
+    uint64_t num_nodes = 0;
+};
+
 }  // namespace pgpu
 
 // ---- host-side internal objects ------------------------------------------
@@ -79,8 +100,8 @@ struct pierce_ctx {
     pgpu::DevCounters* h_counters = nullptr;   // pinned
     int64_t* h_small = nullptr;                // pinned scratch for scalar readbacks (8 values)
     // grow-only scratch buffers reused across joins
-    void* scratch[8] = {nullptr};
-    size_t scratch_bytes[8] = {0};
+    void* scratch[pgpu::kScratchSlots] = {nullptr};
+    size_t scratch_bytes[pgpu::kScratchSlots] = {0};
     uint64_t launches = 0;
     int sm_count = 0;
 };
@@ -139,6 +160,8 @@ int device_alloc(void** p, size_t bytes, const char* what);
 
 // lbvh.cu
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);
+int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, const uint32_t* list,
+               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box);
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds);
 
 // sortscan.cu (CUB library calls)

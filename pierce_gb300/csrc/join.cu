@@ -35,7 +35,7 @@
 namespace pgpu {
 
 enum RayMode { MODE_COUNT = 0, MODE_WRITE = 1, MODE_HASH = 2 };
-enum Precision { PREC_EXACT = 0, PREC_FP32 = 1 };
+enum Precision { PREC_EXACT = 0, PREC_FP32 = 1, PREC_DEFER = 2 };
 
 constexpr int kShortStack = 32;  // stack entries kept in shared memory per thread
 
@@ -111,6 +111,14 @@ struct EdgeRayParams {
     uint64_t mask;
     uint32_t* err;
     DevCounters* ctr;
+    // optional compacted list of edges to trace (object culling)
+    const uint32_t* ray_list;
+    const unsigned long long* ray_count;
+    unsigned long long* ray_cursor;
+    // deferred exact tests: (edge << 32 | soup triangle) entries
+    unsigned long long* amb_queue;
+    unsigned long long* amb_count;
+    uint64_t amb_cap;
 };
 
 __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float hy, float lz, float hz,
@@ -118,64 +126,225 @@ __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float 
     return lx <= hi.x && lo.x <= hx && ly <= hi.y && lo.y <= hy && lz <= hi.z && lo.z <= hz;
 }
 
+struct RayCounters {
+    uint32_t nodes = 0, tests = 0, hits = 0, inserts = 0, probes = 0;
+};
+
+// One edge ray against the target BVH.  PREC_EXACT resolves every test
+// inline; PREC_DEFER classifies in float32 and queues undecided tests for
+// k_resolve_ambiguous (the WRITE pass skips them: they were queued by the
+// COUNT pass); PREC_FP32 is the plain Moller-Trumbore form.
+template <int MODE, int PREC>
+__device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int (*sstack)[128], int* lstack,
+                                           RayCounters& rc, PredCounters& pc) {
+    const int tid = threadIdx.x;
+    const float4 s4 = __ldg(P.src.edges + 2 * e);
+    const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
+    const int32_t src_obj = __float_as_int(s4.w);
+    const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
+    const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
+    const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
+    int64_t out = (MODE == MODE_WRITE) ? P.offsets[e] : 0;
+    int32_t last_obj = -1;
+    int nhit = 0;
+    auto leaf = [&](int first, int count) {
+        for (int k = 0; k < count; ++k) {
+            const int64_t t = (int64_t)first + k;
+            const float4 a4 = __ldg(P.tgt.soup + 3 * t);
+            const int32_t obj = __float_as_int(a4.w);
+            if (obj == last_obj) continue;
+            const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
+            const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
+            if (count > 1) {
+                const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
+                const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
+                const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
+                if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
+            }
+            ++rc.tests;
+            const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
+                         c = make_float3(c4.x, c4.y, c4.z);
+            bool hit;
+            if (PREC == PREC_EXACT) {
+                hit = seg_tri_exact(p, q, a, b, c, pc);
+            } else if (PREC == PREC_FP32) {
+                hit = seg_tri_mt_fp32(p, q, a, b, c);
+            } else {
+                const int cls = seg_tri_fp32_class(p, q, a, b, c);
+                if (cls == SEG_AMBIGUOUS) {
+                    ++pc.fp32_ambiguous;
+                    if (MODE != MODE_WRITE) {
+                        const unsigned long long slot = atomicAdd(P.amb_count, 1ull);
+                        if (slot < P.amb_cap) P.amb_queue[slot] = ((unsigned long long)e << 32) | (uint32_t)t;
+                        else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
+                    }
+                    continue;
+                }
+                hit = cls == SEG_HIT;
+            }
+            if (!hit) continue;
+            last_obj = obj;
+            ++nhit;
+            if (MODE == MODE_COUNT) continue;
+            const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
+            if (MODE == MODE_WRITE) {
+                P.keys[out++] = key;
+            } else {
+                ++rc.inserts;
+                hash_insert(P.table, P.mask, key, P.err, rc.probes);
+            }
+        }
+    };
+    if (P.tgt.root_is_leaf) {
+        if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+    } else {
+        int sp = 0;
+        int node = 0;
+        for (;;) {
+            ++rc.nodes;
+            const Node* nd = P.tgt.nodes + node;
+            const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+            const int4 ch = __ldg(&nd->ch);
+            bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
+            bool h1 = box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
+            if (h0 && ch.x < 0) {
+                leaf(~ch.x, ch.z);
+                h0 = false;
+            }
+            if (h1 && ch.y < 0) {
+                leaf(~ch.y, ch.w);
+                h1 = false;
+            }
+            if (h0 && h1) {
+                if (sp >= kStackSize) {
+                    atomicOr(P.err, ERR_STACK_OVERFLOW);
+                    break;
+                }
+                if (sp < kShortStack) sstack[sp][tid] = ch.y;
+                else lstack[sp - kShortStack] = ch.y;
+                ++sp;
+                node = ch.x;
+            } else if (h0) {
+                node = ch.x;
+            } else if (h1) {
+                node = ch.y;
+            } else {
+                if (sp == 0) break;
+                --sp;
+                node = sp < kShortStack ? sstack[sp][tid] : lstack[sp - kShortStack];
+            }
+        }
+    }
+    if (MODE == MODE_COUNT) P.counts[e] = nhit;
+    rc.hits += (uint32_t)nhit;
+}
+
 template <int MODE, int PREC>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     __shared__ int sstack[kShortStack][128];
     int lstack[kStackSize - kShortStack];
-    const int tid = threadIdx.x;
-    uint32_t n_nodes = 0, n_tests = 0, n_hits = 0, n_inserts = 0, n_probes = 0;
+    RayCounters rc;
     PredCounters pc{0, 0};
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
-    const bool active = e < P.src.num_edges;
-    if (active) {
-        const float4 s4 = __ldg(P.src.edges + 2 * e);
-        const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
-        const int32_t src_obj = __float_as_int(s4.w);
-        const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
-        const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
-        const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
-        int64_t out = (MODE == MODE_WRITE) ? P.offsets[e] : 0;
-        int32_t last_obj = -1;
-        int nhit = 0;
+    uint32_t rays = 0;
+    if (P.ray_list) {
+        // Compacted ray list, persistent blocks: each warp fetches the next 32
+        // rays from a global cursor, so uneven ray costs balance out.
+        const unsigned long long n = *P.ray_count;
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(P.ray_cursor, 32ull);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) break;
+            const unsigned long long i = base + lane;
+            if (i < n) {
+                trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc);
+                ++rays;
+            }
+        }
+    } else {
+        const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        if (e < P.src.num_edges) {
+            trace_edge<MODE, PREC>(P, e, sstack, lstack, rc, pc);
+            ++rays;
+        }
+    }
+    flush_counter(&P.ctr->rays, rays);
+    flush_counter(&P.ctr->node_visits, rc.nodes);
+    flush_counter(&P.ctr->tri_tests, rc.tests);
+    flush_counter(&P.ctr->raw_hits, rc.hits);
+    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+    if (MODE == MODE_HASH) {
+        flush_counter(&P.ctr->hash_accesses, rc.probes);
+        flush_counter(&P.ctr->hash_contentions, rc.probes - rc.inserts);
+    }
+}
+
+// Exact resolution of the queued (edge, triangle) tests.  Hits go to the
+// hash set (table != null) or are appended to keys_out.
+__global__ void __launch_bounds__(128) k_resolve_ambiguous(EdgeRayParams P, uint64_t* keys_out,
+                                                           unsigned long long* keys_count, uint64_t keys_cap) {
+    PredCounters pc{0, 0};
+    uint32_t probes = 0, inserts = 0;
+    const unsigned long long n = min(*P.amb_count, (unsigned long long)P.amb_cap);
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long ent = P.amb_queue[i];
+        const int64_t e = (int64_t)(ent >> 32), t = (int64_t)(ent & 0xFFFFFFFFull);
+        const float4 s4 = __ldg(P.src.edges + 2 * e), e4 = __ldg(P.src.edges + 2 * e + 1);
+        const float4 a4 = __ldg(P.tgt.soup + 3 * t), b4 = __ldg(P.tgt.soup + 3 * t + 1),
+                     c4 = __ldg(P.tgt.soup + 3 * t + 2);
+        if (!seg_tri_exact(make_float3(s4.x, s4.y, s4.z), make_float3(e4.x, e4.y, e4.z),
+                           make_float3(a4.x, a4.y, a4.z), make_float3(b4.x, b4.y, b4.z),
+                           make_float3(c4.x, c4.y, c4.z), pc))
+            continue;
+        const int32_t src_obj = __float_as_int(s4.w), obj = __float_as_int(a4.w);
+        const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
+        if (P.table) {
+            ++inserts;
+            hash_insert(P.table, P.mask, key, P.err, probes);
+        } else {
+            const unsigned long long pos = atomicAdd(keys_count, 1ull);
+            if (pos < keys_cap) keys_out[pos] = key;
+            else atomicOr(P.err, ERR_OUTPUT_OVERFLOW);
+        }
+    }
+    // fp32_ambiguous is counted by the tracing kernel; here only escalations to exact
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+    flush_counter(&P.ctr->hash_accesses, probes);
+    flush_counter(&P.ctr->hash_contentions, probes - inserts);
+}
+
+// Object culling: a source object is active when its box overlaps the box
+// of at least one target triangle (exact comparisons).  A segment's box lies
+// inside its object's box, so inactive objects' edges cannot hit anything.
+__global__ void __launch_bounds__(128) k_object_active(DevDataset src, DevDataset tgt, uint8_t* active) {
+    __shared__ int sstack[kShortStack][128];
+    int lstack[kStackSize - kShortStack];
+    const int tid = threadIdx.x;
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + tid;
+    if (o >= src.num_objects) return;
+    const float* b = src.obj_box + 6 * o;
+    const float3 lo = make_float3(b[0], b[1], b[2]), hi = make_float3(b[3], b[4], b[5]);
+    bool found = false;
+    if (lo.x <= hi.x && tgt.num_tris > 0) {
         auto leaf = [&](int first, int count) {
-            for (int k = 0; k < count; ++k) {
+            for (int k = 0; k < count && !found; ++k) {
                 const int64_t t = (int64_t)first + k;
-                const float4 a4 = __ldg(P.tgt.soup + 3 * t);
-                const int32_t obj = __float_as_int(a4.w);
-                if (obj == last_obj) continue;
-                const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
-                const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
-                if (count > 1) {
-                    const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
-                    const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
-                    const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
-                    if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
-                }
-                ++n_tests;
-                const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
-                             c = make_float3(c4.x, c4.y, c4.z);
-                const bool hit = (PREC == PREC_EXACT) ? seg_tri_exact(p, q, a, b, c, pc) : seg_tri_mt_fp32(p, q, a, b, c);
-                if (!hit) continue;
-                last_obj = obj;
-                ++nhit;
-                if (MODE == MODE_COUNT) continue;
-                const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
-                if (MODE == MODE_WRITE) {
-                    P.keys[out++] = key;
-                } else {
-                    ++n_inserts;
-                    hash_insert(P.table, P.mask, key, P.err, n_probes);
-                }
+                const float4 a4 = __ldg(tgt.soup + 3 * t), b4 = __ldg(tgt.soup + 3 * t + 1),
+                             c4 = __ldg(tgt.soup + 3 * t + 2);
+                found = box_overlap(fminf(a4.x, fminf(b4.x, c4.x)), fmaxf(a4.x, fmaxf(b4.x, c4.x)),
+                                    fminf(a4.y, fminf(b4.y, c4.y)), fmaxf(a4.y, fmaxf(b4.y, c4.y)),
+                                    fminf(a4.z, fminf(b4.z, c4.z)), fmaxf(a4.z, fmaxf(b4.z, c4.z)), lo, hi);
             }
         };
-        if (P.tgt.root_is_leaf) {
-            if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+        if (tgt.root_is_leaf) {
+            leaf(0, tgt.root_leaf_count);
         } else {
-            int sp = 0;
-            int node = 0;
-            for (;;) {
-                ++n_nodes;
-                const Node* nd = P.tgt.nodes + node;
+            int sp = 0, node = 0;
+            while (!found) {
+                const Node* nd = tgt.nodes + node;
                 const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
                 const int4 ch = __ldg(&nd->ch);
                 bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
@@ -184,13 +353,14 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
                     leaf(~ch.x, ch.z);
                     h0 = false;
                 }
-                if (h1 && ch.y < 0) {
+                if (!found && h1 && ch.y < 0) {
                     leaf(~ch.y, ch.w);
                     h1 = false;
                 }
+                if (found) break;
                 if (h0 && h1) {
-                    if (sp >= kStackSize) {
-                        atomicOr(P.err, ERR_STACK_OVERFLOW);
+                    if (sp >= kStackSize) {  // cannot happen for an LBVH; be conservative
+                        found = true;
                         break;
                     }
                     if (sp < kShortStack) sstack[sp][tid] = ch.y;
@@ -208,18 +378,25 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
                 }
             }
         }
-        if (MODE == MODE_COUNT) P.counts[e] = nhit;
-        n_hits = (uint32_t)nhit;
     }
-    flush_counter(&P.ctr->rays, active ? 1ull : 0ull);
-    flush_counter(&P.ctr->node_visits, n_nodes);
-    flush_counter(&P.ctr->tri_tests, n_tests);
-    flush_counter(&P.ctr->raw_hits, n_hits);
-    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
-    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
-    if (MODE == MODE_HASH) {
-        flush_counter(&P.ctr->hash_accesses, n_probes);
-        flush_counter(&P.ctr->hash_contentions, n_probes - n_inserts);
+    active[o] = found ? 1 : 0;
+}
+
+// Edges of active objects -> compacted list (warp-aggregated cursor).
+__global__ void k_collect_rays(const float4* __restrict__ edges, int64_t n, const uint8_t* __restrict__ active,
+                               uint32_t* __restrict__ list, unsigned long long* count) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
+        const int64_t e = base + threadIdx.x;
+        bool keep = false;
+        if (e < n) keep = active[__float_as_int(__ldg(&edges[2 * e].w))] != 0;
+        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
+        if (!ballot) continue;
+        const int lane = threadIdx.x & 31;
+        unsigned long long wbase = 0;
+        if (lane == 0) wbase = atomicAdd(count, (unsigned long long)__popc(ballot));
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+        if (keep) list[wbase + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)e;
     }
 }
 
@@ -385,6 +562,7 @@ __global__ void k_pairs_to_keys(const uint64_t* __restrict__ pairs, uint64_t* __
 // host side
 // =====================================================================
 
+
 static inline int grid_cap(pierce_ctx* ctx, int64_t n, int block) {
     int64_t blocks = (n + block - 1) / block;
     const int64_t cap = (int64_t)ctx->sm_count * 32;
@@ -398,13 +576,13 @@ static uint64_t next_pow2(uint64_t v) {
     return p;
 }
 
-int launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode, int precision,
+int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int mode, int precision,
                      int swap, int32_t* counts, const int64_t* offsets, uint64_t* keys, uint64_t* table,
-                     uint64_t slots) {
-    if (src->ne == 0) return PIERCE_OK;
+                     uint64_t slots, const RayOpts* ro) {
+    if (src.num_edges == 0) return PIERCE_OK;
     EdgeRayParams P;
-    P.src = src->view();
-    P.tgt = tgt->view();
+    P.src = src;
+    P.tgt = tgt;
     P.swap = swap;
     P.counts = counts;
     P.offsets = offsets;
@@ -413,32 +591,140 @@ int launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_da
     P.mask = slots ? slots - 1 : 0;
     P.err = ctx->d_err;
     P.ctr = ctx->d_counters;
+    P.ray_list = ro ? ro->list : nullptr;
+    P.ray_count = ro ? ro->count : nullptr;
+    P.ray_cursor = ro ? ro->cursor : nullptr;
+    P.amb_queue = ro ? ro->amb_queue : nullptr;
+    P.amb_count = ro ? ro->amb_count : nullptr;
+    P.amb_cap = ro ? ro->amb_cap : 0;
+    if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
     const int B = 128;
-    const int64_t blocks = ((int64_t)src->ne + B - 1) / B;
-    if (blocks > 0x7FFFFFFF) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "too many edges for one launch");
-    dim3 g((unsigned)blocks);
+    dim3 g;
+    if (P.ray_list) {
+        cudaMemsetAsync(P.ray_cursor, 0, sizeof(unsigned long long), ctx->stream);
+        const int64_t want = (src.num_edges + B - 1) / B;
+        g = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * 12)));
+    } else {
+        const int64_t blocks = (src.num_edges + B - 1) / B;
+        if (blocks > 0x7FFFFFFF) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "too many edges for one launch");
+        g = dim3((unsigned)blocks);
+    }
     cudaStream_t st = ctx->stream;
 #define PG_LAUNCH(M, PR) k_edge_rays<M, PR><<<g, B, 0, st>>>(P)
-    if (precision == PREC_EXACT) {
-        if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PREC_EXACT);
-        else if (mode == MODE_WRITE) PG_LAUNCH(MODE_WRITE, PREC_EXACT);
-        else PG_LAUNCH(MODE_HASH, PREC_EXACT);
-    } else {
-        if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PREC_FP32);
-        else if (mode == MODE_WRITE) PG_LAUNCH(MODE_WRITE, PREC_FP32);
-        else PG_LAUNCH(MODE_HASH, PREC_FP32);
-    }
+#define PG_MODES(PR)                                  \
+    do {                                              \
+        if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PR); \
+        else if (mode == MODE_WRITE) PG_LAUNCH(MODE_WRITE, PR); \
+        else PG_LAUNCH(MODE_HASH, PR);                \
+    } while (0)
+    if (precision == PREC_EXACT) PG_MODES(PREC_EXACT);
+    else if (precision == PREC_DEFER) PG_MODES(PREC_DEFER);
+    else PG_MODES(PREC_FP32);
+#undef PG_MODES
 #undef PG_LAUNCH
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "edge ray kernel");
 }
 
-int launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int swap, uint64_t* table,
+int launch_resolve(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
+                   uint64_t slots, const RayOpts* ro, uint64_t* keys_out, unsigned long long* keys_count,
+                   uint64_t keys_cap) {
+    EdgeRayParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.src = src;
+    P.tgt = tgt;
+    P.swap = swap;
+    P.table = table;
+    P.mask = slots ? slots - 1 : 0;
+    P.err = ctx->d_err;
+    P.ctr = ctx->d_counters;
+    P.amb_queue = ro->amb_queue;
+    P.amb_count = ro->amb_count;
+    P.amb_cap = ro->amb_cap;
+    k_resolve_ambiguous<<<ctx->sm_count * 4, 128, 0, ctx->stream>>>(P, keys_out, keys_count, keys_cap);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "resolve ambiguous tests");
+}
+
+int launch_object_active(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, uint8_t* active) {
+    if (src.num_objects <= 0) return PIERCE_OK;
+    k_object_active<<<(unsigned)((src.num_objects + 127) / 128), 128, 0, ctx->stream>>>(src, tgt, active);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "object activity");
+}
+
+int launch_collect_rays(pierce_ctx* ctx, const DevDataset& src, const uint8_t* active, uint32_t* list,
+                        unsigned long long* count) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    if (src.num_edges > 0) {
+        k_collect_rays<<<grid_cap(ctx, src.num_edges, 256), 256, 0, ctx->stream>>>(src.edges, src.num_edges, active,
+                                                                                  list, count);
+        ctx->launches += 1;
+    }
+    return check_cuda(cudaGetLastError(), "collect rays");
+}
+
+int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, uint8_t* active, uint32_t* list,
+                unsigned long long* count) {
+    if (int s = launch_object_active(ctx, src, tgt, active)) return s;
+    return launch_collect_rays(ctx, src, active, list, count);
+}
+
+// Triangles of active objects -> compacted list.
+__global__ void k_collect_tris(const int32_t* __restrict__ t2o, int64_t nt, const uint8_t* __restrict__ active,
+                               uint32_t* __restrict__ list, unsigned long long* count) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        bool keep = false;
+        if (t < nt) {
+            const int32_t o = t2o[t];
+            keep = o >= 0 && active[o] != 0;
+        }
+        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
+        if (!ballot) continue;
+        const int lane = threadIdx.x & 31;
+        unsigned long long wbase = 0;
+        if (lane == 0) wbase = atomicAdd(count, (unsigned long long)__popc(ballot));
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+        if (keep) list[wbase + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)t;
+    }
+}
+
+// Object boxes as degenerate triangles (lo, hi, hi): their bounding boxes
+// are exactly the object boxes, so the triangle LBVH builder indexes them.
+__global__ void k_object_pseudo_tris(int32_t n, uint32_t* idx, int32_t* t2o) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        idx[3 * o] = (uint32_t)(2 * o);
+        idx[3 * o + 1] = (uint32_t)(2 * o + 1);
+        idx[3 * o + 2] = (uint32_t)(2 * o + 1);
+        t2o[o] = (int32_t)o;
+    }
+}
+
+int launch_collect_tris(pierce_ctx* ctx, const int32_t* t2o, int64_t nt, const uint8_t* active, uint32_t* list,
+                        unsigned long long* count) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    if (nt > 0) {
+        k_collect_tris<<<grid_cap(ctx, nt, 256), 256, 0, ctx->stream>>>(t2o, nt, active, list, count);
+        ctx->launches += 1;
+    }
+    return check_cuda(cudaGetLastError(), "collect triangles");
+}
+
+int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o) {
+    if (n <= 0) return PIERCE_OK;
+    k_object_pseudo_tris<<<grid_cap(ctx, n, 256), 256, 0, ctx->stream>>>(n, idx, t2o);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "object pseudo triangles");
+}
+
+int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots) {
-    if (src->num_objects <= 0) return PIERCE_OK;
+    if (src.num_objects <= 0) return PIERCE_OK;
     ParityParams P;
-    P.src = src->view();
-    P.tgt = tgt->view();
+    P.src = src;
+    P.tgt = tgt;
     P.swap = swap;
     P.table = table;
     P.parity = parity;
@@ -446,7 +732,7 @@ int launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_datas
     P.err = ctx->d_err;
     P.ctr = ctx->d_counters;
     const int B = 128;
-    k_parity<<<(unsigned)((src->num_objects + B - 1) / B), B, 0, ctx->stream>>>(P);
+    k_parity<<<(unsigned)((src.num_objects + B - 1) / B), B, 0, ctx->stream>>>(P);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "parity kernel");
 }

@@ -18,6 +18,7 @@
 //   7. optional leaf collapse: children covering <= leaf_size triangles
 //      become leaves over their contiguous soup range.
 // All box arithmetic is min/max of input floats, so boxes are exact.
+#include <cuda/atomic>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -44,16 +45,18 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t value, int64_t n) {
 }
 
 // 1. centroids and their bounds (bounds[0..2] ordered min, [3..5] ordered max)
-__global__ void k_centroids(const float* __restrict__ verts, const uint32_t* __restrict__ idx, int64_t nt,
-                            float4* __restrict__ cen, uint32_t* __restrict__ bounds) {
+__global__ void k_centroids(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                            const uint32_t* __restrict__ list, int64_t nt, float4* __restrict__ cen,
+                            uint32_t* __restrict__ bounds) {
     float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = list ? (int64_t)list[i] : i;
         const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
         const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
         const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
         const float3 m = make_float3((a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
                                      (a.z + b.z + c.z) * (1.0f / 3.0f));
-        cen[t] = make_float4(m.x, m.y, m.z, 0.0f);
+        cen[i] = make_float4(m.x, m.y, m.z, 0.0f);
         mn[0] = fminf(mn[0], m.x); mn[1] = fminf(mn[1], m.y); mn[2] = fminf(mn[2], m.z);
         mx[0] = fmaxf(mx[0], m.x); mx[1] = fmaxf(mx[1], m.y); mx[2] = fmaxf(mx[2], m.z);
     }
@@ -102,10 +105,10 @@ __global__ void k_morton(const float4* __restrict__ cen, int64_t nt, const uint3
 
 // 4. triangle soup in sorted order
 __global__ void k_soup(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
-                       const int32_t* __restrict__ t2o, const uint32_t* __restrict__ order, int64_t nt,
-                       float4* __restrict__ soup) {
+                       const int32_t* __restrict__ t2o, const uint32_t* __restrict__ list,
+                       const uint32_t* __restrict__ order, int64_t nt, float4* __restrict__ soup) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nt; j += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t t = order[j];
+        const uint32_t t = list ? list[order[j]] : order[j];
         const float3 a = load_vertex(verts, __ldg(idx + 3 * (size_t)t));
         const float3 b = load_vertex(verts, __ldg(idx + 3 * (size_t)t + 1));
         const float3 c = load_vertex(verts, __ldg(idx + 3 * (size_t)t + 2));
@@ -188,7 +191,10 @@ __device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], 
     hi[2] = __ldcg(bz + 2 * slot + 1);
 }
 
-// 6. refit; root box is written to root_box[0..5]
+// 6. refit; root box is written to root_box[0..5].  The child box goes to
+// L2 (st.cg), the arrival counter is an acquire-release device-scope atomic
+// (it orders the box store before the sibling's load without a full fence),
+// and the sibling box is read from L2 (ld.cg).
 __global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes, const int32_t* __restrict__ parent_int,
                         const int32_t* __restrict__ parent_leaf, uint32_t* arrivals, float* root_box) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
@@ -201,10 +207,8 @@ __global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes,
             Node* nd = nodes + node;
             const int slot = (__ldcg(&nd->ch.x) == code) ? 0 : 1;
             store_child_box(nd, slot, lo, hi);
-            __threadfence();
-            const uint32_t old = atomicAdd(arrivals + node, 1u);
-            if (old == 0) break;  // sibling not done yet; it will continue upward
-            __threadfence();
+            cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrived(arrivals[node]);
+            if (arrived.fetch_add(1u, cuda::memory_order_acq_rel) == 0u) break;  // sibling continues upward
             float olo[3], ohi[3];
             load_child_box(nd, 1 - slot, olo, ohi);
             for (int k = 0; k < 3; ++k) {
@@ -258,22 +262,56 @@ __global__ void k_collapse(Node* nodes, const int2* __restrict__ range, int64_t 
 
 // ---- per-object data: first vertex, bounding box ------------------------
 
+// Per object: lowest triangle index and bounding box.  Triangles of one
+// object are usually contiguous, so a warp whose lanes all belong to one
+// object reduces in registers and issues 7 atomics instead of 224.
 __global__ void k_first_tri(const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj, int32_t* first_tri,
                             uint32_t* obj_box_o, const float* __restrict__ verts, const uint32_t* __restrict__ idx) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t o = t2o[t];
-        if (o < 0 || o >= nobj) continue;
-        atomicMin(first_tri + o, (int32_t)t);
-        const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
-        const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
-        const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
-        uint32_t* bx = obj_box_o + 6 * (size_t)o;
-        atomicMin(bx + 0, f2o(fminf(a.x, fminf(b.x, c.x))));
-        atomicMin(bx + 1, f2o(fminf(a.y, fminf(b.y, c.y))));
-        atomicMin(bx + 2, f2o(fminf(a.z, fminf(b.z, c.z))));
-        atomicMax(bx + 3, f2o(fmaxf(a.x, fmaxf(b.x, c.x))));
-        atomicMax(bx + 4, f2o(fmaxf(a.y, fmaxf(b.y, c.y))));
-        atomicMax(bx + 5, f2o(fmaxf(a.z, fmaxf(b.z, c.z))));
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        const bool valid = t < nt;
+        int32_t o = valid ? t2o[t] : -1;
+        if (o >= nobj) o = -1;
+        float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        if (o >= 0) {
+            const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
+            const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
+            const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
+            mn[0] = fminf(a.x, fminf(b.x, c.x));
+            mn[1] = fminf(a.y, fminf(b.y, c.y));
+            mn[2] = fminf(a.z, fminf(b.z, c.z));
+            mx[0] = fmaxf(a.x, fmaxf(b.x, c.x));
+            mx[1] = fmaxf(a.y, fmaxf(b.y, c.y));
+            mx[2] = fmaxf(a.z, fmaxf(b.z, c.z));
+        }
+        const int32_t o0 = __shfl_sync(0xFFFFFFFFu, o, 0);
+        const bool uniform = __all_sync(0xFFFFFFFFu, o == o0) && o0 >= 0;
+        if (uniform) {
+            int32_t tmin = (int32_t)t;
+            for (int off = 16; off > 0; off >>= 1) {
+                tmin = min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, off));
+                for (int k = 0; k < 3; ++k) {
+                    mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
+                    mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
+                }
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicMin(first_tri + o0, tmin);
+                uint32_t* bx = obj_box_o + 6 * (size_t)o0;
+                for (int k = 0; k < 3; ++k) {
+                    atomicMin(bx + k, f2o(mn[k]));
+                    atomicMax(bx + 3 + k, f2o(mx[k]));
+                }
+            }
+        } else if (o >= 0) {
+            atomicMin(first_tri + o, (int32_t)t);
+            uint32_t* bx = obj_box_o + 6 * (size_t)o;
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(bx + k, f2o(mn[k]));
+                atomicMax(bx + 3 + k, f2o(mx[k]));
+            }
+        }
     }
 }
 
@@ -329,88 +367,104 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
     return check_cuda(cudaGetLastError(), "prepare_objects");
 }
 
-int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
-    const int64_t n = (int64_t)ds->nt;
+// Triangles -> LBVH.  The n triangles are idx[3t..3t+2] for t = list[i]
+// (or t = i without a list); soup and nodes receive the structure; build
+// temporaries live in scratch slots 1..4.  Everything is enqueued on the
+// context stream; when root_box is non-null the root box is read back
+// (synchronously).
+int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, const uint32_t* list,
+               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box) {
     cudaStream_t st = ctx->stream;
     if (leaf_size < 1) leaf_size = 1;
     if (leaf_size > 16) leaf_size = 16;
-    ds->leaf_size = leaf_size;
+    shape->leaf_size = leaf_size;
+    if (n == 0) {
+        shape->root_is_leaf = 1;
+        shape->root_leaf_count = 0;
+        shape->num_nodes = 0;
+        if (root_box)
+            for (int k = 0; k < 6; ++k) root_box[k] = 0.0f;
+        return PIERCE_OK;
+    }
+    // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 parents/range/arrivals/bounds
+    void *pc = nullptr, *pk = nullptr, *pv = nullptr, *pm = nullptr;
+    if (int s = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc)) return s;
+    if (int s = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk)) return s;
+    if (int s = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv)) return s;
+    const size_t misc_bytes =
+        sizeof(int32_t) * (size_t)(n + n) + sizeof(int2) * (size_t)n + sizeof(uint32_t) * (size_t)n + 64;
+    if (int s = scratch(ctx, 4, misc_bytes, &pm)) return s;
+    float4* cen = static_cast<float4*>(pc);
+    uint32_t* keys = static_cast<uint32_t*>(pk);
+    uint32_t* vals = static_cast<uint32_t*>(pv);
+    int32_t* parent_int = static_cast<int32_t*>(pm);
+    int32_t* parent_leaf = parent_int + n;
+    int2* range = reinterpret_cast<int2*>(parent_leaf + n);
+    uint32_t* arrivals = reinterpret_cast<uint32_t*>(range + n);
+    uint32_t* bounds = arrivals + n;                            // 6 words
+    float* d_root_box = reinterpret_cast<float*>(bounds + 6);  // 6 floats
+
+    const int B = 256;
+    k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
+    k_fill_u32<<<1, 32, 0, st>>>(bounds + 3, 0u, 3);       // ordered -max
+    k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, list, n, cen, bounds);
+    k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
+    ctx->launches += 4;
+    if (int s = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30)) return s;
+    const uint32_t* skeys = keys + n;
+    const uint32_t* order = vals + n;
+    k_soup<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, t2o, list, order, n, soup);
+    ctx->launches += 1;
+    if (n == 1) {
+        k_single_box<<<1, 1, 0, st>>>(soup, d_root_box);
+        ctx->launches += 1;
+        shape->root_is_leaf = 1;
+        shape->root_leaf_count = 1;
+        shape->num_nodes = 0;
+    } else {
+        cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * (size_t)n, st);
+        k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, nodes, parent_int, parent_leaf, range);
+        k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, parent_int, parent_leaf, arrivals, d_root_box);
+        ctx->launches += 2;
+        if (leaf_size > 1) {
+            k_collapse<<<grid_for(ctx, n - 1, B), B, 0, st>>>(nodes, range, n, leaf_size);
+            ctx->launches += 1;
+        }
+        shape->num_nodes = (uint64_t)(n - 1);
+        shape->root_is_leaf = (n <= leaf_size) ? 1 : 0;
+        shape->root_leaf_count = (n <= leaf_size) ? (int)n : 0;
+    }
+    if (int s = check_cuda(cudaGetLastError(), "bvh build kernels")) return s;
+    if (root_box) {
+        if (int s = check_cuda(cudaMemcpyAsync(root_box, d_root_box, 6 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                               "bvh root box"))
+            return s;
+        if (int s = check_cuda(cudaStreamSynchronize(st), "bvh build")) return s;
+    }
+    return PIERCE_OK;
+}
+
+int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
     ds->built = 0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
-    int status = PIERCE_OK;
+    cudaEventRecord(e0, ctx->stream);
+    BvhShape shape;
     float root_box[6] = {0, 0, 0, 0, 0, 0};
-    do {
-        if (n == 0) {
-            ds->root_is_leaf = 1;
-            ds->root_leaf_count = 0;
-            ds->num_nodes = 0;
-            break;
-        }
-        // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 parents/range/arrivals/bounds
-        void *pc = nullptr, *pk = nullptr, *pv = nullptr, *pm = nullptr;
-        if ((status = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc))) break;
-        if ((status = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk))) break;
-        if ((status = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv))) break;
-        const size_t misc_bytes = sizeof(int32_t) * (size_t)(n + n) + sizeof(int2) * (size_t)n +
-                                  sizeof(uint32_t) * (size_t)n + 64;
-        if ((status = scratch(ctx, 4, misc_bytes, &pm))) break;
-        float4* cen = static_cast<float4*>(pc);
-        uint32_t* keys = static_cast<uint32_t*>(pk);
-        uint32_t* vals = static_cast<uint32_t*>(pv);
-        int32_t* parent_int = static_cast<int32_t*>(pm);
-        int32_t* parent_leaf = parent_int + n;
-        int2* range = reinterpret_cast<int2*>(parent_leaf + n);
-        uint32_t* arrivals = reinterpret_cast<uint32_t*>(range + n);
-        uint32_t* bounds = arrivals + n;        // 6 words
-        float* d_root_box = reinterpret_cast<float*>(bounds + 6);  // 6 floats
-
-        const uint32_t init_b[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-        cudaMemcpyAsync(bounds, init_b, sizeof(init_b), cudaMemcpyHostToDevice, st);
-        const int B = 256;
-        k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_vertices, ds->d_indices, n, cen, bounds);
-        k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
-        ctx->launches += 2;
-        if ((status = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30))) break;
-        const uint32_t* skeys = keys + n;
-        const uint32_t* order = vals + n;
-        k_soup<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_vertices, ds->d_indices, ds->d_tri_to_object, order, n,
-                                                  ds->d_soup);
-        ctx->launches += 1;
-        if (n == 1) {
-            k_single_box<<<1, 1, 0, st>>>(ds->d_soup, d_root_box);
-            ctx->launches += 1;
-            ds->root_is_leaf = 1;
-            ds->root_leaf_count = 1;
-            ds->num_nodes = 0;
-        } else {
-            cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * (size_t)n, st);
-            k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, ds->d_nodes, parent_int, parent_leaf, range);
-            k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(ds->d_soup, n, ds->d_nodes, parent_int, parent_leaf, arrivals,
-                                                       d_root_box);
-            ctx->launches += 2;
-            if (leaf_size > 1) {
-                k_collapse<<<grid_for(ctx, n - 1, B), B, 0, st>>>(ds->d_nodes, range, n, leaf_size);
-                ctx->launches += 1;
-            }
-            ds->num_nodes = (uint64_t)(n - 1);
-            ds->root_is_leaf = (n <= leaf_size) ? 1 : 0;
-            ds->root_leaf_count = (n <= leaf_size) ? (int)n : 0;
-        }
-        if ((status = check_cuda(cudaMemcpyAsync(root_box, d_root_box, sizeof(root_box), cudaMemcpyDeviceToHost, st),
-                                 "bvh root box")))
-            break;
-    } while (0);
-    cudaEventRecord(e1, st);
-    if (status == PIERCE_OK) status = check_cuda(cudaStreamSynchronize(st), "bvh build");
-    if (status == PIERCE_OK) status = check_cuda(cudaGetLastError(), "bvh build kernels");
+    int status = build_lbvh(ctx, ds->d_vertices, ds->d_indices, ds->d_tri_to_object, nullptr, (int64_t)ds->nt,
+                            leaf_size, ds->d_soup, ds->d_nodes, &shape, root_box);
+    cudaEventRecord(e1, ctx->stream);
+    if (status == PIERCE_OK) status = check_cuda(cudaStreamSynchronize(ctx->stream), "bvh build");
     float ms = 0.0f;
     if (status == PIERCE_OK) cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (status != PIERCE_OK) return status;
+    ds->leaf_size = shape.leaf_size;
+    ds->root_is_leaf = shape.root_is_leaf;
+    ds->root_leaf_count = shape.root_leaf_count;
+    ds->num_nodes = shape.num_nodes;
     for (int k = 0; k < 3; ++k) {
         ds->lo[k] = root_box[k];
         ds->hi[k] = root_box[3 + k];

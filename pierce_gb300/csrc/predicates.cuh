@@ -206,6 +206,11 @@ __device__ __noinline__ int orient2d_exact(float3 a, float3 b, float3 c, int i, 
 
 // ------------------------------------------------------------- FP64 stage
 __device__ __noinline__ int orient3d_fp64_or_exact(float3 a, float3 b, float3 c, float3 d, PredCounters& pc) {
+    // two coincident points make the determinant exactly zero
+    if ((a.x == b.x && a.y == b.y && a.z == b.z) || (a.x == c.x && a.y == c.y && a.z == c.z) ||
+        (a.x == d.x && a.y == d.y && a.z == d.z) || (b.x == c.x && b.y == c.y && b.z == c.z) ||
+        (b.x == d.x && b.y == d.y && b.z == d.z) || (c.x == d.x && c.y == d.y && c.z == d.z))
+        return 0;
     const double ux = (double)b.x - a.x, uy = (double)b.y - a.y, uz = (double)b.z - a.z;
     const double vx = (double)c.x - a.x, vy = (double)c.y - a.y, vz = (double)c.z - a.z;
     const double wx = (double)d.x - a.x, wy = (double)d.y - a.y, wz = (double)d.z - a.z;
@@ -257,6 +262,15 @@ __device__ __forceinline__ int certain_sign(float v, float perm, float k) {
     if (!(perm >= 1e-30f && perm <= 1e36f)) return 0;
     const float bound = k * kEps32 * perm;
     return v > bound ? 1 : (v < -bound ? -1 : 0);
+}
+
+__device__ __forceinline__ bool same_point(float3 x, float3 y) { return x.x == y.x && x.y == y.y && x.z == y.z; }
+
+// A segment endpoint that is a vertex of the triangle is a common point of
+// the two closed sets (exact; covers shared vertices and shared edges).
+__device__ __forceinline__ bool endpoint_is_vertex(float3 p, float3 q, float3 a, float3 b, float3 c) {
+    return same_point(p, a) || same_point(p, b) || same_point(p, c) || same_point(q, a) || same_point(q, b) ||
+           same_point(q, c);
 }
 
 __device__ __forceinline__ int orient3d_robust(float3 a, float3 b, float3 c, float3 d, PredCounters& pc) {
@@ -316,6 +330,13 @@ __device__ __noinline__ bool seg_tri_coplanar(float3 p, float3 q, float3 a, floa
 
 // Exact closed segment / closed triangle test with the FP32 filter.
 __device__ __forceinline__ bool seg_tri_exact(float3 p, float3 q, float3 a, float3 b, float3 c, PredCounters& pc) {
+    if (endpoint_is_vertex(p, q, a, b, c)) {
+        // common point; only a zero-area triangle (empty by definition) is excluded
+        if (orient2d_robust(a, b, c, 0, 1, pc) != 0 || orient2d_robust(a, b, c, 1, 2, pc) != 0 ||
+            orient2d_robust(a, b, c, 2, 0, pc) != 0)
+            return true;
+        return false;
+    }
     // Plane side of p and q: (p-a).n, (q-a).n with n = (b-a) x (c-a).
     const float3 u = f3sub(b, a), v = f3sub(c, a);
     const float3 n = f3cross(u, v), np = f3cross_perm(u, v);
@@ -359,6 +380,40 @@ __device__ __forceinline__ bool seg_tri_exact(float3 p, float3 q, float3 a, floa
     if (pos && neg) return false;
     if (!pos && !neg) return false;  // only for a zero-area triangle
     return true;
+}
+
+// Float32-only classification of the closed segment / triangle test:
+// SEG_MISS and SEG_HIT are certain (the same answer as seg_tri_exact);
+// SEG_AMBIGUOUS means the float32 bound could not decide and the exact test
+// must be run.
+enum SegClass { SEG_MISS = 0, SEG_HIT = 1, SEG_AMBIGUOUS = 2 };
+
+__device__ __forceinline__ int seg_tri_fp32_class(float3 p, float3 q, float3 a, float3 b, float3 c) {
+    if (endpoint_is_vertex(p, q, a, b, c)) {
+        // a common point, unless the triangle has zero area (then it is empty)
+        const float3 u0 = f3sub(b, a), v0 = f3sub(c, a);
+        const float3 n0 = f3cross(u0, v0), np0 = f3cross_perm(u0, v0);
+        if (certain_sign(n0.x, np0.x, 8.0f) != 0 || certain_sign(n0.y, np0.y, 8.0f) != 0 ||
+            certain_sign(n0.z, np0.z, 8.0f) != 0)
+            return SEG_HIT;
+        return SEG_AMBIGUOUS;
+    }
+    const float3 u = f3sub(b, a), v = f3sub(c, a);
+    const float3 n = f3cross(u, v), np = f3cross_perm(u, v);
+    const float3 pa = f3sub(p, a), qa = f3sub(q, a);
+    const int sp = certain_sign(f3dot(pa, n), f3dot_abs(pa, np), 12.0f);
+    const int sq = certain_sign(f3dot(qa, n), f3dot_abs(qa, np), 12.0f);
+    if (sp * sq > 0) return SEG_MISS;
+    if (sp == 0 || sq == 0) return SEG_AMBIGUOUS;
+    const float3 d = f3sub(q, p), A = f3sub(a, p), B = f3sub(b, p), C = f3sub(c, p);
+    const float3 ma = f3cross(d, A), mpa = f3cross_perm(d, A);
+    const float3 mb = f3cross(d, B), mpb = f3cross_perm(d, B);
+    const int s1 = certain_sign(f3dot(B, ma), f3dot_abs(B, mpa), 12.0f);
+    const int s2 = certain_sign(f3dot(C, mb), f3dot_abs(C, mpb), 12.0f);
+    const int s3 = certain_sign(-f3dot(C, ma), f3dot_abs(C, mpa), 12.0f);
+    if ((s1 > 0 || s2 > 0 || s3 > 0) && (s1 < 0 || s2 < 0 || s3 < 0)) return SEG_MISS;
+    if (s1 == 0 || s2 == 0 || s3 == 0) return SEG_AMBIGUOUS;
+    return SEG_HIT;
 }
 
 // Plain float32 Moller-Trumbore on the segment p->q (no fallback).

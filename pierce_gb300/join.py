@@ -143,7 +143,7 @@ class JoinResult:
 
 def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
-              max_retries=4) -> capi.JoinOpts:
+              max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True) -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -156,6 +156,9 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.output_safety = float(output_safety)
     o.include_overlap_pairs = 1 if include_overlap_pairs else 0
     o.max_retries = int(max_retries)
+    o.cull_objects = 1 if cull_objects else 0
+    o.defer_exact = 1 if defer_exact else 0
+    o.active_bvh = 1 if active_bvh else 0
     return o
 
 

@@ -43,7 +43,11 @@ def test_overlap_exact_matches_oracle(ctx, case, sizing, leaf):
     got = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing)
     assert np.array_equal(keys(got), want), name
     passes = 2 if sizing == "two_pass" else 1
-    assert got.stats["rays"] == passes * (A.num_edges + B.num_edges)
+    # object culling traces only the edges of objects near the other side
+    assert 0 < got.stats["rays"] <= passes * (A.num_edges + B.num_edges)
+    plain = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing, cull_objects=False,
+                           active_bvh=False)
+    assert plain.stats["rays"] == passes * (A.num_edges + B.num_edges)
 
 
 def test_overlap_fp32_plain_matches_oracle_fp32(ctx, case):
@@ -125,4 +129,70 @@ def test_identical_datasets_coplanar(ctx):
     assert all((want >> np.uint64(32)) >= 0)
     diag = (want >> np.uint64(32)) == (want & np.uint64(0xFFFFFFFF))
     assert diag.sum() == 50
+
+
+@pytest.mark.parametrize("defer", [False, True])
+def test_one_ulp_shifted_copy_needs_exact_arithmetic(ctx, defer):
+    """B is A moved by one ulp: every B edge lies within rounding of an A
+    face, so the float32 filter is undecided and the exact stages decide."""
+    A = pg.icospheres(9, 40, 2, hi=25.0)
+    v = np.nextafter(A.vertices, np.float32(np.inf)).astype(np.float32)
+    B = pg.Geometry.from_arrays(v, A.indices, A.tri_to_object).extract_edges()
+    want, _ = O.overlap_keys(A, B)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B), defer_exact=defer)
+    assert np.array_equal(keys(got), want)
     assert got.stats["fp32_ambiguous"] > 0
+    inter = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), defer_exact=defer)
+    assert np.array_equal(keys(inter), O.intersection_keys(A, B))
+
+
+@pytest.mark.parametrize("active_bvh", [False, True])
+@pytest.mark.parametrize("cull", [False, True])
+@pytest.mark.parametrize("defer", [False, True])
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+def test_culling_and_deferral_do_not_change_pairs(ctx, case, cull, defer, sizing, active_bvh):
+    name, A, B = case
+    want, _ = O.overlap_keys(A, B)
+    kw = dict(sizing=sizing, cull_objects=cull, defer_exact=defer, active_bvh=active_bvh)
+    got = J.overlap_join(ctx, ds(ctx, A), ds(ctx, B), **kw)
+    assert np.array_equal(keys(got), want), (name, kw)
+    inter = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), **kw)
+    assert np.array_equal(keys(inter), O.intersection_keys(A, B)), (name, kw)
+    cont = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), **kw)
+    assert np.array_equal(keys(cont), O.containment_keys(A, B)), (name, kw)
+    if active_bvh:
+        assert got.stats["active_triangles"][0] <= A.num_triangles
+
+
+def test_active_bvh_needs_no_dataset_bvh(ctx):
+    A, B = pg.icospheres(61, 200, 2, hi=40.0), pg.icospheres(62, 200, 2, hi=40.0)
+    lazy = J.default_tuning(defer_build=1)
+    da, db = ds_t(ctx, A, lazy), ds_t(ctx, B, lazy)
+    assert da.info().built == 0
+    want = O.intersection_keys(A, B)
+    assert np.array_equal(keys(J.intersection_join(ctx, da, db)), want)
+    with pytest.raises(Exception):
+        J.intersection_join(ctx, da, db, active_bvh=False)   # needs built datasets
+
+
+def ds_t(ctx, geom, tuning):
+    return J.Dataset.from_geometry(ctx, geom, tuning)
+
+
+@pytest.mark.parametrize("name", ["icospheres", "ellipsoid_contacts"])
+def test_golden_pair_sets(ctx, name):
+    """GPU joins against the committed oracle answers (tests/golden)."""
+    import importlib.util
+    from pathlib import Path
+    golden = Path(__file__).resolve().parent / "golden"
+    spec = importlib.util.spec_from_file_location("make_golden", golden / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    A, B = mod.JOIN_CASES[name]()
+    g = np.load(golden / f"pairs_{name}.npz")
+    da, db = ds(ctx, A), ds(ctx, B)
+    assert np.array_equal(keys(J.overlap_join(ctx, da, db)), g["overlap"])
+    assert np.array_equal(keys(J.overlap_join(ctx, da, db, precision="fp32", sizing="two_pass",
+                                              cull_objects=False)), g["overlap_fp32"])
+    assert np.array_equal(keys(J.intersection_join(ctx, da, db)), g["intersection"])
+    assert np.array_equal(keys(J.containment_join(ctx, da, db)), g["containment"])
