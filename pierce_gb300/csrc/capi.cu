@@ -311,8 +311,8 @@ void pierce_dataset_destroy(pierce_dataset* ds) {
         cudaSetDevice(ds->ctx->device);
         cudaStreamSynchronize(ds->ctx->stream);
     }
-    void* ptrs[] = {ds->d_vertices, ds->d_indices, ds->d_tri_to_object, ds->d_edges,
-                    ds->d_soup,     ds->d_nodes,   ds->d_first_vertex,  ds->d_obj_box};
+    void* ptrs[] = {ds->d_vertices, ds->d_indices,      ds->d_tri_to_object, ds->d_edges, ds->d_edge_src,
+                    ds->d_soup,     ds->d_nodes,        ds->d_first_vertex,  ds->d_obj_box};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete ds;
@@ -371,20 +371,21 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
         if ((s = device_alloc((void**)&ds->d_indices, ib, "indices"))) break;
         if ((s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object"))) break;
         if ((s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges"))) break;
+        if ((s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources"))) break;
         if ((s = device_alloc((void**)&ds->d_soup, 48 * ds->nt, "triangle soup"))) break;
         if ((s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))) break;
         if ((s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices"))) break;
         if ((s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes"))) break;
-        ds->device_bytes = vb + ib + ob + 32 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
+        ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
         if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, st), "copy vertices"))) break;
         if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, st), "copy indices"))) break;
         if (ob && (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, st), "copy t2o")))
             break;
         if (ds->ne) {
-            void *ps = nullptr, *pe = nullptr, *po = nullptr;
+            void *ps = nullptr, *pe = nullptr;
+            void* po = ds->d_edge_src;
             if ((s = scratch(ctx, SLOT_BUILD_A, 12 * ds->ne, &ps))) break;
             if ((s = scratch(ctx, SLOT_BUILD_B, 12 * ds->ne, &pe))) break;
-            if ((s = scratch(ctx, SLOT_BUILD_C, 4 * ds->ne, &po))) break;
             if ((s = check_cuda(cudaMemcpyAsync(ps, v->edge_starts, 12 * ds->ne, kind, st), "copy edge starts"))) break;
             if ((s = check_cuda(cudaMemcpyAsync(pe, v->edge_ends, 12 * ds->ne, kind, st), "copy edge ends"))) break;
             if ((s = check_cuda(cudaMemcpyAsync(po, v->edge_src, 4 * ds->ne, kind, st), "copy edge src"))) break;

@@ -44,7 +44,8 @@ struct __align__(16) Node {
     float4 bx;   // c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x
     float4 by;   // c0.lo.y, c0.hi.y, c1.lo.y, c1.hi.y
     float4 bz;   // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
-    int4 ch;     // child0, child1, leaf count of child0, leaf count of child1
+    int4 ch;     // child0, child1, leaf counts (count0 | count1 << 8),
+                 // build link (parent << 2 | side << 1 | arrival toggle)
 };
 
 // Device view of one dataset (all pointers into its own allocations).
@@ -58,6 +59,7 @@ struct DevDataset {
     int root_leaf_count;
     // edge rays, 2 float4 per edge: (start.xyz, src object bits), (end.xyz, 0)
     const float4* edges;
+    const int32_t* edge_src;     // source object per edge (compact copy)
     int64_t num_edges;
     // objects
     const float4* first_vertex;  // per object (xyz, 0)
@@ -114,6 +116,7 @@ struct pierce_dataset {
     uint32_t* d_indices = nullptr;
     int32_t* d_tri_to_object = nullptr;
     float4* d_edges = nullptr;
+    int32_t* d_edge_src = nullptr;
     float4* d_soup = nullptr;
     pgpu::Node* d_nodes = nullptr;
     float4* d_first_vertex = nullptr;
@@ -134,6 +137,7 @@ struct pierce_dataset {
         v.root_is_leaf = root_is_leaf;
         v.root_leaf_count = root_leaf_count;
         v.edges = d_edges;
+        v.edge_src = d_edge_src;
         v.num_edges = (int64_t)ne;
         v.first_vertex = d_first_vertex;
         v.obj_box = d_obj_box;

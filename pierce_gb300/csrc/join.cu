@@ -208,11 +208,11 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
             bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
             bool h1 = box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
             if (h0 && ch.x < 0) {
-                leaf(~ch.x, ch.z);
+                leaf(~ch.x, ch.z & 0xFF);
                 h0 = false;
             }
             if (h1 && ch.y < 0) {
-                leaf(~ch.y, ch.w);
+                leaf(~ch.y, (ch.z >> 8) & 0xFF);
                 h1 = false;
             }
             if (h0 && h1) {
@@ -350,11 +350,11 @@ __global__ void __launch_bounds__(128) k_object_active(DevDataset src, DevDatase
                 bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
                 bool h1 = box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
                 if (h0 && ch.x < 0) {
-                    leaf(~ch.x, ch.z);
+                    leaf(~ch.x, ch.z & 0xFF);
                     h0 = false;
                 }
                 if (!found && h1 && ch.y < 0) {
-                    leaf(~ch.y, ch.w);
+                    leaf(~ch.y, (ch.z >> 8) & 0xFF);
                     h1 = false;
                 }
                 if (found) break;
@@ -382,22 +382,54 @@ __global__ void __launch_bounds__(128) k_object_active(DevDataset src, DevDatase
     active[o] = found ? 1 : 0;
 }
 
-// Edges of active objects -> compacted list (warp-aggregated cursor).
-__global__ void k_collect_rays(const float4* __restrict__ edges, int64_t n, const uint8_t* __restrict__ active,
-                               uint32_t* __restrict__ list, unsigned long long* count) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
-        const int64_t e = base + threadIdx.x;
-        bool keep = false;
-        if (e < n) keep = active[__float_as_int(__ldg(&edges[2 * e].w))] != 0;
-        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
-        if (!ballot) continue;
-        const int lane = threadIdx.x & 31;
-        unsigned long long wbase = 0;
-        if (lane == 0) wbase = atomicAdd(count, (unsigned long long)__popc(ballot));
-        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-        if (keep) list[wbase + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)e;
+// Block-aggregated stream compaction: each thread takes ITEMS consecutive
+// elements of a tile, the block scans its keep counts in shared memory and
+// reserves its output range with one atomicAdd per tile, so a single
+// counter sees one atomic per blockDim*ITEMS elements.
+template <int ITEMS, class Keep>
+__device__ __forceinline__ void compact_tiles(int64_t n, Keep keep, uint32_t* __restrict__ out,
+                                              unsigned long long* count) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ unsigned long long block_base;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
+    const int64_t tile = (int64_t)blockDim.x * ITEMS;
+    for (int64_t base = (int64_t)blockIdx.x * tile; base < n; base += (int64_t)gridDim.x * tile) {
+        const int64_t first = base + (int64_t)tid * ITEMS;
+        uint32_t mask = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k)
+            if (first + k < n && keep(first + k)) mask |= 1u << k;
+        const uint32_t c = __popc(mask);
+        uint32_t incl = c;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = lane < nwarps ? warp_tot[lane] : 0;
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, off);
+                if (lane >= off) w += v;
+            }
+            if (lane < nwarps) warp_tot[lane] = w;  // inclusive over warps
+            if (lane == 31) block_base = w ? atomicAdd(count, (unsigned long long)w) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long pos = block_base + (wid ? warp_tot[wid - 1] : 0u) + (incl - c);
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k)
+            if (mask & (1u << k)) out[pos++] = (uint32_t)(first + k);
+        __syncthreads();
     }
+}
+
+// Edges of active objects -> compacted list.
+__global__ void __launch_bounds__(256) k_collect_rays(const int32_t* __restrict__ edge_src, int64_t n,
+                                                      const uint8_t* __restrict__ active, uint32_t* __restrict__ list,
+                                                      unsigned long long* count) {
+    compact_tiles<8>(n, [&](int64_t e) { return active[edge_src[e]] != 0; }, list, count);
 }
 
 struct ParityParams {
@@ -458,11 +490,11 @@ __global__ void __launch_bounds__(128) k_parity(ParityParams P) {
                     bool h0 = bx.x <= p.x && p.x <= bx.y && by.x <= p.y && p.y <= by.y && bz.y >= p.z;
                     bool h1 = bx.z <= p.x && p.x <= bx.w && by.z <= p.y && p.y <= by.w && bz.w >= p.z;
                     if (h0 && ch.x < 0) {
-                        leaf(~ch.x, ch.z);
+                        leaf(~ch.x, ch.z & 0xFF);
                         h0 = false;
                     }
                     if (h1 && ch.y < 0) {
-                        leaf(~ch.y, ch.w);
+                        leaf(~ch.y, (ch.z >> 8) & 0xFF);
                         h1 = false;
                     }
                     if (h0 && h1) {
@@ -657,8 +689,8 @@ int launch_collect_rays(pierce_ctx* ctx, const DevDataset& src, const uint8_t* a
                         unsigned long long* count) {
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     if (src.num_edges > 0) {
-        k_collect_rays<<<grid_cap(ctx, src.num_edges, 256), 256, 0, ctx->stream>>>(src.edges, src.num_edges, active,
-                                                                                  list, count);
+        k_collect_rays<<<grid_cap(ctx, (src.num_edges + 7) / 8, 256), 256, 0, ctx->stream>>>(
+            src.edge_src, src.num_edges, active, list, count);
         ctx->launches += 1;
     }
     return check_cuda(cudaGetLastError(), "collect rays");
@@ -671,24 +703,13 @@ int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, u
 }
 
 // Triangles of active objects -> compacted list.
-__global__ void k_collect_tris(const int32_t* __restrict__ t2o, int64_t nt, const uint8_t* __restrict__ active,
-                               uint32_t* __restrict__ list, unsigned long long* count) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
-        const int64_t t = base + threadIdx.x;
-        bool keep = false;
-        if (t < nt) {
-            const int32_t o = t2o[t];
-            keep = o >= 0 && active[o] != 0;
-        }
-        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
-        if (!ballot) continue;
-        const int lane = threadIdx.x & 31;
-        unsigned long long wbase = 0;
-        if (lane == 0) wbase = atomicAdd(count, (unsigned long long)__popc(ballot));
-        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-        if (keep) list[wbase + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)t;
-    }
+__global__ void __launch_bounds__(256) k_collect_tris(const int32_t* __restrict__ t2o, int64_t nt,
+                                                      const uint8_t* __restrict__ active, uint32_t* __restrict__ list,
+                                                      unsigned long long* count) {
+    compact_tiles<8>(nt, [&](int64_t t) {
+        const int32_t o = t2o[t];
+        return o >= 0 && active[o] != 0;
+    }, list, count);
 }
 
 // Object boxes as degenerate triangles (lo, hi, hi): their bounding boxes
@@ -706,7 +727,7 @@ int launch_collect_tris(pierce_ctx* ctx, const int32_t* t2o, int64_t nt, const u
                         unsigned long long* count) {
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     if (nt > 0) {
-        k_collect_tris<<<grid_cap(ctx, nt, 256), 256, 0, ctx->stream>>>(t2o, nt, active, list, count);
+        k_collect_tris<<<grid_cap(ctx, (nt + 7) / 8, 256), 256, 0, ctx->stream>>>(t2o, nt, active, list, count);
         ctx->launches += 1;
     }
     return check_cuda(cudaGetLastError(), "collect triangles");

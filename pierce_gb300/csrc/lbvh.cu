@@ -15,8 +15,8 @@
 //      reach a node (atomic arrival counter) merges the two child boxes.
 //      Child boxes are stored in the parent (Node::bx/by/bz), which is the
 //      layout the traversal reads;
-//   7. optional leaf collapse: children covering <= leaf_size triangles
-//      become leaves over their contiguous soup range.
+//   7. leaf collapse (in the hierarchy step): children covering <=
+//      leaf_size triangles become leaves over their contiguous soup range.
 // All box arithmetic is min/max of input floats, so boxes are exact.
 #include <cuda/atomic>
 #include <cuda_runtime.h>
@@ -126,10 +126,19 @@ __device__ __forceinline__ int lcp(const uint32_t* keys, int64_t n, int64_t i, i
     return __clz(ki ^ kj);
 }
 
-// 5. Karras hierarchy: internal node i covers sorted range [first, last]
-__global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, Node* __restrict__ nodes,
-                         int32_t* __restrict__ parent_int, int32_t* __restrict__ parent_leaf,
-                         int2* __restrict__ range) {
+// 5. Karras hierarchy with leaf collapse.  Internal node i covers the
+// sorted range [first, last]; a child whose range holds <= leaf_size
+// triangles becomes a leaf over that range, and nodes inside such a range
+// are never created.  Links for the refit are written here:
+//   * node.ch.w of an internal child = parent << 2 | side << 1 (bit 0 is the
+//     arrival toggle, initially 0; the root's parent is kRootParent);
+//   * leaf_rec[first] of a leaf child = parent << 9 | side << 8 | count.
+// Every word is written by exactly one thread (ch.x/y/z by the node's own
+// thread, ch.w by its parent's thread), so no two threads write one word.
+constexpr uint32_t kRootParent = 0x3FFFFFFFu;
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, int leaf_size, Node* __restrict__ nodes,
+                         unsigned long long* __restrict__ leaf_rec) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n - 1; i += (int64_t)gridDim.x * blockDim.x) {
         const int d = (lcp(keys, n, i, i + 1) - lcp(keys, n, i, i - 1)) >= 0 ? 1 : -1;
         const int dmin = lcp(keys, n, i, i - d);
@@ -139,6 +148,8 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, Node* __r
         for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
             if (lcp(keys, n, i, i + (l + t) * d) > dmin) l += t;
         const int64_t j = i + l * d;
+        const int64_t first = i < j ? i : j, last = i < j ? j : i;
+        if (i != 0 && last - first + 1 <= leaf_size) continue;  // inside a collapsed leaf
         const int dnode = lcp(keys, n, i, j);
         int64_t s = 0, t = l;
         do {
@@ -146,25 +157,27 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, Node* __r
             if (lcp(keys, n, i, i + (s + t) * d) > dnode) s += t;
         } while (t > 1);
         const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
-        const int64_t first = i < j ? i : j, last = i < j ? j : i;
-        int c0, c1;
-        if (first == gamma) {
-            c0 = ~(int)gamma;
-            parent_leaf[gamma] = (int)i;
-        } else {
-            c0 = (int)gamma;
-            parent_int[gamma] = (int)i;
+        int child[2];
+        int count[2] = {0, 0};
+        const int64_t cfirst[2] = {first, gamma + 1}, clast[2] = {gamma, last};
+        const int64_t cidx[2] = {gamma, gamma + 1};
+        for (int side = 0; side < 2; ++side) {
+            const int64_t size = clast[side] - cfirst[side] + 1;
+            if (size <= leaf_size) {
+                child[side] = ~(int)cfirst[side];
+                count[side] = (int)size;
+                leaf_rec[cfirst[side]] = ((unsigned long long)i << 9) | ((unsigned long long)side << 8) |
+                                         (unsigned long long)size;
+            } else {
+                child[side] = (int)cidx[side];
+                nodes[cidx[side]].ch.w = (int)(((uint32_t)i << 2) | ((uint32_t)side << 1));
+            }
         }
-        if (last == gamma + 1) {
-            c1 = ~(int)(gamma + 1);
-            parent_leaf[gamma + 1] = (int)i;
-        } else {
-            c1 = (int)(gamma + 1);
-            parent_int[gamma + 1] = (int)i;
-        }
-        nodes[i].ch = make_int4(c0, c1, 1, 1);
-        range[i] = make_int2((int)first, (int)last);
-        if (i == 0) parent_int[0] = -1;
+        Node* nd = nodes + i;
+        nd->ch.x = child[0];
+        nd->ch.y = child[1];
+        nd->ch.z = count[0] | (count[1] << 8);
+        if (i == 0) nd->ch.w = (int)(kRootParent << 2);
     }
 }
 
@@ -191,72 +204,72 @@ __device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], 
     hi[2] = __ldcg(bz + 2 * slot + 1);
 }
 
-// 6. refit; root box is written to root_box[0..5].  The child box goes to
-// L2 (st.cg), the arrival counter is an acquire-release device-scope atomic
-// (it orders the box store before the sibling's load without a full fence),
-// and the sibling box is read from L2 (ld.cg).
-__global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes, const int32_t* __restrict__ parent_int,
-                        const int32_t* __restrict__ parent_leaf, uint32_t* arrivals, float* root_box) {
+// 6. refit: one thread per leaf (a leaf_rec entry) computes the leaf box and
+// walks up.  At each node it stores its child box into its slot and flips the
+// node's arrival toggle with an acquire-release atomic; the second arrival
+// reads the sibling box, merges, and continues to the parent named in the
+// same atomic's result (no separate parent or counter arrays).
+__global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes,
+                        const unsigned long long* __restrict__ leaf_rec, float* root_box) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const float4 a = soup[3 * j], b = soup[3 * j + 1], c = soup[3 * j + 2];
-        float lo[3] = {fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z))};
-        float hi[3] = {fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z))};
-        int code = ~(int)j;
-        int node = parent_leaf[j];
-        while (node >= 0) {
+        const unsigned long long rec = leaf_rec[j];
+        if (rec == ~0ull) continue;  // not the first triangle of a leaf
+        const int count = (int)(rec & 0xFF);
+        int side = (int)((rec >> 8) & 1);
+        uint32_t node = (uint32_t)(rec >> 9);
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        for (int k = 0; k < count; ++k) {
+            for (int v = 0; v < 3; ++v) {
+                const float4 p = soup[3 * (j + k) + v];
+                lo[0] = fminf(lo[0], p.x);
+                lo[1] = fminf(lo[1], p.y);
+                lo[2] = fminf(lo[2], p.z);
+                hi[0] = fmaxf(hi[0], p.x);
+                hi[1] = fmaxf(hi[1], p.y);
+                hi[2] = fmaxf(hi[2], p.z);
+            }
+        }
+        for (;;) {
             Node* nd = nodes + node;
-            const int slot = (__ldcg(&nd->ch.x) == code) ? 0 : 1;
-            store_child_box(nd, slot, lo, hi);
-            cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrived(arrivals[node]);
-            if (arrived.fetch_add(1u, cuda::memory_order_acq_rel) == 0u) break;  // sibling continues upward
+            store_child_box(nd, side, lo, hi);
+            cuda::atomic_ref<int, cuda::thread_scope_device> word(nd->ch.w);
+            const uint32_t old = (uint32_t)word.fetch_xor(1, cuda::memory_order_acq_rel);
+            if ((old & 1u) == 0u) break;  // sibling not done yet; it continues upward
             float olo[3], ohi[3];
-            load_child_box(nd, 1 - slot, olo, ohi);
+            load_child_box(nd, 1 - side, olo, ohi);
             for (int k = 0; k < 3; ++k) {
                 lo[k] = fminf(lo[k], olo[k]);
                 hi[k] = fmaxf(hi[k], ohi[k]);
             }
-            code = node;
-            node = __ldcg(parent_int + node);
-            if (node < 0) {
+            const uint32_t parent = old >> 2;
+            if (parent == kRootParent) {
                 for (int k = 0; k < 3; ++k) {
                     root_box[k] = lo[k];
                     root_box[3 + k] = hi[k];
                 }
+                break;
             }
+            side = (int)((old >> 1) & 1u);
+            node = parent;
         }
     }
 }
 
-// single-triangle dataset: the root box is the triangle's box
-__global__ void k_single_box(const float4* __restrict__ soup, float* root_box) {
-    const float4 a = soup[0], b = soup[1], c = soup[2];
-    root_box[0] = fminf(a.x, fminf(b.x, c.x));
-    root_box[1] = fminf(a.y, fminf(b.y, c.y));
-    root_box[2] = fminf(a.z, fminf(b.z, c.z));
-    root_box[3] = fmaxf(a.x, fmaxf(b.x, c.x));
-    root_box[4] = fmaxf(a.y, fmaxf(b.y, c.y));
-    root_box[5] = fmaxf(a.z, fmaxf(b.z, c.z));
-}
-
-// 7. collapse small subtrees into leaves
-__global__ void k_collapse(Node* nodes, const int2* __restrict__ range, int64_t n, int leaf_size) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n - 1; i += (int64_t)gridDim.x * blockDim.x) {
-        int4 ch = nodes[i].ch;
-        if (ch.x >= 0) {
-            const int2 r = range[ch.x];
-            if (r.y - r.x + 1 <= leaf_size) {
-                ch.x = ~r.x;
-                ch.z = r.y - r.x + 1;
-            }
-        }
-        if (ch.y >= 0) {
-            const int2 r = range[ch.y];
-            if (r.y - r.x + 1 <= leaf_size) {
-                ch.y = ~r.x;
-                ch.w = r.y - r.x + 1;
-            }
-        }
-        nodes[i].ch = ch;
+// whole dataset in one leaf (n <= leaf_size): root box over all triangles
+__global__ void k_single_box(const float4* __restrict__ soup, int64_t n, float* root_box) {
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int64_t t = 0; t < 3 * n; ++t) {
+        const float4 p = soup[t];
+        lo[0] = fminf(lo[0], p.x);
+        lo[1] = fminf(lo[1], p.y);
+        lo[2] = fminf(lo[2], p.z);
+        hi[0] = fmaxf(hi[0], p.x);
+        hi[1] = fmaxf(hi[1], p.y);
+        hi[2] = fmaxf(hi[2], p.z);
+    }
+    for (int k = 0; k < 3; ++k) {
+        root_box[k] = lo[k];
+        root_box[3 + k] = hi[k];
     }
 }
 
@@ -378,6 +391,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     if (leaf_size < 1) leaf_size = 1;
     if (leaf_size > 16) leaf_size = 16;
     shape->leaf_size = leaf_size;
+    if (n >= (int64_t(1) << 30))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "bvh build: at most 2^30 - 1 triangles per hierarchy");
     if (n == 0) {
         shape->root_is_leaf = 1;
         shape->root_leaf_count = 0;
@@ -386,23 +401,18 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
             for (int k = 0; k < 6; ++k) root_box[k] = 0.0f;
         return PIERCE_OK;
     }
-    // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 parents/range/arrivals/bounds
+    // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 leaf records + bounds
     void *pc = nullptr, *pk = nullptr, *pv = nullptr, *pm = nullptr;
     if (int s = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc)) return s;
     if (int s = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk)) return s;
     if (int s = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv)) return s;
-    const size_t misc_bytes =
-        sizeof(int32_t) * (size_t)(n + n) + sizeof(int2) * (size_t)n + sizeof(uint32_t) * (size_t)n + 64;
-    if (int s = scratch(ctx, 4, misc_bytes, &pm)) return s;
+    if (int s = scratch(ctx, 4, sizeof(unsigned long long) * (size_t)n + 64, &pm)) return s;
     float4* cen = static_cast<float4*>(pc);
     uint32_t* keys = static_cast<uint32_t*>(pk);
     uint32_t* vals = static_cast<uint32_t*>(pv);
-    int32_t* parent_int = static_cast<int32_t*>(pm);
-    int32_t* parent_leaf = parent_int + n;
-    int2* range = reinterpret_cast<int2*>(parent_leaf + n);
-    uint32_t* arrivals = reinterpret_cast<uint32_t*>(range + n);
-    uint32_t* bounds = arrivals + n;                            // 6 words
-    float* d_root_box = reinterpret_cast<float*>(bounds + 6);  // 6 floats
+    unsigned long long* leaf_rec = static_cast<unsigned long long*>(pm);
+    uint32_t* bounds = reinterpret_cast<uint32_t*>(leaf_rec + n);  // 6 words
+    float* d_root_box = reinterpret_cast<float*>(bounds + 6);        // 6 floats
 
     const int B = 256;
     k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
@@ -415,24 +425,20 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     const uint32_t* order = vals + n;
     k_soup<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, t2o, list, order, n, soup);
     ctx->launches += 1;
-    if (n == 1) {
-        k_single_box<<<1, 1, 0, st>>>(soup, d_root_box);
+    if (n <= leaf_size) {
+        k_single_box<<<1, 1, 0, st>>>(soup, n, d_root_box);
         ctx->launches += 1;
         shape->root_is_leaf = 1;
-        shape->root_leaf_count = 1;
+        shape->root_leaf_count = (int)n;
         shape->num_nodes = 0;
     } else {
-        cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * (size_t)n, st);
-        k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, nodes, parent_int, parent_leaf, range);
-        k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, parent_int, parent_leaf, arrivals, d_root_box);
+        cudaMemsetAsync(leaf_rec, 0xFF, sizeof(unsigned long long) * (size_t)n, st);
+        k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec);
+        k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, d_root_box);
         ctx->launches += 2;
-        if (leaf_size > 1) {
-            k_collapse<<<grid_for(ctx, n - 1, B), B, 0, st>>>(nodes, range, n, leaf_size);
-            ctx->launches += 1;
-        }
         shape->num_nodes = (uint64_t)(n - 1);
-        shape->root_is_leaf = (n <= leaf_size) ? 1 : 0;
-        shape->root_leaf_count = (n <= leaf_size) ? (int)n : 0;
+        shape->root_is_leaf = 0;
+        shape->root_leaf_count = 0;
     }
     if (int s = check_cuda(cudaGetLastError(), "bvh build kernels")) return s;
     if (root_box) {
