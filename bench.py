@@ -209,7 +209,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full workload (debug only)")
     ap.add_argument("--cpu-sample-objects", type=int, default=3000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--leaf-size", type=int, default=1)
+    ap.add_argument("--leaf-size", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

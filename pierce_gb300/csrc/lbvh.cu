@@ -204,54 +204,114 @@ __device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], 
     hi[2] = __ldcg(bz + 2 * slot + 1);
 }
 
-// 6. refit: one thread per leaf (a leaf_rec entry) computes the leaf box and
-// walks up.  At each node it stores its child box into its slot and flips the
-// node's arrival toggle with an acquire-release atomic; the second arrival
-// reads the sibling box, merges, and continues to the parent named in the
-// same atomic's result (no separate parent or counter arrays).
-__global__ void k_refit(const float4* __restrict__ soup, int64_t n, Node* nodes,
-                        const unsigned long long* __restrict__ leaf_rec, float* root_box) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long rec = leaf_rec[j];
-        if (rec == ~0ull) continue;  // not the first triangle of a leaf
-        const int count = (int)(rec & 0xFF);
-        int side = (int)((rec >> 8) & 1);
-        uint32_t node = (uint32_t)(rec >> 9);
-        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-        for (int k = 0; k < count; ++k) {
-            for (int v = 0; v < 3; ++v) {
-                const float4 p = soup[3 * (j + k) + v];
-                lo[0] = fminf(lo[0], p.x);
-                lo[1] = fminf(lo[1], p.y);
-                lo[2] = fminf(lo[2], p.z);
-                hi[0] = fmaxf(hi[0], p.x);
-                hi[1] = fmaxf(hi[1], p.y);
-                hi[2] = fmaxf(hi[2], p.z);
+// 6. refit in waves.  The leaf wave computes each leaf's box, stores it in
+// its parent's child slot and flips the parent's arrival toggle; the second
+// arrival appends the parent to a list.  Each following wave takes the list
+// of nodes whose two child slots are complete, merges them, stores the
+// result in the grandparent and appends it the same way.  A node is only
+// read in the wave after the one that completed it, so kernel boundaries
+// order the box stores and loads and the toggle needs no memory fence; every
+// wave runs full warps.  The number of waves is the tree height (<= 64).
+__device__ __forceinline__ void block_append(bool has, uint32_t value, uint32_t* out, unsigned long long* count) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ unsigned long long base;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
+    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, has);
+    if (lane == 0) warp_tot[wid] = __popc(ballot);
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = lane < nwarps ? warp_tot[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, off);
+            if (lane >= off) w += v;
+        }
+        if (lane < nwarps) warp_tot[lane] = w;
+        if (lane == 31) base = w ? atomicAdd(count, (unsigned long long)w) : 0ull;
+    }
+    __syncthreads();
+    if (has) out[base + (wid ? warp_tot[wid - 1] : 0u) + __popc(ballot & ((1u << lane) - 1u))] = value;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void write_slot(Node* nd, int slot, const float lo[3], const float hi[3]) {
+    float* bx = reinterpret_cast<float*>(&nd->bx);
+    float* by = reinterpret_cast<float*>(&nd->by);
+    float* bz = reinterpret_cast<float*>(&nd->bz);
+    bx[2 * slot] = lo[0];
+    bx[2 * slot + 1] = hi[0];
+    by[2 * slot] = lo[1];
+    by[2 * slot + 1] = hi[1];
+    bz[2 * slot] = lo[2];
+    bz[2 * slot + 1] = hi[2];
+}
+
+// Store a finished box into node `node`'s slot `side`; true when this was the
+// second arrival (the node is then complete).
+__device__ __forceinline__ bool deliver(Node* nodes, uint32_t node, int side, const float lo[3], const float hi[3]) {
+    Node* nd = nodes + node;
+    write_slot(nd, side, lo, hi);
+    return (atomicXor(reinterpret_cast<unsigned int*>(&nd->ch.w), 1u) & 1u) != 0u;
+}
+
+__global__ void __launch_bounds__(256) k_refit_leaves(const float4* __restrict__ soup, int64_t n, Node* nodes,
+                                                      const unsigned long long* __restrict__ leaf_rec,
+                                                      uint32_t* list_out, unsigned long long* count_out) {
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        bool done = false, bad_leaf = false;
+        uint32_t node = 0;
+        if (j < n) {
+            const unsigned long long rec = leaf_rec[j];
+            if (rec != ~0ull) {
+                const int count = (int)(rec & 0xFF);
+                const int side = (int)((rec >> 8) & 1);
+                node = (uint32_t)(rec >> 9);
+                float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+                if ((int64_t)node >= n - 1 || j + count > n) bad_leaf = true;
+                for (int k = 0; k < count && !bad_leaf; ++k)
+                    for (int v = 0; v < 3; ++v) {
+                        const float4 p = soup[3 * (j + k) + v];
+                        lo[0] = fminf(lo[0], p.x);
+                        lo[1] = fminf(lo[1], p.y);
+                        lo[2] = fminf(lo[2], p.z);
+                        hi[0] = fmaxf(hi[0], p.x);
+                        hi[1] = fmaxf(hi[1], p.y);
+                        hi[2] = fmaxf(hi[2], p.z);
+                    }
+                if (!bad_leaf) done = deliver(nodes, node, side, lo, hi);
             }
         }
-        for (;;) {
-            Node* nd = nodes + node;
-            store_child_box(nd, side, lo, hi);
-            cuda::atomic_ref<int, cuda::thread_scope_device> word(nd->ch.w);
-            const uint32_t old = (uint32_t)word.fetch_xor(1, cuda::memory_order_acq_rel);
-            if ((old & 1u) == 0u) break;  // sibling not done yet; it continues upward
-            float olo[3], ohi[3];
-            load_child_box(nd, 1 - side, olo, ohi);
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = fminf(lo[k], olo[k]);
-                hi[k] = fmaxf(hi[k], ohi[k]);
-            }
-            const uint32_t parent = old >> 2;
+        block_append(done, node, list_out, count_out);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_refit_wave(Node* nodes, int64_t num_nodes, const uint32_t* __restrict__ list_in,
+                                                    const unsigned long long* __restrict__ count_in, int64_t list_cap,
+                                                    uint32_t* list_out, unsigned long long* count_out,
+                                                    float* root_box) {
+    int64_t n = (int64_t)*count_in;
+    if (n > list_cap) n = list_cap;  // never read past the list
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        bool done = false;
+        uint32_t parent = 0;
+        if (i < n && (int64_t)list_in[i] < num_nodes) {
+            const Node* nd = nodes + list_in[i];
+            const float4 bx = nd->bx, by = nd->by, bz = nd->bz;
+            const uint32_t w = (uint32_t)nd->ch.w;
+            const float lo[3] = {fminf(bx.x, bx.z), fminf(by.x, by.z), fminf(bz.x, bz.z)};
+            const float hi[3] = {fmaxf(bx.y, bx.w), fmaxf(by.y, by.w), fmaxf(bz.y, bz.w)};
+            parent = w >> 2;
             if (parent == kRootParent) {
                 for (int k = 0; k < 3; ++k) {
                     root_box[k] = lo[k];
                     root_box[3 + k] = hi[k];
                 }
-                break;
+            } else if ((int64_t)parent < num_nodes) {
+                done = deliver(nodes, parent, (int)((w >> 1) & 1u), lo, hi);
             }
-            side = (int)((old >> 1) & 1u);
-            node = parent;
         }
+        block_append(done, parent, list_out, count_out);
     }
 }
 
@@ -406,13 +466,16 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     if (int s = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc)) return s;
     if (int s = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk)) return s;
     if (int s = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv)) return s;
-    if (int s = scratch(ctx, 4, sizeof(unsigned long long) * (size_t)n + 64, &pm)) return s;
+    if (int s = scratch(ctx, 4, sizeof(unsigned long long) * (size_t)n + 64 + 64, &pm)) return s;
     float4* cen = static_cast<float4*>(pc);
     uint32_t* keys = static_cast<uint32_t*>(pk);
     uint32_t* vals = static_cast<uint32_t*>(pv);
     unsigned long long* leaf_rec = static_cast<unsigned long long*>(pm);
     uint32_t* bounds = reinterpret_cast<uint32_t*>(leaf_rec + n);  // 6 words
     float* d_root_box = reinterpret_cast<float*>(bounds + 6);        // 6 floats
+    // byte layout after the n leaf records: bounds [8n, 8n+24), root box
+    // [8n+24, 8n+48), two wave counters [8n+64, 8n+80); allocation 8n+128
+    unsigned long long* wave_count = leaf_rec + n + 8;
 
     const int B = 256;
     k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
@@ -434,8 +497,29 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     } else {
         cudaMemsetAsync(leaf_rec, 0xFF, sizeof(unsigned long long) * (size_t)n, st);
         k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec);
-        k_refit<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, d_root_box);
+        // wave lists reuse the Morton key buffer (free after the hierarchy step)
+        uint32_t* lists[2] = {keys, keys + (n + 1) / 2 + 1};
+        cudaMemsetAsync(wave_count, 0, 2 * sizeof(unsigned long long), st);
+        k_refit_leaves<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, lists[0], wave_count);
         ctx->launches += 2;
+        // waves until the root is reached: at most one per tree level, and a
+        // Karras tree over 30-bit codes split by 32-bit indices has < 64 levels
+        bool finished = false;
+        for (int wave = 0; wave < 64 && !finished; ++wave) {
+            const int in = wave & 1, out = in ^ 1;
+            cudaMemsetAsync(wave_count + out, 0, sizeof(unsigned long long), st);
+            k_refit_wave<<<grid_for(ctx, n / 2 + 1, B), B, 0, st>>>(nodes, n - 1, lists[in], wave_count + in,
+                                                                       n / 2 + 1, lists[out], wave_count + out,
+                                                                       d_root_box);
+            ctx->launches += 1;
+            if ((wave & 7) == 7) {
+                unsigned long long left = 0;
+                cudaMemcpyAsync(&left, wave_count + out, sizeof(left), cudaMemcpyDeviceToHost, st);
+                if (int s = check_cuda(cudaStreamSynchronize(st), "refit waves")) return s;
+                finished = left == 0;
+            }
+        }
+        if (!finished) return set_error(PIERCE_ERR_CUDA, "bvh refit did not reach the root in 64 waves");
         shape->num_nodes = (uint64_t)(n - 1);
         shape->root_is_leaf = 0;
         shape->root_leaf_count = 0;
