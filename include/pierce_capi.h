@@ -59,6 +59,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "pierce_instance.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -207,6 +209,16 @@ int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_
  * bounding-volume hierarchy (tuning may be NULL for defaults). */
 int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* view, int memory,
                           const pierce_tuning* tuning, pierce_dataset** out);
+/* Generated datasets (no counterpart in the reference, whose datasets are
+ * OBJ files): expand num_meshes instanced icosphere meshes (host array,
+ * pierce_instance.h) directly into device memory, mesh m = object m, edges in
+ * template order; bit-identical to the host's pierce_expand_instances. */
+int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mesh_instance* meshes, int32_t num_meshes,
+                                    const pierce_tuning* tuning, pierce_dataset** out);
+/* Copy a dataset's arrays back to host memory (sizes from
+ * pierce_dataset_info_get; any pointer may be NULL).  Synchronous. */
+int pierce_dataset_download(pierce_ctx* ctx, const pierce_dataset* ds, float* vertices, uint32_t* indices,
+                            int32_t* tri_to_object, float* edge_starts, float* edge_ends, int32_t* edge_src);
 /* Rebuild the hierarchy (e.g. with another leaf size). */
 int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
 int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out);

@@ -26,6 +26,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "pierce_instance.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -127,6 +129,27 @@ int pierce_gen_ellipsoid_pair(uint64_t seed_a, uint64_t seed_b,
 int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris,
                      double step, double branch_prob, double r_lo, double r_hi,
                      int32_t n_sides, double lo, double hi, pierce_geom** out);
+
+/* Unit icosphere template: counts[0..2] = vertices, triangles, unique edges;
+ * any output array may be NULL (query counts first). vertices: 3 doubles each,
+ * tris: 3 indices each, edges: 2 indices each (first-seen orientation). */
+int pierce_icosphere_template(int32_t level, double* vertices, uint32_t* tris, uint32_t* edges, int64_t* counts);
+
+/* Per-mesh parameters of an instanced dataset (pierce_instance.h).
+ * family 0: spheres, radius exp(p0 + p1 * N(0,1)) (p0 = ln mu, p1 = sigma),
+ *           drawing the same random stream as pierce_gen_icospheres;
+ * family 1: ellipsoids, semi-axes U[p0, p1], uniform random rotation,
+ *           radial value noise of relative amplitude noise_amp, drawing the
+ *           same stream as side A of pierce_gen_ellipsoid_pair.
+ * Centres uniform in [lo, hi]^3; level uniform in [level_lo, level_hi]
+ * (no draw when they are equal). */
+int pierce_gen_instances(uint64_t seed, int32_t num_meshes, int32_t family, int32_t level_lo, int32_t level_hi,
+                         double p0, double p1, double noise_amp, double lo, double hi,
+                         pierce_mesh_instance* out);
+
+/* Host expansion of instanced meshes (mesh m = object m); edges are each
+ * mesh's unique template edges in template order. */
+int pierce_expand_instances(const pierce_mesh_instance* meshes, int32_t num_meshes, pierce_geom** out);
 
 /* Concatenate b onto a (object ids of b shifted by a's object count). */
 int pierce_geom_append(pierce_geom* a, const pierce_geom* b);

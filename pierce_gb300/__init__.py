@@ -6,6 +6,8 @@ library ``libpierce_gb300.so`` (sm_103a) reached through its C ABI
 (``include/pierce_capi.h``); the `.pre` format, edge extraction and the
 seeded generators live in ``libpierce_host.so`` (``include/pierce_host.h``).
 """
-from .geometry import Geometry, icospheres, ellipsoid_pair, tubes  # noqa: F401
+from .geometry import (Geometry, icospheres, ellipsoid_pair, tubes, instances, expand_instances,  # noqa: F401
+                       SPHERES, ELLIPSOIDS)
 
-__all__ = ["Geometry", "icospheres", "ellipsoid_pair", "tubes"]
+__all__ = ["Geometry", "icospheres", "ellipsoid_pair", "tubes", "instances", "expand_instances", "SPHERES",
+           "ELLIPSOIDS"]

@@ -32,7 +32,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["pre_io.cpp", "edges.cpp", "generators.cpp", "host_capi.cpp"]
-CUDA_SOURCES = ["lbvh.cu", "join.cu", "sortscan.cu", "capi.cu", "noalloc.cu"]
+CUDA_SOURCES = ["lbvh.cu", "join.cu", "sortscan.cu", "capi.cu", "instanced.cu", "noalloc.cu"]
 APP_COMMON = ["cli.cpp", "timer.cpp", "app_common.cpp"]
 APPS = ["pierce_overlap", "pierce_overlap_two_pass", "pierce_intersection",
         "pierce_containment", "pierce_preprocess"]
@@ -55,7 +55,8 @@ def _newer(target: Path, deps: list[Path]) -> bool:
 
 
 def _headers(directory: Path) -> list[Path]:
-    return sorted(directory.glob("*.h")) + sorted(directory.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+    return (sorted(directory.glob("*.h")) + sorted(directory.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+            + sorted((PKG / "host").glob("*.h")))
 
 
 def _compile_host(src: Path) -> Path:
@@ -68,7 +69,7 @@ def _compile_host(src: Path) -> Path:
 def _compile_cuda(src: Path) -> Path:
     obj = OBJ / (src.stem + ".cu.o")
     if not _newer(obj, [src] + _headers(src.parent)):
-        _run([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        _run([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
     return obj
 

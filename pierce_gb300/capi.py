@@ -10,6 +10,8 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
+
 from . import native
 
 V = C.c_void_p
@@ -47,6 +49,13 @@ class MeshView(C.Structure):
     _fields_ = [("vertices", V), ("num_vertices", U64), ("indices", V), ("num_triangles", U64),
                 ("tri_to_object", V), ("edge_starts", V), ("edge_ends", V), ("edge_src", V),
                 ("num_edges", U64), ("num_objects", I32)]
+
+
+# pierce_mesh_instance (pierce_instance.h), as a numpy record type.
+INSTANCE_DTYPE = np.dtype([("center", "<f8", (3,)), ("axes", "<f8", (3,)), ("rotation", "<f8", (9,)),
+                           ("noise_amp", "<f8"), ("noise_offset", "<f8", (3,)), ("noise_seed", "<u8"),
+                           ("level", "<i4"), ("reserved", "<i4")])
+assert INSTANCE_DTYPE.itemsize == 168
 
 
 class Tuning(C.Structure):
@@ -99,6 +108,8 @@ SIGNATURES = {
     "pierce_device_memory": (C.c_int, [V, C.POINTER(U64), C.POINTER(U64)]),
     "pierce_dataset_create": (C.c_int, [V, C.POINTER(MeshView), C.c_int, C.POINTER(Tuning), C.POINTER(V)]),
     "pierce_dataset_build": (C.c_int, [V, V, C.POINTER(Tuning)]),
+    "pierce_dataset_create_instanced": (C.c_int, [V, V, I32, C.POINTER(Tuning), C.POINTER(V)]),
+    "pierce_dataset_download": (C.c_int, [V, V, V, V, V, V, V, V]),
     "pierce_dataset_info_get": (C.c_int, [V, C.POINTER(DatasetInfo)]),
     "pierce_dataset_destroy": (None, [V]),
     "pierce_join": (C.c_int, [V, V, V, C.POINTER(JoinOpts), C.POINTER(V), C.POINTER(Stats)]),

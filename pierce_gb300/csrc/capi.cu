@@ -192,7 +192,40 @@ struct EventTimer {
     }
 };
 
+// ------------------------------------------------- dataset construction --
+
+namespace pgpu {
+
+int dataset_alloc(pierce_dataset* ds) {
+    const int32_t nobj = ds->num_objects;
+    const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
+    if (int s = device_alloc((void**)&ds->d_vertices, vb, "vertices")) return s;
+    if (int s = device_alloc((void**)&ds->d_indices, ib, "indices")) return s;
+    if (int s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object")) return s;
+    if (int s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges")) return s;
+    if (int s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources")) return s;
+    if (int s = device_alloc((void**)&ds->d_soup, 48 * ds->nt, "triangle soup")) return s;
+    if (int s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))
+        return s;
+    if (int s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices")) return s;
+    if (int s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes")) return s;
+    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
+    return PIERCE_OK;
+}
+
+int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning) {
+    if (int s = prepare_objects(ctx, ds)) return s;
+    pierce_tuning t;
+    pierce_default_tuning(&t);
+    if (tuning) t = *tuning;
+    if (t.defer_build) return sync_ctx(ctx, "dataset upload");
+    return build_bvh(ctx, ds, t.leaf_size);
+}
+
+}  // namespace pgpu
+
 // ------------------------------------------------------------------ C ABI --
+
 extern "C" {
 
 const char* pierce_last_error(void) { return g_err; }
@@ -366,17 +399,8 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
             }
         }
         ds->num_objects = nobj;
+        if ((s = dataset_alloc(ds))) break;
         const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
-        if ((s = device_alloc((void**)&ds->d_vertices, vb, "vertices"))) break;
-        if ((s = device_alloc((void**)&ds->d_indices, ib, "indices"))) break;
-        if ((s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object"))) break;
-        if ((s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges"))) break;
-        if ((s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources"))) break;
-        if ((s = device_alloc((void**)&ds->d_soup, 48 * ds->nt, "triangle soup"))) break;
-        if ((s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))) break;
-        if ((s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices"))) break;
-        if ((s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes"))) break;
-        ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
         if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, st), "copy vertices"))) break;
         if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, st), "copy indices"))) break;
         if (ob && (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, st), "copy t2o")))
@@ -395,21 +419,55 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
             ctx->launches += 1;
             if ((s = check_cuda(cudaGetLastError(), "pack edges"))) break;
         }
-        if ((s = prepare_objects(ctx, ds))) break;
-        pierce_tuning t;
-        pierce_default_tuning(&t);
-        if (tuning) t = *tuning;
-        if (t.defer_build) {
-            if ((s = sync_ctx(ctx, "dataset upload"))) break;
-        } else if ((s = build_bvh(ctx, ds, t.leaf_size))) {
-            break;
-        }
+        if ((s = dataset_finish(ctx, ds, tuning))) break;
     } while (0);
     if (s) {
         pierce_dataset_destroy(ds);
         return s;
     }
     *out = ds;
+    return PIERCE_OK;
+}
+
+int pierce_dataset_download(pierce_ctx* ctx, const pierce_dataset* ds, float* vertices, uint32_t* indices,
+                            int32_t* tri_to_object, float* edge_starts, float* edge_ends, int32_t* edge_src) {
+    if (!ctx || !ds) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_download: null argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    const cudaMemcpyKind d2h = cudaMemcpyDeviceToHost;
+    if (vertices && ds->nv)
+        if (int s = check_cuda(cudaMemcpyAsync(vertices, ds->d_vertices, 12 * ds->nv, d2h, st), "download vertices"))
+            return s;
+    if (indices && ds->nt)
+        if (int s = check_cuda(cudaMemcpyAsync(indices, ds->d_indices, 12 * ds->nt, d2h, st), "download indices"))
+            return s;
+    if (tri_to_object && ds->nt)
+        if (int s = check_cuda(cudaMemcpyAsync(tri_to_object, ds->d_tri_to_object, 4 * ds->nt, d2h, st),
+                               "download t2o"))
+            return s;
+    if (edge_src && ds->ne)
+        if (int s = check_cuda(cudaMemcpyAsync(edge_src, ds->d_edge_src, 4 * ds->ne, d2h, st), "download edge src"))
+            return s;
+    std::vector<float4> packed;
+    if ((edge_starts || edge_ends) && ds->ne) {
+        packed.resize(2 * ds->ne);
+        if (int s = check_cuda(cudaMemcpyAsync(packed.data(), ds->d_edges, 32 * ds->ne, d2h, st), "download edges"))
+            return s;
+    }
+    if (int s = sync_ctx(ctx, "dataset download")) return s;
+    for (uint64_t i = 0; i < (packed.empty() ? 0 : ds->ne); ++i) {
+        const float4 a = packed[2 * i], b = packed[2 * i + 1];
+        if (edge_starts) {
+            edge_starts[3 * i] = a.x;
+            edge_starts[3 * i + 1] = a.y;
+            edge_starts[3 * i + 2] = a.z;
+        }
+        if (edge_ends) {
+            edge_ends[3 * i] = b.x;
+            edge_ends[3 * i + 1] = b.y;
+            edge_ends[3 * i + 2] = b.z;
+        }
+    }
     return PIERCE_OK;
 }
 

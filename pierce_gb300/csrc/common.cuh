@@ -161,6 +161,10 @@ int check_cuda(cudaError_t e, const char* what);
 // grow-only scratch buffer `slot` of at least `bytes`
 int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out);
 int device_alloc(void** p, size_t bytes, const char* what);
+// allocate a dataset's arrays for ds->nv/nt/ne/num_objects (capi.cu)
+int dataset_alloc(pierce_dataset* ds);
+// object data, then the BVH unless tuning->defer_build (capi.cu)
+int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
 
 // lbvh.cu
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);

@@ -215,6 +215,39 @@ def tubes(seed: int, num_meshes: int, target_tris: int = 200_000, step: float = 
     return Geometry(h)
 
 
+SPHERES, ELLIPSOIDS = 0, 1
+
+
+def instances(seed: int, num_meshes: int, family: int = SPHERES, level_lo: int = 3, level_hi: int | None = None,
+              p0: float | None = None, p1: float | None = None, noise_amp: float = 0.05, lo: float = 0.0,
+              hi: float = 200.0) -> np.ndarray:
+    """Per-mesh parameters of an instanced dataset (``pierce_instance.h``).
+
+    Spheres: radius exp(p0 + p1 N(0,1)) (defaults ln 1.5, 0.3); ellipsoids:
+    semi-axes U[p0, p1] (defaults 2, 5), random rotation, radial value noise.
+    Returns a record array of dtype :data:`capi.INSTANCE_DTYPE`."""
+    from .capi import INSTANCE_DTYPE
+    level_hi = level_lo if level_hi is None else level_hi
+    if p0 is None:
+        p0 = float(np.log(1.5)) if family == SPHERES else 2.0
+    if p1 is None:
+        p1 = 0.3 if family == SPHERES else 5.0
+    out = np.zeros(num_meshes, dtype=INSTANCE_DTYPE)
+    _check(native.host().pierce_gen_instances(C.c_uint64(seed), num_meshes, family, level_lo, level_hi,
+                                              C.c_double(p0), C.c_double(p1), C.c_double(noise_amp),
+                                              C.c_double(lo), C.c_double(hi), out.ctypes.data), "gen_instances")
+    return out
+
+
+def expand_instances(inst: np.ndarray) -> Geometry:
+    """Host expansion of instanced meshes (edges in template order)."""
+    from .capi import INSTANCE_DTYPE
+    inst = np.ascontiguousarray(inst, dtype=INSTANCE_DTYPE)
+    h = C.c_void_p()
+    _check(native.host().pierce_expand_instances(inst.ctypes.data, len(inst), C.byref(h)), "expand_instances")
+    return Geometry(h)
+
+
 def write_pre_bytes(geom: Geometry, path: Path) -> bytes:
     geom.write_pre(path)
     return Path(path).read_bytes()

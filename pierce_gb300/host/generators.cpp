@@ -26,6 +26,8 @@
 
 #include "detmath.h"
 #include "geometry.h"
+#include "icosphere.h"
+#include "instance_math.h"
 
 namespace {
 
@@ -49,70 +51,13 @@ struct Template {
     std::vector<uint32_t> tris;     // 3 per triangle, outward CCW
 };
 
-// Icosahedron vertices (+-1, +-phi, 0) and cyclic permutations, with the
-// usual 20 outward-oriented faces, then midpoint subdivision.
 Template make_icosphere(int level) {
-    const double phi = (1.0 + std::sqrt(5.0)) / 2.0;
+    const pierce::inst::IcoTemplate h = pierce::inst::make_icosphere_template(level);
     Template t;
-    const double raw[12][3] = {{-1, phi, 0}, {1, phi, 0},  {-1, -phi, 0}, {1, -phi, 0},
-                               {0, -1, phi}, {0, 1, phi},  {0, -1, -phi}, {0, 1, -phi},
-                               {phi, 0, -1}, {phi, 0, 1},  {-phi, 0, -1}, {-phi, 0, 1}};
-    for (auto& r : raw) t.verts.push_back(normalize({r[0], r[1], r[2]}));
-    const uint32_t faces[20][3] = {{0, 11, 5}, {0, 5, 1},  {0, 1, 7},   {0, 7, 10}, {0, 10, 11},
-                                   {1, 5, 9},  {5, 11, 4}, {11, 10, 2}, {10, 7, 6}, {7, 1, 8},
-                                   {3, 9, 4},  {3, 4, 2},  {3, 2, 6},   {3, 6, 8},  {3, 8, 9},
-                                   {4, 9, 5},  {2, 4, 11}, {6, 2, 10},  {8, 6, 7},  {9, 8, 1}};
-    for (auto& f : faces) t.tris.insert(t.tris.end(), f, f + 3);
-    for (int l = 0; l < level; ++l) {
-        std::map<std::pair<uint32_t, uint32_t>, uint32_t> mid;
-        auto midpoint = [&](uint32_t a, uint32_t b) -> uint32_t {
-            auto key = std::make_pair(std::min(a, b), std::max(a, b));
-            auto it = mid.find(key);
-            if (it != mid.end()) return it->second;
-            V3 m = normalize(mul(add(t.verts[a], t.verts[b]), 0.5));
-            uint32_t id = (uint32_t)t.verts.size();
-            t.verts.push_back(m);
-            mid.emplace(key, id);
-            return id;
-        };
-        std::vector<uint32_t> nt;
-        nt.reserve(t.tris.size() * 4);
-        for (size_t i = 0; i < t.tris.size(); i += 3) {
-            uint32_t a = t.tris[i], b = t.tris[i + 1], c = t.tris[i + 2];
-            uint32_t ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
-            const uint32_t add4[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
-            nt.insert(nt.end(), add4, add4 + 12);
-        }
-        t.tris.swap(nt);
-    }
+    for (size_t i = 0; i < h.v.size(); i += 3) t.verts.push_back({h.v[i], h.v[i + 1], h.v[i + 2]});
+    t.tris = h.t;
     return t;
 }
-
-// Smooth value noise in [-1, 1]: hashed lattice values, trilinear
-// interpolation with smoothstep weights.
-struct ValueNoise {
-    uint64_t seed;
-    double lattice(int64_t i, int64_t j, int64_t k) const {
-        uint64_t h = seed ^ ((uint64_t)i * 0x9E3779B97F4A7C15ULL) ^ ((uint64_t)j * 0xC2B2AE3D27D4EB4FULL) ^
-                     ((uint64_t)k * 0x165667B19E3779F9ULL);
-        h = Rng::splitmix(h);
-        return (double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
-    }
-    static double smooth(double t) { return t * t * (3.0 - 2.0 * t); }
-    double operator()(V3 p) const {
-        double fx = std::floor(p.x), fy = std::floor(p.y), fz = std::floor(p.z);
-        int64_t i = (int64_t)fx, j = (int64_t)fy, k = (int64_t)fz;
-        double u = smooth(p.x - fx), v = smooth(p.y - fy), w = smooth(p.z - fz);
-        double c000 = lattice(i, j, k), c100 = lattice(i + 1, j, k);
-        double c010 = lattice(i, j + 1, k), c110 = lattice(i + 1, j + 1, k);
-        double c001 = lattice(i, j, k + 1), c101 = lattice(i + 1, j, k + 1);
-        double c011 = lattice(i, j + 1, k + 1), c111 = lattice(i + 1, j + 1, k + 1);
-        double x00 = c000 + (c100 - c000) * u, x10 = c010 + (c110 - c010) * u;
-        double x01 = c001 + (c101 - c001) * u, x11 = c011 + (c111 - c011) * u;
-        double y0 = x00 + (x10 - x00) * v, y1 = x01 + (x11 - x01) * v;
-        return y0 + (y1 - y0) * w;
-    }
-};
 
 struct Rot {
     double m[9];
@@ -172,20 +117,32 @@ void append_mesh(pierce_geom& g, const Template& t, const std::vector<float>& po
     g.tri_to_object.insert(g.tri_to_object.end(), t.tris.size() / 3, obj);
 }
 
-void ellipsoid_positions(const Template& t, const EllipsoidParams& p, double noise_amp, std::vector<float>& out) {
-    const double freq = 1.5;
-    ValueNoise vn{p.noise_seed};
+pierce_mesh_instance to_instance(const EllipsoidParams& p, double noise_amp, int level) {
+    pierce_mesh_instance m{};
+    m.center[0] = p.center.x;
+    m.center[1] = p.center.y;
+    m.center[2] = p.center.z;
+    m.axes[0] = p.ax;
+    m.axes[1] = p.ay;
+    m.axes[2] = p.az;
+    for (int k = 0; k < 9; ++k) m.rotation[k] = p.rot.m[k];
+    m.noise_amp = noise_amp;
+    m.noise_offset[0] = p.noise_offset.x;
+    m.noise_offset[1] = p.noise_offset.y;
+    m.noise_offset[2] = p.noise_offset.z;
+    m.noise_seed = p.noise_seed;
+    m.level = level;
+    return m;
+}
+
+void instance_positions(const Template& t, const pierce_mesh_instance& m, std::vector<float>& out) {
     out.resize(3 * t.verts.size());
-    for (size_t i = 0; i < t.verts.size(); ++i) {
-        V3 d = t.verts[i];
-        double n = vn(add(mul(d, freq), p.noise_offset));
-        double f = 1.0 + noise_amp * n;
-        V3 local = {p.ax * d.x * f, p.ay * d.y * f, p.az * d.z * f};
-        V3 w = add(p.center, p.rot.apply(local));
-        out[3 * i + 0] = (float)w.x;
-        out[3 * i + 1] = (float)w.y;
-        out[3 * i + 2] = (float)w.z;
-    }
+    for (size_t i = 0; i < t.verts.size(); ++i)
+        pierce::inst::instance_vertex(m, t.verts[i].x, t.verts[i].y, t.verts[i].z, &out[3 * i]);
+}
+
+void ellipsoid_positions(const Template& t, const EllipsoidParams& p, double noise_amp, std::vector<float>& out) {
+    instance_positions(t, to_instance(p, noise_amp, 0), out);
 }
 
 void finish(pierce_geom& g) {
@@ -258,6 +215,33 @@ void sweep_branch(pierce_geom& g, const std::vector<V3>& pts, double radius, int
 }
 
 }  // namespace
+
+// Unit icosphere template of one subdivision level: vertices (double xyz),
+// triangles and the unique undirected edges (each once, first-seen
+// orientation, in first-seen order).  Used to expand instanced datasets on
+// the device.
+extern "C" int pierce_icosphere_template(int32_t level, double* vertices, uint32_t* tris, uint32_t* edges,
+                                         int64_t* counts) {
+    if (level < 0 || level > 8 || !counts) {
+        pierce::set_last_error("icosphere_template: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    const pierce::inst::IcoTemplate h = pierce::inst::make_icosphere_template(level);
+    Template t = make_icosphere(level);
+    const std::vector<uint32_t>& e = h.e;
+    counts[0] = (int64_t)t.verts.size();
+    counts[1] = (int64_t)(t.tris.size() / 3);
+    counts[2] = (int64_t)(e.size() / 2);
+    if (vertices)
+        for (size_t i = 0; i < t.verts.size(); ++i) {
+            vertices[3 * i] = t.verts[i].x;
+            vertices[3 * i + 1] = t.verts[i].y;
+            vertices[3 * i + 2] = t.verts[i].z;
+        }
+    if (tris) std::copy(t.tris.begin(), t.tris.end(), tris);
+    if (edges) std::copy(e.begin(), e.end(), edges);
+    return PIERCE_HOST_OK;
+}
 
 extern "C" int pierce_gen_icospheres(uint64_t seed, int32_t num_meshes, int32_t level, double ln_mu, double sigma,
                                      double lo, double hi, pierce_geom** out) {
@@ -401,6 +385,70 @@ extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t targe
         }
     }
     finish(*g);
+    *out = g.release();
+    return PIERCE_HOST_OK;
+}
+
+// ---- instanced icosphere datasets -------------------------------------------
+
+extern "C" int pierce_gen_instances(uint64_t seed, int32_t num_meshes, int32_t family, int32_t level_lo,
+                                    int32_t level_hi, double p0, double p1, double noise_amp, double lo, double hi,
+                                    pierce_mesh_instance* out) {
+    if ((!out && num_meshes) || num_meshes < 0 || (family != 0 && family != 1) || level_lo < 0 ||
+        level_hi < level_lo || level_hi > PIERCE_MAX_INSTANCE_LEVEL) {
+        pierce::set_last_error("gen_instances: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    Rng rng(seed);
+    for (int32_t m = 0; m < num_meshes; ++m) {
+        pierce_mesh_instance& r = out[m];
+        if (family == 0) {
+            r = pierce_mesh_instance{};
+            r.center[0] = rng.uniform(lo, hi);
+            r.center[1] = rng.uniform(lo, hi);
+            r.center[2] = rng.uniform(lo, hi);
+            const double radius = pierce::detm::exp(p0 + p1 * rng.normal());
+            r.axes[0] = r.axes[1] = r.axes[2] = radius;
+            r.rotation[0] = r.rotation[4] = r.rotation[8] = 1.0;
+        } else {
+            r = to_instance(random_ellipsoid(rng, lo, hi, p0, p1), noise_amp, 0);
+        }
+        r.level = level_lo == level_hi ? level_lo : level_lo + (int32_t)rng.below((uint64_t)(level_hi - level_lo + 1));
+    }
+    return PIERCE_HOST_OK;
+}
+
+extern "C" int pierce_expand_instances(const pierce_mesh_instance* meshes, int32_t num_meshes, pierce_geom** out) {
+    if (!out || (!meshes && num_meshes) || num_meshes < 0) {
+        pierce::set_last_error("expand_instances: invalid argument");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    for (int32_t m = 0; m < num_meshes; ++m)
+        if (meshes[m].level < 0 || meshes[m].level > PIERCE_MAX_INSTANCE_LEVEL) {
+            pierce::set_last_error("expand_instances: level out of range");
+            return PIERCE_HOST_ERR_INVALID;
+        }
+    std::map<int, std::pair<Template, std::vector<uint32_t>>> templates;
+    std::unique_ptr<pierce_geom> g(new pierce_geom());
+    std::vector<float> pos;
+    for (int32_t m = 0; m < num_meshes; ++m) {
+        auto it = templates.find(meshes[m].level);
+        if (it == templates.end()) {
+            Template t = make_icosphere(meshes[m].level);
+            std::vector<uint32_t> e = pierce::inst::make_icosphere_template(meshes[m].level).e;
+            it = templates.emplace(meshes[m].level, std::make_pair(std::move(t), std::move(e))).first;
+        }
+        const Template& t = it->second.first;
+        const std::vector<uint32_t>& e = it->second.second;
+        instance_positions(t, meshes[m], pos);
+        append_mesh(*g, t, pos, m);
+        for (size_t k = 0; k < e.size(); k += 2) {
+            g->edge_starts.insert(g->edge_starts.end(), &pos[3 * e[k]], &pos[3 * e[k]] + 3);
+            g->edge_ends.insert(g->edge_ends.end(), &pos[3 * e[k + 1]], &pos[3 * e[k + 1]] + 3);
+            g->edge_src.push_back(m);
+        }
+    }
+    g->total_triangles = g->num_triangles();
     *out = g.release();
     return PIERCE_HOST_OK;
 }

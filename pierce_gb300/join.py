@@ -112,9 +112,34 @@ class Dataset:
                                                C.byref(h)), "dataset_create(device)")
         return cls(ctx, h)
 
+    @classmethod
+    def from_instances(cls, ctx: Context, inst: np.ndarray, tuning: capi.Tuning | None = None) -> "Dataset":
+        """Expand instanced meshes directly on the device."""
+        inst = np.ascontiguousarray(inst, dtype=capi.INSTANCE_DTYPE)
+        h = C.c_void_p()
+        t = tuning if tuning is not None else default_tuning()
+        check(capi.lib().pierce_dataset_create_instanced(ctx.handle, inst.ctypes.data if len(inst) else None,
+                                                         len(inst), C.byref(t), C.byref(h)),
+              "dataset_create_instanced")
+        return cls(ctx, h)
+
     def build(self, tuning: capi.Tuning | None = None) -> None:
         t = tuning if tuning is not None else default_tuning()
         check(self._lib.pierce_dataset_build(self.ctx.handle, self._h, C.byref(t)), "dataset_build")
+
+    def download(self) -> dict:
+        """The dataset's arrays, copied back to host memory."""
+        i = self.info()
+        out = {"vertices": np.zeros((i.num_vertices, 3), np.float32),
+               "indices": np.zeros((i.num_triangles, 3), np.uint32),
+               "tri_to_object": np.zeros(i.num_triangles, np.int32),
+               "edge_starts": np.zeros((i.num_edges, 3), np.float32),
+               "edge_ends": np.zeros((i.num_edges, 3), np.float32),
+               "edge_src": np.zeros(i.num_edges, np.int32)}
+        check(self._lib.pierce_dataset_download(self.ctx.handle, self._h, *[a.ctypes.data for a in out.values()]),
+              "dataset_download")
+        out["num_objects"] = i.num_objects
+        return out
 
     def info(self) -> capi.DatasetInfo:
         i = capi.DatasetInfo()

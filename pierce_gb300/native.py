@@ -59,6 +59,9 @@ def host() -> C.CDLL:
             _sig(lib, "pierce_geom_grid_stats", C.c_int, [V, F])
             _sig(lib, "pierce_geom_first_vertices", C.c_int, [V, V, I32])
             _sig(lib, "pierce_geom_append", C.c_int, [V, V])
+            _sig(lib, "pierce_icosphere_template", C.c_int, [I32, V, V, V, V])
+            _sig(lib, "pierce_gen_instances", C.c_int, [U64, I32, I32, I32, I32, D, D, D, D, D, V])
+            _sig(lib, "pierce_expand_instances", C.c_int, [V, I32, C.POINTER(V)])
             _sig(lib, "pierce_gen_icospheres", C.c_int, [U64, I32, I32, D, D, D, D, C.POINTER(V)])
             _sig(lib, "pierce_gen_ellipsoid_pair", C.c_int,
                  [U64, U64, I32, I32, I32, D, D, D, D, D, D, D, D, C.POINTER(V), C.POINTER(V)])
