@@ -81,6 +81,7 @@ typedef enum pierce_status {
 typedef struct pierce_ctx pierce_ctx;
 typedef struct pierce_dataset pierce_dataset;
 typedef struct pierce_result pierce_result;
+typedef struct pierce_mlp pierce_mlp;
 
 typedef struct pierce_pair {
     int32_t a;  /* object id in dataset A (mesh1) */
@@ -118,7 +119,9 @@ typedef enum pierce_direction {
 typedef enum pierce_sizing {
     PIERCE_SIZING_TWO_PASS = 0,   /* count, scan, write, sort + unique */
     PIERCE_SIZING_HASH = 1,       /* hash set sized from expected_pairs */
-    PIERCE_SIZING_FIXED = 2       /* hash set of hash_table_slots slots */
+    PIERCE_SIZING_FIXED = 2,      /* hash set of hash_table_slots slots */
+    PIERCE_SIZING_LEARNED = 3     /* hash set sized by sizing_model's prediction x output_safety;
+                                     two-pass rerun when the pairs do not fit */
 } pierce_sizing;
 
 typedef enum pierce_precision {
@@ -149,6 +152,7 @@ typedef struct pierce_join_opts {
     int32_t defer_exact;          /* 1 (default): queue FP32-undecided tests for a separate exact pass */
     int32_t active_bvh;           /* 1 (default): build per-join BVHs over the triangles of objects whose box
                                      meets an object box of the other side (datasets need no BVH of their own) */
+    const pierce_mlp* sizing_model; /* LEARNED sizing: trained network (pierce_mlp_create) */
 } pierce_join_opts;
 
 typedef struct pierce_stats {
@@ -176,6 +180,11 @@ typedef struct pierce_stats {
     uint64_t hash_contentions;    /* inspections past the first slot of a probe */
     double ms_build;              /* per-join BVH builds (active_bvh) */
     uint64_t active_triangles[2]; /* triangles in the per-join BVHs of A and B */
+    double predicted_pairs;       /* LEARNED sizing: the network's pair-count prediction */
+    double ms_sizing;             /* LEARNED sizing: features + inference */
+    int32_t sizing_overflow;      /* LEARNED sizing: 1 when the pairs exceeded the predicted capacity
+                                     and the join was rerun two-pass */
+    int32_t reserved;
 } pierce_stats;
 
 typedef struct pierce_dataset_info {
@@ -302,6 +311,52 @@ int pierce_deduplicate_pairs_noalloc(const pierce_pair* d_pairs, int64_t n, pier
 int pierce_estimate_pairs(pierce_ctx* ctx, const void* cells_a, uint32_t num_a, const void* cells_b,
                           uint32_t num_b, float cell_size, float epsilon, float gamma, int alpha_correction,
                           double* raw, int64_t* estimate, int32_t* matched_cells);
+
+/* ---- learned output sizing ---------------------------------------------- */
+/* No counterpart in the reference (whose sizing is the grid estimate above).
+ * A 32-64-64-1 FP32 network (ReLU) predicts log(1 + unique pairs) of a join
+ * from 32 summary features of its datasets (pierce_join_features).  Weights
+ * are row-major: W1[64][32], b1[64], W2[64][64], b2[64], W3[64], b3; inputs
+ * are standardised with x_mean / x_scale and the output is de-standardised
+ * as o * y_std + y_mean.  Training (Adam, mean squared error on the
+ * standardised log counts) and inference run on the device. */
+#define PIERCE_MLP_INPUTS 32
+#define PIERCE_MLP_HIDDEN 64
+#define PIERCE_MLP_PARAMS (PIERCE_MLP_HIDDEN * PIERCE_MLP_INPUTS + PIERCE_MLP_HIDDEN + \
+                           PIERCE_MLP_HIDDEN * PIERCE_MLP_HIDDEN + PIERCE_MLP_HIDDEN + PIERCE_MLP_HIDDEN + 1)
+
+typedef struct pierce_mlp_params {
+    float weights[PIERCE_MLP_PARAMS];
+    float x_mean[PIERCE_MLP_INPUTS];
+    float x_scale[PIERCE_MLP_INPUTS];
+    float y_mean;
+    float y_std;
+} pierce_mlp_params;
+
+typedef struct pierce_mlp_train_opts {
+    uint64_t seed;                /* sample order */
+    int32_t epochs;
+    int32_t fit_normalization;    /* 1: set x_mean/x_scale/y_mean/y_std from the training data first */
+    float lr, beta1, beta2, eps;  /* Adam */
+} pierce_mlp_train_opts;
+
+void pierce_default_mlp_train_opts(pierce_mlp_train_opts* o);
+/* Deterministic He-uniform initial weights, zero biases, identity scaling. */
+int pierce_mlp_init_params(pierce_mlp_params* p, uint64_t seed);
+int pierce_mlp_create(pierce_ctx* ctx, const pierce_mlp_params* init, pierce_mlp** out);
+void pierce_mlp_destroy(pierce_mlp* m);
+int pierce_mlp_get(pierce_ctx* ctx, const pierce_mlp* m, pierce_mlp_params* out);
+/* Train on n samples (host arrays X[n][32], y[n] = log1p(pairs)); the
+ * per-epoch mean loss goes to loss_per_epoch (host, epochs floats; may be NULL). */
+int pierce_mlp_train(pierce_ctx* ctx, pierce_mlp* m, const float* X, const float* y, int32_t n,
+                     const pierce_mlp_train_opts* opts, float* loss_per_epoch);
+/* Gradient of the mean squared error over the n samples (host grad[PIERCE_MLP_PARAMS]). */
+int pierce_mlp_gradient(pierce_ctx* ctx, const pierce_mlp* m, const float* X, const float* y, int32_t n,
+                        float* grad, float* loss);
+/* Predicted log1p(pairs) for n feature rows (host arrays). */
+int pierce_mlp_predict(pierce_ctx* ctx, const pierce_mlp* m, const float* X, int32_t n, float* out);
+/* The 32 features of the join (a, b) into host out[32]. */
+int pierce_join_features(pierce_ctx* ctx, const pierce_dataset* a, const pierce_dataset* b, float* out);
 
 #ifdef __cplusplus
 }

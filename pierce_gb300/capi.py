@@ -38,7 +38,7 @@ DEVICE_MEMORY = 1
 
 OVERLAP, INTERSECTION, CONTAINMENT = 0, 1, 2
 BOTH, MESH1_TO_MESH2, MESH2_TO_MESH1 = 0, 1, 2
-SIZING_TWO_PASS, SIZING_HASH, SIZING_FIXED = 0, 1, 2
+SIZING_TWO_PASS, SIZING_HASH, SIZING_FIXED, SIZING_LEARNED = 0, 1, 2, 3
 EXACT, FP32 = 0, 1
 RAYS_COUNT, RAYS_WRITE, RAYS_HASH = 0, 1, 2
 NOALLOC_TABLE_SLOTS = 1 << 22
@@ -67,7 +67,7 @@ class JoinOpts(C.Structure):
     _fields_ = [("predicate", I32), ("direction", I32), ("sizing", I32), ("precision", I32),
                 ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
                 ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
-                ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32)]
+                ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V)]
 
 
 class Stats(C.Structure):
@@ -78,7 +78,8 @@ class Stats(C.Structure):
                 ("overlap_pairs", U64), ("containment_pairs", U64), ("retries", I32),
                 ("launches", I32), ("ms_count_pass", D * 2), ("raw_pairs", U64 * 2),
                 ("hash_accesses", U64), ("hash_contentions", U64), ("ms_build", D),
-                ("active_triangles", U64 * 2)]
+                ("active_triangles", U64 * 2), ("predicted_pairs", D), ("ms_sizing", D),
+                ("sizing_overflow", I32), ("reserved", I32)]
 
     def as_dict(self) -> dict:
         out = {}
@@ -86,6 +87,20 @@ class Stats(C.Structure):
             v = getattr(self, name)
             out[name] = list(v) if hasattr(v, "__len__") else v
         return out
+
+
+MLP_INPUTS, MLP_HIDDEN = 32, 64
+MLP_PARAMS = MLP_HIDDEN * MLP_INPUTS + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
+
+
+class MlpParams(C.Structure):
+    _fields_ = [("weights", F * MLP_PARAMS), ("x_mean", F * MLP_INPUTS), ("x_scale", F * MLP_INPUTS),
+                ("y_mean", F), ("y_std", F)]
+
+
+class MlpTrainOpts(C.Structure):
+    _fields_ = [("seed", U64), ("epochs", I32), ("fit_normalization", I32), ("lr", F), ("beta1", F),
+                ("beta2", F), ("eps", F)]
 
 
 class DatasetInfo(C.Structure):
@@ -125,6 +140,15 @@ SIGNATURES = {
     "pierce_merge_and_deduplicate_pairs": (C.c_int, [V, V, I64, V, I64, V, C.POINTER(I64)]),
     "pierce_compact_hash_table_pairs": (C.c_int, [V, V, U64, V, U64, C.POINTER(U64)]),
     "pierce_deduplicate_pairs_noalloc": (C.c_int, [V, I64, V, V, V]),
+    "pierce_default_mlp_train_opts": (None, [C.POINTER(MlpTrainOpts)]),
+    "pierce_mlp_init_params": (C.c_int, [C.POINTER(MlpParams), U64]),
+    "pierce_mlp_create": (C.c_int, [V, C.POINTER(MlpParams), C.POINTER(V)]),
+    "pierce_mlp_destroy": (None, [V]),
+    "pierce_mlp_get": (C.c_int, [V, V, C.POINTER(MlpParams)]),
+    "pierce_mlp_train": (C.c_int, [V, V, V, V, I32, C.POINTER(MlpTrainOpts), V]),
+    "pierce_mlp_gradient": (C.c_int, [V, V, V, V, I32, V, V]),
+    "pierce_mlp_predict": (C.c_int, [V, V, V, I32, V]),
+    "pierce_join_features": (C.c_int, [V, V, V, V]),
     "pierce_estimate_pairs": (C.c_int, [V, V, C.c_uint32, V, C.c_uint32, F, F, F, C.c_int,
                                         C.POINTER(D), C.POINTER(I64), C.POINTER(I32)]),
 }

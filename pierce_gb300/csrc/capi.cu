@@ -204,12 +204,9 @@ int dataset_alloc(pierce_dataset* ds) {
     if (int s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object")) return s;
     if (int s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges")) return s;
     if (int s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources")) return s;
-    if (int s = device_alloc((void**)&ds->d_soup, 48 * ds->nt, "triangle soup")) return s;
-    if (int s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))
-        return s;
     if (int s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices")) return s;
     if (int s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes")) return s;
-    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * ds->nt + sizeof(Node) * ds->nt + 40 * (size_t)nobj;
+    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 40 * (size_t)nobj;
     return PIERCE_OK;
 }
 
@@ -771,6 +768,7 @@ struct Join {
                 *keys_out = keys;
                 return PIERCE_OK;
             }
+            if (strict_capacity) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "pairs exceed the predicted capacity");
             cap = n;  // output overflow: resize to the exact count and compact again
             st.retries++;
         }
@@ -932,15 +930,45 @@ struct Join {
         return make_result(keys, (uint64_t)nu, out);
     }
 
+    // LEARNED sizing: capacity = prediction x output_safety, no enlargement;
+    // pairs that do not fit send the join to the two-pass method.
+    bool strict_capacity = false;
+
+    int run_predicate(pierce_result** out) {
+        if (o.predicate == PIERCE_OVERLAP) return run_overlap(out);
+        if (o.predicate == PIERCE_INTERSECTION) return run_intersection(out);
+        return run_containment(out);
+    }
+
     int run(pierce_result** out) {
         cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
         cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
         const int t0 = timer.record();
-        int s = prepare();
+        int s = PIERCE_OK;
+        if (o.sizing == PIERCE_SIZING_LEARNED) {
+            double log_pairs = 0.0;
+            const int ts = timer.record();
+            if ((s = learned_log_pairs(ctx, o.sizing_model, A, B, &log_pairs))) return s;
+            timer.span(ts, timer.record(), &st.ms_sizing);
+            // clamp: at most 2^31 expected pairs; a NaN prediction sizes the minimum table
+            const double pred = std::isfinite(log_pairs) ? std::expm1(std::min(std::max(log_pairs, 0.0), 21.5)) : 0.0;
+            st.predicted_pairs = pred;
+            o.expected_pairs = std::max<uint64_t>((uint64_t)std::llround(pred), 1);
+            o.sizing = PIERCE_SIZING_HASH;
+            o.max_retries = 0;
+            strict_capacity = true;
+        }
+        s = prepare();
         if (s) return s;
-        if (o.predicate == PIERCE_OVERLAP) s = run_overlap(out);
-        else if (o.predicate == PIERCE_INTERSECTION) s = run_intersection(out);
-        else s = run_containment(out);
+        s = run_predicate(out);
+        if (strict_capacity && (s == PIERCE_ERR_HASH_FULL || s == PIERCE_ERR_OUTPUT_OVERFLOW)) {
+            // the prediction was too small: the two-pass method sizes exactly
+            st.sizing_overflow = 1;
+            strict_capacity = false;
+            o.sizing = PIERCE_SIZING_TWO_PASS;
+            cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
+            s = run_predicate(out);
+        }
         const int t1 = timer.record();
         timer.span(t0, t1, &st.ms_total);
         if (s) return s;
@@ -1118,9 +1146,11 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
     pierce_join_opts o;
     pierce_default_join_opts(&o);
     if (opts) o = *opts;
-    if (o.predicate < 0 || o.predicate > 2 || o.direction < 0 || o.direction > 2 || o.sizing < 0 || o.sizing > 2 ||
+    if (o.predicate < 0 || o.predicate > 2 || o.direction < 0 || o.direction > 2 || o.sizing < 0 || o.sizing > 3 ||
         o.precision < 0 || o.precision > 1)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: option out of range");
+    if (o.sizing == PIERCE_SIZING_LEARNED && !o.sizing_model)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: LEARNED sizing needs a sizing_model");
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
     cudaSetDevice(ctx->device);

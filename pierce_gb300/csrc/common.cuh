@@ -81,6 +81,7 @@ struct RayOpts {
 };
 
 constexpr int kScratchSlots = 24;
+constexpr int kSizingScratchSlot = 21;  // 21 and 22: learned sizing (sizing.cu)
 
 struct BvhShape {
     int leaf_size = 1;
@@ -165,6 +166,12 @@ int device_alloc(void** p, size_t bytes, const char* what);
 int dataset_alloc(pierce_dataset* ds);
 // object data, then the BVH unless tuning->defer_build (capi.cu)
 int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
+
+// sizing.cu: join features into d_out[32] (device), and the network's
+// log1p(pairs) prediction for a join (synchronous)
+int join_features(pierce_ctx* ctx, const pierce_dataset* A, const pierce_dataset* B, float* d_out);
+int learned_log_pairs(pierce_ctx* ctx, const pierce_mlp* mlp, const pierce_dataset* A, const pierce_dataset* B,
+                      double* pred);
 
 // lbvh.cu
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);

@@ -536,6 +536,17 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
 
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
     ds->built = 0;
+    // The soup and node arrays exist only for datasets that get a hierarchy
+    // of their own (joins with per-join hierarchies never need them).
+    if (!ds->d_soup) {
+        if (int s = device_alloc((void**)&ds->d_soup, 48 * std::max<uint64_t>(ds->nt, 1), "triangle soup")) return s;
+        ds->device_bytes += 48 * ds->nt;
+    }
+    if (!ds->d_nodes) {
+        if (int s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))
+            return s;
+        ds->device_bytes += sizeof(Node) * ds->nt;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -24,7 +24,8 @@ from .capi import check
 
 PREDICATES = {"overlap": capi.OVERLAP, "intersection": capi.INTERSECTION, "containment": capi.CONTAINMENT}
 DIRECTIONS = {"both": capi.BOTH, "mesh1_to_mesh2": capi.MESH1_TO_MESH2, "mesh2_to_mesh1": capi.MESH2_TO_MESH1}
-SIZINGS = {"two_pass": capi.SIZING_TWO_PASS, "hash": capi.SIZING_HASH, "fixed": capi.SIZING_FIXED}
+SIZINGS = {"two_pass": capi.SIZING_TWO_PASS, "hash": capi.SIZING_HASH, "fixed": capi.SIZING_FIXED,
+           "learned": capi.SIZING_LEARNED}
 PRECISIONS = {"exact": capi.EXACT, "fp32": capi.FP32}
 
 
@@ -168,7 +169,8 @@ class JoinResult:
 
 def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
-              max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True) -> capi.JoinOpts:
+              max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
+              sizing_model=None) -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -184,6 +186,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.cull_objects = 1 if cull_objects else 0
     o.defer_exact = 1 if defer_exact else 0
     o.active_bvh = 1 if active_bvh else 0
+    o.sizing_model = sizing_model.handle if sizing_model is not None else None
     return o
 
 
