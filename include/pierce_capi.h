@@ -195,6 +195,7 @@ typedef struct pierce_dataset_info {
     uint64_t device_bytes;
     double ms_build;              /* GPU time of the last build */
     float bounds_lo[3], bounds_hi[3];
+    int32_t num_parts;            /* partitions (0: not partitioned) */
 } pierce_dataset_info;
 
 /* ---- context ------------------------------------------------------------ */
@@ -224,6 +225,13 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* view, int mem
  * template order; bit-identical to the host's pierce_expand_instances. */
 int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mesh_instance* meshes, int32_t num_meshes,
                                     const pierce_tuning* tuning, pierce_dataset** out);
+/* Batches of independent joins: partition a dataset's objects (host array
+ * obj_part[num_objects], ids in [0, num_parts)).  Joining two datasets with
+ * the same partition count joins partition p of A with partition p of B
+ * only, for every p, in the same launches (one hierarchy per dataset with a
+ * subtree per partition).  num_parts = 0 removes the partitioning.  A built
+ * dataset is rebuilt.  No counterpart in the reference (one join per run). */
+int pierce_dataset_set_partitions(pierce_ctx* ctx, pierce_dataset* ds, const int32_t* obj_part, int32_t num_parts);
 /* Copy a dataset's arrays back to host memory (sizes from
  * pierce_dataset_info_get; any pointer may be NULL).  Synchronous. */
 int pierce_dataset_download(pierce_ctx* ctx, const pierce_dataset* ds, float* vertices, uint32_t* indices,
@@ -231,6 +239,7 @@ int pierce_dataset_download(pierce_ctx* ctx, const pierce_dataset* ds, float* ve
 /* Rebuild the hierarchy (e.g. with another leaf size). */
 int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
 int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out);
+/* Release a dataset (also valid after its context was destroyed). */
 void pierce_dataset_destroy(pierce_dataset* ds);
 
 /* ---- joins -------------------------------------------------------------- */

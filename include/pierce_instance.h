@@ -36,7 +36,7 @@ typedef struct pierce_mesh_instance {
     double noise_offset[3];
     uint64_t noise_seed;
     int32_t level;          /* icosphere subdivision level, 0..PIERCE_MAX_INSTANCE_LEVEL */
-    int32_t reserved;
+    int32_t group;          /* partition (join of a batch) the mesh belongs to; 0 for a single join */
 } pierce_mesh_instance;
 
 #define PIERCE_MAX_INSTANCE_LEVEL 6

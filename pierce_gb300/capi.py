@@ -54,7 +54,7 @@ class MeshView(C.Structure):
 # pierce_mesh_instance (pierce_instance.h), as a numpy record type.
 INSTANCE_DTYPE = np.dtype([("center", "<f8", (3,)), ("axes", "<f8", (3,)), ("rotation", "<f8", (9,)),
                            ("noise_amp", "<f8"), ("noise_offset", "<f8", (3,)), ("noise_seed", "<u8"),
-                           ("level", "<i4"), ("reserved", "<i4")])
+                           ("level", "<i4"), ("group", "<i4")])
 assert INSTANCE_DTYPE.itemsize == 168
 
 
@@ -106,7 +106,7 @@ class MlpTrainOpts(C.Structure):
 class DatasetInfo(C.Structure):
     _fields_ = [("num_vertices", U64), ("num_triangles", U64), ("num_edges", U64),
                 ("num_objects", I32), ("built", I32), ("num_nodes", U64), ("device_bytes", U64),
-                ("ms_build", D), ("bounds_lo", F * 3), ("bounds_hi", F * 3)]
+                ("ms_build", D), ("bounds_lo", F * 3), ("bounds_hi", F * 3), ("num_parts", I32)]
 
 
 # Every symbol the header declares, with its signature.
@@ -125,6 +125,7 @@ SIGNATURES = {
     "pierce_dataset_build": (C.c_int, [V, V, C.POINTER(Tuning)]),
     "pierce_dataset_create_instanced": (C.c_int, [V, V, I32, C.POINTER(Tuning), C.POINTER(V)]),
     "pierce_dataset_download": (C.c_int, [V, V, V, V, V, V, V, V]),
+    "pierce_dataset_set_partitions": (C.c_int, [V, V, V, I32]),
     "pierce_dataset_info_get": (C.c_int, [V, C.POINTER(DatasetInfo)]),
     "pierce_dataset_destroy": (None, [V]),
     "pierce_join": (C.c_int, [V, V, V, C.POINTER(JoinOpts), C.POINTER(V), C.POINTER(Stats)]),

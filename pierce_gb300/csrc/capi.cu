@@ -215,6 +215,8 @@ int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tun
     pierce_tuning t;
     pierce_default_tuning(&t);
     if (tuning) t = *tuning;
+    // the leaf size also applies to the per-join hierarchies of a deferred dataset
+    ds->leaf_size = std::min(std::max(t.leaf_size, 1), 16);
     if (t.defer_build) return sync_ctx(ctx, "dataset upload");
     return build_bvh(ctx, ds, t.leaf_size);
 }
@@ -337,15 +339,48 @@ int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_
 
 void pierce_dataset_destroy(pierce_dataset* ds) {
     if (!ds) return;
-    if (ds->ctx) {
-        cudaSetDevice(ds->ctx->device);
-        cudaStreamSynchronize(ds->ctx->stream);
-    }
-    void* ptrs[] = {ds->d_vertices, ds->d_indices,      ds->d_tri_to_object, ds->d_edges, ds->d_edge_src,
-                    ds->d_soup,     ds->d_nodes,        ds->d_first_vertex,  ds->d_obj_box};
+    // The device id is a copy, so a dataset outliving its context is still
+    // released; the device-wide synchronisation covers work still queued.
+    cudaSetDevice(ds->device);
+    cudaDeviceSynchronize();
+    void* ptrs[] = {ds->d_vertices, ds->d_indices,  ds->d_tri_to_object, ds->d_edges,  ds->d_edge_src,
+                    ds->d_soup,     ds->d_nodes,    ds->d_first_vertex,  ds->d_obj_box, ds->d_obj_part,
+                    ds->d_part_roots};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete ds;
+}
+
+int pierce_dataset_set_partitions(pierce_ctx* ctx, pierce_dataset* ds, const int32_t* obj_part, int32_t num_parts) {
+    if (!ctx || !ds || num_parts < 0 || (num_parts > 0 && ds->num_objects > 0 && !obj_part))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_set_partitions: invalid argument");
+    if (num_parts >= (1 << 30))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_set_partitions: at most 2^30 - 1 partitions");
+    for (int32_t o = 0; num_parts > 0 && o < ds->num_objects; ++o)
+        if (obj_part[o] < 0 || obj_part[o] >= num_parts)
+            return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_set_partitions: partition id out of range");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ds->d_obj_part) cudaFree(ds->d_obj_part);
+    if (ds->d_part_roots) cudaFree(ds->d_part_roots);
+    ds->d_obj_part = nullptr;
+    ds->d_part_roots = nullptr;
+    ds->num_parts = 0;
+    const bool was_built = ds->built != 0;
+    ds->built = 0;
+    if (num_parts > 0) {
+        const size_t nobj = (size_t)std::max(ds->num_objects, 1);
+        if (int s = device_alloc((void**)&ds->d_obj_part, 4 * nobj, "object partitions")) return s;
+        if (int s = device_alloc((void**)&ds->d_part_roots, 8 * (size_t)num_parts, "partition roots")) return s;
+        if (ds->num_objects > 0)
+            if (int s = check_cuda(cudaMemcpyAsync(ds->d_obj_part, obj_part, 4 * (size_t)ds->num_objects,
+                                                   cudaMemcpyHostToDevice, ctx->stream),
+                                   "copy partitions"))
+                return s;
+        ds->num_parts = num_parts;
+    }
+    if (was_built) return build_bvh(ctx, ds, ds->leaf_size);
+    return sync_ctx(ctx, "set partitions");
 }
 
 int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning) {
@@ -369,6 +404,7 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
     const cudaMemcpyKind kind = memory == PIERCE_DEVICE_MEMORY ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     pierce_dataset* ds = new pierce_dataset();
     ds->ctx = ctx;
+    ds->device = ctx->device;
     ds->nv = v->num_vertices;
     ds->nt = v->num_triangles;
     ds->ne = v->num_edges;
@@ -475,6 +511,7 @@ int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out) 
     out->num_triangles = ds->nt;
     out->num_edges = ds->ne;
     out->num_objects = ds->num_objects;
+    out->num_parts = ds->num_parts;
     out->built = ds->built;
     out->num_nodes = ds->num_nodes;
     out->device_bytes = ds->device_bytes;
@@ -584,7 +621,8 @@ struct Join {
     int object_bvh(pierce_dataset* ds, int slot, DevDataset* out) {
         const int64_t n = ds->num_objects;
         void* p = nullptr;
-        const size_t bytes = 16 * (size_t)std::max<int64_t>(n, 1) + (48 + 64) * (size_t)std::max<int64_t>(n, 1) + 256;
+        const size_t bytes = 16 * (size_t)std::max<int64_t>(n, 1) + (48 + 64) * (size_t)std::max<int64_t>(n, 1) + 256 +
+                             8 * (size_t)ds->num_parts;
         if (int s = scratch(ctx, slot, bytes, &p)) return s;
         uint32_t* idx = static_cast<uint32_t*>(p);
         int32_t* t2o = reinterpret_cast<int32_t*>(idx + 3 * std::max<int64_t>(n, 1));
@@ -592,15 +630,20 @@ struct Join {
         q += (256 - ((uintptr_t)q & 255)) & 255;
         float4* soup = reinterpret_cast<float4*>(q);
         Node* nodes = reinterpret_cast<Node*>(soup + 3 * std::max<int64_t>(n, 1));
+        int2* roots = ds->num_parts ? reinterpret_cast<int2*>(nodes + std::max<int64_t>(n, 1)) : nullptr;
         if (int s = launch_object_pseudo_tris(ctx, (int32_t)n, idx, t2o)) return s;
         BvhShape shape;
-        if (int s = build_lbvh(ctx, ds->d_obj_box, idx, t2o, nullptr, n, 1, soup, nodes, &shape, nullptr)) return s;
+        if (int s = build_lbvh(ctx, ds->d_obj_box, idx, t2o, nullptr, n, 1, soup, nodes, &shape, nullptr,
+                               ds->d_obj_part, ds->num_parts, roots))
+            return s;
         *out = DevDataset{};
         out->soup = soup;
         out->nodes = nodes;
         out->num_tris = n;
         out->root_is_leaf = shape.root_is_leaf;
         out->root_leaf_count = shape.root_leaf_count;
+        out->obj_part = ds->d_obj_part;
+        out->part_roots = roots;
         return PIERCE_OK;
     }
 
@@ -632,16 +675,25 @@ struct Join {
         const int64_t na = ctx->h_small[0], nb = ctx->h_small[1];
         void *sa = nullptr, *sb = nullptr, *na_p = nullptr, *nb_p = nullptr;
         if (int s = scratch(ctx, SLOT_RED_SOUP_A, 48 * (size_t)std::max<int64_t>(na, 1), &sa)) return s;
-        if (int s = scratch(ctx, SLOT_RED_NODES_A, 64 * (size_t)std::max<int64_t>(na, 1), &na_p)) return s;
+        const size_t roots_bytes = 8 * (size_t)A->num_parts;  // equal partition counts on both sides
+        if (int s = scratch(ctx, SLOT_RED_NODES_A, 64 * (size_t)std::max<int64_t>(na, 1) + roots_bytes, &na_p))
+            return s;
         if (int s = scratch(ctx, SLOT_RED_SOUP_B, 48 * (size_t)std::max<int64_t>(nb, 1), &sb)) return s;
-        if (int s = scratch(ctx, SLOT_RED_NODES_B, 64 * (size_t)std::max<int64_t>(nb, 1), &nb_p)) return s;
+        if (int s = scratch(ctx, SLOT_RED_NODES_B, 64 * (size_t)std::max<int64_t>(nb, 1) + roots_bytes, &nb_p))
+            return s;
+        int2* roots_a = A->num_parts ? reinterpret_cast<int2*>((Node*)na_p + std::max<int64_t>(na, 1)) : nullptr;
+        int2* roots_b = B->num_parts ? reinterpret_cast<int2*>((Node*)nb_p + std::max<int64_t>(nb, 1)) : nullptr;
         BvhShape shA, shB;
         if (int s = build_lbvh(ctx, A->d_vertices, A->d_indices, A->d_tri_to_object, (const uint32_t*)ta, na,
-                               A->leaf_size, (float4*)sa, (Node*)na_p, &shA, nullptr))
+                               A->leaf_size, (float4*)sa, (Node*)na_p, &shA, nullptr, A->d_obj_part, A->num_parts,
+                               roots_a))
             return s;
         if (int s = build_lbvh(ctx, B->d_vertices, B->d_indices, B->d_tri_to_object, (const uint32_t*)tb, nb,
-                               B->leaf_size, (float4*)sb, (Node*)nb_p, &shB, nullptr))
+                               B->leaf_size, (float4*)sb, (Node*)nb_p, &shB, nullptr, B->d_obj_part, B->num_parts,
+                               roots_b))
             return s;
+        va.part_roots = roots_a;
+        vb.part_roots = roots_b;
         va.soup = (const float4*)sa;
         va.nodes = (const Node*)na_p;
         va.num_tris = na;
@@ -1143,6 +1195,8 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
     if ((!opts || !opts->active_bvh) && (!a->built || !b->built))
         return set_error(PIERCE_ERR_NOT_BUILT, "join: dataset not built (or use active_bvh)");
     if (a->ctx != ctx || b->ctx != ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: dataset of other ctx");
+    if (a->num_parts != b->num_parts)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: datasets have different partition counts");
     pierce_join_opts o;
     pierce_default_join_opts(&o);
     if (opts) o = *opts;
@@ -1167,6 +1221,8 @@ int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pi
                             uint64_t* d_table, uint64_t table_slots, pierce_stats* stats) {
     if (!ctx || !src || !tgt) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_edge_rays: null argument");
     if (!tgt->built) return set_error(PIERCE_ERR_NOT_BUILT, "launch_edge_rays: target not built");
+    if (src->num_parts != tgt->num_parts)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_edge_rays: datasets have different partition counts");
     if (mode == PIERCE_RAYS_COUNT && !d_counts) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "COUNT needs d_counts");
     if (mode == PIERCE_RAYS_WRITE && (!d_offsets || !d_keys))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "WRITE needs d_offsets and d_keys");
@@ -1201,6 +1257,8 @@ int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierc
     if (!ctx || !src || !tgt || !d_table || !d_parity || table_slots == 0 || (table_slots & (table_slots - 1)))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_parity: bad argument");
     if (!tgt->built) return set_error(PIERCE_ERR_NOT_BUILT, "launch_parity: target not built");
+    if (src->num_parts != tgt->num_parts)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "launch_parity: datasets have different partition counts");
     cudaSetDevice(ctx->device);
     cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
     if (int s = launch_parity(ctx, src->view(), tgt->view(), swap, d_table, d_parity, table_slots)) return s;

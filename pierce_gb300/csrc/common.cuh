@@ -65,6 +65,11 @@ struct DevDataset {
     const float4* first_vertex;  // per object (xyz, 0)
     const float* obj_box;        // per object 6 floats lo.xyz hi.xyz
     int32_t num_objects;
+    // partitioned datasets (a batch of independent joins): partition of each
+    // object, and per partition the traversal start of this hierarchy
+    // (x >= 0 internal node; x < 0 leaf ~x of y triangles; (-1, 0) empty)
+    const int32_t* obj_part;
+    const int2* part_roots;
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -111,6 +116,7 @@ struct pierce_ctx {
 
 struct pierce_dataset {
     pierce_ctx* ctx = nullptr;
+    int device = 0;  // ctx->device, kept for release
     uint64_t nv = 0, nt = 0, ne = 0;
     int32_t num_objects = 0;
     float* d_vertices = nullptr;
@@ -129,6 +135,10 @@ struct pierce_dataset {
     double ms_build = 0.0;
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     uint64_t device_bytes = 0;
+    // partitions (0: none): object -> partition, and the BVH's per-partition roots
+    int32_t num_parts = 0;
+    int32_t* d_obj_part = nullptr;
+    int2* d_part_roots = nullptr;
 
     pgpu::DevDataset view() const {
         pgpu::DevDataset v;
@@ -143,6 +153,8 @@ struct pierce_dataset {
         v.first_vertex = d_first_vertex;
         v.obj_box = d_obj_box;
         v.num_objects = num_objects;
+        v.obj_part = d_obj_part;
+        v.part_roots = (num_parts && built) ? d_part_roots : nullptr;
         return v;
     }
 };
@@ -175,14 +187,20 @@ int learned_log_pairs(pierce_ctx* ctx, const pierce_mlp* mlp, const pierce_datas
 
 // lbvh.cu
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);
+// With obj_part (num_parts > 0) the hierarchy is partitioned: triangles sort
+// by (partition of their object, Morton code in the partition's bounds), no
+// leaf mixes partitions, and part_roots[p] receives partition p's subtree.
 int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, const uint32_t* list,
-               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box);
+               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box,
+               const int32_t* obj_part = nullptr, int32_t num_parts = 0, int2* part_roots = nullptr);
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds);
 
 // sortscan.cu (CUB library calls)
 int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,
                    int64_t n, int end_bit);
 int sort_u64_keys(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, int64_t n);
+int sort_u64_pairs(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,
+                   int64_t n, int end_bit);
 int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
 int unique_u64(pierce_ctx* ctx, const uint64_t* in, uint64_t* out, int64_t n, int64_t* num_unique);
 }  // namespace pgpu

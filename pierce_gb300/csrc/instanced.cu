@@ -116,8 +116,12 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
     int64_t* toff = voff + num_meshes + 1;
     int64_t* eoff = toff + num_meshes + 1;
     bool used[kLevels] = {false};
+    int32_t max_group = 0;
     for (int32_t m = 0; m < num_meshes; ++m) {
         const int l = meshes[m].level;
+        if (meshes[m].group < 0)
+            return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create_instanced: negative group");
+        max_group = std::max(max_group, meshes[m].group);
         if (l < 0 || l >= kLevels)
             return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create_instanced: level out of range");
         used[l] = true;
@@ -156,6 +160,7 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
     cudaStream_t st = ctx->stream;
     pierce_dataset* ds = new pierce_dataset();
     ds->ctx = ctx;
+    ds->device = ctx->device;
     ds->nv = nv;
     ds->nt = nt;
     ds->ne = ne;
@@ -200,7 +205,20 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
             ctx->launches += 3;
             if ((s = check_cuda(cudaGetLastError(), "instance expansion"))) break;
         }
-        if ((s = dataset_finish(ctx, ds, tuning))) break;
+        if (max_group > 0) {
+            // a batch of joins: the mesh groups partition the dataset
+            std::vector<int32_t> part((size_t)num_meshes);
+            for (int32_t m = 0; m < num_meshes; ++m) part[m] = meshes[m].group;
+            pierce_tuning t;
+            pierce_default_tuning(&t);
+            if (tuning) t = *tuning;
+            t.defer_build = 1;
+            if ((s = dataset_finish(ctx, ds, &t))) break;
+            if ((s = pierce_dataset_set_partitions(ctx, ds, part.data(), max_group + 1))) break;
+            if (!(tuning && tuning->defer_build) && (s = build_bvh(ctx, ds, ds->leaf_size))) break;
+        } else if ((s = dataset_finish(ctx, ds, tuning))) {
+            break;
+        }
     } while (0);
     cudaStreamSynchronize(st);
     for (void* p : {d_blob, d_inst, d_off})

@@ -134,6 +134,28 @@ struct RayCounters {
 // inline; PREC_DEFER classifies in float32 and queues undecided tests for
 // k_resolve_ambiguous (the WRITE pass skips them: they were queued by the
 // COUNT pass); PREC_FP32 is the plain Moller-Trumbore form.
+// Where a traversal of tgt for source object src_obj starts: the root
+// (node 0), a root leaf, or -- for partitioned datasets -- the subtree of the
+// source object's partition.  Returns the start node, or -1 with the leaf
+// range in (first, count) when the start is a leaf (count 0: nothing).
+__device__ __forceinline__ int traversal_start(const DevDataset& src, const DevDataset& tgt, int32_t src_obj,
+                                               int& first, int& count) {
+    first = 0;
+    count = 0;
+    if (tgt.part_roots) {
+        const int2 r = __ldg(tgt.part_roots + __ldg(src.obj_part + src_obj));
+        if (r.x >= 0) return r.x;
+        first = ~r.x;
+        count = r.y;
+        return -1;
+    }
+    if (tgt.root_is_leaf) {
+        count = tgt.root_leaf_count;
+        return -1;
+    }
+    return 0;
+}
+
 template <int MODE, int PREC>
 __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int (*sstack)[128], int* lstack,
                                            RayCounters& rc, PredCounters& pc) {
@@ -195,11 +217,12 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
             }
         }
     };
-    if (P.tgt.root_is_leaf) {
-        if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+    int leaf_first, leaf_count;
+    int node = traversal_start(P.src, P.tgt, src_obj, leaf_first, leaf_count);
+    if (node < 0) {
+        if (leaf_count > 0) leaf(leaf_first, leaf_count);
     } else {
         int sp = 0;
-        int node = 0;
         for (;;) {
             ++rc.nodes;
             const Node* nd = P.tgt.nodes + node;
@@ -339,10 +362,12 @@ __global__ void __launch_bounds__(128) k_object_active(DevDataset src, DevDatase
                                     fminf(a4.z, fminf(b4.z, c4.z)), fmaxf(a4.z, fmaxf(b4.z, c4.z)), lo, hi);
             }
         };
-        if (tgt.root_is_leaf) {
-            leaf(0, tgt.root_leaf_count);
+        int leaf_first, leaf_count;
+        int node = traversal_start(src, tgt, (int32_t)o, leaf_first, leaf_count);
+        if (node < 0) {
+            leaf(leaf_first, leaf_count);
         } else {
-            int sp = 0, node = 0;
+            int sp = 0;
             while (!found) {
                 const Node* nd = tgt.nodes + node;
                 const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
@@ -478,10 +503,12 @@ __global__ void __launch_bounds__(128) k_parity(ParityParams P) {
             }
         };
         if (active) {
-            if (P.tgt.root_is_leaf) {
-                if (P.tgt.root_leaf_count > 0) leaf(0, P.tgt.root_leaf_count);
+            int leaf_first, leaf_count;
+            int node = traversal_start(P.src, P.tgt, (int32_t)o, leaf_first, leaf_count);
+            if (node < 0) {
+                if (leaf_count > 0) leaf(leaf_first, leaf_count);
             } else {
-                int sp = 0, node = 0;
+                int sp = 0;
                 for (;;) {
                     ++n_nodes;
                     const Node* nd = P.tgt.nodes + node;

@@ -103,6 +103,87 @@ __global__ void k_morton(const float4* __restrict__ cen, int64_t nt, const uint3
     }
 }
 
+// 1'/2'. partitioned hierarchy: centroid bounds per partition (warps whose
+// lanes share a partition reduce in registers first), then 64-bit keys
+// (partition << 30 | Morton code in the partition's bounds).
+__global__ void k_centroids_parts(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                  const uint32_t* __restrict__ list, const int32_t* __restrict__ t2o,
+                                  const int32_t* __restrict__ obj_part, int64_t nt, float4* __restrict__ cen,
+                                  uint32_t* __restrict__ bounds) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        int32_t part = -1;
+        float m[3] = {0.0f, 0.0f, 0.0f};
+        if (i < nt) {
+            const int64_t t = list ? (int64_t)list[i] : i;
+            const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
+            const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
+            const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
+            m[0] = (a.x + b.x + c.x) * (1.0f / 3.0f);
+            m[1] = (a.y + b.y + c.y) * (1.0f / 3.0f);
+            m[2] = (a.z + b.z + c.z) * (1.0f / 3.0f);
+            part = __ldg(obj_part + __ldg(t2o + t));
+            cen[i] = make_float4(m[0], m[1], m[2], __int_as_float(part));
+        }
+        const int32_t p0 = __shfl_sync(0xFFFFFFFFu, part, 0);
+        if (__all_sync(0xFFFFFFFFu, part == p0 || part < 0) && p0 >= 0) {
+            float mn[3] = {m[0], m[1], m[2]}, mx[3] = {m[0], m[1], m[2]};
+            if (part < 0)
+                for (int k = 0; k < 3; ++k) {
+                    mn[k] = 3.4e38f;
+                    mx[k] = -3.4e38f;
+                }
+            for (int k = 0; k < 3; ++k)
+                for (int off = 16; off > 0; off >>= 1) {
+                    mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
+                    mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
+                }
+            if ((threadIdx.x & 31) == 0)
+                for (int k = 0; k < 3; ++k) {
+                    atomicMin(bounds + 6 * (int64_t)p0 + k, f2o(mn[k]));
+                    atomicMax(bounds + 6 * (int64_t)p0 + 3 + k, f2o(mx[k]));
+                }
+        } else if (part >= 0) {
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(bounds + 6 * (int64_t)part + k, f2o(m[k]));
+                atomicMax(bounds + 6 * (int64_t)part + 3 + k, f2o(m[k]));
+            }
+        }
+    }
+}
+
+__global__ void k_morton_parts(const float4* __restrict__ cen, int64_t nt, const uint32_t* __restrict__ bounds,
+                               uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const float4 c = cen[t];
+        const int32_t part = __float_as_int(c.w);
+        const uint32_t* b = bounds + 6 * (int64_t)part;
+        const float cc[3] = {c.x, c.y, c.z};
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            const float lo = o2f(b[k]), hi = o2f(b[3 + k]);
+            const float inv = hi > lo ? 1.0f / (hi - lo) : 0.0f;
+            float u = (cc[k] - lo) * inv;
+            u = fminf(fmaxf(u, 0.0f), 1.0f);
+            q[k] = min((uint32_t)(u * 1024.0f), 1023u);
+        }
+        const uint32_t code = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+        keys[t] = ((uint64_t)(uint32_t)part << 30) | code;
+        vals[t] = (uint32_t)t;
+    }
+}
+
+__global__ void k_fill_roots(int2* roots, int32_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        roots[i] = make_int2(-1, 0);
+}
+
+// a one-triangle partitioned hierarchy: its partition's root is that leaf
+__global__ void k_single_part_root(const uint64_t* keys, int2* roots) {
+    roots[keys[0] >> 30] = make_int2(~0, 1);
+}
+
 // 4. triangle soup in sorted order
 __global__ void k_soup(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
                        const int32_t* __restrict__ t2o, const uint32_t* __restrict__ list,
@@ -125,6 +206,16 @@ __device__ __forceinline__ int lcp(const uint32_t* keys, int64_t n, int64_t i, i
     if (ki == kj) return 32 + __clzll((unsigned long long)(i ^ j)) - 32;  // 32 + clz over 32-bit index
     return __clz(ki ^ kj);
 }
+__device__ __forceinline__ int lcp(const uint64_t* keys, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t ki = keys[i], kj = keys[j];
+    if (ki == kj) return 64 + __clzll((unsigned long long)(i ^ j));
+    return __clzll(ki ^ kj);
+}
+
+// partition of sorted key k (32-bit keys carry none)
+__device__ __forceinline__ uint32_t key_part(const uint32_t*, int64_t) { return 0u; }
+__device__ __forceinline__ uint32_t key_part(const uint64_t* keys, int64_t k) { return (uint32_t)(keys[k] >> 30); }
 
 // 5. Karras hierarchy with leaf collapse.  Internal node i covers the
 // sorted range [first, last]; a child whose range holds <= leaf_size
@@ -137,8 +228,20 @@ __device__ __forceinline__ int lcp(const uint32_t* keys, int64_t n, int64_t i, i
 // thread, ch.w by its parent's thread), so no two threads write one word.
 constexpr uint32_t kRootParent = 0x3FFFFFFFu;
 
-__global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, int leaf_size, Node* __restrict__ nodes,
-                         unsigned long long* __restrict__ leaf_rec) {
+//
+// Partitioned keys: a range is collapsed into a leaf only when it lies in
+// one partition, and every range that is exactly one whole partition
+// records itself in part_roots (an internal node, or a leaf child).  The
+// keys of one partition share their partition bits, so they form one
+// subtree of the radix tree.
+template <typename K>
+__global__ void k_karras(const K* __restrict__ keys, int64_t n, int leaf_size, Node* __restrict__ nodes,
+                         unsigned long long* __restrict__ leaf_rec, int2* __restrict__ part_roots) {
+    auto whole_part = [&](int64_t f, int64_t l) {
+        const uint32_t p = key_part(keys, f);
+        return key_part(keys, l) == p && (f == 0 || key_part(keys, f - 1) != p) &&
+               (l == n - 1 || key_part(keys, l + 1) != p);
+    };
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n - 1; i += (int64_t)gridDim.x * blockDim.x) {
         const int d = (lcp(keys, n, i, i + 1) - lcp(keys, n, i, i - 1)) >= 0 ? 1 : -1;
         const int dmin = lcp(keys, n, i, i - d);
@@ -149,7 +252,9 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, int leaf_
             if (lcp(keys, n, i, i + (l + t) * d) > dmin) l += t;
         const int64_t j = i + l * d;
         const int64_t first = i < j ? i : j, last = i < j ? j : i;
-        if (i != 0 && last - first + 1 <= leaf_size) continue;  // inside a collapsed leaf
+        if (i != 0 && last - first + 1 <= leaf_size && key_part(keys, first) == key_part(keys, last))
+            continue;  // inside a collapsed leaf
+        if (part_roots && whole_part(first, last)) part_roots[key_part(keys, first)] = make_int2((int)i, 0);
         const int dnode = lcp(keys, n, i, j);
         int64_t s = 0, t = l;
         do {
@@ -163,11 +268,13 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int64_t n, int leaf_
         const int64_t cidx[2] = {gamma, gamma + 1};
         for (int side = 0; side < 2; ++side) {
             const int64_t size = clast[side] - cfirst[side] + 1;
-            if (size <= leaf_size) {
+            if (size <= leaf_size && key_part(keys, cfirst[side]) == key_part(keys, clast[side])) {
                 child[side] = ~(int)cfirst[side];
                 count[side] = (int)size;
                 leaf_rec[cfirst[side]] = ((unsigned long long)i << 9) | ((unsigned long long)side << 8) |
                                          (unsigned long long)size;
+                if (part_roots && whole_part(cfirst[side], clast[side]))
+                    part_roots[key_part(keys, cfirst[side])] = make_int2(~(int)cfirst[side], (int)size);
             } else {
                 child[side] = (int)cidx[side];
                 nodes[cidx[side]].ch.w = (int)(((uint32_t)i << 2) | ((uint32_t)side << 1));
@@ -446,13 +553,19 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
 // context stream; when root_box is non-null the root box is read back
 // (synchronously).
 int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, const uint32_t* list,
-               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box) {
+               int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box,
+               const int32_t* obj_part, int32_t num_parts, int2* part_roots) {
     cudaStream_t st = ctx->stream;
     if (leaf_size < 1) leaf_size = 1;
     if (leaf_size > 16) leaf_size = 16;
     shape->leaf_size = leaf_size;
     if (n >= (int64_t(1) << 30))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "bvh build: at most 2^30 - 1 triangles per hierarchy");
+    const bool parts = obj_part && num_parts > 0 && part_roots;
+    if (parts) {
+        k_fill_roots<<<grid_for(ctx, num_parts, 256), 256, 0, st>>>(part_roots, num_parts);
+        ctx->launches += 1;
+    }
     if (n == 0) {
         shape->root_is_leaf = 1;
         shape->root_leaf_count = 0;
@@ -464,9 +577,11 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     // scratch: 1 centroids, 2 keys (in|out), 3 vals (in|out), 4 leaf records + bounds
     void *pc = nullptr, *pk = nullptr, *pv = nullptr, *pm = nullptr;
     if (int s = scratch(ctx, 1, sizeof(float4) * (size_t)n, &pc)) return s;
-    if (int s = scratch(ctx, 2, 2 * sizeof(uint32_t) * (size_t)n, &pk)) return s;
+    const size_t key_bytes = parts ? sizeof(uint64_t) : sizeof(uint32_t);
+    if (int s = scratch(ctx, 2, 2 * key_bytes * (size_t)n, &pk)) return s;
     if (int s = scratch(ctx, 3, 2 * sizeof(uint32_t) * (size_t)n, &pv)) return s;
-    if (int s = scratch(ctx, 4, sizeof(unsigned long long) * (size_t)n + 64 + 64, &pm)) return s;
+    const size_t part_bounds = parts ? 24 * (size_t)num_parts : 0;
+    if (int s = scratch(ctx, 4, sizeof(unsigned long long) * (size_t)n + 64 + 64 + part_bounds, &pm)) return s;
     float4* cen = static_cast<float4*>(pc);
     uint32_t* keys = static_cast<uint32_t*>(pk);
     uint32_t* vals = static_cast<uint32_t*>(pv);
@@ -476,28 +591,55 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     // byte layout after the n leaf records: bounds [8n, 8n+24), root box
     // [8n+24, 8n+48), two wave counters [8n+64, 8n+80); allocation 8n+128
     unsigned long long* wave_count = leaf_rec + n + 8;
+    // partitioned: per-partition bounds after the wave counters, [8n+128, ...)
+    uint32_t* pbounds = reinterpret_cast<uint32_t*>(leaf_rec + n + 16);
+    uint64_t* keys64 = static_cast<uint64_t*>(pk);
 
     const int B = 256;
-    k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
-    k_fill_u32<<<1, 32, 0, st>>>(bounds + 3, 0u, 3);       // ordered -max
-    k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, list, n, cen, bounds);
-    k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
-    ctx->launches += 4;
-    if (int s = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30)) return s;
+    if (parts) {
+        const int64_t nb = 6 * (int64_t)num_parts;
+        k_obj_box_init<<<grid_for(ctx, nb, B), B, 0, st>>>(pbounds, num_parts);  // ordered (+max, -max)
+        k_centroids_parts<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, list, t2o, obj_part, n, cen, pbounds);
+        k_morton_parts<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, pbounds, keys64, vals);
+        ctx->launches += 3;
+        int bits = 0;
+        while (bits < 32 && (1ll << bits) < (int64_t)num_parts) ++bits;
+        if (int s = sort_u64_pairs(ctx, keys64, keys64 + n, vals, vals + n, n, 30 + bits)) return s;
+    } else {
+        k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
+        k_fill_u32<<<1, 32, 0, st>>>(bounds + 3, 0u, 3);       // ordered -max
+        k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, list, n, cen, bounds);
+        k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
+        ctx->launches += 4;
+        if (int s = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30)) return s;
+    }
     const uint32_t* skeys = keys + n;
+    const uint64_t* skeys64 = keys64 + n;
     const uint32_t* order = vals + n;
     k_soup<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, t2o, list, order, n, soup);
     ctx->launches += 1;
-    if (n <= leaf_size) {
+    // a partitioned hierarchy keeps an internal root unless it holds one
+    // triangle: a root leaf could mix partitions
+    if (parts ? n == 1 : n <= leaf_size) {
         k_single_box<<<1, 1, 0, st>>>(soup, n, d_root_box);
         ctx->launches += 1;
+        if (parts) {
+            k_single_part_root<<<1, 1, 0, st>>>(skeys64, part_roots);
+            ctx->launches += 1;
+        }
         shape->root_is_leaf = 1;
         shape->root_leaf_count = (int)n;
         shape->num_nodes = 0;
     } else {
         cudaMemsetAsync(leaf_rec, 0xFF, sizeof(unsigned long long) * (size_t)n, st);
-        k_karras<<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec);
-        // wave lists reuse the Morton key buffer (free after the hierarchy step)
+        if (parts)
+            k_karras<uint64_t><<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys64, n, leaf_size, nodes, leaf_rec,
+                                                                      part_roots);
+        else
+            k_karras<uint32_t><<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec,
+                                                                      nullptr);
+        // wave lists reuse the Morton key buffer (free after the hierarchy step;
+        // the sorted keys in its upper half are no longer needed either)
         uint32_t* lists[2] = {keys, keys + (n + 1) / 2 + 1};
         cudaMemsetAsync(wave_count, 0, 2 * sizeof(unsigned long long), st);
         k_refit_leaves<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, lists[0], wave_count);
@@ -554,7 +696,8 @@ int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
     BvhShape shape;
     float root_box[6] = {0, 0, 0, 0, 0, 0};
     int status = build_lbvh(ctx, ds->d_vertices, ds->d_indices, ds->d_tri_to_object, nullptr, (int64_t)ds->nt,
-                            leaf_size, ds->d_soup, ds->d_nodes, &shape, root_box);
+                            leaf_size, ds->d_soup, ds->d_nodes, &shape, root_box, ds->d_obj_part, ds->num_parts,
+                            ds->d_part_roots);
     cudaEventRecord(e1, ctx->stream);
     if (status == PIERCE_OK) status = check_cuda(cudaStreamSynchronize(ctx->stream), "bvh build");
     float ms = 0.0f;

@@ -460,6 +460,7 @@ int grid_for(pierce_ctx* ctx, int64_t n, int block) {
 
 struct pierce_mlp {
     pierce_ctx* ctx = nullptr;
+    int device = 0;  // ctx->device, kept for release
     float* d_model = nullptr;  // MODEL_FLOATS
     float* d_adam = nullptr;   // 2 * NP (first and second moments)
     int64_t steps = 0;
@@ -582,6 +583,7 @@ int pierce_mlp_create(pierce_ctx* ctx, const pierce_mlp_params* init, pierce_mlp
     cudaSetDevice(ctx->device);
     pierce_mlp* m = new pierce_mlp();
     m->ctx = ctx;
+    m->device = ctx->device;
     int s = PIERCE_OK;
     do {
         if ((s = device_alloc((void**)&m->d_model, sizeof(float) * MODEL_FLOATS, "mlp model"))) break;
@@ -600,10 +602,8 @@ int pierce_mlp_create(pierce_ctx* ctx, const pierce_mlp_params* init, pierce_mlp
 
 void pierce_mlp_destroy(pierce_mlp* m) {
     if (!m) return;
-    if (m->ctx) {
-        cudaSetDevice(m->ctx->device);
-        cudaStreamSynchronize(m->ctx->stream);
-    }
+    cudaSetDevice(m->device);
+    cudaDeviceSynchronize();
     if (m->d_model) cudaFree(m->d_model);
     if (m->d_adam) cudaFree(m->d_adam);
     delete m;

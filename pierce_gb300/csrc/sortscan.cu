@@ -29,6 +29,19 @@ int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint3
     return check_cuda(e, "radix sort (pairs)");
 }
 
+int sort_u64_pairs(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,
+                   int64_t n, int end_bit) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys_in, keys_out, vals_in, vals_out, n, 0, end_bit,
+                                    ctx->stream);
+    void* tmp = nullptr;
+    if (int s = scratch(ctx, 0, bytes, &tmp)) return s;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, bytes, keys_in, keys_out, vals_in, vals_out, n, 0, end_bit,
+                                                    ctx->stream);
+    ctx->launches += (end_bit + 7) / 8;
+    return check_cuda(e, "radix sort (64-bit pairs)");
+}
+
 int sort_u64_keys(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, int64_t n) {
     size_t bytes = 0;
     cub::DeviceRadixSort::SortKeys(nullptr, bytes, keys_in, keys_out, n, 0, 64, ctx->stream);

@@ -15,6 +15,7 @@ computation happens in ``libpierce_gb300.so``; there is no other path.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -37,6 +38,11 @@ class Context:
         h = C.c_void_p()
         check(self._lib.pierce_ctx_create(device, C.byref(h)), "ctx_create")
         self._h = h
+        self._children = weakref.WeakSet()
+
+    def adopt(self, child) -> None:
+        """Register an object (dataset, sizing network) released before the context."""
+        self._children.add(child)
 
     @property
     def handle(self):
@@ -55,6 +61,8 @@ class Context:
 
     def close(self) -> None:
         if getattr(self, "_h", None):
+            for child in list(getattr(self, "_children", ())):
+                child.close()
             self._lib.pierce_ctx_destroy(self._h)
             self._h = None
 
@@ -78,6 +86,7 @@ class Dataset:
         self._h = handle
         self._keep = keep
         self._lib = capi.lib()
+        ctx.adopt(self)
 
     @classmethod
     def from_arrays(cls, ctx: Context, vertices, indices, tri_to_object, edge_starts, edge_ends, edge_src,
@@ -127,6 +136,13 @@ class Dataset:
     def build(self, tuning: capi.Tuning | None = None) -> None:
         t = tuning if tuning is not None else default_tuning()
         check(self._lib.pierce_dataset_build(self.ctx.handle, self._h, C.byref(t)), "dataset_build")
+
+    def set_partitions(self, obj_part, num_parts: int) -> None:
+        """Partition the objects: joins then pair partition p of A with
+        partition p of B only (a batch of independent joins)."""
+        part = np.ascontiguousarray(obj_part, np.int32)
+        check(self._lib.pierce_dataset_set_partitions(self.ctx.handle, self._h, part.ctypes.data if len(part) else None,
+                                                      int(num_parts)), "dataset_set_partitions")
 
     def download(self) -> dict:
         """The dataset's arrays, copied back to host memory."""

@@ -64,6 +64,7 @@ class SizingModel:
         h = C.c_void_p()
         check(self._lib.pierce_mlp_create(ctx.handle, C.byref(params), C.byref(h)), "mlp_create")
         self._h = h
+        ctx.adopt(self)
 
     @property
     def handle(self):
@@ -219,3 +220,111 @@ def build_training_set(ctx, specs: list[JoinSpec], log=None) -> dict:
 
 def targets(pairs) -> np.ndarray:
     return np.log1p(np.asarray(pairs, np.float64)).astype(np.float32)
+
+
+def evaluate(ctx, model: "SizingModel", specs: list[JoinSpec], log=None) -> dict:
+    """Held-out comparison of the sizing modes on the same joins: two-pass,
+    learned (prediction x 1.2, two-pass on overflow) and fixed memory (an
+    8 GiB table).  Every mode must return the same pair set."""
+    import time
+    from .join import make_opts, run_join
+    rows = []
+    modes = {"two_pass": make_opts(predicate="overlap", sizing="two_pass"),
+             "learned": make_opts(predicate="overlap", sizing="learned", sizing_model=model),
+             "fixed": make_opts(predicate="overlap", sizing="fixed", hash_table_slots=FIXED_MEMORY_SLOTS)}
+    for i, sp in enumerate(specs):
+        a, b = make_datasets(ctx, sp)
+        row = {"n_a": sp.n_a, "n_b": sp.n_b}
+        ref = None
+        for name, o in modes.items():
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            r = run_join(ctx, a, b, o)
+            row[name + "_s"] = time.perf_counter() - t0
+            row[name + "_gpu_ms"] = r.stats["ms_total"]
+            row[name + "_table_bytes"] = 8 * r.stats["hash_slots"]
+            row[name + "_result_bytes"] = 8 * r.stats["result_capacity"]
+            if name == "learned":
+                row["predicted"] = r.stats["predicted_pairs"]
+                row["overflow"] = r.stats["sizing_overflow"]
+            if ref is None:
+                ref = r.pairs
+                row["pairs"] = len(r.pairs)
+            else:
+                row[name + "_identical"] = bool(np.array_equal(r.pairs, ref))
+        a.close()
+        b.close()
+        rows.append(row)
+        if log and (i % 20 == 0 or i == len(specs) - 1):
+            log(f"{i + 1}/{len(specs)} pairs={row['pairs']} predicted={row['predicted']:.0f}")
+    cols = {k: np.array([r[k] for r in rows]) for k in rows[0]} if rows else {}
+    return cols
+
+
+def summarize(ev: dict) -> dict:
+    y = np.log1p(ev["pairs"].astype(np.float64))
+    p = np.log1p(np.maximum(ev["predicted"], 0.0))
+    out = {"joins": int(len(y)), "overflow_rate": float(ev["overflow"].mean()),
+           "mean_abs_log_error": float(np.abs(p - y).mean()),
+           "identical_pair_sets": bool(ev["learned_identical"].all() and ev["fixed_identical"].all())}
+    for m in ("two_pass", "learned", "fixed"):
+        out[m + "_total_s"] = float(ev[m + "_s"].sum())
+        out[m + "_gpu_ms_total"] = float(ev[m + "_gpu_ms"].sum())
+        out[m + "_mean_buffer_mib"] = float((ev[m + "_table_bytes"] + ev[m + "_result_bytes"]).mean() / 2**20)
+    return out
+
+
+def _main(argv=None) -> int:
+    import argparse
+    import json
+    import sys
+    import time
+    from .join import Context
+    ap = argparse.ArgumentParser(prog="python -m pierce_gb300.sizing")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    s1 = sub.add_parser("sweep", help="features + two-pass counts of sweep joins")
+    s1.add_argument("--seed", type=int, default=2024)
+    s1.add_argument("--count", type=int, default=2200)
+    s1.add_argument("--out", default=str(TRAINING_SET))
+    s2 = sub.add_parser("train", help="train the network on a sweep (GPU kernels)")
+    s2.add_argument("--data", default=str(TRAINING_SET))
+    s2.add_argument("--holdout", type=int, default=200)
+    s2.add_argument("--epochs", type=int, default=600)
+    s2.add_argument("--lr", type=float, default=1e-3)
+    s2.add_argument("--out", default=str(TRAINED_MODEL))
+    s3 = sub.add_parser("evaluate", help="sizing modes on the held-out joins of a sweep")
+    s3.add_argument("--model", default=str(TRAINED_MODEL))
+    s3.add_argument("--seed", type=int, default=2024)
+    s3.add_argument("--skip", type=int, default=2000, help="sweep joins before the held-out ones")
+    s3.add_argument("--count", type=int, default=200)
+    s3.add_argument("--out", default="")
+    a = ap.parse_args(argv)
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    ctx = Context(0)
+    t0 = time.perf_counter()
+    if a.cmd == "sweep":
+        data = build_training_set(ctx, sweep(a.seed, a.count), log)
+        np.savez_compressed(a.out, **data)
+        log(f"sweep of {a.count} joins in {time.perf_counter() - t0:.1f} s -> {a.out}")
+    elif a.cmd == "train":
+        with np.load(a.data) as z:
+            X, y = z["features"], targets(z["pairs"])
+        n = len(y) - a.holdout
+        m = SizingModel(ctx, seed=1)
+        loss = m.train(X[:n], y[:n], epochs=a.epochs, lr=a.lr)
+        pred = m.predict(X[n:])
+        m.save(a.out)
+        print(json.dumps({"train_loss_first": float(loss[0]), "train_loss_last": float(loss[-1]),
+                          "holdout_mean_abs_log_error": float(np.abs(pred - y[n:]).mean()),
+                          "train_s": time.perf_counter() - t0}))
+    else:
+        model = SizingModel.load(ctx, a.model)
+        ev = evaluate(ctx, model, sweep(a.seed, a.skip + a.count)[a.skip:], log)
+        if a.out:
+            np.savez_compressed(a.out, **ev)
+        print(json.dumps(summarize(ev)))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

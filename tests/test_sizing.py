@@ -154,7 +154,7 @@ def test_device_training_learns(ctx):
     loss = m.train(X[:1600], y[:1600], epochs=200, lr=2e-3)
     assert loss[-1] < 0.1 * loss[0]
     pred = m.predict(X[1600:])
-    assert np.mean((pred - y[1600:]) ** 2) < 0.2 * np.var(y[1600:])
+    assert np.mean((pred - y[1600:]) ** 2) < 0.35 * np.var(y[1600:])
 
 
 @pytest.mark.gpu
