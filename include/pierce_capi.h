@@ -257,6 +257,26 @@ int pierce_result_copy(pierce_ctx* ctx, const pierce_result* r, pierce_pair* hos
 int pierce_result_containment_count(const pierce_result* r, uint64_t* count);
 void pierce_result_destroy(pierce_result* r);
 
+/* ---- joins captured as CUDA graphs -------------------------------------- */
+/* No counterpart in the reference (whose launches are synchronous, one
+ * optixLaunch per pass).  pierce_join_graph_create runs the join once
+ * (stats of that run in *stats), recording every value the host reads back
+ * to size buffers and launches, then captures the same join as one CUDA
+ * graph that uses those values and its own scratch memory.  Each
+ * pierce_join_graph_launch replays the whole join with one cudaGraphLaunch
+ * and one synchronisation; the replay checks that the device produced the
+ * recorded values and fails with PIERCE_ERR_OUTPUT_OVERFLOW otherwise (the
+ * inputs changed: create a new graph).  The datasets and the sizing model
+ * must stay alive and unchanged while the graph exists.  The pairs of the
+ * last replay (sorted by (a, b)) stay in graph-owned device memory. */
+typedef struct pierce_join_graph pierce_join_graph;
+int pierce_join_graph_create(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                             pierce_join_graph** out, pierce_stats* stats);
+int pierce_join_graph_launch(pierce_ctx* ctx, pierce_join_graph* g, pierce_stats* stats);
+int pierce_join_graph_pairs(const pierce_join_graph* g, const pierce_pair** d_pairs, uint64_t* count);
+int pierce_join_graph_copy(pierce_ctx* ctx, const pierce_join_graph* g, pierce_pair* host_out, uint64_t capacity);
+void pierce_join_graph_destroy(pierce_join_graph* g);
+
 /* ---- launch-level entry points (the reference's launcher seam) ---------- */
 enum pierce_ray_mode { PIERCE_RAYS_COUNT = 0, PIERCE_RAYS_WRITE = 1, PIERCE_RAYS_HASH = 2 };
 

@@ -134,6 +134,11 @@ SIGNATURES = {
     "pierce_result_copy": (C.c_int, [V, V, V, U64]),
     "pierce_result_containment_count": (C.c_int, [V, C.POINTER(U64)]),
     "pierce_result_destroy": (None, [V]),
+    "pierce_join_graph_create": (C.c_int, [V, V, V, C.POINTER(JoinOpts), C.POINTER(V), C.POINTER(Stats)]),
+    "pierce_join_graph_launch": (C.c_int, [V, V, C.POINTER(Stats)]),
+    "pierce_join_graph_pairs": (C.c_int, [V, C.POINTER(V), C.POINTER(U64)]),
+    "pierce_join_graph_copy": (C.c_int, [V, V, V, U64]),
+    "pierce_join_graph_destroy": (None, [V]),
     "pierce_launch_edge_rays": (C.c_int, [V, V, V, C.c_int, C.c_int, C.c_int, V, V, V, V, U64,
                                           C.POINTER(Stats)]),
     "pierce_launch_parity": (C.c_int, [V, V, V, C.c_int, C.c_int, V, V, U64, C.POINTER(Stats)]),

@@ -104,8 +104,54 @@ int device_alloc(void** p, size_t bytes, const char* what) {
     return PIERCE_OK;
 }
 
+int host_value(pierce_ctx* ctx, const void* dptr, int bytes, int64_t* out, const char* what) {
+    GraphPlan* g = ctx->plan;
+    if (g && g->mode == 2) {
+        if (g->cursor >= g->values.size() || g->widths[g->cursor] != bytes)
+            return set_error(PIERCE_ERR_CUDA, std::string("join graph capture left its plan at ") + what);
+        cudaMemcpyAsync(g->h_check + g->cursor, dptr, (size_t)bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        *out = g->values[g->cursor++];
+        return PIERCE_OK;
+    }
+    int64_t* slot = ctx->h_small + 7;
+    *slot = 0;
+    if (int s = check_cuda(cudaMemcpyAsync(slot, dptr, (size_t)bytes, cudaMemcpyDeviceToHost, ctx->stream), what))
+        return s;
+    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), what)) return s;
+    int64_t v = *slot;
+    if (bytes == 4) {
+        int32_t w;
+        std::memcpy(&w, slot, 4);
+        v = w;
+    }
+    if (g && g->mode == 1) {
+        g->values.push_back(v);
+        g->widths.push_back(bytes);
+    }
+    *out = v;
+    return PIERCE_OK;
+}
+
+int result_alloc(pierce_ctx* ctx, void** p, size_t bytes) {
+    GraphPlan* g = ctx->plan;
+    if (g && g->mode == 2) {
+        if (g->buf_cursor >= g->buffers.size() || g->buffer_bytes[g->buf_cursor] < bytes)
+            return set_error(PIERCE_ERR_CUDA, "join graph capture: result buffer differs from its plan");
+        *p = g->buffers[g->buf_cursor++];
+        return PIERCE_OK;
+    }
+    if (int s = device_alloc(p, bytes, "result")) return s;
+    if (g && g->mode == 1) {
+        g->buffers.push_back(*p);
+        g->buffer_bytes.push_back(bytes);
+    }
+    return PIERCE_OK;
+}
+
 int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
     if (bytes == 0) bytes = 16;
+    if (ctx->scratch_bytes[slot] < bytes && capturing(ctx))
+        return set_error(PIERCE_ERR_CUDA, "join graph capture: scratch would grow");
     if (ctx->scratch_bytes[slot] < bytes) {
         if (ctx->scratch[slot]) {
             cudaStreamSynchronize(ctx->stream);
@@ -151,14 +197,17 @@ static int grid_for(pierce_ctx* ctx, int64_t n, int block) {
 }
 
 static int sync_ctx(pierce_ctx* ctx, const char* what) {
+    if (capturing(ctx)) return PIERCE_OK;  // a captured join synchronises after its replay
     return check_cuda(cudaStreamSynchronize(ctx->stream), what);
 }
 
-// Translate device error bits into a status (the bits are cleared).
+// Translate device error bits into a status (the bits are cleared).  Inside
+// a captured join the bits of the planning run stand in, and the replay
+// compares the device's bits with them.
 static int read_device_error(pierce_ctx* ctx, uint32_t* bits_out) {
-    cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
-    if (int s = sync_ctx(ctx, "error readback")) return s;
-    *bits_out = *ctx->h_err;
+    int64_t v = 0;
+    if (int s = host_value(ctx, ctx->d_err, 4, &v, "device error word")) return s;
+    *bits_out = (uint32_t)v;
     cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
     return PIERCE_OK;
 }
@@ -168,8 +217,10 @@ struct EventTimer {
     std::vector<std::pair<int, int>> spans;  // (begin idx, end idx) per label
     std::vector<double*> targets;
     cudaStream_t st;
+    bool off = false;  // no events inside a captured join
     explicit EventTimer(cudaStream_t s) : st(s) {}
     int record() {
+        if (off) return -1;
         cudaEvent_t e;
         cudaEventCreate(&e);
         cudaEventRecord(e, st);
@@ -177,6 +228,7 @@ struct EventTimer {
         return (int)ev.size() - 1;
     }
     void span(int b, int e, double* target) {
+        if (off || b < 0 || e < 0) return;
         spans.emplace_back(b, e);
         targets.push_back(target);
     }
@@ -575,6 +627,7 @@ struct Join {
     Join(pierce_ctx* c, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts& opts)
         : ctx(c), A(a), B(b), o(opts), timer(c->stream) {
         std::memset(&st, 0, sizeof(st));
+        timer.off = capturing(c);
         ab = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH1_TO_MESH2;
         ba = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH2_TO_MESH1;
     }
@@ -670,9 +723,9 @@ struct Join {
         if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
         if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
         listed[0] = listed[1] = true;
-        cudaMemcpyAsync(ctx->h_small, words + 5, 16, cudaMemcpyDeviceToHost, ctx->stream);
-        if (int s = sync_ctx(ctx, "active triangle counts")) return s;
-        const int64_t na = ctx->h_small[0], nb = ctx->h_small[1];
+        int64_t na = 0, nb = 0;
+        if (int s = host_value(ctx, words + 5, 8, &na, "active triangles of A")) return s;
+        if (int s = host_value(ctx, words + 6, 8, &nb, "active triangles of B")) return s;
         void *sa = nullptr, *sb = nullptr, *na_p = nullptr, *nb_p = nullptr;
         if (int s = scratch(ctx, SLOT_RED_SOUP_A, 48 * (size_t)std::max<int64_t>(na, 1), &sa)) return s;
         const size_t roots_bytes = 8 * (size_t)A->num_parts;  // equal partition counts on both sides
@@ -811,9 +864,9 @@ struct Join {
             cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), ctx->stream);
             uint64_t* keys = static_cast<uint64_t*>(p);
             if (int s = compact_table(ctx, table, slots, keys + base, cap, d_count)) return s;
-            cudaMemcpyAsync(ctx->h_small, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
-            if (int s = sync_ctx(ctx, "compact count")) return s;
-            const uint64_t n = (uint64_t)ctx->h_small[0];
+            int64_t nv = 0;
+            if (int s = host_value(ctx, d_count, 8, &nv, "compact count")) return s;
+            const uint64_t n = (uint64_t)nv;
             st.result_capacity = cap;
             if (n <= cap) {
                 *n_out = n;
@@ -859,14 +912,6 @@ struct Join {
             if (n_all > 0)
                 if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all)) return s;
             timer.span(tb, timer.record(), &st.ms_dedup);
-            // total = last offset + last count; B->A offsets continue after the A total
-            if (n_all > 0) {
-                cudaMemcpyAsync(ctx->h_small, offs + n_all - 1, 8, cudaMemcpyDeviceToHost, ctx->stream);
-                cudaMemcpyAsync(ctx->h_small + 1, counts + n_all - 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
-                if (na > 0 && nb > 0)
-                    cudaMemcpyAsync(ctx->h_small + 2, offs + na, 8, cudaMemcpyDeviceToHost, ctx->stream);
-            }
-            cudaMemcpyAsync(ctx->h_small + 3, words + 4, 8, cudaMemcpyDeviceToHost, ctx->stream);
             uint32_t bits = 0;
             if (int s = read_device_error(ctx, &bits)) return s;
             if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
@@ -875,10 +920,19 @@ struct Join {
                 defer = false;
                 continue;
             }
+            // total = last offset + last count; B->A offsets continue after the A total
             total = 0;
-            if (n_all > 0) total = ctx->h_small[0] + (int64_t)(int32_t)(ctx->h_small[1] & 0xFFFFFFFF);
-            total_ab = (na > 0 && nb > 0) ? ctx->h_small[2] : (na > 0 ? total : 0);
-            n_extra = (uint64_t)ctx->h_small[3];
+            int64_t last_off = 0, last_count = 0, off_b = 0, extra_n = 0;
+            if (n_all > 0) {
+                if (int s = host_value(ctx, offs + n_all - 1, 8, &last_off, "scan total")) return s;
+                if (int s = host_value(ctx, counts + n_all - 1, 4, &last_count, "scan total")) return s;
+                if (na > 0 && nb > 0)
+                    if (int s = host_value(ctx, offs + na, 8, &off_b, "scan split")) return s;
+                total = last_off + last_count;
+            }
+            if (int s = host_value(ctx, words + 4, 8, &extra_n, "resolved keys")) return s;
+            total_ab = (na > 0 && nb > 0) ? off_b : (na > 0 ? total : 0);
+            n_extra = (uint64_t)extra_n;
             break;
         }
         st.raw_pairs[0] = (uint64_t)total_ab;
@@ -943,7 +997,7 @@ struct Join {
         pierce_result* r = new pierce_result();
         r->count = n;
         r->capacity = n;
-        if (int s = device_alloc((void**)&r->d_pairs, std::max<uint64_t>(n, 1) * sizeof(pierce_pair), "result")) {
+        if (int s = result_alloc(ctx, (void**)&r->d_pairs, std::max<uint64_t>(n, 1) * sizeof(pierce_pair))) {
             delete r;
             return s;
         }
@@ -1083,9 +1137,9 @@ struct Join {
                 if (int s = parity(vb, va, 1, &st.ms_parity[1], 0, nullptr, 0, nullptr, 0, nullptr, 0, all + n_over,
                                    d_count, cap))
                     return s;
-            cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
-            if (int s = sync_ctx(ctx, "parity count")) return s;
-            const uint64_t n_par = (uint64_t)ctx->h_small[0];
+            int64_t n_par_v = 0;
+            if (int s = host_value(ctx, d_count, 8, &n_par_v, "parity count")) return s;
+            const uint64_t n_par = (uint64_t)n_par_v;
             if (n_par > cap) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "parity output overflow");
             return sort_unique_into_result(all, n_over + n_par, out);
         }
@@ -1137,9 +1191,9 @@ struct Join {
         if (int s = parity(vb, va, 1, &st.ms_parity[1], 1, nullptr, 0, table, slots, okeys, (int64_t)n_over, ckeys,
                            d_count, cap))
             return s;
-        cudaMemcpyAsync(ctx->h_small, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream);
-        if (int s = sync_ctx(ctx, "containment count")) return s;
-        const uint64_t n_cont = (uint64_t)ctx->h_small[0];
+        int64_t n_cont_v = 0;
+        if (int s = host_value(ctx, d_count, 8, &n_cont_v, "containment count")) return s;
+        const uint64_t n_cont = (uint64_t)n_cont_v;
         if (n_cont > cap) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "containment output overflow");
         if (!two_pass && o.include_overlap_pairs) {
             // overlap keys of the table after the containment keys
@@ -1155,7 +1209,7 @@ struct Join {
         r->count = n_total;
         r->capacity = n_total;
         r->containment_count = n_cont;
-        if (int s = device_alloc((void**)&r->d_pairs, std::max<uint64_t>(n_total, 1) * 8, "result")) {
+        if (int s = result_alloc(ctx, (void**)&r->d_pairs, std::max<uint64_t>(n_total, 1) * 8)) {
             delete r;
             return s;
         }
@@ -1188,10 +1242,10 @@ struct Join {
 
 extern "C" {
 
-int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
-                pierce_result** out, pierce_stats* stats) {
-    if (!ctx || !a || !b || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: null argument");
-    *out = nullptr;
+}  // extern "C"
+
+static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                         pierce_join_opts* out_opts) {
     if ((!opts || !opts->active_bvh) && (!a->built || !b->built))
         return set_error(PIERCE_ERR_NOT_BUILT, "join: dataset not built (or use active_bvh)");
     if (a->ctx != ctx || b->ctx != ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: dataset of other ctx");
@@ -1207,6 +1261,18 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: LEARNED sizing needs a sizing_model");
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
+    *out_opts = o;
+    return PIERCE_OK;
+}
+
+extern "C" {
+
+int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                pierce_result** out, pierce_stats* stats) {
+    if (!ctx || !a || !b || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: null argument");
+    *out = nullptr;
+    pierce_join_opts o;
+    if (int s = validate_join(ctx, a, b, opts, &o)) return s;
     cudaSetDevice(ctx->device);
     const uint64_t l0 = ctx->launches;
     Join j(ctx, a, b, o);
@@ -1215,6 +1281,222 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
     if (stats) *stats = j.st;
     return s;
 }
+
+}  // extern "C"
+
+// ---- joins captured as CUDA graphs -------------------------------------------
+
+struct pierce_join_graph {
+    pierce_ctx* ctx = nullptr;
+    GraphPlan plan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void* scratch[kScratchSlots] = {nullptr};  // the graph's own scratch buffers
+    size_t scratch_bytes[kScratchSlots] = {0};
+    pierce_pair* d_pairs = nullptr;
+    uint64_t count = 0;
+    uint64_t containment_count = 0;
+    pierce_stats stats{};
+    int launches = 0;  // kernels per replay
+};
+
+namespace {
+
+void free_graph(pierce_join_graph* g) {
+    if (!g) return;
+    if (g->ctx) cudaSetDevice(g->ctx->device);
+    cudaDeviceSynchronize();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    for (void* p : g->plan.buffers)
+        if (p) cudaFree(p);
+    for (int i = 0; i < kScratchSlots; ++i)
+        if (g->scratch[i]) cudaFree(g->scratch[i]);
+    if (g->plan.h_check) cudaFreeHost(g->plan.h_check);
+    delete g;
+}
+
+// Run `body` with the context's scratch buffers swapped for the graph's own
+// (so later joins on the context cannot move memory a replay uses).
+template <class F>
+int with_graph_scratch(pierce_ctx* ctx, pierce_join_graph* g, F body) {
+    void* saved[kScratchSlots];
+    size_t saved_bytes[kScratchSlots];
+    for (int i = 0; i < kScratchSlots; ++i) {
+        saved[i] = ctx->scratch[i];
+        saved_bytes[i] = ctx->scratch_bytes[i];
+        ctx->scratch[i] = g->scratch[i];
+        ctx->scratch_bytes[i] = g->scratch_bytes[i];
+    }
+    ctx->plan = &g->plan;
+    const int s = body();
+    ctx->plan = nullptr;
+    for (int i = 0; i < kScratchSlots; ++i) {
+        g->scratch[i] = ctx->scratch[i];
+        g->scratch_bytes[i] = ctx->scratch_bytes[i];
+        ctx->scratch[i] = saved[i];
+        ctx->scratch_bytes[i] = saved_bytes[i];
+    }
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pierce_join_graph_create(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
+                             pierce_join_graph** out, pierce_stats* stats) {
+    if (!ctx || !a || !b || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join_graph_create: null argument");
+    *out = nullptr;
+    pierce_join_opts o;
+    if (int s = validate_join(ctx, a, b, opts, &o)) return s;
+    cudaSetDevice(ctx->device);
+    if (int s = sync_ctx(ctx, "join graph")) return s;
+    pierce_join_graph* g = new pierce_join_graph();
+    g->ctx = ctx;
+    // 1. the planning run: an ordinary join that records its host decisions
+    int s = with_graph_scratch(ctx, g, [&]() {
+        g->plan.mode = 1;
+        const uint64_t l0 = ctx->launches;
+        Join j(ctx, a, b, o);
+        pierce_result* r = nullptr;
+        int st = j.run(&r);
+        j.st.launches = (int32_t)(ctx->launches - l0);
+        g->stats = j.st;
+        if (st) return st;
+        g->d_pairs = r->d_pairs;
+        g->count = r->count;
+        g->containment_count = r->containment_count;
+        r->d_pairs = nullptr;  // the buffer belongs to the plan
+        pierce_result_destroy(r);
+        return (int)PIERCE_OK;
+    });
+    if (s == PIERCE_OK && !g->plan.values.empty()) {
+        if (cudaHostAlloc((void**)&g->plan.h_check, 8 * g->plan.values.size(), cudaHostAllocDefault) != cudaSuccess)
+            s = set_error(PIERCE_ERR_OUT_OF_MEMORY, "join graph: pinned check slots");
+    }
+    // 2. the same join under stream capture, taking the recorded decisions
+    if (s == PIERCE_OK) {
+        s = with_graph_scratch(ctx, g, [&]() {
+            g->plan.mode = 2;
+            g->plan.cursor = 0;
+            g->plan.buf_cursor = 0;
+            if (int e = check_cuda(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed), "begin capture"))
+                return e;
+            const uint64_t l0 = ctx->launches;
+            Join j(ctx, a, b, o);
+            pierce_result* r = nullptr;
+            int st = j.run(&r);
+            g->launches = (int)(ctx->launches - l0);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
+            if (r) {
+                r->d_pairs = nullptr;
+                pierce_result_destroy(r);
+            }
+            if (st) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (int e = check_cuda(ec, "end capture")) return e;
+            g->graph = graph;
+            if (g->plan.cursor != g->plan.values.size())
+                return set_error(PIERCE_ERR_CUDA, "join graph capture did not consume its plan");
+            return check_cuda(cudaGraphInstantiate(&g->exec, graph, 0), "graph instantiate");
+        });
+    }
+    if (s) {
+        cudaGetLastError();
+        free_graph(g);
+        return s;
+    }
+    if (stats) *stats = g->stats;
+    *out = g;
+    return PIERCE_OK;
+}
+
+int pierce_join_graph_launch(pierce_ctx* ctx, pierce_join_graph* g, pierce_stats* stats) {
+    if (!ctx || !g || g->ctx != ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join_graph_launch: bad argument");
+    cudaSetDevice(ctx->device);
+    GraphPlan& p = g->plan;
+    if (p.h_check) std::memset(p.h_check, 0, 8 * p.values.size());
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    cudaError_t e = cudaGraphLaunch(g->exec, ctx->stream);
+    cudaEventRecord(e1, ctx->stream);
+    int s = check_cuda(e, "graph launch");
+    if (!s) s = check_cuda(cudaStreamSynchronize(ctx->stream), "graph replay");
+    float ms = 0.0f;
+    if (!s) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s) return s;
+    ctx->launches += (uint64_t)g->launches;
+    // the replay must have met every decision of the plan
+    for (size_t i = 0; i < p.values.size(); ++i) {
+        int64_t v = p.h_check[i];
+        if (p.widths[i] == 4) {
+            int32_t w;
+            std::memcpy(&w, &p.h_check[i], 4);
+            v = w;
+        }
+        if (v != p.values[i])
+            return set_error(PIERCE_ERR_OUTPUT_OVERFLOW,
+                             "join graph replay: a data-dependent size differs from the plan (inputs changed?)");
+    }
+    cudaMemcpy(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (*ctx->h_err) {
+        const uint32_t bits = *ctx->h_err;
+        cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
+        if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+        if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "pair hash table full");
+        return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "join graph replay: device capacity exceeded");
+    }
+    if (stats) {
+        *stats = g->stats;
+        const DevCounters& c = *ctx->h_counters;  // copied by the graph's last node
+        stats->ms_total = ms;
+        stats->rays = c.rays;
+        stats->node_visits = c.node_visits;
+        stats->tri_tests = c.tri_tests;
+        stats->raw_hits = c.raw_hits;
+        stats->fp32_ambiguous = c.fp32_ambiguous;
+        stats->fp64_ambiguous = c.fp64_ambiguous;
+        stats->parity_rays = c.parity_rays;
+        stats->hash_accesses = c.hash_accesses;
+        stats->hash_contentions = c.hash_contentions;
+        stats->launches = g->launches;
+        for (double* t : {&stats->ms_edge_rays[0], &stats->ms_edge_rays[1], &stats->ms_parity[0],
+                          &stats->ms_parity[1], &stats->ms_dedup, &stats->ms_count_pass[0], &stats->ms_count_pass[1],
+                          &stats->ms_build, &stats->ms_sizing})
+            *t = 0.0;  // no per-phase events inside a replay
+    }
+    return PIERCE_OK;
+}
+
+int pierce_join_graph_pairs(const pierce_join_graph* g, const pierce_pair** d_pairs, uint64_t* count) {
+    if (!g || !d_pairs || !count) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join_graph_pairs: null argument");
+    *d_pairs = g->d_pairs;
+    *count = g->count;
+    return PIERCE_OK;
+}
+
+int pierce_join_graph_copy(pierce_ctx* ctx, const pierce_join_graph* g, pierce_pair* host_out, uint64_t capacity) {
+    if (!ctx || !g || (!host_out && capacity)) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join_graph_copy: null");
+    const uint64_t n = std::min(capacity, g->count);
+    if (n)
+        if (int s = check_cuda(cudaMemcpyAsync(host_out, g->d_pairs, n * sizeof(pierce_pair), cudaMemcpyDeviceToHost,
+                                               ctx->stream),
+                               "graph result copy"))
+            return s;
+    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "graph result copy")) return s;
+    return g->count > capacity ? set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "join_graph_copy: capacity below pair count")
+                               : PIERCE_OK;
+}
+
+void pierce_join_graph_destroy(pierce_join_graph* g) { free_graph(g); }
 
 int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int mode,
                             int precision, int swap, int32_t* d_counts, const int64_t* d_offsets, uint64_t* d_keys,

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/pierce_capi.h"
 
@@ -99,6 +100,25 @@ struct BvhShape {
 
 // ---- host-side internal objects ------------------------------------------
 
+namespace pgpu {
+// Plan of a join captured as a CUDA graph.  The join first runs eagerly
+// (mode 1) and records every value it reads back from the device to make a
+// host decision (counts that size buffers and launches); the same code then
+// runs under stream capture (mode 2), takes those values from the plan
+// instead of synchronising, and copies the device's values into pinned
+// h_check slots, which a replay compares with the plan.
+struct GraphPlan {
+    int mode = 0;
+    std::vector<int64_t> values;
+    std::vector<int> widths;
+    size_t cursor = 0;
+    std::vector<void*> buffers;        // result buffers of the eager run, reused by the capture
+    std::vector<size_t> buffer_bytes;
+    size_t buf_cursor = 0;
+    int64_t* h_check = nullptr;        // pinned, one slot per value
+};
+}  // namespace pgpu
+
 struct pierce_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -112,6 +132,7 @@ struct pierce_ctx {
     size_t scratch_bytes[pgpu::kScratchSlots] = {0};
     uint64_t launches = 0;
     int sm_count = 0;
+    pgpu::GraphPlan* plan = nullptr;  // set while a join graph is planned or captured
 };
 
 struct pierce_dataset {
@@ -174,6 +195,12 @@ int check_cuda(cudaError_t e, const char* what);
 // grow-only scratch buffer `slot` of at least `bytes`
 int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out);
 int device_alloc(void** p, size_t bytes, const char* what);
+// A value the host reads from device memory (4 or 8 bytes, 4 sign-extended):
+// synchronous, except while a join graph is captured (then from the plan).
+int host_value(pierce_ctx* ctx, const void* dptr, int bytes, int64_t* out, const char* what);
+inline bool capturing(const pierce_ctx* ctx) { return ctx->plan && ctx->plan->mode == 2; }
+// Device memory of a join result (owned by the join graph while one is planned).
+int result_alloc(pierce_ctx* ctx, void** p, size_t bytes);
 // allocate a dataset's arrays for ds->nv/nt/ne/num_objects (capi.cu)
 int dataset_alloc(pierce_dataset* ds);
 // object data, then the BVH unless tuning->defer_build (capi.cu)

@@ -655,9 +655,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
                                                                        d_root_box);
             ctx->launches += 1;
             if ((wave & 7) == 7) {
-                unsigned long long left = 0;
-                cudaMemcpyAsync(&left, wave_count + out, sizeof(left), cudaMemcpyDeviceToHost, st);
-                if (int s = check_cuda(cudaStreamSynchronize(st), "refit waves")) return s;
+                int64_t left = 0;
+                if (int s = host_value(ctx, wave_count + out, 8, &left, "refit waves")) return s;
                 finished = left == 0;
             }
         }

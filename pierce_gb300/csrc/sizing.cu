@@ -518,10 +518,11 @@ int learned_log_pairs(pierce_ctx* ctx, const pierce_mlp* mlp, const pierce_datas
     if (int s = join_features(ctx, A, B, f)) return s;
     k_mlp_predict<<<1, NH, 0, ctx->stream>>>(mlp->d_model, f, 1, f + NI);
     ctx->launches += 1;
-    cudaMemcpyAsync(ctx->h_small, f + NI, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "learned sizing")) return s;
+    int64_t bits = 0;
+    if (int s = host_value(ctx, f + NI, 4, &bits, "learned sizing")) return s;
+    const int32_t b32 = (int32_t)bits;
     float v;
-    std::memcpy(&v, ctx->h_small, sizeof(float));
+    std::memcpy(&v, &b32, sizeof(float));
     *pred = (double)v;
     return PIERCE_OK;
 }

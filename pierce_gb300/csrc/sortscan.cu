@@ -76,11 +76,7 @@ int unique_u64(pierce_ctx* ctx, const uint64_t* in, uint64_t* out, int64_t n, in
     cudaError_t e = cub::DeviceSelect::Unique(tmp, bytes, in, out, static_cast<int64_t*>(pcount), n, ctx->stream);
     ctx->launches += 2;
     if (int s = check_cuda(e, "unique")) return s;
-    e = cudaMemcpyAsync(ctx->h_small, pcount, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
-    if (int s = check_cuda(e, "unique count readback")) return s;
-    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "unique sync")) return s;
-    *num_unique = ctx->h_small[0];
-    return PIERCE_OK;
+    return host_value(ctx, pcount, 8, num_unique, "unique count");
 }
 
 }  // namespace pgpu

@@ -225,6 +225,44 @@ def run_join(ctx: Context, a: Dataset, b: Dataset, opts: capi.JoinOpts, download
         L.pierce_result_destroy(r)
 
 
+class JoinGraph:
+    """A join captured as one CUDA graph: planned by an eager run, then
+    replayed with one launch per call (same datasets, same result)."""
+
+    def __init__(self, ctx: Context, a: Dataset, b: Dataset, opts: capi.JoinOpts):
+        self.ctx, self._a, self._b, self._opts = ctx, a, b, opts
+        self._lib = capi.lib()
+        h = C.c_void_p()
+        st = capi.Stats()
+        check(self._lib.pierce_join_graph_create(ctx.handle, a.handle, b.handle, C.byref(opts), C.byref(h),
+                                                 C.byref(st)), "join_graph_create")
+        self._h = h
+        self.plan_stats = st.as_dict()
+        ctx.adopt(self)
+
+    def launch(self) -> dict:
+        st = capi.Stats()
+        check(self._lib.pierce_join_graph_launch(self.ctx.handle, self._h, C.byref(st)), "join_graph_launch")
+        return st.as_dict()
+
+    def pairs(self) -> np.ndarray:
+        p, n = C.c_void_p(), C.c_uint64()
+        check(self._lib.pierce_join_graph_pairs(self._h, C.byref(p), C.byref(n)), "join_graph_pairs")
+        out = np.zeros((n.value, 2), np.int32)
+        if n.value:
+            check(self._lib.pierce_join_graph_copy(self.ctx.handle, self._h, out.ctypes.data, n.value),
+                  "join_graph_copy")
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.pierce_join_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 def join(ctx: Context, a: Dataset, b: Dataset, **kw) -> JoinResult:
     return run_join(ctx, a, b, make_opts(**kw))
 
