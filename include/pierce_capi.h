@@ -153,6 +153,11 @@ typedef struct pierce_join_opts {
     int32_t active_bvh;           /* 1 (default): build per-join BVHs over the triangles of objects whose box
                                      meets an object box of the other side (datasets need no BVH of their own) */
     const pierce_mlp* sizing_model; /* LEARNED sizing: trained network (pierce_mlp_create) */
+    /* tuning (0: default); pierce_autotune_join picks them */
+    int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets') */
+    int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
+    int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 32) */
+    int32_t reserved;
 } pierce_join_opts;
 
 typedef struct pierce_stats {
@@ -257,6 +262,27 @@ int pierce_result_copy(pierce_ctx* ctx, const pierce_result* r, pierce_pair* hos
 int pierce_result_containment_count(const pierce_result* r, uint64_t* count);
 void pierce_result_destroy(pierce_result* r);
 
+/* ---- autotuning ------------------------------------------------------------ */
+/* No counterpart in the reference.  Times the join (a, b) with `base`
+ * options over a grid of tuning values, one parameter at a time (leaf size
+ * of the per-join hierarchies {1, 2, 4, 8} when base->active_bvh, rays per
+ * warp {32, 64, 128}, stack depth {8, 16, 32}, hash load factor
+ * {0.25, 0.5, 0.75} when the sizing uses a hash set), each trial the best
+ * of `repeats` timed runs after one untimed run.  *best receives the
+ * fastest values; trials[0 .. *num_trials) every trial (max_trials slots,
+ * may be NULL). */
+typedef struct pierce_tuned {
+    int32_t leaf_size;
+    int32_t rays_per_warp;
+    int32_t stack_depth;
+    int32_t reserved;
+    double hash_load_factor;
+    double ms;                    /* best GPU time of the join with these values */
+} pierce_tuned;
+int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* base,
+                         int32_t repeats, pierce_tuned* best, pierce_tuned* trials, int32_t max_trials,
+                         int32_t* num_trials);
+
 /* ---- joins captured as CUDA graphs -------------------------------------- */
 /* No counterpart in the reference (whose launches are synchronous, one
  * optixLaunch per pass).  pierce_join_graph_create runs the join once
@@ -267,8 +293,10 @@ void pierce_result_destroy(pierce_result* r);
  * and one synchronisation; the replay checks that the device produced the
  * recorded values and fails with PIERCE_ERR_OUTPUT_OVERFLOW otherwise (the
  * inputs changed: create a new graph).  The datasets and the sizing model
- * must stay alive and unchanged while the graph exists.  The pairs of the
- * last replay (sorted by (a, b)) stay in graph-owned device memory. */
+ * must stay alive and unchanged while the graph exists, and the context
+ * must outlive it.  The graph takes over the context's scratch memory and
+ * returns it when destroyed.  The pairs of the last replay (sorted by
+ * (a, b)) stay in graph-owned device memory. */
 typedef struct pierce_join_graph pierce_join_graph;
 int pierce_join_graph_create(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* opts,
                              pierce_join_graph** out, pierce_stats* stats);

@@ -67,7 +67,8 @@ class JoinOpts(C.Structure):
     _fields_ = [("predicate", I32), ("direction", I32), ("sizing", I32), ("precision", I32),
                 ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
                 ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
-                ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V)]
+                ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V),
+                ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("reserved", I32)]
 
 
 class Stats(C.Structure):
@@ -103,6 +104,11 @@ class MlpTrainOpts(C.Structure):
                 ("beta2", F), ("eps", F)]
 
 
+class Tuned(C.Structure):
+    _fields_ = [("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("reserved", I32),
+                ("hash_load_factor", D), ("ms", D)]
+
+
 class DatasetInfo(C.Structure):
     _fields_ = [("num_vertices", U64), ("num_triangles", U64), ("num_edges", U64),
                 ("num_objects", I32), ("built", I32), ("num_nodes", U64), ("device_bytes", U64),
@@ -134,6 +140,8 @@ SIGNATURES = {
     "pierce_result_copy": (C.c_int, [V, V, V, U64]),
     "pierce_result_containment_count": (C.c_int, [V, C.POINTER(U64)]),
     "pierce_result_destroy": (None, [V]),
+    "pierce_autotune_join": (C.c_int, [V, V, V, C.POINTER(JoinOpts), I32, C.POINTER(Tuned), V, I32,
+                                       C.POINTER(I32)]),
     "pierce_join_graph_create": (C.c_int, [V, V, V, C.POINTER(JoinOpts), C.POINTER(V), C.POINTER(Stats)]),
     "pierce_join_graph_launch": (C.c_int, [V, V, C.POINTER(Stats)]),
     "pierce_join_graph_pairs": (C.c_int, [V, C.POINTER(V), C.POINTER(U64)]),

@@ -737,12 +737,14 @@ struct Join {
         int2* roots_a = A->num_parts ? reinterpret_cast<int2*>((Node*)na_p + std::max<int64_t>(na, 1)) : nullptr;
         int2* roots_b = B->num_parts ? reinterpret_cast<int2*>((Node*)nb_p + std::max<int64_t>(nb, 1)) : nullptr;
         BvhShape shA, shB;
+        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
+        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
         if (int s = build_lbvh(ctx, A->d_vertices, A->d_indices, A->d_tri_to_object, (const uint32_t*)ta, na,
-                               A->leaf_size, (float4*)sa, (Node*)na_p, &shA, nullptr, A->d_obj_part, A->num_parts,
+                               leaf_a, (float4*)sa, (Node*)na_p, &shA, nullptr, A->d_obj_part, A->num_parts,
                                roots_a))
             return s;
         if (int s = build_lbvh(ctx, B->d_vertices, B->d_indices, B->d_tri_to_object, (const uint32_t*)tb, nb,
-                               B->leaf_size, (float4*)sb, (Node*)nb_p, &shB, nullptr, B->d_obj_part, B->num_parts,
+                               leaf_b, (float4*)sb, (Node*)nb_p, &shB, nullptr, B->d_obj_part, B->num_parts,
                                roots_b))
             return s;
         va.part_roots = roots_a;
@@ -793,6 +795,8 @@ struct Join {
                 ro.cursor = words + 2;
                 if (mode == 0) cudaMemsetAsync(counts, 0, 4 * (size_t)src.num_edges, ctx->stream);
             }
+            ro.rays_per_fetch = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
+            ro.short_stack = o.stack_depth > 0 ? o.stack_depth : -1;
             const int prec = precision_mode();
             if (prec == 2) {
                 ro.amb_queue = amb_queue;
@@ -800,8 +804,7 @@ struct Join {
                 ro.amb_cap = amb_cap;
                 if (mode != 1) cudaMemsetAsync(words + 3, 0, 8, ctx->stream);
             }
-            if (int s = launch_edge_rays(ctx, src, tgt, mode, prec, d, counts, offs, keys, table, slots,
-                                         (ro.list || ro.amb_queue) ? &ro : nullptr))
+            if (int s = launch_edge_rays(ctx, src, tgt, mode, prec, d, counts, offs, keys, table, slots, &ro))
                 return s;
             if (prec == 2 && mode != 1)
                 if (int s = launch_resolve(ctx, src, tgt, d, mode == 2 ? table : nullptr, slots, &ro, extra_keys,
@@ -1261,6 +1264,9 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: LEARNED sizing needs a sizing_model");
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
+    if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
+        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
     *out_opts = o;
     return PIERCE_OK;
 }
@@ -1280,6 +1286,66 @@ int pierce_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pie
     j.st.launches = (int32_t)(ctx->launches - l0);
     if (stats) *stats = j.st;
     return s;
+}
+
+int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts* base,
+                         int32_t repeats, pierce_tuned* best, pierce_tuned* trials, int32_t max_trials,
+                         int32_t* num_trials) {
+    if (!ctx || !a || !b || !best) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "autotune: null argument");
+    pierce_join_opts o;
+    if (int s = validate_join(ctx, a, b, base, &o)) return s;
+    if (repeats < 1) repeats = 1;
+    int32_t n_trials = 0;
+    pierce_tuned cur;
+    std::memset(&cur, 0, sizeof(cur));
+    cur.leaf_size = o.leaf_size > 0 ? o.leaf_size : std::max(a->leaf_size, 1);
+    cur.rays_per_warp = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
+    cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 32;
+    cur.hash_load_factor = o.hash_load_factor;
+    cur.ms = 1e300;
+    // time one setting: one untimed run, then the best of `repeats`
+    auto trial = [&](pierce_tuned& t) -> int {
+        pierce_join_opts q = o;
+        q.leaf_size = t.leaf_size;
+        q.rays_per_warp = t.rays_per_warp;
+        q.stack_depth = t.stack_depth;
+        q.hash_load_factor = t.hash_load_factor;
+        t.ms = 1e300;
+        for (int r = 0; r <= repeats; ++r) {
+            pierce_result* res = nullptr;
+            pierce_stats st;
+            if (int s = pierce_join(ctx, a, b, &q, &res, &st)) return s;
+            pierce_result_destroy(res);
+            if (r > 0) t.ms = std::min(t.ms, st.ms_total);
+        }
+        if (trials && n_trials < max_trials) trials[n_trials] = t;
+        ++n_trials;
+        return PIERCE_OK;
+    };
+    const bool hashed = o.sizing != PIERCE_SIZING_TWO_PASS;
+    const std::vector<int> leaves = o.active_bvh ? std::vector<int>{1, 2, 4, 8} : std::vector<int>{cur.leaf_size};
+    const std::vector<int> rays = {32, 64, 128}, stacks = {8, 16, 32};
+    const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
+                                             : std::vector<double>{cur.hash_load_factor};
+    // coordinate descent: one parameter at a time, keeping the best so far
+    for (int param = 0; param < 4; ++param) {
+        const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()
+                                                                                              : loads.size();
+        pierce_tuned winner = cur;
+        for (size_t i = 0; i < n; ++i) {
+            pierce_tuned t = cur;
+            if (param == 0) t.leaf_size = leaves[i];
+            if (param == 1) t.rays_per_warp = rays[i];
+            if (param == 2) t.stack_depth = stacks[i];
+            if (param == 3) t.hash_load_factor = loads[i];
+            if (int s = trial(t)) return s;
+            if (t.ms < winner.ms) winner = t;
+        }
+        cur = winner;
+    }
+    *best = cur;
+    if (num_trials) *num_trials = n_trials;
+    return PIERCE_OK;
 }
 
 }  // extern "C"
@@ -1302,6 +1368,8 @@ struct pierce_join_graph {
 
 namespace {
 
+// The graph's scratch goes back to its context where the context's slot is
+// smaller (the context must outlive its graphs).
 void free_graph(pierce_join_graph* g) {
     if (!g) return;
     if (g->ctx) cudaSetDevice(g->ctx->device);
@@ -1310,8 +1378,16 @@ void free_graph(pierce_join_graph* g) {
     if (g->graph) cudaGraphDestroy(g->graph);
     for (void* p : g->plan.buffers)
         if (p) cudaFree(p);
-    for (int i = 0; i < kScratchSlots; ++i)
-        if (g->scratch[i]) cudaFree(g->scratch[i]);
+    for (int i = 0; i < kScratchSlots; ++i) {
+        if (!g->scratch[i]) continue;
+        if (g->ctx && g->ctx->scratch_bytes[i] < g->scratch_bytes[i]) {
+            if (g->ctx->scratch[i]) cudaFree(g->ctx->scratch[i]);
+            g->ctx->scratch[i] = g->scratch[i];
+            g->ctx->scratch_bytes[i] = g->scratch_bytes[i];
+        } else {
+            cudaFree(g->scratch[i]);
+        }
+    }
     if (g->plan.h_check) cudaFreeHost(g->plan.h_check);
     delete g;
 }
@@ -1354,6 +1430,13 @@ int pierce_join_graph_create(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset*
     if (int s = sync_ctx(ctx, "join graph")) return s;
     pierce_join_graph* g = new pierce_join_graph();
     g->ctx = ctx;
+    // the graph takes over the context's scratch buffers (no second copy)
+    for (int i = 0; i < kScratchSlots; ++i) {
+        g->scratch[i] = ctx->scratch[i];
+        g->scratch_bytes[i] = ctx->scratch_bytes[i];
+        ctx->scratch[i] = nullptr;
+        ctx->scratch_bytes[i] = 0;
+    }
     // 1. the planning run: an ordinary join that records its host decisions
     int s = with_graph_scratch(ctx, g, [&]() {
         g->plan.mode = 1;

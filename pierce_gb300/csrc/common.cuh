@@ -84,6 +84,8 @@ struct RayOpts {
     unsigned long long* amb_queue = nullptr;
     unsigned long long* amb_count = nullptr;
     uint64_t amb_cap = 0;
+    int rays_per_fetch = 32;  // rays a warp takes from the list per fetch
+    int short_stack = -1;     // shared-memory stack entries per thread (-1: default)
 };
 
 constexpr int kScratchSlots = 24;

@@ -119,6 +119,10 @@ struct EdgeRayParams {
     unsigned long long* amb_queue;
     unsigned long long* amb_count;
     uint64_t amb_cap;
+    // tuning: rays a warp takes per fetch from the ray list, and traversal
+    // stack entries kept in (dynamic) shared memory per thread
+    int rays_per_fetch;
+    int short_stack;
 };
 
 __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float hy, float lz, float hz,
@@ -157,8 +161,9 @@ __device__ __forceinline__ int traversal_start(const DevDataset& src, const DevD
 }
 
 template <int MODE, int PREC>
-__device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int (*sstack)[128], int* lstack,
+__device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int* sstack, int* lstack,
                                            RayCounters& rc, PredCounters& pc) {
+    const int depth = P.short_stack;
     const int tid = threadIdx.x;
     const float4 s4 = __ldg(P.src.edges + 2 * e);
     const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
@@ -243,8 +248,8 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
                     atomicOr(P.err, ERR_STACK_OVERFLOW);
                     break;
                 }
-                if (sp < kShortStack) sstack[sp][tid] = ch.y;
-                else lstack[sp - kShortStack] = ch.y;
+                if (sp < depth) sstack[sp * 128 + tid] = ch.y;
+                else lstack[sp - depth] = ch.y;
                 ++sp;
                 node = ch.x;
             } else if (h0) {
@@ -254,7 +259,7 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
             } else {
                 if (sp == 0) break;
                 --sp;
-                node = sp < kShortStack ? sstack[sp][tid] : lstack[sp - kShortStack];
+                node = sp < depth ? sstack[sp * 128 + tid] : lstack[sp - depth];
             }
         }
     }
@@ -264,25 +269,29 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
 
 template <int MODE, int PREC>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
-    __shared__ int sstack[kShortStack][128];
-    int lstack[kStackSize - kShortStack];
+    extern __shared__ int sstack[];  // short_stack x 128 entries
+    int lstack[kStackSize];
     RayCounters rc;
     PredCounters pc{0, 0};
     uint32_t rays = 0;
     if (P.ray_list) {
-        // Compacted ray list, persistent blocks: each warp fetches the next 32
-        // rays from a global cursor, so uneven ray costs balance out.
+        // Compacted ray list, persistent blocks: each warp takes the next
+        // rays_per_fetch rays from a global cursor (the work queue), so uneven
+        // ray costs balance out.
         const unsigned long long n = *P.ray_count;
         const int lane = threadIdx.x & 31;
+        const unsigned long long per = (unsigned long long)P.rays_per_fetch;
         for (;;) {
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(P.ray_cursor, 32ull);
+            if (lane == 0) base = atomicAdd(P.ray_cursor, per);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
-            const unsigned long long i = base + lane;
-            if (i < n) {
-                trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc);
-                ++rays;
+            for (unsigned long long r = lane; r < per; r += 32) {
+                const unsigned long long i = base + r;
+                if (i < n) {
+                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc);
+                    ++rays;
+                }
             }
         }
     } else {
@@ -656,8 +665,13 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.amb_queue = ro ? ro->amb_queue : nullptr;
     P.amb_count = ro ? ro->amb_count : nullptr;
     P.amb_cap = ro ? ro->amb_cap : 0;
+    P.rays_per_fetch = (ro && ro->rays_per_fetch > 0) ? ro->rays_per_fetch : 32;
+    P.short_stack = (ro && ro->short_stack >= 0) ? std::min(ro->short_stack, kShortStack) : kShortStack;
+    if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");
     if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
     const int B = 128;
+    const size_t smem = sizeof(int) * 128 * (size_t)P.short_stack;
     dim3 g;
     if (P.ray_list) {
         cudaMemsetAsync(P.ray_cursor, 0, sizeof(unsigned long long), ctx->stream);
@@ -669,7 +683,7 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
         g = dim3((unsigned)blocks);
     }
     cudaStream_t st = ctx->stream;
-#define PG_LAUNCH(M, PR) k_edge_rays<M, PR><<<g, B, 0, st>>>(P)
+#define PG_LAUNCH(M, PR) k_edge_rays<M, PR><<<g, B, smem, st>>>(P)
 #define PG_MODES(PR)                                  \
     do {                                              \
         if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PR); \

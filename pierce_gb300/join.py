@@ -186,7 +186,7 @@ class JoinResult:
 def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
               max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
-              sizing_model=None) -> capi.JoinOpts:
+              sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0) -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -203,6 +203,25 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.defer_exact = 1 if defer_exact else 0
     o.active_bvh = 1 if active_bvh else 0
     o.sizing_model = sizing_model.handle if sizing_model is not None else None
+    o.leaf_size, o.rays_per_warp, o.stack_depth = int(leaf_size), int(rays_per_warp), int(stack_depth)
+    return o
+
+
+def autotune(ctx: Context, a: Dataset, b: Dataset, opts: capi.JoinOpts, repeats: int = 2):
+    """The library's autotuner: returns (best setting, all trials) as dicts."""
+    best = capi.Tuned()
+    trials = (capi.Tuned * 64)()
+    n = C.c_int32()
+    check(capi.lib().pierce_autotune_join(ctx.handle, a.handle, b.handle, C.byref(opts), int(repeats),
+                                          C.byref(best), trials, 64, C.byref(n)), "autotune_join")
+    as_dict = lambda t: {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
+    return as_dict(best), [as_dict(trials[i]) for i in range(min(n.value, 64))]
+
+
+def tuned_opts(opts: capi.JoinOpts, best: dict) -> capi.JoinOpts:
+    o = capi.JoinOpts.from_buffer_copy(opts)
+    o.leaf_size, o.rays_per_warp = int(best["leaf_size"]), int(best["rays_per_warp"])
+    o.stack_depth, o.hash_load_factor = int(best["stack_depth"]), float(best["hash_load_factor"])
     return o
 
 

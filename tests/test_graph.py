@@ -66,3 +66,38 @@ def test_graph_of_a_batched_join(ctx):
     g = J.JoinGraph(ctx, A, B, J.make_opts(predicate="overlap"))
     g.launch()
     assert np.array_equal(g.pairs(), eager.pairs) and len(eager.pairs) > 20
+
+
+def test_batched_waves_equal_per_query_joins(ctx):
+    """The batched runner (waves of partitioned joins, each captured as a
+    graph) against one join call per query, plain and tuned."""
+    from pierce_gb300 import batched as BT, join as J
+    qs = BT.workload(seed=9, queries=40, n_lo=2, n_hi=60)
+    for q in qs:
+        q.extent *= 0.7  # denser than the workload: more pairs to compare
+    waves = BT.make_waves(qs, budget_tris=2e5)
+    assert len(waves) > 2 and sum(len(w.queries) for w in waves) == 40
+    opts = lambda w: J.make_opts(predicate="overlap", expected_pairs=BT.expected_pairs(w), leaf_size=4)
+    bat = BT.run_batched(ctx, waves, opts, warmup=0, replays=1, keep_pairs=True)
+    plain = BT.run_per_query(ctx, qs, J.make_opts(predicate="overlap", sizing="two_pass", precision="fp32",
+                                                  cull_objects=False, defer_exact=False, active_bvh=False),
+                             build_leaf=4, keep_pairs=True)
+    assert bat["pairs"] == plain["pairs"] > 20
+    for i in range(40):
+        have = bat["results"].get(i, np.zeros((0, 2), np.int32))
+        assert np.array_equal(have, plain["results"][i]), i
+
+
+def test_autotuner_returns_a_tried_setting_with_identical_pairs(ctx, datasets):
+    from pierce_gb300 import join as J
+    A, B = datasets
+    base = J.make_opts(predicate="overlap", expected_pairs=2000)
+    best, trials = J.autotune(ctx, A, B, base, repeats=1)
+    assert len(trials) == 4 + 3 + 3 + 3
+    assert best["ms"] == min(t["ms"] for t in trials)
+    assert best["leaf_size"] in (1, 2, 4, 8) and best["rays_per_warp"] in (32, 64, 128)
+    assert best["stack_depth"] in (8, 16, 32) and best["hash_load_factor"] in (0.25, 0.5, 0.75)
+    ref = J.run_join(ctx, A, B, base)
+    for t in trials[::3]:
+        r = J.run_join(ctx, A, B, J.tuned_opts(base, t))
+        assert np.array_equal(r.pairs, ref.pairs)
