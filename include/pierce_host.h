@@ -125,7 +125,10 @@ int pierce_gen_ellipsoid_pair(uint64_t seed_a, uint64_t seed_b,
 
 /* Branching tube meshes: random-walk skeleton (step, branch probability
  * per segment), radius U[r_lo, r_hi], n_sides-gon cross sections swept and
- * capped, about target_tris triangles per mesh, starts uniform in [lo,hi]^3. */
+ * capped, about target_tris triangles per mesh, starts uniform in [lo,hi]^3.
+ * The unique edges are listed per branch as they are built (ring, segment
+ * and diagonal edges, cap spokes), the same set unique-edge extraction finds;
+ * branches are swept in parallel (OpenMP). */
 int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris,
                      double step, double branch_prob, double r_lo, double r_hi,
                      int32_t n_sides, double lo, double hi, pierce_geom** out);

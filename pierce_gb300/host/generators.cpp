@@ -161,57 +161,96 @@ V3 random_unit(Rng& rng) {
     }
 }
 
-// Sweep an n-gon along a polyline and cap both ends with centre fans.
-void sweep_branch(pierce_geom& g, const std::vector<V3>& pts, double radius, int n, int32_t obj) {
+// Sweep an n-gon along a polyline and cap both ends with centre fans:
+// m*n ring vertices then the two cap centres; per segment and side two
+// triangles (a, b, d), (a, d, c); per side a triangle of each cap.  The
+// unique edges are listed structurally, each once: the ring edges of every
+// ring, the longitudinal and the diagonal edge of every segment side, and
+// the spokes of both caps (3 m n edges for m rings).
+struct Branch {
+    std::vector<V3> pts;
+    double radius;
+    int32_t obj;
+};
+
+inline int64_t branch_vertices(const Branch& b, int n) { return b.pts.size() < 2 ? 0 : (int64_t)b.pts.size() * n + 2; }
+inline int64_t branch_triangles(const Branch& b, int n) {
+    return b.pts.size() < 2 ? 0 : 2 * (int64_t)n * ((int64_t)b.pts.size() - 1) + 2 * (int64_t)n;
+}
+inline int64_t branch_edges(const Branch& b, int n) { return b.pts.size() < 2 ? 0 : 3 * (int64_t)b.pts.size() * n; }
+
+void sweep_branch(const Branch& br, int n, uint32_t base, float* vout, uint32_t* iout, int32_t* tout, float* es,
+                  float* ee, int32_t* esrc) {
+    const std::vector<V3>& pts = br.pts;
     if (pts.size() < 2) return;
-    const uint32_t base = (uint32_t)g.num_vertices();
+    const double radius = br.radius;
     // Frames by parallel transport of an initial perpendicular.
     V3 t0 = normalize(sub(pts[1], pts[0]));
     V3 helper = std::fabs(t0.z) < 0.9 ? V3{0, 0, 1} : V3{1, 0, 0};
     V3 u = normalize(cross(t0, helper));
     const size_t m = pts.size();
+    float* v = vout;
     for (size_t i = 0; i < m; ++i) {
         V3 ti = (i + 1 < m) ? sub(pts[i + 1], pts[i]) : sub(pts[i], pts[i - 1]);
         if (i > 0 && i + 1 < m) ti = add(normalize(sub(pts[i + 1], pts[i])), normalize(sub(pts[i], pts[i - 1])));
         ti = normalize(ti);
         u = normalize(sub(u, mul(ti, dot(u, ti))));
-        V3 v = cross(ti, u);
+        V3 w = cross(ti, u);
         for (int k = 0; k < n; ++k) {
             double ang = pierce::detm::kTwoPi * (double)k / (double)n;
-            V3 q = add(pts[i], add(mul(u, radius * pierce::detm::cos(ang)), mul(v, radius * pierce::detm::sin(ang))));
-            g.vertices.push_back((float)q.x);
-            g.vertices.push_back((float)q.y);
-            g.vertices.push_back((float)q.z);
+            V3 q = add(pts[i], add(mul(u, radius * pierce::detm::cos(ang)), mul(w, radius * pierce::detm::sin(ang))));
+            *v++ = (float)q.x;
+            *v++ = (float)q.y;
+            *v++ = (float)q.z;
         }
     }
-    const uint32_t c0 = (uint32_t)g.num_vertices();
-    g.vertices.push_back((float)pts[0].x);
-    g.vertices.push_back((float)pts[0].y);
-    g.vertices.push_back((float)pts[0].z);
-    const uint32_t c1 = c0 + 1;
-    g.vertices.push_back((float)pts[m - 1].x);
-    g.vertices.push_back((float)pts[m - 1].y);
-    g.vertices.push_back((float)pts[m - 1].z);
-    uint64_t added = 0;
+    *v++ = (float)pts[0].x;
+    *v++ = (float)pts[0].y;
+    *v++ = (float)pts[0].z;
+    *v++ = (float)pts[m - 1].x;
+    *v++ = (float)pts[m - 1].y;
+    *v++ = (float)pts[m - 1].z;
+    const uint32_t c0 = base + (uint32_t)(m * n), c1 = c0 + 1;
+    uint32_t* ix = iout;
     for (size_t i = 0; i + 1 < m; ++i) {
         for (int k = 0; k < n; ++k) {
             uint32_t a = base + (uint32_t)(i * n + k), b = base + (uint32_t)(i * n + (k + 1) % n);
             uint32_t c = a + (uint32_t)n, d = b + (uint32_t)n;
             const uint32_t q[6] = {a, b, d, a, d, c};
-            g.indices.insert(g.indices.end(), q, q + 6);
-            added += 2;
+            ix = std::copy(q, q + 6, ix);
         }
     }
     for (int k = 0; k < n; ++k) {
         uint32_t a = base + (uint32_t)k, b = base + (uint32_t)((k + 1) % n);
         const uint32_t f0[3] = {c0, b, a};
-        g.indices.insert(g.indices.end(), f0, f0 + 3);
+        ix = std::copy(f0, f0 + 3, ix);
         uint32_t la = base + (uint32_t)((m - 1) * n + k), lb = base + (uint32_t)((m - 1) * n + (k + 1) % n);
         const uint32_t f1[3] = {c1, la, lb};
-        g.indices.insert(g.indices.end(), f1, f1 + 3);
-        added += 2;
+        ix = std::copy(f1, f1 + 3, ix);
     }
-    g.tri_to_object.insert(g.tri_to_object.end(), added, obj);
+    std::fill(tout, tout + branch_triangles(br, n), br.obj);
+    // structural unique edges (vertex indices local to the branch)
+    auto vert = [&](uint32_t local) { return vout + 3 * (size_t)local; };
+    size_t e = 0;
+    auto emit = [&](uint32_t la, uint32_t lb) {
+        std::copy(vert(la), vert(la) + 3, es + 3 * e);
+        std::copy(vert(lb), vert(lb) + 3, ee + 3 * e);
+        esrc[e] = br.obj;
+        ++e;
+    };
+    for (size_t i = 0; i < m; ++i)
+        for (int k = 0; k < n; ++k) {
+            const uint32_t a = (uint32_t)(i * n + k), b = (uint32_t)(i * n + (k + 1) % n);
+            emit(a, b);  // ring edge
+            if (i + 1 < m) {
+                emit(a, a + (uint32_t)n);  // longitudinal
+                emit(a, b + (uint32_t)n);  // diagonal
+            }
+        }
+    for (int k = 0; k < n; ++k) {
+        emit((uint32_t)(m * n), (uint32_t)k);                            // first cap spoke
+        emit((uint32_t)(m * n + 1), (uint32_t)((m - 1) * n + k));        // last cap spoke
+    }
 }
 
 }  // namespace
@@ -354,7 +393,8 @@ extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t targe
         pierce::set_last_error("gen_tubes: invalid argument");
         return PIERCE_HOST_ERR_INVALID;
     }
-    std::unique_ptr<pierce_geom> g(new pierce_geom());
+    // 1. skeletons, one random stream in mesh order
+    std::vector<Branch> branches;
     Rng rng(seed);
     const int64_t tris_per_segment = 2 * (int64_t)n_sides;
     for (int32_t m = 0; m < num_meshes; ++m) {
@@ -368,23 +408,47 @@ extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t targe
         while (!pending.empty() && budget > 2 * n_sides + tris_per_segment) {
             Start s = pending.back();
             pending.pop_back();
-            std::vector<V3> pts{s.p};
+            Branch br{{s.p}, radius, m};
             V3 p = s.p, d = s.d;
             budget -= 2 * n_sides;  // caps
             while (budget >= tris_per_segment) {
                 d = normalize(add(d, mul(random_unit(rng), 0.35)));
                 p = add(p, mul(d, step));
-                pts.push_back(p);
+                br.pts.push_back(p);
                 budget -= tris_per_segment;
                 if (rng.uniform() < branch_prob) pending.push_back({p, normalize(add(d, random_unit(rng)))});
                 // Branches end with probability 1/400 per segment once a
                 // branch is queued, so the budget spreads over several arms.
                 if (!pending.empty() && rng.uniform() < 1.0 / 400.0) break;
             }
-            sweep_branch(*g, pts, radius, n_sides, m);
+            if (br.pts.size() >= 2) branches.push_back(std::move(br));
         }
     }
-    finish(*g);
+    // 2. offsets, then every branch swept in parallel into its own ranges
+    const size_t nb = branches.size();
+    std::vector<int64_t> vo(nb + 1, 0), to(nb + 1, 0), eo(nb + 1, 0);
+    for (size_t i = 0; i < nb; ++i) {
+        vo[i + 1] = vo[i] + branch_vertices(branches[i], n_sides);
+        to[i + 1] = to[i] + branch_triangles(branches[i], n_sides);
+        eo[i + 1] = eo[i] + branch_edges(branches[i], n_sides);
+    }
+    if (vo[nb] >= (int64_t)1 << 32) {
+        pierce::set_last_error("gen_tubes: more than 2^32 vertices");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    std::unique_ptr<pierce_geom> g(new pierce_geom());
+    g->vertices.resize(3 * (size_t)vo[nb]);
+    g->indices.resize(3 * (size_t)to[nb]);
+    g->tri_to_object.resize((size_t)to[nb]);
+    g->edge_starts.resize(3 * (size_t)eo[nb]);
+    g->edge_ends.resize(3 * (size_t)eo[nb]);
+    g->edge_src.resize((size_t)eo[nb]);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t i = 0; i < (int64_t)nb; ++i)
+        sweep_branch(branches[i], n_sides, (uint32_t)vo[i], &g->vertices[3 * vo[i]], &g->indices[3 * to[i]],
+                     &g->tri_to_object[to[i]], &g->edge_starts[3 * eo[i]], &g->edge_ends[3 * eo[i]],
+                     &g->edge_src[eo[i]]);
+    g->total_triangles = g->num_triangles();
     *out = g.release();
     return PIERCE_HOST_OK;
 }
