@@ -91,3 +91,12 @@ def test_instanced_join_matches_oracle(ctx):
     got = J.pairs_to_keys(J.intersection_join(ctx, A, B).pairs)
     assert np.array_equal(np.sort(got), np.sort(want))
     assert len(want) > 20
+
+
+def test_tube_structural_edges_equal_extracted_edges():
+    g = pg.tubes(5, 6, 30000, hi=40.0)
+    es, ee, src = g.edge_starts.copy(), g.edge_ends.copy(), g.edge_src.copy()
+    h = pg.Geometry.from_arrays(g.vertices, g.indices, g.tri_to_object)
+    h.extract_edges(order=1)
+    assert h.num_edges == len(src)
+    assert edge_set(es, ee, src) == edge_set(h.edge_starts, h.edge_ends, h.edge_src)
