@@ -216,6 +216,9 @@ void pierce_default_tuning(pierce_tuning* t);
 void pierce_default_join_opts(pierce_join_opts* o);
 /* Kernels launched by this context since its creation. */
 uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx);
+/* Free the context's join scratch memory (kept and reused across joins
+ * otherwise; the next join allocates it again). */
+int pierce_ctx_release_scratch(pierce_ctx* ctx);
 /* Free and total memory of the context's device (cudaMemGetInfo). */
 int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 

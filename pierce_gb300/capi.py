@@ -127,6 +127,7 @@ SIGNATURES = {
     "pierce_default_join_opts": (None, [C.POINTER(JoinOpts)]),
     "pierce_ctx_kernel_launches": (U64, [V]),
     "pierce_device_memory": (C.c_int, [V, C.POINTER(U64), C.POINTER(U64)]),
+    "pierce_ctx_release_scratch": (C.c_int, [V]),
     "pierce_dataset_create": (C.c_int, [V, C.POINTER(MeshView), C.c_int, C.POINTER(Tuning), C.POINTER(V)]),
     "pierce_dataset_build": (C.c_int, [V, V, C.POINTER(Tuning)]),
     "pierce_dataset_create_instanced": (C.c_int, [V, V, I32, C.POINTER(Tuning), C.POINTER(V)]),

@@ -377,6 +377,18 @@ void* pierce_ctx_stream(pierce_ctx* ctx) { return ctx ? (void*)ctx->stream : nul
 
 uint64_t pierce_ctx_kernel_launches(const pierce_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int pierce_ctx_release_scratch(pierce_ctx* ctx) {
+    if (!ctx) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "ctx_release_scratch: null argument");
+    cudaSetDevice(ctx->device);
+    if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "release scratch")) return s;
+    for (int i = 0; i < kScratchSlots; ++i) {
+        if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+        ctx->scratch[i] = nullptr;
+        ctx->scratch_bytes[i] = 0;
+    }
+    return PIERCE_OK;
+}
+
 int pierce_device_memory(pierce_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes) {
     if (!ctx || !free_bytes || !total_bytes) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "device_memory: null");
     cudaSetDevice(ctx->device);

@@ -59,6 +59,10 @@ class Context:
     def synchronize(self) -> None:
         check(self._lib.pierce_ctx_synchronize(self._h), "synchronize")
 
+    def release_scratch(self) -> None:
+        """Free the join scratch memory the context keeps between joins."""
+        check(self._lib.pierce_ctx_release_scratch(self._h), "release_scratch")
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             for child in list(getattr(self, "_children", ())):
