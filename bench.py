@@ -343,7 +343,7 @@ def main_tubes(args):
     Bs.set_edges(B.edge_starts[ebm], B.edge_ends[ebm], remap[B.edge_src[ebm]].astype(np.int32))
     from oracle import pyoracle as O
     tc = time.perf_counter()
-    cpu_keys = O.overlap_keys(As, Bs)
+    cpu_keys, _ = O.overlap_keys(As, Bs)
     cpu_s = time.perf_counter() - tc
     log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s, {len(cpu_keys)} pairs")
 
