@@ -470,8 +470,9 @@ def main_tubes(args):
                   "e2e_speedup_tuned": res["plain"]["e2e_s"] / res["tuned"]["e2e_s"],
                   "device_speedup_tuned": plain_ms / tuned_ms},
         "pairs": len(keys_t), "identical_tuned_plain": identical, "sample_matches_oracle": sample_match,
-        "tuned_stats": {k2: st[k2] for k2 in ("ms_total", "ms_build", "rays", "tri_tests", "fp32_ambiguous",
-                                                "fp64_ambiguous", "predicted_pairs", "sizing_overflow",
+        "tuned_stats": {k2: st[k2] for k2 in ("ms_total", "ms_build", "ms_edge_rays", "ms_dedup", "ms_sizing",
+                                                "rays", "tri_tests", "fp32_ambiguous", "fp64_ambiguous",
+                                                "predicted_pairs", "sizing_overflow", "hash_slots",
                                                 "active_triangles")},
         "cpu_baseline": {"value": 1.0 / (cpu_s * n_tubes / k), "unit": UNIT, "cores": O.max_threads(),
                          "kind": "port",

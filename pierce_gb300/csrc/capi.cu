@@ -27,6 +27,10 @@ int launch_collect_rays(pierce_ctx* ctx, const DevDataset& src, const uint8_t* a
                         unsigned long long* count);
 int launch_collect_tris(pierce_ctx* ctx, const int32_t* t2o, int64_t nt, const uint8_t* active, uint32_t* list,
                         unsigned long long* count);
+int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uint32_t* idx, const int32_t* t2o,
+                      const DevDataset& src, const uint8_t* obj_active, const DevDataset& objs,
+                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box);
+int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots);
@@ -73,6 +77,8 @@ enum : int {
     SLOT_OBJ_B = 18,
     SLOT_TRIS_A = 19,    // active triangle lists
     SLOT_TRIS_B = 20,
+    // 21, 22: learned sizing
+    SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
 };
 }  // namespace
 
@@ -628,6 +634,9 @@ void pierce_result_destroy(pierce_result* r) {
 
 namespace {
 
+// Round a scratch cursor up to a 256-byte boundary.
+static inline void soup_align(char*& q) { q += (256 - ((uintptr_t)q & 255)) & 255; }
+
 struct Join {
     pierce_ctx* ctx;
     pierce_dataset* A;
@@ -651,7 +660,7 @@ struct Join {
     uint8_t* active = nullptr;
     // words: [0] list count A->B, [1] list count B->A, [2] warp cursor,
     //        [3] deferred-test count, [4] exactly resolved key count,
-    //        [5] active triangles of A, [6] active triangles of B
+    //        [5] active triangles of A, [6] active triangles of B, [7] active chunks of A
     unsigned long long* words = nullptr;
     // device views of A and B the kernels traverse (their own BVH, or the
     // per-join BVH over active triangles)
@@ -659,6 +668,7 @@ struct Join {
     unsigned long long* amb_queue = nullptr;
     uint64_t amb_cap = 0;
     bool defer = true;
+    uint8_t* chunk_flags = nullptr;
 
     int prepare() {
         defer = o.defer_exact != 0;
@@ -666,9 +676,12 @@ struct Join {
         vb = B->view();
         void* p = nullptr;
         const size_t nobj_a = (size_t)std::max(A->num_objects, 1), nobj_b = (size_t)std::max(B->num_objects, 1);
-        if (int s = scratch(ctx, SLOT_CULL, 128 + nobj_a + nobj_b, &p)) return s;
+        // words, object flags, then chunk flags (triangles A, B, edges A, B)
+        const size_t chunks = (A->nt + 31) / 32 + (B->nt + 31) / 32 + (A->ne + 31) / 32 + (B->ne + 31) / 32 + 4;
+        if (int s = scratch(ctx, SLOT_CULL, 128 + nobj_a + nobj_b + chunks, &p)) return s;
         words = static_cast<unsigned long long*>(p);
         active = static_cast<uint8_t*>(p) + 128;
+        chunk_flags = active + nobj_a + nobj_b;
         if (o.cull_objects || o.active_bvh) {
             if (int s = scratch(ctx, SLOT_LIST_AB, 4 * std::max<uint64_t>(A->ne, 1), &p)) return s;
             list[0] = static_cast<uint32_t*>(p);
@@ -728,12 +741,85 @@ struct Join {
         void *ta = nullptr, *tb = nullptr;
         if (int s = scratch(ctx, SLOT_TRIS_A, 4 * std::max<uint64_t>(A->nt, 1), &ta)) return s;
         if (int s = scratch(ctx, SLOT_TRIS_B, 4 * std::max<uint64_t>(B->nt, 1), &tb)) return s;
-        if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
-            return s;
-        if (int s = launch_collect_tris(ctx, B->d_tri_to_object, (int64_t)B->nt, act_b, (uint32_t*)tb, words + 6))
-            return s;
-        if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
-        if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
+        // Chunk culling keeps the triangles and edges whose chunk box meets an
+        // object box of the other side.  Parity (intersection, containment)
+        // needs every triangle of a target object above the query point, so
+        // those predicates keep whole objects' triangles and cull edges only.
+        uint8_t* tchunk_a = chunk_flags;
+        uint8_t* tchunk_b = tchunk_a + (A->nt + 31) / 32 + 1;
+        uint8_t* echunk_a = tchunk_b + (B->nt + 31) / 32 + 1;
+        uint8_t* echunk_b = echunk_a + (A->ne + 31) / 32 + 1;
+        const bool chunked = o.cull_objects != 0;
+        // Second round (overlap, unpartitioned): B's chunks are tested against
+        // a hierarchy of A's surviving chunk boxes instead of A's object boxes,
+        // which matters when A's objects are large (long tubes).
+        DevDataset cull_b = objA;
+        const bool two_rounds = chunked && o.predicate == PIERCE_OVERLAP && A->num_parts == 0 && A->nt > 0;
+        if (chunked && o.predicate == PIERCE_OVERLAP) {
+            float* boxes_a = nullptr;
+            uint32_t* clist = nullptr;
+            uint32_t* cidx = nullptr;
+            int32_t* ct2o = nullptr;
+            float4* csoup = nullptr;
+            Node* cnodes = nullptr;
+            const int64_t nca = (int64_t)((A->nt + 31) / 32);
+            if (two_rounds) {
+                void* pc = nullptr;
+                // boxes 24, list 4, pseudo indices 12 + ids 4, soup 48, nodes 64 bytes per chunk
+                const size_t per = 24 + 4 + 16 + 48 + 64;
+                if (int s = scratch(ctx, SLOT_CHUNKS, per * (size_t)nca + 1024, &pc)) return s;
+                char* q = static_cast<char*>(pc);
+                soup_align(q);
+                csoup = reinterpret_cast<float4*>(q);
+                q += 48 * nca;
+                cnodes = reinterpret_cast<Node*>(q);
+                q += 64 * nca;
+                boxes_a = reinterpret_cast<float*>(q);
+                q += 24 * nca;
+                cidx = reinterpret_cast<uint32_t*>(q);
+                q += 12 * nca;
+                ct2o = reinterpret_cast<int32_t*>(q);
+                q += 4 * nca;
+                clist = reinterpret_cast<uint32_t*>(q);
+            }
+            if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
+                                          tchunk_a, (uint32_t*)ta, words + 5, boxes_a))
+                return s;
+            if (two_rounds) {
+                if (int s = launch_flag_list(ctx, tchunk_a, nca, clist, words + 7)) return s;
+                int64_t n_act = 0;
+                if (int s = host_value(ctx, words + 7, 8, &n_act, "active chunks")) return s;
+                if (int s = launch_object_pseudo_tris(ctx, (int32_t)nca, cidx, ct2o)) return s;
+                BvhShape shc;
+                if (int s = build_lbvh(ctx, boxes_a, cidx, ct2o, clist, n_act, 4, csoup, cnodes, &shc, nullptr))
+                    return s;
+                cull_b = DevDataset{};
+                cull_b.soup = csoup;
+                cull_b.nodes = cnodes;
+                cull_b.num_tris = n_act;
+                cull_b.root_is_leaf = shc.root_is_leaf;
+                cull_b.root_leaf_count = shc.root_leaf_count;
+            }
+            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
+                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr))
+                return s;
+        } else {
+            if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
+                return s;
+            if (int s = launch_collect_tris(ctx, B->d_tri_to_object, (int64_t)B->nt, act_b, (uint32_t*)tb, words + 6))
+                return s;
+        }
+        if (chunked) {
+            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a, list[0],
+                                          words + 0, nullptr))
+                return s;
+            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, two_rounds ? cull_b : objA,
+                                          echunk_b, list[1], words + 1, nullptr))
+                return s;
+        } else {
+            if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
+            if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
+        }
         listed[0] = listed[1] = true;
         int64_t na = 0, nb = 0;
         if (int s = host_value(ctx, words + 5, 8, &na, "active triangles of A")) return s;

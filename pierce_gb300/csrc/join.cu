@@ -743,6 +743,201 @@ int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, u
     return launch_collect_rays(ctx, src, active, list, count);
 }
 
+// ---- chunk culling -------------------------------------------------------------
+// Consecutive triangles (and consecutive edges) of a mesh lie close together,
+// so chunks of kChunk of them get one box: a chunk whose box meets no object
+// box of the other side cannot take part in an overlap pair (a triangle or
+// edge lies in its chunk's box, and every triangle of the other side lies in
+// its object's box).  A warp forms the boxes of 32 chunks, one per lane, and
+// every lane then queries the other side's object hierarchy with its box.
+constexpr int kChunk = 32;
+
+// Does [lo, hi] meet an object box of `objs` (the hierarchy of degenerate
+// triangles (lo, hi, hi), one per object), within partition `part`?
+__device__ bool meets_any_object(const DevDataset& objs, int32_t part, const float3& lo, const float3& hi) {
+    auto leaf_hit = [&](int first, int count) {
+        for (int k = 0; k < count; ++k) {
+            const float4 a4 = __ldg(objs.soup + 3 * (int64_t)(first + k));
+            const float4 b4 = __ldg(objs.soup + 3 * (int64_t)(first + k) + 1);
+            if (box_overlap(a4.x, b4.x, a4.y, b4.y, a4.z, b4.z, lo, hi)) return true;
+        }
+        return false;
+    };
+    int node;
+    if (objs.part_roots) {
+        const int2 r = __ldg(objs.part_roots + part);
+        if (r.x < 0) return leaf_hit(~r.x, r.y);
+        node = r.x;
+    } else if (objs.root_is_leaf) {
+        return leaf_hit(0, objs.root_leaf_count);
+    } else {
+        node = 0;
+    }
+    int stack[kStackSize];
+    int sp = 0;
+    for (;;) {
+        const Node* nd = objs.nodes + node;
+        const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+        const int4 ch = __ldg(&nd->ch);
+        bool h0 = box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
+        bool h1 = box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
+        if (h0 && ch.x < 0) {
+            if (leaf_hit(~ch.x, ch.z & 0xFF)) return true;
+            h0 = false;
+        }
+        if (h1 && ch.y < 0) {
+            if (leaf_hit(~ch.y, (ch.z >> 8) & 0xFF)) return true;
+            h1 = false;
+        }
+        if (h0 && h1) {
+            if (sp >= kStackSize) return true;  // cannot happen for an LBVH; stay conservative
+            stack[sp++] = ch.y;
+            node = ch.x;
+        } else if (h0) {
+            node = ch.x;
+        } else if (h1) {
+            node = ch.y;
+        } else {
+            if (sp == 0) return false;
+            node = stack[--sp];
+        }
+    }
+}
+
+// Per chunk of triangles (EDGES = false) or edges (EDGES = true) of `src`:
+// 1 when its box, over the items of active objects, meets an object box of
+// the other side.  A chunk whose items span partitions stays active.
+template <bool EDGES>
+__global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ verts,
+                                                      const uint32_t* __restrict__ idx,
+                                                      const int32_t* __restrict__ t2o, const float4* __restrict__ edges,
+                                                      const int32_t* __restrict__ edge_src, int64_t n,
+                                                      const uint8_t* __restrict__ obj_active,
+                                                      const int32_t* __restrict__ obj_part, DevDataset objs,
+                                                      uint8_t* __restrict__ chunk_active,
+                                                      float* __restrict__ chunk_box) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n_chunks = (n + kChunk - 1) / kChunk;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; c0 < n_chunks;
+         c0 += warps * 32) {
+        float3 mylo = make_float3(0, 0, 0), myhi = make_float3(0, 0, 0);
+        bool myany = false, mymixed = false;
+        int32_t mypart = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int64_t c = c0 + j;
+            if (c >= n_chunks) break;
+            const int64_t i = c * kChunk + lane;
+            bool valid = i < n;
+            int32_t obj = -1;
+            float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+            if (valid) {
+                obj = EDGES ? __ldg(edge_src + i) : __ldg(t2o + i);
+                valid = obj >= 0 && __ldg(obj_active + obj) != 0;
+            }
+            if (valid) {
+                if (EDGES) {
+                    const float4 a = __ldg(edges + 2 * i), b = __ldg(edges + 2 * i + 1);
+                    lo = make_float3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z));
+                    hi = make_float3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z));
+                } else {
+                    for (int v = 0; v < 3; ++v) {
+                        const uint32_t vi = __ldg(idx + 3 * i + v);
+                        const float x = __ldg(verts + 3 * (size_t)vi), y = __ldg(verts + 3 * (size_t)vi + 1),
+                                    z = __ldg(verts + 3 * (size_t)vi + 2);
+                        lo = make_float3(fminf(lo.x, x), fminf(lo.y, y), fminf(lo.z, z));
+                        hi = make_float3(fmaxf(hi.x, x), fmaxf(hi.y, y), fmaxf(hi.z, z));
+                    }
+                }
+            }
+            const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+            int32_t part = (valid && obj_part) ? __ldg(obj_part + obj) : 0;
+            const int leader = vmask ? __ffs(vmask) - 1 : 0;
+            const int32_t p0 = __shfl_sync(0xFFFFFFFFu, part, leader);
+            const bool mixed = __any_sync(0xFFFFFFFFu, valid && part != p0);
+            for (int off = 16; off > 0; off >>= 1) {
+                lo.x = fminf(lo.x, __shfl_xor_sync(0xFFFFFFFFu, lo.x, off));
+                lo.y = fminf(lo.y, __shfl_xor_sync(0xFFFFFFFFu, lo.y, off));
+                lo.z = fminf(lo.z, __shfl_xor_sync(0xFFFFFFFFu, lo.z, off));
+                hi.x = fmaxf(hi.x, __shfl_xor_sync(0xFFFFFFFFu, hi.x, off));
+                hi.y = fmaxf(hi.y, __shfl_xor_sync(0xFFFFFFFFu, hi.y, off));
+                hi.z = fmaxf(hi.z, __shfl_xor_sync(0xFFFFFFFFu, hi.z, off));
+            }
+            if (lane == j) {
+                mylo = lo;
+                myhi = hi;
+                myany = vmask != 0;
+                mymixed = mixed;
+                mypart = p0;
+            }
+        }
+        const int64_t c = c0 + lane;
+        if (c < n_chunks) {
+            bool act = false;
+            if (myany) act = mymixed || meets_any_object(objs, mypart, mylo, myhi);
+            chunk_active[c] = act ? 1 : 0;
+            if (chunk_box) {  // (lo, hi) as two points: the pseudo-triangle (lo, hi, hi) of the chunk
+                float* b = chunk_box + 6 * c;
+                b[0] = mylo.x;
+                b[1] = mylo.y;
+                b[2] = mylo.z;
+                b[3] = myhi.x;
+                b[4] = myhi.y;
+                b[5] = myhi.z;
+            }
+        }
+    }
+}
+
+// Items of active objects in active chunks -> compacted list.
+__global__ void __launch_bounds__(256) k_collect_chunked(const int32_t* __restrict__ item_obj, int64_t n,
+                                                         const uint8_t* __restrict__ active,
+                                                         const uint8_t* __restrict__ chunk_active,
+                                                         uint32_t* __restrict__ list, unsigned long long* count) {
+    compact_tiles<8>(n, [&](int64_t i) {
+        const int32_t o = item_obj[i];
+        return o >= 0 && active[o] != 0 && chunk_active[i / kChunk] != 0;
+    }, list, count);
+}
+
+// Indices i < n with flags[i] != 0 -> compacted list.
+__global__ void __launch_bounds__(256) k_flag_list(const uint8_t* __restrict__ flags, int64_t n,
+                                                   uint32_t* __restrict__ list, unsigned long long* count) {
+    compact_tiles<8>(n, [&](int64_t i) { return flags[i] != 0; }, list, count);
+}
+
+int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    if (n <= 0) return PIERCE_OK;
+    k_flag_list<<<grid_cap(ctx, (n + 7) / 8, 256), 256, 0, ctx->stream>>>(flags, n, list, count);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "flag list");
+}
+
+int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uint32_t* idx, const int32_t* t2o,
+                      const DevDataset& src, const uint8_t* obj_active, const DevDataset& objs,
+                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    const int64_t n = edges ? src.num_edges : src.num_tris;
+    if (n <= 0) return PIERCE_OK;
+    const int64_t n_chunks = (n + kChunk - 1) / kChunk;
+    const int64_t warps = (n_chunks + 31) / 32;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
+                                                                             (int64_t)ctx->sm_count * 32));
+    if (edges)
+        k_chunk_active<true><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n, obj_active,
+                                                              src.obj_part, objs, chunk_active, chunk_box);
+    else
+        k_chunk_active<false><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n,
+                                                               obj_active, src.obj_part, objs, chunk_active,
+                                                               chunk_box);
+    k_collect_chunked<<<grid_cap(ctx, (n + 7) / 8, 256), 256, 0, ctx->stream>>>(edges ? src.edge_src : t2o, n,
+                                                                                obj_active, chunk_active, list,
+                                                                                count);
+    ctx->launches += 2;
+    return check_cuda(cudaGetLastError(), "chunk culling");
+}
+
 // Triangles of active objects -> compacted list.
 __global__ void __launch_bounds__(256) k_collect_tris(const int32_t* __restrict__ t2o, int64_t nt,
                                                       const uint8_t* __restrict__ active, uint32_t* __restrict__ list,

@@ -509,7 +509,8 @@ int join_features(pierce_ctx* ctx, const pierce_dataset* A, const pierce_dataset
     return check_cuda(cudaGetLastError(), "join features");
 }
 
-// Predicted log1p(pairs) of the join into *pred (synchronous).
+// Predicted log1p(pairs) of the join into *pred (synchronous), capped by the
+// sampled box-overlap estimate.
 int learned_log_pairs(pierce_ctx* ctx, const pierce_mlp* mlp, const pierce_dataset* A, const pierce_dataset* B,
                       double* pred) {
     void* p = nullptr;
@@ -518,12 +519,20 @@ int learned_log_pairs(pierce_ctx* ctx, const pierce_mlp* mlp, const pierce_datas
     if (int s = join_features(ctx, A, B, f)) return s;
     k_mlp_predict<<<1, NH, 0, ctx->stream>>>(mlp->d_model, f, 1, f + NI);
     ctx->launches += 1;
-    int64_t bits = 0;
+    int64_t bits = 0, sample_bits = 0;
     if (int s = host_value(ctx, f + NI, 4, &bits, "learned sizing")) return s;
-    const int32_t b32 = (int32_t)bits;
-    float v;
+    if (int s = host_value(ctx, f + 30, 4, &sample_bits, "learned sizing bound")) return s;
+    const int32_t b32 = (int32_t)bits, s32 = (int32_t)sample_bits;
+    float v, sv;
     std::memcpy(&v, &b32, sizeof(float));
-    *pred = (double)v;
+    std::memcpy(&sv, &s32, sizeof(float));
+    // Outside its training distribution the network can predict far more
+    // pairs than can exist: cap it by 4x the sampled box-overlap estimate
+    // (every pair is a box overlap) plus a floor, and by nA nB.  A cap below
+    // the true count only costs the two-pass rerun.
+    const double boxes = std::expm1((double)sv);
+    const double cap = std::min(4.0 * boxes + 4096.0, (double)A->num_objects * (double)B->num_objects + 1.0);
+    *pred = std::min((double)v, std::log1p(cap));
     return PIERCE_OK;
 }
 

@@ -163,7 +163,7 @@ V3 random_unit(Rng& rng) {
 
 // Sweep an n-gon along a polyline and cap both ends with centre fans:
 // m*n ring vertices then the two cap centres; per segment and side two
-// triangles (a, b, d), (a, d, c); per side a triangle of each cap.  The
+// triangles (a, b, d), (a, d, c); then the first cap's fan, then the last's.  The
 // unique edges are listed structurally, each once: the ring edges of every
 // ring, the longitudinal and the diagonal edge of every segment side, and
 // the spokes of both caps (3 m n edges for m rings).
@@ -220,10 +220,13 @@ void sweep_branch(const Branch& br, int n, uint32_t base, float* vout, uint32_t*
             ix = std::copy(q, q + 6, ix);
         }
     }
+    // each cap's fan in one run, so consecutive triangles stay close together
     for (int k = 0; k < n; ++k) {
         uint32_t a = base + (uint32_t)k, b = base + (uint32_t)((k + 1) % n);
         const uint32_t f0[3] = {c0, b, a};
         ix = std::copy(f0, f0 + 3, ix);
+    }
+    for (int k = 0; k < n; ++k) {
         uint32_t la = base + (uint32_t)((m - 1) * n + k), lb = base + (uint32_t)((m - 1) * n + (k + 1) % n);
         const uint32_t f1[3] = {c1, la, lb};
         ix = std::copy(f1, f1 + 3, ix);
