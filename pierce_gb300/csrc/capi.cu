@@ -34,6 +34,8 @@ int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t*
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots);
+int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
+                          int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
                   unsigned long long* d_count);
 int keys_to_pairs(pierce_ctx* ctx, uint64_t* keys, int64_t n);
@@ -264,7 +266,8 @@ int dataset_alloc(pierce_dataset* ds) {
     if (int s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources")) return s;
     if (int s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices")) return s;
     if (int s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes")) return s;
-    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 40 * (size_t)nobj;
+    if (int s = device_alloc((void**)&ds->d_obj_range, 8 * (size_t)std::max(nobj, 1), "object ranges")) return s;
+    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * (size_t)nobj;
     return PIERCE_OK;
 }
 
@@ -415,7 +418,7 @@ void pierce_dataset_destroy(pierce_dataset* ds) {
     cudaDeviceSynchronize();
     void* ptrs[] = {ds->d_vertices, ds->d_indices,  ds->d_tri_to_object, ds->d_edges,  ds->d_edge_src,
                     ds->d_soup,     ds->d_nodes,    ds->d_first_vertex,  ds->d_obj_box, ds->d_obj_part,
-                    ds->d_part_roots};
+                    ds->d_part_roots, ds->d_obj_range};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete ds;
@@ -669,6 +672,10 @@ struct Join {
     uint64_t amb_cap = 0;
     bool defer = true;
     uint8_t* chunk_flags = nullptr;
+    // object hierarchies of the per-join path, and whether parity runs on
+    // object pairs (both datasets store each object's triangles contiguously)
+    DevDataset objA_{}, objB_{};
+    bool object_parity = false;
 
     int prepare() {
         defer = o.defer_exact != 0;
@@ -734,6 +741,9 @@ struct Join {
         DevDataset objA, objB;
         if (int s = object_bvh(A, SLOT_OBJ_A, &objA)) return s;
         if (int s = object_bvh(B, SLOT_OBJ_B, &objB)) return s;
+        objA_ = objA;
+        objB_ = objB;
+        object_parity = A->contiguous && B->contiguous;
         uint8_t* act_a = active;
         uint8_t* act_b = active + std::max(A->num_objects, 1);
         if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
@@ -743,8 +753,9 @@ struct Join {
         if (int s = scratch(ctx, SLOT_TRIS_B, 4 * std::max<uint64_t>(B->nt, 1), &tb)) return s;
         // Chunk culling keeps the triangles and edges whose chunk box meets an
         // object box of the other side.  Parity (intersection, containment)
-        // needs every triangle of a target object above the query point, so
-        // those predicates keep whole objects' triangles and cull edges only.
+        // needs every triangle of a target object above the query point: it
+        // runs on object pairs over the datasets' own triangles when their
+        // objects are contiguous; otherwise the hierarchies keep whole objects.
         uint8_t* tchunk_a = chunk_flags;
         uint8_t* tchunk_b = tchunk_a + (A->nt + 31) / 32 + 1;
         uint8_t* echunk_a = tchunk_b + (B->nt + 31) / 32 + 1;
@@ -754,8 +765,9 @@ struct Join {
         // a hierarchy of A's surviving chunk boxes instead of A's object boxes,
         // which matters when A's objects are large (long tubes).
         DevDataset cull_b = objA;
-        const bool two_rounds = chunked && o.predicate == PIERCE_OVERLAP && A->num_parts == 0 && A->nt > 0;
-        if (chunked && o.predicate == PIERCE_OVERLAP) {
+        const bool tri_chunks = chunked && (o.predicate == PIERCE_OVERLAP || object_parity);
+        const bool two_rounds = tri_chunks && A->num_parts == 0 && A->nt > 0;
+        if (tri_chunks) {
             float* boxes_a = nullptr;
             uint32_t* clist = nullptr;
             uint32_t* cidx = nullptr;
@@ -1076,7 +1088,12 @@ struct Join {
             cudaMemsetAsync(ptable, 0xFF, pslots * 8, ctx->stream);
             cudaMemsetAsync(par, 0, pslots * 4, ctx->stream);
             int b = timer.record();
-            if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots)) return s;
+            if (object_parity) {
+                if (int s = launch_parity_objects(ctx, src, swap ? objA_ : objB_, tgt, swap, ptable, par, pslots))
+                    return s;
+            } else if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots)) {
+                return s;
+            }
             timer.span(b, timer.record(), ms);
             uint32_t bits = 0;
             if (int s = read_device_error(ctx, &bits)) return s;

@@ -71,6 +71,11 @@ struct DevDataset {
     // (x >= 0 internal node; x < 0 leaf ~x of y triangles; (-1, 0) empty)
     const int32_t* obj_part;
     const int2* part_roots;
+    // the dataset's own triangles (parity by object pairs): vertices, indices
+    // and per object its contiguous triangle range (first, count)
+    const float* verts;
+    const uint32_t* idx;
+    const int2* obj_range;
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -162,6 +167,10 @@ struct pierce_dataset {
     int32_t num_parts = 0;
     int32_t* d_obj_part = nullptr;
     int2* d_part_roots = nullptr;
+    // per object (first triangle, triangle count); contiguous = every
+    // object's triangles form one index range
+    int2* d_obj_range = nullptr;
+    int contiguous = 0;
 
     pgpu::DevDataset view() const {
         pgpu::DevDataset v;
@@ -178,6 +187,9 @@ struct pierce_dataset {
         v.num_objects = num_objects;
         v.obj_part = d_obj_part;
         v.part_roots = (num_parts && built) ? d_part_roots : nullptr;
+        v.verts = d_vertices;
+        v.idx = d_indices;
+        v.obj_range = contiguous ? d_obj_range : nullptr;
         return v;
     }
 };

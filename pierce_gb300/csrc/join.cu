@@ -994,6 +994,141 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
     return check_cuda(cudaGetLastError(), "parity kernel");
 }
 
+// Parity by object pairs: a warp per source object walks the target's
+// object hierarchy with the +Z ray of the object's first vertex (candidate
+// target objects: box contains the point in x, y and reaches above it) and
+// counts, across its lanes, the crossings of every triangle of each
+// candidate (the object's contiguous triangle range).  Odd counts go to the
+// parity table.  Needs no triangle hierarchy, so the per-join hierarchies
+// can drop triangles far from the other side.
+struct ParityObjParams {
+    DevDataset src;   // first vertices, partitions
+    DevDataset objs;  // the target's object hierarchy
+    DevDataset tgt;   // the target's triangles (verts, idx, obj_range)
+    int swap;
+    uint64_t* table;
+    uint32_t* parity;
+    uint64_t mask;
+    uint32_t* err;
+    DevCounters* ctr;
+};
+
+__global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    uint32_t n_nodes = 0, n_tests = 0, n_rays = 0;
+    PredCounters pc{0, 0};
+    for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < P.src.num_objects;
+         s += warps) {
+        const float4 fv = __ldg(P.src.first_vertex + s);
+        if (fv.w != 0.0f) continue;  // object without triangles (warp-uniform)
+        ++n_rays;
+        const float3 p = make_float3(fv.x, fv.y, fv.z);
+        auto candidate = [&](int32_t t) {
+            const int2 r = __ldg(P.tgt.obj_range + t);
+            uint32_t crossings = 0;
+            for (int k = lane; k < r.y; k += 32) {
+                const int64_t tri = (int64_t)r.x + k;
+                const uint32_t i0 = __ldg(P.tgt.idx + 3 * tri), i1 = __ldg(P.tgt.idx + 3 * tri + 1),
+                               i2 = __ldg(P.tgt.idx + 3 * tri + 2);
+                const float3 a = make_float3(__ldg(P.tgt.verts + 3 * (size_t)i0), __ldg(P.tgt.verts + 3 * (size_t)i0 + 1),
+                                             __ldg(P.tgt.verts + 3 * (size_t)i0 + 2));
+                const float3 b = make_float3(__ldg(P.tgt.verts + 3 * (size_t)i1), __ldg(P.tgt.verts + 3 * (size_t)i1 + 1),
+                                             __ldg(P.tgt.verts + 3 * (size_t)i1 + 2));
+                const float3 c = make_float3(__ldg(P.tgt.verts + 3 * (size_t)i2), __ldg(P.tgt.verts + 3 * (size_t)i2 + 1),
+                                             __ldg(P.tgt.verts + 3 * (size_t)i2 + 2));
+                if (fminf(a.x, fminf(b.x, c.x)) > p.x || fmaxf(a.x, fmaxf(b.x, c.x)) < p.x ||
+                    fminf(a.y, fminf(b.y, c.y)) > p.y || fmaxf(a.y, fmaxf(b.y, c.y)) < p.y ||
+                    fmaxf(a.z, fmaxf(b.z, c.z)) < p.z)
+                    continue;
+                ++n_tests;
+                if (zray_cross(p, a, b, c, pc)) crossings ^= 1u;
+            }
+            const unsigned odd = __popc(__ballot_sync(0xFFFFFFFFu, crossings != 0)) & 1u;
+            if (odd && lane == 0) {
+                const uint64_t key = P.swap ? pack_key(t, (int32_t)s) : pack_key((int32_t)s, t);
+                uint32_t probes = 0;
+                const int64_t slot = hash_insert(P.table, P.mask, key, P.err, probes);
+                if (slot >= 0) P.parity[slot] = 1u;  // one warp owns the keys of its source object
+            }
+        };
+        auto leaf = [&](int first, int count) {
+            for (int k = 0; k < count; ++k) {
+                const float4 a4 = __ldg(P.objs.soup + 3 * (int64_t)(first + k));
+                const float4 b4 = __ldg(P.objs.soup + 3 * (int64_t)(first + k) + 1);
+                if (a4.x <= p.x && p.x <= b4.x && a4.y <= p.y && p.y <= b4.y && b4.z >= p.z)
+                    candidate(__float_as_int(a4.w));
+            }
+        };
+        int first, count;
+        int node = traversal_start(P.src, P.objs, (int32_t)s, first, count);
+        if (node < 0) {
+            leaf(first, count);
+            continue;
+        }
+        int stack[kStackSize];
+        int sp = 0;
+        for (;;) {
+            ++n_nodes;
+            const Node* nd = P.objs.nodes + node;
+            const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+            const int4 ch = __ldg(&nd->ch);
+            bool h0 = bx.x <= p.x && p.x <= bx.y && by.x <= p.y && p.y <= by.y && bz.y >= p.z;
+            bool h1 = bx.z <= p.x && p.x <= bx.w && by.z <= p.y && p.y <= by.w && bz.w >= p.z;
+            if (h0 && ch.x < 0) {
+                leaf(~ch.x, ch.z & 0xFF);
+                h0 = false;
+            }
+            if (h1 && ch.y < 0) {
+                leaf(~ch.y, (ch.z >> 8) & 0xFF);
+                h1 = false;
+            }
+            if (h0 && h1) {
+                if (sp >= kStackSize) {
+                    if (lane == 0) atomicOr(P.err, ERR_STACK_OVERFLOW);
+                    break;
+                }
+                stack[sp++] = ch.y;
+                node = ch.x;
+            } else if (h0) {
+                node = ch.x;
+            } else if (h1) {
+                node = ch.y;
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp];
+            }
+        }
+    }
+    // per-lane test and ambiguity counts; rays and node visits once per warp
+    flush_counter(&P.ctr->tri_tests, n_tests);
+    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+    flush_counter(&P.ctr->parity_rays, lane == 0 ? n_rays : 0u);
+    flush_counter(&P.ctr->node_visits, lane == 0 ? n_nodes : 0u);
+}
+
+int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
+                          int swap, uint64_t* table, uint32_t* parity, uint64_t slots) {
+    if (src.num_objects <= 0 || !tgt.obj_range) return PIERCE_OK;
+    ParityObjParams P;
+    P.src = src;
+    P.objs = objs;
+    P.tgt = tgt;
+    P.swap = swap;
+    P.table = table;
+    P.parity = parity;
+    P.mask = slots - 1;
+    P.err = ctx->d_err;
+    P.ctr = ctx->d_counters;
+    const int64_t warps = src.num_objects;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
+                                                                             (int64_t)ctx->sm_count * 32));
+    k_parity_objects<<<blocks, 128, 0, ctx->stream>>>(P);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "parity (object pairs) kernel");
+}
+
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
                   unsigned long long* d_count) {
     k_compact<<<grid_cap(ctx, (int64_t)slots, 256), 256, 0, ctx->stream>>>(table, slots, out, d_count, cap);

@@ -495,11 +495,39 @@ __global__ void k_first_tri(const int32_t* __restrict__ t2o, int64_t nt, int32_t
     }
 }
 
-__global__ void k_obj_finish(const int32_t* __restrict__ first_tri, int32_t nobj, int64_t nv,
+// Per object: number of triangles and highest triangle index (warps whose
+// lanes share one object aggregate first).
+__global__ void k_obj_count_last(const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj, int32_t* count,
+                                 int32_t* last) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        int32_t o = t < nt ? t2o[t] : -1;
+        if (o >= nobj) o = -1;
+        const int32_t o0 = __shfl_sync(0xFFFFFFFFu, o, 0);
+        const unsigned valid = __ballot_sync(0xFFFFFFFFu, o >= 0);
+        if (__all_sync(0xFFFFFFFFu, o == o0 || o < 0) && o0 >= 0) {
+            const int hi = 31 - __clz(valid);
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(count + o0, __popc(valid));
+                atomicMax(last + o0, (int32_t)(base + hi));
+            }
+        } else if (o >= 0) {
+            atomicAdd(count + o, 1);
+            atomicMax(last + o, (int32_t)t);
+        }
+    }
+}
+
+__global__ void k_obj_finish(const int32_t* __restrict__ first_tri, const int32_t* __restrict__ count,
+                             const int32_t* __restrict__ last, int32_t nobj, int64_t nv,
                              const float* __restrict__ verts, const uint32_t* __restrict__ idx, float4* first_vertex,
-                             uint32_t* obj_box_o) {
+                             uint32_t* obj_box_o, int2* obj_range, int32_t* contiguous) {
     for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nobj; o += (int64_t)gridDim.x * blockDim.x) {
         const int32_t t = first_tri[o];
+        const int32_t c = count[o];
+        obj_range[o] = make_int2(c > 0 ? t : 0, c);
+        if (c > 0 && last[o] - t + 1 != c) atomicAnd(contiguous, 0);
         float4 fv = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // w = 1: object has no triangle
         if (t != 0x7FFFFFFF) {
             const uint32_t vi = idx[3 * (size_t)t];
@@ -531,20 +559,35 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
     const int32_t nobj = ds->num_objects;
     if (nobj <= 0) return PIERCE_OK;
     void* p = nullptr;
-    if (int s = scratch(ctx, 1, sizeof(int32_t) * (size_t)nobj, &p)) return s;
+    // first triangle, count, last triangle per object, then the contiguity flag
+    if (int s = scratch(ctx, 1, sizeof(int32_t) * (3 * (size_t)nobj + 4), &p)) return s;
     int32_t* first_tri = static_cast<int32_t*>(p);
+    int32_t* count = first_tri + nobj;
+    int32_t* last = count + nobj;
+    int32_t* flag = last + nobj;
     uint32_t* box_o = reinterpret_cast<uint32_t*>(ds->d_obj_box);
     cudaStream_t st = ctx->stream;
     k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(first_tri), 0x7FFFFFFFu, nobj);
+    cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)nobj, st);
+    k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(last), 0xFFFFFFFFu, nobj);
+    k_fill_u32<<<1, 32, 0, st>>>(reinterpret_cast<uint32_t*>(flag), 1u, 1);
     k_obj_box_init<<<grid_for(ctx, 6 * (int64_t)nobj, 256), 256, 0, st>>>(box_o, nobj);
     if (ds->nt > 0)
         k_first_tri<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt, nobj,
                                                                           first_tri, box_o, ds->d_vertices,
                                                                           ds->d_indices);
-    k_obj_finish<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(first_tri, nobj, (int64_t)ds->nv, ds->d_vertices,
-                                                            ds->d_indices, ds->d_first_vertex, box_o);
-    ctx->launches += 3 + (ds->nt > 0 ? 1 : 0);
-    return check_cuda(cudaGetLastError(), "prepare_objects");
+    if (ds->nt > 0)
+        k_obj_count_last<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt,
+                                                                               nobj, count, last);
+    k_obj_finish<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(first_tri, count, last, nobj, (int64_t)ds->nv,
+                                                            ds->d_vertices, ds->d_indices, ds->d_first_vertex, box_o,
+                                                            ds->d_obj_range, flag);
+    ctx->launches += 6 + (ds->nt > 0 ? 2 : 0);
+    if (int s = check_cuda(cudaGetLastError(), "prepare_objects")) return s;
+    int64_t contiguous = 0;
+    if (int s = host_value(ctx, flag, 4, &contiguous, "object ranges")) return s;
+    ds->contiguous = contiguous != 0;
+    return PIERCE_OK;
 }
 
 // Triangles -> LBVH.  The n triangles are idx[3t..3t+2] for t = list[i]

@@ -196,3 +196,21 @@ def test_golden_pair_sets(ctx, name):
                                               cull_objects=False)), g["overlap_fp32"])
     assert np.array_equal(keys(J.intersection_join(ctx, da, db)), g["intersection"])
     assert np.array_equal(keys(J.containment_join(ctx, da, db)), g["containment"])
+
+
+@pytest.mark.parametrize("predicate", ["intersection", "containment"])
+def test_noncontiguous_objects_match_oracle(ctx, predicate):
+    """Objects whose triangles are interleaved take the parity path over the
+    per-join triangle hierarchies (whole objects kept); contiguous ones take
+    the object-pair parity path.  Both must equal the oracle."""
+    A, B = pg.ellipsoid_pair(11, 12, 120, 120, 2, lo=0, hi=45, frac_inside=0.3)
+    rng = np.random.default_rng(4)
+    perm = rng.permutation(B.num_triangles)
+    Bs = pg.Geometry.from_arrays(B.vertices, B.indices[perm], B.tri_to_object[perm])
+    Bs.set_edges(B.edge_starts, B.edge_ends, B.edge_src)
+    want = O.intersection_keys(A, B) if predicate == "intersection" else O.containment_keys(A, B)
+    for geom in (B, Bs):
+        da, db = ds(ctx, A, 4), ds(ctx, geom, 4)
+        got = keys(J.join(ctx, da, db, predicate=predicate))
+        assert np.array_equal(np.sort(got), np.sort(want))
+    assert len(want) > 10
