@@ -201,6 +201,8 @@ typedef struct pierce_dataset_info {
     double ms_build;              /* GPU time of the last build */
     float bounds_lo[3], bounds_hi[3];
     int32_t num_parts;            /* partitions (0: not partitioned) */
+    int32_t objects_contiguous;   /* 1: every object's triangles form one index range */
+    int32_t reserved;
 } pierce_dataset_info;
 
 /* ---- context ------------------------------------------------------------ */

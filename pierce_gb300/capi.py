@@ -112,7 +112,8 @@ class Tuned(C.Structure):
 class DatasetInfo(C.Structure):
     _fields_ = [("num_vertices", U64), ("num_triangles", U64), ("num_edges", U64),
                 ("num_objects", I32), ("built", I32), ("num_nodes", U64), ("device_bytes", U64),
-                ("ms_build", D), ("bounds_lo", F * 3), ("bounds_hi", F * 3), ("num_parts", I32)]
+                ("ms_build", D), ("bounds_lo", F * 3), ("bounds_hi", F * 3), ("num_parts", I32),
+                ("objects_contiguous", I32), ("reserved", I32)]
 
 
 # Every symbol the header declares, with its signature.

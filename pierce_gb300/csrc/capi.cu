@@ -585,6 +585,7 @@ int pierce_dataset_info_get(const pierce_dataset* ds, pierce_dataset_info* out) 
     out->num_edges = ds->ne;
     out->num_objects = ds->num_objects;
     out->num_parts = ds->num_parts;
+    out->objects_contiguous = ds->contiguous;
     out->built = ds->built;
     out->num_nodes = ds->num_nodes;
     out->device_bytes = ds->device_bytes;

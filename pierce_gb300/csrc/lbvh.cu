@@ -508,9 +508,9 @@ __global__ void k_obj_count_last(const int32_t* __restrict__ t2o, int64_t nt, in
         const unsigned valid = __ballot_sync(0xFFFFFFFFu, o >= 0);
         if (__all_sync(0xFFFFFFFFu, o == o0 || o < 0) && o0 >= 0) {
             const int hi = 31 - __clz(valid);
-            if ((threadIdx.x & 31) == 0) {
+            if ((threadIdx.x & 31) == 0) {  // t is this warp's first triangle here
                 atomicAdd(count + o0, __popc(valid));
-                atomicMax(last + o0, (int32_t)(base + hi));
+                atomicMax(last + o0, (int32_t)(t + hi));
             }
         } else if (o >= 0) {
             atomicAdd(count + o, 1);

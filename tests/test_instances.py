@@ -100,3 +100,16 @@ def test_tube_structural_edges_equal_extracted_edges():
     h.extract_edges(order=1)
     assert h.num_edges == len(src)
     assert edge_set(es, ee, src) == edge_set(h.edge_starts, h.edge_ends, h.edge_src)
+
+
+@pytest.mark.gpu
+def test_object_contiguity_flag(ctx):
+    from pierce_gb300 import join as J
+    g = pg.ellipsoid_pair(3, 4, 300, 0, 2, frac_inside=0.0, frac_contact=0.0)[0]
+    d = J.Dataset.from_geometry(ctx, g)
+    assert d.info().objects_contiguous == 1
+    perm = np.random.default_rng(1).permutation(g.num_triangles)
+    s = pg.Geometry.from_arrays(g.vertices, g.indices[perm], g.tri_to_object[perm])
+    s.set_edges(g.edge_starts, g.edge_ends, g.edge_src)
+    assert J.Dataset.from_geometry(ctx, s).info().objects_contiguous == 0
+    assert J.Dataset.from_instances(ctx, pg.instances(1, 500, pg.SPHERES, 0, 4)).info().objects_contiguous == 1
