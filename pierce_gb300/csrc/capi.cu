@@ -267,7 +267,10 @@ int dataset_alloc(pierce_dataset* ds) {
     if (int s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices")) return s;
     if (int s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes")) return s;
     if (int s = device_alloc((void**)&ds->d_obj_range, 8 * (size_t)std::max(nobj, 1), "object ranges")) return s;
-    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * (size_t)nobj;
+    const size_t tcb = 24 * ((ds->nt + 31) / 32 + 1), ecb = 24 * ((ds->ne + 31) / 32 + 1);
+    if (int s = device_alloc((void**)&ds->d_tri_chunk_box, tcb, "triangle chunk boxes")) return s;
+    if (int s = device_alloc((void**)&ds->d_edge_chunk_box, ecb, "edge chunk boxes")) return s;
+    ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * (size_t)nobj + tcb + ecb;
     return PIERCE_OK;
 }
 
@@ -418,7 +421,7 @@ void pierce_dataset_destroy(pierce_dataset* ds) {
     cudaDeviceSynchronize();
     void* ptrs[] = {ds->d_vertices, ds->d_indices,  ds->d_tri_to_object, ds->d_edges,  ds->d_edge_src,
                     ds->d_soup,     ds->d_nodes,    ds->d_first_vertex,  ds->d_obj_box, ds->d_obj_part,
-                    ds->d_part_roots, ds->d_obj_range};
+                    ds->d_part_roots, ds->d_obj_range, ds->d_tri_chunk_box, ds->d_edge_chunk_box};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete ds;

@@ -76,6 +76,9 @@ struct DevDataset {
     const float* verts;
     const uint32_t* idx;
     const int2* obj_range;
+    // boxes (lo.xyz, hi.xyz) of every 32 consecutive triangles / edges
+    const float* tri_chunk_box;
+    const float* edge_chunk_box;
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -171,6 +174,9 @@ struct pierce_dataset {
     // object's triangles form one index range
     int2* d_obj_range = nullptr;
     int contiguous = 0;
+    // boxes of every 32 consecutive triangles and edges (6 floats each)
+    float* d_tri_chunk_box = nullptr;
+    float* d_edge_chunk_box = nullptr;
 
     pgpu::DevDataset view() const {
         pgpu::DevDataset v;
@@ -190,6 +196,8 @@ struct pierce_dataset {
         v.verts = d_vertices;
         v.idx = d_indices;
         v.obj_range = contiguous ? d_obj_range : nullptr;
+        v.tri_chunk_box = d_tri_chunk_box;
+        v.edge_chunk_box = d_edge_chunk_box;
         return v;
     }
 };

@@ -815,7 +815,8 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
                                                       const uint8_t* __restrict__ obj_active,
                                                       const int32_t* __restrict__ obj_part, DevDataset objs,
                                                       uint8_t* __restrict__ chunk_active,
-                                                      float* __restrict__ chunk_box) {
+                                                      float* __restrict__ chunk_box,
+                                                      const float* __restrict__ pre_box) {
     const int lane = threadIdx.x & 31;
     const int64_t n_chunks = (n + kChunk - 1) / kChunk;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -824,7 +825,17 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
         float3 mylo = make_float3(0, 0, 0), myhi = make_float3(0, 0, 0);
         bool myany = false, mymixed = false;
         int32_t mypart = 0;
-        for (int j = 0; j < 32; ++j) {
+        if (pre_box) {
+            // the dataset's own chunk boxes (items of inactive objects are
+            // dropped later, when the list is collected)
+            if (c0 + lane < n_chunks) {
+                const float* b = pre_box + 6 * (c0 + lane);
+                mylo = make_float3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
+                myhi = make_float3(__ldg(b + 3), __ldg(b + 4), __ldg(b + 5));
+                myany = mylo.x <= myhi.x;
+            }
+        }
+        for (int j = 0; j < 32 && !pre_box; ++j) {
             const int64_t c = c0 + j;
             if (c >= n_chunks) break;
             const int64_t i = c * kChunk + lane;
@@ -924,13 +935,15 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
     const int64_t warps = (n_chunks + 31) / 32;
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
                                                                              (int64_t)ctx->sm_count * 32));
+    // unpartitioned datasets read their stored chunk boxes
+    const float* pre = src.obj_part ? nullptr : (edges ? src.edge_chunk_box : src.tri_chunk_box);
     if (edges)
         k_chunk_active<true><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n, obj_active,
-                                                              src.obj_part, objs, chunk_active, chunk_box);
+                                                              src.obj_part, objs, chunk_active, chunk_box, pre);
     else
         k_chunk_active<false><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n,
                                                                obj_active, src.obj_part, objs, chunk_active,
-                                                               chunk_box);
+                                                               chunk_box, pre);
     k_collect_chunked<<<grid_cap(ctx, (n + 7) / 8, 256), 256, 0, ctx->stream>>>(edges ? src.edge_src : t2o, n,
                                                                                 obj_active, chunk_active, list,
                                                                                 count);
@@ -1027,8 +1040,7 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
         auto candidate = [&](int32_t t) {
             const int2 r = __ldg(P.tgt.obj_range + t);
             uint32_t crossings = 0;
-            for (int k = lane; k < r.y; k += 32) {
-                const int64_t tri = (int64_t)r.x + k;
+            auto test = [&](int64_t tri) {
                 const uint32_t i0 = __ldg(P.tgt.idx + 3 * tri), i1 = __ldg(P.tgt.idx + 3 * tri + 1),
                                i2 = __ldg(P.tgt.idx + 3 * tri + 2);
                 const float3 a = make_float3(__ldg(P.tgt.verts + 3 * (size_t)i0), __ldg(P.tgt.verts + 3 * (size_t)i0 + 1),
@@ -1040,9 +1052,32 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                 if (fminf(a.x, fminf(b.x, c.x)) > p.x || fmaxf(a.x, fmaxf(b.x, c.x)) < p.x ||
                     fminf(a.y, fminf(b.y, c.y)) > p.y || fmaxf(a.y, fmaxf(b.y, c.y)) < p.y ||
                     fmaxf(a.z, fmaxf(b.z, c.z)) < p.z)
-                    continue;
+                    return;
                 ++n_tests;
                 if (zray_cross(p, a, b, c, pc)) crossings ^= 1u;
+            };
+            if (P.tgt.tri_chunk_box) {
+                // only the 32-triangle chunks whose box the ray's column meets
+                const int64_t end = (int64_t)r.x + r.y;
+                const int64_t c_first = (int64_t)r.x / 32, c_last = (end - 1) / 32;
+                for (int64_t c0 = c_first; c0 <= c_last; c0 += 32) {
+                    const int64_t c = c0 + lane;
+                    bool hit = false;
+                    if (c <= c_last) {
+                        const float* bb = P.tgt.tri_chunk_box + 6 * c;
+                        hit = __ldg(bb) <= p.x && p.x <= __ldg(bb + 3) && __ldg(bb + 1) <= p.y &&
+                              p.y <= __ldg(bb + 4) && __ldg(bb + 5) >= p.z;
+                    }
+                    unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
+                        m &= m - 1;
+                        const int64_t tri = (c0 + bit) * 32 + lane;
+                        if (tri >= r.x && tri < end) test(tri);
+                    }
+                }
+            } else {
+                for (int k = lane; k < r.y; k += 32) test((int64_t)r.x + k);
             }
             const unsigned odd = __popc(__ballot_sync(0xFFFFFFFFu, crossings != 0)) & 1u;
             if (odd && lane == 0) {

@@ -311,114 +311,71 @@ __device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], 
     hi[2] = __ldcg(bz + 2 * slot + 1);
 }
 
-// 6. refit in waves.  The leaf wave computes each leaf's box, stores it in
-// its parent's child slot and flips the parent's arrival toggle; the second
-// arrival appends the parent to a list.  Each following wave takes the list
-// of nodes whose two child slots are complete, merges them, stores the
-// result in the grandparent and appends it the same way.  A node is only
-// read in the wave after the one that completed it, so kernel boundaries
-// order the box stores and loads and the toggle needs no memory fence; every
-// wave runs full warps.  The number of waves is the tree height (<= 64).
-__device__ __forceinline__ void block_append(bool has, uint32_t value, uint32_t* out, unsigned long long* count) {
-    __shared__ uint32_t warp_tot[32];
-    __shared__ unsigned long long base;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
-    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, has);
-    if (lane == 0) warp_tot[wid] = __popc(ballot);
-    __syncthreads();
-    if (wid == 0) {
-        uint32_t w = lane < nwarps ? warp_tot[lane] : 0;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, off);
-            if (lane >= off) w += v;
+// 6. bottom-up refit in one launch.  A leaf's thread stores the leaf box in
+// its parent's child slot, then flips the parent's arrival toggle with an
+// acquire-release atomic: the release makes the box visible before the flip,
+// and the acquire lets the second arrival see its sibling's box.  The first
+// arrival stops; the second merges both slots and carries on to the
+// grandparent, so every node is completed by exactly one thread and no
+// thread ever waits.  A chain is at most the tree height long; the step
+// bound only guards against a corrupt tree.
+__global__ void __launch_bounds__(256) k_refit_chain(const float4* __restrict__ soup, int64_t n, Node* nodes,
+                                                     const unsigned long long* __restrict__ leaf_rec,
+                                                     float* root_box, uint32_t* err) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long rec = leaf_rec[j];
+        if (rec == ~0ull) continue;
+        const int count = (int)(rec & 0xFF);
+        int side = (int)((rec >> 8) & 1);
+        uint32_t node = (uint32_t)(rec >> 9);
+        if ((int64_t)node >= n - 1 || j + count > n) {
+            atomicOr(err, ERR_STACK_OVERFLOW);
+            continue;
         }
-        if (lane < nwarps) warp_tot[lane] = w;
-        if (lane == 31) base = w ? atomicAdd(count, (unsigned long long)w) : 0ull;
-    }
-    __syncthreads();
-    if (has) out[base + (wid ? warp_tot[wid - 1] : 0u) + __popc(ballot & ((1u << lane) - 1u))] = value;
-    __syncthreads();
-}
-
-__device__ __forceinline__ void write_slot(Node* nd, int slot, const float lo[3], const float hi[3]) {
-    float* bx = reinterpret_cast<float*>(&nd->bx);
-    float* by = reinterpret_cast<float*>(&nd->by);
-    float* bz = reinterpret_cast<float*>(&nd->bz);
-    bx[2 * slot] = lo[0];
-    bx[2 * slot + 1] = hi[0];
-    by[2 * slot] = lo[1];
-    by[2 * slot + 1] = hi[1];
-    bz[2 * slot] = lo[2];
-    bz[2 * slot + 1] = hi[2];
-}
-
-// Store a finished box into node `node`'s slot `side`; true when this was the
-// second arrival (the node is then complete).
-__device__ __forceinline__ bool deliver(Node* nodes, uint32_t node, int side, const float lo[3], const float hi[3]) {
-    Node* nd = nodes + node;
-    write_slot(nd, side, lo, hi);
-    return (atomicXor(reinterpret_cast<unsigned int*>(&nd->ch.w), 1u) & 1u) != 0u;
-}
-
-__global__ void __launch_bounds__(256) k_refit_leaves(const float4* __restrict__ soup, int64_t n, Node* nodes,
-                                                      const unsigned long long* __restrict__ leaf_rec,
-                                                      uint32_t* list_out, unsigned long long* count_out) {
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = base + threadIdx.x;
-        bool done = false, bad_leaf = false;
-        uint32_t node = 0;
-        if (j < n) {
-            const unsigned long long rec = leaf_rec[j];
-            if (rec != ~0ull) {
-                const int count = (int)(rec & 0xFF);
-                const int side = (int)((rec >> 8) & 1);
-                node = (uint32_t)(rec >> 9);
-                float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-                if ((int64_t)node >= n - 1 || j + count > n) bad_leaf = true;
-                for (int k = 0; k < count && !bad_leaf; ++k)
-                    for (int v = 0; v < 3; ++v) {
-                        const float4 p = soup[3 * (j + k) + v];
-                        lo[0] = fminf(lo[0], p.x);
-                        lo[1] = fminf(lo[1], p.y);
-                        lo[2] = fminf(lo[2], p.z);
-                        hi[0] = fmaxf(hi[0], p.x);
-                        hi[1] = fmaxf(hi[1], p.y);
-                        hi[2] = fmaxf(hi[2], p.z);
-                    }
-                if (!bad_leaf) done = deliver(nodes, node, side, lo, hi);
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        for (int k = 0; k < count; ++k)
+            for (int v = 0; v < 3; ++v) {
+                const float4 p = soup[3 * (j + k) + v];
+                lo[0] = fminf(lo[0], p.x);
+                lo[1] = fminf(lo[1], p.y);
+                lo[2] = fminf(lo[2], p.z);
+                hi[0] = fmaxf(hi[0], p.x);
+                hi[1] = fmaxf(hi[1], p.y);
+                hi[2] = fmaxf(hi[2], p.z);
             }
-        }
-        block_append(done, node, list_out, count_out);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_refit_wave(Node* nodes, int64_t num_nodes, const uint32_t* __restrict__ list_in,
-                                                    const unsigned long long* __restrict__ count_in, int64_t list_cap,
-                                                    uint32_t* list_out, unsigned long long* count_out,
-                                                    float* root_box) {
-    int64_t n = (int64_t)*count_in;
-    if (n > list_cap) n = list_cap;  // never read past the list
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = base + threadIdx.x;
-        bool done = false;
-        uint32_t parent = 0;
-        if (i < n && (int64_t)list_in[i] < num_nodes) {
-            const Node* nd = nodes + list_in[i];
-            const float4 bx = nd->bx, by = nd->by, bz = nd->bz;
-            const uint32_t w = (uint32_t)nd->ch.w;
-            const float lo[3] = {fminf(bx.x, bx.z), fminf(by.x, by.z), fminf(bz.x, bz.z)};
-            const float hi[3] = {fmaxf(bx.y, bx.w), fmaxf(by.y, by.w), fmaxf(bz.y, bz.w)};
-            parent = w >> 2;
+        for (int step = 0;; ++step) {
+            if (step >= 256) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                break;
+            }
+            Node* nd = nodes + node;
+            store_child_box(nd, side, lo, hi);
+            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> toggle(
+                *reinterpret_cast<unsigned int*>(&nd->ch.w));
+            const unsigned int old = toggle.fetch_xor(1u, cuda::memory_order_acq_rel);
+            if ((old & 1u) == 0u) break;  // first arrival: the sibling's chain continues
+            float l2[3], h2[3];
+            load_child_box(nd, 0, lo, hi);
+            load_child_box(nd, 1, l2, h2);
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], l2[k]);
+                hi[k] = fmaxf(hi[k], h2[k]);
+            }
+            const uint32_t parent = old >> 2;
             if (parent == kRootParent) {
                 for (int k = 0; k < 3; ++k) {
                     root_box[k] = lo[k];
                     root_box[3 + k] = hi[k];
                 }
-            } else if ((int64_t)parent < num_nodes) {
-                done = deliver(nodes, parent, (int)((w >> 1) & 1u), lo, hi);
+                break;
             }
+            if ((int64_t)parent >= n - 1) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                break;
+            }
+            side = (int)((old >> 1) & 1u);
+            node = parent;
         }
-        block_append(done, parent, list_out, count_out);
     }
 }
 
@@ -555,8 +512,53 @@ static inline int grid_for(pierce_ctx* ctx, int64_t n, int block) {
     return (int)(blocks < 1 ? 1 : blocks);
 }
 
+// Boxes of every 32 consecutive triangles (EDGES = false) or edges: a warp
+// per chunk, one item per lane, reduced with shuffles.
+template <bool EDGES>
+__global__ void __launch_bounds__(256) k_chunk_boxes(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                                     const float4* __restrict__ edges, int64_t n,
+                                                     float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t chunks = (n + 31) / 32;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+        const int64_t i = c * 32 + lane;
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        if (i < n) {
+            if (EDGES) {
+                const float4 a = __ldg(edges + 2 * i), b = __ldg(edges + 2 * i + 1);
+                lo[0] = fminf(a.x, b.x); lo[1] = fminf(a.y, b.y); lo[2] = fminf(a.z, b.z);
+                hi[0] = fmaxf(a.x, b.x); hi[1] = fmaxf(a.y, b.y); hi[2] = fmaxf(a.z, b.z);
+            } else {
+                for (int v = 0; v < 3; ++v) {
+                    const float3 p = load_vertex(verts, __ldg(idx + 3 * i + v));
+                    lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+                    hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+                }
+            }
+        }
+        for (int k = 0; k < 3; ++k)
+            for (int off = 16; off > 0; off >>= 1) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], off));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], off));
+            }
+        if (lane < 6) out[6 * c + lane] = lane < 3 ? lo[lane] : hi[lane - 3];
+    }
+}
+
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
     const int32_t nobj = ds->num_objects;
+    {
+        cudaStream_t st = ctx->stream;
+        const int64_t tc = (int64_t)(ds->nt + 31) / 32, ec = (int64_t)(ds->ne + 31) / 32;
+        if (tc > 0 && ds->d_tri_chunk_box)
+            k_chunk_boxes<false><<<grid_for(ctx, 32 * tc, 256), 256, 0, st>>>(ds->d_vertices, ds->d_indices, nullptr,
+                                                                              (int64_t)ds->nt, ds->d_tri_chunk_box);
+        if (ec > 0 && ds->d_edge_chunk_box)
+            k_chunk_boxes<true><<<grid_for(ctx, 32 * ec, 256), 256, 0, st>>>(nullptr, nullptr, ds->d_edges,
+                                                                             (int64_t)ds->ne, ds->d_edge_chunk_box);
+        ctx->launches += (tc > 0) + (ec > 0);
+    }
     if (nobj <= 0) return PIERCE_OK;
     void* p = nullptr;
     // first triangle, count, last triangle per object, then the contiguity flag
@@ -632,9 +634,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     uint32_t* bounds = reinterpret_cast<uint32_t*>(leaf_rec + n);  // 6 words
     float* d_root_box = reinterpret_cast<float*>(bounds + 6);        // 6 floats
     // byte layout after the n leaf records: bounds [8n, 8n+24), root box
-    // [8n+24, 8n+48), two wave counters [8n+64, 8n+80); allocation 8n+128
-    unsigned long long* wave_count = leaf_rec + n + 8;
-    // partitioned: per-partition bounds after the wave counters, [8n+128, ...)
+    // [8n+24, 8n+48); allocation 8n+128
+    // partitioned: per-partition bounds after that, [8n+128, ...)
     uint32_t* pbounds = reinterpret_cast<uint32_t*>(leaf_rec + n + 16);
     uint64_t* keys64 = static_cast<uint64_t*>(pk);
 
@@ -681,29 +682,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
         else
             k_karras<uint32_t><<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec,
                                                                       nullptr);
-        // wave lists reuse the Morton key buffer (free after the hierarchy step;
-        // the sorted keys in its upper half are no longer needed either)
-        uint32_t* lists[2] = {keys, keys + (n + 1) / 2 + 1};
-        cudaMemsetAsync(wave_count, 0, 2 * sizeof(unsigned long long), st);
-        k_refit_leaves<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, lists[0], wave_count);
+        k_refit_chain<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, d_root_box, ctx->d_err);
         ctx->launches += 2;
-        // waves until the root is reached: at most one per tree level, and a
-        // Karras tree over 30-bit codes split by 32-bit indices has < 64 levels
-        bool finished = false;
-        for (int wave = 0; wave < 64 && !finished; ++wave) {
-            const int in = wave & 1, out = in ^ 1;
-            cudaMemsetAsync(wave_count + out, 0, sizeof(unsigned long long), st);
-            k_refit_wave<<<grid_for(ctx, n / 2 + 1, B), B, 0, st>>>(nodes, n - 1, lists[in], wave_count + in,
-                                                                       n / 2 + 1, lists[out], wave_count + out,
-                                                                       d_root_box);
-            ctx->launches += 1;
-            if ((wave & 7) == 7) {
-                int64_t left = 0;
-                if (int s = host_value(ctx, wave_count + out, 8, &left, "refit waves")) return s;
-                finished = left == 0;
-            }
-        }
-        if (!finished) return set_error(PIERCE_ERR_CUDA, "bvh refit did not reach the root in 64 waves");
         shape->num_nodes = (uint64_t)(n - 1);
         shape->root_is_leaf = 0;
         shape->root_leaf_count = 0;
