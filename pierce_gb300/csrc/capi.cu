@@ -29,7 +29,8 @@ int launch_collect_tris(pierce_ctx* ctx, const int32_t* t2o, int64_t nt, const u
                         unsigned long long* count);
 int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uint32_t* idx, const int32_t* t2o,
                       const DevDataset& src, const uint8_t* obj_active, const DevDataset& objs,
-                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box);
+                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box,
+                      uint32_t* chunk_list, unsigned long long* chunk_count);
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
@@ -81,6 +82,7 @@ enum : int {
     SLOT_TRIS_B = 20,
     // 21, 22: learned sizing
     SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
+    SLOT_CHUNK_LIST = 24,  // active chunk ids of one culling pass
 };
 }  // namespace
 
@@ -676,6 +678,7 @@ struct Join {
     uint64_t amb_cap = 0;
     bool defer = true;
     uint8_t* chunk_flags = nullptr;
+    uint32_t* chunk_list = nullptr;  // active chunk ids of the culling pass in flight
     // object hierarchies of the per-join path, and whether parity runs on
     // object pairs (both datasets store each object's triangles contiguously)
     DevDataset objA_{}, objB_{};
@@ -694,9 +697,10 @@ struct Join {
         active = static_cast<uint8_t*>(p) + 128;
         chunk_flags = active + nobj_a + nobj_b;
         if (o.cull_objects || o.active_bvh) {
-            if (int s = scratch(ctx, SLOT_LIST_AB, 4 * std::max<uint64_t>(A->ne, 1), &p)) return s;
+            // chunk lists round up to whole chunks: 32 spare entries
+            if (int s = scratch(ctx, SLOT_LIST_AB, 4 * (A->ne + 64), &p)) return s;
             list[0] = static_cast<uint32_t*>(p);
-            if (int s = scratch(ctx, SLOT_LIST_BA, 4 * std::max<uint64_t>(B->ne, 1), &p)) return s;
+            if (int s = scratch(ctx, SLOT_LIST_BA, 4 * (B->ne + 64), &p)) return s;
             list[1] = static_cast<uint32_t*>(p);
         }
         amb_cap = std::min<uint64_t>(std::max<uint64_t>(A->ne + B->ne, 1024), 1ull << 24);
@@ -753,8 +757,13 @@ struct Join {
         if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
         if (int s = launch_object_active(ctx, vb, objA, act_b)) return s;
         void *ta = nullptr, *tb = nullptr;
-        if (int s = scratch(ctx, SLOT_TRIS_A, 4 * std::max<uint64_t>(A->nt, 1), &ta)) return s;
-        if (int s = scratch(ctx, SLOT_TRIS_B, 4 * std::max<uint64_t>(B->nt, 1), &tb)) return s;
+        if (int s = scratch(ctx, SLOT_TRIS_A, 4 * (A->nt + 64), &ta)) return s;
+        if (int s = scratch(ctx, SLOT_TRIS_B, 4 * (B->nt + 64), &tb)) return s;
+        void* pcl = nullptr;
+        const size_t max_chunks = std::max((A->nt + 31) / 32, std::max((B->nt + 31) / 32,
+                                           std::max((A->ne + 31) / 32, (B->ne + 31) / 32)));
+        if (int s = scratch(ctx, SLOT_CHUNK_LIST, 4 * max_chunks + 64, &pcl)) return s;
+        chunk_list = static_cast<uint32_t*>(pcl);
         // Chunk culling keeps the triangles and edges whose chunk box meets an
         // object box of the other side.  Parity (intersection, containment)
         // needs every triangle of a target object above the query point: it
@@ -799,7 +808,7 @@ struct Join {
                 clist = reinterpret_cast<uint32_t*>(q);
             }
             if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
-                                          tchunk_a, (uint32_t*)ta, words + 5, boxes_a))
+                                          tchunk_a, (uint32_t*)ta, words + 5, boxes_a, chunk_list, words + 8))
                 return s;
             if (two_rounds) {
                 if (int s = launch_flag_list(ctx, tchunk_a, nca, clist, words + 7)) return s;
@@ -817,7 +826,7 @@ struct Join {
                 cull_b.root_leaf_count = shc.root_leaf_count;
             }
             if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
-                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr))
+                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
                 return s;
         } else {
             if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
@@ -827,10 +836,10 @@ struct Join {
         }
         if (chunked) {
             if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a, list[0],
-                                          words + 0, nullptr))
+                                          words + 0, nullptr, chunk_list, words + 8))
                 return s;
             if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, two_rounds ? cull_b : objA,
-                                          echunk_b, list[1], words + 1, nullptr))
+                                          echunk_b, list[1], words + 1, nullptr, chunk_list, words + 8))
                 return s;
         } else {
             if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;

@@ -96,7 +96,7 @@ struct RayOpts {
     int short_stack = -1;     // shared-memory stack entries per thread (-1: default)
 };
 
-constexpr int kScratchSlots = 24;
+constexpr int kScratchSlots = 32;
 constexpr int kSizingScratchSlot = 21;  // 21 and 22: learned sizing (sizing.cu)
 
 struct BvhShape {

@@ -268,7 +268,9 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
 }
 
 template <int MODE, int PREC>
-__global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
+// 10 resident blocks per SM (48 registers): the traversal is bound by the
+// latency of dependent node loads, so more resident warps hide more of it.
+__global__ void __launch_bounds__(128, 10) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
     int lstack[kStackSize];
     RayCounters rc;
@@ -900,17 +902,6 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
     }
 }
 
-// Items of active objects in active chunks -> compacted list.
-__global__ void __launch_bounds__(256) k_collect_chunked(const int32_t* __restrict__ item_obj, int64_t n,
-                                                         const uint8_t* __restrict__ active,
-                                                         const uint8_t* __restrict__ chunk_active,
-                                                         uint32_t* __restrict__ list, unsigned long long* count) {
-    compact_tiles<8>(n, [&](int64_t i) {
-        const int32_t o = item_obj[i];
-        return o >= 0 && active[o] != 0 && chunk_active[i / kChunk] != 0;
-    }, list, count);
-}
-
 // Indices i < n with flags[i] != 0 -> compacted list.
 __global__ void __launch_bounds__(256) k_flag_list(const uint8_t* __restrict__ flags, int64_t n,
                                                    uint32_t* __restrict__ list, unsigned long long* count) {
@@ -925,9 +916,28 @@ int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t*
     return check_cuda(cudaGetLastError(), "flag list");
 }
 
+// Active chunks -> item list: list[32 k + j] = item j of the k-th listed
+// chunk.  A partial final chunk repeats its first item in the unused
+// positions (a repeated triangle or ray only repeats hits, which the
+// de-duplication removes).  Items of inactive objects inside active chunks
+// stay in: they cannot produce pairs, only work.
+__global__ void __launch_bounds__(256) k_expand_chunks(const uint32_t* __restrict__ chunk_list,
+                                                       const unsigned long long* __restrict__ chunk_count, int64_t n,
+                                                       uint32_t* __restrict__ list, unsigned long long* count) {
+    const int64_t total = (int64_t)*chunk_count * kChunk;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = (unsigned long long)total;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = chunk_list[i / kChunk];
+        int64_t item = c * kChunk + (i % kChunk);
+        if (item >= n) item = c * kChunk;
+        list[i] = (uint32_t)item;
+    }
+}
+
 int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uint32_t* idx, const int32_t* t2o,
                       const DevDataset& src, const uint8_t* obj_active, const DevDataset& objs,
-                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box) {
+                      uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box,
+                      uint32_t* chunk_list, unsigned long long* chunk_count) {
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     const int64_t n = edges ? src.num_edges : src.num_tris;
     if (n <= 0) return PIERCE_OK;
@@ -944,9 +954,9 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
         k_chunk_active<false><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n,
                                                                obj_active, src.obj_part, objs, chunk_active,
                                                                chunk_box, pre);
-    k_collect_chunked<<<grid_cap(ctx, (n + 7) / 8, 256), 256, 0, ctx->stream>>>(edges ? src.edge_src : t2o, n,
-                                                                                obj_active, chunk_active, list,
-                                                                                count);
+    if (int s = launch_flag_list(ctx, chunk_active, n_chunks, chunk_list, chunk_count)) return s;
+    k_expand_chunks<<<grid_cap(ctx, n_chunks * kChunk, 256), 256, 0, ctx->stream>>>(chunk_list, chunk_count, n, list,
+                                                                                    count);
     ctx->launches += 2;
     return check_cuda(cudaGetLastError(), "chunk culling");
 }

@@ -311,57 +311,150 @@ __device__ __forceinline__ void load_child_box(Node* nd, int slot, float lo[3], 
     hi[2] = __ldcg(bz + 2 * slot + 1);
 }
 
-// 6. bottom-up refit in one launch.  A leaf's thread stores the leaf box in
-// its parent's child slot, then flips the parent's arrival toggle with an
-// acquire-release atomic: the release makes the box visible before the flip,
-// and the acquire lets the second arrival see its sibling's box.  The first
-// arrival stops; the second merges both slots and carries on to the
-// grandparent, so every node is completed by exactly one thread and no
-// thread ever waits.  A chain is at most the tree height long; the step
-// bound only guards against a corrupt tree.
-__global__ void __launch_bounds__(256) k_refit_chain(const float4* __restrict__ soup, int64_t n, Node* nodes,
-                                                     const unsigned long long* __restrict__ leaf_rec,
+// 6. refit: the first levels in waves, the rest in chains.  The leaf wave
+// computes each leaf's box, stores it in its parent's child slot and flips
+// the parent's arrival toggle; the second arrival appends the parent to a
+// list.  Each following wave takes the list of nodes whose two child slots
+// are complete, merges them, stores the result in the grandparent and
+// appends it the same way.  A node is only read in the wave after the one
+// that completed it, so kernel boundaries order the box stores and loads and
+// these toggles need no memory fence; every wave runs full warps.  After a
+// few waves the remaining nodes (a small fraction near the top) finish in
+// one chain launch (k_refit_chain).
+__device__ __forceinline__ void block_append(bool has, uint32_t value, uint32_t* out, unsigned long long* count) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ unsigned long long base;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
+    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, has);
+    if (lane == 0) warp_tot[wid] = __popc(ballot);
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = lane < nwarps ? warp_tot[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, off);
+            if (lane >= off) w += v;
+        }
+        if (lane < nwarps) warp_tot[lane] = w;
+        if (lane == 31) base = w ? atomicAdd(count, (unsigned long long)w) : 0ull;
+    }
+    __syncthreads();
+    if (has) out[base + (wid ? warp_tot[wid - 1] : 0u) + __popc(ballot & ((1u << lane) - 1u))] = value;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void write_slot(Node* nd, int slot, const float lo[3], const float hi[3]) {
+    float* bx = reinterpret_cast<float*>(&nd->bx);
+    float* by = reinterpret_cast<float*>(&nd->by);
+    float* bz = reinterpret_cast<float*>(&nd->bz);
+    bx[2 * slot] = lo[0];
+    bx[2 * slot + 1] = hi[0];
+    by[2 * slot] = lo[1];
+    by[2 * slot + 1] = hi[1];
+    bz[2 * slot] = lo[2];
+    bz[2 * slot + 1] = hi[2];
+}
+
+// Store a finished box into node `node`'s slot `side`; true when this was the
+// second arrival (the node is then complete).
+__device__ __forceinline__ bool deliver(Node* nodes, uint32_t node, int side, const float lo[3], const float hi[3]) {
+    Node* nd = nodes + node;
+    write_slot(nd, side, lo, hi);
+    return (atomicXor(reinterpret_cast<unsigned int*>(&nd->ch.w), 1u) & 1u) != 0u;
+}
+
+__global__ void __launch_bounds__(256) k_refit_leaves(const float4* __restrict__ soup, int64_t n, Node* nodes,
+                                                      const unsigned long long* __restrict__ leaf_rec,
+                                                      uint32_t* list_out, unsigned long long* count_out) {
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        bool done = false, bad_leaf = false;
+        uint32_t node = 0;
+        if (j < n) {
+            const unsigned long long rec = leaf_rec[j];
+            if (rec != ~0ull) {
+                const int count = (int)(rec & 0xFF);
+                const int side = (int)((rec >> 8) & 1);
+                node = (uint32_t)(rec >> 9);
+                float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+                if ((int64_t)node >= n - 1 || j + count > n) bad_leaf = true;
+                for (int k = 0; k < count && !bad_leaf; ++k)
+                    for (int v = 0; v < 3; ++v) {
+                        const float4 p = soup[3 * (j + k) + v];
+                        lo[0] = fminf(lo[0], p.x);
+                        lo[1] = fminf(lo[1], p.y);
+                        lo[2] = fminf(lo[2], p.z);
+                        hi[0] = fmaxf(hi[0], p.x);
+                        hi[1] = fmaxf(hi[1], p.y);
+                        hi[2] = fmaxf(hi[2], p.z);
+                    }
+                if (!bad_leaf) done = deliver(nodes, node, side, lo, hi);
+            }
+        }
+        block_append(done, node, list_out, count_out);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_refit_wave(Node* nodes, int64_t num_nodes, const uint32_t* __restrict__ list_in,
+                                                    const unsigned long long* __restrict__ count_in, int64_t list_cap,
+                                                    uint32_t* list_out, unsigned long long* count_out,
+                                                    float* root_box) {
+    int64_t n = (int64_t)*count_in;
+    if (n > list_cap) n = list_cap;  // never read past the list
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        bool done = false;
+        uint32_t parent = 0;
+        if (i < n && (int64_t)list_in[i] < num_nodes) {
+            const Node* nd = nodes + list_in[i];
+            const float4 bx = nd->bx, by = nd->by, bz = nd->bz;
+            const uint32_t w = (uint32_t)nd->ch.w;
+            const float lo[3] = {fminf(bx.x, bx.z), fminf(by.x, by.z), fminf(bz.x, bz.z)};
+            const float hi[3] = {fmaxf(bx.y, bx.w), fmaxf(by.y, by.w), fmaxf(bz.y, bz.w)};
+            parent = w >> 2;
+            if (parent == kRootParent) {
+                for (int k = 0; k < 3; ++k) {
+                    root_box[k] = lo[k];
+                    root_box[3 + k] = hi[k];
+                }
+            } else if ((int64_t)parent < num_nodes) {
+                done = deliver(nodes, parent, (int)((w >> 1) & 1u), lo, hi);
+            }
+        }
+        block_append(done, parent, list_out, count_out);
+    }
+}
+
+// Chains from the last wave's list: each listed node (both slots complete)
+// merges its slots and delivers the box to its parent with an
+// acquire-release flip of the parent's toggle: the release makes the box
+// visible before the flip, the acquire lets the second arrival see its
+// sibling's box (delivered in this launch or an earlier one).  The first
+// arrival stops; the second merges and carries on upward, so every node is
+// completed by exactly one thread and no thread waits.  A chain is at most
+// the tree height long; the step bound only guards against a corrupt tree.
+__global__ void __launch_bounds__(256) k_refit_chain(Node* nodes, int64_t num_nodes,
+                                                     const uint32_t* __restrict__ list,
+                                                     const unsigned long long* __restrict__ count, int64_t list_cap,
                                                      float* root_box, uint32_t* err) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long rec = leaf_rec[j];
-        if (rec == ~0ull) continue;
-        const int count = (int)(rec & 0xFF);
-        int side = (int)((rec >> 8) & 1);
-        uint32_t node = (uint32_t)(rec >> 9);
-        if ((int64_t)node >= n - 1 || j + count > n) {
+    int64_t n = (int64_t)*count;
+    if (n > list_cap) n = list_cap;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t node = list[i];
+        if ((int64_t)node >= num_nodes) {
             atomicOr(err, ERR_STACK_OVERFLOW);
             continue;
         }
-        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-        for (int k = 0; k < count; ++k)
-            for (int v = 0; v < 3; ++v) {
-                const float4 p = soup[3 * (j + k) + v];
-                lo[0] = fminf(lo[0], p.x);
-                lo[1] = fminf(lo[1], p.y);
-                lo[2] = fminf(lo[2], p.z);
-                hi[0] = fmaxf(hi[0], p.x);
-                hi[1] = fmaxf(hi[1], p.y);
-                hi[2] = fmaxf(hi[2], p.z);
-            }
+        float lo[3], hi[3], l2[3], h2[3];
+        Node* nd = nodes + node;
+        load_child_box(nd, 0, lo, hi);
+        load_child_box(nd, 1, l2, h2);
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], l2[k]);
+            hi[k] = fmaxf(hi[k], h2[k]);
+        }
+        uint32_t w = (uint32_t)__ldcg(&nd->ch.w);
         for (int step = 0;; ++step) {
-            if (step >= 256) {
-                atomicOr(err, ERR_STACK_OVERFLOW);
-                break;
-            }
-            Node* nd = nodes + node;
-            store_child_box(nd, side, lo, hi);
-            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> toggle(
-                *reinterpret_cast<unsigned int*>(&nd->ch.w));
-            const unsigned int old = toggle.fetch_xor(1u, cuda::memory_order_acq_rel);
-            if ((old & 1u) == 0u) break;  // first arrival: the sibling's chain continues
-            float l2[3], h2[3];
-            load_child_box(nd, 0, lo, hi);
-            load_child_box(nd, 1, l2, h2);
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = fminf(lo[k], l2[k]);
-                hi[k] = fmaxf(hi[k], h2[k]);
-            }
-            const uint32_t parent = old >> 2;
+            const uint32_t parent = w >> 2;
             if (parent == kRootParent) {
                 for (int k = 0; k < 3; ++k) {
                     root_box[k] = lo[k];
@@ -369,12 +462,23 @@ __global__ void __launch_bounds__(256) k_refit_chain(const float4* __restrict__ 
                 }
                 break;
             }
-            if ((int64_t)parent >= n - 1) {
+            if ((int64_t)parent >= num_nodes || step >= 256) {
                 atomicOr(err, ERR_STACK_OVERFLOW);
                 break;
             }
-            side = (int)((old >> 1) & 1u);
-            node = parent;
+            Node* pn = nodes + parent;
+            store_child_box(pn, (int)((w >> 1) & 1u), lo, hi);
+            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> toggle(
+                *reinterpret_cast<unsigned int*>(&pn->ch.w));
+            const unsigned int old = toggle.fetch_xor(1u, cuda::memory_order_acq_rel);
+            if ((old & 1u) == 0u) break;  // first arrival: the sibling's chain continues
+            load_child_box(pn, 0, lo, hi);
+            load_child_box(pn, 1, l2, h2);
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], l2[k]);
+                hi[k] = fmaxf(hi[k], h2[k]);
+            }
+            w = old;
         }
     }
 }
@@ -634,7 +738,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     uint32_t* bounds = reinterpret_cast<uint32_t*>(leaf_rec + n);  // 6 words
     float* d_root_box = reinterpret_cast<float*>(bounds + 6);        // 6 floats
     // byte layout after the n leaf records: bounds [8n, 8n+24), root box
-    // [8n+24, 8n+48); allocation 8n+128
+    // [8n+24, 8n+48), two wave counters [8n+64, 8n+80); allocation 8n+128
+    unsigned long long* wave_count = leaf_rec + n + 8;
     // partitioned: per-partition bounds after that, [8n+128, ...)
     uint32_t* pbounds = reinterpret_cast<uint32_t*>(leaf_rec + n + 16);
     uint64_t* keys64 = static_cast<uint64_t*>(pk);
@@ -682,8 +787,23 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
         else
             k_karras<uint32_t><<<grid_for(ctx, n - 1, B), B, 0, st>>>(skeys, n, leaf_size, nodes, leaf_rec,
                                                                       nullptr);
-        k_refit_chain<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, d_root_box, ctx->d_err);
-        ctx->launches += 2;
+        // waves for the wide bottom levels, then one chain launch for the rest;
+        // the lists reuse the Morton key buffer (free after the hierarchy step)
+        uint32_t* lists[2] = {keys, keys + (n + 1) / 2 + 1};
+        cudaMemsetAsync(wave_count, 0, 2 * sizeof(unsigned long long), st);
+        k_refit_leaves<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, lists[0], wave_count);
+        constexpr int kWaves = 3;
+        for (int wave = 0; wave < kWaves; ++wave) {
+            const int in = wave & 1, out = in ^ 1;
+            cudaMemsetAsync(wave_count + out, 0, sizeof(unsigned long long), st);
+            k_refit_wave<<<grid_for(ctx, n / 2 + 1, B), B, 0, st>>>(nodes, n - 1, lists[in], wave_count + in,
+                                                                       n / 2 + 1, lists[out], wave_count + out,
+                                                                       d_root_box);
+        }
+        const int last = kWaves & 1;
+        k_refit_chain<<<grid_for(ctx, n / 2 + 1, B), B, 0, st>>>(nodes, n - 1, lists[last], wave_count + last,
+                                                                    n / 2 + 1, d_root_box, ctx->d_err);
+        ctx->launches += 3 + kWaves;
         shape->num_nodes = (uint64_t)(n - 1);
         shape->root_is_leaf = 0;
         shape->root_leaf_count = 0;
