@@ -268,9 +268,7 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
 }
 
 template <int MODE, int PREC>
-// 10 resident blocks per SM (48 registers): the traversal is bound by the
-// latency of dependent node loads, so more resident warps hide more of it.
-__global__ void __launch_bounds__(128, 10) k_edge_rays(EdgeRayParams P) {
+__global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
     int lstack[kStackSize];
     RayCounters rc;
