@@ -157,7 +157,7 @@ typedef struct pierce_join_opts {
     int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets') */
     int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
     int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 32) */
-    int32_t reserved;
+    int32_t traversal;            /* culled rays: 0 a warp traverses its 32 rays together, 1 one ray per thread */
 } pierce_join_opts;
 
 typedef struct pierce_stats {

@@ -68,7 +68,7 @@ class JoinOpts(C.Structure):
                 ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
                 ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
                 ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V),
-                ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("reserved", I32)]
+                ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("traversal", I32)]
 
 
 class Stats(C.Structure):

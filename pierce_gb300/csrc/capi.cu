@@ -920,6 +920,7 @@ struct Join {
             }
             ro.rays_per_fetch = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
             ro.short_stack = o.stack_depth > 0 ? o.stack_depth : -1;
+            ro.packets = o.traversal == 0 ? 1 : 0;
             const int prec = precision_mode();
             if (prec == 2) {
                 ro.amb_queue = amb_queue;
@@ -1393,7 +1394,7 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
     if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
-        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32)
+        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 1)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
     *out_opts = o;
     return PIERCE_OK;

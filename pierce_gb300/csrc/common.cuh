@@ -94,6 +94,7 @@ struct RayOpts {
     uint64_t amb_cap = 0;
     int rays_per_fetch = 32;  // rays a warp takes from the list per fetch
     int short_stack = -1;     // shared-memory stack entries per thread (-1: default)
+    int packets = 1;          // warp-cooperative traversal of the listed rays
 };
 
 constexpr int kScratchSlots = 32;

@@ -123,6 +123,7 @@ struct EdgeRayParams {
     // stack entries kept in (dynamic) shared memory per thread
     int rays_per_fetch;
     int short_stack;
+    int packets;  // 1: a warp traverses its 32 rays together (ray-list mode)
 };
 
 __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float hy, float lz, float hz,
@@ -162,8 +163,7 @@ __device__ __forceinline__ int traversal_start(const DevDataset& src, const DevD
 
 template <int MODE, int PREC>
 __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int* sstack, int* lstack,
-                                           RayCounters& rc, PredCounters& pc) {
-    const int depth = P.short_stack;
+                                           RayCounters& rc, PredCounters& pc, int depth) {
     const int tid = threadIdx.x;
     const float4 s4 = __ldg(P.src.edges + 2 * e);
     const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
@@ -267,6 +267,148 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
     rc.hits += (uint32_t)nhit;
 }
 
+// Warp-cooperative traversal of 32 rays (one per lane, e < 0: none).  The
+// rays of a fetch come from one 32-edge chunk, so they are close together:
+// the warp walks the hierarchy once, each node is loaded once for all lanes
+// (one broadcast load), every lane tests its own segment against the two
+// child boxes, and a child is entered with the mask of the lanes that meet
+// it (__ballot_sync).  The node stack (node, lane mask) is shared by the
+// warp.  Leaves are tested per lane with the same code as trace_edge, so the
+// hits of each ray equal those of the one-ray-per-thread traversal.  When
+// the lanes start in different subtrees (partitions) each lane falls back
+// to the one-ray traversal with a local stack.
+template <int MODE, int PREC>
+__device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, int2* wstack, int* lstack,
+                                             RayCounters& rc, PredCounters& pc) {
+    const int lane = threadIdx.x & 31;
+    const bool valid = e >= 0;
+    const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!vmask) return;
+    float4 s4 = make_float4(0, 0, 0, 0), e4 = make_float4(0, 0, 0, 0);
+    if (valid) {
+        s4 = __ldg(P.src.edges + 2 * e);
+        e4 = __ldg(P.src.edges + 2 * e + 1);
+    }
+    const int32_t src_obj = __float_as_int(s4.w);
+    int lf = 0, lc = 0;
+    const int node0 = valid ? traversal_start(P.src, P.tgt, src_obj, lf, lc) : 0;
+    const int leader = __ffs(vmask) - 1;
+    const int n0 = __shfl_sync(0xFFFFFFFFu, node0, leader);
+    const int lf0 = __shfl_sync(0xFFFFFFFFu, lf, leader), lc0 = __shfl_sync(0xFFFFFFFFu, lc, leader);
+    const bool same = __all_sync(0xFFFFFFFFu, !valid || (node0 == n0 && (n0 >= 0 || (lf == lf0 && lc == lc0))));
+    if (!same) {
+        if (valid) trace_edge<MODE, PREC>(P, e, nullptr, lstack, rc, pc, 0);
+        return;
+    }
+    const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
+    const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
+    const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
+    int64_t out = (MODE == MODE_WRITE && valid) ? P.offsets[e] : 0;
+    int32_t last_obj = -1;
+    int nhit = 0;
+    auto leaf = [&](int first, int count) {
+        for (int k = 0; k < count; ++k) {
+            const int64_t t = (int64_t)first + k;
+            const float4 a4 = __ldg(P.tgt.soup + 3 * t);
+            const int32_t obj = __float_as_int(a4.w);
+            if (obj == last_obj) continue;
+            const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
+            const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
+            if (count > 1) {
+                const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
+                const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
+                const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
+                if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
+            }
+            ++rc.tests;
+            const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
+                         c = make_float3(c4.x, c4.y, c4.z);
+            bool hit;
+            if (PREC == PREC_EXACT) {
+                hit = seg_tri_exact(p, q, a, b, c, pc);
+            } else if (PREC == PREC_FP32) {
+                hit = seg_tri_mt_fp32(p, q, a, b, c);
+            } else {
+                const int cls = seg_tri_fp32_class(p, q, a, b, c);
+                if (cls == SEG_AMBIGUOUS) {
+                    ++pc.fp32_ambiguous;
+                    if (MODE != MODE_WRITE) {
+                        const unsigned long long slot = atomicAdd(P.amb_count, 1ull);
+                        if (slot < P.amb_cap) P.amb_queue[slot] = ((unsigned long long)e << 32) | (uint32_t)t;
+                        else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
+                    }
+                    continue;
+                }
+                hit = cls == SEG_HIT;
+            }
+            if (!hit) continue;
+            last_obj = obj;
+            ++nhit;
+            if (MODE == MODE_COUNT) continue;
+            const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
+            if (MODE == MODE_WRITE) {
+                P.keys[out++] = key;
+            } else {
+                ++rc.inserts;
+                hash_insert(P.table, P.mask, key, P.err, rc.probes);
+            }
+        }
+    };
+    if (n0 < 0) {
+        if (valid && lc0 > 0) leaf(lf0, lc0);
+    } else {
+        int node = n0, sp = 0;
+        unsigned mask = vmask;
+        for (;;) {
+            if (lane == 0) ++rc.nodes;
+            const Node* nd = P.tgt.nodes + node;
+            const float4 bx = __ldg(&nd->bx), by = __ldg(&nd->by), bz = __ldg(&nd->bz);
+            const int4 ch = __ldg(&nd->ch);
+            const bool in = (mask >> lane) & 1u;
+            const bool h0 = in && box_overlap(bx.x, bx.y, by.x, by.y, bz.x, bz.y, lo, hi);
+            const bool h1 = in && box_overlap(bx.z, bx.w, by.z, by.w, bz.z, bz.w, lo, hi);
+            unsigned m0 = __ballot_sync(0xFFFFFFFFu, h0), m1 = __ballot_sync(0xFFFFFFFFu, h1);
+            if (ch.x < 0 && m0) {
+                if (h0) leaf(~ch.x, ch.z & 0xFF);
+                m0 = 0;
+            }
+            if (ch.y < 0 && m1) {
+                if (h1) leaf(~ch.y, (ch.z >> 8) & 0xFF);
+                m1 = 0;
+            }
+            __syncwarp();
+            if (m0 && m1) {
+                if (sp >= kStackSize) {
+                    if (lane == 0) atomicOr(P.err, ERR_STACK_OVERFLOW);
+                    break;
+                }
+                if (lane == 0) wstack[sp] = make_int2(ch.y, (int)m1);
+                ++sp;
+                node = ch.x;
+                mask = m0;
+            } else if (m0) {
+                node = ch.x;
+                mask = m0;
+            } else if (m1) {
+                node = ch.y;
+                mask = m1;
+            } else {
+                if (sp == 0) break;
+                --sp;
+                __syncwarp();
+                const int2 top = wstack[sp];
+                node = top.x;
+                mask = (unsigned)top.y;
+            }
+            __syncwarp();
+        }
+    }
+    if (valid) {
+        if (MODE == MODE_COUNT) P.counts[e] = nhit;
+        rc.hits += (uint32_t)nhit;
+    }
+}
+
 template <int MODE, int PREC>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
@@ -281,15 +423,20 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
         const unsigned long long n = *P.ray_count;
         const int lane = threadIdx.x & 31;
         const unsigned long long per = (unsigned long long)P.rays_per_fetch;
+        int2* wstack = reinterpret_cast<int2*>(sstack + P.short_stack * 128) + (threadIdx.x >> 5) * kStackSize;
         for (;;) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(P.ray_cursor, per);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
-            for (unsigned long long r = lane; r < per; r += 32) {
+            for (unsigned long long r = lane; r < per; r += 32) {  // per/32 rounds for every lane
                 const unsigned long long i = base + r;
-                if (i < n) {
-                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc);
+                if (P.packets) {
+                    const bool has = i < n;
+                    trace_packet<MODE, PREC>(P, has ? (int64_t)P.ray_list[i] : -1, wstack, lstack, rc, pc);
+                    rays += has ? 1u : 0u;
+                } else if (i < n) {
+                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc, P.short_stack);
                     ++rays;
                 }
             }
@@ -297,7 +444,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     } else {
         const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         if (e < P.src.num_edges) {
-            trace_edge<MODE, PREC>(P, e, sstack, lstack, rc, pc);
+            trace_edge<MODE, PREC>(P, e, sstack, lstack, rc, pc, P.short_stack);
             ++rays;
         }
     }
@@ -667,11 +814,13 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.amb_cap = ro ? ro->amb_cap : 0;
     P.rays_per_fetch = (ro && ro->rays_per_fetch > 0) ? ro->rays_per_fetch : 32;
     P.short_stack = (ro && ro->short_stack >= 0) ? std::min(ro->short_stack, kShortStack) : kShortStack;
+    P.packets = (ro && ro->packets && ro->list) ? 1 : 0;
     if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");
     if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
     const int B = 128;
-    const size_t smem = sizeof(int) * 128 * (size_t)P.short_stack;
+    // per-thread short stacks, then (packets) one (node, mask) stack per warp
+    const size_t smem = sizeof(int) * 128 * (size_t)P.short_stack + (P.packets ? sizeof(int2) * 4 * kStackSize : 0);
     dim3 g;
     if (P.ray_list) {
         cudaMemsetAsync(P.ray_cursor, 0, sizeof(unsigned long long), ctx->stream);

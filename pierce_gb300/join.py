@@ -190,7 +190,8 @@ class JoinResult:
 def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
               max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
-              sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0) -> capi.JoinOpts:
+              sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0,
+              traversal="packets") -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -208,6 +209,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.active_bvh = 1 if active_bvh else 0
     o.sizing_model = sizing_model.handle if sizing_model is not None else None
     o.leaf_size, o.rays_per_warp, o.stack_depth = int(leaf_size), int(rays_per_warp), int(stack_depth)
+    o.traversal = {"packets": 0, "per_ray": 1}[traversal] if isinstance(traversal, str) else int(traversal)
     return o
 
 

@@ -214,3 +214,17 @@ def test_noncontiguous_objects_match_oracle(ctx, predicate):
         got = keys(J.join(ctx, da, db, predicate=predicate))
         assert np.array_equal(np.sort(got), np.sort(want))
     assert len(want) > 10
+
+
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+@pytest.mark.parametrize("predicate", ["overlap", "intersection"])
+def test_warp_packets_equal_per_ray_traversal(ctx, case, sizing, predicate):
+    """Warp-cooperative traversal of the culled rays against one ray per
+    thread: same pairs, same raw hit counts, same triangle tests."""
+    name, A, B = case
+    da, db = ds(ctx, A, 8), ds(ctx, B, 8)
+    r1 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="packets")
+    r2 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="per_ray")
+    assert np.array_equal(r1.pairs, r2.pairs)
+    assert r1.stats["raw_hits"] == r2.stats["raw_hits"] and r1.stats["tri_tests"] == r2.stats["tri_tests"]
+    assert r1.stats["node_visits"] < r2.stats["node_visits"]
