@@ -253,4 +253,5 @@ int sort_u64_pairs(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, uint3
                    int64_t n, int end_bit);
 int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
 int unique_u64(pierce_ctx* ctx, const uint64_t* in, uint64_t* out, int64_t n, int64_t* num_unique);
+int select_flagged(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* out, unsigned long long* d_count);
 }  // namespace pgpu

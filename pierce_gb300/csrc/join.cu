@@ -1049,18 +1049,10 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
     }
 }
 
-// Indices i < n with flags[i] != 0 -> compacted list.
-__global__ void __launch_bounds__(256) k_flag_list(const uint8_t* __restrict__ flags, int64_t n,
-                                                   uint32_t* __restrict__ list, unsigned long long* count) {
-    compact_tiles<8>(n, [&](int64_t i) { return flags[i] != 0; }, list, count);
-}
-
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count) {
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     if (n <= 0) return PIERCE_OK;
-    k_flag_list<<<grid_cap(ctx, (n + 7) / 8, 256), 256, 0, ctx->stream>>>(flags, n, list, count);
-    ctx->launches += 1;
-    return check_cuda(cudaGetLastError(), "flag list");
+    return select_flagged(ctx, flags, n, list, count);  // in index order: deterministic lists
 }
 
 // Active chunks -> item list: list[32 k + j] = item j of the k-th listed

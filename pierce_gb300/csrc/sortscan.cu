@@ -4,6 +4,7 @@
 // (pierce/query/src/cuda/scan_utils.cu:11-28,
 //  pierce/query/src/cuda/mesh_query_deduplication.cu:56-90).
 #include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
 #include <thrust/iterator/transform_iterator.h>
 
 #include "common.cuh"
@@ -61,6 +62,20 @@ int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, 
     cudaError_t e = cub::DeviceScan::ExclusiveSum(tmp, bytes, it, out, n, ctx->stream);
     ctx->launches += 2;
     return check_cuda(e, "exclusive scan");
+}
+
+// Indices i < n with flags[i] != 0, in increasing order, into out; the count
+// stays on the device (*d_count, 64-bit).  Order-preserving, so lists built
+// from it (and the hierarchies built over them) do not depend on scheduling.
+int select_flagged(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* out, unsigned long long* d_count) {
+    thrust::counting_iterator<uint32_t> ids(0);
+    size_t bytes = 0;
+    cub::DeviceSelect::Flagged(nullptr, bytes, ids, flags, out, d_count, n, ctx->stream);
+    void* tmp = nullptr;
+    if (int s = scratch(ctx, 0, bytes, &tmp)) return s;
+    cudaError_t e = cub::DeviceSelect::Flagged(tmp, bytes, ids, flags, out, d_count, n, ctx->stream);
+    ctx->launches += 2;
+    return check_cuda(e, "select flagged");
 }
 
 // Unique of a sorted key array; the count is read back synchronously.
