@@ -157,7 +157,7 @@ typedef struct pierce_join_opts {
     int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets') */
     int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
     int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 32) */
-    int32_t traversal;            /* culled rays: 0 a warp traverses its 32 rays together, 1 one ray per thread */
+    int32_t traversal;            /* culled rays: 0 one ray per thread, 1 a warp traverses its 32 rays together */
 } pierce_join_opts;
 
 typedef struct pierce_stats {
@@ -272,7 +272,8 @@ void pierce_result_destroy(pierce_result* r);
  * options over a grid of tuning values, one parameter at a time (leaf size
  * of the per-join hierarchies {1, 2, 4, 8} when base->active_bvh, rays per
  * warp {32, 64, 128}, stack depth {8, 16, 32}, hash load factor
- * {0.25, 0.5, 0.75} when the sizing uses a hash set), each trial the best
+ * {0.25, 0.5, 0.75} when the sizing uses a hash set, traversal {one ray per
+ * thread, warp packets}), each trial the best
  * of `repeats` timed runs after one untimed run.  *best receives the
  * fastest values; trials[0 .. *num_trials) every trial (max_trials slots,
  * may be NULL). */
@@ -280,7 +281,7 @@ typedef struct pierce_tuned {
     int32_t leaf_size;
     int32_t rays_per_warp;
     int32_t stack_depth;
-    int32_t reserved;
+    int32_t traversal;
     double hash_load_factor;
     double ms;                    /* best GPU time of the join with these values */
 } pierce_tuned;

@@ -920,7 +920,7 @@ struct Join {
             }
             ro.rays_per_fetch = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
             ro.short_stack = o.stack_depth > 0 ? o.stack_depth : -1;
-            ro.packets = o.traversal == 0 ? 1 : 0;
+            ro.packets = o.traversal == 1 ? 1 : 0;
             const int prec = precision_mode();
             if (prec == 2) {
                 ro.amb_queue = amb_queue;
@@ -1431,6 +1431,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     cur.rays_per_warp = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
     cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 32;
     cur.hash_load_factor = o.hash_load_factor;
+    cur.traversal = o.traversal;
     cur.ms = 1e300;
     // time one setting: one untimed run, then the best of `repeats`
     auto trial = [&](pierce_tuned& t) -> int {
@@ -1439,6 +1440,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
         q.rays_per_warp = t.rays_per_warp;
         q.stack_depth = t.stack_depth;
         q.hash_load_factor = t.hash_load_factor;
+        q.traversal = t.traversal;
         t.ms = 1e300;
         for (int r = 0; r <= repeats; ++r) {
             pierce_result* res = nullptr;
@@ -1456,10 +1458,11 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     const std::vector<int> rays = {32, 64, 128}, stacks = {8, 16, 32};
     const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
                                              : std::vector<double>{cur.hash_load_factor};
+    const std::vector<int> traversals = {0, 1};
     // coordinate descent: one parameter at a time, keeping the best so far
-    for (int param = 0; param < 4; ++param) {
+    for (int param = 0; param < 5; ++param) {
         const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()
-                                                                                              : loads.size();
+                         : param == 3 ? loads.size() : traversals.size();
         pierce_tuned winner = cur;
         for (size_t i = 0; i < n; ++i) {
             pierce_tuned t = cur;
@@ -1467,6 +1470,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
             if (param == 1) t.rays_per_warp = rays[i];
             if (param == 2) t.stack_depth = stacks[i];
             if (param == 3) t.hash_load_factor = loads[i];
+            if (param == 4) t.traversal = traversals[i];
             if (int s = trial(t)) return s;
             if (t.ms < winner.ms) winner = t;
         }

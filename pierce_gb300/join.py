@@ -191,7 +191,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
               max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
               sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0,
-              traversal="packets") -> capi.JoinOpts:
+              traversal="per_ray") -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -209,7 +209,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.active_bvh = 1 if active_bvh else 0
     o.sizing_model = sizing_model.handle if sizing_model is not None else None
     o.leaf_size, o.rays_per_warp, o.stack_depth = int(leaf_size), int(rays_per_warp), int(stack_depth)
-    o.traversal = {"packets": 0, "per_ray": 1}[traversal] if isinstance(traversal, str) else int(traversal)
+    o.traversal = {"per_ray": 0, "packets": 1}[traversal] if isinstance(traversal, str) else int(traversal)
     return o
 
 
@@ -220,7 +220,7 @@ def autotune(ctx: Context, a: Dataset, b: Dataset, opts: capi.JoinOpts, repeats:
     n = C.c_int32()
     check(capi.lib().pierce_autotune_join(ctx.handle, a.handle, b.handle, C.byref(opts), int(repeats),
                                           C.byref(best), trials, 64, C.byref(n)), "autotune_join")
-    as_dict = lambda t: {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
+    as_dict = lambda t: {k: getattr(t, k) for k, _ in t._fields_}
     return as_dict(best), [as_dict(trials[i]) for i in range(min(n.value, 64))]
 
 
@@ -228,6 +228,7 @@ def tuned_opts(opts: capi.JoinOpts, best: dict) -> capi.JoinOpts:
     o = capi.JoinOpts.from_buffer_copy(opts)
     o.leaf_size, o.rays_per_warp = int(best["leaf_size"]), int(best["rays_per_warp"])
     o.stack_depth, o.hash_load_factor = int(best["stack_depth"]), float(best["hash_load_factor"])
+    o.traversal = int(best.get("traversal", 0))
     return o
 
 
