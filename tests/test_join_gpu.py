@@ -228,3 +228,19 @@ def test_warp_packets_equal_per_ray_traversal(ctx, case, sizing, predicate):
     assert np.array_equal(r1.pairs, r2.pairs)
     assert r1.stats["raw_hits"] == r2.stats["raw_hits"] and r1.stats["tri_tests"] == r2.stats["tri_tests"]
     assert r1.stats["node_visits"] < r2.stats["node_visits"]
+
+
+def test_config1_full_size_matches_oracle(ctx):
+    """The small CPU-runnable configuration at its full size: 2 x 2,000
+    level-3 icospheres, radii lognormal(ln 1.5, 0.3), centres in [0, 200]^3;
+    a pair overlaps when the surfaces meet or one mesh contains the other
+    (the intersection predicate)."""
+    A = pg.icospheres(1, 2000, 3, hi=200.0)
+    B = pg.icospheres(2, 2000, 3, hi=200.0)
+    want = O.intersection_keys(A, B)
+    da, db = ds(ctx, A, 8), ds(ctx, B, 8)
+    for kw in (dict(), dict(sizing="two_pass"), dict(precision="fp32", cull_objects=False, active_bvh=False,
+                                                      sizing="two_pass")):
+        got = keys(J.intersection_join(ctx, da, db, **kw))
+        assert np.array_equal(np.sort(got), np.sort(want)), kw
+    assert len(want) > 50
