@@ -83,7 +83,6 @@ enum : int {
     // 21, 22: learned sizing
     SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
     SLOT_CHUNK_LIST = 24,  // active chunk ids of one culling pass
-    SLOT_CHUNKS_B = 25,  // the same for B's chunks (third culling round)
 };
 }  // namespace
 
@@ -775,78 +774,60 @@ struct Join {
         uint8_t* echunk_a = tchunk_b + (B->nt + 31) / 32 + 1;
         uint8_t* echunk_b = echunk_a + (A->ne + 31) / 32 + 1;
         const bool chunked = o.cull_objects != 0;
-        // Later rounds (unpartitioned): B's chunks are tested against a
-        // hierarchy of A's surviving chunk boxes instead of A's object boxes
-        // (which matters when A's objects are large, like long tubes), then
-        // A's chunks and edges against a hierarchy of B's surviving chunks.
-        DevDataset cull_b = objA, cull_a = objB;
+        // Second round (overlap, unpartitioned): B's chunks are tested against
+        // a hierarchy of A's surviving chunk boxes instead of A's object boxes,
+        // which matters when A's objects are large (long tubes).
+        DevDataset cull_b = objA;
         const bool tri_chunks = chunked && (o.predicate == PIERCE_OVERLAP || object_parity);
         const bool two_rounds = tri_chunks && A->num_parts == 0 && A->nt > 0;
         if (tri_chunks) {
-            // Hierarchy over the active chunk boxes of one side (degenerate
-            // triangles (lo, hi, hi) in scratch `slot`), from its flags.
-            auto chunk_bvh = [&](int slot, const uint8_t* flags, int64_t nc, float** boxes_out,
-                                 DevDataset* out) -> int {
+            float* boxes_a = nullptr;
+            uint32_t* clist = nullptr;
+            uint32_t* cidx = nullptr;
+            int32_t* ct2o = nullptr;
+            float4* csoup = nullptr;
+            Node* cnodes = nullptr;
+            const int64_t nca = (int64_t)((A->nt + 31) / 32);
+            if (two_rounds) {
                 void* pc = nullptr;
-                // soup 48, nodes 64, boxes 24, pseudo indices 12 + ids 4, list 4 bytes per chunk
-                const size_t per = 48 + 64 + 24 + 16 + 4;
-                if (int s = scratch(ctx, slot, per * (size_t)nc + 1024, &pc)) return s;
+                // boxes 24, list 4, pseudo indices 12 + ids 4, soup 48, nodes 64 bytes per chunk
+                const size_t per = 24 + 4 + 16 + 48 + 64;
+                if (int s = scratch(ctx, SLOT_CHUNKS, per * (size_t)nca + 1024, &pc)) return s;
                 char* q = static_cast<char*>(pc);
                 soup_align(q);
-                float4* csoup = reinterpret_cast<float4*>(q);
-                q += 48 * nc;
-                Node* cnodes = reinterpret_cast<Node*>(q);
-                q += 64 * nc;
-                float* boxes = reinterpret_cast<float*>(q);
-                q += 24 * nc;
-                uint32_t* cidx = reinterpret_cast<uint32_t*>(q);
-                q += 12 * nc;
-                int32_t* ct2o = reinterpret_cast<int32_t*>(q);
-                q += 4 * nc;
-                uint32_t* clist = reinterpret_cast<uint32_t*>(q);
-                if (!flags) {  // first call: only hand out the box array
-                    *boxes_out = boxes;
-                    return (int)PIERCE_OK;
-                }
-                if (int s = launch_flag_list(ctx, flags, nc, clist, words + 7)) return s;
-                int64_t n_act = 0;
-                if (int s = host_value(ctx, words + 7, 8, &n_act, "active chunks")) return s;
-                if (int s = launch_object_pseudo_tris(ctx, (int32_t)nc, cidx, ct2o)) return s;
-                BvhShape shc;
-                if (int s = build_lbvh(ctx, boxes, cidx, ct2o, clist, n_act, 4, csoup, cnodes, &shc, nullptr))
-                    return s;
-                *out = DevDataset{};
-                out->soup = csoup;
-                out->nodes = cnodes;
-                out->num_tris = n_act;
-                out->root_is_leaf = shc.root_is_leaf;
-                out->root_leaf_count = shc.root_leaf_count;
-                return (int)PIERCE_OK;
-            };
-            const int64_t nca = (int64_t)((A->nt + 31) / 32), ncb = (int64_t)((B->nt + 31) / 32);
-            float *boxes_a = nullptr, *boxes_b = nullptr;
-            if (two_rounds) {
-                if (int s = chunk_bvh(SLOT_CHUNKS, nullptr, nca, &boxes_a, nullptr)) return s;
-                if (int s = chunk_bvh(SLOT_CHUNKS_B, nullptr, ncb, &boxes_b, nullptr)) return s;
+                csoup = reinterpret_cast<float4*>(q);
+                q += 48 * nca;
+                cnodes = reinterpret_cast<Node*>(q);
+                q += 64 * nca;
+                boxes_a = reinterpret_cast<float*>(q);
+                q += 24 * nca;
+                cidx = reinterpret_cast<uint32_t*>(q);
+                q += 12 * nca;
+                ct2o = reinterpret_cast<int32_t*>(q);
+                q += 4 * nca;
+                clist = reinterpret_cast<uint32_t*>(q);
             }
-            // round 1: A's chunks against B's object boxes
             if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
                                           tchunk_a, (uint32_t*)ta, words + 5, boxes_a, chunk_list, words + 8))
                 return s;
-            // round 2: B's chunks against A's surviving chunks
-            if (two_rounds)
-                if (int s = chunk_bvh(SLOT_CHUNKS, tchunk_a, nca, &boxes_a, &cull_b)) return s;
-            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
-                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, boxes_b, chunk_list, words + 8))
-                return s;
-            // round 3: A's chunks again, against B's surviving chunks
             if (two_rounds) {
-                if (int s = chunk_bvh(SLOT_CHUNKS_B, tchunk_b, ncb, &boxes_b, &cull_a)) return s;
-                if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a,
-                                              cull_a, tchunk_a, (uint32_t*)ta, words + 5, nullptr, chunk_list,
-                                              words + 8))
+                if (int s = launch_flag_list(ctx, tchunk_a, nca, clist, words + 7)) return s;
+                int64_t n_act = 0;
+                if (int s = host_value(ctx, words + 7, 8, &n_act, "active chunks")) return s;
+                if (int s = launch_object_pseudo_tris(ctx, (int32_t)nca, cidx, ct2o)) return s;
+                BvhShape shc;
+                if (int s = build_lbvh(ctx, boxes_a, cidx, ct2o, clist, n_act, 4, csoup, cnodes, &shc, nullptr))
                     return s;
+                cull_b = DevDataset{};
+                cull_b.soup = csoup;
+                cull_b.nodes = cnodes;
+                cull_b.num_tris = n_act;
+                cull_b.root_is_leaf = shc.root_is_leaf;
+                cull_b.root_leaf_count = shc.root_leaf_count;
             }
+            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
+                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
+                return s;
         } else {
             if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
                 return s;
@@ -854,8 +835,8 @@ struct Join {
                 return s;
         }
         if (chunked) {
-            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, two_rounds ? cull_a : objB,
-                                          echunk_a, list[0], words + 0, nullptr, chunk_list, words + 8))
+            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a, list[0],
+                                          words + 0, nullptr, chunk_list, words + 8))
                 return s;
             if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, two_rounds ? cull_b : objA,
                                           echunk_b, list[1], words + 1, nullptr, chunk_list, words + 8))
