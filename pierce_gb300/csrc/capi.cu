@@ -83,6 +83,7 @@ enum : int {
     // 21, 22: learned sizing
     SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
     SLOT_CHUNK_LIST = 24,  // active chunk ids of one culling pass
+    SLOT_GROUPS = 25,    // group boxes and group hierarchy soup of a grouped build
 };
 }  // namespace
 
@@ -669,7 +670,8 @@ struct Join {
     uint8_t* active = nullptr;
     // words: [0] list count A->B, [1] list count B->A, [2] warp cursor,
     //        [3] deferred-test count, [4] exactly resolved key count,
-    //        [5] active triangles of A, [6] active triangles of B, [7] active chunks of A
+    //        [5] active triangles of A, [6] active triangles of B, [7] active chunks (chunk
+    //        hierarchy), [8] chunk count of a culling pass, [9] [10] active chunks of A, B
     unsigned long long* words = nullptr;
     // device views of A and B the kernels traverse (their own BVH, or the
     // per-join BVH over active triangles)
@@ -846,6 +848,13 @@ struct Join {
             if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
         }
         listed[0] = listed[1] = true;
+        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
+        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
+        // Unpartitioned chunk-culled sides build over groups of consecutive
+        // triangles (leaf = one group of `leaf` triangles, rounded to a power
+        // of two): the active chunk lists replace the triangle lists.
+        const bool grouped = tri_chunks && A->num_parts == 0;
+        if (grouped) return grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, b0);
         int64_t na = 0, nb = 0;
         if (int s = host_value(ctx, words + 5, 8, &na, "active triangles of A")) return s;
         if (int s = host_value(ctx, words + 6, 8, &nb, "active triangles of B")) return s;
@@ -860,8 +869,6 @@ struct Join {
         int2* roots_a = A->num_parts ? reinterpret_cast<int2*>((Node*)na_p + std::max<int64_t>(na, 1)) : nullptr;
         int2* roots_b = B->num_parts ? reinterpret_cast<int2*>((Node*)nb_p + std::max<int64_t>(nb, 1)) : nullptr;
         BvhShape shA, shB;
-        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
-        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
         if (int s = build_lbvh(ctx, A->d_vertices, A->d_indices, A->d_tri_to_object, (const uint32_t*)ta, na,
                                leaf_a, (float4*)sa, (Node*)na_p, &shA, nullptr, A->d_obj_part, A->num_parts,
                                roots_a))
@@ -884,6 +891,52 @@ struct Join {
         vb.root_leaf_count = shB.root_leaf_count;
         st.active_triangles[0] = (uint64_t)na;
         st.active_triangles[1] = (uint64_t)nb;
+        timer.span(b0, timer.record(), &st.ms_build);
+        return PIERCE_OK;
+    }
+
+    // Per side: active chunk ids (into the side's triangle-list buffer), then
+    // a hierarchy over groups of G consecutive triangles of those chunks.
+    int grouped_builds(const uint8_t* tchunk_a, const uint8_t* tchunk_b, uint32_t* ids_a, uint32_t* ids_b,
+                       int leaf_a, int leaf_b, int b0) {
+        auto group_of = [](int leaf) {
+            int g = 1;
+            while (g < leaf && g < 32) g <<= 1;
+            return g;
+        };
+        pierce_dataset* ds[2] = {A, B};
+        const uint8_t* flags[2] = {tchunk_a, tchunk_b};
+        uint32_t* ids[2] = {ids_a, ids_b};
+        const int G[2] = {group_of(leaf_a), group_of(leaf_b)};
+        DevDataset* views[2] = {&va, &vb};
+        const int soup_slot[2] = {SLOT_RED_SOUP_A, SLOT_RED_SOUP_B}, node_slot[2] = {SLOT_RED_NODES_A, SLOT_RED_NODES_B};
+        int64_t nc[2] = {0, 0};
+        for (int sd = 0; sd < 2; ++sd) {
+            const int64_t chunks = (int64_t)((ds[sd]->nt + 31) / 32);
+            if (int s = launch_flag_list(ctx, flags[sd], chunks, ids[sd], words + 9 + sd)) return s;
+        }
+        for (int sd = 0; sd < 2; ++sd)
+            if (int s = host_value(ctx, words + 9 + sd, 8, &nc[sd], "active chunks")) return s;
+        for (int sd = 0; sd < 2; ++sd) {
+            const int64_t ng = nc[sd] * (32 / G[sd]);
+            void *sp = nullptr, *np = nullptr, *gp = nullptr;
+            if (int s = scratch(ctx, soup_slot[sd], 48 * 32 * (size_t)std::max<int64_t>(nc[sd], 1), &sp)) return s;
+            if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1), &np)) return s;
+            if (int s = scratch(ctx, SLOT_GROUPS, 88 * (size_t)std::max<int64_t>(ng, 1) + 256, &gp)) return s;
+            BvhShape sh;
+            if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
+                                           (int64_t)ds[sd]->nt, ids[sd], nc[sd], G[sd], gp, (float4*)sp, (Node*)np,
+                                           &sh))
+                return s;
+            DevDataset& v = *views[sd];
+            v.soup = (const float4*)sp;
+            v.nodes = (const Node*)np;
+            v.num_tris = nc[sd] * 32;
+            v.root_is_leaf = sh.root_is_leaf;
+            v.root_leaf_count = sh.root_leaf_count;
+            v.part_roots = nullptr;
+            st.active_triangles[sd] = (uint64_t)(nc[sd] * 32);
+        }
         timer.span(b0, timer.record(), &st.ms_build);
         return PIERCE_OK;
     }

@@ -244,6 +244,11 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
                int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box,
                const int32_t* obj_part = nullptr, int32_t num_parts = 0, int2* part_roots = nullptr);
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds);
+// hierarchy over groups of G consecutive triangles (G divides 32) of the
+// listed 32-triangle chunks; group_scratch holds 88 bytes per group
+int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
+                       const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
+                       Node* nodes, BvhShape* shape);
 
 // sortscan.cu (CUB library calls)
 int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,

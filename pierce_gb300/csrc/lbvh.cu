@@ -818,6 +818,137 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     return PIERCE_OK;
 }
 
+// ---- hierarchies over groups of consecutive triangles --------------------
+// The per-join hierarchies are built over the chunks that survive culling.
+// Consecutive triangles of a mesh lie close together, so a group of G of
+// them (G divides 32) makes a tight leaf by itself: the hierarchy is built
+// over the group boxes (32/G per active 32-triangle chunk) instead of over
+// single triangles, which sorts and links G times fewer primitives; the
+// triangle soup then takes the groups in leaf order, G triangles per leaf.
+
+// Per listed chunk, the boxes of its groups as degenerate triangles
+// (lo, hi, hi).  Triangles past the end of the dataset (final partial chunk)
+// repeat the chunk's first triangle.
+__global__ void __launch_bounds__(256) k_group_boxes(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                                     const int32_t* __restrict__ t2o, int64_t nt,
+                                                     const uint32_t* __restrict__ chunk_list, int64_t n_chunks,
+                                                     int G, float* __restrict__ gbox, uint32_t* __restrict__ gidx,
+                                                     int32_t* __restrict__ gt2o) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n_chunks; k += warps) {
+        const int64_t c = chunk_list[k];
+        int64_t t = c * 32 + lane;
+        if (t >= nt) t = c * 32;
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        for (int v = 0; v < 3; ++v) {
+            const float3 p = load_vertex(verts, __ldg(idx + 3 * t + v));
+            lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+            hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+        }
+        for (int off = 1; off < G; off <<= 1)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = fminf(lo[d], __shfl_xor_sync(0xFFFFFFFFu, lo[d], off));
+                hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xFFFFFFFFu, hi[d], off));
+            }
+        if (lane % G == 0) {
+            const int64_t g = k * (32 / G) + lane / G;
+            float* b = gbox + 6 * g;
+            b[0] = lo[0]; b[1] = lo[1]; b[2] = lo[2];
+            b[3] = hi[0]; b[4] = hi[1]; b[5] = hi[2];
+            gidx[3 * g] = (uint32_t)(2 * g);
+            gidx[3 * g + 1] = (uint32_t)(2 * g + 1);
+            gidx[3 * g + 2] = (uint32_t)(2 * g + 1);
+            gt2o[g] = __ldg(t2o + t);
+        }
+    }
+}
+
+// Triangle soup in group leaf order: leaf position j takes group g (its
+// original index, stored by k_soup in the group soup), G triangles each.
+__global__ void __launch_bounds__(256) k_group_soup(const float4* __restrict__ gsoup, int64_t n_groups, int G,
+                                                    const uint32_t* __restrict__ chunk_list,
+                                                    const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                                    const int32_t* __restrict__ t2o, int64_t nt,
+                                                    float4* __restrict__ soup) {
+    const int per_chunk = 32 / G;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_groups * G;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = i / G;
+        const int64_t g = __float_as_int(__ldg(&gsoup[3 * j + 1].w));
+        const int64_t c = chunk_list[g / per_chunk];
+        int64_t t = c * 32 + (g % per_chunk) * G + (i % G);
+        if (t >= nt) t = c * 32;
+        const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
+        const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
+        const float3 cc = load_vertex(verts, __ldg(idx + 3 * t + 2));
+        soup[3 * i + 0] = make_float4(a.x, a.y, a.z, __int_as_float(__ldg(t2o + t)));
+        soup[3 * i + 1] = make_float4(b.x, b.y, b.z, __int_as_float((int)t));
+        soup[3 * i + 2] = make_float4(cc.x, cc.y, cc.z, 0.0f);
+    }
+}
+
+// Leaves of the group hierarchy (one group each) become soup ranges of G.
+__global__ void k_group_leaves(Node* nodes, int64_t num_nodes, int G) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < num_nodes; i += (int64_t)gridDim.x * blockDim.x) {
+        int4 ch = nodes[i].ch;
+        int c0 = ch.z & 0xFF, c1 = (ch.z >> 8) & 0xFF;
+        if (ch.x < 0) {
+            ch.x = ~((~ch.x) * G);
+            c0 = G;
+        }
+        if (ch.y < 0) {
+            ch.y = ~((~ch.y) * G);
+            c1 = G;
+        }
+        ch.z = c0 | (c1 << 8);
+        nodes[i].ch = ch;
+    }
+}
+
+int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
+                       const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
+                       Node* nodes, BvhShape* shape) {
+    cudaStream_t st = ctx->stream;
+    const int64_t ng = n_chunks * (32 / G);
+    shape->leaf_size = G;
+    if (ng == 0) {
+        shape->root_is_leaf = 1;
+        shape->root_leaf_count = 0;
+        shape->num_nodes = 0;
+        return PIERCE_OK;
+    }
+    if (ng * G >= (int64_t(1) << 30))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "bvh build: at most 2^30 - 1 triangles per hierarchy");
+    // group scratch: soup 48, boxes 24, pseudo indices 12, ids 4 bytes per group
+    char* q = static_cast<char*>(group_scratch);
+    float4* gsoup = reinterpret_cast<float4*>(q);
+    float* gbox = reinterpret_cast<float*>(q + 48 * ng);
+    uint32_t* gidx = reinterpret_cast<uint32_t*>(q + 72 * ng);
+    int32_t* gt2o = reinterpret_cast<int32_t*>(q + 84 * ng);
+    const int64_t warps = n_chunks;
+    k_group_boxes<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->sm_count * 16)),
+                    256, 0, st>>>(verts, idx, t2o, nt, chunk_list, n_chunks, G, gbox, gidx, gt2o);
+    ctx->launches += 1;
+    BvhShape gshape;
+    if (int s = build_lbvh(ctx, gbox, gidx, gt2o, nullptr, ng, 1, gsoup, nodes, &gshape, nullptr)) return s;
+    k_group_soup<<<grid_for(ctx, ng * G, 256), 256, 0, st>>>(gsoup, ng, G, chunk_list, verts, idx, t2o, nt, soup);
+    ctx->launches += 1;
+    if (gshape.root_is_leaf) {
+        shape->root_is_leaf = 1;
+        shape->root_leaf_count = (int)(gshape.root_leaf_count * G);
+        shape->num_nodes = 0;
+    } else {
+        k_group_leaves<<<grid_for(ctx, (int64_t)gshape.num_nodes, 256), 256, 0, st>>>(nodes,
+                                                                                     (int64_t)gshape.num_nodes, G);
+        ctx->launches += 1;
+        shape->root_is_leaf = 0;
+        shape->root_leaf_count = 0;
+        shape->num_nodes = gshape.num_nodes;
+    }
+    return check_cuda(cudaGetLastError(), "grouped bvh build");
+}
+
 int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
     ds->built = 0;
     // The soup and node arrays exist only for datasets that get a hierarchy
