@@ -240,7 +240,7 @@ def main_batched(args):
     # the same queries one join call each: the plain form, and the tuned form
     plain_opts = J.make_opts(predicate="overlap", sizing="two_pass", precision="fp32", cull_objects=False,
                              defer_exact=False, active_bvh=False)
-    plain = BT.run_per_query(ctx, qs, plain_opts, build_leaf=args.leaf_size, log=log, keep_pairs=True)
+    plain = BT.run_per_query(ctx, qs, plain_opts, build_leaf=args.plain_leaf_size, log=log, keep_pairs=True)
     log(f"plain per query: {plain['s']:.2f} s")
     tuned_q = J.tuned_opts(J.make_opts(predicate="overlap", sizing="hash"), best)
     per_q = BT.run_per_query(ctx, qs, tuned_q, log=log, keep_pairs=True)
@@ -386,9 +386,9 @@ def main_tubes(args):
         capi.check(L.pierce_dataset_create(ctx.handle, C.byref(views["B"]), capi.HOST_MEMORY, C.byref(upload),
                                            C.byref(hb)), "dataset B")
         if build:
-            capi.check(L.pierce_dataset_build(ctx.handle, ha, C.byref(J.default_tuning(leaf_size=args.leaf_size))),
+            capi.check(L.pierce_dataset_build(ctx.handle, ha, C.byref(J.default_tuning(leaf_size=args.plain_leaf_size))),
                        "build A")
-            capi.check(L.pierce_dataset_build(ctx.handle, hb, C.byref(J.default_tuning(leaf_size=args.leaf_size))),
+            capi.check(L.pierce_dataset_build(ctx.handle, hb, C.byref(J.default_tuning(leaf_size=args.plain_leaf_size))),
                        "build B")
         r = C.c_void_p()
         st = capi.Stats()
@@ -449,8 +449,8 @@ def main_tubes(args):
     ctx.release_scratch()
 
     def plain_dev():
-        da.build(J.default_tuning(leaf_size=args.leaf_size))
-        db.build(J.default_tuning(leaf_size=args.leaf_size))
+        da.build(J.default_tuning(leaf_size=args.plain_leaf_size))
+        db.build(J.default_tuning(leaf_size=args.plain_leaf_size))
         J.run_join(ctx, da, db, plain_o, download=False)
 
     plain_ms = device_ms(plain_dev, max(1, args.steps // 2))
@@ -493,7 +493,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full workload (debug only)")
     ap.add_argument("--cpu-sample-objects", type=int, default=3000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--leaf-size", type=int, default=8)
+    ap.add_argument("--leaf-size", type=int, default=4, help="leaf size of the tuned form's per-join hierarchies")
+    ap.add_argument("--plain-leaf-size", type=int, default=8, help="leaf size of the plain form's dataset hierarchies")
     ap.add_argument("--workload", default="ellipsoids", choices=["ellipsoids", "batched", "tubes"],
                     help="ellipsoids: the default intersection+containment line; batched: 4,096 overlap queries; "
                          "tubes: 2,000 tubes against 100,000 ellipsoids")
@@ -585,9 +586,10 @@ def main():
     torch.cuda.synchronize()
     p0 = torch.cuda.Event(enable_timing=True)
     p1 = torch.cuda.Event(enable_timing=True)
+    plain_tuning = J.default_tuning(leaf_size=args.plain_leaf_size)
     p0.record(stream)
-    da.build(tuning)
-    db.build(tuning)
+    da.build(plain_tuning)
+    db.build(plain_tuning)
     rpi = J.run_join(ctx, da, db, opts_pi)
     rpc = J.run_join(ctx, da, db, opts_pc)
     p1.record(stream)
@@ -681,7 +683,8 @@ def main():
         return 0
     clk = clocks.summary(local_rank)
     cfg.update({"l2": "inputs larger than L2 (about 9 GB of geometry and BVH per side, 129 MB L2)",
-                "leaf_size": args.leaf_size, "sizing": "hash", "precision": "exact (fp32 filter, fp64, expansions)",
+                "leaf_size": args.leaf_size, "plain_leaf_size": args.plain_leaf_size, "sizing": "hash",
+                "precision": "exact (fp32 filter, fp64, expansions)",
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
