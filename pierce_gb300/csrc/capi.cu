@@ -742,10 +742,11 @@ struct Join {
         return PIERCE_OK;
     }
 
-    // Per-join BVHs over the triangles of objects whose box meets an object
-    // box of the other side.  Exact: a segment lies in its object's box, and
-    // a first vertex with odd parity lies inside the target object's box, so
-    // no pair involves a triangle left out.
+    // Per-join BVHs over the triangles that can take part in an overlap pair
+    // (objects, then 32-triangle chunks, whose box meets a box of the other
+    // side).  Exact: a segment lies in its object's and chunk's box, and so
+    // does every target triangle.  Parity runs on object pairs over the
+    // datasets' own triangles, or keeps every triangle (see below).
     int prepare_active_bvh() {
         const int b0 = timer.record();
         DevDataset objA, objB;
@@ -831,9 +832,17 @@ struct Join {
                                           cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
                 return s;
         } else {
-            if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, act_a, (uint32_t*)ta, words + 5))
+            // Parity over these hierarchies counts every crossing above a first
+            // vertex; for meshes that are not closed a crossing can come from
+            // an object whose box the source's box does not meet, so the
+            // parity predicates keep every triangle.  Overlap keeps the
+            // triangles of active objects.
+            const bool keep_all = o.predicate != PIERCE_OVERLAP;
+            if (int s = launch_collect_tris(ctx, A->d_tri_to_object, (int64_t)A->nt, keep_all ? nullptr : act_a,
+                                            (uint32_t*)ta, words + 5))
                 return s;
-            if (int s = launch_collect_tris(ctx, B->d_tri_to_object, (int64_t)B->nt, act_b, (uint32_t*)tb, words + 6))
+            if (int s = launch_collect_tris(ctx, B->d_tri_to_object, (int64_t)B->nt, keep_all ? nullptr : act_b,
+                                            (uint32_t*)tb, words + 6))
                 return s;
         }
         if (chunked) {

@@ -79,6 +79,7 @@ struct DevDataset {
     // boxes (lo.xyz, hi.xyz) of every 32 consecutive triangles / edges
     const float* tri_chunk_box;
     const float* edge_chunk_box;
+    int edges_grouped;  // edges stored grouped by source object
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -178,6 +179,7 @@ struct pierce_dataset {
     // boxes of every 32 consecutive triangles and edges (6 floats each)
     float* d_tri_chunk_box = nullptr;
     float* d_edge_chunk_box = nullptr;
+    int edges_grouped = 0;  // edge sources non-decreasing (edges grouped by object)
 
     pgpu::DevDataset view() const {
         pgpu::DevDataset v;
@@ -199,6 +201,7 @@ struct pierce_dataset {
         v.obj_range = contiguous ? d_obj_range : nullptr;
         v.tri_chunk_box = d_tri_chunk_box;
         v.edge_chunk_box = d_edge_chunk_box;
+        v.edges_grouped = edges_grouped;
         return v;
     }
 };

@@ -965,7 +965,7 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
                                                       const int32_t* __restrict__ obj_part, DevDataset objs,
                                                       uint8_t* __restrict__ chunk_active,
                                                       float* __restrict__ chunk_box,
-                                                      const float* __restrict__ pre_box) {
+                                                      const float* __restrict__ pre_box, bool items_contiguous) {
     const int lane = threadIdx.x & 31;
     const int64_t n_chunks = (n + kChunk - 1) / kChunk;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -975,13 +975,22 @@ __global__ void __launch_bounds__(128) k_chunk_active(const float* __restrict__ 
         bool myany = false, mymixed = false;
         int32_t mypart = 0;
         if (pre_box) {
-            // the dataset's own chunk boxes (items of inactive objects are
-            // dropped later, when the list is collected)
+            // the dataset's own chunk boxes; with objects stored contiguously
+            // a chunk inside one inactive object is skipped outright
             if (c0 + lane < n_chunks) {
-                const float* b = pre_box + 6 * (c0 + lane);
-                mylo = make_float3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
-                myhi = make_float3(__ldg(b + 3), __ldg(b + 4), __ldg(b + 5));
-                myany = mylo.x <= myhi.x;
+                const int64_t i0 = (c0 + lane) * kChunk, i1 = min(i0 + kChunk, n) - 1;
+                const int32_t* io = EDGES ? edge_src : t2o;
+                bool dead = false;
+                if (items_contiguous) {
+                    const int32_t o0 = __ldg(io + i0), o1 = __ldg(io + i1);
+                    dead = o0 == o1 && (o0 < 0 || __ldg(obj_active + o0) == 0);
+                }
+                if (!dead) {
+                    const float* b = pre_box + 6 * (c0 + lane);
+                    mylo = make_float3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
+                    myhi = make_float3(__ldg(b + 3), __ldg(b + 4), __ldg(b + 5));
+                    myany = mylo.x <= myhi.x;
+                }
             }
         }
         for (int j = 0; j < 32 && !pre_box; ++j) {
@@ -1086,13 +1095,16 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
                                                                              (int64_t)ctx->sm_count * 32));
     // unpartitioned datasets read their stored chunk boxes
     const float* pre = src.obj_part ? nullptr : (edges ? src.edge_chunk_box : src.tri_chunk_box);
+    // items grouped by object: triangles of a dataset with contiguous objects,
+    // edges when the dataset's edges are grouped by source object
+    const bool grouped_items = edges ? src.edges_grouped != 0 : src.obj_range != nullptr;
     if (edges)
         k_chunk_active<true><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n, obj_active,
-                                                              src.obj_part, objs, chunk_active, chunk_box, pre);
+                                                              src.obj_part, objs, chunk_active, chunk_box, pre, grouped_items);
     else
         k_chunk_active<false><<<blocks, 128, 0, ctx->stream>>>(verts, idx, t2o, src.edges, src.edge_src, n,
                                                                obj_active, src.obj_part, objs, chunk_active,
-                                                               chunk_box, pre);
+                                                               chunk_box, pre, grouped_items);
     if (int s = launch_flag_list(ctx, chunk_active, n_chunks, chunk_list, chunk_count)) return s;
     k_expand_chunks<<<grid_cap(ctx, n_chunks * kChunk, 256), 256, 0, ctx->stream>>>(chunk_list, chunk_count, n, list,
                                                                                     count);
@@ -1106,7 +1118,7 @@ __global__ void __launch_bounds__(256) k_collect_tris(const int32_t* __restrict_
                                                       unsigned long long* count) {
     compact_tiles<8>(nt, [&](int64_t t) {
         const int32_t o = t2o[t];
-        return o >= 0 && active[o] != 0;
+        return o >= 0 && (!active || active[o] != 0);
     }, list, count);
 }
 

@@ -60,16 +60,32 @@ __global__ void k_centroids(const float* __restrict__ verts, const uint32_t* __r
         mn[0] = fminf(mn[0], m.x); mn[1] = fminf(mn[1], m.y); mn[2] = fminf(mn[2], m.z);
         mx[0] = fmaxf(mx[0], m.x); mx[1] = fmaxf(mx[1], m.y); mx[2] = fmaxf(mx[2], m.z);
     }
+    // warp, then block reduction: one set of six atomics per block
+    __shared__ float red[2][3][32];
     for (int k = 0; k < 3; ++k) {
         for (int off = 16; off > 0; off >>= 1) {
             mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
             mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
         }
     }
-    if ((threadIdx.x & 31) == 0) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0)
         for (int k = 0; k < 3; ++k) {
-            atomicMin(bounds + k, f2o(mn[k]));
-            atomicMax(bounds + 3 + k, f2o(mx[k]));
+            red[0][k][wid] = mn[k];
+            red[1][k][wid] = mx[k];
+        }
+    __syncthreads();
+    if (wid == 0) {
+        for (int k = 0; k < 3; ++k) {
+            float a = lane < nw ? red[0][k][lane] : 3.4e38f, b = lane < nw ? red[1][k][lane] : -3.4e38f;
+            for (int off = 16; off > 0; off >>= 1) {
+                a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, off));
+                b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, off));
+            }
+            if (lane == 0) {
+                atomicMin(bounds + k, f2o(a));
+                atomicMax(bounds + 3 + k, f2o(b));
+            }
         }
     }
 }
@@ -603,6 +619,12 @@ __global__ void k_obj_finish(const int32_t* __restrict__ first_tri, const int32_
     }
 }
 
+// Clears *flag when edge sources ever decrease (edges not grouped by object).
+__global__ void k_edges_grouped(const int32_t* __restrict__ src, int64_t ne, int32_t* flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1; i < ne; i += (int64_t)gridDim.x * blockDim.x)
+        if (__ldg(src + i) < __ldg(src + i - 1)) atomicAnd(flag, 0);
+}
+
 __global__ void k_obj_box_init(uint32_t* box_o, int32_t nobj) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 6 * (int64_t)nobj;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -676,7 +698,11 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
     k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(first_tri), 0x7FFFFFFFu, nobj);
     cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)nobj, st);
     k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(last), 0xFFFFFFFFu, nobj);
-    k_fill_u32<<<1, 32, 0, st>>>(reinterpret_cast<uint32_t*>(flag), 1u, 1);
+    k_fill_u32<<<1, 32, 0, st>>>(reinterpret_cast<uint32_t*>(flag), 1u, 2);
+    if (ds->ne > 1) {
+        k_edges_grouped<<<grid_for(ctx, (int64_t)ds->ne, 256), 256, 0, st>>>(ds->d_edge_src, (int64_t)ds->ne, flag + 1);
+        ctx->launches += 1;
+    }
     k_obj_box_init<<<grid_for(ctx, 6 * (int64_t)nobj, 256), 256, 0, st>>>(box_o, nobj);
     if (ds->nt > 0)
         k_first_tri<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt, nobj,
@@ -690,9 +716,11 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
                                                             ds->d_obj_range, flag);
     ctx->launches += 6 + (ds->nt > 0 ? 2 : 0);
     if (int s = check_cuda(cudaGetLastError(), "prepare_objects")) return s;
-    int64_t contiguous = 0;
+    int64_t contiguous = 0, grouped = 0;
     if (int s = host_value(ctx, flag, 4, &contiguous, "object ranges")) return s;
+    if (int s = host_value(ctx, flag + 1, 4, &grouped, "edge order")) return s;
     ds->contiguous = contiguous != 0;
+    ds->edges_grouped = grouped != 0;
     return PIERCE_OK;
 }
 
@@ -757,7 +785,7 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
     } else {
         k_fill_u32<<<1, 32, 0, st>>>(bounds, 0xFFFFFFFFu, 3);  // ordered +max
         k_fill_u32<<<1, 32, 0, st>>>(bounds + 3, 0u, 3);       // ordered -max
-        k_centroids<<<grid_for(ctx, n, B), B, 0, st>>>(verts, idx, list, n, cen, bounds);
+        k_centroids<<<std::min(grid_for(ctx, n, B), ctx->sm_count * 4), B, 0, st>>>(verts, idx, list, n, cen, bounds);
         k_morton<<<grid_for(ctx, n, B), B, 0, st>>>(cen, n, bounds, keys, vals);
         ctx->launches += 4;
         if (int s = sort_u32_pairs(ctx, keys, keys + n, vals, vals + n, n, 30)) return s;

@@ -244,3 +244,29 @@ def test_config1_full_size_matches_oracle(ctx):
         got = keys(J.intersection_join(ctx, da, db, **kw))
         assert np.array_equal(np.sort(got), np.sort(want)), kw
     assert len(want) > 50
+
+
+def test_parity_with_open_meshes_far_above(ctx):
+    """An open surface (two separate triangles of one object, interleaved with
+    another object's triangles) high above a closed mesh: the +Z ray from the
+    mesh's first vertex crosses it once, so the pair is in the intersection
+    set although the boxes do not meet.  Both parity paths must see it."""
+    A = pg.icospheres(3, 3, 1, hi=6.0)
+    fv = A.first_vertices()[0].astype(np.float64)
+    # object 0: two triangles far above object-0 first vertex; object 1: a triangle elsewhere
+    z = fv[2] + 50.0
+    tri = lambda cx, cy, cz, s: [[cx - s, cy - s, cz], [cx + s, cy - s, cz + 0.1], [cx, cy + s, cz + 0.2]]
+    verts = np.array(tri(fv[0] + 0.01, fv[1] + 0.013, z, 3.0) + tri(300, 300, 300, 1.0)
+                     + tri(fv[0] + 40.0, fv[1], z, 1.0), np.float32)
+    idx = np.arange(9, dtype=np.uint32).reshape(3, 3)
+    t2o = np.array([0, 1, 0], np.int32)            # object 0 not contiguous
+    B = pg.Geometry.from_arrays(verts, idx, t2o)
+    B.extract_edges(1)
+    want = O.intersection_keys(A, B)
+    assert len(want) >= 1
+    Bc = pg.Geometry.from_arrays(verts[[0, 1, 2, 6, 7, 8, 3, 4, 5]], idx, np.array([0, 0, 1], np.int32))
+    Bc.extract_edges(1)
+    for geom in (B, Bc):
+        da, db = ds(ctx, A, 4), ds(ctx, geom, 4)
+        got = keys(J.intersection_join(ctx, da, db))
+        assert np.array_equal(np.sort(got), np.sort(O.intersection_keys(A, geom)))
