@@ -36,7 +36,10 @@ int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots);
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
-                          int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
+                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
+size_t column_grid_bytes(int32_t n);
+int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int64_t* n_entries);
+int column_grid_fill(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int32_t* entries, ColumnGrid* g);
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
                   unsigned long long* d_count);
 int keys_to_pairs(pierce_ctx* ctx, uint64_t* keys, int64_t n);
@@ -84,6 +87,10 @@ enum : int {
     SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
     SLOT_CHUNK_LIST = 24,  // active chunk ids of one culling pass
     SLOT_GROUPS = 25,    // group boxes and group hierarchy soup of a grouped build
+    SLOT_GRID_A = 26,    // column grids (parity candidates): A's, then B's
+    SLOT_GRID_A_ENTRIES = 27,
+    SLOT_GRID_B = 28,
+    SLOT_GRID_B_ENTRIES = 29,
 };
 }  // namespace
 
@@ -685,6 +692,18 @@ struct Join {
     // object pairs (both datasets store each object's triangles contiguously)
     DevDataset objA_{}, objB_{};
     bool object_parity = false;
+    ColumnGrid gridA_{}, gridB_{};  // parity candidates of each side as a target
+
+    // Column grid of one side's object boxes in scratch slots meta/entries.
+    int column_grid(const DevDataset& v, int meta_slot, int entries_slot, ColumnGrid* g) {
+        void* pm = nullptr;
+        if (int s = scratch(ctx, meta_slot, column_grid_bytes(v.num_objects), &pm)) return s;
+        int64_t n = 0;
+        if (int s = column_grid_count(ctx, v, pm, &n)) return s;
+        void* pe = nullptr;
+        if (int s = scratch(ctx, entries_slot, 4 * (size_t)std::max<int64_t>(n, 1), &pe)) return s;
+        return column_grid_fill(ctx, v, pm, (int32_t*)pe, g);
+    }
 
     int prepare() {
         defer = o.defer_exact != 0;
@@ -755,6 +774,10 @@ struct Join {
         objA_ = objA;
         objB_ = objB;
         object_parity = A->contiguous && B->contiguous;
+        if (object_parity && o.predicate != PIERCE_OVERLAP) {
+            if (int s = column_grid(va, SLOT_GRID_A, SLOT_GRID_A_ENTRIES, &gridA_)) return s;
+            if (int s = column_grid(vb, SLOT_GRID_B, SLOT_GRID_B_ENTRIES, &gridB_)) return s;
+        }
         uint8_t* act_a = active;
         uint8_t* act_b = active + std::max(A->num_objects, 1);
         if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
@@ -1165,7 +1188,8 @@ struct Join {
             cudaMemsetAsync(par, 0, pslots * 4, ctx->stream);
             int b = timer.record();
             if (object_parity) {
-                if (int s = launch_parity_objects(ctx, src, swap ? objA_ : objB_, tgt, swap, ptable, par, pslots))
+                if (int s = launch_parity_objects(ctx, src, swap ? objA_ : objB_, tgt, swap ? &gridA_ : &gridB_, swap,
+                                                  ptable, par, pslots))
                     return s;
             } else if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots)) {
                 return s;

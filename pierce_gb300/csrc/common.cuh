@@ -99,6 +99,16 @@ struct RayOpts {
 };
 
 constexpr int kScratchSlots = 32;
+
+// Uniform xy grid over a dataset's object boxes: per cell the objects whose
+// box covers the cell in x and y (parity candidates).
+struct ColumnGrid {
+    int nx = 0, ny = 0;
+    const float* bounds = nullptr;   // lo.x, lo.y, hi.x, hi.y (device)
+    const int32_t* offsets = nullptr; // nx*ny + 1
+    const int32_t* entries = nullptr;
+};
+
 constexpr int kSizingScratchSlot = 21;  // 21 and 22: learned sizing (sizing.cu)
 
 struct BvhShape {
@@ -260,6 +270,7 @@ int sort_u64_keys(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, int64_
 int sort_u64_pairs(pierce_ctx* ctx, uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,
                    int64_t n, int end_bit);
 int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
+int exclusive_scan_i32(pierce_ctx* ctx, const int32_t* in, int32_t* out, int64_t n);
 int unique_u64(pierce_ctx* ctx, const uint64_t* in, uint64_t* out, int64_t n, int64_t* num_unique);
 int select_flagged(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* out, unsigned long long* d_count);
 }  // namespace pgpu

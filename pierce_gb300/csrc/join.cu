@@ -1168,6 +1168,79 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
     return check_cuda(cudaGetLastError(), "parity kernel");
 }
 
+__global__ void k_fill_u32_j(uint32_t* p, uint32_t value, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+// ---- column grid over object boxes ---------------------------------------
+// Parity candidates are the target objects whose box contains the query
+// point in x and y and reaches above it.  A uniform grid over the xy plane
+// lists, per cell, every object whose box covers the cell in x and y, so a
+// query reads one cell's list instead of walking a hierarchy with a column
+// that is unbounded above.  About one object per cell on average.
+
+
+__device__ __forceinline__ void grid_cell_range(const float* b, int nx, int ny, float lo, float hi, int axis,
+                                                int& c0, int& c1) {
+    const float o = b[axis], e = b[2 + axis] - b[axis];
+    const int n = axis ? ny : nx;
+    const float inv = e > 0.0f ? (float)n / e : 0.0f;
+    c0 = min(max((int)floorf((lo - o) * inv), 0), n - 1);
+    c1 = min(max((int)floorf((hi - o) * inv), 0), n - 1);
+}
+
+__global__ void k_grid_bounds(const float* __restrict__ obj_box, int32_t n, uint32_t* ob) {
+    float lo[2] = {3.4e38f, 3.4e38f}, hi[2] = {-3.4e38f, -3.4e38f};
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        const float* b = obj_box + 6 * o;
+        if (!(b[0] <= b[3])) continue;  // object without triangles
+        lo[0] = fminf(lo[0], b[0]); lo[1] = fminf(lo[1], b[1]);
+        hi[0] = fmaxf(hi[0], b[3]); hi[1] = fmaxf(hi[1], b[4]);
+    }
+    for (int k = 0; k < 2; ++k)
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], off));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], off));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t ul = __float_as_uint(lo[k]), uh = __float_as_uint(hi[k]);
+            atomicMin(ob + k, (ul & 0x80000000u) ? ~ul : (ul | 0x80000000u));
+            atomicMax(ob + 2 + k, (uh & 0x80000000u) ? ~uh : (uh | 0x80000000u));
+        }
+}
+
+__global__ void k_grid_decode(const uint32_t* ob, float* b) {
+    const int k = threadIdx.x;
+    if (k < 4) {
+        const uint32_t u = ob[k];
+        float v = __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+        if (!(v == v) || fabsf(v) > 3.0e38f) v = 0.0f;  // no object: empty grid at the origin
+        b[k] = v;
+    }
+}
+
+// MODE 0: count covered cells per cell; MODE 1: write object ids.
+template <int MODE>
+__global__ void k_grid_fill(const float* __restrict__ obj_box, int32_t n, const float* __restrict__ b, int nx, int ny,
+                            int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
+                            int32_t* __restrict__ cursor, int32_t* __restrict__ entries) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        const float* ob = obj_box + 6 * o;
+        if (!(ob[0] <= ob[3])) continue;
+        int x0, x1, y0, y1;
+        grid_cell_range(b, nx, ny, ob[0], ob[3], 0, x0, x1);
+        grid_cell_range(b, nx, ny, ob[1], ob[4], 1, y0, y1);
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const int c = y * nx + x;
+                if (MODE == 0) atomicAdd(counts + c, 1);
+                else entries[offsets[c] + atomicAdd(cursor + c, 1)] = (int32_t)o;
+            }
+    }
+}
+
 // Parity by object pairs: a warp per source object walks the target's
 // object hierarchy with the +Z ray of the object's first vertex (candidate
 // target objects: box contains the point in x, y and reaches above it) and
@@ -1177,6 +1250,7 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
 // can drop triangles far from the other side.
 struct ParityObjParams {
     DevDataset src;   // first vertices, partitions
+    ColumnGrid grid;  // the target's column grid (nx == 0: use the object hierarchy)
     DevDataset objs;  // the target's object hierarchy
     DevDataset tgt;   // the target's triangles (verts, idx, obj_range)
     int swap;
@@ -1256,6 +1330,24 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                     candidate(__float_as_int(a4.w));
             }
         };
+        if (P.grid.nx > 0) {
+            const float* gb = P.grid.bounds;
+            int cx, cx1, cy, cy1;
+            grid_cell_range(gb, P.grid.nx, P.grid.ny, p.x, p.x, 0, cx, cx1);
+            grid_cell_range(gb, P.grid.nx, P.grid.ny, p.y, p.y, 1, cy, cy1);
+            const int c = cy * P.grid.nx + cx;
+            const int32_t e0 = __ldg(P.grid.offsets + c), e1 = __ldg(P.grid.offsets + c + 1);
+            const int32_t part = P.src.obj_part ? __ldg(P.src.obj_part + s) : 0;
+            for (int32_t e = e0; e < e1; ++e) {
+                const int32_t t = __ldg(P.grid.entries + e);
+                if (P.tgt.obj_part && __ldg(P.tgt.obj_part + t) != part) continue;
+                const float* ob = P.tgt.obj_box + 6 * (int64_t)t;
+                if (__ldg(ob) <= p.x && p.x <= __ldg(ob + 3) && __ldg(ob + 1) <= p.y && p.y <= __ldg(ob + 4) &&
+                    __ldg(ob + 5) >= p.z)
+                    candidate(t);
+            }
+            continue;
+        }
         int first, count;
         int node = traversal_start(P.src, P.objs, (int32_t)s, first, count);
         if (node < 0) {
@@ -1304,11 +1396,68 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
     flush_counter(&P.ctr->node_visits, lane == 0 ? n_nodes : 0u);
 }
 
+// Column grid of a dataset's object boxes in `mem` (grid_bytes(n) bytes).
+size_t column_grid_bytes(int32_t n) {
+    const int side = std::max(1, (int)std::ceil(std::sqrt((double)std::max(n, 1))));
+    return 16 + 4 * ((size_t)side * side + 1) * 3 + 256;
+}
+
+// Column grid, first phase: bounds, per-cell counts and offsets in `mem`;
+// *n_entries receives the number of (cell, object) entries.
+int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int64_t* n_entries) {
+    const int32_t n = tgt.num_objects;
+    const int side = std::max(1, (int)std::ceil(std::sqrt((double)std::max(n, 1))));
+    const int cells = side * side;
+    char* q = static_cast<char*>(mem);
+    uint32_t* ob = reinterpret_cast<uint32_t*>(q);
+    float* b = reinterpret_cast<float*>(q);  // decoded in place
+    int32_t* counts = reinterpret_cast<int32_t*>(q + 16);
+    int32_t* offsets = counts + cells + 1;
+    int32_t* cursor = offsets + cells + 1;
+    cudaStream_t st = ctx->stream;
+    k_fill_u32_j<<<1, 32, 0, st>>>(ob, 0xFFFFFFFFu, 2);
+    k_fill_u32_j<<<1, 32, 0, st>>>(ob + 2, 0u, 2);
+    cudaMemsetAsync(counts, 0, 4 * ((size_t)cells + 1), st);
+    cudaMemsetAsync(cursor, 0, 4 * ((size_t)cells + 1), st);
+    if (n > 0) k_grid_bounds<<<grid_cap(ctx, n, 256), 256, 0, st>>>(tgt.obj_box, n, ob);
+    k_grid_decode<<<1, 32, 0, st>>>(ob, b);
+    if (n > 0)
+        k_grid_fill<0><<<grid_cap(ctx, n, 256), 256, 0, st>>>(tgt.obj_box, n, b, side, side, counts, nullptr, nullptr,
+                                                               nullptr);
+    ctx->launches += 5;
+    if (int s = exclusive_scan_i32(ctx, counts, offsets, cells + 1)) return s;
+    return host_value(ctx, offsets + cells, 4, n_entries, "column grid size");
+}
+
+// Second phase: the object ids of every cell into `entries` (n_entries).
+int column_grid_fill(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int32_t* entries, ColumnGrid* g) {
+    const int32_t n = tgt.num_objects;
+    const int side = std::max(1, (int)std::ceil(std::sqrt((double)std::max(n, 1))));
+    const int cells = side * side;
+    char* q = static_cast<char*>(mem);
+    float* b = reinterpret_cast<float*>(q);
+    int32_t* counts = reinterpret_cast<int32_t*>(q + 16);
+    int32_t* offsets = counts + cells + 1;
+    int32_t* cursor = offsets + cells + 1;
+    if (n > 0) {
+        k_grid_fill<1><<<grid_cap(ctx, n, 256), 256, 0, ctx->stream>>>(tgt.obj_box, n, b, side, side, nullptr,
+                                                                       offsets, cursor, entries);
+        ctx->launches += 1;
+    }
+    g->nx = side;
+    g->ny = side;
+    g->bounds = b;
+    g->offsets = offsets;
+    g->entries = entries;
+    return check_cuda(cudaGetLastError(), "column grid");
+}
+
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
-                          int swap, uint64_t* table, uint32_t* parity, uint64_t slots) {
+                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots) {
     if (src.num_objects <= 0 || !tgt.obj_range) return PIERCE_OK;
     ParityObjParams P;
     P.src = src;
+    P.grid = grid ? *grid : ColumnGrid{};
     P.objs = objs;
     P.tgt = tgt;
     P.swap = swap;

@@ -64,6 +64,16 @@ int exclusive_scan_i32_to_i64(pierce_ctx* ctx, const int32_t* in, int64_t* out, 
     return check_cuda(e, "exclusive scan");
 }
 
+int exclusive_scan_i32(pierce_ctx* ctx, const int32_t* in, int32_t* out, int64_t n) {
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, ctx->stream);
+    void* tmp = nullptr;
+    if (int s = scratch(ctx, 0, bytes, &tmp)) return s;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, ctx->stream);
+    ctx->launches += 2;
+    return check_cuda(e, "exclusive scan (int32)");
+}
+
 // Indices i < n with flags[i] != 0, in increasing order, into out; the count
 // stays on the device (*d_count, 64-bit).  Order-preserving, so lists built
 // from it (and the hierarchies built over them) do not depend on scheduling.
