@@ -15,8 +15,10 @@ Printed JSON line (rank 0):
   e2e        – the same metric through the C ABI from pinned host buffers:
                H2D of both datasets, BVH builds, both joins, D2H of the pairs;
   roofline   – the edge-ray traversal kernel against measured HBM bandwidth,
-               with algorithmic bytes per launch
-               28*E_src + 16*F_tgt + 12*V_tgt + 32*(2*F_tgt - 1) + 8*P_raw;
+               with algorithmic bytes over the units the launches process
+               28*E_traced + 16*F_tgt + 12*V_tgt + 32*(2*F_tgt - 1) + 8*P_raw,
+               E_traced the edges that survive culling and F_tgt the
+               triangles of the target's per-join hierarchy;
   cpu_baseline – the CPU oracle (exact Face-style restatement, OpenMP) on a
                spatial sample of the same workload, extrapolated.
 
@@ -126,9 +128,35 @@ def max_over_ranks(value: float, dist) -> float:
 
 
 def edge_ray_bytes(src, tgt, raw_hits):
-    """Algorithmic bytes of one edge-ray launch (src edges vs tgt BVH)."""
+    """Algorithmic bytes of one unculled edge-ray launch (every src edge
+    against a hierarchy over every tgt triangle)."""
     E, F, V = src.num_edges, tgt.num_triangles, tgt.vertices.shape[0]
     return 28 * E + 16 * F + 12 * V + 32 * (2 * F - 1) + 8 * raw_hits
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced edge
+# of k_edge_rays, from one ncu capture of the two launches of the
+# intersection join of the default workload (profiles/
+# k_edge_rays_ellipsoids_50000.md); None until such a capture exists.
+EDGE_RAY_DRAM_BYTES_PER_RAY = None
+
+
+def traffic_estimate(rays):
+    return None if EDGE_RAY_DRAM_BYTES_PER_RAY is None else EDGE_RAY_DRAM_BYTES_PER_RAY * rays
+
+
+def traced_edge_ray_bytes(rays, raw_hits, targets):
+    """Algorithmic bytes of the edge-ray launches of one join over the units
+    they process: each traced edge read once (28 B), a raw hit written once
+    (8 B), and per direction the target's per-join hierarchy over its
+    surviving triangles -- indices and object id (16 B per triangle), the
+    vertices in proportion to the triangles kept (12 B each) and one 32-B
+    node per node of a minimal binary tree.  targets: (dataset, triangles)."""
+    b = 28 * rays + 8 * raw_hits
+    for G, f in targets:
+        v = G.vertices.shape[0] * f / max(G.num_triangles, 1)
+        b += 16 * f + 12 * v + 32 * max(2 * f - 1, 0)
+    return b
 
 
 def cpu_sample(A_full, B_full, target_objects: int, seed: int = 7):
@@ -569,9 +597,10 @@ def main():
     ri, rc = collected[-1]
     edge_ms = ri.stats["ms_edge_rays"][0] + ri.stats["ms_edge_rays"][1]
     raw_hits = ri.stats["raw_hits"]
-    bytes_ab = edge_ray_bytes(A, B, raw_hits / 2)
-    bytes_ba = edge_ray_bytes(B, A, raw_hits / 2)
-    achieved = (bytes_ab + bytes_ba) / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else 0.0
+    act = ri.stats["active_triangles"]
+    traced_bytes = traced_edge_ray_bytes(ri.stats["rays"], raw_hits, [(B, act[1]), (A, act[0])])
+    achieved = traced_bytes / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else 0.0
+    unculled_bytes = edge_ray_bytes(A, B, raw_hits / 2) + edge_ray_bytes(B, A, raw_hits / 2)
     peak, peak_kind = peaks()
     tri_tests = ri.stats["tri_tests"] + rc.stats["tri_tests"]
     join_ms = ri.stats["ms_total"] + rc.stats["ms_total"]
@@ -703,8 +732,10 @@ def main():
                        "unit": UNIT, "note": "BVH builds excluded, as in the reference benchmark adapters"},
         "active_triangles": list(ri.stats["active_triangles"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
-                     "kernel": "k_edge_rays (exact, hash mode)", "peak_kind": peak_kind},
+                     "frac": achieved / peak if peak else None, "traffic": traffic_estimate(ri.stats["rays"]),
+                     "kernel": "k_edge_rays (exact, hash mode), both directions of the intersection join",
+                     "peak_kind": peak_kind, "algorithmic_bytes": traced_bytes,
+                     "unculled_equivalent_gbs": unculled_bytes / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else None},
         "plain": plain, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
     }
     print(json.dumps(line))

@@ -156,7 +156,8 @@ typedef struct pierce_join_opts {
     /* tuning (0: default); pierce_autotune_join picks them */
     int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets') */
     int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
-    int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 32) */
+    int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 8 for culled
+                                     rays, 32 otherwise) */
     int32_t traversal;            /* culled rays: 0 one ray per thread, 1 a warp traverses its 32 rays together */
 } pierce_join_opts;
 

@@ -122,6 +122,33 @@ int device_alloc(void** p, size_t bytes, const char* what) {
     return PIERCE_OK;
 }
 
+int dataset_array(pierce_ctx* ctx, void** p, size_t bytes, cudaStream_t stream, const char* what) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
+    if (e == cudaErrorMemoryAllocation) {
+        // memory other datasets returned to the pool goes back to the device first
+        cudaGetLastError();
+        cudaStreamSynchronize(stream);
+        cudaMemPoolTrimTo(ctx->pool, 0);
+        e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_error(e == cudaErrorMemoryAllocation ? PIERCE_ERR_OUT_OF_MEMORY : PIERCE_ERR_CUDA,
+                         std::string("device allocation (") + std::to_string(bytes) + ") for " + what + ": " +
+                             cudaGetErrorString(e));
+    }
+    return PIERCE_OK;
+}
+
+// Only called with the device idle (pierce_dataset_destroy synchronises
+// first), so the legacy stream orders nothing that still runs.
+void dataset_free(void* p) {
+    if (p) cudaFreeAsync(p, 0);
+}
+
 int host_value(pierce_ctx* ctx, const void* dptr, int bytes, int64_t* out, const char* what) {
     GraphPlan* g = ctx->plan;
     if (g && g->mode == 2) {
@@ -178,7 +205,13 @@ int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
             ctx->scratch_bytes[slot] = 0;
         }
         size_t want = bytes + bytes / 8;  // headroom against repeated growth
-        if (int s = device_alloc(&ctx->scratch[slot], want, "scratch")) return s;
+        if (device_alloc(&ctx->scratch[slot], want, "scratch") != PIERCE_OK && ctx->pool) {
+            // arrays of destroyed datasets still held by the pool go back first
+            cudaDeviceSynchronize();
+            cudaMemPoolTrimTo(ctx->pool, 0);
+            if (int s = device_alloc(&ctx->scratch[slot], want, "scratch")) return s;
+        }
+        if (!ctx->scratch[slot]) return PIERCE_ERR_OUT_OF_MEMORY;
         ctx->scratch_bytes[slot] = want;
     }
     *out = ctx->scratch[slot];
@@ -188,6 +221,58 @@ int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
 }  // namespace pgpu
 
 // ---------------------------------------------------------------- kernels --
+
+// Edge upload: a warp per 32-edge chunk packs its edges (start + source
+// object bits, end), copies the source ids, writes the chunk's box (the
+// values k_chunk_boxes computes) and clears *grouped when a source id
+// decreases.  The inputs may be host memory the device reads directly
+// (pinned, or any host memory where the device has pageable memory access),
+// so the transfer and the packing are one pass.
+__global__ void __launch_bounds__(256) k_upload_edges(const float* s, const float* e, const int32_t* src, int64_t n,
+                                                      float4* __restrict__ out, int32_t* __restrict__ src_out,
+                                                      float* __restrict__ chunk_box, int32_t* __restrict__ grouped) {
+    const int lane = threadIdx.x & 31;
+    const int64_t chunks = (n + 31) / 32;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+        const int64_t i = c * 32 + lane;
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        int32_t o = 0;
+        if (i < n) {
+            const float sx = s[3 * i], sy = s[3 * i + 1], sz = s[3 * i + 2];
+            const float ex = e[3 * i], ey = e[3 * i + 1], ez = e[3 * i + 2];
+            o = src[i];
+            out[2 * i] = make_float4(sx, sy, sz, __int_as_float(o));
+            out[2 * i + 1] = make_float4(ex, ey, ez, 0.0f);
+            src_out[i] = o;
+            lo[0] = fminf(sx, ex); lo[1] = fminf(sy, ey); lo[2] = fminf(sz, ez);
+            hi[0] = fmaxf(sx, ex); hi[1] = fmaxf(sy, ey); hi[2] = fmaxf(sz, ez);
+        }
+        int32_t next = __shfl_down_sync(0xFFFFFFFFu, o, 1);
+        if (lane == 31 && i + 1 < n) next = src[i + 1];
+        if (i + 1 < n && next < o) atomicAnd(grouped, 0);
+        for (int k = 0; k < 3; ++k)
+            for (int off = 16; off > 0; off >>= 1) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], off));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], off));
+            }
+        if (lane < 6) chunk_box[6 * c + lane] = lane < 3 ? lo[lane] : hi[lane - 3];
+    }
+}
+
+// A pointer the device can read for host array `h`: the device alias of
+// pinned (registered) memory, device memory itself, or -- where the device
+// has pageable memory access -- the host pointer; nullptr otherwise.
+static const void* device_readable(const pierce_ctx* ctx, const void* h) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return h;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    return ctx->pageable_access ? h : nullptr;
+}
 
 __global__ void k_pack_edges(const float* __restrict__ s, const float* __restrict__ e, const int32_t* __restrict__ src,
                              int64_t n, float4* __restrict__ out) {
@@ -266,26 +351,33 @@ struct EventTimer {
 
 namespace pgpu {
 
-int dataset_alloc(pierce_dataset* ds) {
+int dataset_alloc(pierce_dataset* ds, cudaStream_t stream) {
     const int32_t nobj = ds->num_objects;
     const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
-    if (int s = device_alloc((void**)&ds->d_vertices, vb, "vertices")) return s;
-    if (int s = device_alloc((void**)&ds->d_indices, ib, "indices")) return s;
-    if (int s = device_alloc((void**)&ds->d_tri_to_object, ob, "triangle to object")) return s;
-    if (int s = device_alloc((void**)&ds->d_edges, 32 * ds->ne, "edges")) return s;
-    if (int s = device_alloc((void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), "edge sources")) return s;
-    if (int s = device_alloc((void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), "first vertices")) return s;
-    if (int s = device_alloc((void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), "object boxes")) return s;
-    if (int s = device_alloc((void**)&ds->d_obj_range, 8 * (size_t)std::max(nobj, 1), "object ranges")) return s;
+    pierce_ctx* c = ds->ctx;
+    if (int s = dataset_array(c, (void**)&ds->d_vertices, vb, stream, "vertices")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_indices, ib, stream, "indices")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_tri_to_object, ob, stream, "triangle to object")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_edges, 32 * ds->ne, stream, "edges")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_edge_src, 4 * std::max<uint64_t>(ds->ne, 1), stream, "edge sources"))
+        return s;
+    if (int s = dataset_array(c, (void**)&ds->d_first_vertex, 16 * (size_t)std::max(nobj, 1), stream,
+                              "first vertices"))
+        return s;
+    if (int s = dataset_array(c, (void**)&ds->d_obj_box, 24 * (size_t)std::max(nobj, 1), stream, "object boxes"))
+        return s;
+    if (int s = dataset_array(c, (void**)&ds->d_obj_range, 8 * (size_t)std::max(nobj, 1), stream, "object ranges"))
+        return s;
     const size_t tcb = 24 * ((ds->nt + 31) / 32 + 1), ecb = 24 * ((ds->ne + 31) / 32 + 1);
-    if (int s = device_alloc((void**)&ds->d_tri_chunk_box, tcb, "triangle chunk boxes")) return s;
-    if (int s = device_alloc((void**)&ds->d_edge_chunk_box, ecb, "edge chunk boxes")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_tri_chunk_box, tcb, stream, "triangle chunk boxes")) return s;
+    if (int s = dataset_array(c, (void**)&ds->d_edge_chunk_box, ecb, stream, "edge chunk boxes")) return s;
     ds->device_bytes = vb + ib + ob + 36 * ds->ne + 48 * (size_t)nobj + tcb + ecb;
     return PIERCE_OK;
 }
 
-int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning) {
-    if (int s = prepare_objects(ctx, ds)) return s;
+int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning, cudaEvent_t edges_ready,
+                   const int32_t* grouped_flag) {
+    if (int s = prepare_objects(ctx, ds, edges_ready, grouped_flag)) return s;
     pierce_tuning t;
     pierce_default_tuning(&t);
     if (tuning) t = *tuning;
@@ -365,6 +457,26 @@ int pierce_ctx_create(int device, pierce_ctx** out) {
     if (!st) st = check_cuda(cudaMallocHost((void**)&ctx->h_counters, sizeof(DevCounters)), "pinned");
     if (!st) st = check_cuda(cudaMallocHost((void**)&ctx->h_small, 8 * sizeof(int64_t)), "pinned");
     if (!st) st = check_cuda(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
+    if (!st) st = check_cuda(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "stream create");
+    if (!st) st = check_cuda(cudaEventCreateWithFlags(&ctx->ev_tris, cudaEventDisableTiming), "event create");
+    if (!st) st = check_cuda(cudaEventCreateWithFlags(&ctx->ev_edges, cudaEventDisableTiming), "event create");
+    if (!st) st = device_alloc((void**)&ctx->d_upload_flag, 16, "upload flag");
+    if (!st) {
+        if (cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->pageable_access = 0;
+        }
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        st = check_cuda(cudaMemPoolCreate(&ctx->pool, &props), "memory pool");
+        if (!st) {
+            uint64_t keep = ~0ull;
+            st = check_cuda(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool");
+        }
+    }
     if (!st) st = check_cuda(cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream), "memset");
     if (!st) st = sync_ctx(ctx, "ctx init");
     if (st) {
@@ -379,8 +491,16 @@ void pierce_ctx_destroy(pierce_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     for (int i = 0; i < kScratchSlots; ++i)
         if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+    if (ctx->d_upload_flag) cudaFree(ctx->d_upload_flag);
+    if (ctx->ev_tris) cudaEventDestroy(ctx->ev_tris);
+    if (ctx->ev_edges) cudaEventDestroy(ctx->ev_edges);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    // arrays of datasets that outlive the context stay valid; the pool's
+    // memory is released once they are freed
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -408,6 +528,8 @@ int pierce_ctx_release_scratch(pierce_ctx* ctx) {
         ctx->scratch[i] = nullptr;
         ctx->scratch_bytes[i] = 0;
     }
+    // and the arrays of destroyed datasets that the pool still holds
+    if (ctx->pool) cudaMemPoolTrimTo(ctx->pool, 0);
     return PIERCE_OK;
 }
 
@@ -432,8 +554,9 @@ void pierce_dataset_destroy(pierce_dataset* ds) {
     void* ptrs[] = {ds->d_vertices, ds->d_indices,  ds->d_tri_to_object, ds->d_edges,  ds->d_edge_src,
                     ds->d_soup,     ds->d_nodes,    ds->d_first_vertex,  ds->d_obj_box, ds->d_obj_part,
                     ds->d_part_roots, ds->d_obj_range, ds->d_tri_chunk_box, ds->d_edge_chunk_box};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+    for (void* p : ptrs) dataset_free(p);
+    // the frees complete now, so the next dataset of the context reuses the memory
+    cudaStreamSynchronize(0);
     delete ds;
 }
 
@@ -447,8 +570,9 @@ int pierce_dataset_set_partitions(pierce_ctx* ctx, pierce_dataset* ds, const int
             return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_set_partitions: partition id out of range");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    if (ds->d_obj_part) cudaFree(ds->d_obj_part);
-    if (ds->d_part_roots) cudaFree(ds->d_part_roots);
+    cudaDeviceSynchronize();  // dataset_free needs an idle device
+    dataset_free(ds->d_obj_part);
+    dataset_free(ds->d_part_roots);
     ds->d_obj_part = nullptr;
     ds->d_part_roots = nullptr;
     ds->num_parts = 0;
@@ -456,8 +580,10 @@ int pierce_dataset_set_partitions(pierce_ctx* ctx, pierce_dataset* ds, const int
     ds->built = 0;
     if (num_parts > 0) {
         const size_t nobj = (size_t)std::max(ds->num_objects, 1);
-        if (int s = device_alloc((void**)&ds->d_obj_part, 4 * nobj, "object partitions")) return s;
-        if (int s = device_alloc((void**)&ds->d_part_roots, 8 * (size_t)num_parts, "partition roots")) return s;
+        if (int s = dataset_array(ctx, (void**)&ds->d_obj_part, 4 * nobj, ctx->stream, "object partitions")) return s;
+        if (int s = dataset_array(ctx, (void**)&ds->d_part_roots, 8 * (size_t)num_parts, ctx->stream,
+                                  "partition roots"))
+            return s;
         if (ds->num_objects > 0)
             if (int s = check_cuda(cudaMemcpyAsync(ds->d_obj_part, obj_part, 4 * (size_t)ds->num_objects,
                                                    cudaMemcpyHostToDevice, ctx->stream),
@@ -518,7 +644,51 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
             }
         }
         ds->num_objects = nobj;
-        if ((s = dataset_alloc(ds))) break;
+        // Pipelined upload when the device reads the edge arrays in place:
+        // the triangle-side copies, then the edge upload kernel, run on the
+        // copy stream; the object preparation of the triangles starts on the
+        // context stream as soon as they have arrived (ev_tris) and overlaps
+        // the edge transfer.  Otherwise everything runs on the context stream
+        // through staging buffers.
+        const void* es = nullptr;
+        const void* ee = nullptr;
+        const void* esrc = nullptr;
+        if (ds->ne) {
+            es = device_readable(ctx, v->edge_starts);
+            ee = device_readable(ctx, v->edge_ends);
+            esrc = device_readable(ctx, v->edge_src);
+        }
+        const bool direct = ds->ne == 0 || (es && ee && esrc);
+        if (direct) {
+            cudaStream_t cs = ctx->copy_stream;
+            if ((s = dataset_alloc(ds, cs))) break;
+            const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
+            if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, cs), "copy vertices")))
+                break;
+            if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, cs), "copy indices")))
+                break;
+            if (ob &&
+                (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, cs), "copy t2o")))
+                break;
+            if ((s = check_cuda(cudaEventRecord(ctx->ev_tris, cs), "upload event"))) break;
+            if ((s = check_cuda(cudaMemsetAsync(ctx->d_upload_flag, 1, sizeof(int32_t), cs), "upload flag"))) break;
+            if (ds->ne) {
+                const int64_t chunks = (int64_t)((ds->ne + 31) / 32);
+                const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((chunks + 7) / 8, ctx->sm_count * 4));
+                k_upload_edges<<<blocks, 256, 0, cs>>>((const float*)es, (const float*)ee, (const int32_t*)esrc,
+                                                       (int64_t)ds->ne, ds->d_edges, ds->d_edge_src,
+                                                       ds->d_edge_chunk_box, ctx->d_upload_flag);
+                ctx->launches += 1;
+                if ((s = check_cuda(cudaGetLastError(), "upload edges"))) break;
+            }
+            if ((s = check_cuda(cudaEventRecord(ctx->ev_edges, cs), "upload event"))) break;
+            if ((s = check_cuda(cudaStreamWaitEvent(st, ctx->ev_tris, 0), "upload wait"))) break;
+            s = dataset_finish(ctx, ds, tuning, ctx->ev_edges, ctx->d_upload_flag);
+            // the caller's arrays are free to change once this returns
+            if (int s2 = check_cuda(cudaStreamSynchronize(cs), "dataset upload")) s = s ? s : s2;
+            break;
+        }
+        if ((s = dataset_alloc(ds, st))) break;
         const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
         if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, st), "copy vertices"))) break;
         if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, st), "copy indices"))) break;
@@ -1515,7 +1685,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     std::memset(&cur, 0, sizeof(cur));
     cur.leaf_size = o.leaf_size > 0 ? o.leaf_size : std::max(a->leaf_size, 1);
     cur.rays_per_warp = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
-    cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 32;
+    cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 8;
     cur.hash_load_factor = o.hash_load_factor;
     cur.traversal = o.traversal;
     cur.ms = 1e300;

@@ -155,6 +155,18 @@ struct pierce_ctx {
     uint64_t launches = 0;
     int sm_count = 0;
     pgpu::GraphPlan* plan = nullptr;  // set while a join graph is planned or captured
+    // dataset uploads: copies and the edge upload kernel run on copy_stream,
+    // so the object preparation of the triangles (on stream) overlaps the
+    // transfer of the edges
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_tris = nullptr, ev_edges = nullptr;
+    int32_t* d_upload_flag = nullptr;  // edges grouped by source object (nonzero) after an upload
+    int pageable_access = 0;           // kernels may read pageable host memory
+    // Dataset arrays come from this stream-ordered pool; freed arrays stay
+    // in it (release threshold: never), so datasets created and destroyed
+    // per query skip the driver's mapping work.  pierce_ctx_release_scratch
+    // trims it.
+    cudaMemPool_t pool = nullptr;
 };
 
 struct pierce_dataset {
@@ -231,6 +243,10 @@ int check_cuda(cudaError_t e, const char* what);
 // grow-only scratch buffer `slot` of at least `bytes`
 int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out);
 int device_alloc(void** p, size_t bytes, const char* what);
+// dataset arrays: from the context's pool, in order on `stream`; freed by
+// dataset_free (after the device is idle)
+int dataset_array(pierce_ctx* ctx, void** p, size_t bytes, cudaStream_t stream, const char* what);
+void dataset_free(void* p);
 // A value the host reads from device memory (4 or 8 bytes, 4 sign-extended):
 // synchronous, except while a join graph is captured (then from the plan).
 int host_value(pierce_ctx* ctx, const void* dptr, int bytes, int64_t* out, const char* what);
@@ -238,9 +254,10 @@ inline bool capturing(const pierce_ctx* ctx) { return ctx->plan && ctx->plan->mo
 // Device memory of a join result (owned by the join graph while one is planned).
 int result_alloc(pierce_ctx* ctx, void** p, size_t bytes);
 // allocate a dataset's arrays for ds->nv/nt/ne/num_objects (capi.cu)
-int dataset_alloc(pierce_dataset* ds);
+int dataset_alloc(pierce_dataset* ds, cudaStream_t stream);
 // object data, then the BVH unless tuning->defer_build (capi.cu)
-int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning);
+int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tuning,
+                   cudaEvent_t edges_ready = nullptr, const int32_t* grouped_flag = nullptr);
 
 // sizing.cu: join features into d_out[32] (device), and the network's
 // log1p(pairs) prediction for a join (synchronous)
@@ -256,7 +273,11 @@ int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size);
 int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, const uint32_t* list,
                int64_t n, int leaf_size, float4* soup, Node* nodes, BvhShape* shape, float* root_box,
                const int32_t* obj_part = nullptr, int32_t num_parts = 0, int2* part_roots = nullptr);
-int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds);
+// Chunk boxes, object boxes, ranges and flags.  With edges_ready (the edge
+// upload kernel already wrote the edge chunk boxes and the edge-order flag
+// *grouped_flag), the edge-side work waits for ev_edges instead.
+int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready = nullptr,
+                    const int32_t* grouped_flag = nullptr);
 // hierarchy over groups of G consecutive triangles (G divides 32) of the
 // listed 32-triangle chunks; group_scratch holds 88 bytes per group
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,

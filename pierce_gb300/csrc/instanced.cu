@@ -168,7 +168,7 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
     void *d_blob = nullptr, *d_inst = nullptr, *d_off = nullptr;
     int s = PIERCE_OK;
     do {
-        if ((s = dataset_alloc(ds))) break;
+        if ((s = dataset_alloc(ds, st))) break;
         if ((s = device_alloc(&d_blob, blob.size(), "instance templates"))) break;
         if ((s = device_alloc(&d_inst, sizeof(pierce_mesh_instance) * std::max(num_meshes, 1), "instances"))) break;
         if ((s = device_alloc(&d_off, 8 * off.size(), "instance offsets"))) break;

@@ -37,7 +37,13 @@ namespace pgpu {
 enum RayMode { MODE_COUNT = 0, MODE_WRITE = 1, MODE_HASH = 2 };
 enum Precision { PREC_EXACT = 0, PREC_FP32 = 1, PREC_DEFER = 2 };
 
-constexpr int kShortStack = 32;  // stack entries kept in shared memory per thread
+constexpr int kShortStack = 32;  // stack entries kept in shared memory per thread (at most)
+// default for culled edge rays against a per-join hierarchy: 8 entries
+// (4 KB per block) leave more of the SM's shared memory / L1 to cache the
+// hierarchy; deeper entries spill to local memory (2 % faster than 32 on the
+// 2 x 50k ellipsoid join).  Unculled rays through a whole dataset's deeper
+// hierarchy keep 32.
+constexpr int kCulledShortStack = 8;
 
 __device__ __forceinline__ uint64_t fmix64(uint64_t k) {
     k ^= k >> 33;
@@ -813,7 +819,8 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.amb_count = ro ? ro->amb_count : nullptr;
     P.amb_cap = ro ? ro->amb_cap : 0;
     P.rays_per_fetch = (ro && ro->rays_per_fetch > 0) ? ro->rays_per_fetch : 32;
-    P.short_stack = (ro && ro->short_stack >= 0) ? std::min(ro->short_stack, kShortStack) : kShortStack;
+    P.short_stack = (ro && ro->short_stack >= 0) ? std::min(ro->short_stack, kShortStack)
+                                                  : (P.ray_list ? kCulledShortStack : kShortStack);
     P.packets = (ro && ro->packets && ro->list) ? 1 : 0;
     if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");

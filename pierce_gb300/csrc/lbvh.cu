@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(256) k_chunk_boxes(const float* __restrict__ v
     }
 }
 
-int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
+int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready, const int32_t* grouped_flag) {
     const int32_t nobj = ds->num_objects;
     {
         cudaStream_t st = ctx->stream;
@@ -680,12 +680,17 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
         if (tc > 0 && ds->d_tri_chunk_box)
             k_chunk_boxes<false><<<grid_for(ctx, 32 * tc, 256), 256, 0, st>>>(ds->d_vertices, ds->d_indices, nullptr,
                                                                               (int64_t)ds->nt, ds->d_tri_chunk_box);
-        if (ec > 0 && ds->d_edge_chunk_box)
+        ctx->launches += (tc > 0);
+        if (!edges_ready && ec > 0 && ds->d_edge_chunk_box) {
             k_chunk_boxes<true><<<grid_for(ctx, 32 * ec, 256), 256, 0, st>>>(nullptr, nullptr, ds->d_edges,
                                                                              (int64_t)ds->ne, ds->d_edge_chunk_box);
-        ctx->launches += (tc > 0) + (ec > 0);
+            ctx->launches += 1;
+        }
     }
-    if (nobj <= 0) return PIERCE_OK;
+    if (nobj <= 0) {
+        if (edges_ready) return check_cuda(cudaStreamWaitEvent(ctx->stream, edges_ready, 0), "upload wait");
+        return PIERCE_OK;
+    }
     void* p = nullptr;
     // first triangle, count, last triangle per object, then the contiguity flag
     if (int s = scratch(ctx, 1, sizeof(int32_t) * (3 * (size_t)nobj + 4), &p)) return s;
@@ -699,7 +704,7 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
     cudaMemsetAsync(count, 0, sizeof(int32_t) * (size_t)nobj, st);
     k_fill_u32<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(last), 0xFFFFFFFFu, nobj);
     k_fill_u32<<<1, 32, 0, st>>>(reinterpret_cast<uint32_t*>(flag), 1u, 2);
-    if (ds->ne > 1) {
+    if (ds->ne > 1 && !grouped_flag) {
         k_edges_grouped<<<grid_for(ctx, (int64_t)ds->ne, 256), 256, 0, st>>>(ds->d_edge_src, (int64_t)ds->ne, flag + 1);
         ctx->launches += 1;
     }
@@ -716,9 +721,12 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds) {
                                                             ds->d_obj_range, flag);
     ctx->launches += 6 + (ds->nt > 0 ? 2 : 0);
     if (int s = check_cuda(cudaGetLastError(), "prepare_objects")) return s;
+    // the edge side (uploaded on the copy stream) must have arrived
+    if (edges_ready)
+        if (int s = check_cuda(cudaStreamWaitEvent(st, edges_ready, 0), "upload wait")) return s;
     int64_t contiguous = 0, grouped = 0;
     if (int s = host_value(ctx, flag, 4, &contiguous, "object ranges")) return s;
-    if (int s = host_value(ctx, flag + 1, 4, &grouped, "edge order")) return s;
+    if (int s = host_value(ctx, grouped_flag ? grouped_flag : flag + 1, 4, &grouped, "edge order")) return s;
     ds->contiguous = contiguous != 0;
     ds->edges_grouped = grouped != 0;
     return PIERCE_OK;
@@ -982,11 +990,14 @@ int build_bvh(pierce_ctx* ctx, pierce_dataset* ds, int leaf_size) {
     // The soup and node arrays exist only for datasets that get a hierarchy
     // of their own (joins with per-join hierarchies never need them).
     if (!ds->d_soup) {
-        if (int s = device_alloc((void**)&ds->d_soup, 48 * std::max<uint64_t>(ds->nt, 1), "triangle soup")) return s;
+        if (int s = dataset_array(ctx, (void**)&ds->d_soup, 48 * std::max<uint64_t>(ds->nt, 1), ctx->stream,
+                                  "triangle soup"))
+            return s;
         ds->device_bytes += 48 * ds->nt;
     }
     if (!ds->d_nodes) {
-        if (int s = device_alloc((void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), "bvh nodes"))
+        if (int s = dataset_array(ctx, (void**)&ds->d_nodes, sizeof(Node) * std::max<uint64_t>(ds->nt, 1), ctx->stream,
+                                  "bvh nodes"))
             return s;
         ds->device_bytes += sizeof(Node) * ds->nt;
     }
