@@ -158,7 +158,9 @@ typedef struct pierce_join_opts {
     int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
     int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 8 for culled
                                      rays, 32 otherwise) */
-    int32_t traversal;            /* culled rays: 0 one ray per thread, 1 a warp traverses its 32 rays together */
+    int32_t traversal;            /* culled rays: 0 one ray per thread over four-wide copies of the per-join
+                                     hierarchies, 1 a warp traverses its 32 rays together, 2 one ray per thread
+                                     over the binary nodes */
 } pierce_join_opts;
 
 typedef struct pierce_stats {

@@ -91,6 +91,8 @@ enum : int {
     SLOT_GRID_A_ENTRIES = 27,
     SLOT_GRID_B = 28,
     SLOT_GRID_B_ENTRIES = 29,
+    SLOT_NODES4_A = 30,  // four-wide copies of the per-join hierarchies
+    SLOT_NODES4_B = 31,
 };
 }  // namespace
 
@@ -225,9 +227,8 @@ int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
 // Edge upload: a warp per 32-edge chunk packs its edges (start + source
 // object bits, end), copies the source ids, writes the chunk's box (the
 // values k_chunk_boxes computes) and clears *grouped when a source id
-// decreases.  The inputs may be host memory the device reads directly
-// (pinned, or any host memory where the device has pageable memory access),
-// so the transfer and the packing are one pass.
+// decreases.  The inputs may be pinned host memory the device reads in
+// place, so the transfer and the packing are one pass.
 __global__ void __launch_bounds__(256) k_upload_edges(const float* s, const float* e, const int32_t* src, int64_t n,
                                                       float4* __restrict__ out, int32_t* __restrict__ src_out,
                                                       float* __restrict__ chunk_box, int32_t* __restrict__ grouped) {
@@ -260,10 +261,11 @@ __global__ void __launch_bounds__(256) k_upload_edges(const float* s, const floa
     }
 }
 
-// A pointer the device can read for host array `h`: the device alias of
-// pinned (registered) memory, device memory itself, or -- where the device
-// has pageable memory access -- the host pointer; nullptr otherwise.
-static const void* device_readable(const pierce_ctx* ctx, const void* h) {
+// A pointer the device can read for array `h`: the device alias of pinned
+// (registered) host memory, or device memory itself; nullptr for pageable
+// host memory, which goes through the copy engines (they read it at the
+// link's full rate).
+static const void* device_readable(const void* h) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
         cudaGetLastError();
@@ -271,7 +273,7 @@ static const void* device_readable(const pierce_ctx* ctx, const void* h) {
     }
     if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return h;
     if (a.type == cudaMemoryTypeHost) return a.devicePointer;
-    return ctx->pageable_access ? h : nullptr;
+    return nullptr;
 }
 
 __global__ void k_pack_edges(const float* __restrict__ s, const float* __restrict__ e, const int32_t* __restrict__ src,
@@ -462,10 +464,6 @@ int pierce_ctx_create(int device, pierce_ctx** out) {
     if (!st) st = check_cuda(cudaEventCreateWithFlags(&ctx->ev_edges, cudaEventDisableTiming), "event create");
     if (!st) st = device_alloc((void**)&ctx->d_upload_flag, 16, "upload flag");
     if (!st) {
-        if (cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
-            cudaGetLastError();
-            ctx->pageable_access = 0;
-        }
         cudaMemPoolProps props;
         std::memset(&props, 0, sizeof(props));
         props.allocType = cudaMemAllocationTypePinned;
@@ -644,7 +642,8 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
             }
         }
         ds->num_objects = nobj;
-        // Pipelined upload when the device reads the edge arrays in place:
+        // Pipelined upload when the device reads the edge arrays in place
+        // (pinned host memory or device memory):
         // the triangle-side copies, then the edge upload kernel, run on the
         // copy stream; the object preparation of the triangles starts on the
         // context stream as soon as they have arrived (ev_tris) and overlaps
@@ -654,9 +653,9 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
         const void* ee = nullptr;
         const void* esrc = nullptr;
         if (ds->ne) {
-            es = device_readable(ctx, v->edge_starts);
-            ee = device_readable(ctx, v->edge_ends);
-            esrc = device_readable(ctx, v->edge_src);
+            es = device_readable(v->edge_starts);
+            ee = device_readable(v->edge_ends);
+            esrc = device_readable(v->edge_src);
         }
         const bool direct = ds->ne == 0 || (es && ee && esrc);
         if (direct) {
@@ -1091,9 +1090,24 @@ struct Join {
         vb.num_tris = nb;
         vb.root_is_leaf = shB.root_is_leaf;
         vb.root_leaf_count = shB.root_leaf_count;
+        if (int s = wide_nodes(va, shA.num_nodes, SLOT_NODES4_A)) return s;
+        if (int s = wide_nodes(vb, shB.num_nodes, SLOT_NODES4_B)) return s;
         st.active_triangles[0] = (uint64_t)na;
         st.active_triangles[1] = (uint64_t)nb;
         timer.span(b0, timer.record(), &st.ms_build);
+        return PIERCE_OK;
+    }
+
+    // Four-wide copy of a per-join hierarchy for the one-ray-per-thread walk
+    // (traversal 0); the other traversals use the binary nodes.
+    int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot) {
+        v.nodes4 = nullptr;
+        if (o.traversal != 0 || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
+        void* p = nullptr;
+        if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) return s;
+        // Node4 is 128-byte aligned; cudaMalloc returns 256-byte aligned memory
+        if (int s = collapse4(ctx, v.nodes, (int64_t)num_nodes, static_cast<Node4*>(p))) return s;
+        v.nodes4 = static_cast<const Node4*>(p);
         return PIERCE_OK;
     }
 
@@ -1137,6 +1151,7 @@ struct Join {
             v.root_is_leaf = sh.root_is_leaf;
             v.root_leaf_count = sh.root_leaf_count;
             v.part_roots = nullptr;
+            if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A)) return s;
             st.active_triangles[sd] = (uint64_t)(nc[sd] * 32);
         }
         timer.span(b0, timer.record(), &st.ms_build);
@@ -1650,7 +1665,7 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
     if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
-        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 1)
+        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 2)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
     *out_opts = o;
     return PIERCE_OK;

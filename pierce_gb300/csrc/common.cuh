@@ -23,6 +23,8 @@ enum ErrBits : uint32_t {
 
 constexpr uint64_t kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kStackSize = 64;  // >= depth of any LBVH over 30-bit Morton + index keys
+// a Node4 walk pushes at most 3 entries per Node4 level, half as many levels
+constexpr int kStackSize4 = 96;
 
 // Counters accumulated by traversal kernels (one atomicAdd per warp).
 struct DevCounters {
@@ -49,12 +51,25 @@ struct __align__(16) Node {
                  // build link (parent << 2 | side << 1 | arrival toggle)
 };
 
+// Four-wide node collapsed from a binary hierarchy: Node4[n] holds the
+// (up to) four grandchildren of binary internal node n, where a child that
+// is a leaf stands for itself.  Node4 indices are binary node indices, so a
+// traversal entering internal node c reads Node4[c] and skips a level: half
+// the dependent node loads of the binary walk, one 128-byte line each.
+// Unused entries have an empty box (lo > hi).
+struct __align__(128) Node4 {
+    float4 lox, hix, loy, hiy, loz, hiz;  // entry j: (lo.x, hi.x, ...)[j]
+    int4 ch;                              // >= 0 internal node index, < 0 leaf ~first
+    int4 meta;                            // x: leaf counts, 8 bits per entry
+};
+
 // Device view of one dataset (all pointers into its own allocations).
 struct DevDataset {
     // triangle soup in BVH leaf order: per triangle 3 float4:
     //   (v0.xyz, object id bits), (v1.xyz, original triangle index bits), (v2.xyz, 0)
     const float4* soup;
     const Node* nodes;
+    const Node4* nodes4;    // optional four-wide copy of nodes (per-join hierarchies)
     int64_t num_tris;
     int root_is_leaf;       // 1 when the whole dataset is a single leaf
     int root_leaf_count;
@@ -161,7 +176,6 @@ struct pierce_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_tris = nullptr, ev_edges = nullptr;
     int32_t* d_upload_flag = nullptr;  // edges grouped by source object (nonzero) after an upload
-    int pageable_access = 0;           // kernels may read pageable host memory
     // Dataset arrays come from this stream-ordered pool; freed arrays stay
     // in it (release threshold: never), so datasets created and destroyed
     // per query skip the driver's mapping work.  pierce_ctx_release_scratch
@@ -207,6 +221,7 @@ struct pierce_dataset {
         pgpu::DevDataset v;
         v.soup = d_soup;
         v.nodes = d_nodes;
+        v.nodes4 = nullptr;
         v.num_tris = (int64_t)nt;
         v.root_is_leaf = root_is_leaf;
         v.root_leaf_count = root_leaf_count;
@@ -276,6 +291,8 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
 // Chunk boxes, object boxes, ranges and flags.  With edges_ready (the edge
 // upload kernel already wrote the edge chunk boxes and the edge-order flag
 // *grouped_flag), the edge-side work waits for ev_edges instead.
+// Node4 copy of a binary hierarchy with num_nodes internal nodes
+int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out);
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready = nullptr,
                     const int32_t* grouped_flag = nullptr);
 // hierarchy over groups of G consecutive triangles (G divides 32) of the

@@ -232,6 +232,52 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
     int node = traversal_start(P.src, P.tgt, src_obj, leaf_first, leaf_count);
     if (node < 0) {
         if (leaf_count > 0) leaf(leaf_first, leaf_count);
+    } else if (P.tgt.nodes4) {
+        // four-wide walk: a Node4 visit tests the four grandchildren of a
+        // binary node; leaves are tested at once, the first internal hit is
+        // entered and the others pushed
+        int sp = 0;
+        for (;;) {
+            ++rc.nodes;
+            const Node4* nd = P.tgt.nodes4 + node;
+            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+            const int4 ch = __ldg(&nd->ch);
+            const int cnt = __ldg(&nd->meta.x);
+            const bool h[4] = {box_overlap(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, lo, hi),
+                               box_overlap(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, lo, hi),
+                               box_overlap(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, lo, hi),
+                               box_overlap(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, lo, hi)};
+            const int c[4] = {ch.x, ch.y, ch.z, ch.w};
+            int next = -1;
+            bool overflow = false;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (!h[j]) continue;
+                if (c[j] < 0) {
+                    leaf(~c[j], (cnt >> (8 * j)) & 0xFF);
+                } else if (next < 0) {
+                    next = c[j];
+                } else if (sp >= kStackSize4) {
+                    overflow = true;
+                } else {
+                    if (sp < depth) sstack[sp * 128 + tid] = c[j];
+                    else lstack[sp - depth] = c[j];
+                    ++sp;
+                }
+            }
+            if (overflow) {
+                atomicOr(P.err, ERR_STACK_OVERFLOW);
+                break;
+            }
+            if (next >= 0) {
+                node = next;
+            } else {
+                if (sp == 0) break;
+                --sp;
+                node = sp < depth ? sstack[sp * 128 + tid] : lstack[sp - depth];
+            }
+        }
     } else {
         int sp = 0;
         for (;;) {
@@ -418,7 +464,7 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
 template <int MODE, int PREC>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
-    int lstack[kStackSize];
+    int lstack[kStackSize4];
     RayCounters rc;
     PredCounters pc{0, 0};
     uint32_t rays = 0;

@@ -942,6 +942,66 @@ __global__ void k_group_leaves(Node* nodes, int64_t num_nodes, int G) {
     }
 }
 
+// One thread per binary internal node: entries 0-1 come from child 0 and
+// 2-3 from child 1 -- the child's own two children when it is internal, the
+// child itself (and an empty entry) when it is a leaf.
+__device__ __forceinline__ void node4_half(const Node* __restrict__ nodes, const float4& bx, const float4& by,
+                                           const float4& bz, const int4& c, int side, float (&lo)[3][2],
+                                           float (&hi)[3][2], int (&ch)[2], int (&cnt)[2]) {
+    const int r = side ? c.y : c.x;
+    if (r < 0) {
+        lo[0][0] = side ? bx.z : bx.x; hi[0][0] = side ? bx.w : bx.y;
+        lo[1][0] = side ? by.z : by.x; hi[1][0] = side ? by.w : by.y;
+        lo[2][0] = side ? bz.z : bz.x; hi[2][0] = side ? bz.w : bz.y;
+        ch[0] = r;
+        cnt[0] = (c.z >> (8 * side)) & 0xFF;
+        for (int k = 0; k < 3; ++k) {
+            lo[k][1] = 3.4e38f;
+            hi[k][1] = -3.4e38f;
+        }
+        ch[1] = -1;
+        cnt[1] = 0;
+        return;
+    }
+    const float4 gx = __ldg(&nodes[r].bx), gy = __ldg(&nodes[r].by), gz = __ldg(&nodes[r].bz);
+    const int4 gc = __ldg(&nodes[r].ch);
+    lo[0][0] = gx.x; hi[0][0] = gx.y; lo[0][1] = gx.z; hi[0][1] = gx.w;
+    lo[1][0] = gy.x; hi[1][0] = gy.y; lo[1][1] = gy.z; hi[1][1] = gy.w;
+    lo[2][0] = gz.x; hi[2][0] = gz.y; lo[2][1] = gz.z; hi[2][1] = gz.w;
+    ch[0] = gc.x;
+    ch[1] = gc.y;
+    cnt[0] = gc.z & 0xFF;
+    cnt[1] = (gc.z >> 8) & 0xFF;
+}
+
+__global__ void __launch_bounds__(256) k_collapse4(const Node* __restrict__ nodes, int64_t n, Node4* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 bx = __ldg(&nodes[i].bx), by = __ldg(&nodes[i].by), bz = __ldg(&nodes[i].bz);
+        const int4 c = __ldg(&nodes[i].ch);
+        float lo0[3][2], hi0[3][2], lo1[3][2], hi1[3][2];
+        int ch0[2], ch1[2], n0[2], n1[2];
+        node4_half(nodes, bx, by, bz, c, 0, lo0, hi0, ch0, n0);
+        node4_half(nodes, bx, by, bz, c, 1, lo1, hi1, ch1, n1);
+        Node4 q;
+        q.lox = make_float4(lo0[0][0], lo0[0][1], lo1[0][0], lo1[0][1]);
+        q.hix = make_float4(hi0[0][0], hi0[0][1], hi1[0][0], hi1[0][1]);
+        q.loy = make_float4(lo0[1][0], lo0[1][1], lo1[1][0], lo1[1][1]);
+        q.hiy = make_float4(hi0[1][0], hi0[1][1], hi1[1][0], hi1[1][1]);
+        q.loz = make_float4(lo0[2][0], lo0[2][1], lo1[2][0], lo1[2][1]);
+        q.hiz = make_float4(hi0[2][0], hi0[2][1], hi1[2][0], hi1[2][1]);
+        q.ch = make_int4(ch0[0], ch0[1], ch1[0], ch1[1]);
+        q.meta = make_int4(n0[0] | (n0[1] << 8) | (n1[0] << 16) | (n1[1] << 24), 0, 0, 0);
+        out[i] = q;
+    }
+}
+
+int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out) {
+    if (num_nodes <= 0) return PIERCE_OK;
+    k_collapse4<<<grid_for(ctx, num_nodes, 256), 256, 0, ctx->stream>>>(nodes, num_nodes, out);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "collapse to four-wide nodes");
+}
+
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
                        Node* nodes, BvhShape* shape) {

@@ -224,10 +224,26 @@ def test_warp_packets_equal_per_ray_traversal(ctx, case, sizing, predicate):
     name, A, B = case
     da, db = ds(ctx, A, 8), ds(ctx, B, 8)
     r1 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="packets")
-    r2 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="per_ray")
+    r2 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="per_ray_binary")
     assert np.array_equal(r1.pairs, r2.pairs)
     assert r1.stats["raw_hits"] == r2.stats["raw_hits"] and r1.stats["tri_tests"] == r2.stats["tri_tests"]
     assert r1.stats["node_visits"] < r2.stats["node_visits"]
+
+
+@pytest.mark.parametrize("sizing", ["hash", "two_pass"])
+@pytest.mark.parametrize("predicate", ["overlap", "intersection", "containment"])
+def test_four_wide_nodes_equal_binary_walk(ctx, case, sizing, predicate):
+    """One ray per thread over the four-wide copies of the per-join
+    hierarchies against the same walk over the binary nodes: same pairs, and
+    fewer (wider) node visits."""
+    name, A, B = case
+    da, db = ds(ctx, A, 4), ds(ctx, B, 4)
+    r4 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="per_ray")
+    r2 = J.join(ctx, da, db, predicate=predicate, sizing=sizing, traversal="per_ray_binary")
+    assert np.array_equal(r4.pairs, r2.pairs)
+    assert r4.stats["rays"] == r2.stats["rays"]
+    if r2.stats["node_visits"] > 100:
+        assert r4.stats["node_visits"] < 0.75 * r2.stats["node_visits"]
 
 
 def test_config1_full_size_matches_oracle(ctx):
