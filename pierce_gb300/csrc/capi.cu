@@ -93,6 +93,9 @@ enum : int {
     SLOT_GRID_B_ENTRIES = 29,
     SLOT_NODES4_A = 30,  // four-wide copies of the per-join hierarchies
     SLOT_NODES4_B = 31,
+    SLOT_NODES4_OBJ_A = 32,  // ... of the object hierarchies (culling)
+    SLOT_NODES4_OBJ_B = 33,
+    SLOT_NODES4_CHUNKS = 34,  // ... of the hierarchy of A's surviving chunk boxes
 };
 }  // namespace
 
@@ -901,7 +904,7 @@ struct Join {
     }
 
     // BVH of one dataset's object boxes (degenerate triangles lo, hi, hi).
-    int object_bvh(pierce_dataset* ds, int slot, DevDataset* out) {
+    int object_bvh(pierce_dataset* ds, int slot, int slot4, DevDataset* out) {
         const int64_t n = ds->num_objects;
         void* p = nullptr;
         const size_t bytes = 16 * (size_t)std::max<int64_t>(n, 1) + (48 + 64) * (size_t)std::max<int64_t>(n, 1) + 256 +
@@ -927,7 +930,7 @@ struct Join {
         out->root_leaf_count = shape.root_leaf_count;
         out->obj_part = ds->d_obj_part;
         out->part_roots = roots;
-        return PIERCE_OK;
+        return wide_nodes(*out, shape.num_nodes, slot4, true);
     }
 
     // Per-join BVHs over the triangles that can take part in an overlap pair
@@ -938,8 +941,8 @@ struct Join {
     int prepare_active_bvh() {
         const int b0 = timer.record();
         DevDataset objA, objB;
-        if (int s = object_bvh(A, SLOT_OBJ_A, &objA)) return s;
-        if (int s = object_bvh(B, SLOT_OBJ_B, &objB)) return s;
+        if (int s = object_bvh(A, SLOT_OBJ_A, SLOT_NODES4_OBJ_A, &objA)) return s;
+        if (int s = object_bvh(B, SLOT_OBJ_B, SLOT_NODES4_OBJ_B, &objB)) return s;
         objA_ = objA;
         objB_ = objB;
         object_parity = A->contiguous && B->contiguous;
@@ -1019,6 +1022,7 @@ struct Join {
                 cull_b.num_tris = n_act;
                 cull_b.root_is_leaf = shc.root_is_leaf;
                 cull_b.root_leaf_count = shc.root_leaf_count;
+                if (int s = wide_nodes(cull_b, shc.num_nodes, SLOT_NODES4_CHUNKS, true)) return s;
             }
             if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
                                           cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
@@ -1099,10 +1103,11 @@ struct Join {
     }
 
     // Four-wide copy of a per-join hierarchy for the one-ray-per-thread walk
-    // (traversal 0); the other traversals use the binary nodes.
-    int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot) {
+    // (traversal 0; the other traversals use the binary nodes), and of the
+    // culling hierarchies (always).
+    int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot, bool always = false) {
         v.nodes4 = nullptr;
-        if (o.traversal != 0 || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
+        if ((o.traversal != 0 && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
         void* p = nullptr;
         if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) return s;
         // Node4 is 128-byte aligned; cudaMalloc returns 256-byte aligned memory

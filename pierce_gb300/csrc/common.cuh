@@ -113,7 +113,7 @@ struct RayOpts {
     int packets = 1;          // warp-cooperative traversal of the listed rays
 };
 
-constexpr int kScratchSlots = 32;
+constexpr int kScratchSlots = 40;
 
 // Uniform xy grid over a dataset's object boxes: per cell the objects whose
 // box covers the cell in x and y (parity candidates).

@@ -137,6 +137,47 @@ __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float 
     return lx <= hi.x && lo.x <= hx && ly <= hi.y && lo.y <= hy && lz <= hi.z && lo.z <= hz;
 }
 
+// Any-hit box query over a Node4 hierarchy from internal node `node`: true
+// as soon as leaf_hit(first, count) is true for a leaf whose box meets
+// [lo, hi] (and, conservatively, if the stack would overflow).
+template <class LeafHit>
+__device__ __forceinline__ bool any_hit4(const Node4* nodes4, int node, const float3& lo, const float3& hi,
+                                         LeafHit&& leaf_hit) {
+    int stack[kStackSize4];
+    int sp = 0;
+    for (;;) {
+        const Node4* nd = nodes4 + node;
+        const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+        const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+        const int4 ch = __ldg(&nd->ch);
+        const int cnt = __ldg(&nd->meta.x);
+        const bool h[4] = {box_overlap(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, lo, hi),
+                           box_overlap(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, lo, hi),
+                           box_overlap(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, lo, hi),
+                           box_overlap(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, lo, hi)};
+        const int c[4] = {ch.x, ch.y, ch.z, ch.w};
+        int next = -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (!h[j]) continue;
+            if (c[j] < 0) {
+                if (leaf_hit(~c[j], (cnt >> (8 * j)) & 0xFF)) return true;
+            } else if (next < 0) {
+                next = c[j];
+            } else {
+                if (sp >= kStackSize4) return true;
+                stack[sp++] = c[j];
+            }
+        }
+        if (next >= 0) {
+            node = next;
+        } else {
+            if (sp == 0) return false;
+            node = stack[--sp];
+        }
+    }
+}
+
 struct RayCounters {
     uint32_t nodes = 0, tests = 0, hits = 0, inserts = 0, probes = 0;
 };
@@ -167,7 +208,63 @@ __device__ __forceinline__ int traversal_start(const DevDataset& src, const DevD
     return 0;
 }
 
+// The triangles [first, first + count) of a reached leaf against segment
+// (p, q) with box [lo, hi]; hits of one target object in a row are emitted
+// once (last_obj).
 template <int MODE, int PREC>
+__device__ __forceinline__ void leaf_tests(const EdgeRayParams& P, int64_t e, int first, int count, const float3& p,
+                                           const float3& q, const float3& lo, const float3& hi, int32_t src_obj,
+                                           int32_t& last_obj, int& nhit, int64_t& out, RayCounters& rc,
+                                           PredCounters& pc) {
+    for (int k = 0; k < count; ++k) {
+        const int64_t t = (int64_t)first + k;
+        const float4 a4 = __ldg(P.tgt.soup + 3 * t);
+        const int32_t obj = __float_as_int(a4.w);
+        if (obj == last_obj) continue;
+        const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
+        const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
+        if (count > 1) {
+            const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
+            const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
+            const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
+            if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
+        }
+        ++rc.tests;
+        const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
+                     c = make_float3(c4.x, c4.y, c4.z);
+        bool hit;
+        if (PREC == PREC_EXACT) {
+            hit = seg_tri_exact(p, q, a, b, c, pc);
+        } else if (PREC == PREC_FP32) {
+            hit = seg_tri_mt_fp32(p, q, a, b, c);
+        } else {
+            const int cls = seg_tri_fp32_class(p, q, a, b, c);
+            if (cls == SEG_AMBIGUOUS) {
+                ++pc.fp32_ambiguous;
+                if (MODE != MODE_WRITE) {
+                    const unsigned long long slot = atomicAdd(P.amb_count, 1ull);
+                    if (slot < P.amb_cap) P.amb_queue[slot] = ((unsigned long long)e << 32) | (uint32_t)t;
+                    else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
+                }
+                continue;
+            }
+            hit = cls == SEG_HIT;
+        }
+        if (!hit) continue;
+        last_obj = obj;
+        ++nhit;
+        if (MODE == MODE_COUNT) continue;
+        const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
+        if (MODE == MODE_WRITE) {
+            P.keys[out++] = key;
+        } else {
+            ++rc.inserts;
+            hash_insert(P.table, P.mask, key, P.err, rc.probes);
+        }
+    }
+}
+
+template <int MODE, int PREC, bool WIDE = true>
 __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int* sstack, int* lstack,
                                            RayCounters& rc, PredCounters& pc, int depth) {
     const int tid = threadIdx.x;
@@ -181,58 +278,13 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
     int32_t last_obj = -1;
     int nhit = 0;
     auto leaf = [&](int first, int count) {
-        for (int k = 0; k < count; ++k) {
-            const int64_t t = (int64_t)first + k;
-            const float4 a4 = __ldg(P.tgt.soup + 3 * t);
-            const int32_t obj = __float_as_int(a4.w);
-            if (obj == last_obj) continue;
-            const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
-            const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
-            if (count > 1) {
-                const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
-                const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
-                const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
-                if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
-            }
-            ++rc.tests;
-            const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
-                         c = make_float3(c4.x, c4.y, c4.z);
-            bool hit;
-            if (PREC == PREC_EXACT) {
-                hit = seg_tri_exact(p, q, a, b, c, pc);
-            } else if (PREC == PREC_FP32) {
-                hit = seg_tri_mt_fp32(p, q, a, b, c);
-            } else {
-                const int cls = seg_tri_fp32_class(p, q, a, b, c);
-                if (cls == SEG_AMBIGUOUS) {
-                    ++pc.fp32_ambiguous;
-                    if (MODE != MODE_WRITE) {
-                        const unsigned long long slot = atomicAdd(P.amb_count, 1ull);
-                        if (slot < P.amb_cap) P.amb_queue[slot] = ((unsigned long long)e << 32) | (uint32_t)t;
-                        else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
-                    }
-                    continue;
-                }
-                hit = cls == SEG_HIT;
-            }
-            if (!hit) continue;
-            last_obj = obj;
-            ++nhit;
-            if (MODE == MODE_COUNT) continue;
-            const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
-            if (MODE == MODE_WRITE) {
-                P.keys[out++] = key;
-            } else {
-                ++rc.inserts;
-                hash_insert(P.table, P.mask, key, P.err, rc.probes);
-            }
-        }
+        leaf_tests<MODE, PREC>(P, e, first, count, p, q, lo, hi, src_obj, last_obj, nhit, out, rc, pc);
     };
     int leaf_first, leaf_count;
     int node = traversal_start(P.src, P.tgt, src_obj, leaf_first, leaf_count);
     if (node < 0) {
         if (leaf_count > 0) leaf(leaf_first, leaf_count);
-    } else if (P.tgt.nodes4) {
+    } else if (WIDE && P.tgt.nodes4) {
         // four-wide walk: a Node4 visit tests the four grandchildren of a
         // binary node; leaves are tested at once, the first internal hit is
         // entered and the others pushed
@@ -359,52 +411,7 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
     int32_t last_obj = -1;
     int nhit = 0;
     auto leaf = [&](int first, int count) {
-        for (int k = 0; k < count; ++k) {
-            const int64_t t = (int64_t)first + k;
-            const float4 a4 = __ldg(P.tgt.soup + 3 * t);
-            const int32_t obj = __float_as_int(a4.w);
-            if (obj == last_obj) continue;
-            const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
-            const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
-            if (count > 1) {
-                const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
-                const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
-                const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
-                if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
-            }
-            ++rc.tests;
-            const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
-                         c = make_float3(c4.x, c4.y, c4.z);
-            bool hit;
-            if (PREC == PREC_EXACT) {
-                hit = seg_tri_exact(p, q, a, b, c, pc);
-            } else if (PREC == PREC_FP32) {
-                hit = seg_tri_mt_fp32(p, q, a, b, c);
-            } else {
-                const int cls = seg_tri_fp32_class(p, q, a, b, c);
-                if (cls == SEG_AMBIGUOUS) {
-                    ++pc.fp32_ambiguous;
-                    if (MODE != MODE_WRITE) {
-                        const unsigned long long slot = atomicAdd(P.amb_count, 1ull);
-                        if (slot < P.amb_cap) P.amb_queue[slot] = ((unsigned long long)e << 32) | (uint32_t)t;
-                        else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
-                    }
-                    continue;
-                }
-                hit = cls == SEG_HIT;
-            }
-            if (!hit) continue;
-            last_obj = obj;
-            ++nhit;
-            if (MODE == MODE_COUNT) continue;
-            const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
-            if (MODE == MODE_WRITE) {
-                P.keys[out++] = key;
-            } else {
-                ++rc.inserts;
-                hash_insert(P.table, P.mask, key, P.err, rc.probes);
-            }
-        }
+        leaf_tests<MODE, PREC>(P, e, first, count, p, q, lo, hi, src_obj, last_obj, nhit, out, rc, pc);
     };
     if (n0 < 0) {
         if (valid && lc0 > 0) leaf(lf0, lc0);
@@ -461,14 +468,18 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
     }
 }
 
-template <int MODE, int PREC>
+// FORM 1: the culled ray list, one ray per thread (four-wide or binary
+// walk); FORM 2: the culled ray list in warp packets; FORM 0: one thread per
+// edge over a binary hierarchy (the unculled plain form).  Each form is its
+// own kernel, so none carries the registers of another's code.
+template <int MODE, int PREC, int FORM>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
-    int lstack[kStackSize4];
+    int lstack[FORM ? kStackSize4 : kStackSize];
     RayCounters rc;
     PredCounters pc{0, 0};
     uint32_t rays = 0;
-    if (P.ray_list) {
+    if (FORM) {
         // Compacted ray list, persistent blocks: each warp takes the next
         // rays_per_fetch rays from a global cursor (the work queue), so uneven
         // ray costs balance out.
@@ -483,7 +494,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
             if (base >= n) break;
             for (unsigned long long r = lane; r < per; r += 32) {  // per/32 rounds for every lane
                 const unsigned long long i = base + r;
-                if (P.packets) {
+                if (FORM == 2) {
                     const bool has = i < n;
                     trace_packet<MODE, PREC>(P, has ? (int64_t)P.ray_list[i] : -1, wstack, lstack, rc, pc);
                     rays += has ? 1u : 0u;
@@ -496,7 +507,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     } else {
         const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         if (e < P.src.num_edges) {
-            trace_edge<MODE, PREC>(P, e, sstack, lstack, rc, pc, P.short_stack);
+            trace_edge<MODE, PREC, false>(P, e, sstack, lstack, rc, pc, P.short_stack);
             ++rays;
         }
     }
@@ -574,6 +585,11 @@ __global__ void __launch_bounds__(128) k_object_active(DevDataset src, DevDatase
         int node = traversal_start(src, tgt, (int32_t)o, leaf_first, leaf_count);
         if (node < 0) {
             leaf(leaf_first, leaf_count);
+        } else if (tgt.nodes4) {
+            found = any_hit4(tgt.nodes4, node, lo, hi, [&](int first, int count) {
+                leaf(first, count);
+                return found;
+            });
         } else {
             int sp = 0;
             while (!found) {
@@ -885,7 +901,12 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
         g = dim3((unsigned)blocks);
     }
     cudaStream_t st = ctx->stream;
-#define PG_LAUNCH(M, PR) k_edge_rays<M, PR><<<g, B, smem, st>>>(P)
+#define PG_LAUNCH(M, PR)                                    \
+    do {                                                    \
+        if (P.ray_list && P.packets) k_edge_rays<M, PR, 2><<<g, B, smem, st>>>(P); \
+        else if (P.ray_list) k_edge_rays<M, PR, 1><<<g, B, smem, st>>>(P);          \
+        else k_edge_rays<M, PR, 0><<<g, B, smem, st>>>(P);                          \
+    } while (0)
 #define PG_MODES(PR)                                  \
     do {                                              \
         if (mode == MODE_COUNT) PG_LAUNCH(MODE_COUNT, PR); \
@@ -975,6 +996,7 @@ __device__ bool meets_any_object(const DevDataset& objs, int32_t part, const flo
     } else {
         node = 0;
     }
+    if (objs.nodes4) return any_hit4(objs.nodes4, node, lo, hi, leaf_hit);
     int stack[kStackSize];
     int sp = 0;
     for (;;) {

@@ -944,11 +944,26 @@ __global__ void k_group_leaves(Node* nodes, int64_t num_nodes, int G) {
 
 // One thread per binary internal node: entries 0-1 come from child 0 and
 // 2-3 from child 1 -- the child's own two children when it is internal, the
-// child itself (and an empty entry) when it is a leaf.
-__device__ __forceinline__ void node4_half(const Node* __restrict__ nodes, const float4& bx, const float4& by,
-                                           const float4& bz, const int4& c, int side, float (&lo)[3][2],
-                                           float (&hi)[3][2], int (&ch)[2], int (&cnt)[2]) {
+// child itself (and an empty entry) when it is a leaf.  With leaf sizes
+// above one, the internal nodes inside a collapsed leaf are never written by
+// the build and hold stale values: a child index outside [0, n) is not
+// followed (it only occurs in such unreachable nodes, whose Node4 copies are
+// never read).
+__device__ __forceinline__ void node4_half(const Node* __restrict__ nodes, int64_t n, const float4& bx,
+                                           const float4& by, const float4& bz, const int4& c, int side,
+                                           float (&lo)[3][2], float (&hi)[3][2], int (&ch)[2], int (&cnt)[2]) {
     const int r = side ? c.y : c.x;
+    if (r >= 0 && (int64_t)r >= n) {
+        for (int j = 0; j < 2; ++j) {
+            for (int k = 0; k < 3; ++k) {
+                lo[k][j] = 3.4e38f;
+                hi[k][j] = -3.4e38f;
+            }
+            ch[j] = -1;
+            cnt[j] = 0;
+        }
+        return;
+    }
     if (r < 0) {
         lo[0][0] = side ? bx.z : bx.x; hi[0][0] = side ? bx.w : bx.y;
         lo[1][0] = side ? by.z : by.x; hi[1][0] = side ? by.w : by.y;
@@ -980,8 +995,8 @@ __global__ void __launch_bounds__(256) k_collapse4(const Node* __restrict__ node
         const int4 c = __ldg(&nodes[i].ch);
         float lo0[3][2], hi0[3][2], lo1[3][2], hi1[3][2];
         int ch0[2], ch1[2], n0[2], n1[2];
-        node4_half(nodes, bx, by, bz, c, 0, lo0, hi0, ch0, n0);
-        node4_half(nodes, bx, by, bz, c, 1, lo1, hi1, ch1, n1);
+        node4_half(nodes, n, bx, by, bz, c, 0, lo0, hi0, ch0, n0);
+        node4_half(nodes, n, bx, by, bz, c, 1, lo1, hi1, ch1, n1);
         Node4 q;
         q.lox = make_float4(lo0[0][0], lo0[0][1], lo1[0][0], lo1[0][1]);
         q.hix = make_float4(hi0[0][0], hi0[0][1], hi1[0][0], hi1[0][1]);
