@@ -135,10 +135,10 @@ def edge_ray_bytes(src, tgt, raw_hits):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced edge
-# of k_edge_rays, from one ncu capture of the two launches of the
-# intersection join of the default workload (profiles/
-# k_edge_rays_ellipsoids_50000.md); None until such a capture exists.
-EDGE_RAY_DRAM_BYTES_PER_RAY = None
+# of k_edge_rays, from one full-size ncu capture of the two launches of the
+# intersection join of the default workload (1,191.7 MB for 28,852,896
+# traced edges; profiles/k_edge_rays_ellipsoids_50000.md).
+EDGE_RAY_DRAM_BYTES_PER_RAY = 41.30
 
 
 def traffic_estimate(rays):

@@ -88,7 +88,10 @@ typedef struct pierce_pair {
     int32_t b;  /* object id in dataset B (mesh2) */
 } pierce_pair;
 
-/* Arrays of one preprocessed dataset, as stored in a `.pre` file. */
+/* Arrays of one preprocessed dataset, as stored in a `.pre` file.  The
+ * edges of object o are edges of o's triangles (as pierce_preprocess
+ * extracts them): the joins' box culling relies on every edge lying in the
+ * boxes of its object's triangles. */
 typedef struct pierce_mesh_view {
     const float* vertices;        /* 3 * num_vertices (xyz) */
     uint64_t num_vertices;

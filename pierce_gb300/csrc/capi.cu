@@ -1059,7 +1059,9 @@ struct Join {
         // triangles (leaf = one group of `leaf` triangles, rounded to a power
         // of two): the active chunk lists replace the triangle lists.
         const bool grouped = tri_chunks && A->num_parts == 0;
-        if (grouped) return grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, b0);
+        if (grouped)
+            return grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b,
+                                  two_rounds ? cull_b : objA, b0);
         int64_t na = 0, nb = 0;
         if (int s = host_value(ctx, words + 5, 8, &na, "active triangles of A")) return s;
         if (int s = host_value(ctx, words + 6, 8, &nb, "active triangles of B")) return s;
@@ -1119,7 +1121,7 @@ struct Join {
     // Per side: active chunk ids (into the side's triangle-list buffer), then
     // a hierarchy over groups of G consecutive triangles of those chunks.
     int grouped_builds(const uint8_t* tchunk_a, const uint8_t* tchunk_b, uint32_t* ids_a, uint32_t* ids_b,
-                       int leaf_a, int leaf_b, int b0) {
+                       int leaf_a, int leaf_b, const DevDataset& filter_b, int b0) {
         auto group_of = [](int leaf) {
             int g = 1;
             while (g < leaf && g < 32) g <<= 1;
@@ -1138,26 +1140,41 @@ struct Join {
         }
         for (int sd = 0; sd < 2; ++sd)
             if (int s = host_value(ctx, words + 9 + sd, 8, &nc[sd], "active chunks")) return s;
-        for (int sd = 0; sd < 2; ++sd) {
+        // B first, keeping the groups that meet a surviving chunk box of A
+        // (or an object box of A); then A, keeping the groups that meet a
+        // kept group of B (or an object box of B)
+        for (int sd = 1; sd >= 0; --sd) {
             const int64_t ng = nc[sd] * (32 / G[sd]);
             void *sp = nullptr, *np = nullptr, *gp = nullptr;
             if (int s = scratch(ctx, soup_slot[sd], 48 * 32 * (size_t)std::max<int64_t>(nc[sd], 1), &sp)) return s;
             if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1), &np)) return s;
-            if (int s = scratch(ctx, SLOT_GROUPS, 88 * (size_t)std::max<int64_t>(ng, 1) + 256, &gp)) return s;
+            if (int s = scratch(ctx, SLOT_GROUPS, 96 * (size_t)std::max<int64_t>(ng, 1) + 512, &gp)) return s;
+            const DevDataset* filter = nullptr;
+            int soup_boxes = 1;
+            if (sd == 1) {
+                filter = &filter_b;
+            } else if (vb.nodes4 && !vb.root_is_leaf) {
+                filter = &vb;
+                soup_boxes = 0;
+            } else {
+                filter = &objB_;
+            }
+            if (!filter->nodes4) filter = nullptr;
             BvhShape sh;
+            int64_t kept = ng;
             if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
                                            (int64_t)ds[sd]->nt, ids[sd], nc[sd], G[sd], gp, (float4*)sp, (Node*)np,
-                                           &sh))
+                                           &sh, filter, soup_boxes, words + 11 + sd, &kept))
                 return s;
             DevDataset& v = *views[sd];
             v.soup = (const float4*)sp;
             v.nodes = (const Node*)np;
-            v.num_tris = nc[sd] * 32;
+            v.num_tris = kept * G[sd];
             v.root_is_leaf = sh.root_is_leaf;
             v.root_leaf_count = sh.root_leaf_count;
             v.part_roots = nullptr;
             if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A)) return s;
-            st.active_triangles[sd] = (uint64_t)(nc[sd] * 32);
+            st.active_triangles[sd] = (uint64_t)(kept * G[sd]);
         }
         timer.span(b0, timer.record(), &st.ms_build);
         return PIERCE_OK;

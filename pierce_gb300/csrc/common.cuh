@@ -296,10 +296,15 @@ int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out)
 int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready = nullptr,
                     const int32_t* grouped_flag = nullptr);
 // hierarchy over groups of G consecutive triangles (G divides 32) of the
-// listed 32-triangle chunks; group_scratch holds 88 bytes per group
+// listed 32-triangle chunks; group_scratch holds 96 bytes per group (+ 512).
+// With `filter` only the groups whose box meets a leaf of that four-wide
+// hierarchy are kept (join.cu k_group_filter); *kept receives their number.
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
-                       Node* nodes, BvhShape* shape);
+                       Node* nodes, BvhShape* shape, const DevDataset* filter = nullptr, int filter_soup_boxes = 0,
+                       unsigned long long* d_count = nullptr, int64_t* kept = nullptr);
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, int soup_boxes,
+                        uint8_t* flags);
 
 // sortscan.cu (CUB library calls)
 int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,

@@ -975,6 +975,46 @@ int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, u
 // every lane then queries the other side's object hierarchy with its box.
 constexpr int kChunk = 32;
 
+// Per-join builds over groups of triangles keep only the groups whose box
+// meets a leaf of `other`, a four-wide hierarchy of the other side: with
+// soup_boxes its leaves hold boxes as degenerate triangles (lo, hi, hi) --
+// object boxes or surviving chunk boxes -- tested one by one; otherwise (the
+// other side's per-join hierarchy) a leaf is tested by its entry box, the
+// box of its group.  A group that meets none cannot meet the other side's
+// edges, which lie in those boxes.
+__global__ void __launch_bounds__(256) k_group_filter(const float* __restrict__ gbox, int64_t ng, DevDataset other,
+                                                      int soup_boxes, uint8_t* __restrict__ flags) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
+        const float* b = gbox + 6 * g;
+        const float3 lo = make_float3(b[0], b[1], b[2]), hi = make_float3(b[3], b[4], b[5]);
+        bool keep = true;  // without a hierarchy (a single root leaf) keep everything
+        if (!other.root_is_leaf && other.nodes4 && lo.x <= hi.x) {
+            keep = any_hit4(other.nodes4, 0, lo, hi, [&](int first, int count) {
+                if (!soup_boxes) return true;
+                for (int k = 0; k < count; ++k) {
+                    const float4 a4 = __ldg(other.soup + 3 * (int64_t)(first + k));
+                    const float4 b4 = __ldg(other.soup + 3 * (int64_t)(first + k) + 1);
+                    if (box_overlap(a4.x, b4.x, a4.y, b4.y, a4.z, b4.z, lo, hi)) return true;
+                }
+                return false;
+            });
+        } else if (other.num_tris == 0) {
+            keep = false;
+        }
+        flags[g] = keep ? 1 : 0;
+    }
+}
+
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, int soup_boxes,
+                        uint8_t* flags) {
+    if (ng <= 0) return PIERCE_OK;
+    const int64_t blocks = std::min<int64_t>((ng + 255) / 256, (int64_t)ctx->sm_count * 16);
+    k_group_filter<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(gbox, ng, other, soup_boxes,
+                                                                                  flags);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "group filter");
+}
+
 // Does [lo, hi] meet an object box of `objs` (the hierarchy of degenerate
 // triangles (lo, hi, hi), one per object), within partition `part`?
 __device__ bool meets_any_object(const DevDataset& objs, int32_t part, const float3& lo, const float3& hi) {

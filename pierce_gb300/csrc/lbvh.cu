@@ -1019,7 +1019,8 @@ int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out)
 
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
-                       Node* nodes, BvhShape* shape) {
+                       Node* nodes, BvhShape* shape, const DevDataset* filter, int filter_soup_boxes,
+                       unsigned long long* d_count, int64_t* kept) {
     cudaStream_t st = ctx->stream;
     const int64_t ng = n_chunks * (32 / G);
     shape->leaf_size = G;
@@ -1027,11 +1028,13 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
         shape->root_is_leaf = 1;
         shape->root_leaf_count = 0;
         shape->num_nodes = 0;
+        if (kept) *kept = 0;
         return PIERCE_OK;
     }
     if (ng * G >= (int64_t(1) << 30))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "bvh build: at most 2^30 - 1 triangles per hierarchy");
-    // group scratch: soup 48, boxes 24, pseudo indices 12, ids 4 bytes per group
+    // group scratch: soup 48, boxes 24, pseudo indices 12, ids 4, filter flags 1
+    // and kept-group list 4 bytes per group
     char* q = static_cast<char*>(group_scratch);
     float4* gsoup = reinterpret_cast<float4*>(q);
     float* gbox = reinterpret_cast<float*>(q + 48 * ng);
@@ -1041,9 +1044,29 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
     k_group_boxes<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)ctx->sm_count * 16)),
                     256, 0, st>>>(verts, idx, t2o, nt, chunk_list, n_chunks, G, gbox, gidx, gt2o);
     ctx->launches += 1;
+    // optional filter: keep the groups that can meet the other side
+    const uint32_t* list = nullptr;
+    int64_t n = ng;
+    if (filter) {
+        uint8_t* flags = reinterpret_cast<uint8_t*>(q + 88 * ng);
+        char* lq = q + 88 * ng + ng;
+        lq += (256 - ((uintptr_t)lq & 255)) & 255;
+        uint32_t* glist = reinterpret_cast<uint32_t*>(lq);
+        if (int s = launch_group_filter(ctx, gbox, ng, *filter, filter_soup_boxes, flags)) return s;
+        if (int s = select_flagged(ctx, flags, ng, glist, d_count)) return s;
+        if (int s = host_value(ctx, d_count, 8, &n, "kept groups")) return s;
+        list = glist;
+    }
+    if (kept) *kept = n;
+    if (n == 0) {
+        shape->root_is_leaf = 1;
+        shape->root_leaf_count = 0;
+        shape->num_nodes = 0;
+        return check_cuda(cudaGetLastError(), "grouped bvh build");
+    }
     BvhShape gshape;
-    if (int s = build_lbvh(ctx, gbox, gidx, gt2o, nullptr, ng, 1, gsoup, nodes, &gshape, nullptr)) return s;
-    k_group_soup<<<grid_for(ctx, ng * G, 256), 256, 0, st>>>(gsoup, ng, G, chunk_list, verts, idx, t2o, nt, soup);
+    if (int s = build_lbvh(ctx, gbox, gidx, gt2o, list, n, 1, gsoup, nodes, &gshape, nullptr)) return s;
+    k_group_soup<<<grid_for(ctx, n * G, 256), 256, 0, st>>>(gsoup, n, G, chunk_list, verts, idx, t2o, nt, soup);
     ctx->launches += 1;
     if (gshape.root_is_leaf) {
         shape->root_is_leaf = 1;
