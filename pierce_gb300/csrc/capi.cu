@@ -930,6 +930,7 @@ struct Join {
         out->root_leaf_count = shape.root_leaf_count;
         out->obj_part = ds->d_obj_part;
         out->part_roots = roots;
+        out->soup_boxes = 1;
         return wide_nodes(*out, shape.num_nodes, slot4, true);
     }
 
@@ -1022,6 +1023,7 @@ struct Join {
                 cull_b.num_tris = n_act;
                 cull_b.root_is_leaf = shc.root_is_leaf;
                 cull_b.root_leaf_count = shc.root_leaf_count;
+                cull_b.soup_boxes = 1;
                 if (int s = wide_nodes(cull_b, shc.num_nodes, SLOT_NODES4_CHUNKS, true)) return s;
             }
             if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
@@ -1041,6 +1043,27 @@ struct Join {
                                             (uint32_t*)tb, words + 6))
                 return s;
         }
+        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
+        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
+        // Unpartitioned chunk-culled sides build over groups of consecutive
+        // triangles (leaf = one group of `leaf` triangles, rounded to a power
+        // of two): the active chunk lists replace the triangle lists.  Their
+        // edge chunks are then culled against the other side's kept
+        // triangles: an edge that meets the other side meets a kept triangle.
+        const bool grouped = tri_chunks && A->num_parts == 0;
+        if (grouped) {
+            if (int s = grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, cull_b))
+                return s;
+            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
+                                          words + 0, nullptr, chunk_list, words + 8))
+                return s;
+            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, va, echunk_b, list[1],
+                                          words + 1, nullptr, chunk_list, words + 8))
+                return s;
+            listed[0] = listed[1] = true;
+            timer.span(b0, timer.record(), &st.ms_build);
+            return PIERCE_OK;
+        }
         if (chunked) {
             if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a, list[0],
                                           words + 0, nullptr, chunk_list, words + 8))
@@ -1053,15 +1076,6 @@ struct Join {
             if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
         }
         listed[0] = listed[1] = true;
-        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
-        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
-        // Unpartitioned chunk-culled sides build over groups of consecutive
-        // triangles (leaf = one group of `leaf` triangles, rounded to a power
-        // of two): the active chunk lists replace the triangle lists.
-        const bool grouped = tri_chunks && A->num_parts == 0;
-        if (grouped)
-            return grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b,
-                                  two_rounds ? cull_b : objA, b0);
         int64_t na = 0, nb = 0;
         if (int s = host_value(ctx, words + 5, 8, &na, "active triangles of A")) return s;
         if (int s = host_value(ctx, words + 6, 8, &nb, "active triangles of B")) return s;
@@ -1104,9 +1118,9 @@ struct Join {
         return PIERCE_OK;
     }
 
-    // Four-wide copy of a per-join hierarchy for the one-ray-per-thread walk
-    // (traversal 0; the other traversals use the binary nodes), and of the
-    // culling hierarchies (always).
+    // Four-wide copy of a hierarchy: per-join hierarchies for the
+    // one-ray-per-thread walk (traversal 0; the other traversals walk the
+    // binary nodes) and, always, the hierarchies that culling walks.
     int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot, bool always = false) {
         v.nodes4 = nullptr;
         if ((o.traversal != 0 && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
@@ -1121,7 +1135,7 @@ struct Join {
     // Per side: active chunk ids (into the side's triangle-list buffer), then
     // a hierarchy over groups of G consecutive triangles of those chunks.
     int grouped_builds(const uint8_t* tchunk_a, const uint8_t* tchunk_b, uint32_t* ids_a, uint32_t* ids_b,
-                       int leaf_a, int leaf_b, const DevDataset& filter_b, int b0) {
+                       int leaf_a, int leaf_b, const DevDataset& filter_b) {
         auto group_of = [](int leaf) {
             int g = 1;
             while (g < leaf && g < 32) g <<= 1;
@@ -1150,21 +1164,15 @@ struct Join {
             if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1), &np)) return s;
             if (int s = scratch(ctx, SLOT_GROUPS, 96 * (size_t)std::max<int64_t>(ng, 1) + 512, &gp)) return s;
             const DevDataset* filter = nullptr;
-            int soup_boxes = 1;
-            if (sd == 1) {
-                filter = &filter_b;
-            } else if (vb.nodes4 && !vb.root_is_leaf) {
-                filter = &vb;
-                soup_boxes = 0;
-            } else {
-                filter = &objB_;
-            }
+            if (sd == 1) filter = &filter_b;
+            else if (vb.nodes4 && !vb.root_is_leaf) filter = &vb;
+            else filter = &objB_;
             if (!filter->nodes4) filter = nullptr;
             BvhShape sh;
             int64_t kept = ng;
             if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
                                            (int64_t)ds[sd]->nt, ids[sd], nc[sd], G[sd], gp, (float4*)sp, (Node*)np,
-                                           &sh, filter, soup_boxes, words + 11 + sd, &kept))
+                                           &sh, filter, words + 11 + sd, &kept))
                 return s;
             DevDataset& v = *views[sd];
             v.soup = (const float4*)sp;
@@ -1173,10 +1181,11 @@ struct Join {
             v.root_is_leaf = sh.root_is_leaf;
             v.root_leaf_count = sh.root_leaf_count;
             v.part_roots = nullptr;
-            if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A)) return s;
+            // four-wide copy in every traversal mode: it also filters the
+            // other side's groups and culls the edge chunks
+            if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A, true)) return s;
             st.active_triangles[sd] = (uint64_t)(kept * G[sd]);
         }
-        timer.span(b0, timer.record(), &st.ms_build);
         return PIERCE_OK;
     }
 
@@ -1195,7 +1204,9 @@ struct Join {
         for (int d = 0; d < 2; ++d) {
             if (!dirs[d]) continue;
             const DevDataset& src = d ? vb : va;
-            const DevDataset& tgt = d ? va : vb;
+            // the four-wide copies also serve culling; only traversal 0 walks them
+            DevDataset tgt = d ? va : vb;
+            if (o.traversal != 0) tgt.nodes4 = nullptr;
             int32_t* counts = d ? counts_ba : counts_ab;
             const int64_t* offs = d ? off_ba : off_ab;
             const int b = timer.record();

@@ -95,6 +95,7 @@ struct DevDataset {
     const float* tri_chunk_box;
     const float* edge_chunk_box;
     int edges_grouped;  // edges stored grouped by source object
+    int soup_boxes;     // the soup holds boxes as degenerate triangles (lo, hi, hi), not triangles
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -239,6 +240,7 @@ struct pierce_dataset {
         v.tri_chunk_box = d_tri_chunk_box;
         v.edge_chunk_box = d_edge_chunk_box;
         v.edges_grouped = edges_grouped;
+        v.soup_boxes = 0;
         return v;
     }
 };
@@ -301,10 +303,9 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready
 // hierarchy are kept (join.cu k_group_filter); *kept receives their number.
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
-                       Node* nodes, BvhShape* shape, const DevDataset* filter = nullptr, int filter_soup_boxes = 0,
+                       Node* nodes, BvhShape* shape, const DevDataset* filter = nullptr,
                        unsigned long long* d_count = nullptr, int64_t* kept = nullptr);
-int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, int soup_boxes,
-                        uint8_t* flags);
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, uint8_t* flags);
 
 // sortscan.cu (CUB library calls)
 int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,

@@ -975,29 +975,41 @@ int launch_cull(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, u
 // every lane then queries the other side's object hierarchy with its box.
 constexpr int kChunk = 32;
 
+// Does leaf [first, first + count) of `h` meet [lo, hi]?  A soup of boxes
+// (degenerate triangles lo, hi, hi) is tested box by box, a soup of
+// triangles by each triangle's box.
+__device__ __forceinline__ bool leaf_meets_box(const DevDataset& h, int first, int count, const float3& lo,
+                                               const float3& hi) {
+    for (int k = 0; k < count; ++k) {
+        const int64_t t = (int64_t)first + k;
+        const float4 a4 = __ldg(h.soup + 3 * t), b4 = __ldg(h.soup + 3 * t + 1);
+        if (h.soup_boxes) {
+            if (box_overlap(a4.x, b4.x, a4.y, b4.y, a4.z, b4.z, lo, hi)) return true;
+        } else {
+            const float4 c4 = __ldg(h.soup + 3 * t + 2);
+            if (box_overlap(fminf(a4.x, fminf(b4.x, c4.x)), fmaxf(a4.x, fmaxf(b4.x, c4.x)),
+                            fminf(a4.y, fminf(b4.y, c4.y)), fmaxf(a4.y, fmaxf(b4.y, c4.y)),
+                            fminf(a4.z, fminf(b4.z, c4.z)), fmaxf(a4.z, fmaxf(b4.z, c4.z)), lo, hi))
+                return true;
+        }
+    }
+    return false;
+}
+
 // Per-join builds over groups of triangles keep only the groups whose box
-// meets a leaf of `other`, a four-wide hierarchy of the other side: with
-// soup_boxes its leaves hold boxes as degenerate triangles (lo, hi, hi) --
-// object boxes or surviving chunk boxes -- tested one by one; otherwise (the
-// other side's per-join hierarchy) a leaf is tested by its entry box, the
-// box of its group.  A group that meets none cannot meet the other side's
-// edges, which lie in those boxes.
+// meets a leaf item of `other`, a four-wide hierarchy of the other side:
+// object boxes, surviving chunk boxes, or the other side's kept triangles.
+// A group that meets none cannot meet the other side's edges, which lie in
+// those boxes.
 __global__ void __launch_bounds__(256) k_group_filter(const float* __restrict__ gbox, int64_t ng, DevDataset other,
-                                                      int soup_boxes, uint8_t* __restrict__ flags) {
+                                                      uint8_t* __restrict__ flags) {
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
         const float* b = gbox + 6 * g;
         const float3 lo = make_float3(b[0], b[1], b[2]), hi = make_float3(b[3], b[4], b[5]);
         bool keep = true;  // without a hierarchy (a single root leaf) keep everything
         if (!other.root_is_leaf && other.nodes4 && lo.x <= hi.x) {
-            keep = any_hit4(other.nodes4, 0, lo, hi, [&](int first, int count) {
-                if (!soup_boxes) return true;
-                for (int k = 0; k < count; ++k) {
-                    const float4 a4 = __ldg(other.soup + 3 * (int64_t)(first + k));
-                    const float4 b4 = __ldg(other.soup + 3 * (int64_t)(first + k) + 1);
-                    if (box_overlap(a4.x, b4.x, a4.y, b4.y, a4.z, b4.z, lo, hi)) return true;
-                }
-                return false;
-            });
+            keep = any_hit4(other.nodes4, 0, lo, hi,
+                            [&](int first, int count) { return leaf_meets_box(other, first, count, lo, hi); });
         } else if (other.num_tris == 0) {
             keep = false;
         }
@@ -1005,27 +1017,19 @@ __global__ void __launch_bounds__(256) k_group_filter(const float* __restrict__ 
     }
 }
 
-int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, int soup_boxes,
-                        uint8_t* flags) {
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, uint8_t* flags) {
     if (ng <= 0) return PIERCE_OK;
     const int64_t blocks = std::min<int64_t>((ng + 255) / 256, (int64_t)ctx->sm_count * 16);
-    k_group_filter<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(gbox, ng, other, soup_boxes,
-                                                                                  flags);
+    k_group_filter<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(gbox, ng, other, flags);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "group filter");
 }
 
-// Does [lo, hi] meet an object box of `objs` (the hierarchy of degenerate
-// triangles (lo, hi, hi), one per object), within partition `part`?
+// Does [lo, hi] meet an item of `objs` within partition `part`?  Items are
+// the boxes of a box hierarchy (object or chunk boxes as degenerate
+// triangles) or the triangles of a per-join hierarchy (by their boxes).
 __device__ bool meets_any_object(const DevDataset& objs, int32_t part, const float3& lo, const float3& hi) {
-    auto leaf_hit = [&](int first, int count) {
-        for (int k = 0; k < count; ++k) {
-            const float4 a4 = __ldg(objs.soup + 3 * (int64_t)(first + k));
-            const float4 b4 = __ldg(objs.soup + 3 * (int64_t)(first + k) + 1);
-            if (box_overlap(a4.x, b4.x, a4.y, b4.y, a4.z, b4.z, lo, hi)) return true;
-        }
-        return false;
-    };
+    auto leaf_hit = [&](int first, int count) { return leaf_meets_box(objs, first, count, lo, hi); };
     int node;
     if (objs.part_roots) {
         const int2 r = __ldg(objs.part_roots + part);

@@ -1019,8 +1019,8 @@ int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out)
 
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
-                       Node* nodes, BvhShape* shape, const DevDataset* filter, int filter_soup_boxes,
-                       unsigned long long* d_count, int64_t* kept) {
+                       Node* nodes, BvhShape* shape, const DevDataset* filter, unsigned long long* d_count,
+                       int64_t* kept) {
     cudaStream_t st = ctx->stream;
     const int64_t ng = n_chunks * (32 / G);
     shape->leaf_size = G;
@@ -1052,7 +1052,7 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
         char* lq = q + 88 * ng + ng;
         lq += (256 - ((uintptr_t)lq & 255)) & 255;
         uint32_t* glist = reinterpret_cast<uint32_t*>(lq);
-        if (int s = launch_group_filter(ctx, gbox, ng, *filter, filter_soup_boxes, flags)) return s;
+        if (int s = launch_group_filter(ctx, gbox, ng, *filter, flags)) return s;
         if (int s = select_flagged(ctx, flags, ng, glist, d_count)) return s;
         if (int s = host_value(ctx, d_count, 8, &n, "kept groups")) return s;
         list = glist;
