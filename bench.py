@@ -136,9 +136,9 @@ def edge_ray_bytes(src, tgt, raw_hits):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced edge
 # of k_edge_rays, from one full-size ncu capture of the two launches of the
-# intersection join of the default workload (1,191.7 MB for 28,852,896
-# traced edges; profiles/k_edge_rays_ellipsoids_50000.md).
-EDGE_RAY_DRAM_BYTES_PER_RAY = 41.30
+# intersection join of the default workload (608.8 MB for 13,316,000 traced
+# edges; profiles/k_edge_rays_ellipsoids_50000.md).
+EDGE_RAY_DRAM_BYTES_PER_RAY = 45.72
 
 
 def traffic_estimate(rays):
