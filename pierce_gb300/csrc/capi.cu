@@ -38,7 +38,7 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
                           const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
 size_t column_grid_bytes(int32_t n);
-int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int64_t* n_entries);
+int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, const int32_t** d_total);
 int column_grid_fill(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int32_t* entries, ColumnGrid* g);
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,
                   unsigned long long* d_count);
@@ -866,15 +866,26 @@ struct Join {
     bool object_parity = false;
     ColumnGrid gridA_{}, gridB_{};  // parity candidates of each side as a target
 
-    // Column grid of one side's object boxes in scratch slots meta/entries.
-    int column_grid(const DevDataset& v, int meta_slot, int entries_slot, ColumnGrid* g) {
-        void* pm = nullptr;
-        if (int s = scratch(ctx, meta_slot, column_grid_bytes(v.num_objects), &pm)) return s;
-        int64_t n = 0;
-        if (int s = column_grid_count(ctx, v, pm, &n)) return s;
-        void* pe = nullptr;
-        if (int s = scratch(ctx, entries_slot, 4 * (size_t)std::max<int64_t>(n, 1), &pe)) return s;
-        return column_grid_fill(ctx, v, pm, (int32_t*)pe, g);
+    // Column grids of both sides' object boxes (scratch slots meta/entries):
+    // both counting passes, then the two sizes read back together.
+    int column_grids() {
+        const DevDataset* v[2] = {&va, &vb};
+        const int meta_slot[2] = {SLOT_GRID_A, SLOT_GRID_B}, entries_slot[2] = {SLOT_GRID_A_ENTRIES, SLOT_GRID_B_ENTRIES};
+        ColumnGrid* g[2] = {&gridA_, &gridB_};
+        void* pm[2] = {nullptr, nullptr};
+        const int32_t* total[2] = {nullptr, nullptr};
+        for (int sd = 0; sd < 2; ++sd) {
+            if (int s = scratch(ctx, meta_slot[sd], column_grid_bytes(v[sd]->num_objects), &pm[sd])) return s;
+            if (int s = column_grid_count(ctx, *v[sd], pm[sd], &total[sd])) return s;
+        }
+        for (int sd = 0; sd < 2; ++sd) {
+            int64_t n = 0;
+            if (int s = host_value(ctx, total[sd], 4, &n, "column grid size")) return s;
+            void* pe = nullptr;
+            if (int s = scratch(ctx, entries_slot[sd], 4 * (size_t)std::max<int64_t>(n, 1), &pe)) return s;
+            if (int s = column_grid_fill(ctx, *v[sd], pm[sd], (int32_t*)pe, g[sd])) return s;
+        }
+        return PIERCE_OK;
     }
 
     int prepare() {
@@ -947,10 +958,8 @@ struct Join {
         objA_ = objA;
         objB_ = objB;
         object_parity = A->contiguous && B->contiguous;
-        if (object_parity && o.predicate != PIERCE_OVERLAP) {
-            if (int s = column_grid(va, SLOT_GRID_A, SLOT_GRID_A_ENTRIES, &gridA_)) return s;
-            if (int s = column_grid(vb, SLOT_GRID_B, SLOT_GRID_B_ENTRIES, &gridB_)) return s;
-        }
+        if (object_parity && o.predicate != PIERCE_OVERLAP)
+            if (int s = column_grids()) return s;
         uint8_t* act_a = active;
         uint8_t* act_b = active + std::max(A->num_objects, 1);
         if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
@@ -1429,6 +1438,56 @@ struct Join {
         }
     }
 
+    // Parity of both directions into the pair table: both launches, one
+    // error check, then both emits.  A full parity table falls back to one
+    // direction at a time (each with its own enlarging retries).
+    int parity_both(uint64_t* table, uint64_t slots) {
+        const bool need[2] = {ab, ba};
+        const int slot_of[2] = {SLOT_BUILD_C, SLOT_BUILD_D};
+        uint64_t pslots[2] = {0, 0};
+        uint64_t* ptable[2] = {nullptr, nullptr};
+        uint32_t* par[2] = {nullptr, nullptr};
+        for (int d = 0; d < 2; ++d) {
+            if (!need[d]) continue;
+            const DevDataset& src = d ? vb : va;
+            const DevDataset& tgt = d ? va : vb;
+            pslots[d] = table_slots_for(8 * (uint64_t)std::max(src.num_objects, 1), 0.5);
+            void* p = nullptr;
+            if (int s = scratch(ctx, slot_of[d], pslots[d] * 12, &p)) return s;
+            ptable[d] = static_cast<uint64_t*>(p);
+            par[d] = reinterpret_cast<uint32_t*>(ptable[d] + pslots[d]);
+            cudaMemsetAsync(ptable[d], 0xFF, pslots[d] * 8, ctx->stream);
+            cudaMemsetAsync(par[d], 0, pslots[d] * 4, ctx->stream);
+            const int b = timer.record();
+            if (object_parity) {
+                if (int s = launch_parity_objects(ctx, src, d ? objA_ : objB_, tgt, d ? &gridA_ : &gridB_, d,
+                                                  ptable[d], par[d], pslots[d]))
+                    return s;
+            } else if (int s = launch_parity(ctx, src, tgt, d, ptable[d], par[d], pslots[d])) {
+                return s;
+            }
+            timer.span(b, timer.record(), &st.ms_parity[d]);
+        }
+        uint32_t bits = 0;
+        if (int s = read_device_error(ctx, &bits)) return s;
+        if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+        if (bits & ERR_HASH_FULL) {
+            st.retries++;
+            for (int d = 0; d < 2; ++d)
+                if (need[d])
+                    if (int s = parity(d ? vb : va, d ? va : vb, d, &st.ms_parity[d], 0, table, slots, nullptr, 0,
+                                       nullptr, 0, nullptr, nullptr, 0))
+                        return s;
+            return PIERCE_OK;
+        }
+        for (int d = 0; d < 2; ++d)
+            if (need[d])
+                if (int s = parity_emit(ctx, ptable[d], par[d], pslots[d], 0, nullptr, 0, nullptr, 0, table, slots,
+                                        nullptr, nullptr, 0))
+                    return s;
+        return PIERCE_OK;
+    }
+
     int make_result(const uint64_t* keys_sorted, uint64_t n, pierce_result** out) {
         pierce_result* r = new pierce_result();
         r->count = n;
@@ -1582,12 +1641,7 @@ struct Join {
         uint64_t* table = nullptr;
         uint64_t slots = 0, n = 0;
         if (int s = overlap_hash(&table, &slots)) return s;
-        if (ab)
-            if (int s = parity(va, vb, 0, &st.ms_parity[0], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
-                return s;
-        if (ba)
-            if (int s = parity(vb, va, 1, &st.ms_parity[1], 0, table, slots, nullptr, 0, nullptr, 0, nullptr, nullptr, 0))
-                return s;
+        if (int s = parity_both(table, slots)) return s;
         uint32_t bits = 0;
         if (int s = read_device_error(ctx, &bits)) return s;
         if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "pair table full while adding parity pairs");

@@ -1523,7 +1523,7 @@ size_t column_grid_bytes(int32_t n) {
 
 // Column grid, first phase: bounds, per-cell counts and offsets in `mem`;
 // *n_entries receives the number of (cell, object) entries.
-int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int64_t* n_entries) {
+int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, const int32_t** d_total) {
     const int32_t n = tgt.num_objects;
     const int side = std::max(1, (int)std::ceil(std::sqrt((double)std::max(n, 1))));
     const int cells = side * side;
@@ -1545,7 +1545,8 @@ int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int64_t
                                                                nullptr);
     ctx->launches += 5;
     if (int s = exclusive_scan_i32(ctx, counts, offsets, cells + 1)) return s;
-    return host_value(ctx, offsets + cells, 4, n_entries, "column grid size");
+    *d_total = offsets + cells;  // the number of entries, read by the caller
+    return PIERCE_OK;
 }
 
 // Second phase: the object ids of every cell into `entries` (n_entries).

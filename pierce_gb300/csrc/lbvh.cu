@@ -828,7 +828,9 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
         uint32_t* lists[2] = {keys, keys + (n + 1) / 2 + 1};
         cudaMemsetAsync(wave_count, 0, 2 * sizeof(unsigned long long), st);
         k_refit_leaves<<<grid_for(ctx, n, B), B, 0, st>>>(soup, n, nodes, leaf_rec, lists[0], wave_count);
-        constexpr int kWaves = 3;
+        // small hierarchies (object and chunk boxes) go straight to the chain:
+        // their waves would be launches of a few blocks each
+        const int kWaves = n >= (1 << 18) ? 3 : 0;
         for (int wave = 0; wave < kWaves; ++wave) {
             const int in = wave & 1, out = in ^ 1;
             cudaMemsetAsync(wave_count + out, 0, sizeof(unsigned long long), st);
