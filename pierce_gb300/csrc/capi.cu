@@ -127,15 +127,28 @@ int device_alloc(void** p, size_t bytes, const char* what) {
     return PIERCE_OK;
 }
 
+// Free every scratch slot that the running join (generation `keep_gen`)
+// has not used, and the pool's unused memory.  keep_gen 0: free all slots.
+static void release_idle_memory(pierce_ctx* ctx, uint64_t keep_gen) {
+    cudaDeviceSynchronize();
+    for (int i = 0; i < kScratchSlots; ++i) {
+        if (!ctx->scratch[i] || (keep_gen && ctx->scratch_used[i] == keep_gen)) continue;
+        cudaFree(ctx->scratch[i]);
+        ctx->scratch[i] = nullptr;
+        ctx->scratch_bytes[i] = 0;
+    }
+    if (ctx->pool) cudaMemPoolTrimTo(ctx->pool, 0);
+}
+
 int dataset_array(pierce_ctx* ctx, void** p, size_t bytes, cudaStream_t stream, const char* what) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
     if (e == cudaErrorMemoryAllocation) {
-        // memory other datasets returned to the pool goes back to the device first
+        // the joins' scratch and the memory other datasets returned to the
+        // pool go back to the device first (no join is running)
         cudaGetLastError();
-        cudaStreamSynchronize(stream);
-        cudaMemPoolTrimTo(ctx->pool, 0);
+        release_idle_memory(ctx, 0);
         e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, stream);
     }
     if (e != cudaSuccess) {
@@ -202,6 +215,7 @@ int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
     if (bytes == 0) bytes = 16;
     if (ctx->scratch_bytes[slot] < bytes && capturing(ctx))
         return set_error(PIERCE_ERR_CUDA, "join graph capture: scratch would grow");
+    ctx->scratch_used[slot] = ctx->scratch_gen;
     if (ctx->scratch_bytes[slot] < bytes) {
         if (ctx->scratch[slot]) {
             cudaStreamSynchronize(ctx->stream);
@@ -210,10 +224,12 @@ int scratch(pierce_ctx* ctx, int slot, size_t bytes, void** out) {
             ctx->scratch_bytes[slot] = 0;
         }
         size_t want = bytes + bytes / 8;  // headroom against repeated growth
-        if (device_alloc(&ctx->scratch[slot], want, "scratch") != PIERCE_OK && ctx->pool) {
-            // arrays of destroyed datasets still held by the pool go back first
-            cudaDeviceSynchronize();
-            cudaMemPoolTrimTo(ctx->pool, 0);
+        if (device_alloc(&ctx->scratch[slot], want, "scratch") != PIERCE_OK) {
+            // slots earlier joins left behind and the pool's unused memory go
+            // back to the device first (not while a join graph is planned:
+            // the plan holds on to its buffers)
+            if (ctx->plan) return PIERCE_ERR_OUT_OF_MEMORY;
+            release_idle_memory(ctx, ctx->scratch_gen ? ctx->scratch_gen : ~0ull);
             if (int s = device_alloc(&ctx->scratch[slot], want, "scratch")) return s;
         }
         if (!ctx->scratch[slot]) return PIERCE_ERR_OUT_OF_MEMORY;
@@ -474,7 +490,16 @@ int pierce_ctx_create(int device, pierce_ctx** out) {
         props.location.id = device;
         st = check_cuda(cudaMemPoolCreate(&ctx->pool, &props), "memory pool");
         if (!st) {
-            uint64_t keep = ~0ull;
+            // keep up to 32 GiB (at most a quarter of the device) of freed
+            // arrays for the next datasets; beyond that the pool returns
+            // memory at synchronisation points, so datasets of changing sizes
+            // do not strand memory in it
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+                cudaGetLastError();
+                total_b = (size_t)64 << 30;
+            }
+            uint64_t keep = std::min<uint64_t>((uint64_t)total_b / 4, 32ull << 30);
             st = check_cuda(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool");
         }
     }
@@ -836,6 +861,7 @@ struct Join {
     bool ab, ba;
     Join(pierce_ctx* c, pierce_dataset* a, pierce_dataset* b, const pierce_join_opts& opts)
         : ctx(c), A(a), B(b), o(opts), timer(c->stream) {
+        ++c->scratch_gen;
         std::memset(&st, 0, sizeof(st));
         timer.off = capturing(c);
         ab = o.direction == PIERCE_BOTH || o.direction == PIERCE_MESH1_TO_MESH2;

@@ -168,6 +168,10 @@ struct pierce_ctx {
     // grow-only scratch buffers reused across joins
     void* scratch[pgpu::kScratchSlots] = {nullptr};
     size_t scratch_bytes[pgpu::kScratchSlots] = {0};
+    // join generation and the generation that last used each slot: a join
+    // short of memory frees the slots it has not touched
+    uint64_t scratch_gen = 0;
+    uint64_t scratch_used[pgpu::kScratchSlots] = {0};
     uint64_t launches = 0;
     int sm_count = 0;
     pgpu::GraphPlan* plan = nullptr;  // set while a join graph is planned or captured
@@ -178,9 +182,9 @@ struct pierce_ctx {
     cudaEvent_t ev_tris = nullptr, ev_edges = nullptr;
     int32_t* d_upload_flag = nullptr;  // edges grouped by source object (nonzero) after an upload
     // Dataset arrays come from this stream-ordered pool; freed arrays stay
-    // in it (release threshold: never), so datasets created and destroyed
-    // per query skip the driver's mapping work.  pierce_ctx_release_scratch
-    // trims it.
+    // in it up to 32 GiB, so datasets created and destroyed per query skip
+    // the driver's mapping work.
+    // pierce_ctx_release_scratch trims it.
     cudaMemPool_t pool = nullptr;
 };
 

@@ -63,6 +63,12 @@ class Context:
         """Free the join scratch memory the context keeps between joins."""
         check(self._lib.pierce_ctx_release_scratch(self._h), "release_scratch")
 
+    def device_memory(self) -> tuple[int, int]:
+        """(free, total) bytes of the context's device."""
+        f, t = C.c_uint64(), C.c_uint64()
+        check(self._lib.pierce_device_memory(self._h, C.byref(f), C.byref(t)), "device_memory")
+        return int(f.value), int(t.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             for child in list(getattr(self, "_children", ())):

@@ -212,10 +212,19 @@ def build_training_set(ctx, specs: list[JoinSpec], log=None) -> dict:
         tris[i] = (a.info().num_triangles, b.info().num_triangles)
         a.close()
         b.close()
+        _bound_memory(ctx)
         if log and (i % 50 == 0 or i == len(specs) - 1):
             log(f"{i + 1}/{len(specs)} nA={sp.n_a} nB={sp.n_b} pairs={counts[i]}")
     cols = {k: np.array([getattr(s, k) for s in specs]) for k in asdict(specs[0])} if specs else {}
     return {"features": X, "pairs": counts, "triangles": tris, **{"spec_" + k: v for k, v in cols.items()}}
+
+
+def _bound_memory(ctx, keep_free: float = 0.25) -> None:
+    """Between joins of very different sizes: hand the context's grow-only
+    scratch back to the device once free memory runs below `keep_free`."""
+    free, total = ctx.device_memory()
+    if free < keep_free * total:
+        ctx.release_scratch()
 
 
 def targets(pairs) -> np.ndarray:
@@ -254,6 +263,7 @@ def evaluate(ctx, model: "SizingModel", specs: list[JoinSpec], log=None) -> dict
                 row[name + "_identical"] = bool(np.array_equal(r.pairs, ref))
         a.close()
         b.close()
+        _bound_memory(ctx)
         rows.append(row)
         if log and (i % 20 == 0 or i == len(specs) - 1):
             log(f"{i + 1}/{len(specs)} pairs={row['pairs']} predicted={row['predicted']:.0f}")
