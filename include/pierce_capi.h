@@ -157,7 +157,7 @@ typedef struct pierce_join_opts {
                                      meets an object box of the other side (datasets need no BVH of their own) */
     const pierce_mlp* sizing_model; /* LEARNED sizing: trained network (pierce_mlp_create) */
     /* tuning (0: default); pierce_autotune_join picks them */
-    int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets') */
+    int32_t leaf_size;            /* leaf size of the per-join hierarchies (0: the datasets' when above 1, else 4) */
     int32_t rays_per_warp;        /* rays a warp takes per fetch from the ray queue (multiple of 32; 0: 32) */
     int32_t stack_depth;          /* traversal stack entries in shared memory per thread (1..32; 0: 8 for culled
                                      rays, 32 otherwise) */

@@ -127,6 +127,15 @@ int device_alloc(void** p, size_t bytes, const char* what) {
     return PIERCE_OK;
 }
 
+// Leaf size of a join's per-join hierarchies over dataset ds: the join's
+// own setting, else the dataset's when above one, else 4 (groups of four
+// consecutive triangles: the fastest on the measured workloads, and a
+// quarter of the build memory of single-triangle leaves).
+static int join_leaf(const pierce_join_opts& o, const pierce_dataset* ds) {
+    if (o.leaf_size > 0) return o.leaf_size;
+    return ds->leaf_size > 1 ? ds->leaf_size : 4;
+}
+
 // Free every scratch slot that the running join (generation `keep_gen`)
 // has not used, and the pool's unused memory.  keep_gen 0: free all slots.
 static void release_idle_memory(pierce_ctx* ctx, uint64_t keep_gen) {
@@ -402,7 +411,7 @@ int dataset_finish(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tuning* tun
     pierce_tuning t;
     pierce_default_tuning(&t);
     if (tuning) t = *tuning;
-    // the leaf size also applies to the per-join hierarchies of a deferred dataset
+    // a leaf size above one also applies to the per-join hierarchies
     ds->leaf_size = std::min(std::max(t.leaf_size, 1), 16);
     if (t.defer_build) return sync_ctx(ctx, "dataset upload");
     return build_bvh(ctx, ds, t.leaf_size);
@@ -490,16 +499,16 @@ int pierce_ctx_create(int device, pierce_ctx** out) {
         props.location.id = device;
         st = check_cuda(cudaMemPoolCreate(&ctx->pool, &props), "memory pool");
         if (!st) {
-            // keep up to 32 GiB (at most a quarter of the device) of freed
-            // arrays for the next datasets; beyond that the pool returns
-            // memory at synchronisation points, so datasets of changing sizes
-            // do not strand memory in it
+            // keep up to a quarter of the device's memory of freed arrays for
+            // the next datasets; beyond that the pool returns memory at
+            // synchronisation points (and an allocation short of memory trims
+            // it first)
             size_t free_b = 0, total_b = 0;
             if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
                 cudaGetLastError();
                 total_b = (size_t)64 << 30;
             }
-            uint64_t keep = std::min<uint64_t>((uint64_t)total_b / 4, 32ull << 30);
+            uint64_t keep = (uint64_t)total_b / 4;
             st = check_cuda(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool");
         }
     }
@@ -1078,8 +1087,7 @@ struct Join {
                                             (uint32_t*)tb, words + 6))
                 return s;
         }
-        const int leaf_a = o.leaf_size > 0 ? o.leaf_size : A->leaf_size;
-        const int leaf_b = o.leaf_size > 0 ? o.leaf_size : B->leaf_size;
+        const int leaf_a = join_leaf(o, A), leaf_b = join_leaf(o, B);
         // Unpartitioned chunk-culled sides build over groups of consecutive
         // triangles (leaf = one group of `leaf` triangles, rounded to a power
         // of two): the active chunk lists replace the triangle lists.  Their
@@ -1160,7 +1168,11 @@ struct Join {
         v.nodes4 = nullptr;
         if ((o.traversal != 0 && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
         void* p = nullptr;
-        if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) return s;
+        if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) {
+            // short of memory: the binary nodes serve every walk (slower)
+            if (s != PIERCE_ERR_OUT_OF_MEMORY) return s;
+            return PIERCE_OK;
+        }
         // Node4 is 128-byte aligned; cudaMalloc returns 256-byte aligned memory
         if (int s = collapse4(ctx, v.nodes, (int64_t)num_nodes, static_cast<Node4*>(p))) return s;
         v.nodes4 = static_cast<const Node4*>(p);
@@ -1811,7 +1823,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     int32_t n_trials = 0;
     pierce_tuned cur;
     std::memset(&cur, 0, sizeof(cur));
-    cur.leaf_size = o.leaf_size > 0 ? o.leaf_size : std::max(a->leaf_size, 1);
+    cur.leaf_size = join_leaf(o, a);
     cur.rays_per_warp = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
     cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 8;
     cur.hash_load_factor = o.hash_load_factor;

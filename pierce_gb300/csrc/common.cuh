@@ -182,8 +182,8 @@ struct pierce_ctx {
     cudaEvent_t ev_tris = nullptr, ev_edges = nullptr;
     int32_t* d_upload_flag = nullptr;  // edges grouped by source object (nonzero) after an upload
     // Dataset arrays come from this stream-ordered pool; freed arrays stay
-    // in it up to 32 GiB, so datasets created and destroyed per query skip
-    // the driver's mapping work.
+    // in it up to a quarter of the device's memory, so datasets created and
+    // destroyed per query skip the driver's mapping work.
     // pierce_ctx_release_scratch trims it.
     cudaMemPool_t pool = nullptr;
 };

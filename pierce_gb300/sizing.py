@@ -190,9 +190,9 @@ def sweep(seed: int, count: int, n_lo: int = 1000, n_hi: int = 200_000) -> list[
 
 def make_datasets(ctx, spec: JoinSpec, level_lo: int = 2, level_hi: int = 4):
     """Both sides of a sweep join, expanded on the device (no dataset BVHs:
-    the joins build per-join hierarchies)."""
+    the joins build per-join hierarchies, with leaves of 4 triangles)."""
     from .join import Dataset, default_tuning
-    t = default_tuning(defer_build=1)
+    t = default_tuning(leaf_size=4, defer_build=1)
     ia = instances(spec.seed_a, spec.n_a, spec.family_a, level_lo, level_hi, hi=spec.extent)
     ib = instances(spec.seed_b, spec.n_b, spec.family_b, level_lo, level_hi, hi=spec.extent)
     return Dataset.from_instances(ctx, ia, t), Dataset.from_instances(ctx, ib, t)
