@@ -64,6 +64,13 @@ def workload(scale: float = 1.0, seed_a: int = 2024, seed_b: int = 2025):
                   "edges_per_side": A.num_edges, "seeds": [seed_a, seed_b]}
 
 
+def clocks_path(name: str) -> Path:
+    """Where the nvidia-smi samples of a timed region go: $PIERCE_CLOCKS_DIR
+    when set, else the system's temporary directory."""
+    d = os.environ.get("PIERCE_CLOCKS_DIR")
+    return Path(d) / name if d else Path(tempfile.gettempdir()) / f"pierce_{name}"
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -258,8 +265,7 @@ def main_batched(args):
     def opts_fn(w):
         return J.tuned_opts(J.make_opts(predicate="overlap", expected_pairs=BT.expected_pairs(w)), best)
 
-    clocks = Clocks(ROOT / "gpurun_out" / "clocks_batched.csv" if (ROOT / "gpurun_out").exists()
-                    else Path(tempfile.gettempdir()) / "pierce_clocks_batched.csv")
+    clocks = Clocks(clocks_path("clocks_batched.csv"))
     with clocks:
         bat = BT.run_batched(ctx, waves, opts_fn, warmup=max(1, args.warmup), replays=max(1, args.steps),
                              log=log, keep_pairs=True)
@@ -445,8 +451,7 @@ def main_tubes(args):
     cpu_global = ((cpu_keys >> np.uint64(32)) << np.uint64(32)) | near64[(cpu_keys & np.uint64(0xFFFFFFFF)).astype(np.int64)]
     sample_match = bool(np.array_equal(np.sort(sample_gpu), np.sort(cpu_global)))
     log(f"pairs {len(keys_t)} tuned == plain: {identical}; sample vs oracle: {sample_match}")
-    clocks = Clocks(ROOT / "gpurun_out" / "clocks_tubes.csv" if (ROOT / "gpurun_out").exists()
-                    else Path(tempfile.gettempdir()) / "pierce_clocks_tubes.csv")
+    clocks = Clocks(clocks_path("clocks_tubes.csv"))
     res = {}
     with clocks:
         for name, opts, build in (("tuned", tuned_o, False), ("plain", plain_o, True)):
@@ -574,8 +579,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv" if (ROOT / "gpurun_out").exists()
-                    else Path(tempfile.gettempdir()) / f"pierce_clocks_{rank}.csv")
+    clocks = Clocks(clocks_path(f"clocks_rank{rank}.csv"))
     collected = []
     l0 = ctx.kernel_launches
     with clocks:
