@@ -1093,7 +1093,23 @@ struct Join {
         // of two): the active chunk lists replace the triangle lists.  Their
         // edge chunks are then culled against the other side's kept
         // triangles: an edge that meets the other side meets a kept triangle.
-        const bool grouped = tri_chunks && A->num_parts == 0;
+        bool grouped = tri_chunks;
+        if (grouped && A->num_parts > 0) {
+            // partitioned: groups must not span two partitions (instanced
+            // meshes never do); otherwise the hierarchies are built over the
+            // surviving triangles
+            int32_t* mixed = reinterpret_cast<int32_t*>(words + 13);
+            cudaMemsetAsync(mixed, 0, sizeof(int32_t), ctx->stream);
+            if (int s = launch_group_mixed(ctx, tchunk_a, (int64_t)((A->nt + 31) / 32), A->d_tri_to_object,
+                                           A->d_obj_part, (int64_t)A->nt, group_size(leaf_a), mixed))
+                return s;
+            if (int s = launch_group_mixed(ctx, tchunk_b, (int64_t)((B->nt + 31) / 32), B->d_tri_to_object,
+                                           B->d_obj_part, (int64_t)B->nt, group_size(leaf_b), mixed))
+                return s;
+            int64_t m = 0;
+            if (int s = host_value(ctx, mixed, 4, &m, "group partitions")) return s;
+            grouped = m == 0;
+        }
         if (grouped) {
             if (int s = grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, cull_b))
                 return s;
@@ -1181,13 +1197,16 @@ struct Join {
 
     // Per side: active chunk ids (into the side's triangle-list buffer), then
     // a hierarchy over groups of G consecutive triangles of those chunks.
+    // triangles per group of a grouped build for leaf size `leaf`
+    static int group_size(int leaf) {
+        int g = 1;
+        while (g < leaf && g < 32) g <<= 1;
+        return g;
+    }
+
     int grouped_builds(const uint8_t* tchunk_a, const uint8_t* tchunk_b, uint32_t* ids_a, uint32_t* ids_b,
                        int leaf_a, int leaf_b, const DevDataset& filter_b) {
-        auto group_of = [](int leaf) {
-            int g = 1;
-            while (g < leaf && g < 32) g <<= 1;
-            return g;
-        };
+        auto group_of = [](int leaf) { return group_size(leaf); };
         pierce_dataset* ds[2] = {A, B};
         const uint8_t* flags[2] = {tchunk_a, tchunk_b};
         uint32_t* ids[2] = {ids_a, ids_b};
@@ -1206,9 +1225,12 @@ struct Join {
         // kept group of B (or an object box of B)
         for (int sd = 1; sd >= 0; --sd) {
             const int64_t ng = nc[sd] * (32 / G[sd]);
+            const int32_t parts = ds[sd]->num_parts;
             void *sp = nullptr, *np = nullptr, *gp = nullptr;
             if (int s = scratch(ctx, soup_slot[sd], 48 * 32 * (size_t)std::max<int64_t>(nc[sd], 1), &sp)) return s;
-            if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1), &np)) return s;
+            if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1) + 8 * (size_t)parts, &np))
+                return s;
+            int2* roots = parts ? reinterpret_cast<int2*>((Node*)np + std::max<int64_t>(ng, 1)) : nullptr;
             if (int s = scratch(ctx, SLOT_GROUPS, 96 * (size_t)std::max<int64_t>(ng, 1) + 512, &gp)) return s;
             const DevDataset* filter = nullptr;
             if (sd == 1) filter = &filter_b;
@@ -1219,7 +1241,7 @@ struct Join {
             int64_t kept = ng;
             if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
                                            (int64_t)ds[sd]->nt, ids[sd], nc[sd], G[sd], gp, (float4*)sp, (Node*)np,
-                                           &sh, filter, words + 11 + sd, &kept))
+                                           &sh, filter, words + 11 + sd, &kept, ds[sd]->d_obj_part, parts, roots))
                 return s;
             DevDataset& v = *views[sd];
             v.soup = (const float4*)sp;
@@ -1227,7 +1249,7 @@ struct Join {
             v.num_tris = kept * G[sd];
             v.root_is_leaf = sh.root_is_leaf;
             v.root_leaf_count = sh.root_leaf_count;
-            v.part_roots = nullptr;
+            v.part_roots = roots;
             // four-wide copy in every traversal mode: it also filters the
             // other side's groups and culls the edge chunks
             if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A, true)) return s;

@@ -308,8 +308,13 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
                        Node* nodes, BvhShape* shape, const DevDataset* filter = nullptr,
-                       unsigned long long* d_count = nullptr, int64_t* kept = nullptr);
-int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, uint8_t* flags);
+                       unsigned long long* d_count = nullptr, int64_t* kept = nullptr,
+                       const int32_t* obj_part = nullptr, int32_t num_parts = 0, int2* part_roots = nullptr);
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other,
+                        const int32_t* gt2o, const int32_t* obj_part, uint8_t* flags);
+// partitioned datasets: *mixed |= some group of a flagged chunk spans two partitions
+int launch_group_mixed(pierce_ctx* ctx, const uint8_t* chunk_flags, int64_t n_chunks, const int32_t* t2o,
+                       const int32_t* obj_part, int64_t nt, int G, int32_t* mixed);
 
 // sortscan.cu (CUB library calls)
 int sort_u32_pairs(pierce_ctx* ctx, uint32_t* keys_in, uint32_t* keys_out, uint32_t* vals_in, uint32_t* vals_out,

@@ -1001,15 +1001,25 @@ __device__ __forceinline__ bool leaf_meets_box(const DevDataset& h, int first, i
 // object boxes, surviving chunk boxes, or the other side's kept triangles.
 // A group that meets none cannot meet the other side's edges, which lie in
 // those boxes.
+// Partitioned sides (gt2o and obj_part given): a group only meets the other
+// side's subtree of its own partition.
 __global__ void __launch_bounds__(256) k_group_filter(const float* __restrict__ gbox, int64_t ng, DevDataset other,
+                                                      const int32_t* __restrict__ gt2o,
+                                                      const int32_t* __restrict__ obj_part,
                                                       uint8_t* __restrict__ flags) {
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
         const float* b = gbox + 6 * g;
         const float3 lo = make_float3(b[0], b[1], b[2]), hi = make_float3(b[3], b[4], b[5]);
+        auto leaf_hit = [&](int first, int count) { return leaf_meets_box(other, first, count, lo, hi); };
         bool keep = true;  // without a hierarchy (a single root leaf) keep everything
-        if (!other.root_is_leaf && other.nodes4 && lo.x <= hi.x) {
-            keep = any_hit4(other.nodes4, 0, lo, hi,
-                            [&](int first, int count) { return leaf_meets_box(other, first, count, lo, hi); });
+        if (gt2o && obj_part && other.part_roots) {
+            const int32_t o = __ldg(gt2o + g);
+            const int2 r = o >= 0 ? __ldg(other.part_roots + __ldg(obj_part + o)) : make_int2(-1, 0);
+            if (!(lo.x <= hi.x)) keep = true;
+            else if (r.x >= 0) keep = other.nodes4 ? any_hit4(other.nodes4, r.x, lo, hi, leaf_hit) : true;
+            else keep = r.y > 0 && leaf_hit(~r.x, r.y);
+        } else if (!other.root_is_leaf && other.nodes4 && lo.x <= hi.x) {
+            keep = any_hit4(other.nodes4, 0, lo, hi, leaf_hit);
         } else if (other.num_tris == 0) {
             keep = false;
         }
@@ -1017,10 +1027,12 @@ __global__ void __launch_bounds__(256) k_group_filter(const float* __restrict__ 
     }
 }
 
-int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other, uint8_t* flags) {
+int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const DevDataset& other,
+                        const int32_t* gt2o, const int32_t* obj_part, uint8_t* flags) {
     if (ng <= 0) return PIERCE_OK;
     const int64_t blocks = std::min<int64_t>((ng + 255) / 256, (int64_t)ctx->sm_count * 16);
-    k_group_filter<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(gbox, ng, other, flags);
+    k_group_filter<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(gbox, ng, other, gt2o, obj_part,
+                                                                                  flags);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "group filter");
 }

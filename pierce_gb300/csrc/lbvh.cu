@@ -867,6 +867,16 @@ int build_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const i
 // Per listed chunk, the boxes of its groups as degenerate triangles
 // (lo, hi, hi).  Triangles past the end of the dataset (final partial chunk)
 // repeat the chunk's first triangle.
+// Triangle k of group j of chunk c.  Past the last triangle a group repeats
+// its own first triangle (or, when it has none, the chunk's first), so a
+// group never mixes objects that its real triangles do not.
+__device__ __forceinline__ int64_t group_item(int64_t c, int j, int G, int k, int64_t nt) {
+    const int64_t first = c * 32 + (int64_t)j * G;
+    const int64_t t = first + k;
+    if (t < nt) return t;
+    return first < nt ? first : c * 32;
+}
+
 __global__ void __launch_bounds__(256) k_group_boxes(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
                                                      const int32_t* __restrict__ t2o, int64_t nt,
                                                      const uint32_t* __restrict__ chunk_list, int64_t n_chunks,
@@ -876,8 +886,7 @@ __global__ void __launch_bounds__(256) k_group_boxes(const float* __restrict__ v
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n_chunks; k += warps) {
         const int64_t c = chunk_list[k];
-        int64_t t = c * 32 + lane;
-        if (t >= nt) t = c * 32;
+        int64_t t = group_item(c, lane / G, G, lane % G, nt);
         float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
         for (int v = 0; v < 3; ++v) {
             const float3 p = load_vertex(verts, __ldg(idx + 3 * t + v));
@@ -915,8 +924,7 @@ __global__ void __launch_bounds__(256) k_group_soup(const float4* __restrict__ g
         const int64_t j = i / G;
         const int64_t g = __float_as_int(__ldg(&gsoup[3 * j + 1].w));
         const int64_t c = chunk_list[g / per_chunk];
-        int64_t t = c * 32 + (g % per_chunk) * G + (i % G);
-        if (t >= nt) t = c * 32;
+        const int64_t t = group_item(c, (int)(g % per_chunk), G, (int)(i % G), nt);
         const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
         const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
         const float3 cc = load_vertex(verts, __ldg(idx + 3 * t + 2));
@@ -1019,19 +1027,61 @@ int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out)
     return check_cuda(cudaGetLastError(), "collapse to four-wide nodes");
 }
 
+// Partitioned datasets: does any group of G triangles of a flagged chunk
+// hold triangles of two partitions?  (Then the join builds over triangles.)
+__global__ void __launch_bounds__(256) k_group_mixed(const uint8_t* __restrict__ chunk_flags, int64_t n_chunks,
+                                                     const int32_t* __restrict__ t2o,
+                                                     const int32_t* __restrict__ obj_part, int64_t nt, int G,
+                                                     int32_t* mixed) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_chunks; c += warps) {
+        if (!chunk_flags[c]) continue;  // warp-uniform
+        const int64_t t = group_item(c, lane / G, G, lane % G, nt);
+        const int32_t o = __ldg(t2o + t);
+        const int32_t p = o >= 0 ? __ldg(obj_part + o) : -1;
+        const int32_t p0 = __shfl_sync(0xFFFFFFFFu, p, lane & ~(G - 1));
+        if (__any_sync(0xFFFFFFFFu, p != p0) && lane == 0) atomicOr(mixed, 1);
+    }
+}
+
+int launch_group_mixed(pierce_ctx* ctx, const uint8_t* chunk_flags, int64_t n_chunks, const int32_t* t2o,
+                       const int32_t* obj_part, int64_t nt, int G, int32_t* mixed) {
+    if (n_chunks <= 0) return PIERCE_OK;
+    k_group_mixed<<<grid_for(ctx, n_chunks * 32, 256), 256, 0, ctx->stream>>>(chunk_flags, n_chunks, t2o, obj_part,
+                                                                             nt, G, mixed);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "group partition check");
+}
+
+// Partition roots of a group hierarchy: a root leaf of one group becomes the
+// soup range of its G triangles.
+__global__ void k_group_roots(int2* roots, int32_t num_parts, int G) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < num_parts;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int2 r = roots[p];
+        if (r.x < 0 && r.y > 0) roots[p] = make_int2(~((~r.x) * G), r.y * G);
+    }
+}
+
 int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx, const int32_t* t2o, int64_t nt,
                        const uint32_t* chunk_list, int64_t n_chunks, int G, void* group_scratch, float4* soup,
                        Node* nodes, BvhShape* shape, const DevDataset* filter, unsigned long long* d_count,
-                       int64_t* kept) {
+                       int64_t* kept, const int32_t* obj_part, int32_t num_parts, int2* part_roots) {
     cudaStream_t st = ctx->stream;
     const int64_t ng = n_chunks * (32 / G);
     shape->leaf_size = G;
+    const bool parts = obj_part && num_parts > 0 && part_roots;
     if (ng == 0) {
         shape->root_is_leaf = 1;
         shape->root_leaf_count = 0;
         shape->num_nodes = 0;
         if (kept) *kept = 0;
-        return PIERCE_OK;
+        if (parts) {
+            k_fill_roots<<<grid_for(ctx, num_parts, 256), 256, 0, st>>>(part_roots, num_parts);
+            ctx->launches += 1;
+        }
+        return check_cuda(cudaGetLastError(), "grouped bvh build");
     }
     if (ng * G >= (int64_t(1) << 30))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "bvh build: at most 2^30 - 1 triangles per hierarchy");
@@ -1054,7 +1104,7 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
         char* lq = q + 88 * ng + ng;
         lq += (256 - ((uintptr_t)lq & 255)) & 255;
         uint32_t* glist = reinterpret_cast<uint32_t*>(lq);
-        if (int s = launch_group_filter(ctx, gbox, ng, *filter, flags)) return s;
+        if (int s = launch_group_filter(ctx, gbox, ng, *filter, parts ? gt2o : nullptr, obj_part, flags)) return s;
         if (int s = select_flagged(ctx, flags, ng, glist, d_count)) return s;
         if (int s = host_value(ctx, d_count, 8, &n, "kept groups")) return s;
         list = glist;
@@ -1064,10 +1114,16 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
         shape->root_is_leaf = 1;
         shape->root_leaf_count = 0;
         shape->num_nodes = 0;
+        if (parts) {
+            k_fill_roots<<<grid_for(ctx, num_parts, 256), 256, 0, st>>>(part_roots, num_parts);
+            ctx->launches += 1;
+        }
         return check_cuda(cudaGetLastError(), "grouped bvh build");
     }
     BvhShape gshape;
-    if (int s = build_lbvh(ctx, gbox, gidx, gt2o, list, n, 1, gsoup, nodes, &gshape, nullptr)) return s;
+    if (int s = build_lbvh(ctx, gbox, gidx, gt2o, list, n, 1, gsoup, nodes, &gshape, nullptr,
+                           parts ? obj_part : nullptr, parts ? num_parts : 0, parts ? part_roots : nullptr))
+        return s;
     k_group_soup<<<grid_for(ctx, n * G, 256), 256, 0, st>>>(gsoup, n, G, chunk_list, verts, idx, t2o, nt, soup);
     ctx->launches += 1;
     if (gshape.root_is_leaf) {
@@ -1078,6 +1134,12 @@ int build_grouped_lbvh(pierce_ctx* ctx, const float* verts, const uint32_t* idx,
         k_group_leaves<<<grid_for(ctx, (int64_t)gshape.num_nodes, 256), 256, 0, st>>>(nodes,
                                                                                      (int64_t)gshape.num_nodes, G);
         ctx->launches += 1;
+    }
+    if (parts) {
+        k_group_roots<<<grid_for(ctx, num_parts, 256), 256, 0, st>>>(part_roots, num_parts, G);
+        ctx->launches += 1;
+    }
+    if (!gshape.root_is_leaf) {
         shape->root_is_leaf = 0;
         shape->root_leaf_count = 0;
         shape->num_nodes = gshape.num_nodes;
