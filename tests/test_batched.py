@@ -111,3 +111,28 @@ def test_partition_count_mismatch_is_rejected(ctx, case):
     B.set_partitions(concat(B_parts)["group"], 12)
     r = J.overlap_join(ctx, A, B)
     assert len(r.pairs) > 0
+
+
+@pytest.mark.parametrize("level,leaf", [(1, 4), (0, 8), (0, 4)])
+def test_partitions_by_object_equal_filtered_join(ctx, level, leaf):
+    """Objects dealt round-robin into 3 partitions of one dataset: the
+    partitioned join equals the unpartitioned join restricted to pairs
+    within one partition.  Level-0 meshes (20 triangles) with leaves of 8 put
+    groups across objects of different partitions, which takes the fallback
+    over the surviving triangles; the other cases take the group path."""
+    from pierce_gb300 import join as J
+    A = pg.icospheres(31, 300, level, hi=30.0)
+    B = pg.icospheres(32, 300, level, hi=30.0)
+    t = J.default_tuning(leaf_size=leaf)
+    for predicate in ("overlap", "intersection"):
+        da, db = J.Dataset.from_geometry(ctx, A, t), J.Dataset.from_geometry(ctx, B, t)
+        full = J.join(ctx, da, db, predicate=predicate).pairs
+        pa, pb = np.arange(A.num_objects) % 3, np.arange(B.num_objects) % 3
+        da.set_partitions(pa, 3)
+        db.set_partitions(pb, 3)
+        got = J.join(ctx, da, db, predicate=predicate).pairs
+        want = full[pa[full[:, 0]] == pb[full[:, 1]]]
+        assert np.array_equal(got, want), predicate
+        assert len(want) > 20
+        da.close()
+        db.close()
