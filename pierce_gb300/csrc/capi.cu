@@ -1876,7 +1876,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     const std::vector<int> rays = {32, 64, 128}, stacks = {8, 16, 32};
     const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
                                              : std::vector<double>{cur.hash_load_factor};
-    const std::vector<int> traversals = {0, 1};
+    const std::vector<int> traversals = {0, 1, 2};
     // coordinate descent: one parameter at a time, keeping the best so far
     for (int param = 0; param < 5; ++param) {
         const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()
