@@ -279,7 +279,8 @@ void pierce_result_destroy(pierce_result* r);
  * of the per-join hierarchies {1, 2, 4, 8} when base->active_bvh, rays per
  * warp {32, 64, 128}, stack depth {8, 16, 32}, hash load factor
  * {0.25, 0.5, 0.75} when the sizing uses a hash set, traversal {one ray per
- * thread, warp packets}), each trial the best
+ * thread over four-wide nodes, warp packets, one ray per thread over binary
+ * nodes}), each trial the best
  * of `repeats` timed runs after one untimed run.  *best receives the
  * fastest values; trials[0 .. *num_trials) every trial (max_trials slots,
  * may be NULL). */

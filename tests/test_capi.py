@@ -2,8 +2,11 @@
 (CPU only: no compute call is made)."""
 import ctypes as C
 import re
+import shutil
+import subprocess
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from pierce_gb300 import capi, native
@@ -54,3 +57,56 @@ def test_invalid_arguments_are_reported_without_a_device():
     d = C.c_void_p(16)  # never dereferenced: the size check comes first
     assert L.pierce_deduplicate_pairs_noalloc(d, capi.NOALLOC_MAX_PAIRS + 1, d, d, None) == \
         capi.ERR_INVALID_ARGUMENT
+
+
+def _c_layout(header: str, structs: dict[str, list[str]], tmp_path: Path) -> dict[str, dict]:
+    """sizeof and offsetof of each struct field as gcc lays them out from the header."""
+    lines = [f'#include "{header}"', "#include <stddef.h>", "#include <stdio.h>", "int main(void) {"]
+    for s, fields in structs.items():
+        lines.append(f'printf("{s} size %zu\\n", sizeof({s}));')
+        for f in fields:
+            lines.append(f'printf("{s} {f} %zu\\n", offsetof({s}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    exe = tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-std=c11", "-I", str(INCLUDE), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    layout: dict[str, dict] = {s: {} for s in structs}
+    for line in out.splitlines():
+        s, key, val = line.split()
+        layout[s][key] = int(val)
+    return layout
+
+
+def _py_layout(t) -> dict:
+    if isinstance(t, np.dtype):
+        out = {name: t.fields[name][1] for name in t.names}
+        out["size"] = t.itemsize
+        return out
+    out = {name: getattr(t, name).offset for name, _ in t._fields_}
+    out["size"] = C.sizeof(t)
+    return out
+
+
+def _names(t) -> list[str]:
+    return list(t.names) if isinstance(t, np.dtype) else [name for name, _ in t._fields_]
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
+def test_python_mirrors_match_the_c_struct_layouts(tmp_path):
+    from pierce_gb300 import geometry
+    mirrors = {
+        "pierce_capi.h": {
+            "pierce_mesh_view": capi.MeshView, "pierce_tuning": capi.Tuning,
+            "pierce_join_opts": capi.JoinOpts, "pierce_stats": capi.Stats,
+            "pierce_mlp_params": capi.MlpParams, "pierce_mlp_train_opts": capi.MlpTrainOpts,
+            "pierce_tuned": capi.Tuned, "pierce_dataset_info": capi.DatasetInfo,
+            "pierce_mesh_instance": capi.INSTANCE_DTYPE,
+        },
+        "pierce_host.h": {"pierce_geom_view": geometry.GeomView, "pierce_grid_entry": geometry.GRID_DTYPE},
+    }
+    for header, types in mirrors.items():
+        layout = _c_layout(header, {s: _names(t) for s, t in types.items()}, tmp_path)
+        for s, t in types.items():
+            assert _py_layout(t) == layout[s], s
