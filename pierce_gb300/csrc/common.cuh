@@ -98,8 +98,6 @@ struct DevDataset {
     int soup_boxes;     // the soup holds boxes as degenerate triangles (lo, hi, hi), not triangles
 };
 
-inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
-
 // Optional inputs of an edge-ray launch: a compacted ray list (object
 // culling) and the queue of deferred exact tests.
 struct RayOpts {
