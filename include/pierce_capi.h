@@ -23,6 +23,10 @@
  *                                    pierce/query/src/raytracing/MeshIntersectionLauncher.cpp:242-283
  *          MeshContainmentLauncher::launchPointInMesh
  *                                    pierce/query/src/raytracing/MeshContainmentLauncher.cpp:195-213
+ *   pierce_parity_tracking
+ *       <- PairHitTrackingBuffers / ContainmentTrackingBuffers (--enable-tracking)
+ *                                    pierce/query/src/utilities/PairHitTracking.h:31-110,
+ *                                    pierce/query/src/utilities/ContainmentTracking.h:22-95
  *   pierce_exclusive_scan
  *       <- exclusive_scan_gpu        pierce/query/src/cuda/scan_utils.h:6-9, scan_utils.cu:11-28
  *   pierce_merge_and_deduplicate_pairs
@@ -336,6 +340,26 @@ int pierce_launch_edge_rays(pierce_ctx* ctx, const pierce_dataset* src, const pi
 int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int precision,
                          int swap, uint64_t* d_table, uint32_t* d_parity, uint64_t table_slots,
                          pierce_stats* stats);
+/* Diagnostics of the parity rays (pierce_intersection --enable-tracking):
+ * the +Z ray from the first vertex of every object s of `src` against the
+ * objects of `tgt`, whose triangles must be stored object by object
+ * (objects_contiguous in pierce_dataset_info).  Host arrays, n = src's
+ * object count, any of them may be NULL:
+ *   target_ids[n * max_targets], target_hits[n * max_targets]: from
+ *     s * max_targets on, the target objects s's ray crosses an odd number
+ *     of times (s inside them by parity) and their crossing counts;
+ *     unused slots hold -1 and 0;
+ *   targets_crossed[n]: the target objects s's ray crosses at all;
+ *   overflows[n]: odd targets that found no slot.
+ * Objects without triangles trace no ray (all zero).  Partitioned datasets:
+ * targets of the source's partition only.  Synchronous.  Counterpart of
+ * the reference's pair-hit and containment tracking buffers
+ * (pierce/query/src/utilities/PairHitTracking.h:31-110,
+ * ContainmentTracking.h:22-95), filled by __raygen__mesh_containment_anyhit
+ * (pierce/query/src/cuda/mesh_intersection_anyhit.cu:108-146). */
+int pierce_parity_tracking(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int32_t max_targets,
+                           int32_t* target_ids, uint32_t* target_hits, uint32_t* targets_crossed,
+                           uint32_t* overflows);
 
 /* ---- helpers replacing the reference's extern "C" device helpers -------- */
 /* Exclusive scan of n int32 counts into int64 offsets; *total = sum. */

@@ -527,6 +527,54 @@ void parity_join(const float* first_vertices, int32_t nsrc, const Mesh& tgt, con
     for (auto& v : per) out.insert(out.end(), v.begin(), v.end());
 }
 
+// Crossing counts of the parity rays: for every source object s and target
+// object t that s's +Z ray crosses, the entry (s << 32 | t, crossings), in
+// key order.  The diagnostics of --enable-tracking list, per source, the
+// targets of odd count with their counts (mesh_intersection_anyhit.cu:108-146,
+// hit counts gathered by __anyhit__ah_containment :194-240).
+void parity_crossings(const float* first_vertices, int32_t nsrc, const Mesh& tgt, const Bvh& bvh,
+                      std::vector<uint64_t>& out) {
+    int nth = 1;
+#ifdef _OPENMP
+    nth = omp_get_max_threads();
+#endif
+    std::vector<std::vector<uint64_t>> per(nth);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int32_t s = 0; s < nsrc; ++s) {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        const P3 p{first_vertices[3 * s], first_vertices[3 * s + 1], first_vertices[3 * s + 2]};
+        std::vector<int32_t> hits;
+        bvh.query(
+            [&](const Box& b) {
+                return b.lo[0] <= p.x && p.x <= b.hi[0] && b.lo[1] <= p.y && p.y <= b.hi[1] && b.hi[2] >= p.z;
+            },
+            [&](uint64_t t) {
+                P3 a, b, c;
+                tgt.tri(t, a, b, c);
+                if (zray_crosses(p, a, b, c)) hits.push_back(tgt.obj[t]);
+            });
+        std::sort(hits.begin(), hits.end());
+        for (size_t i = 0; i < hits.size();) {
+            size_t j = i;
+            while (j < hits.size() && hits[j] == hits[i]) ++j;
+            per[tid].push_back(pack(s, hits[i]));
+            per[tid].push_back((uint64_t)(j - i));
+            i = j;
+        }
+    }
+    std::vector<std::pair<uint64_t, uint64_t>> all;
+    for (auto& v : per)
+        for (size_t i = 0; i < v.size(); i += 2) all.emplace_back(v[i], v[i + 1]);
+    std::sort(all.begin(), all.end());
+    for (auto& e : all) {
+        out.push_back(e.first);
+        out.push_back(e.second);
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ C interface --
@@ -606,6 +654,21 @@ uint64_t* oracle_parity_pairs(const float* first_vertices, int32_t nsrc, const f
     parity_join(first_vertices, nsrc, T, bvh, swap, keys);
     sort_unique(keys);
     return to_malloc(keys, n_out);
+}
+
+// Parity-ray crossing counts: 2 * *n_out words, (src << 32 | tgt, count)
+// per crossed (source, target) pair, in key order.
+uint64_t* oracle_parity_crossings(const float* first_vertices, int32_t nsrc, const float* tv, const uint32_t* ti,
+                                  const int32_t* to, uint64_t tnt, uint64_t* n_out) {
+    Mesh T{tv, ti, to, tnt};
+    Bvh bvh;
+    bvh.build(T);
+    std::vector<uint64_t> words;
+    parity_crossings(first_vertices, nsrc, T, bvh, words);
+    uint64_t n = 0;
+    uint64_t* out = to_malloc(words, &n);
+    *n_out = n / 2;
+    return out;
 }
 
 // Face baseline restated: for every A triangle, every B triangle whose box

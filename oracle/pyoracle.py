@@ -44,6 +44,8 @@ def lib() -> C.CDLL:
                                            C.c_int, C.c_int, C.POINTER(U64), C.POINTER(U64)]
         L.oracle_parity_pairs.restype = C.POINTER(C.c_uint64)
         L.oracle_parity_pairs.argtypes = [V, C.c_int32, V, V, V, U64, C.c_int, C.POINTER(U64)]
+        L.oracle_parity_crossings.restype = C.POINTER(C.c_uint64)
+        L.oracle_parity_crossings.argtypes = [V, C.c_int32, V, V, V, U64, C.POINTER(U64)]
         L.oracle_face_pairs.restype = C.POINTER(C.c_uint64)
         L.oracle_face_pairs.argtypes = [V, V, V, U64, V, V, V, U64, U64, U64, C.POINTER(U64)]
         L.oracle_free.argtypes = [V]
@@ -110,6 +112,19 @@ def parity_keys(first_vertices: np.ndarray, T, swap: int = 0) -> np.ndarray:
     n = U64()
     ptr = lib().oracle_parity_pairs(fv.ctypes.data, fv.shape[0], *gt, swap, C.byref(n))
     return _take(ptr, n.value)
+
+
+def parity_crossings(first_vertices: np.ndarray, T) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(source, target, crossings) of every target object the +Z ray from
+    each source first vertex crosses, sorted by (source, target)."""
+    fv = _f32(first_vertices).reshape(-1, 3)
+    gt, keep = _geom_args(T)
+    n = U64()
+    ptr = lib().oracle_parity_crossings(fv.ctypes.data, fv.shape[0], *gt, C.byref(n))
+    words = _take(ptr, 2 * n.value).reshape(-1, 2)
+    keys = words[:, 0]
+    return ((keys >> np.uint64(32)).astype(np.int32), (keys & np.uint64(0xFFFFFFFF)).astype(np.int32),
+            words[:, 1].astype(np.int64))
 
 
 def face_keys(A, B, tri_begin: int = 0, tri_end: int | None = None) -> np.ndarray:

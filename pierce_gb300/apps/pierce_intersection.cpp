@@ -2,9 +2,11 @@
 // directions, de-duplicated in one hash set.  Flags, stdout lines,
 // timing-JSON keys and the pairs CSV follow
 // pierce/query/src/applications/pierce_intersection_main.cpp:329-978.
+#include <algorithm>
 #include <fstream>
 #include <iostream>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "app_common.h"
@@ -53,6 +55,95 @@ struct Options : CliBase {
                    "Intersection join: overlapping surfaces or one object's first vertex inside the other.", o);
     }
 };
+// Tracked targets of one direction's parity rays (kMaxPairTargetsPerSource
+// slots per source object, as PairHitTrackingBuffers holds them).
+struct Tracking {
+    static constexpr int kSlots = 256;
+    int32_t num_sources = 0;
+    std::vector<int32_t> ids;
+    std::vector<uint32_t> hits, crossed, overflow, rays;
+};
+
+// pierce_parity_tracking for one direction; objects without triangles trace
+// no ray (iterations 0).  False (message on stderr) when the target's
+// objects are not stored contiguously.
+bool track(pierce_ctx* ctx, pierce_dataset* src, pierce_dataset* tgt, const HostDataset& src_host, Tracking& t) {
+    pierce_dataset_info info;
+    check(pierce_dataset_info_get(src, &info), "dataset info");
+    t.num_sources = std::max(info.num_objects, 0);
+    const size_t n = (size_t)t.num_sources;
+    t.ids.assign(n * Tracking::kSlots, -1);
+    t.hits.assign(n * Tracking::kSlots, 0);
+    t.crossed.assign(n, 0);
+    t.overflow.assign(n, 0);
+    t.rays.assign(n, 0);
+    for (uint64_t i = 0; i < src_host.view.num_mappings; ++i) {
+        const int32_t o = src_host.view.tri_to_object[i];
+        if (o >= 0 && (size_t)o < n) t.rays[o] = 1;
+    }
+    if (n == 0) return true;
+    const int s = pierce_parity_tracking(ctx, src, tgt, Tracking::kSlots, t.ids.data(), t.hits.data(),
+                                         t.crossed.data(), t.overflow.data());
+    if (s != PIERCE_OK) {
+        std::cerr << "Tracking unavailable: " << pierce_last_error() << std::endl;
+        return false;
+    }
+    return true;
+}
+
+inline unsigned long long pair_key(int32_t a, int32_t b) {
+    return ((unsigned long long)(uint32_t)a << 32) | (uint32_t)b;
+}
+
+// The two tracking CSVs of pierce_intersection_main.cpp:425-539: every
+// tracked (odd-parity) target with its crossing count and whether the pair
+// is in the result, then one summary row per source object.  Crossing
+// counts follow the exact parity rule (each triangle the ray crosses under
+// the symbolic perturbation counts once); candidate_count is the number of
+// target objects the ray crosses (no list cap), candidate_overflow_events
+// the odd targets beyond the 256 slots.
+void write_tracking(const std::string& hits_path, const std::string& track_path, const Tracking& t12,
+                    const Tracking& t21, const std::vector<pierce_pair>& pairs) {
+    std::unordered_set<unsigned long long> final_pairs;
+    final_pairs.reserve(2 * pairs.size() + 1);
+    for (const auto& p : pairs) final_pairs.insert(pair_key(p.a, p.b));
+    const Tracking* dirs[2] = {&t12, &t21};
+    const char* names[2] = {"mesh1_to_mesh2", "mesh2_to_mesh1"};
+    auto is_final = [&](int d, int32_t src, int32_t tgt) {
+        return final_pairs.count(d == 0 ? pair_key(src, tgt) : pair_key(tgt, src)) > 0;
+    };
+    std::ofstream h(hits_path);
+    h << "direction,source_object_id,target_object_id,target_ray_hits,final_pair\n";
+    for (int d = 0; d < 2; ++d) {
+        const Tracking& t = *dirs[d];
+        for (int32_t s = 0; s < t.num_sources; ++s)
+            for (int i = 0; i < Tracking::kSlots; ++i) {
+                const size_t at = (size_t)s * Tracking::kSlots + i;
+                if (t.ids[at] < 0) continue;
+                h << names[d] << ',' << s << ',' << t.ids[at] << ',' << t.hits[at] << ','
+                  << (is_final(d, s, t.ids[at]) ? 1 : 0) << "\n";
+            }
+    }
+    std::ofstream c(track_path);
+    c << "direction,source_object_id,iterations,candidate_count,tracked_target_count,tracked_hit_total,"
+         "candidate_overflow_events,final_pair_count,tracked_final_pair_count\n";
+    for (int d = 0; d < 2; ++d) {
+        const Tracking& t = *dirs[d];
+        for (int32_t s = 0; s < t.num_sources; ++s) {
+            int tracked = 0, tracked_final = 0;
+            unsigned long long hit_total = 0;
+            for (int i = 0; i < Tracking::kSlots; ++i) {
+                const size_t at = (size_t)s * Tracking::kSlots + i;
+                if (t.ids[at] < 0) continue;
+                ++tracked;
+                hit_total += t.hits[at];
+                if (is_final(d, s, t.ids[at])) ++tracked_final;
+            }
+            c << names[d] << ',' << s << ',' << t.rays[s] << ',' << t.crossed[s] << ',' << tracked << ','
+              << hit_total << ',' << t.overflow[s] << ',' << tracked_final << ',' << tracked_final << "\n";
+        }
+    }
+}
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -183,31 +274,36 @@ int main(int argc, char** argv) {
     std::vector<pierce_pair> pairs = download(ctx, r);
     pierce_result_destroy(r);
     write_pairs_csv(pairs_path, "a_object_id,b_object_id", pairs);
+    bool tracked = false;
     if (opt.tracking) {
-        // Per-object summaries of the final pair set: how many partners each
-        // object has on the other side.
-        std::vector<unsigned> deg1((size_t)m1.view.num_objects, 0), deg2((size_t)m2.view.num_objects, 0);
-        for (const auto& p : pairs) {
-            if (p.a >= 0 && (size_t)p.a < deg1.size()) deg1[p.a]++;
-            if (p.b >= 0 && (size_t)p.b < deg2.size()) deg2[p.b]++;
-        }
-        std::ofstream h(hits_path);
-        h << "source_mesh,source_object_id,target_object_id,in_final_pairs\n";
-        for (const auto& p : pairs) h << "mesh1," << p.a << "," << p.b << ",1\n";
-        std::ofstream c(track_path);
-        c << "source_mesh,source_object_id,final_pair_count\n";
-        for (size_t i = 0; i < deg1.size(); ++i) c << "mesh1," << i << "," << deg1[i] << "\n";
-        for (size_t i = 0; i < deg2.size(); ++i) c << "mesh2," << i << "," << deg2[i] << "\n";
+        // both directions' parity rays, as the reference copies both
+        // directions' tracking buffers whatever the query direction
+        Tracking t12, t21;
+        tracked = track(ctx, g1.ds, g2.ds, m1, t12) && track(ctx, g2.ds, g1.ds, m2, t21);
+        if (tracked) write_tracking(hits_path, track_path, t12, t21, pairs);
     }
     std::cout << "Intersection pairs CSV: " << pairs_path << std::endl;
-    if (opt.tracking) {
+    if (tracked) {
         std::cout << "Pair hit tracking CSV: " << hits_path << std::endl;
         std::cout << "Containment tracking CSV: " << track_path << std::endl;
     }
     if (opt.profiling) {
+        // Counters of MeshIntersectionProfilingStats (mesh_intersection.h:7-22,
+        // pierce_intersection_main.cpp:924-948) that this design has: one
+        // traversal per edge ray collects all its hits, so iterations equal
+        // rays; no hit is suppressed and no candidate list overflows.
+        const unsigned long long it_x1000 = st.rays ? 1000ull : 0ull, pit_x1000 = st.parity_rays ? 1000ull : 0ull;
         timer.add_counter("Profile_Overlap_Trace_Calls", st.rays);
+        timer.add_counter("Profile_Overlap_Iterations_Total", st.rays);
         timer.add_counter("Profile_Overlap_Hits_Total", st.raw_hits);
+        timer.add_counter("Profile_Overlap_Max_Iterations_Per_Trace", st.rays ? 1 : 0);
         timer.add_counter("Profile_Containment_Rays_Total", st.parity_rays);
+        timer.add_counter("Profile_Containment_Iterations_Total", st.parity_rays);
+        timer.add_counter("Profile_Containment_Max_Iterations_Per_Ray", st.parity_rays ? 1 : 0);
+        timer.add_counter("Profile_Containment_Same_Hit_Suppressed", 0);
+        timer.add_counter("Profile_Containment_Candidate_Overflow", 0);
+        timer.add_counter("Profile_Overlap_Avg_Iterations_x1000", it_x1000);
+        timer.add_counter("Profile_Containment_Avg_Iterations_x1000", pit_x1000);
         timer.add_counter("Profile_Node_Visits", st.node_visits);
         timer.add_counter("Profile_Triangle_Tests", st.tri_tests);
         timer.add_counter("Profile_Fp32_Ambiguous", st.fp32_ambiguous);

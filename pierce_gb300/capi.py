@@ -152,6 +152,7 @@ SIGNATURES = {
     "pierce_launch_edge_rays": (C.c_int, [V, V, V, C.c_int, C.c_int, C.c_int, V, V, V, V, U64,
                                           C.POINTER(Stats)]),
     "pierce_launch_parity": (C.c_int, [V, V, V, C.c_int, C.c_int, V, V, U64, C.POINTER(Stats)]),
+    "pierce_parity_tracking": (C.c_int, [V, V, V, I32, V, V, V, V]),
     "pierce_exclusive_scan": (C.c_int, [V, V, V, I64, C.POINTER(I64)]),
     "pierce_merge_and_deduplicate_pairs": (C.c_int, [V, V, I64, V, I64, V, C.POINTER(I64)]),
     "pierce_compact_hash_table_pairs": (C.c_int, [V, V, U64, V, U64, C.POINTER(U64)]),

@@ -37,6 +37,8 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
                   uint32_t* parity, uint64_t slots);
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
                           const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
+int launch_parity_tracking(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, const ColumnGrid& grid,
+                           int32_t k, int32_t* ids, uint32_t* hits, uint32_t* crossed, uint32_t* overflow);
 size_t column_grid_bytes(int32_t n);
 int column_grid_count(pierce_ctx* ctx, const DevDataset& tgt, void* mem, const int32_t** d_total);
 int column_grid_fill(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int32_t* entries, ColumnGrid* g);
@@ -2190,6 +2192,63 @@ int pierce_launch_parity(pierce_ctx* ctx, const pierce_dataset* src, const pierc
     }
     if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
     if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "parity table full");
+    return PIERCE_OK;
+}
+
+int pierce_parity_tracking(pierce_ctx* ctx, const pierce_dataset* src, const pierce_dataset* tgt, int32_t max_targets,
+                           int32_t* target_ids, uint32_t* target_hits, uint32_t* targets_crossed,
+                           uint32_t* overflows) {
+    if (!ctx || !src || !tgt || max_targets < 1 || max_targets > (1 << 16))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "parity_tracking: bad argument");
+    if (src->num_parts != tgt->num_parts)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "parity_tracking: datasets have different partition counts");
+    if (tgt->num_objects > 0 && !tgt->contiguous)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT,
+                         "parity_tracking: the target's objects do not store their triangles contiguously");
+    const int64_t n = src->num_objects;
+    if (n <= 0) return PIERCE_OK;
+    cudaSetDevice(ctx->device);
+    ++ctx->scratch_gen;
+    const DevDataset vs = src->view(), vt = tgt->view();
+    // candidates: the column grid of the target's object boxes
+    void* meta = nullptr;
+    if (int s = scratch(ctx, SLOT_GRID_B, column_grid_bytes(tgt->num_objects), &meta)) return s;
+    const int32_t* d_total = nullptr;
+    if (int s = column_grid_count(ctx, vt, meta, &d_total)) return s;
+    int64_t entries = 0;
+    if (int s = host_value(ctx, d_total, 4, &entries, "column grid size")) return s;
+    void* pe = nullptr;
+    if (int s = scratch(ctx, SLOT_GRID_B_ENTRIES, 4 * (size_t)std::max<int64_t>(entries, 1), &pe)) return s;
+    ColumnGrid grid{};
+    if (int s = column_grid_fill(ctx, vt, meta, static_cast<int32_t*>(pe), &grid)) return s;
+    // ids and hits (max_targets slots per source object), then crossed and overflow
+    const size_t slots = (size_t)n * (size_t)max_targets;
+    void* d = nullptr;
+    if (int s = device_alloc(&d, 8 * slots + 8 * (size_t)n, "parity tracking")) return s;
+    int32_t* ids = static_cast<int32_t*>(d);
+    uint32_t* hits = reinterpret_cast<uint32_t*>(ids + slots);
+    uint32_t* crossed = hits + slots;
+    uint32_t* overflow = crossed + n;
+    cudaStream_t st = ctx->stream;
+    int s = check_cuda(cudaMemsetAsync(ids, 0xFF, 4 * slots, st), "parity tracking");
+    if (!s) s = check_cuda(cudaMemsetAsync(hits, 0, 4 * slots + 8 * (size_t)n, st), "parity tracking");
+    if (!s) s = launch_parity_tracking(ctx, vs, vt, grid, max_targets, ids, hits, crossed, overflow);
+    if (!s && target_ids)
+        s = check_cuda(cudaMemcpyAsync(target_ids, ids, 4 * slots, cudaMemcpyDeviceToHost, st), "parity tracking");
+    if (!s && target_hits)
+        s = check_cuda(cudaMemcpyAsync(target_hits, hits, 4 * slots, cudaMemcpyDeviceToHost, st), "parity tracking");
+    if (!s && targets_crossed)
+        s = check_cuda(cudaMemcpyAsync(targets_crossed, crossed, 4 * (size_t)n, cudaMemcpyDeviceToHost, st),
+                       "parity tracking");
+    if (!s && overflows)
+        s = check_cuda(cudaMemcpyAsync(overflows, overflow, 4 * (size_t)n, cudaMemcpyDeviceToHost, st),
+                       "parity tracking");
+    uint32_t bits = 0;
+    if (!s) s = read_device_error(ctx, &bits);  // synchronises the stream
+    cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (s) return s;
+    if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
     return PIERCE_OK;
 }
 

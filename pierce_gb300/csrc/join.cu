@@ -1402,8 +1402,19 @@ struct ParityObjParams {
     uint64_t mask;
     uint32_t* err;
     DevCounters* ctr;
+    // k_parity_objects<true> (diagnostics) writes, instead of table entries,
+    // per source object s: the targets its ray crosses an odd number of times
+    // with their crossing counts (slots s * track_k ..., in candidate order),
+    // the number of targets it crosses at all, and the odd targets that found
+    // no slot
+    int32_t track_k;
+    int32_t* track_ids;
+    uint32_t* track_hits;
+    uint32_t* track_crossed;
+    uint32_t* track_overflow;
 };
 
+template <bool TRACK>
 __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -1415,9 +1426,11 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
         if (fv.w != 0.0f) continue;  // object without triangles (warp-uniform)
         ++n_rays;
         const float3 p = make_float3(fv.x, fv.y, fv.z);
+        uint32_t n_crossed = 0, n_odd = 0;  // TRACK: lane 0's tallies of this source
         auto candidate = [&](int32_t t) {
             const int2 r = __ldg(P.tgt.obj_range + t);
             uint32_t crossings = 0;
+            uint32_t ncross = 0;  // TRACK: this lane's crossings
             auto test = [&](int64_t tri) {
                 const uint32_t i0 = __ldg(P.tgt.idx + 3 * tri), i1 = __ldg(P.tgt.idx + 3 * tri + 1),
                                i2 = __ldg(P.tgt.idx + 3 * tri + 2);
@@ -1432,7 +1445,10 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                     fmaxf(a.z, fmaxf(b.z, c.z)) < p.z)
                     return;
                 ++n_tests;
-                if (zray_cross(p, a, b, c, pc)) crossings ^= 1u;
+                if (zray_cross(p, a, b, c, pc)) {
+                    crossings ^= 1u;
+                    if constexpr (TRACK) ++ncross;
+                }
             };
             if (P.tgt.tri_chunk_box) {
                 // only the 32-triangle chunks whose box the ray's column meets
@@ -1458,11 +1474,32 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                 for (int k = lane; k < r.y; k += 32) test((int64_t)r.x + k);
             }
             const unsigned odd = __popc(__ballot_sync(0xFFFFFFFFu, crossings != 0)) & 1u;
-            if (odd && lane == 0) {
+            if constexpr (TRACK) {
+                const uint32_t hits = __reduce_add_sync(0xFFFFFFFFu, ncross);
+                if (hits && lane == 0) {
+                    ++n_crossed;
+                    if (odd) {
+                        if (n_odd < (uint32_t)P.track_k) {
+                            const int64_t at = s * (int64_t)P.track_k + n_odd;
+                            P.track_ids[at] = t;
+                            P.track_hits[at] = hits;
+                        }
+                        ++n_odd;
+                    }
+                }
+            } else if (odd && lane == 0) {
                 const uint64_t key = P.swap ? pack_key(t, (int32_t)s) : pack_key((int32_t)s, t);
                 uint32_t probes = 0;
                 const int64_t slot = hash_insert(P.table, P.mask, key, P.err, probes);
                 if (slot >= 0) P.parity[slot] = 1u;  // one warp owns the keys of its source object
+            }
+        };
+        auto finish = [&]() {
+            if constexpr (TRACK) {
+                if (lane == 0) {
+                    P.track_crossed[s] = n_crossed;
+                    P.track_overflow[s] = n_odd > (uint32_t)P.track_k ? n_odd - (uint32_t)P.track_k : 0u;
+                }
             }
         };
         auto leaf = [&](int first, int count) {
@@ -1489,12 +1526,14 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                     __ldg(ob + 5) >= p.z)
                     candidate(t);
             }
+            finish();
             continue;
         }
         int first, count;
         int node = traversal_start(P.src, P.objs, (int32_t)s, first, count);
         if (node < 0) {
             leaf(first, count);
+            finish();
             continue;
         }
         int stack[kStackSize];
@@ -1530,6 +1569,7 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
                 node = stack[--sp];
             }
         }
+        finish();
     }
     // per-lane test and ambiguity counts; rays and node visits once per warp
     flush_counter(&P.ctr->tri_tests, n_tests);
@@ -1610,12 +1650,48 @@ int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDatas
     P.mask = slots - 1;
     P.err = ctx->d_err;
     P.ctr = ctx->d_counters;
+    P.track_k = 0;
+    P.track_ids = nullptr;
+    P.track_hits = nullptr;
+    P.track_crossed = nullptr;
+    P.track_overflow = nullptr;
     const int64_t warps = src.num_objects;
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
                                                                              (int64_t)ctx->sm_count * 32));
-    k_parity_objects<<<blocks, 128, 0, ctx->stream>>>(P);
+    k_parity_objects<false><<<blocks, 128, 0, ctx->stream>>>(P);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "parity (object pairs) kernel");
+}
+
+// Parity-ray diagnostics of src's objects against tgt over tgt's column
+// grid: ids[src.num_objects * k] (preset to -1 by the caller), hits (same
+// shape), crossed and overflow (src.num_objects each; entries of objects
+// without triangles are left as they are).
+int launch_parity_tracking(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, const ColumnGrid& grid,
+                           int32_t k, int32_t* ids, uint32_t* hits, uint32_t* crossed, uint32_t* overflow) {
+    if (src.num_objects <= 0 || !tgt.obj_range || grid.nx <= 0) return PIERCE_OK;
+    ParityObjParams P;
+    P.src = src;
+    P.grid = grid;
+    P.objs = DevDataset{};
+    P.tgt = tgt;
+    P.swap = 0;
+    P.table = nullptr;
+    P.parity = nullptr;
+    P.mask = 0;
+    P.err = ctx->d_err;
+    P.ctr = ctx->d_counters;
+    P.track_k = k;
+    P.track_ids = ids;
+    P.track_hits = hits;
+    P.track_crossed = crossed;
+    P.track_overflow = overflow;
+    const int64_t warps = src.num_objects;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
+                                                                             (int64_t)ctx->sm_count * 32));
+    k_parity_objects<true><<<blocks, 128, 0, ctx->stream>>>(P);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "parity tracking kernel");
 }
 
 int compact_table(pierce_ctx* ctx, const uint64_t* table, uint64_t slots, uint64_t* out, uint64_t cap,

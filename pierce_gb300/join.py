@@ -187,6 +187,34 @@ class Dataset:
 
 
 @dataclass
+class ParityTracking:
+    """Parity-ray diagnostics of one direction (source objects against
+    target objects), per source object s: ids[s, :] the targets its +Z ray
+    crosses an odd number of times (-1 in unused slots), hits[s, :] their
+    crossing counts, crossed[s] the targets it crosses at all, overflow[s]
+    the odd targets beyond the slots."""
+    ids: np.ndarray        # (n, max_targets) int32
+    hits: np.ndarray       # (n, max_targets) uint32
+    crossed: np.ndarray    # (n,) uint32
+    overflow: np.ndarray   # (n,) uint32
+
+
+def parity_tracking(ctx: Context, src: Dataset, tgt: Dataset, max_targets: int = 256) -> ParityTracking:
+    """The parity rays of src's objects against tgt's, as the reference's
+    --enable-tracking buffers hold them (pierce_parity_tracking)."""
+    n = max(src.info().num_objects, 0)
+    ids = np.full((n, max_targets), -1, np.int32)
+    hits = np.zeros((n, max_targets), np.uint32)
+    crossed = np.zeros(n, np.uint32)
+    overflow = np.zeros(n, np.uint32)
+    if n:
+        check(capi.lib().pierce_parity_tracking(ctx.handle, src.handle, tgt.handle, int(max_targets),
+                                                ids.ctypes.data, hits.ctypes.data, crossed.ctypes.data,
+                                                overflow.ctypes.data), "parity_tracking")
+    return ParityTracking(ids, hits, crossed, overflow)
+
+
+@dataclass
 class JoinResult:
     pairs: np.ndarray          # (n, 2) int32, sorted by (a, b)
     stats: dict

@@ -221,3 +221,43 @@ def test_direction_split_and_swap():
     rev, _ = O.overlap_keys(B, A)
     swapped = np.sort((rev << np.uint64(32)) | (rev >> np.uint64(32)))
     assert np.array_equal(both, swapped)
+
+
+def _lattice_cube(lo, hi, obj):
+    """Closed lattice cube [lo, hi]^3 as 12 triangles of object `obj`."""
+    v = np.array([[x, y, z] for x in (lo, hi) for y in (lo, hi) for z in (lo, hi)], np.float32)
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    tris = []
+    for a, b, c, d in faces:
+        tris += [(a, b, c), (a, c, d)]
+    return v, np.array(tris, np.uint32), np.full(12, obj, np.int32)
+
+
+def test_parity_crossing_counts_of_nested_cubes():
+    """Crossing counts of the parity rays (the --enable-tracking hit counts):
+    a ray from inside the inner of two nested cubes crosses each once, one
+    from below both crosses each twice, one between them crosses the outer
+    once and the inner not at all."""
+    v0, i0, o0 = _lattice_cube(0, 8, 0)
+    v1, i1, o1 = _lattice_cube(2, 6, 1)
+    T = pg.Geometry.from_arrays(np.concatenate([v0, v1]), np.concatenate([i0, i1 + len(v0)]),
+                                np.concatenate([o0, o1]))
+    points = np.array([[3, 3, 3], [3, 3, -1], [1, 1, 1], [7, 7, 9], [3, 3, 7]], np.float32)
+    src, tgt, hits = O.parity_crossings(points, T)
+    got = {(int(s), int(t)): int(h) for s, t, h in zip(src, tgt, hits)}
+    assert got == {(0, 0): 1, (0, 1): 1, (1, 0): 2, (1, 1): 2, (2, 0): 1, (4, 0): 1}
+
+
+def test_parity_crossing_counts_agree_with_parity_pairs():
+    """Targets of odd crossing count are exactly the parity pairs, in both
+    directions of a dataset pair with nested and touching ellipsoids."""
+    A, B = pg.ellipsoid_pair(41, 42, 150, 150, 2, lo=0, hi=60, frac_inside=0.3, frac_contact=0.05)
+    for S, T in ((A, B), (B, A)):
+        fv = S.first_vertices()
+        src, tgt, hits = O.parity_crossings(fv, T)
+        assert np.all(hits >= 1)
+        keys = (src.astype(np.uint64) << np.uint64(32)) | tgt.astype(np.uint64)
+        assert np.all(np.diff(keys.astype(np.int64)) > 0)  # unique, sorted by (source, target)
+        odd = keys[(hits & 1) == 1]
+        assert np.array_equal(odd, O.parity_keys(fv, T, swap=0))
+    assert (hits & 1).sum() > 10
