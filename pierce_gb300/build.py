@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["pre_io.cpp", "edges.cpp", "generators.cpp", "host_capi.cpp"]
 CUDA_SOURCES = ["lbvh.cu", "join.cu", "sortscan.cu", "capi.cu", "instanced.cu", "sizing.cu", "noalloc.cu"]
-APP_COMMON = ["cli.cpp", "timer.cpp", "app_common.cpp"]
+APP_COMMON = ["cli.cpp", "timer.cpp", "app_common.cpp", "tracking_csv.cpp"]
 APPS = ["pierce_overlap", "pierce_overlap_two_pass", "pierce_intersection",
         "pierce_containment", "pierce_preprocess"]
 

@@ -170,3 +170,59 @@ def test_containment_executable(pre_files, include):
         assert np.array_equal(keys_of_csv(d / "mesh_containment_results.csv"), cont)
     phases = json.loads((d / "c.json").read_text())["phases"]
     assert "compact_hash_table_pairs (containment)_1" in phases
+
+
+HARNESS = r"""
+#include "tracking_csv.h"
+static Tracking make(int n) {
+    Tracking t;
+    t.num_sources = n;
+    t.ids.assign((size_t)n * Tracking::kSlots, -1);
+    t.hits.assign((size_t)n * Tracking::kSlots, 0);
+    t.crossed.assign(n, 0);
+    t.overflow.assign(n, 0);
+    t.rays.assign(n, 0);
+    return t;
+}
+int main(int argc, char** argv) {
+    if (argc < 3) return 2;
+    Tracking a = make(3), b = make(2);
+    a.ids[0] = 5; a.hits[0] = 1; a.ids[1] = 7; a.hits[1] = 3; a.overflow[0] = 1;
+    a.crossed = {4, 2, 0}; a.rays = {1, 1, 0};
+    b.ids[0] = 0; b.hits[0] = 1; b.crossed = {1, 0}; b.rays = {1, 1};
+    std::vector<pierce_pair> pairs = {{0, 5}, {0, 0}, {2, 2}};
+    return write_tracking(argv[1], argv[2], a, b, pairs) ? 0 : 1;
+}
+"""
+
+
+def test_tracking_csv_writer(tmp_path):
+    """The --enable-tracking CSVs from given tracking tables (no device):
+    final_pair looks the pair up as (source, target) for mesh1's rays and
+    (target, source) for mesh2's."""
+    from pierce_gb300 import build as B
+    B.build(verbose=False)
+    src = tmp_path / "harness.cpp"
+    src.write_text(HARNESS)
+    exe = tmp_path / "harness"
+    apps = Path(B.__file__).resolve().parent / "apps"
+    subprocess.run(["g++", "-std=c++17", "-I", str(apps), str(src), str(LIB / "obj" / "tracking_csv.host.o"),
+                    "-o", str(exe)], check=True)
+    subprocess.run([str(exe), str(tmp_path / "hits.csv"), str(tmp_path / "track.csv")], check=True)
+    assert (tmp_path / "hits.csv").read_text().splitlines() == [
+        "direction,source_object_id,target_object_id,target_ray_hits,final_pair",
+        "mesh1_to_mesh2,0,5,1,1",
+        "mesh1_to_mesh2,0,7,3,0",
+        "mesh2_to_mesh1,0,0,1,1",
+    ]
+    assert (tmp_path / "track.csv").read_text().splitlines() == [
+        "direction,source_object_id,iterations,candidate_count,tracked_target_count,tracked_hit_total,"
+        "candidate_overflow_events,final_pair_count,tracked_final_pair_count",
+        "mesh1_to_mesh2,0,1,4,2,4,1,1,1",
+        "mesh1_to_mesh2,1,1,2,0,0,0,0,0",
+        "mesh1_to_mesh2,2,0,0,0,0,0,0,0",
+        "mesh2_to_mesh1,0,1,1,1,1,0,1,1",
+        "mesh2_to_mesh1,1,1,0,0,0,0,0,0",
+    ]
+    bad = subprocess.run([str(exe), str(tmp_path / "missing" / "h.csv"), str(tmp_path / "t.csv")])
+    assert bad.returncode == 1
