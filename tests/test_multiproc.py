@@ -1,4 +1,5 @@
-"""bench.py's multi-rank aggregation with world_size 2 over gloo (CPU)."""
+"""bench.py on the CPU: multi-rank aggregation with world_size 2 over gloo,
+and the reference arm's JSON line."""
 import os
 import socket
 import sys
@@ -48,3 +49,24 @@ def test_max_over_ranks_single_process():
     sys.path.insert(0, str(ROOT))
     import bench
     assert bench.max_over_ranks(3.5, None) == 3.5
+
+
+def test_reference_arm_json_line():
+    """bench.py --impl reference (the oracle port on the host cores, no GPU)
+    prints one JSON line of the bench contract on a small workload."""
+    import json
+    import subprocess
+    root = ROOT
+    p = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--scale", "0.02",
+                        "--steps", "1", "--warmup", "0", "--cpu-sample-objects", "200"],
+                       capture_output=True, text=True, cwd=root, timeout=600)
+    assert p.returncode == 0, p.stderr
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "join queries/s"
+    assert d["higher_is_better"] is True and d["n_gpus"] == 1 and d["steps"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["meshes_per_side"] == 1000
