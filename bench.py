@@ -517,6 +517,69 @@ def main_tubes(args):
     return 0
 
 
+def main_preprocess(args):
+    """Edge extraction of the `.pre` producer (host code, no GPU): read a
+    `.pre` file, extract the unique per-object edges in the reference's map
+    order, write the file.  This repository's extractor (all host threads,
+    and one thread) against the reference's own EdgePreprocessor::extractEdges
+    with its BinaryIO reader and writer, compiled from the reference sources
+    into oracle/_ref/ref_pre_tool where they are present.  Workload: side A
+    of the plain overlap configuration, 2,000 level-3 icospheres (2.56 M
+    triangles, 3.84 M unique edges)."""
+    import pierce_gb300 as pg
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    n = max(10, int(round(2000 * args.scale)))
+    G = pg.icospheres(2024, n, 3, hi=200.0 * args.scale ** (1.0 / 3.0))
+    tris = G.num_triangles
+    work = Path(tempfile.mkdtemp(prefix="pierce_pre_"))
+    src = work / "in.pre"
+    G.write_pre(src)
+
+    def ours(threads):
+        t0 = time.perf_counter()
+        H = pg.Geometry.read_pre(src)
+        H.extract_edges(0, threads)
+        H.write_pre(work / "ours.pre")
+        return time.perf_counter() - t0
+
+    def reference():
+        tool = ROOT / "oracle" / "_ref" / "ref_pre_tool"
+        if not tool.exists():
+            return None
+        t0 = time.perf_counter()
+        r = subprocess.run([str(tool), str(src), str(work / "ref.pre")], capture_output=True, text=True)
+        if r.returncode != 0:
+            return None
+        return time.perf_counter() - t0
+
+    for _ in range(max(args.warmup, 0)):
+        ours(0)
+    t_all = min(ours(0) for _ in range(max(args.steps, 1)))
+    t_one = min(ours(1) for _ in range(max(args.steps, 1)))
+    ref = [reference() for _ in range(max(args.steps, 1))]
+    t_ref = None if any(r is None for r in ref) else min(ref)
+    identical = None
+    if t_ref is not None:
+        a, b = (work / "ref.pre").read_bytes(), (work / "ours.pre").read_bytes()
+        identical = len(a) == len(b) and a[:50] == b[:50] and a[56:] == b[56:]  # header padding excluded
+    threads = os.cpu_count() or 1
+    log(f"preprocess: {tris} triangles; ours {t_all:.3f} s ({threads} threads), {t_one:.3f} s (1 thread); "
+        f"reference {t_ref if t_ref is None else round(t_ref, 3)} s; identical {identical}")
+    line = {"metric": "edge extraction of the .pre producer (read, extract, write)", "unit": "triangles/s",
+            "value": tris / t_all, "value_one_thread": tris / t_one, "threads": threads,
+            "reference": None if t_ref is None else {"value": tris / t_ref, "threads": 1,
+                                                     "kind": "reference (EdgePreprocessor, BinaryIO)"},
+            "byte_identical_to_reference": identical, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": "pre-edge-extraction", "meshes": n, "subdivision": 3,
+                       "triangles": tris, "edges": G.num_edges, "seed": 2024}}
+    print(json.dumps(line))
+    for f in ("in.pre", "ours.pre", "ref.pre"):
+        (work / f).unlink(missing_ok=True)
+    work.rmdir()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -528,9 +591,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf-size", type=int, default=4, help="leaf size of the tuned form's per-join hierarchies")
     ap.add_argument("--plain-leaf-size", type=int, default=8, help="leaf size of the plain form's dataset hierarchies")
-    ap.add_argument("--workload", default="ellipsoids", choices=["ellipsoids", "batched", "tubes"],
+    ap.add_argument("--workload", default="ellipsoids", choices=["ellipsoids", "batched", "tubes", "preprocess"],
                     help="ellipsoids: the default intersection+containment line; batched: 4,096 overlap queries; "
-                         "tubes: 2,000 tubes against 100,000 ellipsoids")
+                         "tubes: 2,000 tubes against 100,000 ellipsoids; preprocess: edge extraction of the "
+                         ".pre producer on the host cores")
     ap.add_argument("--cpu-sample-tubes", type=int, default=10)
     ap.add_argument("--wave-tris", type=float, default=1.0e9, help="batched: triangles per wave (both sides)")
     args = ap.parse_args()
@@ -540,6 +604,8 @@ def main():
         return main_batched(args)
     if args.workload == "tubes":
         return main_tubes(args)
+    if args.workload == "preprocess":
+        return main_preprocess(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -96,8 +96,11 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
     const uint64_t nv = g.num_vertices();
     if (nt == 0 || nv == 0 || g.tri_to_object.size() != nt) return;
 
+    // Thread count of this call only (the process-wide OpenMP setting stays
+    // as it is): num_threads > 0, else every thread OpenMP offers.
+    int nthreads = 1;
 #ifdef _OPENMP
-    if (num_threads > 0) omp_set_num_threads(num_threads);
+    nthreads = num_threads > 0 ? num_threads : omp_get_max_threads();
 #else
     (void)num_threads;
 #endif
@@ -130,13 +133,9 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
         int arena;
         uint64_t offset, count;
     };
-    int nthreads = 1;
-#ifdef _OPENMP
-    nthreads = omp_get_max_threads();
-#endif
     std::vector<std::vector<Ref>> arenas(nthreads);
     std::vector<Slot> slots(nobj);
-#pragma omp parallel
+#pragma omp parallel num_threads(nthreads)
     {
         int tid = 0;
 #ifdef _OPENMP
@@ -180,7 +179,7 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
     for (int64_t o = 0; o < nobj; ++o) off[o + 1] = off[o] + slots[o].count;
     const uint64_t ne = off[nobj];
     std::vector<Ref> all(ne);
-#pragma omp parallel for schedule(dynamic, 64)
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
     for (int64_t o = 0; o < nobj; ++o) {
         const Slot& s = slots[o];
         if (s.count)
@@ -191,7 +190,7 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
     if (order == 0) {
         // Global key order: rebuild keys for the unique edges and sort them.
         std::vector<EdgeRec> keyed(ne);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nthreads)
         for (int64_t i = 0; i < (int64_t)ne; ++i) {
             const Ref& r = all[i];
             const uint32_t* tri = &g.indices[3 * r.tri];
@@ -209,18 +208,19 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
             k.tri = r.tri;
         }
 #ifdef _OPENMP
-        __gnu_parallel::sort(keyed.begin(), keyed.end(), key_less);
+        __gnu_parallel::sort(keyed.begin(), keyed.end(), key_less,
+                             __gnu_parallel::default_parallel_tag((__gnu_parallel::_ThreadIndex)nthreads));
 #else
         std::sort(keyed.begin(), keyed.end(), key_less);
 #endif
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nthreads)
         for (int64_t i = 0; i < (int64_t)ne; ++i) all[i] = Ref{keyed[i].tri, keyed[i].corner, keyed[i].obj};
     }
 
     g.edge_starts.resize(3 * ne);
     g.edge_ends.resize(3 * ne);
     g.edge_src.resize(ne);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nthreads)
     for (int64_t i = 0; i < (int64_t)ne; ++i) {
         const Ref& r = all[i];
         const uint32_t* tri = &g.indices[3 * r.tri];

@@ -143,3 +143,22 @@ def test_inside_copies_are_inside():
     from oracle import pyoracle as O
     cont = O.containment_keys(A, B)
     assert len(cont) == 200     # every B is a scaled copy strictly inside some A
+
+
+def test_edge_extraction_thread_count_is_per_call():
+    """A call with an explicit thread count leaves the process-wide OpenMP
+    setting alone (an earlier form set it, so one single-threaded call made
+    every later extraction single-threaded)."""
+    import ctypes
+    try:
+        gomp = ctypes.CDLL("libgomp.so.1")
+    except OSError:
+        pytest.skip("libgomp not loadable")
+    before = gomp.omp_get_max_threads()
+    G = pg.icospheres(5, 20, 2, hi=20.0)
+    G.extract_edges(0, 1)
+    assert gomp.omp_get_max_threads() == before
+    one = (G.edge_starts.copy(), G.edge_ends.copy(), G.edge_src.copy())
+    G.extract_edges(0, 0)
+    for a, b in zip(one, (G.edge_starts, G.edge_ends, G.edge_src)):
+        assert np.array_equal(a, b)

@@ -70,3 +70,19 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["meshes_per_side"] == 1000
+
+
+def test_preprocess_workload_json_line():
+    """bench.py --workload preprocess (host code only) prints its JSON line;
+    where the reference's extractor was built, the output files are
+    byte-identical to its own (header padding excluded)."""
+    import json
+    import subprocess
+    p = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--workload", "preprocess", "--scale", "0.05",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, cwd=ROOT, timeout=600)
+    assert p.returncode == 0, p.stderr
+    d = json.loads([ln for ln in p.stdout.splitlines() if ln.startswith("{")][-1])
+    assert d["unit"] == "triangles/s" and d["value"] > 0 and d["value_one_thread"] > 0
+    assert d["config"]["triangles"] == 100 * 1280
+    if d["reference"] is not None:
+        assert d["byte_identical_to_reference"] is True
