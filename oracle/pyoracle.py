@@ -157,3 +157,55 @@ def set_threads(n: int) -> None:
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def grid_estimate(cells_a: np.ndarray, cells_b: np.ndarray, cell_size: float, epsilon: float, gamma: float,
+                  alpha_correction: bool = True) -> tuple[float, int, int]:
+    """Grid selectivity estimate of the reference, restated in numpy:
+    (raw sum over matched cells, alpha-corrected estimate, matched cells).
+
+    Cells of B are matched with the cell of A of the same index
+    (pierce/query/src/applications/pierce_overlap_main.cpp:376-414); each
+    matched pair contributes touchA * touchB * min(1, (sizeA + sizeB + eps)^3
+    / cellVolume * sqrt(ratioA * ratioB)^gamma), evaluated in float32 in the
+    kernel's order (pierce/query/src/cuda/estimated_overlap.cu:8-41, the
+    same in estimated_intersection.cu:8-42).  The raw sum is taken exactly
+    here (the reference reduces in float32, in the order of its reduction).
+    The estimate divides the float32 sum by alpha = max(1, (effA + effB)^3 /
+    cellVolume), eff = touch-weighted mean size * cbrt(touch-weighted mean
+    volume ratio) over all cells of a side (pierce_overlap_main.cpp:431-451,
+    pierce_intersection_main.cpp:181-211), and truncates."""
+    import math
+    f = np.float32
+    a = np.asarray(cells_a)
+    b = np.asarray(cells_b)
+    index_a = {(int(c["ix"]), int(c["iy"]), int(c["iz"])): k for k, c in enumerate(a)}
+    pairs = [(index_a[(int(c["ix"]), int(c["iy"]), int(c["iz"]))], k) for k, c in enumerate(b)
+             if (int(c["ix"]), int(c["iy"]), int(c["iz"])) in index_a]
+    vol = f(cell_size) * f(cell_size) * f(cell_size)
+    terms = []
+    for ka, kb in pairs:
+        A, B = a[ka], b[kb]
+        if A["touch_count"] == 0 or B["touch_count"] == 0:
+            continue
+        comb = f(f(A["avg_size_mean"]) + f(B["avg_size_mean"])) + f(epsilon)
+        prob = (comb * comb * comb) / vol
+        ratio = np.sqrt(f(A["vol_ratio"]) * f(B["vol_ratio"]))
+        prob = f(prob * np.power(ratio, f(gamma)))
+        prob = min(prob, f(1.0))
+        terms.append(float(f(f(A["touch_count"]) * f(B["touch_count"])) * prob))
+    raw = math.fsum(terms)
+
+    def avg(c, field, empty):
+        t = c["touch_count"].astype(np.float64)
+        if t.sum() == 0:
+            return f(empty)
+        return f(float(np.sum(c[field].astype(np.float64) * t)) / float(t.sum()))
+
+    eff = [avg(c, "avg_size_mean", 0.0) * np.cbrt(avg(c, "vol_ratio", 1.0)) for c in (a, b)]
+    comb = f(eff[0] + eff[1])
+    vol = max(vol, f(1e-9))
+    alpha = f(1.0)
+    if alpha_correction:
+        alpha = max(f((comb * comb * comb) / vol), f(1.0))
+    return raw, int(f(f(raw) / alpha)), len(pairs)

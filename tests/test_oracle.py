@@ -261,3 +261,27 @@ def test_parity_crossing_counts_agree_with_parity_pairs():
         odd = keys[(hits & 1) == 1]
         assert np.array_equal(odd, O.parity_keys(fv, T, swap=0))
     assert (hits & 1).sum() > 10
+
+
+def _cells(rows):
+    from pierce_gb300.geometry import GRID_DTYPE
+    return np.array(rows, dtype=GRID_DTYPE)
+
+
+def test_grid_estimate_hand_computed():
+    """The grid selectivity estimate on cells whose arithmetic is exact in
+    float32: one matched cell contributes 4 * 2 * (0.5 + 0.5)^3 / 2^3 = 1;
+    unmatched cells and cells without touches contribute nothing."""
+    A = _cells([(0, 0, 0, 1, 4, 0.5, 1.0), (1, 0, 0, 1, 2, 0.5, 1.0), (2, 0, 0, 0, 0, 0.5, 1.0)])
+    B = _cells([(0, 0, 0, 1, 2, 0.5, 1.0), (5, 5, 5, 1, 1, 0.5, 1.0), (2, 0, 0, 0, 0, 0.5, 1.0)])
+    raw, est, matched = O.grid_estimate(A, B, 2.0, 0.0, 0.8)
+    assert (raw, est, matched) == (1.0, 1, 2)
+    # cells smaller than the objects: probability capped at 1, alpha = (0.5 + 0.5)^3 / 0.5^3 = 8
+    raw, est, matched = O.grid_estimate(A, B, 0.5, 0.0, 0.8)
+    assert (raw, est) == (8.0, 1)
+    raw, est, _ = O.grid_estimate(A, B, 0.5, 0.0, 0.8, alpha_correction=False)
+    assert (raw, est) == (8.0, 8)
+    # shape correction: ratios 0.25 and 1 give sqrt(0.25)^1 = 0.5 with gamma 1
+    A2 = _cells([(0, 0, 0, 1, 4, 0.5, 0.25)])
+    raw, _, _ = O.grid_estimate(A2, B, 2.0, 0.0, 1.0)
+    assert raw == 0.5

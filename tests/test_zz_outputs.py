@@ -1,6 +1,9 @@
-"""Parity-ray diagnostics: pierce_parity_tracking and pierce_intersection
---enable-tracking / --enable-profiling-stats, checked against the oracle's
-crossing counts (exact parity rule, each crossed triangle counted once).
+"""Diagnostic and estimation outputs against the oracle: the parity-ray
+tracking tables (pierce_parity_tracking, pierce_intersection
+--enable-tracking / --enable-profiling-stats) against its crossing counts
+(exact parity rule, each crossed triangle counted once), and the grid
+selectivity estimate (pierce_estimate_pairs) against its restatement of the
+reference's formula.
 
 Collected after the other GPU files, so that a failure here cannot hide
 theirs.
@@ -129,3 +132,27 @@ def test_intersection_executable_tracking_outputs(tmp_path, pair):
     assert counters["profile_containment_rays_total"] > 0
     assert counters["profile_containment_iterations_total"] == counters["profile_containment_rays_total"]
     assert counters["profile_containment_candidate_overflow"] == 0
+
+
+def test_grid_estimate_matches_oracle(ctx):
+    """pierce_estimate_pairs against the restated estimator on the grid
+    statistics of two generated datasets.  Tolerance: the per-cell float32
+    terms may differ in the last bits (powf), so the raw sum agrees to a
+    relative 1e-6 and the truncated estimate to 1 + 1e-6 of itself."""
+    import ctypes as C
+    from pierce_gb300 import capi
+    A, B = pg.ellipsoid_pair(61, 62, 3000, 3000, 2, lo=0, hi=150, frac_contact=0.05)
+    A.grid_stats(8.0)
+    B.grid_stats(8.0)
+    ca, cb = A.grid_cells, B.grid_cells
+    cs = A.view().grid_cell_size
+    L = capi.lib()
+    for eps, gamma, alpha in ((0.001, 0.8, 1), (0.0, 1.0, 0), (0.5, 0.5, 1)):
+        raw, est, matched = C.c_double(), C.c_int64(), C.c_int32()
+        capi.check(L.pierce_estimate_pairs(ctx.handle, ca.ctypes.data, len(ca), cb.ctypes.data, len(cb), cs, eps,
+                                           gamma, alpha, C.byref(raw), C.byref(est), C.byref(matched)),
+                   "estimate_pairs")
+        want_raw, want_est, want_matched = O.grid_estimate(ca, cb, cs, eps, gamma, bool(alpha))
+        assert matched.value == want_matched > 50
+        assert raw.value == pytest.approx(want_raw, rel=1e-6)
+        assert abs(est.value - want_est) <= 1 + 1e-6 * want_est
