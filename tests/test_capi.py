@@ -54,6 +54,8 @@ def test_invalid_arguments_are_reported_without_a_device():
     assert L.pierce_join(None, None, None, None, None, None) == capi.ERR_INVALID_ARGUMENT
     assert b"null" in L.pierce_last_error()
     assert L.pierce_dataset_info_get(None, None) == capi.ERR_INVALID_ARGUMENT
+    assert L.pierce_parity_tracking(None, None, None, 256, None, None, None, None) == capi.ERR_INVALID_ARGUMENT
+    assert b"parity_tracking" in L.pierce_last_error()
     d = C.c_void_p(16)  # never dereferenced: the size check comes first
     assert L.pierce_deduplicate_pairs_noalloc(d, capi.NOALLOC_MAX_PAIRS + 1, d, d, None) == \
         capi.ERR_INVALID_ARGUMENT
