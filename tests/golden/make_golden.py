@@ -10,8 +10,12 @@ where the reference sources are present).
 * ``pairs_*.npz`` — oracle pair sets for small joins (overlap, intersection,
   containment, FP32 plain overlap), so the GPU tests also compare against
   stored answers.
+* ``pairs_ellipsoids_50000.npz`` (``--full``) — the oracle's intersection and
+  containment pair sets of the full benchmark workload, 2 x 50,000 level-3
+  ellipsoids (the datasets of ``bench.workload(1.0)``), a few minutes of
+  host time.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [--full]
 """
 from __future__ import annotations
 
@@ -56,7 +60,24 @@ def raw_without_edges(geom) -> "pg.Geometry":
     return pg.Geometry.from_arrays(geom.vertices, geom.indices, geom.tri_to_object)
 
 
+def full_workload() -> None:
+    """Intersection and containment pairs of the benchmark's 2 x 50,000
+    ellipsoids, as the oracle computes them."""
+    import time
+    import bench
+    A, B, cfg = bench.workload(1.0)
+    t0 = time.perf_counter()
+    inter = O.intersection_keys(A, B)
+    cont = O.containment_keys(A, B)
+    np.savez_compressed(HERE / "pairs_ellipsoids_50000.npz", intersection=inter, containment=cont,
+                        seeds=np.array(cfg["seeds"]), meshes_per_side=cfg["meshes_per_side"])
+    print("ellipsoids_50000", len(inter), len(cont), f"{time.perf_counter() - t0:.1f} s")
+
+
 def main() -> None:
+    if "--full" in sys.argv[1:]:
+        full_workload()
+        return
     if not REF_TOOL.exists():
         raise SystemExit("oracle/_ref/ref_pre_tool missing: run oracle/build_ref.sh first")
     digests = {}

@@ -285,3 +285,16 @@ def test_grid_estimate_hand_computed():
     A2 = _cells([(0, 0, 0, 1, 4, 0.5, 0.25)])
     raw, _, _ = O.grid_estimate(A2, B, 2.0, 0.0, 1.0)
     assert raw == 0.5
+
+
+def test_full_workload_golden_fixture():
+    """The stored oracle pair sets of the full benchmark workload (made by
+    make_golden.py --full): sorted, unique, containment pairs are
+    intersection pairs of B inside A, and the seeds are the benchmark's."""
+    g = np.load(GOLDEN / "pairs_ellipsoids_50000.npz")
+    inter, cont = g["intersection"], g["containment"]
+    assert (len(inter), len(cont)) == (13666, 10122)
+    for k in (inter, cont):
+        assert k.dtype == np.uint64 and np.all(np.diff(k.astype(np.int64)) > 0)
+    assert np.isin(cont, inter).all()
+    assert [int(x) for x in g["seeds"]] == [2024, 2025] and int(g["meshes_per_side"]) == 50000

@@ -1,9 +1,9 @@
-"""Diagnostic and estimation outputs against the oracle: the parity-ray
-tracking tables (pierce_parity_tracking, pierce_intersection
---enable-tracking / --enable-profiling-stats) against its crossing counts
-(exact parity rule, each crossed triangle counted once), and the grid
-selectivity estimate (pierce_estimate_pairs) against its restatement of the
-reference's formula.
+"""Outputs checked against the oracle: the parity-ray tracking tables
+(pierce_parity_tracking, pierce_intersection --enable-tracking /
+--enable-profiling-stats) against its crossing counts (exact parity rule,
+each crossed triangle counted once), the grid selectivity estimate
+(pierce_estimate_pairs) against its restatement of the reference's formula,
+and the full benchmark workload's pair sets against the stored oracle sets.
 
 Collected after the other GPU files, so that a failure here cannot hide
 theirs.
@@ -156,3 +156,23 @@ def test_grid_estimate_matches_oracle(ctx):
         assert matched.value == want_matched > 50
         assert raw.value == pytest.approx(want_raw, rel=1e-6)
         assert abs(est.value - want_est) <= 1 + 1e-6 * want_est
+
+
+def test_full_benchmark_workload_matches_golden(ctx):
+    """The benchmark's full workload, 2 x 50,000 level-3 ellipsoids (64 M
+    triangles and 96 M edges per side, inside copies and exact contacts):
+    the intersection and containment pair sets equal the oracle's, stored in
+    tests/golden/pairs_ellipsoids_50000.npz by make_golden.py --full."""
+    import bench
+    from pierce_gb300 import join as J
+    g = np.load(Path(__file__).resolve().parent / "golden" / "pairs_ellipsoids_50000.npz")
+    A, B, cfg = bench.workload(1.0)
+    assert [int(x) for x in g["seeds"]] == cfg["seeds"] and int(g["meshes_per_side"]) == A.num_objects
+    t = J.default_tuning(leaf_size=4)
+    da, db = J.Dataset.from_geometry(ctx, A, t), J.Dataset.from_geometry(ctx, B, t)
+    inter = J.intersection_join(ctx, da, db)
+    assert np.array_equal(J.pairs_to_keys(inter.pairs), g["intersection"])
+    cont = J.containment_join(ctx, da, db)
+    assert np.array_equal(J.pairs_to_keys(cont.pairs), g["containment"])
+    da.close()
+    db.close()
