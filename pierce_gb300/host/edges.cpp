@@ -11,9 +11,10 @@
 //    lexicographically; the first triangle edge that produces a key wins and
 //    keeps its own (unswapped) float endpoints;
 //  * output order is ascending key order (the std::map iteration order).
-// Here the map is replaced by a sort of (key, arrival index) records, done
-// per object in parallel: equal keys always share an object, so "first
-// arrival per key" is decided inside one object.  order == 0 then merges all
+// Here the map is replaced, per object and in parallel, by a hash set that
+// keeps the first arrival of each key (records are generated in arrival
+// order) and a sort of the surviving records by key: equal keys always
+// share an object, so "first arrival per key" is decided inside one object.  order == 0 then merges all
 // objects into global key order (byte-identical to the reference output);
 // order == 1 keeps objects in id order (same edge set, cheaper for large
 // datasets whose edge order does not matter to the join).
@@ -22,8 +23,10 @@
 // (pierce/preprocess/src/pierce_preprocess.cpp:49-167).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <numeric>
 #include <tuple>
 #include <vector>
@@ -56,11 +59,19 @@ inline bool key_equal(const EdgeRec& x, const EdgeRec& y) {
     return x.obj == y.obj && std::memcmp(x.a, y.a, sizeof(x.a)) == 0 &&
            std::memcmp(x.b, y.b, sizeof(x.b)) == 0;
 }
-inline bool rec_less(const EdgeRec& x, const EdgeRec& y) {
-    if (key_less(x, y)) return true;
-    if (key_less(y, x)) return false;
-    if (x.tri != y.tri) return x.tri < y.tri;
-    return x.corner < y.corner;
+// Hash of a record's key (both quantised endpoints and the object id),
+// 64-bit multiply-xorshift mixing.
+inline uint64_t key_hash(const EdgeRec& r) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t)(uint32_t)r.obj;
+    for (int i = 0; i < 3; ++i) {
+        h = (h ^ (uint64_t)r.a[i]) * 0xff51afd7ed558ccdull;
+        h ^= h >> 33;
+    }
+    for (int i = 0; i < 3; ++i) {
+        h = (h ^ (uint64_t)r.b[i]) * 0xc4ceb9fe1a85ec53ull;
+        h ^= h >> 33;
+    }
+    return h;
 }
 
 // llround(double(x) * 1e5) without the libm call: truncate, then round half
@@ -141,7 +152,8 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
 #ifdef _OPENMP
         tid = omp_get_thread_num();
 #endif
-        std::vector<EdgeRec> buf;
+        std::vector<EdgeRec> buf, uniq;
+        std::vector<size_t> table;
         std::vector<Ref>& arena = arenas[tid];
 #pragma omp for schedule(dynamic, 16)
         for (int64_t o = 0; o < nobj; ++o) {
@@ -165,13 +177,28 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
                     buf.push_back(r);
                 }
             }
-            std::sort(buf.begin(), buf.end(), rec_less);
-            Slot s{tid, arena.size(), 0};
-            for (size_t i = 0; i < buf.size(); ++i) {
-                if (i > 0 && key_equal(buf[i], buf[i - 1])) continue;
-                arena.push_back(Ref{buf[i].tri, buf[i].corner, buf[i].obj});
-                s.count++;
+            // records are in arrival order (triangles ascending, then
+            // corners): the first insert of a key is its first arrival
+            size_t cap = 16;
+            while (cap < 2 * buf.size()) cap <<= 1;
+            table.assign(cap, SIZE_MAX);
+            uniq.clear();
+            for (const EdgeRec& r : buf) {
+                size_t h = (size_t)key_hash(r) & (cap - 1);
+                for (;;) {
+                    const size_t j = table[h];
+                    if (j == SIZE_MAX) {
+                        table[h] = uniq.size();
+                        uniq.push_back(r);
+                        break;
+                    }
+                    if (key_equal(uniq[j], r)) break;
+                    h = (h + 1) & (cap - 1);
+                }
             }
+            std::sort(uniq.begin(), uniq.end(), key_less);  // keys are unique here
+            Slot s{tid, arena.size(), uniq.size()};
+            for (const EdgeRec& r : uniq) arena.push_back(Ref{r.tri, r.corner, r.obj});
             slots[o] = s;
         }
     }
@@ -189,7 +216,8 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
 
     if (order == 0) {
         // Global key order: rebuild keys for the unique edges and sort them.
-        std::vector<EdgeRec> keyed(ne);
+        // uninitialised storage: every record is written below
+        std::unique_ptr<EdgeRec[]> keyed(new EdgeRec[ne]);
 #pragma omp parallel for schedule(static) num_threads(nthreads)
         for (int64_t i = 0; i < (int64_t)ne; ++i) {
             const Ref& r = all[i];
@@ -207,11 +235,19 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
             k.corner = r.corner;
             k.tri = r.tri;
         }
+        // Each object's records form a run sorted by key (the runs lie in
+        // object order): a multiway merge of the runs gives the global order.
 #ifdef _OPENMP
-        __gnu_parallel::sort(keyed.begin(), keyed.end(), key_less,
-                             __gnu_parallel::default_parallel_tag((__gnu_parallel::_ThreadIndex)nthreads));
+        std::vector<std::pair<EdgeRec*, EdgeRec*>> runs;
+        runs.reserve((size_t)nobj);
+        for (int64_t o = 0; o < nobj; ++o)
+            if (off[o + 1] > off[o]) runs.emplace_back(keyed.get() + off[o], keyed.get() + off[o + 1]);
+        std::unique_ptr<EdgeRec[]> merged(new EdgeRec[ne]);
+        __gnu_parallel::multiway_merge(runs.begin(), runs.end(), merged.get(), (int64_t)ne, key_less,
+                                       __gnu_parallel::default_parallel_tag((__gnu_parallel::_ThreadIndex)nthreads));
+        keyed.swap(merged);
 #else
-        std::sort(keyed.begin(), keyed.end(), key_less);
+        std::sort(keyed.get(), keyed.get() + ne, key_less);
 #endif
 #pragma omp parallel for schedule(static) num_threads(nthreads)
         for (int64_t i = 0; i < (int64_t)ne; ++i) all[i] = Ref{keyed[i].tri, keyed[i].corner, keyed[i].obj};
