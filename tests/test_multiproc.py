@@ -86,3 +86,17 @@ def test_preprocess_workload_json_line():
     assert d["config"]["triangles"] == 100 * 1280
     if d["reference"] is not None:
         assert d["byte_identical_to_reference"] is True
+
+
+def test_roofline_algorithmic_bytes():
+    """bench.py's algorithmic bytes of the edge-ray launches: 28 B per traced
+    edge, 8 B per raw hit, and per target hierarchy 16 B per kept triangle,
+    12 B per vertex in proportion to the triangles kept and 32 B per node of
+    a minimal binary tree."""
+    import types
+    import numpy as np
+    import bench
+    G = types.SimpleNamespace(vertices=np.zeros((600, 3), np.float32), num_triangles=1000)
+    got = bench.traced_edge_ray_bytes(10, 2, [(G, 500), (G, 0)])
+    assert got == 28 * 10 + 8 * 2 + 16 * 500 + 12 * 300 + 32 * 999
+    assert bench.traffic_estimate(100) == pytest.approx(bench.EDGE_RAY_DRAM_BYTES_PER_RAY * 100)
