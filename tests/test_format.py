@@ -162,3 +162,32 @@ def test_edge_extraction_thread_count_is_per_call():
     G.extract_edges(0, 0)
     for a, b in zip(one, (G.edge_starts, G.edge_ends, G.edge_src)):
         assert np.array_equal(a, b)
+
+
+def test_grid_stats_hand_computed():
+    """Grid statistics (generateGridStats semantics) of two closed meshes
+    whose values are exact: a 2x2x2 cube at the origin (volume ratio 1, mean
+    extent 2) and a corner tetrahedron of the same box moved to (10,10,10)
+    (volume 8/6 of an 8 box: ratio 1/6).  A cell counts an object's box
+    centre and every cell its box touches (upper bound minus 1e-5)."""
+    cube_v = np.array([[x, y, z] for x in (0, 2) for y in (0, 2) for z in (0, 2)], np.float32)
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    cube_t = [t for a, b, c, d in quads for t in ((a, b, c), (a, c, d))]
+    tet_v = np.array([[10, 10, 10], [12, 10, 10], [10, 12, 10], [10, 10, 12]], np.float32)
+    tet_t = [(0, 2, 1), (0, 1, 3), (0, 3, 2), (1, 2, 3)]
+    v = np.concatenate([cube_v, tet_v])
+    t = np.array(cube_t + [(a + 8, b + 8, c + 8) for a, b, c in tet_t], np.uint32)
+    o = np.array([0] * 12 + [1] * 4, np.int32)
+    G = pg.Geometry.from_arrays(v, t, o)
+    ratio_tet = float(np.float32(np.float32(8.0) / np.float32(6.0)) / np.float32(8.0))
+    G.grid_stats(4.0)
+    got = [tuple(c.item()) for c in G.grid_cells]
+    assert got == [(0, 0, 0, 1, 1, 2.0, 1.0), (2, 2, 2, 1, 1, 2.0, pytest.approx(ratio_tet))]
+    G.grid_stats(1.0)
+    cells = {tuple(int(x) for x in c.item()[:3]): c.item()[3:] for c in G.grid_cells}
+    cube_cells = {(x, y, z) for x in (0, 1) for y in (0, 1) for z in (0, 1)}
+    tet_cells = {(x, y, z) for x in (10, 11) for y in (10, 11) for z in (10, 11)}
+    assert set(cells) == cube_cells | tet_cells
+    assert cells[(1, 1, 1)][0] == 1 and cells[(11, 11, 11)][0] == 1          # box centres
+    assert sum(c[0] for c in cells.values()) == 2
+    assert all(c[1] == 1 and c[2] == 2.0 for c in cells.values())
