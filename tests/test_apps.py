@@ -226,3 +226,32 @@ def test_tracking_csv_writer(tmp_path):
     ]
     bad = subprocess.run([str(exe), str(tmp_path / "missing" / "h.csv"), str(tmp_path / "t.csv")])
     assert bad.returncode == 1
+
+
+def test_preprocess_obj_shapes_polygons_and_relative_indices(tmp_path):
+    """OBJ rules of the producer (tinyobjloader's shapes, as the reference's
+    loader uses them): a quad becomes a fan of two triangles, `o`/`g` lines
+    start a new object only after faces, corners may be negative (relative)
+    and carry texture/normal indices, a shape without faces is skipped."""
+    (tmp_path / "s.obj").write_text("\n".join([
+        "# two objects",
+        "v 0 0 0", "v 1 0 0", "v 1 1 0", "v 0 1 0",
+        "o first",
+        "f 1 2 3 4",
+        "g empty_group",
+        "g second",
+        "v 0 0 1", "v 1 0 1", "v 0 1 1",
+        "vt 0 0", "vn 0 0 1",
+        "f -3/1 -2/1/1 -1//1",
+        "o third_without_faces",
+        "",
+    ]))
+    run("pierce_preprocess", "--dataset", tmp_path / "s.obj", "--output-geometry", tmp_path / "s.pre")
+    h = pg.Geometry.read_pre(tmp_path / "s.pre")
+    assert h.num_objects == 2 and h.num_triangles == 3
+    tris = h.vertices[h.indices].reshape(-1, 3, 3).tolist()
+    assert tris == [[[0, 0, 0], [1, 0, 0], [1, 1, 0]], [[0, 0, 0], [1, 1, 0], [0, 1, 0]],
+                    [[0, 0, 1], [1, 0, 1], [0, 1, 1]]]
+    assert h.tri_to_object.tolist() == [0, 0, 1]
+    # unique edges per object: the quad's fan has 5, the triangle 3
+    assert sorted(np.bincount(h.edge_src).tolist()) == [3, 5]
