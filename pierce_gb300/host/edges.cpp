@@ -269,6 +269,9 @@ void extract_edges(pierce_geom& g, int order, int num_threads) {
 }
 
 void grid_stats(pierce_geom& g, float cell_size) {
+    // Objects run in parallel; every floating-point sum keeps the order of
+    // a serial pass (an object's triangles ascending, a cell's objects
+    // ascending), so the statistics do not depend on the thread count.
     struct ObjStats {
         float mn[3] = {1e30f, 1e30f, 1e30f};
         float mx[3] = {-1e30f, -1e30f, -1e30f};
@@ -276,89 +279,146 @@ void grid_stats(pierce_geom& g, float cell_size) {
         bool seen = false;
     };
     const uint64_t nt = g.num_triangles(), nv = g.num_vertices();
-    int32_t max_obj = -1;
-    for (int32_t o : g.tri_to_object) max_obj = std::max(max_obj, o);
-    std::vector<ObjStats> objs((size_t)(max_obj + 1));
     const uint64_t nmap = std::min<uint64_t>(nt, g.tri_to_object.size());
-    for (uint64_t t = 0; t < nmap; ++t) {
-        const int32_t o = g.tri_to_object[t];
+    int32_t max_obj = -1;
+    for (uint64_t t = 0; t < nmap; ++t) max_obj = std::max(max_obj, g.tri_to_object[t]);
+    const int64_t nobj = (int64_t)max_obj + 1;
+    std::vector<ObjStats> objs((size_t)nobj);
+    auto valid = [&](uint64_t t) {
         const uint32_t* tri = &g.indices[3 * t];
-        if (o < 0 || tri[0] >= nv || tri[1] >= nv || tri[2] >= nv) continue;
+        return g.tri_to_object[t] >= 0 && tri[0] < nv && tri[1] < nv && tri[2] < nv;
+    };
+    // triangles grouped by object, ascending within each object
+    std::vector<uint64_t> start((size_t)nobj + 1, 0);
+    for (uint64_t t = 0; t < nmap; ++t)
+        if (valid(t)) start[(size_t)g.tri_to_object[t] + 1]++;
+    for (int64_t o = 0; o < nobj; ++o) start[o + 1] += start[o];
+    std::vector<uint64_t> tris(start[(size_t)nobj]);
+    {
+        std::vector<uint64_t> cur(start.begin(), start.end() - 1);
+        for (uint64_t t = 0; t < nmap; ++t)
+            if (valid(t)) tris[cur[(size_t)g.tri_to_object[t]]++] = t;
+    }
+    // Per object: bounding box, then the signed volume relative to the box
+    // centre (float products summed in double as in the reference).
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t o = 0; o < nobj; ++o) {
         ObjStats& s = objs[o];
-        s.seen = true;
-        for (int k = 0; k < 3; ++k) {
-            const float* v = &g.vertices[3 * (uint64_t)tri[k]];
-            for (int d = 0; d < 3; ++d) {
-                s.mn[d] = std::min(s.mn[d], v[d]);
-                s.mx[d] = std::max(s.mx[d], v[d]);
+        for (uint64_t k = start[o]; k < start[o + 1]; ++k) {
+            const uint32_t* tri = &g.indices[3 * tris[k]];
+            s.seen = true;
+            for (int j = 0; j < 3; ++j) {
+                const float* v = &g.vertices[3 * (uint64_t)tri[j]];
+                for (int d = 0; d < 3; ++d) {
+                    s.mn[d] = std::min(s.mn[d], v[d]);
+                    s.mx[d] = std::max(s.mx[d], v[d]);
+                }
             }
         }
-    }
-    // Signed volume relative to the AABB centre, float products summed in
-    // double as in the reference.
-    for (uint64_t t = 0; t < nmap; ++t) {
-        const int32_t o = g.tri_to_object[t];
-        const uint32_t* tri = &g.indices[3 * t];
-        if (o < 0 || tri[0] >= nv || tri[1] >= nv || tri[2] >= nv) continue;
-        ObjStats& s = objs[o];
-        float c[3], p[3][3];
+        float c[3];
         for (int d = 0; d < 3; ++d) c[d] = (s.mn[d] + s.mx[d]) * 0.5f;
-        for (int k = 0; k < 3; ++k)
-            for (int d = 0; d < 3; ++d) p[k][d] = g.vertices[3 * (uint64_t)tri[k] + d] - c[d];
-        float cx = p[0][1] * p[1][2] - p[0][2] * p[1][1];
-        float cy = p[0][2] * p[1][0] - p[0][0] * p[1][2];
-        float cz = p[0][0] * p[1][1] - p[0][1] * p[1][0];
-        s.volume += (cx * p[2][0] + cy * p[2][1] + cz * p[2][2]);
+        for (uint64_t k = start[o]; k < start[o + 1]; ++k) {
+            const uint32_t* tri = &g.indices[3 * tris[k]];
+            float p[3][3];
+            for (int j = 0; j < 3; ++j)
+                for (int d = 0; d < 3; ++d) p[j][d] = g.vertices[3 * (uint64_t)tri[j] + d] - c[d];
+            float cx = p[0][1] * p[1][2] - p[0][2] * p[1][1];
+            float cy = p[0][2] * p[1][0] - p[0][0] * p[1][2];
+            float cz = p[0][0] * p[1][1] - p[0][1] * p[1][0];
+            s.volume += (cx * p[2][0] + cy * p[2][1] + cz * p[2][2]);
+        }
     }
-    struct Acc {
-        uint32_t center = 0, touch = 0;
-        float size = 0.0f, ratio = 0.0f;
+    // One record per (cell, object): the cell of the box centre, and every
+    // cell the box touches (upper bound minus 1e-5); seq numbers the records
+    // in object order.
+    struct CellRec {
+        int32_t x, y, z;
+        uint32_t center;  // 1: the object's centre cell
+        uint64_t seq;
+        uint32_t touch;   // 1: the object's box touches the cell
+        float size, ratio;
     };
-    std::map<std::tuple<int, int, int>, Acc> cells;
-    for (const ObjStats& s : objs) {
+    struct ObjCells {
+        int lo[3], hi[3], cc[3];
+        float avg, ratio;
+    };
+    std::vector<ObjCells> oc((size_t)nobj);
+    std::vector<uint64_t> rstart((size_t)nobj + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t o = 0; o < nobj; ++o) {
+        const ObjStats& s = objs[o];
         if (!s.seen) continue;
+        ObjCells& q = oc[o];
         float mesh_vol = std::fabs((float)s.volume) / 6.0f;
         float w = s.mx[0] - s.mn[0], h = s.mx[1] - s.mn[1], dpt = s.mx[2] - s.mn[2];
         float aabb_vol = w * h * dpt;
         if (aabb_vol < 1e-9f) aabb_vol = 1e-9f;
         float ratio = mesh_vol / aabb_vol;
         if (ratio > 1.0f) ratio = 1.0f;
-        float c[3];
-        for (int d = 0; d < 3; ++d) c[d] = (s.mn[d] + s.mx[d]) * 0.5f;
-        float avg = (w + h + dpt) / 3.0f;
-        cells[std::make_tuple((int)std::floor(c[0] / cell_size), (int)std::floor(c[1] / cell_size),
-                              (int)std::floor(c[2] / cell_size))]
-            .center++;
-        int lo[3], hi[3];
+        q.ratio = ratio;
+        q.avg = (w + h + dpt) / 3.0f;
+        uint64_t n = 1;
         for (int d = 0; d < 3; ++d) {
-            lo[d] = (int)std::floor(s.mn[d] / cell_size);
-            hi[d] = (int)std::floor((s.mx[d] - 1e-5f) / cell_size);
+            const float c = (s.mn[d] + s.mx[d]) * 0.5f;
+            q.cc[d] = (int)std::floor(c / cell_size);
+            q.lo[d] = (int)std::floor(s.mn[d] / cell_size);
+            q.hi[d] = (int)std::floor((s.mx[d] - 1e-5f) / cell_size);
+            n *= (uint64_t)std::max<int64_t>(0, (int64_t)q.hi[d] - q.lo[d] + 1);
         }
-        for (int z = lo[2]; z <= hi[2]; ++z)
-            for (int y = lo[1]; y <= hi[1]; ++y)
-                for (int x = lo[0]; x <= hi[0]; ++x) {
-                    Acc& a = cells[std::make_tuple(x, y, z)];
-                    a.touch++;
-                    a.size += avg;
-                    a.ratio += ratio;
-                }
+        rstart[o + 1] = 1 + n;
     }
+    for (int64_t o = 0; o < nobj; ++o) rstart[o + 1] += rstart[o];
+    const uint64_t nrec = rstart[(size_t)nobj];
+    std::unique_ptr<CellRec[]> recs(new CellRec[nrec]);
+#pragma omp parallel for schedule(static)
+    for (int64_t o = 0; o < nobj; ++o) {
+        if (!objs[o].seen) continue;
+        const ObjCells& q = oc[o];
+        uint64_t r = rstart[o];
+        recs[r] = CellRec{q.cc[0], q.cc[1], q.cc[2], 1u, r, 0u, 0.0f, 0.0f};
+        ++r;
+        for (int z = q.lo[2]; z <= q.hi[2]; ++z)
+            for (int y = q.lo[1]; y <= q.hi[1]; ++y)
+                for (int x = q.lo[0]; x <= q.hi[0]; ++x, ++r) recs[r] = CellRec{x, y, z, 0u, r, 1u, q.avg, q.ratio};
+    }
+    auto rec_less = [](const CellRec& a, const CellRec& b) {
+        if (a.x != b.x) return a.x < b.x;
+        if (a.y != b.y) return a.y < b.y;
+        if (a.z != b.z) return a.z < b.z;
+        return a.seq < b.seq;
+    };
+#ifdef _OPENMP
+    __gnu_parallel::sort(recs.get(), recs.get() + nrec, rec_less);
+#else
+    std::sort(recs.get(), recs.get() + nrec, rec_less);
+#endif
     g.grid_cells.clear();
-    g.grid_cells.reserve(cells.size());
-    for (auto& kv : cells) {
+    for (uint64_t i = 0; i < nrec;) {
         pierce_grid_entry e;
-        e.ix = std::get<0>(kv.first);
-        e.iy = std::get<1>(kv.first);
-        e.iz = std::get<2>(kv.first);
-        e.center_count = kv.second.center;
-        e.touch_count = kv.second.touch;
-        e.avg_size_mean = kv.second.size;
-        e.vol_ratio = kv.second.ratio;
-        if (e.touch_count > 0) {
-            e.avg_size_mean /= (float)e.touch_count;
-            e.vol_ratio /= (float)e.touch_count;
+        e.ix = recs[i].x;
+        e.iy = recs[i].y;
+        e.iz = recs[i].z;
+        uint32_t center = 0, touch = 0;
+        float size = 0.0f, ratio = 0.0f;
+        uint64_t j = i;
+        for (; j < nrec && recs[j].x == e.ix && recs[j].y == e.iy && recs[j].z == e.iz; ++j) {
+            center += recs[j].center;
+            if (recs[j].touch) {
+                touch++;
+                size += recs[j].size;
+                ratio += recs[j].ratio;
+            }
+        }
+        e.center_count = center;
+        e.touch_count = touch;
+        e.avg_size_mean = size;
+        e.vol_ratio = ratio;
+        if (touch > 0) {
+            e.avg_size_mean /= (float)touch;
+            e.vol_ratio /= (float)touch;
         }
         g.grid_cells.push_back(e);
+        i = j;
     }
     g.has_grid = true;
     g.grid_cell_size = cell_size;
