@@ -191,3 +191,21 @@ def test_grid_stats_hand_computed():
     assert cells[(1, 1, 1)][0] == 1 and cells[(11, 11, 11)][0] == 1          # box centres
     assert sum(c[0] for c in cells.values()) == 2
     assert all(c[1] == 1 and c[2] == 2.0 for c in cells.values())
+
+
+def test_grid_stats_independent_of_thread_count(tmp_path):
+    """Grid statistics summed in the serial order: one thread and all
+    threads give the same bytes."""
+    import os
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, sys.argv[1]); import pierce_gb300 as pg; "
+            "g = pg.ellipsoid_pair(3, 4, 400, 400, 2, lo=0, hi=80)[0]; g.grid_stats(3.0); "
+            "open(sys.argv[2], 'wb').write(g.grid_cells.tobytes())")
+    root = str(Path(__file__).resolve().parents[1])
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([sys.executable, "-c", code, root, str(tmp_path / "one.bin")], check=True, env=env)
+    g = pg.ellipsoid_pair(3, 4, 400, 400, 2, lo=0, hi=80)[0]
+    g.grid_stats(3.0)
+    assert len(g.grid_cells) > 100
+    assert (tmp_path / "one.bin").read_bytes() == g.grid_cells.tobytes()
