@@ -562,6 +562,13 @@ def main_preprocess(args):
     if t_ref is not None:
         a, b = (work / "ref.pre").read_bytes(), (work / "ours.pre").read_bytes()
         identical = len(a) == len(b) and a[:50] == b[:50] and a[56:] == b[56:]  # header padding excluded
+    def grid_seconds():
+        H = pg.Geometry.read_pre(src)
+        t0 = time.perf_counter()
+        H.grid_stats(8.0)
+        return time.perf_counter() - t0
+
+    t_grid = min(grid_seconds() for _ in range(max(args.steps, 1)))
     threads = os.cpu_count() or 1
     log(f"preprocess: {tris} triangles; ours {t_all:.3f} s ({threads} threads), {t_one:.3f} s (1 thread); "
         f"reference {t_ref if t_ref is None else round(t_ref, 3)} s; identical {identical}")
@@ -569,7 +576,8 @@ def main_preprocess(args):
             "value": tris / t_all, "value_one_thread": tris / t_one, "threads": threads,
             "reference": None if t_ref is None else {"value": tris / t_ref, "threads": 1,
                                                      "kind": "reference (EdgePreprocessor, BinaryIO)"},
-            "byte_identical_to_reference": identical, "steps": args.steps, "warmup": args.warmup,
+            "byte_identical_to_reference": identical, "grid_stats_s": t_grid, "steps": args.steps,
+            "warmup": args.warmup,
             "higher_is_better": True, "data": "synthetic",
             "config": {"workload": "pre-edge-extraction", "meshes": n, "subdivision": 3,
                        "triangles": tris, "edges": G.num_edges, "seed": 2024}}
