@@ -389,8 +389,11 @@ int pierce_compact_hash_table_pairs(pierce_ctx* ctx, const uint64_t* d_table, ui
  * PIERCE_ERR_INVALID_ARGUMENT.  The call enqueues its work on `stream` (a
  * cudaStream_t of the current device) and returns without waiting; the
  * unique pairs land in d_out[0 .. *d_num_unique) in no particular order.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the one array, so
+ * Every call looks up the array's device address (cudaGetSymbolAddress,
+ * which allocates nothing); the first call on a device also clears the
+ * array (it starts zeroed), so make that first call before any stream
+ * capture.  Each call leaves the table empty for the next one.  The pair
+ * (-1, -1) is accepted like any other.  All calls share the one array, so
  * calls whose work overlaps on the GPU race: order them on one stream. */
 #define PIERCE_NOALLOC_TABLE_SLOTS (1u << 22)
 #define PIERCE_NOALLOC_MAX_PAIRS (1u << 21)

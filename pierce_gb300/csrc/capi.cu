@@ -1630,6 +1630,8 @@ struct Join {
             strict_capacity = false;
             o.sizing = PIERCE_SIZING_TWO_PASS;
             cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream);
+            // the traversal counters describe the join that produced the pairs
+            cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), ctx->stream);
             s = run_predicate(out);
         }
         const int t1 = timer.record();

@@ -246,7 +246,8 @@ def test_preprocess_obj_shapes_polygons_and_relative_indices(tmp_path):
         "o third_without_faces",
         "",
     ]))
-    run("pierce_preprocess", "--dataset", tmp_path / "s.obj", "--output-geometry", tmp_path / "s.pre")
+    run("pierce_preprocess", "--dataset", tmp_path / "s.obj", "--output-geometry", tmp_path / "s.pre",
+        "--output-timing", tmp_path / "t.json")
     h = pg.Geometry.read_pre(tmp_path / "s.pre")
     assert h.num_objects == 2 and h.num_triangles == 3
     tris = h.vertices[h.indices].reshape(-1, 3, 3).tolist()

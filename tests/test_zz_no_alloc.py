@@ -54,6 +54,28 @@ def test_noalloc_matches_merge_and_deduplicate_two_calls():
     ctx.close()
 
 
+def test_noalloc_keeps_the_pair_minus_one_minus_one():
+    """(-1, -1) packs to the empty-slot marker of the hash set; it must come
+    out like any other pair, once, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    from pierce_gb300 import capi
+
+    L = capi.lib()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    ids = np.array([[-1, -1], [0, 0], [-1, -1], [5, -1], [-1, 5], [0, 0], [7, 9]], np.int32)
+    for _ in range(2):
+        d_in = torch.from_numpy(ids).cuda()
+        d_out = torch.full((len(ids), 2), -7, dtype=torch.int32, device="cuda")
+        d_cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+        assert L.pierce_deduplicate_pairs_noalloc(d_in.data_ptr(), len(ids), d_out.data_ptr(), d_cnt.data_ptr(),
+                                                  stream.cuda_stream) == capi.OK, L.pierce_last_error()
+        torch.cuda.synchronize()
+        got = d_out[: int(d_cnt.item())].cpu().numpy()
+        assert np.array_equal(_unique_sorted(got), _unique_sorted(ids))
+        assert len(got) == len(_unique_sorted(ids))
+
+
 def test_noalloc_rejects_oversized_input():
     pytest.importorskip("torch")
     from pierce_gb300 import capi
