@@ -1,29 +1,37 @@
 """Benchmark of the mesh spatial-join path on one GB300.
 
-Workload (default): two datasets of 50,000 perturbed ellipsoids each
-(subdivision-3 icospheres, semi-axes U[2,5], random rotation, 5 % radial
-smooth value noise, in [0,1000]^3; 20 % of B scaled 0.3 inside a random A
-mesh, 1 % of B sharing exact vertices or faces with an A mesh), float32,
-seeded synthetic data.  One step = the join work a user of the executables
-runs per query pair: rebuild both BVHs from the resident geometry, then an
-intersection join and a containment join (2 join queries), from resident
-device geometry to the sorted device pair sets.
+Default workload: the large tube-mesh overlap join.  Side A is 2,000
+branching tube meshes of about 200k triangles each (random-walk skeletons,
+step 1.0, branching probability 0.02, radius U[0.5, 3], 12-gon sections swept
+and capped) in [0,1000]^3, about 400 M triangles; side B is 100,000 perturbed
+ellipsoids (level-3 icospheres, semi-axes U[2,5], random rotation, 5 % radial
+value noise) in [0,1000]^3, 128 M triangles; float32, seeded synthetic data.
+One step = one overlap join (``pierce_overlap``'s query) from resident device
+geometry to the sorted device pair set, per-join hierarchies included.
 
 Printed JSON line (rank 0):
-  value      – join queries/s with inputs resident in HBM (CUDA events on the
-               library's stream);
-  e2e        – the same metric through the C ABI from pinned host buffers:
-               H2D of both datasets, BVH builds, both joins, D2H of the pairs;
-  roofline   – the edge-ray traversal kernel against measured HBM bandwidth,
-               with algorithmic bytes over the units the launches process
-               28*E_traced + 16*F_tgt + 12*V_tgt + 32*(2*F_tgt - 1) + 8*P_raw,
-               E_traced the edges that survive culling and F_tgt the
-               triangles of the target's per-join hierarchy;
-  cpu_baseline – the CPU oracle (exact Face-style restatement, OpenMP) on a
-               spatial sample of the same workload, extrapolated.
+  value      - join queries/s with inputs resident in HBM (CUDA events on the
+               library's stream), the tuned form: exact predicates behind an
+               FP32 filter, culling, per-join hierarchies, the persistent ray
+               queue, learned output sizing;
+  e2e        - the same metric through the C ABI from pinned host buffers:
+               dataset creation (host to device), the join, the pairs copied
+               back, the datasets destroyed, every step;
+  plain      - the plain GPU form (dataset hierarchies, FP32
+               Moller-Trumbore, two-pass sizing, no culling), device and e2e;
+  roofline   - the edge-ray traversal kernel against the measured HBM
+               bandwidth, with algorithmic bytes over the units the launches
+               process: 28*E_traced + 16*F_tgt + 12*V_tgt + 32*(2*F_tgt - 1)
+               + 8*P_raw, E_traced the traced edges and F_tgt the triangles
+               of the target's per-join hierarchy;
+  cpu_baseline - the CPU oracle (exact restatement, OpenMP) on the first 10
+               tubes against every ellipsoid near them, scaled to the join.
 
-``--impl reference`` times the CPU restatement of the reference path instead
-(the reference's GPU path needs OptiX and cannot run here).
+``--workload ellipsoids`` runs the intersection + containment line on
+2 x 50,000 ellipsoids; ``batched`` the 4,096-query batch; ``preprocess`` the
+`.pre` producer.  ``--impl reference`` times the CPU restatement of the
+reference path on the same workload (the reference's GPU path needs OptiX
+and cannot run here).
 """
 from __future__ import annotations
 
@@ -61,7 +69,8 @@ def workload(scale: float = 1.0, seed_a: int = 2024, seed_b: int = 2025):
     A, B = pg.ellipsoid_pair(seed_a, seed_b, n, n, 3, 2.0, 5.0, 0.05, 0.0, hi, 0.2, 0.3, 0.01)
     return A, B, {"workload": "ellipsoids-intersection+containment", "meshes_per_side": n,
                   "subdivision": 3, "box": [0.0, round(hi, 3)], "triangles_per_side": A.num_triangles,
-                  "edges_per_side": A.num_edges, "seeds": [seed_a, seed_b]}
+                  "edges_per_side": A.num_edges, "seeds": [seed_a, seed_b],
+                  "l2": "inputs larger than L2 (about 9 GB of geometry and BVH per side, 129 MB L2)"}
 
 
 def clocks_path(name: str) -> Path:
@@ -142,14 +151,15 @@ def edge_ray_bytes(src, tgt, raw_hits):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced edge
-# of k_edge_rays, from one full-size ncu capture of the two launches of the
-# intersection join of the default workload (608.8 MB for 13,316,000 traced
-# edges; profiles/k_edge_rays_ellipsoids_50000.md).
-EDGE_RAY_DRAM_BYTES_PER_RAY = 45.72
+# of k_edge_rays, from one ncu capture of the edge-ray launches of this
+# build on a reduced case of the same workload (the traffic per traced edge
+# is then scaled by the traced edges of the full join).
+EDGE_RAY_DRAM_BYTES_PER_RAY = {"tubes": 45.72, "ellipsoids": 45.72}
 
 
-def traffic_estimate(rays):
-    return None if EDGE_RAY_DRAM_BYTES_PER_RAY is None else EDGE_RAY_DRAM_BYTES_PER_RAY * rays
+def traffic_estimate(rays, workload="tubes"):
+    per = EDGE_RAY_DRAM_BYTES_PER_RAY.get(workload)
+    return None if per is None else per * rays
 
 
 def traced_edge_ray_bytes(rays, raw_hits, targets):
@@ -207,11 +217,163 @@ def cpu_join_seconds(As, Bs) -> float:
     return time.perf_counter() - t0
 
 
+# ---- the tube-mesh overlap workload -------------------------------------------
+
+TUBE_SEED, ELLIPSOID_SEED = 5, 6
+
+
+def tube_counts(scale: float = 1.0):
+    return max(2, int(round(2000 * scale))), max(2, int(round(100_000 * scale)))
+
+
+def tube_geometry(scale: float = 1.0, first: int | None = None):
+    """Side A: the branching tubes (all, or only tubes 0 .. first-1)."""
+    import pierce_gb300 as pg
+    n_tubes, _ = tube_counts(scale)
+    return pg.tubes(TUBE_SEED, n_tubes, 200_000, 1.0, 0.02, 0.5, 3.0, 12, 0.0, 1000.0, first=first)
+
+
+def ellipsoid_instances(scale: float = 1.0):
+    """Side B: per-mesh parameters of the 100,000 ellipsoids."""
+    import pierce_gb300 as pg
+    _, n_ell = tube_counts(scale)
+    return pg.instances(ELLIPSOID_SEED, n_ell, pg.ELLIPSOIDS, 3, p0=2.0, p1=5.0, noise_amp=0.05, lo=0.0, hi=1000.0)
+
+
+def tubes_config(scale: float = 1.0) -> dict:
+    n_tubes, n_ell = tube_counts(scale)
+    return {"workload": "tubes-vs-ellipsoids-overlap", "predicate": "overlap", "tubes": n_tubes,
+            "tube_triangles_target": 200_000, "tube_step": 1.0, "tube_branch_prob": 0.02,
+            "tube_radius": [0.5, 3.0], "tube_sides": 12, "ellipsoids": n_ell, "ellipsoid_level": 3,
+            "ellipsoid_axes": [2.0, 5.0], "box": [0.0, 1000.0], "seeds": [TUBE_SEED, ELLIPSOID_SEED],
+            "l2": "inputs larger than L2 (about 40 GB of geometry resident, 129 MB L2)"}
+
+
+def _cell_keys(c: np.ndarray) -> np.ndarray:
+    c = c.astype(np.int64) + (1 << 20)
+    return (c[:, 0] << 42) | (c[:, 1] << 21) | c[:, 2]
+
+
+def boxes_near(tri_lo, tri_hi, obj_lo, obj_hi, cell: float = 8.0) -> np.ndarray:
+    """Objects whose box shares a grid cell with the box of one of the given
+    triangles: a superset of the objects whose box meets one of those
+    triangle boxes (two boxes that meet share the cell of a common point)."""
+    t0 = np.floor(tri_lo / cell).astype(np.int64)
+    t1 = np.floor(tri_hi / cell).astype(np.int64)
+    ext = t1 - t0
+    keys = []
+    for dx in range(int(ext[:, 0].max(initial=0)) + 1):
+        for dy in range(int(ext[:, 1].max(initial=0)) + 1):
+            for dz in range(int(ext[:, 2].max(initial=0)) + 1):
+                sel = (ext[:, 0] >= dx) & (ext[:, 1] >= dy) & (ext[:, 2] >= dz)
+                keys.append(np.unique(_cell_keys(t0[sel] + np.array([dx, dy, dz]))))
+    cells = np.unique(np.concatenate(keys)) if keys else np.zeros(0, np.int64)
+    o0 = np.floor(obj_lo / cell).astype(np.int64)
+    o1 = np.floor(obj_hi / cell).astype(np.int64)
+    oext = o1 - o0
+    near = np.zeros(len(obj_lo), bool)
+    for dx in range(int(oext[:, 0].max(initial=0)) + 1):
+        for dy in range(int(oext[:, 1].max(initial=0)) + 1):
+            for dz in range(int(oext[:, 2].max(initial=0)) + 1):
+                sel = (oext[:, 0] >= dx) & (oext[:, 1] >= dy) & (oext[:, 2] >= dz) & ~near
+                idx = np.nonzero(sel)[0]
+                hit = np.isin(_cell_keys(o0[idx] + np.array([dx, dy, dz])), cells)
+                near[idx[hit]] = True
+    return near
+
+
+def instance_boxes(inst, batch: int = 8192):
+    """Box (lo, hi) of every instanced mesh, from its host expansion in
+    batches (the vertices of mesh m are contiguous)."""
+    import pierce_gb300 as pg
+    lo = np.empty((len(inst), 3), np.float32)
+    hi = np.empty((len(inst), 3), np.float32)
+    for s0 in range(0, len(inst), batch):
+        part = inst[s0:s0 + batch].copy()
+        part["group"] = 0
+        G = pg.expand_instances(part)
+        vobj = np.empty(G.vertices.shape[0], np.int64)
+        vobj[G.indices.reshape(-1)] = np.repeat(G.tri_to_object.astype(np.int64), 3)
+        if np.any(vobj[1:] < vobj[:-1]):
+            raise AssertionError("instanced vertices are not stored mesh by mesh")
+        starts = np.searchsorted(vobj, np.arange(len(part)))
+        lo[s0:s0 + len(part)] = np.minimum.reduceat(G.vertices, starts)
+        hi[s0:s0 + len(part)] = np.maximum.reduceat(G.vertices, starts)
+    return lo, hi
+
+
+def tube_sample(k: int, scale: float = 1.0, inst_b=None, boxes=None):
+    """The first k tubes and the ellipsoids whose boxes share a grid cell
+    with the box of one of their triangles: every ellipsoid that can meet
+    those tubes.  Returns (tubes, ellipsoids, ellipsoid ids)."""
+    import pierce_gb300 as pg
+    As = tube_geometry(scale, first=k)
+    if inst_b is None:
+        inst_b = ellipsoid_instances(scale)
+    lo, hi = boxes if boxes is not None else instance_boxes(inst_b)
+    tri = As.vertices[As.indices]
+    near = np.nonzero(boxes_near(tri.min(1), tri.max(1), lo, hi))[0]
+    del tri
+    sub = inst_b[near].copy()
+    sub["group"] = 0
+    Bs = pg.expand_instances(sub)
+    return As, Bs, near
+
+
+def sample_keys_global(keys: np.ndarray, near: np.ndarray) -> np.ndarray:
+    """Pair keys (a << 32 | local b) of a sample -> keys with global b ids, sorted."""
+    a = keys >> np.uint64(32)
+    b = near.astype(np.uint64)[(keys & np.uint64(0xFFFFFFFF)).astype(np.int64)]
+    return np.sort((a << np.uint64(32)) | b)
+
+
+def run_reference_tubes(args):
+    """CPU restatement of the reference's overlap join (the oracle port, all
+    host threads) on the tube workload: each step joins the first
+    --cpu-sample-tubes tubes with every ellipsoid near them; the join
+    queries/s of the whole join are the sample's time scaled by the tube
+    count (every tube holds the same triangle budget)."""
+    from oracle import pyoracle as O
+    O.build()
+    n_tubes, _ = tube_counts(args.scale)
+    k = max(1, min(n_tubes, args.cpu_sample_tubes))
+    t0 = time.perf_counter()
+    As, Bs, near = tube_sample(k, args.scale)
+    prep_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 0)):
+        O.overlap_keys(As, Bs)
+    times, npairs = [], 0
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        keys, _ = O.overlap_keys(As, Bs)
+        times.append(time.perf_counter() - t1)
+        npairs = len(keys)
+    step_s = statistics.mean(times)
+    full_s = step_s * n_tubes / k
+    value = 1.0 / full_s
+    sample = (f"tubes 0..{k - 1} ({As.num_triangles} triangles) of {n_tubes} against the {len(near)} ellipsoids "
+              f"near them ({Bs.num_triangles} triangles): {step_s:.3f} s per step ({npairs} pairs), "
+              f"scaled by {n_tubes}/{k}; sample set-up {prep_s:.1f} s untimed")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_s,
+            "ms_per_join_extrapolated": 1000.0 * full_s, "sample_fraction": k / n_tubes,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (exact predicates)",
+            "data": "synthetic", "config": tubes_config(args.scale),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
-    """CPU restatement of the reference path (the oracle port), all host threads."""
+    """CPU restatement of the reference path (the oracle port), all host
+    threads, on the workload of --workload; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    if args.workload == "tubes":
+        return run_reference_tubes(args)
     from oracle import pyoracle as O
     O.build()
     A, B, cfg = workload(args.scale)
@@ -226,7 +388,8 @@ def run_reference(args):
     sample = (f"spatial sub-cube holding {As.num_objects}+{Bs.num_objects} of "
               f"{A.num_objects}+{B.num_objects} objects (fraction {frac:.4f}); time scaled by 1/fraction")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * full_s,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_s,
+            "ms_per_step_extrapolated": 1000.0 * full_s, "sample_fraction": frac,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/exact",
             "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
@@ -312,206 +475,238 @@ def main_batched(args):
     return 0
 
 
-def main_tubes(args):
-    """Large tube-mesh overlap join: 2,000 branching tubes of about 200k
-    triangles against 100,000 perturbed ellipsoids, the tuned form (exact
-    predicates with FP32 filter, culling, per-join hierarchies, the
-    persistent ray queue, learned sizing) against the plain GPU form (dataset
-    hierarchies, FP32 Moller-Trumbore, two-pass sizing), both end to end from
-    pinned host buffers through the C ABI, plus the CPU oracle on a sample."""
-    import ctypes as C
+TRIANGLE_FIELDS = ("vertices", "indices", "tri_to_object")
+
+
+def pinned_view(G, keep: list):
+    """A pierce_mesh_view over pinned host copies of G's arrays (the copies
+    are appended to keep).  Returns (view, bytes of the triangle arrays,
+    bytes of the edge arrays)."""
     import torch
-    import pierce_gb300 as pg
     from pierce_gb300 import capi
-    from pierce_gb300 import join as J
-    from pierce_gb300 import sizing as S
-    log = lambda m: print(m, file=sys.stderr, flush=True)
-    n_tubes = max(2, int(round(2000 * args.scale)))
-    n_ell = max(2, int(round(100_000 * args.scale)))
-    t0 = time.perf_counter()
-    A = pg.tubes(5, n_tubes, 200_000, 1.0, 0.02, 0.5, 3.0, 12, 0.0, 1000.0)
-    B = pg.expand_instances(pg.instances(6, n_ell, pg.ELLIPSOIDS, 3, p0=2.0, p1=5.0, noise_amp=0.05,
-                                         lo=0.0, hi=1000.0))
-    log(f"tubes {A.num_triangles / 1e6:.0f} M tris, ellipsoids {B.num_triangles / 1e6:.0f} M tris "
-        f"({time.perf_counter() - t0:.1f} s host generation)")
-    # CPU oracle sample: a few tubes against the ellipsoids near them.  An
-    # ellipsoid is kept when its box meets a grid cell that the box of one of
-    # the sampled tubes' triangles meets, a superset of the ellipsoids that
-    # can meet those tubes, so the sample's pair set is exact.
-    k = max(1, min(n_tubes, args.cpu_sample_tubes))
-    tri_obj = A.tri_to_object
-    tmask = tri_obj < k
-    As = pg.Geometry.from_arrays(A.vertices, A.indices[tmask], tri_obj[tmask])
-    em = A.edge_src < k
-    As.set_edges(A.edge_starts[em], A.edge_ends[em], A.edge_src[em])
-    cell = 8.0
-    ta = A.vertices[A.indices[tmask]]
-    c_lo = np.floor(ta.min(1) / cell).astype(np.int64)
-    c_hi = np.floor(ta.max(1) / cell).astype(np.int64)
-    cells = set()
-    for lo_c, hi_c in zip(c_lo, c_hi):
-        for x in range(lo_c[0], hi_c[0] + 1):
-            for y in range(lo_c[1], hi_c[1] + 1):
-                for z in range(lo_c[2], hi_c[2] + 1):
-                    cells.add((x, y, z))
-    bobj = B.tri_to_object
-    blo = np.full((B.num_objects, 3), np.inf, np.float32)
-    bhi = np.full((B.num_objects, 3), -np.inf, np.float32)
-    tri = B.vertices[B.indices]
-    np.minimum.at(blo, bobj, tri.min(1))
-    np.maximum.at(bhi, bobj, tri.max(1))
-    del tri
-    b_lo = np.floor(blo / cell).astype(np.int64)
-    b_hi = np.floor(bhi / cell).astype(np.int64)
-    keep = np.zeros(B.num_objects, bool)
-    for o in range(B.num_objects):
-        lo_c, hi_c = b_lo[o], b_hi[o]
-        keep[o] = any((x, y, z) in cells for x in range(lo_c[0], hi_c[0] + 1)
-                      for y in range(lo_c[1], hi_c[1] + 1) for z in range(lo_c[2], hi_c[2] + 1))
-    near = np.nonzero(keep)[0]
-    remap = -np.ones(B.num_objects, np.int64)
-    remap[near] = np.arange(len(near))
-    bm = remap[bobj] >= 0
-    Bs = pg.Geometry.from_arrays(B.vertices, B.indices[bm], remap[bobj[bm]].astype(np.int32))
-    ebm = remap[B.edge_src] >= 0
-    Bs.set_edges(B.edge_starts[ebm], B.edge_ends[ebm], remap[B.edge_src[ebm]].astype(np.int32))
-    from oracle import pyoracle as O
-    tc = time.perf_counter()
-    cpu_keys, _ = O.overlap_keys(As, Bs)
-    cpu_s = time.perf_counter() - tc
-    log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s, {len(cpu_keys)} pairs")
+    ptr, nbytes = {}, {}
+    for field in ("vertices", "indices", "tri_to_object", "edge_starts", "edge_ends", "edge_src"):
+        src = np.ascontiguousarray(getattr(G, field))
+        pin = torch.empty(max(src.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        pin.numpy()[:src.nbytes] = src.view(np.uint8).reshape(-1)
+        keep.append(pin)
+        ptr[field] = pin.data_ptr()
+        nbytes[field] = src.nbytes
+    v = capi.MeshView()
+    v.vertices, v.num_vertices = ptr["vertices"], G.vertices.shape[0]
+    v.indices, v.num_triangles = ptr["indices"], G.num_triangles
+    v.tri_to_object = ptr["tri_to_object"]
+    v.edge_starts, v.edge_ends, v.edge_src = ptr["edge_starts"], ptr["edge_ends"], ptr["edge_src"]
+    v.num_edges, v.num_objects = G.num_edges, G.num_objects
+    tri = sum(nbytes[f] for f in TRIANGLE_FIELDS)
+    return v, tri, sum(nbytes.values()) - tri
 
-    ctx = J.Context(0)
-    L = capi.lib()
-    pins, h2d = {}, 0
-    for name, G in (("A", A), ("B", B)):
-        for field in ("vertices", "indices", "tri_to_object", "edge_starts", "edge_ends", "edge_src"):
-            src = np.ascontiguousarray(getattr(G, field))
-            pin = torch.empty(src.nbytes, dtype=torch.uint8, pin_memory=True)
-            pin.numpy()[:] = src.view(np.uint8).reshape(-1)
-            pins[(name, field)] = pin
-            h2d += src.nbytes
-    shapes = {n: (G.vertices.shape[0], G.num_triangles, G.num_edges, G.num_objects) for n, G in (("A", A), ("B", B))}
 
-    def view_of(name):
-        nv, nt, ne, no = shapes[name]
-        v = capi.MeshView()
-        v.vertices, v.num_vertices = pins[(name, "vertices")].data_ptr(), nv
-        v.indices, v.num_triangles = pins[(name, "indices")].data_ptr(), nt
-        v.tri_to_object = pins[(name, "tri_to_object")].data_ptr()
-        v.edge_starts = pins[(name, "edge_starts")].data_ptr()
-        v.edge_ends = pins[(name, "edge_ends")].data_ptr()
-        v.edge_src = pins[(name, "edge_src")].data_ptr()
-        v.num_edges, v.num_objects = ne, no
-        return v
+class E2E:
+    """One end-to-end join through the C ABI: both datasets created from
+    pinned host buffers (views with every `.pre` array), the join, the pairs
+    copied to pinned host memory, the datasets destroyed."""
 
-    views = {"A": view_of("A"), "B": view_of("B")}
-    upload = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
-    model = S.SizingModel.load(ctx, S.TRAINED_MODEL)
-    tuned_o = J.make_opts(predicate="overlap", sizing="learned", sizing_model=model)
-    plain_o = J.make_opts(predicate="overlap", sizing="two_pass", precision="fp32", cull_objects=False,
-                          defer_exact=False, active_bvh=False)
-    out_pin = torch.empty(8 * (1 << 26), dtype=torch.uint8, pin_memory=True)
+    def __init__(self, ctx, views, out_pairs: int):
+        import torch
+        from pierce_gb300 import capi
+        self.ctx, self.views = ctx, views
+        self.L = capi.lib()
+        self.out = torch.empty(8 * out_pairs, dtype=torch.uint8, pin_memory=True)
 
-    def e2e_step(opts, build):
+    def step(self, opts, upload, build_tuning=None, want_keys=False):
+        """upload: the datasets' pierce_tuning (skip_edges = 1: the edge
+        arrays are neither read nor copied)."""
+        import ctypes as C
+        from pierce_gb300 import capi
+        from pierce_gb300 import join as J
+        L, ctx = self.L, self.ctx
         ha, hb = C.c_void_p(), C.c_void_p()
-        capi.check(L.pierce_dataset_create(ctx.handle, C.byref(views["A"]), capi.HOST_MEMORY, C.byref(upload),
+        capi.check(L.pierce_dataset_create(ctx.handle, C.byref(self.views[0]), capi.HOST_MEMORY, C.byref(upload),
                                            C.byref(ha)), "dataset A")
-        capi.check(L.pierce_dataset_create(ctx.handle, C.byref(views["B"]), capi.HOST_MEMORY, C.byref(upload),
+        capi.check(L.pierce_dataset_create(ctx.handle, C.byref(self.views[1]), capi.HOST_MEMORY, C.byref(upload),
                                            C.byref(hb)), "dataset B")
-        if build:
-            capi.check(L.pierce_dataset_build(ctx.handle, ha, C.byref(J.default_tuning(leaf_size=args.plain_leaf_size))),
-                       "build A")
-            capi.check(L.pierce_dataset_build(ctx.handle, hb, C.byref(J.default_tuning(leaf_size=args.plain_leaf_size))),
-                       "build B")
+        if build_tuning is not None:
+            capi.check(L.pierce_dataset_build(ctx.handle, ha, C.byref(build_tuning)), "build A")
+            capi.check(L.pierce_dataset_build(ctx.handle, hb, C.byref(build_tuning)), "build B")
         r = C.c_void_p()
         st = capi.Stats()
         capi.check(L.pierce_join(ctx.handle, ha, hb, C.byref(opts), C.byref(r), C.byref(st)), "join")
         n = C.c_uint64()
         L.pierce_result_count(r, C.byref(n))
-        cap = min(n.value, out_pin.numel() // 8)
-        capi.check(L.pierce_result_copy(ctx.handle, r, out_pin.data_ptr(), cap), "copy")
-        keys = None
-        if collect_keys[0]:
-            keys = J.pairs_to_keys(out_pin.numpy()[:8 * cap].view(np.int32).reshape(-1, 2).copy())
+        cap = min(n.value, self.out.numel() // 8)
+        capi.check(L.pierce_result_copy(ctx.handle, r, self.out.data_ptr(), cap), "copy")
+        keys = J.pairs_to_keys(self.out.numpy()[:8 * cap].view(np.int32).reshape(-1, 2).copy()) if want_keys else None
         L.pierce_result_destroy(r)
         L.pierce_dataset_destroy(ha)
         L.pierce_dataset_destroy(hb)
         return st.as_dict(), keys, 8 * cap
 
-    collect_keys = [True]
-    st_t, keys_t, d2h_t = e2e_step(tuned_o, False)
-    ctx.release_scratch()
-    st_p, keys_p, d2h_p = e2e_step(plain_o, True)
-    ctx.release_scratch()
-    collect_keys[0] = False
-    identical = bool(np.array_equal(keys_t, keys_p))
-    sample_gpu = keys_t[(keys_t >> np.uint64(32)) < np.uint64(k)]
-    near64 = near.astype(np.uint64)
-    cpu_global = ((cpu_keys >> np.uint64(32)) << np.uint64(32)) | near64[(cpu_keys & np.uint64(0xFFFFFFFF)).astype(np.int64)]
-    sample_match = bool(np.array_equal(np.sort(sample_gpu), np.sort(cpu_global)))
-    log(f"pairs {len(keys_t)} tuned == plain: {identical}; sample vs oracle: {sample_match}")
-    clocks = Clocks(clocks_path("clocks_tubes.csv"))
-    res = {}
-    with clocks:
-        for name, opts, build in (("tuned", tuned_o, False), ("plain", plain_o, True)):
-            for _ in range(max(1, args.warmup - 1)):
-                e2e_step(opts, build)
-            ctx.synchronize()
-            ts = time.perf_counter()
-            sts = [e2e_step(opts, build)[0] for _ in range(args.steps)]
-            res[name] = {"e2e_s": (time.perf_counter() - ts) / args.steps, "stats": sts[-1]}
-            ctx.release_scratch()
-    # device-resident legs: the same joins with inputs already in HBM
-    da = J.Dataset.from_geometry(ctx, A, upload)
-    db = J.Dataset.from_geometry(ctx, B, upload)
+
+def main_tubes(args):
+    """Large tube-mesh overlap join (the default line): the tuned form with
+    inputs resident in HBM (value), end to end through the C ABI (e2e), the
+    plain GPU form, the edge-ray roofline and the CPU oracle on a sample."""
+    import torch
+    import pierce_gb300 as pg
+    from pierce_gb300 import join as J
+    from pierce_gb300 import sizing as S
+    from oracle import pyoracle as O
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    n_tubes, n_ell = tube_counts(args.scale)
+    t0 = time.perf_counter()
+    A = tube_geometry(args.scale)
+    inst_b = ellipsoid_instances(args.scale)
+    inst_b_host = inst_b.copy()
+    inst_b_host["group"] = 0
+    B = pg.expand_instances(inst_b_host)
+    log(f"tubes {A.num_triangles / 1e6:.0f} M tris, ellipsoids {B.num_triangles / 1e6:.0f} M tris "
+        f"({time.perf_counter() - t0:.1f} s host generation)")
+
+    # CPU oracle on a sample: the first k tubes against every ellipsoid near them
+    cpu, sample_keys = None, None
+    k = max(1, min(n_tubes, args.cpu_sample_tubes))
+    if not args.no_cpu_baseline:
+        tb = time.perf_counter()
+        As, Bs, near = tube_sample(k, args.scale, inst_b)
+        prep_s = time.perf_counter() - tb
+        tc = time.perf_counter()
+        cpu_keys, _ = O.overlap_keys(As, Bs)
+        cpu_s = time.perf_counter() - tc
+        sample_keys = sample_keys_global(cpu_keys, near)
+        cpu = {"value": 1.0 / (cpu_s * n_tubes / k), "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+               "sample": (f"tubes 0..{k - 1} of {n_tubes} against the {len(near)} ellipsoids near them: "
+                          f"{cpu_s:.2f} s, scaled by {n_tubes}/{k}")}
+        log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s ({prep_s:.1f} s set-up), "
+            f"{len(sample_keys)} pairs")
+
+    ctx = J.Context(0)
+    upload = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
+    model = S.SizingModel.load(ctx, S.TRAINED_MODEL)
+    tuned_o = J.make_opts(predicate="overlap", sizing="learned", sizing_model=model)
+    plain_o = J.make_opts(predicate="overlap", sizing="two_pass", precision="fp32", cull_objects=False,
+                          defer_exact=False, active_bvh=False)
+    plain_build = J.default_tuning(leaf_size=args.plain_leaf_size)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
 
-    def device_ms(fn, reps):
-        fn()
-        torch.cuda.synchronize()
+    # device-resident legs: inputs already in HBM
+    da = J.Dataset.from_geometry(ctx, A, upload)
+    db = J.Dataset.from_geometry(ctx, B, upload)
+    for _ in range(max(args.warmup, 3)):
+        r = J.run_join(ctx, da, db, tuned_o, download=False)
+    torch.cuda.synchronize()
+    clocks = Clocks(clocks_path("clocks_tubes.csv"))
+    l0 = ctx.kernel_launches
+    stats = []
+    with clocks:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(reps):
-            fn()
+        for _ in range(args.steps):
+            r = J.run_join(ctx, da, db, tuned_o, download=False)
+            stats.append(r.stats)
         e1.record(stream)
         e1.synchronize()
-        return e0.elapsed_time(e1) / reps
-
-    tuned_ms = device_ms(lambda: J.run_join(ctx, da, db, tuned_o, download=False), args.steps)
+    launches = ctx.kernel_launches - l0
+    tuned_ms = e0.elapsed_time(e1) / args.steps
+    st = stats[-1]
+    tuned = J.run_join(ctx, da, db, tuned_o)
+    keys_t = J.pairs_to_keys(tuned.pairs)
     ctx.release_scratch()
 
+    # plain form on the same resident data: dataset hierarchies + two-pass join
     def plain_dev():
-        da.build(J.default_tuning(leaf_size=args.plain_leaf_size))
-        db.build(J.default_tuning(leaf_size=args.plain_leaf_size))
-        J.run_join(ctx, da, db, plain_o, download=False)
+        da.build(plain_build)
+        db.build(plain_build)
+        return J.run_join(ctx, da, db, plain_o, download=False)
 
-    plain_ms = device_ms(plain_dev, max(1, args.steps // 2))
-    st = res["tuned"]["stats"]
+    plain_dev()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    plain_steps = max(1, min(args.steps, 3))
+    p0.record(stream)
+    for _ in range(plain_steps):
+        plain_dev()
+    p1.record(stream)
+    p1.synchronize()
+    plain_ms = p0.elapsed_time(p1) / plain_steps
+    keys_p = J.pairs_to_keys(J.run_join(ctx, da, db, plain_o).pairs)
+    identical = bool(np.array_equal(keys_t, keys_p))
+    sample_match = None
+    if sample_keys is not None:
+        sample_match = bool(np.array_equal(np.sort(keys_t[(keys_t >> np.uint64(32)) < np.uint64(k)]), sample_keys))
+    log(f"tuned {tuned_ms:.2f} ms, plain {plain_ms:.2f} ms; {len(keys_t)} pairs; tuned == plain: {identical}; "
+        f"sample == oracle: {sample_match}")
+    da.close()
+    db.close()
+    ctx.release_scratch()
+
+    # end to end through the C ABI from pinned host buffers.  The tuned form
+    # traces its kept triangles' edges, so its datasets skip the edge arrays
+    # (skip_edges); the plain form traces the edge list and uploads it.
+    keep = []
+    va, a_tri, a_edge = pinned_view(A, keep)
+    vb, b_tri, b_edge = pinned_view(B, keep)
+    e2e = E2E(ctx, (va, vb), out_pairs=max(1 << 22, 2 * len(keys_t)))
+    upload_tri = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
+
+    def timed(opts, up, build, n):
+        e2e.step(opts, up, build)
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(n):
+            e2e.step(opts, up, build)
+        dt = (time.perf_counter() - t1) / n
+        ctx.release_scratch()
+        return dt
+
+    _, keys_e, d2h = e2e.step(tuned_o, upload_tri, want_keys=True)
+    e2e_identical = bool(np.array_equal(keys_e, keys_t))
+    e2e_s = timed(tuned_o, upload_tri, None, max(1, min(args.steps, 5)))
+    e2e_edges_s = timed(tuned_o, upload, None, max(1, min(args.steps, 2)))
+    plain_e2e_s = timed(plain_o, upload, plain_build, max(1, min(args.steps, 2)))
+    log(f"e2e tuned {1000 * e2e_s:.1f} ms ({1000 * e2e_edges_s:.1f} ms uploading the edges too), "
+        f"plain {1000 * plain_e2e_s:.1f} ms")
+
+    # roofline of the dominant kernel: the edge rays of both directions
+    edge_ms = st["ms_edge_rays"][0] + st["ms_edge_rays"][1]
+    act = st["active_triangles"]
+    traced_bytes = traced_edge_ray_bytes(st["rays"], st["raw_hits"], [(B, act[1]), (A, act[0])])
+    achieved = traced_bytes / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else 0.0
+    peak, peak_kind = peaks()
+    cfg = tubes_config(args.scale)
     line = {
         "metric": METRIC, "value": 1000.0 / tuned_ms, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": tuned_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic",
-        "config": {"workload": "tubes-vs-ellipsoids-overlap", "tubes": n_tubes, "tube_triangles": A.num_triangles,
-                   "ellipsoids": n_ell, "ellipsoid_triangles": B.num_triangles, "leaf_size": args.leaf_size,
-                   "sizing": "learned", "l2": "inputs larger than L2"},
-        "e2e": {"value": 1.0 / res["tuned"]["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h_t), "ms_per_step": 1000.0 * res["tuned"]["e2e_s"]},
-        "plain": {"e2e": {"value": 1.0 / res["plain"]["e2e_s"], "ms_per_step": 1000.0 * res["plain"]["e2e_s"]},
-                  "device": {"value": 1000.0 / plain_ms, "ms_per_step": plain_ms},
+        "warmup": max(args.warmup, 3), "ms_per_step": tuned_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic", "config": cfg,
+        "settings": {"leaf_size": args.leaf_size, "plain_leaf_size": args.plain_leaf_size, "sizing": "learned",
+                     "precision": "exact (fp32 filter, fp64, expansions)", "parallelism": "single GPU"},
+        "sizes": {"tube_triangles": A.num_triangles, "tube_edges": A.num_edges,
+                  "ellipsoid_triangles": B.num_triangles, "ellipsoid_edges": B.num_edges},
+        "ray_tri_tests_per_s": st["tri_tests"] / (st["ms_total"] / 1000.0) if st["ms_total"] > 0 else None,
+        "rays_per_s": st["rays"] / (edge_ms / 1000.0) if edge_ms > 0 else None,
+        "pairs": len(keys_t), "identical_tuned_plain": identical, "identical_e2e": e2e_identical,
+        "sample_matches_oracle": sample_match,
+        "phase_ms": {"total": st["ms_total"], "builds_and_culling": st["ms_build"],
+                     "edge_rays": st["ms_edge_rays"], "dedup": st["ms_dedup"], "sizing": st["ms_sizing"]},
+        "tuned_stats": {k2: st[k2] for k2 in ("rays", "tri_tests", "node_visits", "raw_hits", "fp32_ambiguous",
+                                              "fp64_ambiguous", "predicted_pairs", "sizing_overflow", "hash_slots",
+                                              "active_triangles", "launches")},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic_estimate(st["rays"], "tubes"),
+                     "kernel": "k_edge_rays, both directions of the tube join", "peak_kind": peak_kind,
+                     "algorithmic_bytes": traced_bytes, "kernel_ms": edge_ms},
+        "plain": {"value": 1000.0 / plain_ms, "unit": UNIT, "ms_per_step": plain_ms,
                   "form": "dataset BVH builds + fp32 Moller-Trumbore two-pass join, no culling",
-                  "e2e_speedup_tuned": res["plain"]["e2e_s"] / res["tuned"]["e2e_s"],
-                  "device_speedup_tuned": plain_ms / tuned_ms},
-        "pairs": len(keys_t), "identical_tuned_plain": identical, "sample_matches_oracle": sample_match,
-        "tuned_stats": {k2: st[k2] for k2 in ("ms_total", "ms_build", "ms_edge_rays", "ms_dedup", "ms_sizing",
-                                                "rays", "tri_tests", "fp32_ambiguous", "fp64_ambiguous",
-                                                "predicted_pairs", "sizing_overflow", "hash_slots",
-                                                "active_triangles")},
-        "cpu_baseline": {"value": 1.0 / (cpu_s * n_tubes / k), "unit": UNIT, "cores": O.max_threads(),
-                         "kind": "port",
-                         "sample": f"{k} of {n_tubes} tubes against the {len(near)} ellipsoids whose boxes meet "
-                                   f"them: {cpu_s:.2f} s, scaled by {n_tubes}/{k}"},
-        "gpu_launches": int(st["launches"]), "clocks": clocks.summary(0),
+                  "tuned_speedup": plain_ms / tuned_ms,
+                  "e2e": {"value": 1.0 / plain_e2e_s, "ms_per_step": 1000.0 * plain_e2e_s,
+                          "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)},
+                  "e2e_speedup_tuned": plain_e2e_s / e2e_s},
+        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(a_tri + b_tri),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s,
+                "edges_uploaded": False,
+                "with_edge_upload": {"value": 1.0 / e2e_edges_s, "ms_per_step": 1000.0 * e2e_edges_s,
+                                     "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)}},
+        "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks.summary(0),
     }
     print(json.dumps(line))
     return 0
@@ -599,10 +794,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf-size", type=int, default=4, help="leaf size of the tuned form's per-join hierarchies")
     ap.add_argument("--plain-leaf-size", type=int, default=8, help="leaf size of the plain form's dataset hierarchies")
-    ap.add_argument("--workload", default="ellipsoids", choices=["ellipsoids", "batched", "tubes", "preprocess"],
-                    help="ellipsoids: the default intersection+containment line; batched: 4,096 overlap queries; "
-                         "tubes: 2,000 tubes against 100,000 ellipsoids; preprocess: edge extraction of the "
-                         ".pre producer on the host cores")
+    ap.add_argument("--workload", default="tubes", choices=["tubes", "ellipsoids", "batched", "preprocess"],
+                    help="tubes (default): 2,000 tubes against 100,000 ellipsoids, overlap; ellipsoids: "
+                         "intersection + containment of 2 x 50,000 ellipsoids; batched: 4,096 overlap queries; "
+                         "preprocess: edge extraction of the .pre producer on the host cores")
     ap.add_argument("--cpu-sample-tubes", type=int, default=10)
     ap.add_argument("--wave-tris", type=float, default=1.0e9, help="batched: triangles per wave (both sides)")
     args = ap.parse_args()
@@ -614,7 +809,12 @@ def main():
         return main_tubes(args)
     if args.workload == "preprocess":
         return main_preprocess(args)
+    return main_ellipsoids(args)
 
+
+def main_ellipsoids(args):
+    """Intersection + containment joins of 2 x 50,000 ellipsoids; under
+    torchrun every rank runs a replica (weak scaling, max time over ranks)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -722,7 +922,9 @@ def main():
                 pin = torch.empty(src.nbytes, dtype=torch.uint8, pin_memory=True)
                 pin.numpy()[:] = src.view(np.uint8).reshape(-1)
                 arrs[(name, field)] = (pin, src.shape)
-        h2d = sum(p.numel() for p, _ in arrs.values())
+        # the tuned joins trace their kept triangles' edges: the datasets
+        # skip the edge arrays (skip_edges), so only the triangle arrays move
+        h2d = sum(p.numel() for (nm, f), (p, _) in arrs.items() if f in TRIANGLE_FIELDS)
 
         def view_of(name, G):
             v = capi.MeshView()
@@ -739,7 +941,7 @@ def main():
             return v
 
         va, vb = view_of("A", A), view_of("B", B)
-        upload_only = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
+        upload_only = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
         out_pairs = torch.empty(8 * (1 << 22), dtype=torch.uint8, pin_memory=True)
 
         def e2e_step():
@@ -771,7 +973,8 @@ def main():
             d2h_total += e2e_step()
         e2e_s = (time.perf_counter() - t0) / e2e_steps
         e2e = {"value": 2.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h_total // e2e_steps), "ms_per_step": 1000.0 * e2e_s}
+               "d2h_bytes_per_step": int(d2h_total // e2e_steps), "ms_per_step": 1000.0 * e2e_s,
+               "edges_uploaded": False}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -789,14 +992,13 @@ def main():
     if rank != 0:
         return 0
     clk = clocks.summary(local_rank)
-    cfg.update({"l2": "inputs larger than L2 (about 9 GB of geometry and BVH per side, 129 MB L2)",
-                "leaf_size": args.leaf_size, "plain_leaf_size": args.plain_leaf_size, "sizing": "hash",
-                "precision": "exact (fp32 filter, fp64, expansions)",
-                "parallelism": f"replicas x{world}" if world > 1 else "single GPU"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic", "config": cfg,
+        "settings": {"leaf_size": args.leaf_size, "plain_leaf_size": args.plain_leaf_size, "sizing": "hash",
+                     "precision": "exact (fp32 filter, fp64, expansions)",
+                     "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "ray_tri_tests_per_s": tri_tests / (join_ms / 1000.0) if join_ms > 0 else None,
         "rays_per_s": (ri.stats["rays"]) / (edge_ms / 1000.0) if edge_ms > 0 else None,
         "pairs": {"intersection": ri.stats["num_pairs"], "containment": rc.stats["num_pairs"]},
@@ -810,7 +1012,8 @@ def main():
                        "unit": UNIT, "note": "BVH builds excluded, as in the reference benchmark adapters"},
         "active_triangles": list(ri.stats["active_triangles"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic_estimate(ri.stats["rays"]),
+                     "frac": achieved / peak if peak else None,
+                     "traffic": traffic_estimate(ri.stats["rays"], "ellipsoids"),
                      "kernel": "k_edge_rays (exact, hash mode), both directions of the intersection join",
                      "peak_kind": peak_kind, "algorithmic_bytes": traced_bytes,
                      "unculled_equivalent_gbs": unculled_bytes / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else None},

@@ -142,7 +142,18 @@ typedef struct pierce_tuning {
     int32_t sort_rays;        /* 1: trace edge rays in Morton order of their midpoints */
     int32_t cull_objects;     /* 1: skip source objects whose box meets no target object */
     int32_t defer_build;      /* 1: pierce_dataset_create uploads only; call pierce_dataset_build */
+    int32_t skip_edges;       /* 1: pierce_dataset_create neither reads nor uploads the view's edge arrays
+                                 (joins then take their rays from the triangles: edge_source) */
 } pierce_tuning;
+
+/* Where a join's edge rays come from (pierce_join_opts.edge_source). */
+enum pierce_edge_source {
+    PIERCE_EDGES_AUTO = 0,       /* triangles wherever the join builds grouped per-join hierarchies, else the
+                                    dataset's edges (triangles when the dataset has none) */
+    PIERCE_EDGES_DATASET = 1,    /* the dataset's edge list (the `.pre` edges) */
+    PIERCE_EDGES_TRIANGLES = 2   /* the edges of the triangles kept for the join's per-join hierarchies, each
+                                    segment of a leaf group once (needs active_bvh) */
+};
 
 typedef struct pierce_join_opts {
     int32_t predicate;            /* pierce_predicate */
@@ -168,6 +179,11 @@ typedef struct pierce_join_opts {
     int32_t traversal;            /* culled rays: 0 one ray per thread over four-wide copies of the per-join
                                      hierarchies, 1 a warp traverses its 32 rays together, 2 one ray per thread
                                      over the binary nodes */
+    int32_t edge_source;          /* pierce_edge_source.  Exact predicates give the same pairs from either
+                                     source when the dataset's edges are its triangles' edges (as
+                                     pierce_preprocess extracts them): a segment's hits do not depend on
+                                     its orientation */
+    int32_t reserved;
 } pierce_join_opts;
 
 typedef struct pierce_stats {

@@ -132,6 +132,13 @@ int pierce_gen_ellipsoid_pair(uint64_t seed_a, uint64_t seed_b,
 int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris,
                      double step, double branch_prob, double r_lo, double r_hi,
                      int32_t n_sides, double lo, double hi, pierce_geom** out);
+/* The first `first_meshes` tubes of pierce_gen_tubes(seed, num_meshes, ...),
+ * bit-identical to those meshes of the full dataset (same object ids and
+ * coordinates; vertex indices renumbered): samples of a large tube dataset
+ * without building all of it. */
+int pierce_gen_tubes_head(uint64_t seed, int32_t num_meshes, int32_t first_meshes, int64_t target_tris,
+                          double step, double branch_prob, double r_lo, double r_hi,
+                          int32_t n_sides, double lo, double hi, pierce_geom** out);
 
 /* Unit icosphere template: counts[0..2] = vertices, triangles, unique edges;
  * any output array may be NULL (query counts first). vertices: 3 doubles each,

@@ -37,6 +37,7 @@ HOST_MEMORY = 0
 DEVICE_MEMORY = 1
 
 OVERLAP, INTERSECTION, CONTAINMENT = 0, 1, 2
+EDGES_AUTO, EDGES_DATASET, EDGES_TRIANGLES = 0, 1, 2
 BOTH, MESH1_TO_MESH2, MESH2_TO_MESH1 = 0, 1, 2
 SIZING_TWO_PASS, SIZING_HASH, SIZING_FIXED, SIZING_LEARNED = 0, 1, 2, 3
 EXACT, FP32 = 0, 1
@@ -60,7 +61,7 @@ assert INSTANCE_DTYPE.itemsize == 168
 
 class Tuning(C.Structure):
     _fields_ = [("leaf_size", I32), ("block_size", I32), ("sort_rays", I32), ("cull_objects", I32),
-                ("defer_build", I32)]
+                ("defer_build", I32), ("skip_edges", I32)]
 
 
 class JoinOpts(C.Structure):
@@ -68,7 +69,8 @@ class JoinOpts(C.Structure):
                 ("expected_pairs", U64), ("hash_table_slots", U64), ("hash_load_factor", D),
                 ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
                 ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V),
-                ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("traversal", I32)]
+                ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("traversal", I32),
+                ("edge_source", I32), ("reserved", I32)]
 
 
 class Stats(C.Structure):

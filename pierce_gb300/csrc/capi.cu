@@ -32,6 +32,8 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
                       uint8_t* chunk_active, uint32_t* list, unsigned long long* count, float* chunk_box,
                       uint32_t* chunk_list, unsigned long long* chunk_count);
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
+int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
+                     const int32_t* obj_part, uint32_t* list, unsigned long long* count);
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots);
@@ -450,6 +452,7 @@ void pierce_default_tuning(pierce_tuning* t) {
     t->sort_rays = 0;
     t->cull_objects = 0;
     t->defer_build = 0;
+    t->skip_edges = 0;
 }
 
 void pierce_default_join_opts(pierce_join_opts* o) {
@@ -644,10 +647,14 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
                           pierce_dataset** out) {
     if (!ctx || !v || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: null argument");
     *out = nullptr;
+    // skip_edges: the edge arrays are neither read nor uploaded (the joins
+    // take their rays from the triangles)
+    const bool skip_edges = tuning && tuning->skip_edges;
+    const uint64_t num_edges = skip_edges ? 0 : v->num_edges;
     if ((v->num_vertices && !v->vertices) || (v->num_triangles && (!v->indices || !v->tri_to_object)) ||
-        (v->num_edges && (!v->edge_starts || !v->edge_ends || !v->edge_src)))
+        (num_edges && (!v->edge_starts || !v->edge_ends || !v->edge_src)))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: missing array");
-    if (v->num_triangles >= (1ull << 31) || v->num_edges >= (1ull << 40) || v->num_vertices >= (1ull << 32))
+    if (v->num_triangles >= (1ull << 31) || num_edges >= (1ull << 40) || v->num_vertices >= (1ull << 32))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: dataset too large for 32-bit ids");
     cudaSetDevice(ctx->device);
     const cudaMemcpyKind kind = memory == PIERCE_DEVICE_MEMORY ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -656,7 +663,7 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
     ds->device = ctx->device;
     ds->nv = v->num_vertices;
     ds->nt = v->num_triangles;
-    ds->ne = v->num_edges;
+    ds->ne = num_edges;
     cudaStream_t st = ctx->stream;
     int s = PIERCE_OK;
     do {
@@ -883,6 +890,44 @@ struct Join {
     // direction and the queue of deferred exact tests.
     bool listed[2] = {false, false};
     uint32_t* list[2] = {nullptr, nullptr};
+    // rays from triangles, per direction: the source side's per-join soup
+    // (list entries name its triangles' edges) and the list's capacity
+    const float4* ray_soup[2] = {nullptr, nullptr};
+    int64_t ray_bound[2] = {-1, -1};
+    // rays the launches of direction d index (list capacity or edge count)
+    int64_t rays_of(int d) const { return ray_soup[d] ? ray_bound[d] : (int64_t)(d ? B->ne : A->ne); }
+    // whether side d takes its rays from its kept triangles
+    bool triangle_rays(int d, bool grouped) const {
+        const pierce_dataset* ds = d ? B : A;
+        if (o.edge_source == PIERCE_EDGES_TRIANGLES) return true;
+        if (o.edge_source == PIERCE_EDGES_DATASET) return false;
+        return grouped || (ds->ne == 0 && ds->nt > 0);
+    }
+    // Ray lists of the sides that trace their kept triangles' edges: the
+    // edges of the side's per-join soup, G triangles per group, listed group
+    // by group; a side's groups are filtered against the other side's
+    // per-join hierarchy unless `prefiltered[d]` (a culling round already
+    // kept only the groups that meet it).
+    int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2]) {
+        const DevDataset* v[2] = {&va, &vb};
+        const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA};
+        for (int d = 0; d < 2; ++d) {
+            if (!use[d]) continue;
+            const DevDataset& src = *v[d];
+            const DevDataset& other = *v[1 - d];
+            const int64_t n = src.soup ? src.num_tris : 0;
+            void* p = nullptr;
+            if (int s = scratch(ctx, slot[d], 4 * (3 * (size_t)n + 64), &p)) return s;
+            list[d] = static_cast<uint32_t*>(p);
+            if (int s = launch_soup_rays(ctx, src.soup, n, G[d], prefiltered[d] ? nullptr : &other,
+                                         (d ? B : A)->d_obj_part, list[d], words + d))
+                return s;
+            ray_soup[d] = src.soup;
+            ray_bound[d] = 3 * n;
+            listed[d] = true;
+        }
+        return PIERCE_OK;
+    }
     uint8_t* active = nullptr;
     // words: [0] list count A->B, [1] list count B->A, [2] warp cursor,
     //        [3] deferred-test count, [4] exactly resolved key count,
@@ -901,6 +946,7 @@ struct Join {
     // object pairs (both datasets store each object's triangles contiguously)
     DevDataset objA_{}, objB_{};
     bool object_parity = false;
+    bool a_groups_met_b_ = false;  // A's kept groups were filtered against B's per-join hierarchy
     ColumnGrid gridA_{}, gridB_{};  // parity candidates of each side as a target
 
     // Column grids of both sides' object boxes (scratch slots meta/entries):
@@ -944,7 +990,8 @@ struct Join {
             if (int s = scratch(ctx, SLOT_LIST_BA, 4 * (B->ne + 64), &p)) return s;
             list[1] = static_cast<uint32_t*>(p);
         }
-        amb_cap = std::min<uint64_t>(std::max<uint64_t>(A->ne + B->ne, 1024), 1ull << 24);
+        const uint64_t rays_hint = std::max<uint64_t>(A->ne + B->ne, 3 * (A->nt + B->nt) / 2);
+        amb_cap = std::min<uint64_t>(std::max<uint64_t>(rays_hint, 1024), 1ull << 24);
         if (int s = scratch(ctx, SLOT_AMB, 8 * amb_cap, &p)) return s;
         amb_queue = static_cast<unsigned long long*>(p);
         if (o.active_bvh) return prepare_active_bvh();
@@ -1115,26 +1162,39 @@ struct Join {
         if (grouped) {
             if (int s = grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, cull_b))
                 return s;
-            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
-                                          words + 0, nullptr, chunk_list, words + 8))
-                return s;
-            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, va, echunk_b, list[1],
-                                          words + 1, nullptr, chunk_list, words + 8))
-                return s;
+            const bool use[2] = {triangle_rays(0, true), triangle_rays(1, true)};
+            const int G[2] = {group_size(leaf_a), group_size(leaf_b)};
+            // A's groups were filtered against B's kept triangles already
+            const bool pre[2] = {a_groups_met_b_, false};
+            if (int s = soup_ray_lists(use, G, pre)) return s;
+            if (!use[0])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
+                                              words + 0, nullptr, chunk_list, words + 8))
+                    return s;
+            if (!use[1])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, va, echunk_b, list[1],
+                                              words + 1, nullptr, chunk_list, words + 8))
+                    return s;
             listed[0] = listed[1] = true;
             timer.span(b0, timer.record(), &st.ms_build);
             return PIERCE_OK;
         }
+        const bool use_tri[2] = {triangle_rays(0, false), triangle_rays(1, false)};
         if (chunked) {
-            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a, list[0],
-                                          words + 0, nullptr, chunk_list, words + 8))
-                return s;
-            if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, two_rounds ? cull_b : objA,
-                                          echunk_b, list[1], words + 1, nullptr, chunk_list, words + 8))
-                return s;
+            if (!use_tri[0])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, objB, echunk_a,
+                                              list[0], words + 0, nullptr, chunk_list, words + 8))
+                    return s;
+            if (!use_tri[1])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b,
+                                              two_rounds ? cull_b : objA, echunk_b, list[1], words + 1, nullptr,
+                                              chunk_list, words + 8))
+                    return s;
         } else {
-            if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
-            if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
+            if (!use_tri[0])
+                if (int s = launch_collect_rays(ctx, va, act_a, list[0], words + 0)) return s;
+            if (!use_tri[1])
+                if (int s = launch_collect_rays(ctx, vb, act_b, list[1], words + 1)) return s;
         }
         listed[0] = listed[1] = true;
         int64_t na = 0, nb = 0;
@@ -1173,6 +1233,13 @@ struct Join {
         vb.root_leaf_count = shB.root_leaf_count;
         if (int s = wide_nodes(va, shA.num_nodes, SLOT_NODES4_A)) return s;
         if (int s = wide_nodes(vb, shB.num_nodes, SLOT_NODES4_B)) return s;
+        {
+            // the hierarchies hold the triangles of active objects: each
+            // side's groups of 4 soup triangles against the other side's
+            const int G[2] = {4, 4};
+            const bool pre[2] = {false, false};
+            if (int s = soup_ray_lists(use_tri, G, pre)) return s;
+        }
         st.active_triangles[0] = (uint64_t)na;
         st.active_triangles[1] = (uint64_t)nb;
         timer.span(b0, timer.record(), &st.ms_build);
@@ -1239,6 +1306,7 @@ struct Join {
             else if (vb.nodes4 && !vb.root_is_leaf) filter = &vb;
             else filter = &objB_;
             if (!filter->nodes4) filter = nullptr;
+            if (sd == 0) a_groups_met_b_ = filter == &vb;
             BvhShape sh;
             int64_t kept = ng;
             if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
@@ -1282,7 +1350,7 @@ struct Join {
             const int64_t* offs = d ? off_ba : off_ab;
             const int b = timer.record();
             RayOpts ro;
-            if ((o.cull_objects || o.active_bvh) && src.num_edges > 0) {
+            if ((o.cull_objects || o.active_bvh) && (src.num_edges > 0 || ray_soup[d])) {
                 if (!listed[d]) {
                     if (int s = launch_cull(ctx, src, tgt, active, list[d], words + d)) return s;
                     listed[d] = true;
@@ -1290,7 +1358,9 @@ struct Join {
                 ro.list = list[d];
                 ro.count = words + d;
                 ro.cursor = words + 2;
-                if (mode == 0) cudaMemsetAsync(counts, 0, 4 * (size_t)src.num_edges, ctx->stream);
+                ro.soup = ray_soup[d];
+                ro.bound = rays_of(d);
+                if (mode == 0) cudaMemsetAsync(counts, 0, 4 * (size_t)rays_of(d), ctx->stream);
             }
             ro.rays_per_fetch = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
             ro.short_stack = o.stack_depth > 0 ? o.stack_depth : -1;
@@ -1383,7 +1453,7 @@ struct Join {
 
     // Two-pass overlap: count, scan, write, sort + unique into SLOT_KEYS.
     int overlap_two_pass(uint64_t** keys_out, uint64_t* n_out) {
-        const uint64_t na = ab ? A->ne : 0, nb = ba ? B->ne : 0;
+        const uint64_t na = ab ? (uint64_t)rays_of(0) : 0, nb = ba ? (uint64_t)rays_of(1) : 0;
         void* pc = nullptr;
         // counts (int32) and offsets (int64) for both directions
         const size_t cbytes = 4 * (na + nb) + 64, obytes = 8 * (na + nb) + 64;
@@ -1818,6 +1888,15 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
         o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 2)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
+    if (o.edge_source < 0 || o.edge_source > 2)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: edge_source out of range");
+    const bool edgeless = (a->ne == 0 && a->nt > 0) || (b->ne == 0 && b->nt > 0);
+    if (!o.active_bvh && (edgeless || o.edge_source == PIERCE_EDGES_TRIANGLES))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT,
+                         "join: without active_bvh the rays are the datasets' edges (a dataset has none, or "
+                         "edge_source asks for triangles)");
+    if (o.edge_source == PIERCE_EDGES_DATASET && edgeless)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: edge_source DATASET but a dataset has no edges");
     *out_opts = o;
     return PIERCE_OK;
 }

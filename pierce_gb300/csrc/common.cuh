@@ -110,6 +110,10 @@ struct RayOpts {
     int rays_per_fetch = 32;  // rays a warp takes from the list per fetch
     int short_stack = -1;     // shared-memory stack entries per thread (-1: default)
     int packets = 1;          // warp-cooperative traversal of the listed rays
+    // rays from triangles: list entries (t << 2 | k) are edges of this soup's
+    // triangles (the source side's per-join hierarchy)
+    const float4* soup = nullptr;
+    int64_t bound = -1;       // listed rays at most (-1: the source's edge count)
 };
 
 constexpr int kScratchSlots = 40;

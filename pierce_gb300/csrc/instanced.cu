@@ -163,7 +163,7 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
     ds->device = ctx->device;
     ds->nv = nv;
     ds->nt = nt;
-    ds->ne = ne;
+    ds->ne = (tuning && tuning->skip_edges) ? 0 : ne;  // skip_edges: rays come from the triangles
     ds->num_objects = num_meshes;
     void *d_blob = nullptr, *d_inst = nullptr, *d_off = nullptr;
     int s = PIERCE_OK;
@@ -200,9 +200,13 @@ extern "C" int pierce_dataset_create_instanced(pierce_ctx* ctx, const pierce_mes
             k_inst_triangles<<<grid_for(ctx, (int64_t)nt, 256), 256, 0, st>>>(di, dv, dt, num_meshes, ts,
                                                                              ds->d_indices, ds->d_tri_to_object,
                                                                              (int64_t)nt);
-            k_inst_edges<<<grid_for(ctx, (int64_t)ne, 256), 256, 0, st>>>(di, dv, de, num_meshes, ts, ds->d_vertices,
-                                                                         ds->d_edges, ds->d_edge_src, (int64_t)ne);
-            ctx->launches += 3;
+            ctx->launches += 2;
+            if (ds->ne) {
+                k_inst_edges<<<grid_for(ctx, (int64_t)ne, 256), 256, 0, st>>>(di, dv, de, num_meshes, ts,
+                                                                             ds->d_vertices, ds->d_edges,
+                                                                             ds->d_edge_src, (int64_t)ne);
+                ctx->launches += 1;
+            }
             if ((s = check_cuda(cudaGetLastError(), "instance expansion"))) break;
         }
         if (max_group > 0) {

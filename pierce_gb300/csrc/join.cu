@@ -130,7 +130,42 @@ struct EdgeRayParams {
     int rays_per_fetch;
     int short_stack;
     int packets;  // 1: a warp traverses its 32 rays together (ray-list mode)
+    // rays from triangles: list entries (t << 2 | k) name edge k of triangle
+    // t of this soup (the source side's per-join hierarchy) instead of a
+    // packed dataset edge
+    const float4* ray_soup;
+    int64_t ray_bound;  // ray indices of a listed launch lie below this
 };
+
+// The segment of ray e and its source object: packed dataset edge e, or --
+// with a ray soup -- edge k = e & 3 of soup triangle t = e >> 2: (v0, v1),
+// (v1, v2) or (v2, v0), v0 carrying the object id.
+__device__ __forceinline__ void load_ray(const EdgeRayParams& P, int64_t e, float3& p, float3& q, int32_t& obj) {
+    if (P.ray_soup) {
+        const float4* tri = P.ray_soup + 3 * (e >> 2);
+        const int k = (int)(e & 3);
+        const float4 v0 = __ldg(tri);
+        const float4 x = __ldg(tri + (k == 2 ? 2 : 1));  // v1 (k = 0, 1) or v2 (k = 2)
+        obj = __float_as_int(v0.w);
+        if (k == 0) {
+            p = make_float3(v0.x, v0.y, v0.z);
+            q = make_float3(x.x, x.y, x.z);
+        } else if (k == 1) {
+            const float4 v2 = __ldg(tri + 2);
+            p = make_float3(x.x, x.y, x.z);
+            q = make_float3(v2.x, v2.y, v2.z);
+        } else {
+            p = make_float3(x.x, x.y, x.z);
+            q = make_float3(v0.x, v0.y, v0.z);
+        }
+        return;
+    }
+    const float4 s4 = __ldg(P.src.edges + 2 * e);
+    const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
+    obj = __float_as_int(s4.w);
+    p = make_float3(s4.x, s4.y, s4.z);
+    q = make_float3(e4.x, e4.y, e4.z);
+}
 
 __device__ __forceinline__ bool box_overlap(float lx, float hx, float ly, float hy, float lz, float hz,
                                             const float3& lo, const float3& hi) {
@@ -264,17 +299,18 @@ __device__ __forceinline__ void leaf_tests(const EdgeRayParams& P, int64_t e, in
     }
 }
 
+// Ray e; `slot` indexes the per-ray counts and offsets of the two-pass
+// method (the ray's position in the launch's ray list, or e without one).
 template <int MODE, int PREC, bool WIDE = true>
-__device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int* sstack, int* lstack,
+__device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int64_t slot, int* sstack, int* lstack,
                                            RayCounters& rc, PredCounters& pc, int depth) {
     const int tid = threadIdx.x;
-    const float4 s4 = __ldg(P.src.edges + 2 * e);
-    const float4 e4 = __ldg(P.src.edges + 2 * e + 1);
-    const int32_t src_obj = __float_as_int(s4.w);
-    const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
+    float3 p, q;
+    int32_t src_obj;
+    load_ray(P, e, p, q, src_obj);
     const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
     const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
-    int64_t out = (MODE == MODE_WRITE) ? P.offsets[e] : 0;
+    int64_t out = (MODE == MODE_WRITE) ? P.offsets[slot] : 0;
     int32_t last_obj = -1;
     int nhit = 0;
     auto leaf = [&](int first, int count) {
@@ -379,7 +415,7 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
             }
         }
     }
-    if (MODE == MODE_COUNT) P.counts[e] = nhit;
+    if (MODE == MODE_COUNT) P.counts[slot] = nhit;
     rc.hits += (uint32_t)nhit;
 }
 
@@ -394,18 +430,15 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
 // the lanes start in different subtrees (partitions) each lane falls back
 // to the one-ray traversal with a local stack.
 template <int MODE, int PREC>
-__device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, int2* wstack, int* lstack,
-                                             RayCounters& rc, PredCounters& pc) {
+__device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, int64_t slot, int2* wstack,
+                                             int* lstack, RayCounters& rc, PredCounters& pc) {
     const int lane = threadIdx.x & 31;
     const bool valid = e >= 0;
     const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
     if (!vmask) return;
-    float4 s4 = make_float4(0, 0, 0, 0), e4 = make_float4(0, 0, 0, 0);
-    if (valid) {
-        s4 = __ldg(P.src.edges + 2 * e);
-        e4 = __ldg(P.src.edges + 2 * e + 1);
-    }
-    const int32_t src_obj = __float_as_int(s4.w);
+    float3 p = make_float3(0, 0, 0), q = make_float3(0, 0, 0);
+    int32_t src_obj = 0;
+    if (valid) load_ray(P, e, p, q, src_obj);
     int lf = 0, lc = 0;
     const int node0 = valid ? traversal_start(P.src, P.tgt, src_obj, lf, lc) : 0;
     const int leader = __ffs(vmask) - 1;
@@ -413,13 +446,12 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
     const int lf0 = __shfl_sync(0xFFFFFFFFu, lf, leader), lc0 = __shfl_sync(0xFFFFFFFFu, lc, leader);
     const bool same = __all_sync(0xFFFFFFFFu, !valid || (node0 == n0 && (n0 >= 0 || (lf == lf0 && lc == lc0))));
     if (!same) {
-        if (valid) trace_edge<MODE, PREC>(P, e, nullptr, lstack, rc, pc, 0);
+        if (valid) trace_edge<MODE, PREC>(P, e, slot, nullptr, lstack, rc, pc, 0);
         return;
     }
-    const float3 p = make_float3(s4.x, s4.y, s4.z), q = make_float3(e4.x, e4.y, e4.z);
     const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
     const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
-    int64_t out = (MODE == MODE_WRITE && valid) ? P.offsets[e] : 0;
+    int64_t out = (MODE == MODE_WRITE && valid) ? P.offsets[slot] : 0;
     int32_t last_obj = -1;
     int nhit = 0;
     auto leaf = [&](int first, int count) {
@@ -475,7 +507,7 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
         }
     }
     if (valid) {
-        if (MODE == MODE_COUNT) P.counts[e] = nhit;
+        if (MODE == MODE_COUNT) P.counts[slot] = nhit;
         rc.hits += (uint32_t)nhit;
     }
 }
@@ -508,10 +540,12 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
                 const unsigned long long i = base + r;
                 if (FORM == 2) {
                     const bool has = i < n;
-                    trace_packet<MODE, PREC>(P, has ? (int64_t)P.ray_list[i] : -1, wstack, lstack, rc, pc);
+                    trace_packet<MODE, PREC>(P, has ? (int64_t)P.ray_list[i] : -1, (int64_t)i, wstack, lstack, rc,
+                                             pc);
                     rays += has ? 1u : 0u;
                 } else if (i < n) {
-                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], sstack, lstack, rc, pc, P.short_stack);
+                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], (int64_t)i, sstack, lstack, rc, pc,
+                                           P.short_stack);
                     ++rays;
                 }
             }
@@ -519,7 +553,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     } else {
         const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         if (e < P.src.num_edges) {
-            trace_edge<MODE, PREC, false>(P, e, sstack, lstack, rc, pc, P.short_stack);
+            trace_edge<MODE, PREC, false>(P, e, e, sstack, lstack, rc, pc, P.short_stack);
             ++rays;
         }
     }
@@ -546,14 +580,15 @@ __global__ void __launch_bounds__(128) k_resolve_ambiguous(EdgeRayParams P, uint
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const unsigned long long ent = P.amb_queue[i];
         const int64_t e = (int64_t)(ent >> 32), t = (int64_t)(ent & 0xFFFFFFFFull);
-        const float4 s4 = __ldg(P.src.edges + 2 * e), e4 = __ldg(P.src.edges + 2 * e + 1);
+        float3 p, q;
+        int32_t src_obj;
+        load_ray(P, e, p, q, src_obj);
         const float4 a4 = __ldg(P.tgt.soup + 3 * t), b4 = __ldg(P.tgt.soup + 3 * t + 1),
                      c4 = __ldg(P.tgt.soup + 3 * t + 2);
-        if (!seg_tri_exact(make_float3(s4.x, s4.y, s4.z), make_float3(e4.x, e4.y, e4.z),
-                           make_float3(a4.x, a4.y, a4.z), make_float3(b4.x, b4.y, b4.z),
+        if (!seg_tri_exact(p, q, make_float3(a4.x, a4.y, a4.z), make_float3(b4.x, b4.y, b4.z),
                            make_float3(c4.x, c4.y, c4.z), pc))
             continue;
-        const int32_t src_obj = __float_as_int(s4.w), obj = __float_as_int(a4.w);
+        const int32_t obj = __float_as_int(a4.w);
         const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
         if (P.table) {
             ++inserts;
@@ -874,7 +909,8 @@ static uint64_t next_pow2(uint64_t v) {
 int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int mode, int precision,
                      int swap, int32_t* counts, const int64_t* offsets, uint64_t* keys, uint64_t* table,
                      uint64_t slots, const RayOpts* ro) {
-    if (src.num_edges == 0) return PIERCE_OK;
+    const int64_t n_rays = (ro && ro->list && ro->bound >= 0) ? ro->bound : src.num_edges;
+    if (n_rays == 0) return PIERCE_OK;
     EdgeRayParams P;
     P.src = src;
     P.tgt = tgt;
@@ -896,6 +932,8 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.short_stack = (ro && ro->short_stack >= 0) ? std::min(ro->short_stack, kShortStack)
                                                   : (P.ray_list ? kCulledShortStack : kShortStack);
     P.packets = (ro && ro->packets && ro->list) ? 1 : 0;
+    P.ray_soup = (ro && ro->list) ? ro->soup : nullptr;
+    P.ray_bound = n_rays;
     if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");
     if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
@@ -905,7 +943,7 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     dim3 g;
     if (P.ray_list) {
         cudaMemsetAsync(P.ray_cursor, 0, sizeof(unsigned long long), ctx->stream);
-        const int64_t want = (src.num_edges + B - 1) / B;
+        const int64_t want = (n_rays + B - 1) / B;
         g = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * 12)));
     } else {
         const int64_t blocks = (src.num_edges + B - 1) / B;
@@ -949,6 +987,7 @@ int launch_resolve(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt
     P.amb_queue = ro->amb_queue;
     P.amb_count = ro->amb_count;
     P.amb_cap = ro->amb_cap;
+    P.ray_soup = ro->list ? ro->soup : nullptr;
     k_resolve_ambiguous<<<ctx->sm_count * 4, 128, 0, ctx->stream>>>(P, keys_out, keys_count, keys_cap);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "resolve ambiguous tests");
@@ -1047,6 +1086,128 @@ int launch_group_filter(pierce_ctx* ctx, const float* gbox, int64_t ng, const De
                                                                                   flags);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "group filter");
+}
+
+// ---- rays from the kept triangles ---------------------------------------------
+// A join that builds per-join hierarchies over the triangles that can take
+// part in an overlap pair traces the edges of those triangles instead of the
+// dataset's edge list: an edge of one side that meets the other side at x is
+// an edge of a triangle of its own side that contains x, and the culling
+// rounds keep every triangle that contains a point of the other side.  The
+// soup holds the kept triangles G at a time (one group per leaf).  A group's
+// rays are the edges of its triangles, each segment once per group (an edge
+// two triangles of the group share, in either orientation, is listed once;
+// an edge shared across groups is traced once per group, which only repeats
+// work: pairs are de-duplicated).  With a filter hierarchy only the groups
+// whose box meets one of its leaf items are listed.  List entry (t << 2) | k:
+// edge k of soup triangle t.
+
+__device__ __forceinline__ bool same_point(const float4& a, const float4& b) {
+    return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+
+// Edge k (0: v0 v1, 1: v1 v2, 2: v2 v0) of soup triangle t repeats an edge
+// listed before it in its group: an edge of triangles first .. t - 1, or
+// edges 0 .. k - 1 of t.
+__device__ bool edge_listed_before(const float4* __restrict__ soup, int64_t first, int64_t t, int k, const float4& p,
+                                   const float4& q) {
+    for (int64_t u = first; u <= t; ++u) {
+        const float4 w[3] = {__ldg(soup + 3 * u), __ldg(soup + 3 * u + 1), __ldg(soup + 3 * u + 2)};
+        const int kmax = u < t ? 3 : k;
+        for (int j = 0; j < kmax; ++j) {
+            const float4& a = w[j];
+            const float4& b = w[j == 2 ? 0 : j + 1];
+            if ((same_point(a, p) && same_point(b, q)) || (same_point(a, q) && same_point(b, p))) return true;
+        }
+    }
+    return false;
+}
+
+// Does the box [lo, hi] of a group of object `obj` meet a leaf item of the
+// four-wide hierarchy `other` (within the object's partition)?
+__device__ bool group_meets(const DevDataset& other, const int32_t* __restrict__ obj_part, int32_t obj,
+                            const float3& lo, const float3& hi) {
+    if (!(lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z)) return true;  // NaN coordinates: keep
+    auto leaf_hit = [&](int first, int count) { return leaf_meets_box(other, first, count, lo, hi); };
+    if (obj_part && other.part_roots) {
+        const int2 r = __ldg(other.part_roots + __ldg(obj_part + obj));
+        if (r.x >= 0) return other.nodes4 ? any_hit4(other.nodes4, r.x, lo, hi, leaf_hit) : true;
+        return r.y > 0 && leaf_hit(~r.x, r.y);
+    }
+    if (other.num_tris == 0) return false;
+    if (other.root_is_leaf) return leaf_hit(0, other.root_leaf_count);
+    return other.nodes4 ? any_hit4(other.nodes4, 0, lo, hi, leaf_hit) : true;
+}
+
+// One thread per group; whole blocks step through the groups together so
+// that a warp reserves its list range with one atomicAdd.
+__global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ soup, int64_t n_tris, int G,
+                                                   DevDataset filter, int use_filter,
+                                                   const int32_t* __restrict__ obj_part, uint32_t* __restrict__ list,
+                                                   unsigned long long* __restrict__ count) {
+    const int64_t n_groups = (n_tris + G - 1) / G;
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n_groups; base += stride) {
+        const int64_t g = base + threadIdx.x;
+        const int64_t first = g * G;
+        const int64_t last = min(first + (int64_t)G, n_tris);
+        bool keep = g < n_groups;
+        if (keep && use_filter) {
+            float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+            for (int64_t t = first; t < last; ++t)
+                for (int v = 0; v < 3; ++v) {
+                    const float4 a = __ldg(soup + 3 * t + v);
+                    lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+                    hi.x = fmaxf(hi.x, a.x); hi.y = fmaxf(hi.y, a.y); hi.z = fmaxf(hi.z, a.z);
+                }
+            const int32_t obj0 = __float_as_int(__ldg(&soup[3 * first].w));
+            bool one_part = true;  // a group spanning partitions is kept
+            if (obj_part && filter.part_roots) {
+                const int32_t p0 = __ldg(obj_part + obj0);
+                for (int64_t t = first + 1; t < last; ++t)
+                    one_part = one_part && __ldg(obj_part + __float_as_int(__ldg(&soup[3 * t].w))) == p0;
+            }
+            keep = !one_part || group_meets(filter, obj_part, obj0, lo, hi);
+        }
+        int n = 0;
+        if (keep)
+            for (int64_t t = first; t < last; ++t)
+                for (int k = 0; k < 3; ++k) {
+                    const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
+                    if (!edge_listed_before(soup, first, t, k, p, q)) ++n;
+                }
+        int incl = n;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= off) incl += y;
+        }
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        unsigned long long wbase = 0;
+        if (lane == 31 && total) wbase = atomicAdd(count, (unsigned long long)total);
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+        unsigned long long pos = wbase + (unsigned long long)(incl - n);
+        if (n)
+            for (int64_t t = first; t < last; ++t)
+                for (int k = 0; k < 3; ++k) {
+                    const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
+                    if (!edge_listed_before(soup, first, t, k, p, q)) list[pos++] = (uint32_t)((t << 2) | k);
+                }
+    }
+}
+
+int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
+                     const int32_t* obj_part, uint32_t* list, unsigned long long* count) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    if (n_tris <= 0) return check_cuda(cudaGetLastError(), "rays from triangles");
+    if (n_tris >= (int64_t(1) << 30))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays from triangles: at most 2^30 - 1 triangles");
+    const int64_t n_groups = (n_tris + G - 1) / G;
+    const int64_t blocks = std::min<int64_t>((n_groups + 255) / 256, (int64_t)ctx->sm_count * 16);
+    k_soup_rays<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(
+        soup, n_tris, G, filter ? *filter : DevDataset{}, filter ? 1 : 0, obj_part, list, count);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "rays from triangles");
 }
 
 // Does [lo, hi] meet an item of `objs` within partition `part`?  Items are

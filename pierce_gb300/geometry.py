@@ -206,12 +206,20 @@ def ellipsoid_pair(seed_a: int, seed_b: int, num_a: int, num_b: int, level: int 
 
 def tubes(seed: int, num_meshes: int, target_tris: int = 200_000, step: float = 1.0,
           branch_prob: float = 0.02, r_lo: float = 0.5, r_hi: float = 3.0, n_sides: int = 12,
-          lo: float = 0.0, hi: float = 1000.0) -> Geometry:
+          lo: float = 0.0, hi: float = 1000.0, first: int | None = None) -> Geometry:
+    """Branching tube meshes; with `first`, only tubes 0 .. first-1 of the
+    same dataset (identical coordinates and object ids)."""
     h = C.c_void_p()
-    _check(native.host().pierce_gen_tubes(C.c_uint64(seed), num_meshes, C.c_int64(target_tris),
-                                          C.c_double(step), C.c_double(branch_prob), C.c_double(r_lo),
-                                          C.c_double(r_hi), n_sides, C.c_double(lo), C.c_double(hi),
-                                          C.byref(h)), "gen_tubes")
+    if first is None:
+        _check(native.host().pierce_gen_tubes(C.c_uint64(seed), num_meshes, C.c_int64(target_tris),
+                                              C.c_double(step), C.c_double(branch_prob), C.c_double(r_lo),
+                                              C.c_double(r_hi), n_sides, C.c_double(lo), C.c_double(hi),
+                                              C.byref(h)), "gen_tubes")
+    else:
+        _check(native.host().pierce_gen_tubes_head(C.c_uint64(seed), num_meshes, first, C.c_int64(target_tris),
+                                                   C.c_double(step), C.c_double(branch_prob), C.c_double(r_lo),
+                                                   C.c_double(r_hi), n_sides, C.c_double(lo), C.c_double(hi),
+                                                   C.byref(h)), "gen_tubes_head")
     return Geometry(h)
 
 

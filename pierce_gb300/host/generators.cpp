@@ -389,9 +389,12 @@ extern "C" int pierce_gen_ellipsoid_pair(uint64_t seed_a, uint64_t seed_b, int32
     return PIERCE_HOST_OK;
 }
 
-extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris, double step,
-                                double branch_prob, double r_lo, double r_hi, int32_t n_sides, double lo, double hi,
-                                pierce_geom** out) {
+namespace {
+
+// Tubes 0 .. num_meshes - 1 from one random stream; only the branches of
+// meshes below `sweep_meshes` are swept into the output.
+int gen_tubes(uint64_t seed, int32_t num_meshes, int32_t sweep_meshes, int64_t target_tris, double step,
+              double branch_prob, double r_lo, double r_hi, int32_t n_sides, double lo, double hi, pierce_geom** out) {
     if (!out || num_meshes < 0 || target_tris <= 0 || n_sides < 3 || step <= 0) {
         pierce::set_last_error("gen_tubes: invalid argument");
         return PIERCE_HOST_ERR_INVALID;
@@ -424,7 +427,7 @@ extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t targe
                 // branch is queued, so the budget spreads over several arms.
                 if (!pending.empty() && rng.uniform() < 1.0 / 400.0) break;
             }
-            if (br.pts.size() >= 2) branches.push_back(std::move(br));
+            if (br.pts.size() >= 2 && m < sweep_meshes) branches.push_back(std::move(br));
         }
     }
     // 2. offsets, then every branch swept in parallel into its own ranges
@@ -454,6 +457,24 @@ extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t targe
     g->total_triangles = g->num_triangles();
     *out = g.release();
     return PIERCE_HOST_OK;
+}
+
+}  // namespace
+
+extern "C" int pierce_gen_tubes(uint64_t seed, int32_t num_meshes, int64_t target_tris, double step,
+                                double branch_prob, double r_lo, double r_hi, int32_t n_sides, double lo, double hi,
+                                pierce_geom** out) {
+    return gen_tubes(seed, num_meshes, num_meshes, target_tris, step, branch_prob, r_lo, r_hi, n_sides, lo, hi, out);
+}
+
+extern "C" int pierce_gen_tubes_head(uint64_t seed, int32_t num_meshes, int32_t first_meshes, int64_t target_tris,
+                                     double step, double branch_prob, double r_lo, double r_hi, int32_t n_sides,
+                                     double lo, double hi, pierce_geom** out) {
+    if (first_meshes < 0 || first_meshes > num_meshes) {
+        pierce::set_last_error("gen_tubes_head: first_meshes out of range");
+        return PIERCE_HOST_ERR_INVALID;
+    }
+    return gen_tubes(seed, num_meshes, first_meshes, target_tris, step, branch_prob, r_lo, r_hi, n_sides, lo, hi, out);
 }
 
 // ---- instanced icosphere datasets -------------------------------------------

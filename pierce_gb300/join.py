@@ -225,7 +225,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
               max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
               sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0,
-              traversal="per_ray") -> capi.JoinOpts:
+              traversal="per_ray", edge_source="auto") -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -245,6 +245,8 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.leaf_size, o.rays_per_warp, o.stack_depth = int(leaf_size), int(rays_per_warp), int(stack_depth)
     o.traversal = ({"per_ray": 0, "packets": 1, "per_ray_binary": 2}[traversal] if isinstance(traversal, str)
                    else int(traversal))
+    o.edge_source = ({"auto": 0, "dataset": 1, "triangles": 2}[edge_source] if isinstance(edge_source, str)
+                     else int(edge_source))
     return o
 
 

@@ -66,6 +66,7 @@ def host() -> C.CDLL:
             _sig(lib, "pierce_gen_ellipsoid_pair", C.c_int,
                  [U64, U64, I32, I32, I32, D, D, D, D, D, D, D, D, C.POINTER(V), C.POINTER(V)])
             _sig(lib, "pierce_gen_tubes", C.c_int, [U64, I32, I64, D, D, D, D, I32, D, D, C.POINTER(V)])
+            _sig(lib, "pierce_gen_tubes_head", C.c_int, [U64, I32, I32, I64, D, D, D, D, I32, D, D, C.POINTER(V)])
             _host = lib
         return _host
 

@@ -14,8 +14,17 @@ where the reference sources are present).
   containment pair sets of the full benchmark workload, 2 x 50,000 level-3
   ellipsoids (the datasets of ``bench.workload(1.0)``), a few minutes of
   host time.
+* ``pairs_tubes_head50.npz`` (``--tubes``) — the oracle's overlap pairs of
+  the first 50 tubes of the tube workload (``bench.tube_geometry``) against
+  every one of the 100,000 ellipsoids (``bench.ellipsoid_instances``) whose
+  box shares a grid cell with one of those tubes' triangle boxes, with
+  global ellipsoid ids: the full tube join restricted to tubes 0..49 must
+  equal it.
+* ``pairs_batched_64.npz`` (``--batched``) — the oracle's overlap pairs of 64
+  queries drawn (seed 64) from the 4,096-query batched workload
+  (``pierce_gb300.batched.workload(seed=3)``), at their full mesh sizes.
 
-Usage:  python tests/golden/make_golden.py [--full]
+Usage:  python tests/golden/make_golden.py [--full | --tubes | --batched]
 """
 from __future__ import annotations
 
@@ -74,9 +83,56 @@ def full_workload() -> None:
     print("ellipsoids_50000", len(inter), len(cont), f"{time.perf_counter() - t0:.1f} s")
 
 
+TUBE_HEAD = 50
+BATCHED_SEED, BATCHED_QUERIES = 64, 64
+
+
+def tubes_head() -> None:
+    """Overlap pairs of tubes 0..TUBE_HEAD-1 against every ellipsoid."""
+    import time
+    import bench
+    t0 = time.perf_counter()
+    As, Bs, near = bench.tube_sample(TUBE_HEAD)
+    t1 = time.perf_counter()
+    keys, _ = O.overlap_keys(As, Bs)
+    glob = bench.sample_keys_global(keys, near)
+    np.savez_compressed(HERE / "pairs_tubes_head50.npz", overlap=glob, first=TUBE_HEAD,
+                        near=near.astype(np.int32), seeds=np.array([bench.TUBE_SEED, bench.ELLIPSOID_SEED]))
+    print(f"tubes head {TUBE_HEAD}: {As.num_triangles} + {Bs.num_triangles} triangles ({len(near)} ellipsoids), "
+          f"{len(glob)} pairs, set-up {t1 - t0:.1f} s, oracle {time.perf_counter() - t1:.1f} s")
+
+
+def batched_queries() -> list[int]:
+    return sorted(np.random.default_rng(BATCHED_SEED).choice(4096, BATCHED_QUERIES, replace=False).tolist())
+
+
+def batched_subset() -> None:
+    """Overlap pairs of 64 queries of the batched workload, one join each."""
+    import time
+    from pierce_gb300 import batched as BT
+    qs = BT.workload(seed=3, queries=4096)
+    out = {}
+    t0 = time.perf_counter()
+    for i in batched_queries():
+        q = qs[i]
+        A = pg.expand_instances(BT.side_instances(q, 0))
+        B = pg.expand_instances(BT.side_instances(q, 1))
+        keys, _ = O.overlap_keys(A, B)
+        out[f"q{i}"] = keys
+        print(f"query {i}: {A.num_triangles} + {B.num_triangles} triangles, {len(keys)} pairs, "
+              f"{time.perf_counter() - t0:.0f} s", flush=True)
+    np.savez_compressed(HERE / "pairs_batched_64.npz", queries=np.array(batched_queries()), **out)
+
+
 def main() -> None:
     if "--full" in sys.argv[1:]:
         full_workload()
+        return
+    if "--tubes" in sys.argv[1:]:
+        tubes_head()
+        return
+    if "--batched" in sys.argv[1:]:
+        batched_subset()
         return
     if not REF_TOOL.exists():
         raise SystemExit("oracle/_ref/ref_pre_tool missing: run oracle/build_ref.sh first")

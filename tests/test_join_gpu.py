@@ -35,16 +35,19 @@ def case(request):
     return request.param, A, B
 
 
+@pytest.mark.parametrize("edge_source", ["dataset", "triangles"])
 @pytest.mark.parametrize("sizing", ["hash", "two_pass"])
 @pytest.mark.parametrize("leaf", [1, 4])
-def test_overlap_exact_matches_oracle(ctx, case, sizing, leaf):
+def test_overlap_exact_matches_oracle(ctx, case, sizing, leaf, edge_source):
     name, A, B = case
     want, _ = O.overlap_keys(A, B)
-    got = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing)
+    got = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing, edge_source=edge_source)
     assert np.array_equal(keys(got), want), name
     passes = 2 if sizing == "two_pass" else 1
-    # object culling traces only the edges of objects near the other side
-    assert 0 < got.stats["rays"] <= passes * (A.num_edges + B.num_edges)
+    # culling traces only edges near the other side: dataset edges at most
+    # once, the kept triangles' edges at most once per triangle
+    bound = (A.num_edges + B.num_edges) if edge_source == "dataset" else 3 * (A.num_triangles + B.num_triangles)
+    assert 0 < got.stats["rays"] <= passes * bound
     plain = J.overlap_join(ctx, ds(ctx, A, leaf), ds(ctx, B, leaf), sizing=sizing, cull_objects=False,
                            active_bvh=False)
     assert plain.stats["rays"] == passes * (A.num_edges + B.num_edges)
@@ -65,19 +68,21 @@ def test_overlap_direction(ctx, case, direction):
     assert np.array_equal(keys(got), want), name
 
 
+@pytest.mark.parametrize("edge_source", ["dataset", "triangles"])
 @pytest.mark.parametrize("sizing", ["hash", "two_pass"])
-def test_intersection_matches_oracle(ctx, case, sizing):
+def test_intersection_matches_oracle(ctx, case, sizing, edge_source):
     name, A, B = case
     want = O.intersection_keys(A, B)
-    got = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
+    got = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing, edge_source=edge_source)
     assert np.array_equal(keys(got), want), name
 
 
+@pytest.mark.parametrize("edge_source", ["dataset", "triangles"])
 @pytest.mark.parametrize("sizing", ["hash", "two_pass"])
-def test_containment_matches_oracle(ctx, case, sizing):
+def test_containment_matches_oracle(ctx, case, sizing, edge_source):
     name, A, B = case
     want = O.containment_keys(A, B)
-    got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
+    got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing, edge_source=edge_source)
     assert np.array_equal(keys(got), want), name
     assert got.containment_count == len(want)
 

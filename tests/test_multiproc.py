@@ -5,6 +5,7 @@ import socket
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -51,14 +52,18 @@ def test_max_over_ranks_single_process():
     assert bench.max_over_ranks(3.5, None) == 3.5
 
 
-def test_reference_arm_json_line():
+@pytest.mark.parametrize("workload", ["tubes", "ellipsoids"])
+def test_reference_arm_json_line(workload):
     """bench.py --impl reference (the oracle port on the host cores, no GPU)
-    prints one JSON line of the bench contract on a small workload."""
+    prints one JSON line of the bench contract on a small workload, with the
+    config our arm prints for the same workload."""
     import json
     import subprocess
+    import bench
     root = ROOT
-    p = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--scale", "0.02",
-                        "--steps", "1", "--warmup", "0", "--cpu-sample-objects", "200"],
+    p = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--workload", workload,
+                        "--scale", "0.02", "--steps", "1", "--warmup", "0", "--cpu-sample-objects", "200",
+                        "--cpu-sample-tubes", "2"],
                        capture_output=True, text=True, cwd=root, timeout=600)
     assert p.returncode == 0, p.stderr
     lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
@@ -69,7 +74,25 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    assert d["config"]["meshes_per_side"] == 1000
+    if workload == "tubes":
+        assert d["config"] == bench.tubes_config(0.02)
+        assert d["sample_fraction"] == pytest.approx(2 / 40)
+    else:
+        assert d["config"] == bench.workload(0.02)[2]
+        assert d["config"]["meshes_per_side"] == 1000
+
+
+def test_boxes_near_is_a_superset_of_box_overlap():
+    """The sample selection keeps every object whose box meets a triangle box."""
+    import bench
+    rng = np.random.default_rng(3)
+    tri_lo = rng.uniform(0, 100, (400, 3)).astype(np.float32)
+    tri_hi = tri_lo + rng.uniform(0, 5, (400, 3)).astype(np.float32)
+    obj_lo = rng.uniform(0, 100, (3000, 3)).astype(np.float32)
+    obj_hi = obj_lo + rng.uniform(0, 12, (3000, 3)).astype(np.float32)
+    meets = np.any(np.all((obj_lo[:, None, :] <= tri_hi[None]) & (tri_lo[None] <= obj_hi[:, None, :]), axis=2), axis=1)
+    near = bench.boxes_near(tri_lo, tri_hi, obj_lo, obj_hi, cell=8.0)
+    assert np.all(near[meets]) and meets.sum() > 50 and near.sum() < len(near)
 
 
 def test_preprocess_workload_json_line():
@@ -99,4 +122,4 @@ def test_roofline_algorithmic_bytes():
     G = types.SimpleNamespace(vertices=np.zeros((600, 3), np.float32), num_triangles=1000)
     got = bench.traced_edge_ray_bytes(10, 2, [(G, 500), (G, 0)])
     assert got == 28 * 10 + 8 * 2 + 16 * 500 + 12 * 300 + 32 * 999
-    assert bench.traffic_estimate(100) == pytest.approx(bench.EDGE_RAY_DRAM_BYTES_PER_RAY * 100)
+    assert bench.traffic_estimate(100, "tubes") == pytest.approx(bench.EDGE_RAY_DRAM_BYTES_PER_RAY["tubes"] * 100)
