@@ -183,6 +183,17 @@ typedef struct pierce_join_opts {
                                      source when the dataset's edges are its triangles' edges (as
                                      pierce_preprocess extracts them): a segment's hits do not depend on
                                      its orientation */
+    /* Shard shard_index of shard_count (0 or 1: the whole join), for one
+     * process per GPU: the edge rays of each direction are split into
+     * shard_count contiguous ranges of the join's ray list and the parity
+     * rays into ranges of source objects; the union of the shards' pairs is
+     * the join's pair set (overlap, intersection).  Containment is split by
+     * B object (each shard's pairs are those of its B objects; needs
+     * active_bvh, both datasets' objects stored contiguously and no
+     * include_overlap_pairs).  Every shard builds the same per-join
+     * hierarchies. */
+    int32_t shard_index;
+    int32_t shard_count;
     int32_t reserved;
 } pierce_join_opts;
 

@@ -70,7 +70,7 @@ class JoinOpts(C.Structure):
                 ("output_safety", D), ("include_overlap_pairs", I32), ("max_retries", I32),
                 ("cull_objects", I32), ("defer_exact", I32), ("active_bvh", I32), ("sizing_model", V),
                 ("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("traversal", I32),
-                ("edge_source", I32), ("reserved", I32)]
+                ("edge_source", I32), ("shard_index", I32), ("shard_count", I32), ("reserved", I32)]
 
 
 class Stats(C.Structure):

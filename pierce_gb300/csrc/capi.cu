@@ -34,11 +34,14 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count);
+int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
+                                  uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
-                  uint32_t* parity, uint64_t slots);
+                  uint32_t* parity, uint64_t slots, int64_t src_lo = 0, int64_t src_hi = -1);
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
-                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots);
+                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots,
+                          int64_t src_lo = 0, int64_t src_hi = -1);
 int launch_parity_tracking(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, const ColumnGrid& grid,
                            int32_t k, int32_t* ids, uint32_t* hits, uint32_t* crossed, uint32_t* overflow);
 size_t column_grid_bytes(int32_t n);
@@ -100,6 +103,7 @@ enum : int {
     SLOT_NODES4_OBJ_A = 32,  // ... of the object hierarchies (culling)
     SLOT_NODES4_OBJ_B = 33,
     SLOT_NODES4_CHUNKS = 34,  // ... of the hierarchy of A's surviving chunk boxes
+    SLOT_CONT_PARITY = 35,    // containment: parity table of B's first vertices in A
 };
 }  // namespace
 
@@ -947,6 +951,55 @@ struct Join {
     DevDataset objA_{}, objB_{};
     bool object_parity = false;
     bool a_groups_met_b_ = false;  // A's kept groups were filtered against B's per-join hierarchy
+    // containment: the parity table of B's first vertices in A (odd entries
+    // are the candidate pairs), computed once per join
+    uint64_t min_table_slots = 0;  // pair table size floor after a table that proved too small
+    // shards: this join traces shard `shard_i` of `shard_n` (rays by list
+    // position, parity rays by source object)
+    int shard_i() const { return o.shard_count > 1 ? o.shard_index : 0; }
+    int shard_n() const { return o.shard_count > 1 ? o.shard_count : 1; }
+    int64_t shard_lo(int64_t n) const { return n * shard_i() / shard_n(); }
+    int64_t shard_hi(int64_t n) const { return n * (shard_i() + 1) / shard_n(); }
+    bool rays_by_candidates = false;  // containment split by B object: every shard traces all its candidates' rays
+    uint64_t* cont_ptable = nullptr;
+    uint32_t* cont_par = nullptr;
+    uint64_t cont_pslots = 0;
+
+    // Parity of B's first vertices against A into SLOT_CONT_PARITY (a full
+    // table is enlarged and the parity rerun).
+    int containment_parity() {
+        uint64_t pslots = table_slots_for(8 * (uint64_t)std::max(B->num_objects, 1), 0.5);
+        for (int attempt = 0;; ++attempt) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_CONT_PARITY, pslots * 12, &p)) return s;
+            uint64_t* ptable = static_cast<uint64_t*>(p);
+            uint32_t* par = reinterpret_cast<uint32_t*>(ptable + pslots);
+            cudaMemsetAsync(ptable, 0xFF, pslots * 8, ctx->stream);
+            cudaMemsetAsync(par, 0, pslots * 4, ctx->stream);
+            const int b = timer.record();
+            const int64_t lo = shard_lo(B->num_objects), hi = shard_hi(B->num_objects);
+            if (object_parity) {
+                if (int s = launch_parity_objects(ctx, vb, objA_, va, &gridA_, 1, ptable, par, pslots, lo, hi))
+                    return s;
+            } else if (int s = launch_parity(ctx, vb, va, 1, ptable, par, pslots, lo, hi)) {
+                return s;
+            }
+            timer.span(b, timer.record(), &st.ms_parity[1]);
+            uint32_t bits = 0;
+            if (int s = read_device_error(ctx, &bits)) return s;
+            if (bits & ERR_STACK_OVERFLOW) return set_error(PIERCE_ERR_STACK_OVERFLOW, "BVH traversal stack overflow");
+            if (bits & ERR_HASH_FULL) {
+                if (attempt >= std::max(o.max_retries, 4)) return set_error(PIERCE_ERR_HASH_FULL, "parity table full");
+                pslots *= 4;
+                st.retries++;
+                continue;
+            }
+            cont_ptable = ptable;
+            cont_par = par;
+            cont_pslots = pslots;
+            return PIERCE_OK;
+        }
+    }
     ColumnGrid gridA_{}, gridB_{};  // parity candidates of each side as a target
 
     // Column grids of both sides' object boxes (scratch slots meta/entries):
@@ -1048,6 +1101,15 @@ struct Join {
         uint8_t* act_b = active + std::max(A->num_objects, 1);
         if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
         if (int s = launch_object_active(ctx, vb, objA, act_b)) return s;
+        if (o.predicate == PIERCE_CONTAINMENT && !o.include_overlap_pairs && object_parity) {
+            // containment = parity(B in A) \ overlap: only the objects of odd
+            // parity pairs need their overlaps, so culling keeps just those
+            if (int s = containment_parity()) return s;
+            if (int s = launch_containment_candidates(ctx, cont_ptable, cont_par, cont_pslots, act_a, A->num_objects,
+                                                      act_b, B->num_objects))
+                return s;
+            rays_by_candidates = true;
+        }
         void *ta = nullptr, *tb = nullptr;
         if (int s = scratch(ctx, SLOT_TRIS_A, 4 * (A->nt + 64), &ta)) return s;
         if (int s = scratch(ctx, SLOT_TRIS_B, 4 * (B->nt + 64), &tb)) return s;
@@ -1360,7 +1422,15 @@ struct Join {
                 ro.cursor = words + 2;
                 ro.soup = ray_soup[d];
                 ro.bound = rays_of(d);
+                if (!rays_by_candidates) {
+                    ro.shard_index = shard_i();
+                    ro.shard_count = shard_n();
+                }
                 if (mode == 0) cudaMemsetAsync(counts, 0, 4 * (size_t)rays_of(d), ctx->stream);
+            }
+            if (!ro.list && !rays_by_candidates) {
+                ro.shard_index = shard_i();
+                ro.shard_count = shard_n();
             }
             ro.rays_per_fetch = o.rays_per_warp > 0 ? o.rays_per_warp : 32;
             ro.short_stack = o.stack_depth > 0 ? o.stack_depth : -1;
@@ -1393,6 +1463,7 @@ struct Join {
             const uint64_t expected = o.expected_pairs ? o.expected_pairs : (8u << 20);
             slots = table_slots_for(expected, o.hash_load_factor);
         }
+        while (slots < min_table_slots) slots <<= 1;
         for (int attempt = 0;; ++attempt) {
             void* p = nullptr;
             if (int s = scratch(ctx, SLOT_TABLE, slots * 8, &p)) return s;
@@ -1546,11 +1617,12 @@ struct Join {
             cudaMemsetAsync(ptable, 0xFF, pslots * 8, ctx->stream);
             cudaMemsetAsync(par, 0, pslots * 4, ctx->stream);
             int b = timer.record();
+            const int64_t lo = shard_lo(src.num_objects), hi = shard_hi(src.num_objects);
             if (object_parity) {
                 if (int s = launch_parity_objects(ctx, src, swap ? objA_ : objB_, tgt, swap ? &gridA_ : &gridB_, swap,
-                                                  ptable, par, pslots))
+                                                  ptable, par, pslots, lo, hi))
                     return s;
-            } else if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots)) {
+            } else if (int s = launch_parity(ctx, src, tgt, swap, ptable, par, pslots, lo, hi)) {
                 return s;
             }
             timer.span(b, timer.record(), ms);
@@ -1591,11 +1663,12 @@ struct Join {
             cudaMemsetAsync(ptable[d], 0xFF, pslots[d] * 8, ctx->stream);
             cudaMemsetAsync(par[d], 0, pslots[d] * 4, ctx->stream);
             const int b = timer.record();
+            const int64_t lo = shard_lo(src.num_objects), hi = shard_hi(src.num_objects);
             if (object_parity) {
                 if (int s = launch_parity_objects(ctx, src, d ? objA_ : objB_, tgt, d ? &gridA_ : &gridB_, d,
-                                                  ptable[d], par[d], pslots[d]))
+                                                  ptable[d], par[d], pslots[d], lo, hi))
                     return s;
-            } else if (int s = launch_parity(ctx, src, tgt, d, ptable[d], par[d], pslots[d])) {
+            } else if (int s = launch_parity(ctx, src, tgt, d, ptable[d], par[d], pslots[d], lo, hi)) {
                 return s;
             }
             timer.span(b, timer.record(), &st.ms_parity[d]);
@@ -1774,11 +1847,18 @@ struct Join {
         }
         uint64_t* table = nullptr;
         uint64_t slots = 0, n = 0;
-        if (int s = overlap_hash(&table, &slots)) return s;
-        if (int s = parity_both(table, slots)) return s;
-        uint32_t bits = 0;
-        if (int s = read_device_error(ctx, &bits)) return s;
-        if (bits & ERR_HASH_FULL) return set_error(PIERCE_ERR_HASH_FULL, "pair table full while adding parity pairs");
+        for (int attempt = 0;; ++attempt) {
+            if (int s = overlap_hash(&table, &slots)) return s;
+            if (int s = parity_both(table, slots)) return s;
+            uint32_t bits = 0;
+            if (int s = read_device_error(ctx, &bits)) return s;
+            if (!(bits & ERR_HASH_FULL)) break;
+            // the parity pairs did not fit: a larger table, overlap and parity again
+            if (attempt >= o.max_retries)
+                return set_error(PIERCE_ERR_HASH_FULL, "pair table full while adding parity pairs");
+            min_table_slots = 4 * slots;
+            st.retries++;
+        }
         uint64_t* keys = nullptr;
         int tb = timer.record();
         if (int s = compact(table, slots, 0, &n, &keys)) return s;
@@ -1803,22 +1883,32 @@ struct Join {
         }
         ab = save_ab;
         ba = save_ba;
-        // containment keys buffer (SLOT_TABLE is the hash table or raw keys; use SLOT_BUILD_D)
-        const uint64_t cap = 8 * (uint64_t)std::max(B->num_objects, 1) + 16;
-        void* p = nullptr;
-        if (int s = scratch(ctx, SLOT_BUILD_D, cap * 8, &p)) return s;
-        uint64_t* ckeys = static_cast<uint64_t*>(p);
-        void* pc = nullptr;
-        if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
-        unsigned long long* d_count = static_cast<unsigned long long*>(pc);
-        cudaMemsetAsync(d_count, 0, 8, ctx->stream);
-        if (int s = parity(vb, va, 1, &st.ms_parity[1], 1, nullptr, 0, table, slots, okeys, (int64_t)n_over, ckeys,
-                           d_count, cap))
-            return s;
-        int64_t n_cont_v = 0;
-        if (int s = host_value(ctx, d_count, 8, &n_cont_v, "containment count")) return s;
-        const uint64_t n_cont = (uint64_t)n_cont_v;
-        if (n_cont > cap) return set_error(PIERCE_ERR_OUTPUT_OVERFLOW, "containment output overflow");
+        if (!cont_ptable)
+            if (int s = containment_parity()) return s;
+        // odd parity pairs absent from the overlap set -> SLOT_BUILD_D (SLOT_TABLE
+        // holds the hash table or the raw keys); a buffer that turns out too
+        // small is enlarged to the count and the pairs emitted again
+        uint64_t cap = 8 * (uint64_t)std::max(B->num_objects, 1) + 16;
+        uint64_t* ckeys = nullptr;
+        uint64_t n_cont = 0;
+        for (;;) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_BUILD_D, cap * 8, &p)) return s;
+            ckeys = static_cast<uint64_t*>(p);
+            void* pc = nullptr;
+            if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+            unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+            cudaMemsetAsync(d_count, 0, 8, ctx->stream);
+            if (int s = parity_emit(ctx, cont_ptable, cont_par, cont_pslots, 1, table, slots, okeys, (int64_t)n_over,
+                                    nullptr, 0, ckeys, d_count, cap))
+                return s;
+            int64_t n_cont_v = 0;
+            if (int s = host_value(ctx, d_count, 8, &n_cont_v, "containment count")) return s;
+            n_cont = (uint64_t)n_cont_v;
+            if (n_cont <= cap) break;
+            cap = n_cont;
+            st.retries++;
+        }
         if (!two_pass && o.include_overlap_pairs) {
             // overlap keys of the table after the containment keys
             uint64_t* keys = nullptr;
@@ -1897,6 +1987,14 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
                          "edge_source asks for triangles)");
     if (o.edge_source == PIERCE_EDGES_DATASET && edgeless)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: edge_source DATASET but a dataset has no edges");
+    if (o.shard_count < 0 || o.shard_count > 65536 || o.shard_index < 0 ||
+        (o.shard_count > 1 && o.shard_index >= o.shard_count) || (o.shard_count <= 1 && o.shard_index != 0))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: shard_index must lie in [0, shard_count)");
+    if (o.shard_count > 1 && o.predicate == PIERCE_CONTAINMENT &&
+        (o.include_overlap_pairs || !o.active_bvh || !a->contiguous || !b->contiguous))
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT,
+                         "join: sharded containment splits by B object: it needs active_bvh, objects stored "
+                         "contiguously and no include_overlap_pairs");
     *out_opts = o;
     return PIERCE_OK;
 }

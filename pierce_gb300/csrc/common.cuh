@@ -114,6 +114,8 @@ struct RayOpts {
     // triangles (the source side's per-join hierarchy)
     const float4* soup = nullptr;
     int64_t bound = -1;       // listed rays at most (-1: the source's edge count)
+    int shard_index = 0;      // trace shard shard_index of shard_count of the rays
+    int shard_count = 1;
 };
 
 constexpr int kScratchSlots = 40;

@@ -135,6 +135,9 @@ struct EdgeRayParams {
     // packed dataset edge
     const float4* ray_soup;
     int64_t ray_bound;  // ray indices of a listed launch lie below this
+    // shard k of n: this launch traces rays [N k / n, N (k + 1) / n) of its
+    // N rays (list positions, or edge indices without a list)
+    int shard_index, shard_count;
 };
 
 // The segment of ray e and its source object: packed dataset edge e, or --
@@ -527,13 +530,15 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
         // Compacted ray list, persistent blocks: each warp takes the next
         // rays_per_fetch rays from a global cursor (the work queue), so uneven
         // ray costs balance out.
-        const unsigned long long n = *P.ray_count;
+        const unsigned long long n_all = *P.ray_count;
+        const unsigned long long lo = n_all * (unsigned long long)P.shard_index / (unsigned long long)P.shard_count;
+        const unsigned long long n = n_all * (unsigned long long)(P.shard_index + 1) / (unsigned long long)P.shard_count;
         const int lane = threadIdx.x & 31;
         const unsigned long long per = (unsigned long long)P.rays_per_fetch;
         int2* wstack = reinterpret_cast<int2*>(sstack + P.short_stack * 128) + (threadIdx.x >> 5) * kStackSize;
         for (;;) {
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(P.ray_cursor, per);
+            if (lane == 0) base = lo + atomicAdd(P.ray_cursor, per);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
             for (unsigned long long r = lane; r < per; r += 32) {  // per/32 rounds for every lane
@@ -552,7 +557,9 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
         }
     } else {
         const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-        if (e < P.src.num_edges) {
+        const int64_t lo = P.src.num_edges * P.shard_index / P.shard_count;
+        const int64_t hi = P.src.num_edges * (P.shard_index + 1) / P.shard_count;
+        if (e >= lo && e < hi) {
             trace_edge<MODE, PREC, false>(P, e, e, sstack, lstack, rc, pc, P.short_stack);
             ++rays;
         }
@@ -730,6 +737,7 @@ __global__ void __launch_bounds__(256) k_collect_rays(const int32_t* __restrict_
 
 struct ParityParams {
     DevDataset src, tgt;
+    int64_t src_lo, src_hi;  // source objects [src_lo, src_hi) cast rays (a shard)
     int swap;
     uint64_t* table;
     uint32_t* parity;
@@ -744,8 +752,8 @@ __global__ void __launch_bounds__(128) k_parity(ParityParams P) {
     const int tid = threadIdx.x;
     uint32_t n_nodes = 0, n_tests = 0, n_cross = 0;
     PredCounters pc{0, 0};
-    const int64_t o = blockIdx.x * (int64_t)blockDim.x + tid;
-    bool active = o < P.src.num_objects;
+    const int64_t o = P.src_lo + blockIdx.x * (int64_t)blockDim.x + tid;
+    bool active = o < P.src_hi;
     if (active) {
         const float4 fv = __ldg(P.src.first_vertex + o);
         active = fv.w == 0.0f;
@@ -850,6 +858,27 @@ __global__ void k_parity_emit(const uint64_t* __restrict__ ptable, const uint32_
     }
 }
 
+// Containment candidates: the objects of the odd (a, b) entries of a parity
+// table (key a << 32 | b).  Activity flags are 0 or 1; a candidate's flag
+// gains bit 1 (only ever OR-ed in, so concurrent stores of one byte agree),
+// then k_keep_candidates keeps the objects that are both active and
+// candidates.
+__global__ void k_mark_candidates(const uint64_t* __restrict__ ptable, const uint32_t* __restrict__ parity,
+                                  uint64_t pslots, uint8_t* act_a, uint8_t* act_b) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < pslots; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = ptable[i];
+        if (key == kEmptyKey || !(parity[i] & 1u)) continue;
+        const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+        act_a[a] = (uint8_t)(act_a[a] | 2u);
+        act_b[b] = (uint8_t)(act_b[b] | 2u);
+    }
+}
+
+__global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flags[i] = flags[i] == 3u ? 1u : 0u;
+}
+
 // Occupied slots -> dense key array (warp-aggregated cursor).  The counter
 // counts every occupied slot, so an undersized output is detected.
 __global__ void k_compact(const uint64_t* __restrict__ table, uint64_t slots, uint64_t* __restrict__ out,
@@ -934,6 +963,8 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.packets = (ro && ro->packets && ro->list) ? 1 : 0;
     P.ray_soup = (ro && ro->list) ? ro->soup : nullptr;
     P.ray_bound = n_rays;
+    P.shard_count = (ro && ro->shard_count > 1) ? ro->shard_count : 1;
+    P.shard_index = (ro && ro->shard_count > 1) ? ro->shard_index : 0;
     if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");
     if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
@@ -1455,11 +1486,16 @@ int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t
 }
 
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
-                  uint32_t* parity, uint64_t slots) {
-    if (src.num_objects <= 0) return PIERCE_OK;
+                  uint32_t* parity, uint64_t slots, int64_t src_lo, int64_t src_hi) {
+    if (src_hi < 0) src_hi = src.num_objects;
+    src_lo = std::max<int64_t>(src_lo, 0);
+    src_hi = std::min<int64_t>(src_hi, src.num_objects);
+    if (src_hi <= src_lo) return PIERCE_OK;
     ParityParams P;
     P.src = src;
     P.tgt = tgt;
+    P.src_lo = src_lo;
+    P.src_hi = src_hi;
     P.swap = swap;
     P.table = table;
     P.parity = parity;
@@ -1467,7 +1503,7 @@ int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt,
     P.err = ctx->d_err;
     P.ctr = ctx->d_counters;
     const int B = 128;
-    k_parity<<<(unsigned)((src.num_objects + B - 1) / B), B, 0, ctx->stream>>>(P);
+    k_parity<<<(unsigned)((src_hi - src_lo + B - 1) / B), B, 0, ctx->stream>>>(P);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "parity kernel");
 }
@@ -1554,6 +1590,7 @@ __global__ void k_grid_fill(const float* __restrict__ obj_box, int32_t n, const 
 // can drop triangles far from the other side.
 struct ParityObjParams {
     DevDataset src;   // first vertices, partitions
+    int64_t src_lo, src_hi;  // source objects [src_lo, src_hi) cast rays (a shard)
     ColumnGrid grid;  // the target's column grid (nx == 0: use the object hierarchy)
     DevDataset objs;  // the target's object hierarchy
     DevDataset tgt;   // the target's triangles (verts, idx, obj_range)
@@ -1581,7 +1618,7 @@ __global__ void __launch_bounds__(128) k_parity_objects(ParityObjParams P) {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     uint32_t n_nodes = 0, n_tests = 0, n_rays = 0;
     PredCounters pc{0, 0};
-    for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < P.src.num_objects;
+    for (int64_t s = P.src_lo + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < P.src_hi;
          s += warps) {
         const float4 fv = __ldg(P.src.first_vertex + s);
         if (fv.w != 0.0f) continue;  // object without triangles (warp-uniform)
@@ -1798,10 +1835,16 @@ int column_grid_fill(pierce_ctx* ctx, const DevDataset& tgt, void* mem, int32_t*
 }
 
 int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDataset& objs, const DevDataset& tgt,
-                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots) {
-    if (src.num_objects <= 0 || !tgt.obj_range) return PIERCE_OK;
+                          const ColumnGrid* grid, int swap, uint64_t* table, uint32_t* parity, uint64_t slots,
+                          int64_t src_lo, int64_t src_hi) {
+    if (src_hi < 0) src_hi = src.num_objects;
+    src_lo = std::max<int64_t>(src_lo, 0);
+    src_hi = std::min<int64_t>(src_hi, src.num_objects);
+    if (src_hi <= src_lo || !tgt.obj_range) return PIERCE_OK;
     ParityObjParams P;
     P.src = src;
+    P.src_lo = src_lo;
+    P.src_hi = src_hi;
     P.grid = grid ? *grid : ColumnGrid{};
     P.objs = objs;
     P.tgt = tgt;
@@ -1816,7 +1859,7 @@ int launch_parity_objects(pierce_ctx* ctx, const DevDataset& src, const DevDatas
     P.track_hits = nullptr;
     P.track_crossed = nullptr;
     P.track_overflow = nullptr;
-    const int64_t warps = src.num_objects;
+    const int64_t warps = src_hi - src_lo;
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 3) / 4,
                                                                              (int64_t)ctx->sm_count * 32));
     k_parity_objects<false><<<blocks, 128, 0, ctx->stream>>>(P);
@@ -1833,6 +1876,8 @@ int launch_parity_tracking(pierce_ctx* ctx, const DevDataset& src, const DevData
     if (src.num_objects <= 0 || !tgt.obj_range || grid.nx <= 0) return PIERCE_OK;
     ParityObjParams P;
     P.src = src;
+    P.src_lo = 0;
+    P.src_hi = src.num_objects;
     P.grid = grid;
     P.objs = DevDataset{};
     P.tgt = tgt;
@@ -1885,6 +1930,16 @@ int parity_emit(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity,
         out_table, out_slots ? out_slots - 1 : 0, out_keys, out_count, out_cap, ctx->d_err);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "parity emit");
+}
+
+int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
+                                  uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb) {
+    k_mark_candidates<<<grid_cap(ctx, (int64_t)pslots, 256), 256, 0, ctx->stream>>>(ptable, parity, pslots, act_a,
+                                                                                   act_b);
+    k_keep_candidates<<<grid_cap(ctx, na, 256), 256, 0, ctx->stream>>>(act_a, na);
+    k_keep_candidates<<<grid_cap(ctx, nb, 256), 256, 0, ctx->stream>>>(act_b, nb);
+    ctx->launches += 3;
+    return check_cuda(cudaGetLastError(), "containment candidates");
 }
 
 // Grid selectivity estimate per matched cell (estimateSelectivityKernel,

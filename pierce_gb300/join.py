@@ -38,6 +38,7 @@ class Context:
         h = C.c_void_p()
         check(self._lib.pierce_ctx_create(device, C.byref(h)), "ctx_create")
         self._h = h
+        self.device = int(device)
         self._children = weakref.WeakSet()
 
     def adopt(self, child) -> None:
@@ -225,7 +226,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
               hash_table_slots=0, hash_load_factor=0.5, output_safety=1.2, include_overlap_pairs=False,
               max_retries=4, cull_objects=True, defer_exact=True, active_bvh=True,
               sizing_model=None, leaf_size=0, rays_per_warp=0, stack_depth=0,
-              traversal="per_ray", edge_source="auto") -> capi.JoinOpts:
+              traversal="per_ray", edge_source="auto", shard_index=0, shard_count=1) -> capi.JoinOpts:
     o = capi.JoinOpts()
     capi.lib().pierce_default_join_opts(C.byref(o))
     o.predicate = PREDICATES[predicate] if isinstance(predicate, str) else int(predicate)
@@ -247,6 +248,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
                    else int(traversal))
     o.edge_source = ({"auto": 0, "dataset": 1, "triangles": 2}[edge_source] if isinstance(edge_source, str)
                      else int(edge_source))
+    o.shard_index, o.shard_count = int(shard_index), int(shard_count)
     return o
 
 

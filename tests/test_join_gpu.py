@@ -291,3 +291,23 @@ def test_parity_with_open_meshes_far_above(ctx):
         da, db = ds(ctx, A, 4), ds(ctx, geom, 4)
         got = keys(J.intersection_join(ctx, da, db))
         assert np.array_equal(np.sort(got), np.sort(O.intersection_keys(A, geom)))
+
+
+def test_nested_containers_enlarge_and_rerun(ctx):
+    """Thirty concentric spheres around small spheres: every B object lies
+    in about thirty A objects, far beyond the containment buffer's first
+    size (8 per B object) and a pair table sized for a handful of pairs.
+    Both are enlarged and the pairs stay exact."""
+    A = pg.icospheres(41, 30, 2, ln_mu=float(np.log(5.0)), sigma=0.5, lo=0.0, hi=0.0)
+    B = pg.icospheres(42, 40, 1, ln_mu=float(np.log(0.5)), sigma=0.2, lo=-0.5, hi=0.5)
+    cont = O.containment_keys(A, B)
+    inter = O.intersection_keys(A, B)
+    assert len(cont) >= 10 * B.num_objects
+    for sizing in ("hash", "two_pass"):
+        got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
+        assert np.array_equal(keys(got), cont), sizing
+    got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), include_overlap_pairs=True)
+    assert np.array_equal(keys(got)[: got.containment_count], cont)
+    got = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B), sizing="fixed", hash_table_slots=64, max_retries=8)
+    assert np.array_equal(keys(got), inter)
+    assert got.stats["retries"] > 0
