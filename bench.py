@@ -282,6 +282,17 @@ def boxes_near(tri_lo, tri_hi, obj_lo, obj_hi, cell: float = 8.0) -> np.ndarray:
     return near
 
 
+def mesh_boxes(G):
+    """Box (lo, hi) of every object of G whose vertices are stored object by
+    object (generated and instanced meshes)."""
+    vobj = np.empty(G.vertices.shape[0], np.int64)
+    vobj[G.indices.reshape(-1)] = np.repeat(G.tri_to_object.astype(np.int64), 3)
+    if np.any(vobj[1:] < vobj[:-1]):
+        raise AssertionError("vertices are not stored object by object")
+    starts = np.searchsorted(vobj, np.arange(G.num_objects))
+    return np.minimum.reduceat(G.vertices, starts), np.maximum.reduceat(G.vertices, starts)
+
+
 def instance_boxes(inst, batch: int = 8192):
     """Box (lo, hi) of every instanced mesh, from its host expansion in
     batches (the vertices of mesh m are contiguous)."""
@@ -291,14 +302,7 @@ def instance_boxes(inst, batch: int = 8192):
     for s0 in range(0, len(inst), batch):
         part = inst[s0:s0 + batch].copy()
         part["group"] = 0
-        G = pg.expand_instances(part)
-        vobj = np.empty(G.vertices.shape[0], np.int64)
-        vobj[G.indices.reshape(-1)] = np.repeat(G.tri_to_object.astype(np.int64), 3)
-        if np.any(vobj[1:] < vobj[:-1]):
-            raise AssertionError("instanced vertices are not stored mesh by mesh")
-        starts = np.searchsorted(vobj, np.arange(len(part)))
-        lo[s0:s0 + len(part)] = np.minimum.reduceat(G.vertices, starts)
-        hi[s0:s0 + len(part)] = np.maximum.reduceat(G.vertices, starts)
+        lo[s0:s0 + len(part)], hi[s0:s0 + len(part)] = mesh_boxes(pg.expand_instances(part))
     return lo, hi
 
 
@@ -564,11 +568,11 @@ def main_tubes(args):
         f"({time.perf_counter() - t0:.1f} s host generation)")
 
     # CPU oracle on a sample: the first k tubes against every ellipsoid near them
-    cpu, sample_keys = None, None
+    cpu, cpu_touch, sample_keys = None, None, None
     k = max(1, min(n_tubes, args.cpu_sample_tubes))
     if not args.no_cpu_baseline:
         tb = time.perf_counter()
-        As, Bs, near = tube_sample(k, args.scale, inst_b)
+        As, Bs, near = tube_sample(k, args.scale, inst_b, boxes=mesh_boxes(B))
         prep_s = time.perf_counter() - tb
         tc = time.perf_counter()
         cpu_keys, _ = O.overlap_keys(As, Bs)
@@ -577,8 +581,16 @@ def main_tubes(args):
         cpu = {"value": 1.0 / (cpu_s * n_tubes / k), "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                "sample": (f"tubes 0..{k - 1} of {n_tubes} against the {len(near)} ellipsoids near them: "
                           f"{cpu_s:.2f} s, scaled by {n_tubes}/{k}")}
+        # the reference's second CPU baseline, TOUCH, on the same sample
+        tt = time.perf_counter()
+        touch_keys, touch_cand = O.touch_keys(As, Bs)
+        touch_s = time.perf_counter() - tt
+        cpu_touch = {"value": 1.0 / (touch_s * n_tubes / k), "unit": UNIT, "cores": O.max_threads(),
+                     "kind": "port (TOUCH: STR tree fanout 2, exact refinement)",
+                     "sample": f"the same sample: {touch_s:.2f} s, {touch_cand} candidates, scaled by {n_tubes}/{k}",
+                     "pairs_equal_oracle": bool(np.array_equal(touch_keys, cpu_keys))}
         log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s ({prep_s:.1f} s set-up), "
-            f"{len(sample_keys)} pairs")
+            f"{len(sample_keys)} pairs; TOUCH {touch_s:.2f} s")
 
     ctx = J.Context(0)
     upload = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
@@ -706,7 +718,8 @@ def main_tubes(args):
                 "edges_uploaded": False,
                 "with_edge_upload": {"value": 1.0 / e2e_edges_s, "ms_per_step": 1000.0 * e2e_edges_s,
                                      "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)}},
-        "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks.summary(0),
+        "cpu_baseline": cpu, "cpu_baseline_touch": cpu_touch, "gpu_launches": int(launches),
+        "clocks": clocks.summary(0),
     }
     print(json.dumps(line))
     return 0

@@ -43,6 +43,7 @@
 // Zero-area triangles (all three coordinate-plane projections collinear) are
 // treated as empty by every test here, as by the CUDA path.
 #include <algorithm>
+#include <limits>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -575,6 +576,225 @@ void parity_crossings(const float* first_vertices, int32_t nsrc, const Mesh& tgt
     }
 }
 
+// ------------------------------------------------------------------ TOUCH --
+// Node of the STR tree over A's objects: its box, its children (internal)
+// or A objects (leaf), and the B objects assigned to it.
+struct TouchNode {
+    Box box;
+    bool leaf = false;
+    std::vector<int> kids;
+    std::vector<int32_t> objs;
+    std::vector<int32_t> assigned;
+};
+
+Box touch_empty_box() {
+    Box b;
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = std::numeric_limits<float>::max();
+        b.hi[k] = -std::numeric_limits<float>::max();
+    }
+    return b;
+}
+
+void touch_extend(Box& b, const Box& o) {
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = std::min(b.lo[k], o.lo[k]);
+        b.hi[k] = std::max(b.hi[k], o.hi[k]);
+    }
+}
+
+bool touch_overlaps(const Box& a, const Box& b) {
+    for (int k = 0; k < 3; ++k)
+        if (a.hi[k] < b.lo[k] || a.lo[k] > b.hi[k]) return false;
+    return true;
+}
+
+// One STR level: items sorted by box centre along x, cut into Sx slabs,
+// each slab sorted along y and cut into Sy runs, each run sorted along z
+// and cut into groups of `fanout` consecutive items; P = ceil(n / fanout),
+// Sx = ceil(P^(1/3)), Sy = ceil(sqrt(P / Sx)) (touch_query.cpp:125-163).
+std::vector<std::vector<int>> str_groups(std::vector<int> items, const std::vector<Box>& box, int fanout) {
+    const size_t n = items.size();
+    const double P = (double)((n + fanout - 1) / fanout);
+    const int Sx = (int)std::ceil(std::pow(P, 1.0 / 3.0));
+    const int Sy = (int)std::ceil(std::sqrt(P / Sx));
+    auto by = [&](int d) {
+        return [&box, d](int x, int y) { return box[x].lo[d] + box[x].hi[d] < box[y].lo[d] + box[y].hi[d]; };
+    };
+    std::sort(items.begin(), items.end(), by(0));
+    std::vector<std::vector<int>> groups;
+    size_t ix = 0;
+    int sx = Sx;
+    while (ix < n) {
+        const size_t end_x = std::min(n, ix + (n - ix + sx - 1) / sx);
+        std::sort(items.begin() + ix, items.begin() + end_x, by(1));
+        size_t iy = ix;
+        int sy = Sy;
+        while (iy < end_x) {
+            const size_t end_y = std::min(end_x, iy + (end_x - iy + sy - 1) / sy);
+            std::sort(items.begin() + iy, items.begin() + end_y, by(2));
+            for (size_t iz = iy; iz < end_y;) {
+                std::vector<int> g;
+                for (int i = 0; i < fanout && iz < end_y; ++i, ++iz) g.push_back(items[iz]);
+                groups.push_back(std::move(g));
+            }
+            --sy;
+            iy = end_y;
+        }
+        --sx;
+        ix = end_x;
+    }
+    return groups;
+}
+
+void touch_join(const Mesh& A, const Mesh& B, std::vector<uint64_t>& keys, uint64_t* candidates_out) {
+    // object boxes and per-object triangle lists
+    auto objects = [](const Mesh& m, std::vector<Box>& box, std::vector<std::vector<uint32_t>>& tris) {
+        int32_t n = 0;
+        for (uint64_t t = 0; t < m.nt; ++t) n = std::max(n, m.obj[t] + 1);
+        box.assign((size_t)n, touch_empty_box());
+        tris.assign((size_t)n, {});
+        for (uint64_t t = 0; t < m.nt; ++t) {
+            const int32_t o = m.obj[t];
+            if (o < 0) continue;
+            P3 a, b, c;
+            m.tri(t, a, b, c);
+            touch_extend(box[o], tri_box(a, b, c));
+            tris[o].push_back((uint32_t)t);
+        }
+    };
+    std::vector<Box> boxA, boxB;
+    std::vector<std::vector<uint32_t>> trisA, trisB;
+    objects(A, boxA, trisA);
+    objects(B, boxB, trisB);
+    // STR tree over A's objects with triangles, fanout 2
+    std::vector<TouchNode> nodes;
+    std::vector<Box> level_box;
+    std::vector<int> level;
+    {
+        std::vector<int> items;
+        for (size_t o = 0; o < boxA.size(); ++o)
+            if (!trisA[o].empty()) items.push_back((int)o);
+        if (items.empty()) {
+            if (candidates_out) *candidates_out = 0;
+            return;
+        }
+        for (auto& g : str_groups(items, boxA, 2)) {
+            TouchNode leaf;
+            leaf.leaf = true;
+            leaf.box = touch_empty_box();
+            for (int o : g) {
+                leaf.objs.push_back(o);
+                touch_extend(leaf.box, boxA[o]);
+            }
+            level.push_back((int)nodes.size());
+            nodes.push_back(std::move(leaf));
+        }
+    }
+    while (level.size() > 1) {
+        level_box.resize(nodes.size());
+        for (size_t i = 0; i < nodes.size(); ++i) level_box[i] = nodes[i].box;
+        std::vector<int> next;
+        for (auto& g : str_groups(level, level_box, 2)) {
+            TouchNode parent;
+            parent.box = touch_empty_box();
+            for (int c : g) {
+                parent.kids.push_back(c);
+                touch_extend(parent.box, nodes[c].box);
+            }
+            next.push_back((int)nodes.size());
+            nodes.push_back(std::move(parent));
+        }
+        level = std::move(next);
+    }
+    const int root = level.front();
+    // B objects: down the tree while exactly one child's box meets theirs;
+    // assigned where several do, or to the leaf reached (touch_query.cpp:221-253)
+    for (size_t o = 0; o < boxB.size(); ++o) {
+        if (trisB[o].empty() || !touch_overlaps(boxB[o], nodes[root].box)) continue;
+        int p = root;
+        bool assigned = false;
+        while (!nodes[p].leaf) {
+            int count = 0, only = -1;
+            for (int c : nodes[p].kids)
+                if (touch_overlaps(boxB[o], nodes[c].box)) {
+                    ++count;
+                    only = c;
+                }
+            if (count == 0) break;
+            if (count > 1) {
+                nodes[p].assigned.push_back((int32_t)o);
+                assigned = true;
+                break;
+            }
+            p = only;
+        }
+        if (!assigned && nodes[p].leaf) nodes[p].assigned.push_back((int32_t)o);
+    }
+    // candidates: per work node, its descendant leaves' A objects whose box
+    // meets an assigned B object's box (touch_query.cpp:268-302)
+    std::vector<std::pair<int32_t, int32_t>> cand;
+    std::vector<int> stack;
+    for (size_t w = 0; w < nodes.size(); ++w) {
+        if (nodes[w].assigned.empty()) continue;
+        stack.assign(1, (int)w);
+        while (!stack.empty()) {
+            const int n = stack.back();
+            stack.pop_back();
+            if (!nodes[n].leaf) {
+                for (int c : nodes[n].kids) stack.push_back(c);
+                continue;
+            }
+            for (int32_t b : nodes[w].assigned) {
+                if (!touch_overlaps(boxB[b], nodes[n].box)) continue;
+                for (int32_t a : nodes[n].objs)
+                    if (touch_overlaps(boxB[b], boxA[a])) cand.emplace_back(a, b);
+            }
+        }
+    }
+    if (candidates_out) *candidates_out = cand.size();
+    // per B object with candidates: a hierarchy over its triangles
+    std::vector<int> need(boxB.size(), 0);
+    for (auto& c : cand) need[c.second] = 1;
+    std::vector<std::vector<uint32_t>> idxB(boxB.size());
+    std::vector<std::vector<int32_t>> objB(boxB.size());
+    std::vector<Bvh> bvhB(boxB.size());
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t o = 0; o < (int64_t)boxB.size(); ++o) {
+        if (!need[o]) continue;
+        for (uint32_t t : trisB[o])
+            for (int k = 0; k < 3; ++k) idxB[o].push_back(B.idx[3 * (size_t)t + k]);
+        objB[o].assign(trisB[o].size(), (int32_t)o);
+        bvhB[o].build(Mesh{B.v, idxB[o].data(), objB[o].data(), trisB[o].size()});
+    }
+    // refinement: a candidate is a pair when a triangle of a meets b
+    std::vector<uint8_t> hit(cand.size(), 0);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t i = 0; i < (int64_t)cand.size(); ++i) {
+        const int32_t a = cand[i].first, b = cand[i].second;
+        const Mesh Bo{B.v, idxB[b].data(), objB[b].data(), trisB[b].size()};
+        bool found = false;
+        for (uint32_t t : trisA[a]) {
+            P3 p, q, r;
+            A.tri(t, p, q, r);
+            const Box tb = tri_box(p, q, r);
+            bvhB[b].query([&](const Box& bx) { return !found && boxes_overlap(tb, bx); },
+                          [&](uint64_t u) {
+                              if (found) return;
+                              P3 d, e, f;
+                              Bo.tri(u, d, e, f);
+                              found = seg_tri_exact(p, q, d, e, f) || seg_tri_exact(q, r, d, e, f) ||
+                                      seg_tri_exact(r, p, d, e, f) || seg_tri_exact(d, e, p, q, r) ||
+                                      seg_tri_exact(e, f, p, q, r) || seg_tri_exact(f, d, p, q, r);
+                          });
+            if (found) break;
+        }
+        hit[i] = found ? 1 : 0;
+    }
+    for (size_t i = 0; i < cand.size(); ++i)
+        if (hit[i]) keys.push_back(pack(cand[i].first, cand[i].second));
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ C interface --
@@ -709,6 +929,23 @@ uint64_t* oracle_face_pairs(const float* av, const uint32_t* ai, const int32_t* 
     }
     std::vector<uint64_t> keys;
     for (auto& v : per) keys.insert(keys.end(), v.begin(), v.end());
+    sort_unique(keys);
+    return to_malloc(keys, n_out);
+}
+
+// TOUCH baseline restated (baselines/face/src/touch_query.cpp): an STR tree
+// of fanout 2 over A's object boxes (:125-219), B's objects assigned to it
+// (:221-253), candidate pairs from the work nodes' descendant leaves
+// (:268-302), then each candidate refined with the exact closed
+// triangle-triangle predicate: any triangle of a against a hierarchy over
+// b's triangles (:462-480, CGAL's do_intersect there).  Objects without
+// triangles take no part.  OpenMP over the candidates.
+uint64_t* oracle_touch_pairs(const float* av, const uint32_t* ai, const int32_t* ao, uint64_t ant,
+                             const float* bv, const uint32_t* bi, const int32_t* bo, uint64_t bnt,
+                             uint64_t* n_out, uint64_t* candidates_out) {
+    Mesh A{av, ai, ao, ant}, B{bv, bi, bo, bnt};
+    std::vector<uint64_t> keys;
+    touch_join(A, B, keys, candidates_out);
     sort_unique(keys);
     return to_malloc(keys, n_out);
 }

@@ -48,6 +48,8 @@ def lib() -> C.CDLL:
         L.oracle_parity_crossings.argtypes = [V, C.c_int32, V, V, V, U64, C.POINTER(U64)]
         L.oracle_face_pairs.restype = C.POINTER(C.c_uint64)
         L.oracle_face_pairs.argtypes = [V, V, V, U64, V, V, V, U64, U64, U64, C.POINTER(U64)]
+        L.oracle_touch_pairs.restype = C.POINTER(C.c_uint64)
+        L.oracle_touch_pairs.argtypes = [V, V, V, U64, V, V, V, U64, C.POINTER(U64), C.POINTER(U64)]
         L.oracle_free.argtypes = [V]
         L.oracle_free.restype = None
         for name in ("oracle_orient3d", "oracle_orient3d_exact"):
@@ -134,6 +136,15 @@ def face_keys(A, B, tri_begin: int = 0, tri_end: int | None = None) -> np.ndarra
     n = U64()
     ptr = lib().oracle_face_pairs(*ga, *gb, tri_begin, tri_end, C.byref(n))
     return _take(ptr, n.value)
+
+
+def touch_keys(A, B) -> tuple[np.ndarray, int]:
+    """TOUCH baseline restated (baselines/face/src/touch_query.cpp): sorted
+    unique overlap keys and the number of candidate pairs it refined."""
+    (ga, ka), (gb, kb) = _geom_args(A), _geom_args(B)
+    n, cand = U64(), U64()
+    ptr = lib().oracle_touch_pairs(*ga, *gb, C.byref(n), C.byref(cand))
+    return _take(ptr, n.value), cand.value
 
 
 def intersection_keys(A, B) -> np.ndarray:

@@ -197,6 +197,28 @@ def test_face_restatement_equals_edge_definition():
     assert len(edge) > 50
 
 
+@pytest.mark.parametrize("case", ["ellipsoid_contacts", "tubes_vs_spheres", "one_object_each", "disjoint",
+                                  "nested"])
+def test_touch_restatement_equals_face_and_edge_definition(case):
+    """TOUCH's candidates are every pair of overlapping object boxes whatever
+    the tree's shape, so after exact refinement its pairs are Face's."""
+    A, B = {
+        "ellipsoid_contacts": lambda: pg.ellipsoid_pair(21, 22, 120, 120, 2, lo=0, hi=40, frac_contact=0.1),
+        "tubes_vs_spheres": lambda: (pg.tubes(4, 3, 4000, hi=30.0), pg.icospheres(5, 150, 2, hi=30.0)),
+        "one_object_each": lambda: (pg.icospheres(6, 1, 2, hi=0.0), pg.icospheres(7, 1, 2, lo=0.5, hi=0.5)),
+        "disjoint": lambda: (pg.icospheres(8, 40, 1, hi=10.0), pg.icospheres(9, 40, 1, lo=100.0, hi=110.0)),
+        "nested": lambda: (pg.icospheres(41, 30, 2, ln_mu=float(np.log(5.0)), sigma=0.5, lo=0.0, hi=0.0),
+                           pg.icospheres(42, 40, 1, ln_mu=float(np.log(0.5)), sigma=0.2, lo=-0.5, hi=0.5)),
+    }[case]()
+    touch, candidates = O.touch_keys(A, B)
+    face = O.face_keys(A, B)
+    edge, _ = O.overlap_keys(A, B)
+    assert np.array_equal(touch, face) and np.array_equal(touch, edge), case
+    assert candidates >= len(touch)
+    if case == "disjoint":
+        assert candidates == 0 and len(touch) == 0
+
+
 @pytest.mark.parametrize("name", ["icospheres", "ellipsoid_contacts"])
 def test_golden_pair_sets_reproduce(name):
     import importlib.util
