@@ -568,7 +568,7 @@ def main_tubes(args):
         f"({time.perf_counter() - t0:.1f} s host generation)")
 
     # CPU oracle on a sample: the first k tubes against every ellipsoid near them
-    cpu, cpu_touch, sample_keys = None, None, None
+    cpu, cpu_touch, sample_keys, ref_sem = None, None, None, None
     k = max(1, min(n_tubes, args.cpu_sample_tubes))
     if not args.no_cpu_baseline:
         tb = time.perf_counter()
@@ -589,8 +589,11 @@ def main_tubes(args):
                      "kind": "port (TOUCH: STR tree fanout 2, exact refinement)",
                      "sample": f"the same sample: {touch_s:.2f} s, {touch_cand} candidates, scaled by {n_tubes}/{k}",
                      "pairs_equal_oracle": bool(np.array_equal(touch_keys, cpu_keys))}
+        # |exact set Δ the reference's edge-ray semantics| on the same sample
+        ref_sem = O.reference_semantics_diff(As, Bs, 100)
+        ref_sem["sample"] = f"tubes 0..{k - 1} against the {len(near)} ellipsoids near them"
         log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s ({prep_s:.1f} s set-up), "
-            f"{len(sample_keys)} pairs; TOUCH {touch_s:.2f} s")
+            f"{len(sample_keys)} pairs; TOUCH {touch_s:.2f} s; reference semantics {ref_sem}")
 
     ctx = J.Context(0)
     upload = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
@@ -718,6 +721,7 @@ def main_tubes(args):
                 "edges_uploaded": False,
                 "with_edge_upload": {"value": 1.0 / e2e_edges_s, "ms_per_step": 1000.0 * e2e_edges_s,
                                      "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)}},
+        "reference_semantics_diff": ref_sem,
         "cpu_baseline": cpu, "cpu_baseline_touch": cpu_touch, "gpu_launches": int(launches),
         "clocks": clocks.summary(0),
     }
@@ -989,11 +993,13 @@ def main_ellipsoids(args):
                "d2h_bytes_per_step": int(d2h_total // e2e_steps), "ms_per_step": 1000.0 * e2e_s,
                "edges_uploaded": False}
 
-    cpu = None
+    cpu, ref_sem = None, None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import pyoracle as O
         As, Bs, frac = cpu_sample(A, B, args.cpu_sample_objects)
         secs = cpu_join_seconds(As, Bs)
+        ref_sem = O.reference_semantics_diff(As, Bs, 100)
+        ref_sem["sample"] = f"overlap pairs of the spatial sub-cube sample (fraction {frac:.4f})"
         full = secs / max(frac, 1e-12)
         cpu = {"value": 2.0 / full, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                "sample": (f"intersection+containment joins of the objects in a spatial sub-cube "
@@ -1030,7 +1036,8 @@ def main_ellipsoids(args):
                      "kernel": "k_edge_rays (exact, hash mode), both directions of the intersection join",
                      "peak_kind": peak_kind, "algorithmic_bytes": traced_bytes,
                      "unculled_equivalent_gbs": unculled_bytes / (edge_ms / 1000.0) / 1e9 if edge_ms > 0 else None},
-        "plain": plain, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "plain": plain, "cpu_baseline": cpu, "reference_semantics_diff": ref_sem, "e2e": e2e,
+        "gpu_launches": int(launches), "clocks": clk,
     }
     print(json.dumps(line))
     if dist:

@@ -140,8 +140,8 @@ inline float comp(const P3& p, int k) { return k == 0 ? p.x : (k == 1 ? p.y : p.
 
 std::atomic<uint64_t> g_exact_calls{0};
 
-// sign of det[b-a, c-a, d-a]
-int orient3d_exact(const P3& a, const P3& b, const P3& c, const P3& d) {
+// det[b-a, c-a, d-a], exact, scaled by 2^(3 * 173)
+void orient3d_value(const P3& a, const P3& b, const P3& c, const P3& d, Big& s) {
     Big A[3], B[3], C[3], D[3];
     for (int k = 0; k < 3; ++k) {
         big_from_float(comp(a, k), A[k]);
@@ -156,13 +156,19 @@ int orient3d_exact(const P3& a, const P3& b, const P3& c, const P3& d) {
         big_sub(D[k], A[k], w[k]);
     }
     // det = u . (v x w)
-    Big t1, t2, cx, cy, cz, s, r;
+    Big t1, t2, cx, cy, cz, r;
     big_mul(v[1], w[2], t1); big_mul(v[2], w[1], t2); big_sub(t1, t2, cx);
     big_mul(v[2], w[0], t1); big_mul(v[0], w[2], t2); big_sub(t1, t2, cy);
     big_mul(v[0], w[1], t1); big_mul(v[1], w[0], t2); big_sub(t1, t2, cz);
     big_mul(u[0], cx, s);
     big_mul(u[1], cy, t1); big_add(s, t1, r);
     big_mul(u[2], cz, t1); big_add(r, t1, s);
+}
+
+// sign of det[b-a, c-a, d-a]
+int orient3d_exact(const P3& a, const P3& b, const P3& c, const P3& d) {
+    Big s;
+    orient3d_value(a, b, c, d, s);
     return big_sign(s);
 }
 
@@ -490,6 +496,89 @@ void edge_join(const float* es, const float* ee, const int32_t* esrc, uint64_t n
     for (auto& v : per) out.insert(out.end(), v.begin(), v.end());
     if (tests)
         for (uint64_t c : cnt) *tests += c;
+}
+
+// The reference's edge-ray semantics (pierce/query/src/cuda/
+// mesh_overlap_edges.cu:105-176) on exact hits: the ray starts at the edge's
+// start point with tmin = nextafterf(0), so a hit there is not seen; a ray in
+// a triangle's plane is parallel to it and misses; each closest-hit
+// iteration reports one hit and moves tmin past its t, so hits at one t
+// count once (here the lowest target object wins the tie; the reference's
+// winner depends on its traversal order); at most max_iter iterations
+// report.  Hit parameters t = D(p) / (D(p) - D(q)), D(x) = det[b-a, c-a,
+// x-a], are exact rationals compared by cross-multiplication (exact for
+// coordinates below 2^20 in magnitude).  A zero-length edge reports nothing.
+struct RefHit {
+    Big num, den;  // t = num / den, den > 0
+    int32_t obj;
+};
+
+bool ref_t_less(const RefHit& x, const RefHit& y) {
+    Big l, r, d;
+    big_mul(x.num, y.den, l);
+    big_mul(y.num, x.den, r);
+    big_sub(l, r, d);
+    return big_neg(d);
+}
+
+bool ref_t_equal(const RefHit& x, const RefHit& y) {
+    Big l, r, d;
+    big_mul(x.num, y.den, l);
+    big_mul(y.num, x.den, r);
+    big_sub(l, r, d);
+    return big_is_zero(d);
+}
+
+void edge_join_reference(const float* es, const float* ee, const int32_t* esrc, uint64_t ne, const Mesh& tgt,
+                         const Bvh& bvh, int swap, int max_iter, std::vector<uint64_t>& out) {
+    int nth = 1;
+#ifdef _OPENMP
+    nth = omp_get_max_threads();
+#endif
+    std::vector<std::vector<uint64_t>> per(nth);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t e = 0; e < (int64_t)ne; ++e) {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        const P3 p{es[3 * e], es[3 * e + 1], es[3 * e + 2]};
+        const P3 q{ee[3 * e], ee[3 * e + 1], ee[3 * e + 2]};
+        if (p.x == q.x && p.y == q.y && p.z == q.z) continue;
+        const Box sb = seg_box(p, q);
+        const int32_t so = esrc[e];
+        std::vector<RefHit> hits;
+        bvh.query([&](const Box& b) { return boxes_overlap(sb, b); },
+                  [&](uint64_t t) {
+                      P3 a, b, c;
+                      tgt.tri(t, a, b, c);
+                      if (!seg_tri_exact(p, q, a, b, c)) return;
+                      RefHit h;
+                      Big dq;
+                      orient3d_value(a, b, c, p, h.num);
+                      orient3d_value(a, b, c, q, dq);
+                      if (big_is_zero(h.num)) return;  // in the plane (parallel ray) or at the start point
+                      big_sub(h.num, dq, h.den);
+                      if (big_neg(h.den)) {
+                          big_negate(h.num, h.num);
+                          big_negate(h.den, h.den);
+                      }
+                      h.obj = tgt.obj[t];
+                      hits.push_back(h);
+                  });
+        std::sort(hits.begin(), hits.end(), [](const RefHit& x, const RefHit& y) {
+            if (ref_t_less(x, y)) return true;
+            if (ref_t_less(y, x)) return false;
+            return x.obj < y.obj;
+        });
+        int iters = 0;
+        for (size_t i = 0; i < hits.size(); ++i) {
+            if (i > 0 && ref_t_equal(hits[i], hits[i - 1])) continue;
+            if (++iters > max_iter) break;
+            per[tid].push_back(swap ? pack(hits[i].obj, so) : pack(so, hits[i].obj));
+        }
+    }
+    for (auto& v : per) out.insert(out.end(), v.begin(), v.end());
 }
 
 // Parity pairs: first vertex of each source object against target triangles.
@@ -860,6 +949,30 @@ uint64_t* oracle_overlap_pairs(const float* av, const uint32_t* ai, const int32_
     }
     sort_unique(keys);
     if (tests_out) *tests_out = tests;
+    return to_malloc(keys, n_out);
+}
+
+// Overlap pairs under the reference's edge-ray semantics (see
+// edge_join_reference), sorted like oracle_overlap_pairs.
+uint64_t* oracle_overlap_pairs_reference(const float* av, const uint32_t* ai, const int32_t* ao, uint64_t ant,
+                                         const float* aes, const float* aee, const int32_t* aesrc, uint64_t ane,
+                                         const float* bv, const uint32_t* bi, const int32_t* bo, uint64_t bnt,
+                                         const float* bes, const float* bee, const int32_t* besrc, uint64_t bne,
+                                         int direction, int max_iter, uint64_t* n_out) {
+    Mesh A{av, ai, ao, ant}, B{bv, bi, bo, bnt};
+    std::vector<uint64_t> keys;
+    if (max_iter <= 0) max_iter = 100;  // the reference's default (mesh_overlap_edges.cu:111-112)
+    if (direction == 0 || direction == 1) {
+        Bvh bb;
+        bb.build(B);
+        edge_join_reference(aes, aee, aesrc, ane, B, bb, 0, max_iter, keys);
+    }
+    if (direction == 0 || direction == 2) {
+        Bvh ab;
+        ab.build(A);
+        edge_join_reference(bes, bee, besrc, bne, A, ab, 1, max_iter, keys);
+    }
+    sort_unique(keys);
     return to_malloc(keys, n_out);
 }
 

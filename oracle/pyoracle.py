@@ -48,6 +48,9 @@ def lib() -> C.CDLL:
         L.oracle_parity_crossings.argtypes = [V, C.c_int32, V, V, V, U64, C.POINTER(U64)]
         L.oracle_face_pairs.restype = C.POINTER(C.c_uint64)
         L.oracle_face_pairs.argtypes = [V, V, V, U64, V, V, V, U64, U64, U64, C.POINTER(U64)]
+        L.oracle_overlap_pairs_reference.restype = C.POINTER(C.c_uint64)
+        L.oracle_overlap_pairs_reference.argtypes = [V, V, V, U64, V, V, V, U64, V, V, V, U64, V, V, V, U64,
+                                                     C.c_int, C.c_int, C.POINTER(U64)]
         L.oracle_touch_pairs.restype = C.POINTER(C.c_uint64)
         L.oracle_touch_pairs.argtypes = [V, V, V, U64, V, V, V, U64, C.POINTER(U64), C.POINTER(U64)]
         L.oracle_free.argtypes = [V]
@@ -106,6 +109,26 @@ def overlap_keys(A, B, direction: int = 0, mode: int = 0):
     n, tests = U64(), U64()
     ptr = lib().oracle_overlap_pairs(*ga, *ea, *gb, *eb, direction, mode, C.byref(n), C.byref(tests))
     return _take(ptr, n.value), tests.value
+
+
+def overlap_keys_reference(A, B, max_iterations: int = 100, direction: int = 0) -> np.ndarray:
+    """Overlap keys under the reference's edge-ray semantics: hits at an
+    edge's start point and rays in a triangle's plane are not seen, hits at
+    one t count once, at most max_iterations hits per edge
+    (pierce/query/src/cuda/mesh_overlap_edges.cu:105-176)."""
+    (ga, ka), (gb, kb) = _geom_args(A), _geom_args(B)
+    (ea, kea), (eb, keb) = _edge_args(A), _edge_args(B)
+    n = U64()
+    ptr = lib().oracle_overlap_pairs_reference(*ga, *ea, *gb, *eb, direction, max_iterations, C.byref(n))
+    return _take(ptr, n.value)
+
+
+def reference_semantics_diff(A, B, max_iterations: int = 100) -> dict:
+    """|exact set Δ reference-semantics set| of the overlap join."""
+    exact, _ = overlap_keys(A, B)
+    ref = overlap_keys_reference(A, B, max_iterations)
+    return {"max_iterations": int(max_iterations), "exact_pairs": int(len(exact)), "reference_pairs": int(len(ref)),
+            "only_exact": int(len(np.setdiff1d(exact, ref))), "only_reference": int(len(np.setdiff1d(ref, exact)))}
 
 
 def parity_keys(first_vertices: np.ndarray, T, swap: int = 0) -> np.ndarray:
