@@ -604,9 +604,11 @@ def main_tubes(args):
     plain_build = J.default_tuning(leaf_size=args.plain_leaf_size)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
 
-    # device-resident legs: inputs already in HBM
-    da = J.Dataset.from_geometry(ctx, A, upload)
-    db = J.Dataset.from_geometry(ctx, B, upload)
+    # device-resident legs: inputs already in HBM (profiling runs skip the
+    # edge arrays, which only the plain form reads)
+    resident = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1 if args.only_tuned else 0)
+    da = J.Dataset.from_geometry(ctx, A, resident)
+    db = J.Dataset.from_geometry(ctx, B, resident)
     for _ in range(max(args.warmup, 3)):
         r = J.run_join(ctx, da, db, tuned_o, download=False)
     torch.cuda.synchronize()
@@ -615,12 +617,16 @@ def main_tubes(args):
     stats = []
     with clocks:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if args.only_tuned:
+            torch.cuda.nvtx.range_push("timed")  # profilers select the timed joins by this range
         e0.record(stream)
         for _ in range(args.steps):
             r = J.run_join(ctx, da, db, tuned_o, download=False)
             stats.append(r.stats)
         e1.record(stream)
         e1.synchronize()
+        if args.only_tuned:
+            torch.cuda.nvtx.range_pop()
     launches = ctx.kernel_launches - l0
     tuned_ms = e0.elapsed_time(e1) / args.steps
     st = stats[-1]

@@ -91,7 +91,6 @@ enum : int {
     SLOT_TRIS_A = 19,    // active triangle lists
     SLOT_TRIS_B = 20,
     // 21, 22: learned sizing
-    SLOT_CHUNKS = 23,    // chunk boxes of A, their list and hierarchy (second culling round)
     SLOT_CHUNK_LIST = 24,  // active chunk ids of one culling pass
     SLOT_GROUPS = 25,    // group boxes and group hierarchy soup of a grouped build
     SLOT_GRID_A = 26,    // column grids (parity candidates): A's, then B's
@@ -102,7 +101,6 @@ enum : int {
     SLOT_NODES4_B = 31,
     SLOT_NODES4_OBJ_A = 32,  // ... of the object hierarchies (culling)
     SLOT_NODES4_OBJ_B = 33,
-    SLOT_NODES4_CHUNKS = 34,  // ... of the hierarchy of A's surviving chunk boxes
     SLOT_CONT_PARITY = 35,    // containment: parity table of B's first vertices in A
 };
 }  // namespace
@@ -950,7 +948,6 @@ struct Join {
     // object pairs (both datasets store each object's triangles contiguously)
     DevDataset objA_{}, objB_{};
     bool object_parity = false;
-    bool a_groups_met_b_ = false;  // A's kept groups were filtered against B's per-join hierarchy
     // containment: the parity table of B's first vertices in A (odd entries
     // are the candidate pairs), computed once per join
     uint64_t min_table_slots = 0;  // pair table size floor after a table that proved too small
@@ -1128,61 +1125,70 @@ struct Join {
         uint8_t* echunk_a = tchunk_b + (B->nt + 31) / 32 + 1;
         uint8_t* echunk_b = echunk_a + (A->ne + 31) / 32 + 1;
         const bool chunked = o.cull_objects != 0;
-        // Second round (overlap, unpartitioned): B's chunks are tested against
-        // a hierarchy of A's surviving chunk boxes instead of A's object boxes,
-        // which matters when A's objects are large (long tubes).
-        DevDataset cull_b = objA;
         const bool tri_chunks = chunked && (o.predicate == PIERCE_OVERLAP || object_parity);
-        const bool two_rounds = tri_chunks && A->num_parts == 0 && A->nt > 0;
-        if (tri_chunks) {
-            float* boxes_a = nullptr;
-            uint32_t* clist = nullptr;
-            uint32_t* cidx = nullptr;
-            int32_t* ct2o = nullptr;
-            float4* csoup = nullptr;
-            Node* cnodes = nullptr;
-            const int64_t nca = (int64_t)((A->nt + 31) / 32);
-            if (two_rounds) {
-                void* pc = nullptr;
-                // boxes 24, list 4, pseudo indices 12 + ids 4, soup 48, nodes 64 bytes per chunk
-                const size_t per = 24 + 4 + 16 + 48 + 64;
-                if (int s = scratch(ctx, SLOT_CHUNKS, per * (size_t)nca + 1024, &pc)) return s;
-                char* q = static_cast<char*>(pc);
-                soup_align(q);
-                csoup = reinterpret_cast<float4*>(q);
-                q += 48 * nca;
-                cnodes = reinterpret_cast<Node*>(q);
-                q += 64 * nca;
-                boxes_a = reinterpret_cast<float*>(q);
-                q += 24 * nca;
-                cidx = reinterpret_cast<uint32_t*>(q);
-                q += 12 * nca;
-                ct2o = reinterpret_cast<int32_t*>(q);
-                q += 4 * nca;
-                clist = reinterpret_cast<uint32_t*>(q);
-            }
-            if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
-                                          tchunk_a, (uint32_t*)ta, words + 5, boxes_a, chunk_list, words + 8))
+        const int leaf_a = join_leaf(o, A), leaf_b = join_leaf(o, B);
+        // Chunk-culled sides build over groups of consecutive triangles (leaf
+        // = one group of `leaf` triangles, rounded to a power of two).  In a
+        // partitioned dataset no group may span two partitions (instanced
+        // meshes never do); otherwise the hierarchies are built over the
+        // surviving triangles.
+        bool grouped = tri_chunks;
+        if (grouped && A->num_parts > 0) {
+            int32_t* mixed = reinterpret_cast<int32_t*>(words + 13);
+            cudaMemsetAsync(mixed, 0, sizeof(int32_t), ctx->stream);
+            if (int s = launch_group_mixed(ctx, nullptr, (int64_t)((A->nt + 31) / 32), A->d_tri_to_object,
+                                           A->d_obj_part, (int64_t)A->nt, group_size(leaf_a), mixed))
                 return s;
-            if (two_rounds) {
-                if (int s = launch_flag_list(ctx, tchunk_a, nca, clist, words + 7)) return s;
-                int64_t n_act = 0;
-                if (int s = host_value(ctx, words + 7, 8, &n_act, "active chunks")) return s;
-                if (int s = launch_object_pseudo_tris(ctx, (int32_t)nca, cidx, ct2o)) return s;
-                BvhShape shc;
-                if (int s = build_lbvh(ctx, boxes_a, cidx, ct2o, clist, n_act, 4, csoup, cnodes, &shc, nullptr))
+            if (int s = launch_group_mixed(ctx, nullptr, (int64_t)((B->nt + 31) / 32), B->d_tri_to_object,
+                                           B->d_obj_part, (int64_t)B->nt, group_size(leaf_b), mixed))
+                return s;
+            int64_t m = 0;
+            if (int s = host_value(ctx, mixed, 4, &m, "group partitions")) return s;
+            grouped = m == 0;
+        }
+        if (grouped) {
+            // 1. A's triangle chunks against B's object boxes; 2. A's per-join
+            // hierarchy over the groups of those chunks that meet a B object
+            // box; 3. B's chunks against A's kept triangles; 4. B's per-join
+            // hierarchy over the groups of those chunks that meet one.  Groups
+            // of a few consecutive triangles have tight boxes (a 32-triangle
+            // chunk can straddle the ends of two tube branches), so B's
+            // culling against A's kept triangles is much finer than against
+            // boxes of A's chunks.  Every round keeps the triangles that
+            // contain a point of the other side.
+            if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
+                                          tchunk_a, (uint32_t*)ta, words + 5, nullptr, chunk_list, words + 8))
+                return s;
+            bool filtered[2] = {false, false};
+            if (int s = grouped_side(0, tchunk_a, (uint32_t*)ta, leaf_a, &objB_, &filtered[0])) return s;
+            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b, va,
+                                          tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
+                return s;
+            if (int s = grouped_side(1, tchunk_b, (uint32_t*)tb, leaf_b, &va, &filtered[1])) return s;
+            const bool use[2] = {triangle_rays(0, true), triangle_rays(1, true)};
+            const int G[2] = {group_size(leaf_a), group_size(leaf_b)};
+            // rays: A's groups against B's kept triangles; B's groups met A's already
+            const bool pre[2] = {false, filtered[1]};
+            if (int s = soup_ray_lists(use, G, pre)) return s;
+            if (!use[0])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
+                                              words + 0, nullptr, chunk_list, words + 8))
                     return s;
-                cull_b = DevDataset{};
-                cull_b.soup = csoup;
-                cull_b.nodes = cnodes;
-                cull_b.num_tris = n_act;
-                cull_b.root_is_leaf = shc.root_is_leaf;
-                cull_b.root_leaf_count = shc.root_leaf_count;
-                cull_b.soup_boxes = 1;
-                if (int s = wide_nodes(cull_b, shc.num_nodes, SLOT_NODES4_CHUNKS, true)) return s;
-            }
-            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b,
-                                          cull_b, tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
+            if (!use[1])
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, va, echunk_b, list[1],
+                                              words + 1, nullptr, chunk_list, words + 8))
+                    return s;
+            listed[0] = listed[1] = true;
+            timer.span(b0, timer.record(), &st.ms_build);
+            return PIERCE_OK;
+        }
+        if (tri_chunks) {
+            // groups spanning partitions: the surviving chunks' triangles
+            if (int s = launch_chunk_cull(ctx, false, A->d_vertices, A->d_indices, A->d_tri_to_object, va, act_a, objB,
+                                          tchunk_a, (uint32_t*)ta, words + 5, nullptr, chunk_list, words + 8))
+                return s;
+            if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b, objA,
+                                          tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
                 return s;
         } else {
             // Parity over these hierarchies counts every crossing above a first
@@ -1198,49 +1204,6 @@ struct Join {
                                             (uint32_t*)tb, words + 6))
                 return s;
         }
-        const int leaf_a = join_leaf(o, A), leaf_b = join_leaf(o, B);
-        // Unpartitioned chunk-culled sides build over groups of consecutive
-        // triangles (leaf = one group of `leaf` triangles, rounded to a power
-        // of two): the active chunk lists replace the triangle lists.  Their
-        // edge chunks are then culled against the other side's kept
-        // triangles: an edge that meets the other side meets a kept triangle.
-        bool grouped = tri_chunks;
-        if (grouped && A->num_parts > 0) {
-            // partitioned: groups must not span two partitions (instanced
-            // meshes never do); otherwise the hierarchies are built over the
-            // surviving triangles
-            int32_t* mixed = reinterpret_cast<int32_t*>(words + 13);
-            cudaMemsetAsync(mixed, 0, sizeof(int32_t), ctx->stream);
-            if (int s = launch_group_mixed(ctx, tchunk_a, (int64_t)((A->nt + 31) / 32), A->d_tri_to_object,
-                                           A->d_obj_part, (int64_t)A->nt, group_size(leaf_a), mixed))
-                return s;
-            if (int s = launch_group_mixed(ctx, tchunk_b, (int64_t)((B->nt + 31) / 32), B->d_tri_to_object,
-                                           B->d_obj_part, (int64_t)B->nt, group_size(leaf_b), mixed))
-                return s;
-            int64_t m = 0;
-            if (int s = host_value(ctx, mixed, 4, &m, "group partitions")) return s;
-            grouped = m == 0;
-        }
-        if (grouped) {
-            if (int s = grouped_builds(tchunk_a, tchunk_b, (uint32_t*)ta, (uint32_t*)tb, leaf_a, leaf_b, cull_b))
-                return s;
-            const bool use[2] = {triangle_rays(0, true), triangle_rays(1, true)};
-            const int G[2] = {group_size(leaf_a), group_size(leaf_b)};
-            // A's groups were filtered against B's kept triangles already
-            const bool pre[2] = {a_groups_met_b_, false};
-            if (int s = soup_ray_lists(use, G, pre)) return s;
-            if (!use[0])
-                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
-                                              words + 0, nullptr, chunk_list, words + 8))
-                    return s;
-            if (!use[1])
-                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, va, echunk_b, list[1],
-                                              words + 1, nullptr, chunk_list, words + 8))
-                    return s;
-            listed[0] = listed[1] = true;
-            timer.span(b0, timer.record(), &st.ms_build);
-            return PIERCE_OK;
-        }
         const bool use_tri[2] = {triangle_rays(0, false), triangle_rays(1, false)};
         if (chunked) {
             if (!use_tri[0])
@@ -1248,9 +1211,8 @@ struct Join {
                                               list[0], words + 0, nullptr, chunk_list, words + 8))
                     return s;
             if (!use_tri[1])
-                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b,
-                                              two_rounds ? cull_b : objA, echunk_b, list[1], words + 1, nullptr,
-                                              chunk_list, words + 8))
+                if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, vb, act_b, objA, echunk_b,
+                                              list[1], words + 1, nullptr, chunk_list, words + 8))
                     return s;
         } else {
             if (!use_tri[0])
@@ -1335,58 +1297,45 @@ struct Join {
         return g;
     }
 
-    int grouped_builds(const uint8_t* tchunk_a, const uint8_t* tchunk_b, uint32_t* ids_a, uint32_t* ids_b,
-                       int leaf_a, int leaf_b, const DevDataset& filter_b) {
-        auto group_of = [](int leaf) { return group_size(leaf); };
-        pierce_dataset* ds[2] = {A, B};
-        const uint8_t* flags[2] = {tchunk_a, tchunk_b};
-        uint32_t* ids[2] = {ids_a, ids_b};
-        const int G[2] = {group_of(leaf_a), group_of(leaf_b)};
-        DevDataset* views[2] = {&va, &vb};
-        const int soup_slot[2] = {SLOT_RED_SOUP_A, SLOT_RED_SOUP_B}, node_slot[2] = {SLOT_RED_NODES_A, SLOT_RED_NODES_B};
-        int64_t nc[2] = {0, 0};
-        for (int sd = 0; sd < 2; ++sd) {
-            const int64_t chunks = (int64_t)((ds[sd]->nt + 31) / 32);
-            if (int s = launch_flag_list(ctx, flags[sd], chunks, ids[sd], words + 9 + sd)) return s;
-        }
-        for (int sd = 0; sd < 2; ++sd)
-            if (int s = host_value(ctx, words + 9 + sd, 8, &nc[sd], "active chunks")) return s;
-        // B first, keeping the groups that meet a surviving chunk box of A
-        // (or an object box of A); then A, keeping the groups that meet a
-        // kept group of B (or an object box of B)
-        for (int sd = 1; sd >= 0; --sd) {
-            const int64_t ng = nc[sd] * (32 / G[sd]);
-            const int32_t parts = ds[sd]->num_parts;
-            void *sp = nullptr, *np = nullptr, *gp = nullptr;
-            if (int s = scratch(ctx, soup_slot[sd], 48 * 32 * (size_t)std::max<int64_t>(nc[sd], 1), &sp)) return s;
-            if (int s = scratch(ctx, node_slot[sd], 64 * (size_t)std::max<int64_t>(ng, 1) + 8 * (size_t)parts, &np))
-                return s;
-            int2* roots = parts ? reinterpret_cast<int2*>((Node*)np + std::max<int64_t>(ng, 1)) : nullptr;
-            if (int s = scratch(ctx, SLOT_GROUPS, 96 * (size_t)std::max<int64_t>(ng, 1) + 512, &gp)) return s;
-            const DevDataset* filter = nullptr;
-            if (sd == 1) filter = &filter_b;
-            else if (vb.nodes4 && !vb.root_is_leaf) filter = &vb;
-            else filter = &objB_;
-            if (!filter->nodes4) filter = nullptr;
-            if (sd == 0) a_groups_met_b_ = filter == &vb;
-            BvhShape sh;
-            int64_t kept = ng;
-            if (int s = build_grouped_lbvh(ctx, ds[sd]->d_vertices, ds[sd]->d_indices, ds[sd]->d_tri_to_object,
-                                           (int64_t)ds[sd]->nt, ids[sd], nc[sd], G[sd], gp, (float4*)sp, (Node*)np,
-                                           &sh, filter, words + 11 + sd, &kept, ds[sd]->d_obj_part, parts, roots))
-                return s;
-            DevDataset& v = *views[sd];
-            v.soup = (const float4*)sp;
-            v.nodes = (const Node*)np;
-            v.num_tris = kept * G[sd];
-            v.root_is_leaf = sh.root_is_leaf;
-            v.root_leaf_count = sh.root_leaf_count;
-            v.part_roots = roots;
-            // four-wide copy in every traversal mode: it also filters the
-            // other side's groups and culls the edge chunks
-            if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A, true)) return s;
-            st.active_triangles[sd] = (uint64_t)(kept * G[sd]);
-        }
+    // One side's per-join hierarchy over groups of G consecutive triangles of
+    // its flagged 32-triangle chunks (ids: the side's chunk-list buffer),
+    // keeping only the groups whose box meets a leaf item of `filter` (a
+    // four-wide hierarchy of the other side; none: every group).
+    // *filtered tells whether the filter ran.
+    int grouped_side(int sd, const uint8_t* flags, uint32_t* ids, int leaf, const DevDataset* filter, bool* filtered) {
+        pierce_dataset* ds = sd ? B : A;
+        const int G = group_size(leaf);
+        const int64_t chunks = (int64_t)((ds->nt + 31) / 32);
+        if (int s = launch_flag_list(ctx, flags, chunks, ids, words + 9 + sd)) return s;
+        int64_t nc = 0;
+        if (int s = host_value(ctx, words + 9 + sd, 8, &nc, "active chunks")) return s;
+        const int64_t ng = nc * (32 / G);
+        const int32_t parts = ds->num_parts;
+        const int soup_slot = sd ? SLOT_RED_SOUP_B : SLOT_RED_SOUP_A, node_slot = sd ? SLOT_RED_NODES_B : SLOT_RED_NODES_A;
+        void *sp = nullptr, *np = nullptr, *gp = nullptr;
+        if (int s = scratch(ctx, soup_slot, 48 * 32 * (size_t)std::max<int64_t>(nc, 1), &sp)) return s;
+        if (int s = scratch(ctx, node_slot, 64 * (size_t)std::max<int64_t>(ng, 1) + 8 * (size_t)parts, &np)) return s;
+        int2* roots = parts ? reinterpret_cast<int2*>((Node*)np + std::max<int64_t>(ng, 1)) : nullptr;
+        if (int s = scratch(ctx, SLOT_GROUPS, 96 * (size_t)std::max<int64_t>(ng, 1) + 512, &gp)) return s;
+        if (filter && !filter->nodes4) filter = nullptr;
+        *filtered = filter != nullptr;
+        BvhShape sh;
+        int64_t kept = ng;
+        if (int s = build_grouped_lbvh(ctx, ds->d_vertices, ds->d_indices, ds->d_tri_to_object, (int64_t)ds->nt, ids,
+                                       nc, G, gp, (float4*)sp, (Node*)np, &sh, filter, words + 11 + sd, &kept,
+                                       ds->d_obj_part, parts, roots))
+            return s;
+        DevDataset& v = sd ? vb : va;
+        v.soup = (const float4*)sp;
+        v.nodes = (const Node*)np;
+        v.num_tris = kept * G;
+        v.root_is_leaf = sh.root_is_leaf;
+        v.root_leaf_count = sh.root_leaf_count;
+        v.part_roots = roots;
+        // four-wide copy in every traversal mode: it also culls the other
+        // side's chunks and filters its groups and rays
+        if (int s = wide_nodes(v, sh.num_nodes, sd ? SLOT_NODES4_B : SLOT_NODES4_A, true)) return s;
+        st.active_triangles[sd] = (uint64_t)(kept * G);
         return PIERCE_OK;
     }
 

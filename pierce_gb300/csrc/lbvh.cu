@@ -1028,7 +1028,8 @@ int collapse4(pierce_ctx* ctx, const Node* nodes, int64_t num_nodes, Node4* out)
 }
 
 // Partitioned datasets: does any group of G triangles of a flagged chunk
-// hold triangles of two partitions?  (Then the join builds over triangles.)
+// (every chunk when chunk_flags is null) hold triangles of two partitions?
+// (Then the join builds over triangles.)
 __global__ void __launch_bounds__(256) k_group_mixed(const uint8_t* __restrict__ chunk_flags, int64_t n_chunks,
                                                      const int32_t* __restrict__ t2o,
                                                      const int32_t* __restrict__ obj_part, int64_t nt, int G,
@@ -1036,7 +1037,7 @@ __global__ void __launch_bounds__(256) k_group_mixed(const uint8_t* __restrict__
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_chunks; c += warps) {
-        if (!chunk_flags[c]) continue;  // warp-uniform
+        if (chunk_flags && !chunk_flags[c]) continue;  // warp-uniform
         const int64_t t = group_item(c, lane / G, G, lane % G, nt);
         const int32_t o = __ldg(t2o + t);
         const int32_t p = o >= 0 ? __ldg(obj_part + o) : -1;
