@@ -36,6 +36,9 @@ int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count);
 int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                                   uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
+int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
+                             const DevDataset& a, const DevDataset& b, uint64_t* out, unsigned long long* count,
+                             uint64_t cap, unsigned long long* fallback);
 int launch_object_pseudo_tris(pierce_ctx* ctx, int32_t n, uint32_t* idx, int32_t* t2o);
 int launch_parity(pierce_ctx* ctx, const DevDataset& src, const DevDataset& tgt, int swap, uint64_t* table,
                   uint32_t* parity, uint64_t slots, int64_t src_lo = 0, int64_t src_hi = -1);
@@ -951,6 +954,64 @@ struct Join {
     // containment: the parity table of B's first vertices in A (odd entries
     // are the candidate pairs), computed once per join
     uint64_t min_table_slots = 0;  // pair table size floor after a table that proved too small
+    bool pairs_pending = false;    // containment: candidate pairs to test before any hierarchy is built
+
+    // Containment from the candidate pairs directly (k_containment_pairs):
+    // the odd parity pairs none of whose triangles meet.  *fallback: some
+    // pair was too large to test this way (nothing is emitted then).
+    int containment_by_pairs(pierce_result** out, bool* fallback) {
+        *fallback = false;
+        uint64_t cap = 8 * (uint64_t)std::max(B->num_objects, 1) + 16;
+        uint64_t* ckeys = nullptr;
+        uint64_t n = 0;
+        const int b = timer.record();
+        for (;;) {
+            void* p = nullptr;
+            if (int s = scratch(ctx, SLOT_BUILD_D, cap * 8, &p)) return s;
+            ckeys = static_cast<uint64_t*>(p);
+            void* pc = nullptr;
+            if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+            unsigned long long* d_count = static_cast<unsigned long long*>(pc);
+            cudaMemsetAsync(d_count, 0, 16, ctx->stream);
+            if (int s = launch_containment_pairs(ctx, cont_ptable, cont_par, cont_pslots, va, vb, ckeys, d_count, cap,
+                                                 d_count + 1))
+                return s;
+            int64_t nf = 0, nv = 0;
+            if (int s = host_value(ctx, d_count + 1, 8, &nf, "containment pairs left over")) return s;
+            if (nf > 0) {
+                *fallback = true;
+                return PIERCE_OK;
+            }
+            if (int s = host_value(ctx, d_count, 8, &nv, "containment count")) return s;
+            n = (uint64_t)nv;
+            if (n <= cap) break;
+            cap = n;
+            st.retries++;
+        }
+        timer.span(b, timer.record(), &st.ms_edge_rays[1]);
+        st.containment_pairs = n;
+        pierce_result* r = new pierce_result();
+        r->count = n;
+        r->capacity = n;
+        r->containment_count = n;
+        if (int s = result_alloc(ctx, (void**)&r->d_pairs, std::max<uint64_t>(n, 1) * 8)) {
+            delete r;
+            return s;
+        }
+        const int tb = timer.record();
+        if (n)
+            if (int s = sort_u64_keys(ctx, ckeys, reinterpret_cast<uint64_t*>(r->d_pairs), (int64_t)n)) {
+                pierce_result_destroy(r);
+                return s;
+            }
+        timer.span(tb, timer.record(), &st.ms_dedup);
+        if (int s = keys_to_pairs(ctx, reinterpret_cast<uint64_t*>(r->d_pairs), (int64_t)n)) {
+            pierce_result_destroy(r);
+            return s;
+        }
+        *out = r;
+        return PIERCE_OK;
+    }
     // shards: this join traces shard `shard_i` of `shard_n` (rays by list
     // position, parity rays by source object)
     int shard_i() const { return o.shard_count > 1 ? o.shard_index : 0; }
@@ -1106,7 +1167,21 @@ struct Join {
                                                       act_b, B->num_objects))
                 return s;
             rays_by_candidates = true;
+            // the candidate pairs are tested directly; the hierarchies are
+            // built only if some pair is too large for that
+            pairs_pending = true;
+            timer.span(b0, timer.record(), &st.ms_build);
+            return PIERCE_OK;
         }
+        return build_hierarchies(b0);
+    }
+
+    // Culling rounds and per-join hierarchies (from the object flags
+    // prepare_active_bvh computed).
+    int build_hierarchies(int b0) {
+        uint8_t* act_a = active;
+        uint8_t* act_b = active + std::max(A->num_objects, 1);
+        const DevDataset objA = objA_, objB = objB_;
         void *ta = nullptr, *tb = nullptr;
         if (int s = scratch(ctx, SLOT_TRIS_A, 4 * (A->nt + 64), &ta)) return s;
         if (int s = scratch(ctx, SLOT_TRIS_B, 4 * (B->nt + 64), &tb)) return s;
@@ -1816,6 +1891,13 @@ struct Join {
     }
 
     int run_containment(pierce_result** out) {
+        if (pairs_pending) {
+            bool fallback = false;
+            if (int s = containment_by_pairs(out, &fallback)) return s;
+            if (!fallback) return PIERCE_OK;
+            pairs_pending = false;
+            if (int s = build_hierarchies(timer.record())) return s;
+        }
         // Overlap set of A vs B (both directions as in the reference), then
         // parity of B's first vertices against A, filtered by the overlap set.
         const bool save_ab = ab, save_ba = ba;

@@ -879,6 +879,137 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
         flags[i] = flags[i] == 3u ? 1u : 0u;
 }
 
+// ---- containment by candidate pairs -------------------------------------------
+// Containment is parity(B in A) \ overlap (pierce_containment_main.cpp:
+// 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
+// warp takes one such pair: the triangles of a, then of b, whose boxes meet
+// the intersection of the two object boxes are listed in shared memory, and
+// every listed pair of triangles whose boxes meet is tested with the exact
+// closed triangle-triangle predicate (an edge of one meets the other: six
+// segment tests, the edge definition for the edges of triangles).  The pair
+// is a containment pair when none meets.  A pair whose objects hold more than
+// kPairScanMax triangles together, or whose lists outgrow kPairList, is
+// counted in *fallback and the join takes the culling pipeline instead.
+constexpr int kPairList = 384;
+constexpr int kPairScanMax = 1 << 16;
+constexpr int kPairWarps = 4;
+
+struct PairParams {
+    const uint64_t* ptable;
+    const uint32_t* parity;
+    uint64_t pslots;
+    DevDataset a, b;  // vertices, indices, object ranges and boxes
+    uint64_t* out;
+    unsigned long long* count;
+    uint64_t cap;
+    unsigned long long* fallback;
+    DevCounters* ctr;
+};
+
+__device__ __forceinline__ float3 tri_vertex(const DevDataset& d, uint32_t tri, int k) {
+    const uint32_t i = __ldg(d.idx + 3 * (size_t)tri + k);
+    return make_float3(__ldg(d.verts + 3 * (size_t)i), __ldg(d.verts + 3 * (size_t)i + 1),
+                       __ldg(d.verts + 3 * (size_t)i + 2));
+}
+
+__device__ __forceinline__ bool tri_box_meets(const float3& p, const float3& q, const float3& r, const float3& lo,
+                                              const float3& hi) {
+    return box_overlap(fminf(p.x, fminf(q.x, r.x)), fmaxf(p.x, fmaxf(q.x, r.x)), fminf(p.y, fminf(q.y, r.y)),
+                       fmaxf(p.y, fmaxf(q.y, r.y)), fminf(p.z, fminf(q.z, r.z)), fmaxf(p.z, fmaxf(q.z, r.z)), lo, hi);
+}
+
+// The warp lists the triangles of range r (first, count) of d whose box
+// meets [lo, hi]; returns their number, or -1 when they exceed kPairList.
+__device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const float3& hi, uint32_t* list, int lane) {
+    int n = 0;
+    for (int base = 0; base < r.y; base += 32) {
+        const int k = base + lane;
+        bool meet = false;
+        uint32_t t = 0;
+        if (k < r.y) {
+            t = (uint32_t)(r.x + k);
+            meet = tri_box_meets(tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2), lo, hi);
+        }
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
+        const int pos = n + __popc(m & ((1u << lane) - 1u));
+        if (meet && pos < kPairList) list[pos] = t;
+        n += __popc(m);
+    }
+    __syncwarp();
+    return n > kPairList ? -1 : n;
+}
+
+__global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
+    __shared__ uint32_t s_list[kPairWarps][2][kPairList];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    PredCounters pc{0, 0};
+    uint32_t tests = 0;
+    const int64_t warps = (int64_t)gridDim.x * kPairWarps;
+    for (int64_t i = blockIdx.x * (int64_t)kPairWarps + w; i < (int64_t)P.pslots; i += warps) {
+        const uint64_t key = P.ptable[i];
+        if (key == kEmptyKey || !(P.parity[i] & 1u)) continue;  // warp-uniform
+        const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+        const float* ba = P.a.obj_box + 6 * (size_t)a;
+        const float* bb = P.b.obj_box + 6 * (size_t)b;
+        const float3 lo = make_float3(fmaxf(__ldg(ba), __ldg(bb)), fmaxf(__ldg(ba + 1), __ldg(bb + 1)),
+                                      fmaxf(__ldg(ba + 2), __ldg(bb + 2)));
+        const float3 hi = make_float3(fminf(__ldg(ba + 3), __ldg(bb + 3)), fminf(__ldg(ba + 4), __ldg(bb + 4)),
+                                      fminf(__ldg(ba + 5), __ldg(bb + 5)));
+        bool meets = false, undecided = false;
+        if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
+            const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
+            if ((int64_t)ra.y + rb.y > kPairScanMax) {
+                undecided = true;
+            } else {
+                const int na = list_near(P.a, ra, lo, hi, s_list[w][0], lane);
+                const int nb = na > 0 ? list_near(P.b, rb, lo, hi, s_list[w][1], lane) : 0;
+                if (na < 0 || nb < 0) {
+                    undecided = true;
+                } else {
+                    const int total = na * nb;
+                    for (int base = 0; base < total; base += 32) {
+                        const int k = base + lane;
+                        bool hit = false;
+                        if (k < total) {
+                            const uint32_t ta = s_list[w][0][k / nb], tb = s_list[w][1][k % nb];
+                            const float3 a0 = tri_vertex(P.a, ta, 0), a1 = tri_vertex(P.a, ta, 1),
+                                         a2 = tri_vertex(P.a, ta, 2);
+                            const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
+                                         b2 = tri_vertex(P.b, tb, 2);
+                            const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
+                                                           fminf(b0.z, fminf(b1.z, b2.z)));
+                            const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
+                                                           fmaxf(b0.z, fmaxf(b1.z, b2.z)));
+                            if (tri_box_meets(a0, a1, a2, blo, bhi)) {
+                                ++tests;
+                                hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
+                                      seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
+                                      seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                            }
+                        }
+                        if (__any_sync(0xFFFFFFFFu, hit)) {
+                            meets = true;
+                            break;
+                        }
+                    }
+                }
+            }
+        }
+        if (lane == 0) {
+            if (undecided) {
+                atomicAdd(P.fallback, 1ull);
+            } else if (!meets) {
+                const unsigned long long pos = atomicAdd(P.count, 1ull);
+                if (pos < P.cap) P.out[pos] = key;
+            }
+        }
+        __syncwarp();
+    }
+    flush_counter(&P.ctr->tri_tests, tests);
+    flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
+    flush_counter(&P.ctr->fp64_ambiguous, pc.fp64_ambiguous);
+}
+
 // Occupied slots -> dense key array (warp-aggregated cursor).  The counter
 // counts every occupied slot, so an undersized output is detected.
 __global__ void k_compact(const uint64_t* __restrict__ table, uint64_t slots, uint64_t* __restrict__ out,
@@ -1940,6 +2071,28 @@ int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const
     k_keep_candidates<<<grid_cap(ctx, nb, 256), 256, 0, ctx->stream>>>(act_b, nb);
     ctx->launches += 3;
     return check_cuda(cudaGetLastError(), "containment candidates");
+}
+
+int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
+                             const DevDataset& a, const DevDataset& b, uint64_t* out, unsigned long long* count,
+                             uint64_t cap, unsigned long long* fallback) {
+    if (!a.obj_range || !b.obj_range)
+        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "containment by pairs: objects must be stored contiguously");
+    PairParams P;
+    P.ptable = ptable;
+    P.parity = parity;
+    P.pslots = pslots;
+    P.a = a;
+    P.b = b;
+    P.out = out;
+    P.count = count;
+    P.cap = cap;
+    P.fallback = fallback;
+    P.ctr = ctx->d_counters;
+    const int64_t blocks = std::min<int64_t>(((int64_t)pslots + kPairWarps - 1) / kPairWarps, (int64_t)ctx->sm_count * 16);
+    k_containment_pairs<<<(unsigned)std::max<int64_t>(blocks, 1), 32 * kPairWarps, 0, ctx->stream>>>(P);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "containment by pairs");
 }
 
 // Grid selectivity estimate per matched cell (estimateSelectivityKernel,
