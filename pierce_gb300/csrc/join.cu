@@ -1301,8 +1301,52 @@ __device__ bool group_meets(const DevDataset& other, const int32_t* __restrict__
     return other.nodes4 ? any_hit4(other.nodes4, 0, lo, hi, leaf_hit) : true;
 }
 
+// Unique edges of a group of up to GMAX soup triangles [first, last): bit
+// 3 t + k of the result is set when edge k of triangle first + t is the first
+// occurrence of its segment in the group.  The group's vertices are loaded
+// once; each gets the id of the first vertex with the same coordinates, and
+// edges compare as unordered id pairs.
+template <int GMAX>
+__device__ __forceinline__ uint32_t group_unique_edges(const float4* __restrict__ soup, int64_t first, int64_t last,
+                                                       float3& lo, float3& hi) {
+    constexpr int NV = 3 * GMAX;
+    const int nv = 3 * (int)(last - first);
+    float4 v[NV];
+    int cid[NV];
+    lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
+    hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        cid[i] = i;
+        if (i < nv) {
+            v[i] = __ldg(soup + 3 * first + i);
+            lo.x = fminf(lo.x, v[i].x); lo.y = fminf(lo.y, v[i].y); lo.z = fminf(lo.z, v[i].z);
+            hi.x = fmaxf(hi.x, v[i].x); hi.y = fmaxf(hi.y, v[i].y); hi.z = fmaxf(hi.z, v[i].z);
+#pragma unroll
+            for (int j = 0; j < i; ++j)
+                if (cid[i] == i && same_point(v[j], v[i])) cid[i] = cid[j];
+        }
+    }
+    int key[NV];
+    uint32_t mask = 0;
+#pragma unroll
+    for (int e = 0; e < NV; ++e) {
+        const int t = e / 3, k = e % 3;
+        const int a = cid[3 * t + k], b = cid[3 * t + (k == 2 ? 0 : k + 1)];
+        key[e] = a < b ? a * 64 + b : b * 64 + a;
+        bool dup = e >= nv;
+#pragma unroll
+        for (int f = 0; f < e; ++f) dup = dup || key[f] == key[e];
+        if (!dup) mask |= 1u << e;
+    }
+    return mask;
+}
+
 // One thread per group; whole blocks step through the groups together so
-// that a warp reserves its list range with one atomicAdd.
+// that a warp reserves its list range with one atomicAdd.  GMAX: the group
+// size the kernel keeps in registers (G <= GMAX); larger groups take the
+// loop over the soup (edge_listed_before).
+template <int GMAX>
 __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ soup, int64_t n_tris, int G,
                                                    DevDataset filter, int use_filter,
                                                    const int32_t* __restrict__ obj_part, uint32_t* __restrict__ list,
@@ -1315,14 +1359,23 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
         const int64_t first = g * G;
         const int64_t last = min(first + (int64_t)G, n_tris);
         bool keep = g < n_groups;
+        uint32_t mask = 0;
+        float3 lo = make_float3(0, 0, 0), hi = make_float3(0, 0, 0);
+        if (keep) {
+            if constexpr (GMAX > 0) {
+                mask = group_unique_edges<GMAX>(soup, first, last, lo, hi);
+            } else {
+                lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
+                hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+                for (int64_t t = first; t < last; ++t)
+                    for (int v = 0; v < 3; ++v) {
+                        const float4 a = __ldg(soup + 3 * t + v);
+                        lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+                        hi.x = fmaxf(hi.x, a.x); hi.y = fmaxf(hi.y, a.y); hi.z = fmaxf(hi.z, a.z);
+                    }
+            }
+        }
         if (keep && use_filter) {
-            float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-            for (int64_t t = first; t < last; ++t)
-                for (int v = 0; v < 3; ++v) {
-                    const float4 a = __ldg(soup + 3 * t + v);
-                    lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
-                    hi.x = fmaxf(hi.x, a.x); hi.y = fmaxf(hi.y, a.y); hi.z = fmaxf(hi.z, a.z);
-                }
             const int32_t obj0 = __float_as_int(__ldg(&soup[3 * first].w));
             bool one_part = true;  // a group spanning partitions is kept
             if (obj_part && filter.part_roots) {
@@ -1333,12 +1386,17 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
             keep = !one_part || group_meets(filter, obj_part, obj0, lo, hi);
         }
         int n = 0;
-        if (keep)
-            for (int64_t t = first; t < last; ++t)
-                for (int k = 0; k < 3; ++k) {
-                    const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
-                    if (!edge_listed_before(soup, first, t, k, p, q)) ++n;
-                }
+        if (keep) {
+            if constexpr (GMAX > 0) {
+                n = __popc(mask);
+            } else {
+                for (int64_t t = first; t < last; ++t)
+                    for (int k = 0; k < 3; ++k) {
+                        const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
+                        if (!edge_listed_before(soup, first, t, k, p, q)) ++n;
+                    }
+            }
+        }
         int incl = n;
         for (int off = 1; off < 32; off <<= 1) {
             const int y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
@@ -1349,12 +1407,20 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
         if (lane == 31 && total) wbase = atomicAdd(count, (unsigned long long)total);
         wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
         unsigned long long pos = wbase + (unsigned long long)(incl - n);
-        if (n)
-            for (int64_t t = first; t < last; ++t)
-                for (int k = 0; k < 3; ++k) {
-                    const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
-                    if (!edge_listed_before(soup, first, t, k, p, q)) list[pos++] = (uint32_t)((t << 2) | k);
+        if (n) {
+            if constexpr (GMAX > 0) {
+                for (uint32_t m = mask; m; m &= m - 1) {
+                    const int e = __ffs(m) - 1;
+                    list[pos++] = (uint32_t)(((first + e / 3) << 2) | (e % 3));
                 }
+            } else {
+                for (int64_t t = first; t < last; ++t)
+                    for (int k = 0; k < 3; ++k) {
+                        const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
+                        if (!edge_listed_before(soup, first, t, k, p, q)) list[pos++] = (uint32_t)((t << 2) | k);
+                    }
+            }
+        }
     }
 }
 
@@ -1366,8 +1432,16 @@ int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G,
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays from triangles: at most 2^30 - 1 triangles");
     const int64_t n_groups = (n_tris + G - 1) / G;
     const int64_t blocks = std::min<int64_t>((n_groups + 255) / 256, (int64_t)ctx->sm_count * 16);
-    k_soup_rays<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(
-        soup, n_tris, G, filter ? *filter : DevDataset{}, filter ? 1 : 0, obj_part, list, count);
+    const unsigned grid = (unsigned)std::max<int64_t>(blocks, 1);
+    const DevDataset f = filter ? *filter : DevDataset{};
+    if (G <= 1)
+        k_soup_rays<1><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+    else if (G <= 2)
+        k_soup_rays<2><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+    else if (G <= 4)
+        k_soup_rays<4><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+    else
+        k_soup_rays<0><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "rays from triangles");
 }

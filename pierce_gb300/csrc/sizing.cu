@@ -325,6 +325,15 @@ __global__ void k_obj_tri_counts(const int32_t* __restrict__ t2o, int64_t nt, in
     }
 }
 
+// Per-object triangle counts of a dataset whose objects are stored
+// contiguously: the count of each object's triangle range (no atomics; a
+// long object would otherwise have thousands of warps add to one counter).
+__global__ void k_obj_counts_from_ranges(const int2* __restrict__ ranges, int32_t nobj,
+                                         unsigned int* __restrict__ counts) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nobj; o += (int64_t)gridDim.x * blockDim.x)
+        counts[o] = (unsigned int)__ldg(&ranges[o].y);
+}
+
 // Side statistics: acc[0] valid objects, [1..3] sum extent, [4..6] sum
 // extent^2, [7..14] histogram; bounds (ordered-int lo[3], hi[3]).
 constexpr int kAcc = 16;
@@ -491,8 +500,12 @@ int join_features(pierce_ctx* ctx, const pierce_dataset* A, const pierce_dataset
     unsigned int* cnt[2] = {cnt_a, cnt_b};
     for (int s = 0; s < 2; ++s) {
         if (ds[s]->nt > 0 && ds[s]->num_objects > 0) {
-            k_obj_tri_counts<<<grid_for(ctx, (int64_t)ds[s]->nt, 256), 256, 0, st>>>(
-                ds[s]->d_tri_to_object, (int64_t)ds[s]->nt, ds[s]->num_objects, cnt[s]);
+            if (ds[s]->contiguous && ds[s]->d_obj_range)
+                k_obj_counts_from_ranges<<<grid_for(ctx, ds[s]->num_objects, 256), 256, 0, st>>>(
+                    ds[s]->d_obj_range, ds[s]->num_objects, cnt[s]);
+            else
+                k_obj_tri_counts<<<grid_for(ctx, (int64_t)ds[s]->nt, 256), 256, 0, st>>>(
+                    ds[s]->d_tri_to_object, (int64_t)ds[s]->nt, ds[s]->num_objects, cnt[s]);
             k_side_stats<<<grid_for(ctx, ds[s]->num_objects, 256), 256, 0, st>>>(
                 ds[s]->d_obj_box, cnt[s], ds[s]->num_objects, acc + kAcc * s, bounds + 6 * s);
             launches += 2;
