@@ -184,10 +184,11 @@ typedef struct pierce_join_opts {
                                      pierce_preprocess extracts them): a segment's hits do not depend on
                                      its orientation */
     /* Shard shard_index of shard_count (0 or 1: the whole join), for one
-     * process per GPU: the edge rays of each direction are split into
-     * shard_count contiguous ranges of the join's ray list and the parity
-     * rays into ranges of source objects; the union of the shards' pairs is
-     * the join's pair set (overlap, intersection).  Containment is split by
+     * process per GPU: each edge ray belongs to one shard by a hash of its
+     * segment's endpoints (rays from triangles) or by its range of edge
+     * indices (the dataset's edges), and the parity rays by ranges of source
+     * objects; the union of the shards' pairs is the join's pair set
+     * (overlap, intersection).  Containment is split by
      * B object (each shard's pairs are those of its B objects; needs
      * active_bvh, both datasets' objects stored contiguously and no
      * include_overlap_pairs).  Every shard builds the same per-join
@@ -226,7 +227,8 @@ typedef struct pierce_stats {
     double ms_sizing;             /* LEARNED sizing: features + inference */
     int32_t sizing_overflow;      /* LEARNED sizing: 1 when the pairs exceeded the predicted capacity
                                      and the join was rerun two-pass */
-    int32_t reserved;
+    int32_t containment_by_pairs; /* containment: 1 when the odd-parity candidate pairs were tested directly
+                                     (no per-join hierarchies were built) */
 } pierce_stats;
 
 typedef struct pierce_dataset_info {

@@ -82,7 +82,7 @@ class Stats(C.Structure):
                 ("launches", I32), ("ms_count_pass", D * 2), ("raw_pairs", U64 * 2),
                 ("hash_accesses", U64), ("hash_contentions", U64), ("ms_build", D),
                 ("active_triangles", U64 * 2), ("predicted_pairs", D), ("ms_sizing", D),
-                ("sizing_overflow", I32), ("reserved", I32)]
+                ("sizing_overflow", I32), ("containment_by_pairs", I32)]
 
     def as_dict(self) -> dict:
         out = {}

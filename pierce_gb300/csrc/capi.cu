@@ -33,7 +33,8 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
                       uint32_t* chunk_list, unsigned long long* chunk_count);
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
-                     const int32_t* obj_part, uint32_t* list, unsigned long long* count);
+                     const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
+                     int shard_count);
 int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                                   uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
 int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
@@ -924,8 +925,11 @@ struct Join {
             void* p = nullptr;
             if (int s = scratch(ctx, slot[d], 4 * (3 * (size_t)n + 64), &p)) return s;
             list[d] = static_cast<uint32_t*>(p);
+            // a split join lists its shard's segments only (containment is
+            // split by B object instead: every candidate's rays are traced)
+            const int si = rays_by_candidates ? 0 : shard_i(), sn = rays_by_candidates ? 1 : shard_n();
             if (int s = launch_soup_rays(ctx, src.soup, n, G[d], prefiltered[d] ? nullptr : &other,
-                                         (d ? B : A)->d_obj_part, list[d], words + d))
+                                         (d ? B : A)->d_obj_part, list[d], words + d, si, sn))
                 return s;
             ray_soup[d] = src.soup;
             ray_bound[d] = 3 * n;
@@ -990,6 +994,7 @@ struct Join {
         }
         timer.span(b, timer.record(), &st.ms_edge_rays[1]);
         st.containment_pairs = n;
+        st.containment_by_pairs = 1;
         pierce_result* r = new pierce_result();
         r->count = n;
         r->capacity = n;

@@ -135,8 +135,9 @@ struct EdgeRayParams {
     // packed dataset edge
     const float4* ray_soup;
     int64_t ray_bound;  // ray indices of a listed launch lie below this
-    // shard k of n: this launch traces rays [N k / n, N (k + 1) / n) of its
-    // N rays (list positions, or edge indices without a list)
+    // shard k of n: dataset-edge rays with edge index in [E k / n,
+    // E (k + 1) / n) of the source's E edges (ray lists from triangles hold
+    // only the shard's rays already: k_soup_rays)
     int shard_index, shard_count;
 };
 
@@ -530,27 +531,29 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
         // Compacted ray list, persistent blocks: each warp takes the next
         // rays_per_fetch rays from a global cursor (the work queue), so uneven
         // ray costs balance out.
-        const unsigned long long n_all = *P.ray_count;
-        const unsigned long long lo = n_all * (unsigned long long)P.shard_index / (unsigned long long)P.shard_count;
-        const unsigned long long n = n_all * (unsigned long long)(P.shard_index + 1) / (unsigned long long)P.shard_count;
+        const unsigned long long n = *P.ray_count;
+        // the shard of a dataset-edge ray depends on its edge index only, not
+        // on its position in the list (whose order varies between runs)
+        const bool by_edge = P.shard_count > 1 && !P.ray_soup;
+        const int64_t elo = P.src.num_edges * P.shard_index / P.shard_count;
+        const int64_t ehi = P.src.num_edges * (P.shard_index + 1) / P.shard_count;
         const int lane = threadIdx.x & 31;
         const unsigned long long per = (unsigned long long)P.rays_per_fetch;
         int2* wstack = reinterpret_cast<int2*>(sstack + P.short_stack * 128) + (threadIdx.x >> 5) * kStackSize;
         for (;;) {
             unsigned long long base = 0;
-            if (lane == 0) base = lo + atomicAdd(P.ray_cursor, per);
+            if (lane == 0) base = atomicAdd(P.ray_cursor, per);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
             for (unsigned long long r = lane; r < per; r += 32) {  // per/32 rounds for every lane
                 const unsigned long long i = base + r;
+                const int64_t e = i < n ? (int64_t)P.ray_list[i] : -1;
+                const bool mine = e >= 0 && (!by_edge || (e >= elo && e < ehi));
                 if (FORM == 2) {
-                    const bool has = i < n;
-                    trace_packet<MODE, PREC>(P, has ? (int64_t)P.ray_list[i] : -1, (int64_t)i, wstack, lstack, rc,
-                                             pc);
-                    rays += has ? 1u : 0u;
-                } else if (i < n) {
-                    trace_edge<MODE, PREC>(P, (int64_t)P.ray_list[i], (int64_t)i, sstack, lstack, rc, pc,
-                                           P.short_stack);
+                    trace_packet<MODE, PREC>(P, mine ? e : -1, (int64_t)i, wstack, lstack, rc, pc);
+                    rays += mine ? 1u : 0u;
+                } else if (mine) {
+                    trace_edge<MODE, PREC>(P, e, (int64_t)i, sstack, lstack, rc, pc, P.short_stack);
                     ++rays;
                 }
             }
@@ -1306,9 +1309,23 @@ __device__ bool group_meets(const DevDataset& other, const int32_t* __restrict__
 // occurrence of its segment in the group.  The group's vertices are loaded
 // once; each gets the id of the first vertex with the same coordinates, and
 // edges compare as unordered id pairs.
+// Shard of a segment among n shards, from its endpoints alone: the same
+// segment listed by any triangle, in either orientation, lands in one shard
+// (coordinates in lexicographic order, -0 taken as +0, hashed).
+__device__ __forceinline__ int seg_shard(const float4& p, const float4& q, int n) {
+    const bool swap = q.x < p.x || (q.x == p.x && (q.y < p.y || (q.y == p.y && q.z < p.z)));
+    const float4& a = swap ? q : p;
+    const float4& b = swap ? p : q;
+    auto bits = [](float f) { return (uint64_t)__float_as_uint(__fadd_rn(f, 0.0f)); };
+    uint64_t h = fmix64((bits(a.x) << 32) | bits(a.y));
+    h = fmix64(h ^ ((bits(a.z) << 32) | bits(b.x)));
+    h = fmix64(h ^ ((bits(b.y) << 32) | bits(b.z)));
+    return (int)(h % (uint64_t)n);
+}
+
 template <int GMAX>
 __device__ __forceinline__ uint32_t group_unique_edges(const float4* __restrict__ soup, int64_t first, int64_t last,
-                                                       float3& lo, float3& hi) {
+                                                       float3& lo, float3& hi, int shard_index, int shard_count) {
     constexpr int NV = 3 * GMAX;
     const int nv = 3 * (int)(last - first);
     float4 v[NV];
@@ -1337,6 +1354,8 @@ __device__ __forceinline__ uint32_t group_unique_edges(const float4* __restrict_
         bool dup = e >= nv;
 #pragma unroll
         for (int f = 0; f < e; ++f) dup = dup || key[f] == key[e];
+        if (!dup && shard_count > 1)
+            dup = seg_shard(v[3 * t + k], v[3 * t + (k == 2 ? 0 : k + 1)], shard_count) != shard_index;
         if (!dup) mask |= 1u << e;
     }
     return mask;
@@ -1350,8 +1369,13 @@ template <int GMAX>
 __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ soup, int64_t n_tris, int G,
                                                    DevDataset filter, int use_filter,
                                                    const int32_t* __restrict__ obj_part, uint32_t* __restrict__ list,
-                                                   unsigned long long* __restrict__ count) {
+                                                   unsigned long long* __restrict__ count, int shard_index,
+                                                   int shard_count) {
     const int64_t n_groups = (n_tris + G - 1) / G;
+    // a split join lists only the segments of its shard (seg_shard)
+    auto mine = [&](const float4& p, const float4& q) {
+        return shard_count <= 1 || seg_shard(p, q, shard_count) == shard_index;
+    };
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n_groups; base += stride) {
@@ -1363,7 +1387,7 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
         float3 lo = make_float3(0, 0, 0), hi = make_float3(0, 0, 0);
         if (keep) {
             if constexpr (GMAX > 0) {
-                mask = group_unique_edges<GMAX>(soup, first, last, lo, hi);
+                mask = group_unique_edges<GMAX>(soup, first, last, lo, hi, shard_index, shard_count);
             } else {
                 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
                 hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
@@ -1393,7 +1417,7 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
                 for (int64_t t = first; t < last; ++t)
                     for (int k = 0; k < 3; ++k) {
                         const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
-                        if (!edge_listed_before(soup, first, t, k, p, q)) ++n;
+                        if (!edge_listed_before(soup, first, t, k, p, q) && mine(p, q)) ++n;
                     }
             }
         }
@@ -1417,7 +1441,8 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
                 for (int64_t t = first; t < last; ++t)
                     for (int k = 0; k < 3; ++k) {
                         const float4 p = __ldg(soup + 3 * t + k), q = __ldg(soup + 3 * t + (k == 2 ? 0 : k + 1));
-                        if (!edge_listed_before(soup, first, t, k, p, q)) list[pos++] = (uint32_t)((t << 2) | k);
+                        if (!edge_listed_before(soup, first, t, k, p, q) && mine(p, q))
+                            list[pos++] = (uint32_t)((t << 2) | k);
                     }
             }
         }
@@ -1425,7 +1450,8 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
 }
 
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
-                     const int32_t* obj_part, uint32_t* list, unsigned long long* count) {
+                     const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
+                     int shard_count) {
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     if (n_tris <= 0) return check_cuda(cudaGetLastError(), "rays from triangles");
     if (n_tris >= (int64_t(1) << 30))
@@ -1435,13 +1461,17 @@ int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G,
     const unsigned grid = (unsigned)std::max<int64_t>(blocks, 1);
     const DevDataset f = filter ? *filter : DevDataset{};
     if (G <= 1)
-        k_soup_rays<1><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+        k_soup_rays<1><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
+                                                             shard_index, shard_count);
     else if (G <= 2)
-        k_soup_rays<2><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+        k_soup_rays<2><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
+                                                             shard_index, shard_count);
     else if (G <= 4)
-        k_soup_rays<4><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+        k_soup_rays<4><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
+                                                             shard_index, shard_count);
     else
-        k_soup_rays<0><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count);
+        k_soup_rays<0><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
+                                                             shard_index, shard_count);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "rays from triangles");
 }

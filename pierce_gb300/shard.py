@@ -1,9 +1,11 @@
 """Joins split across processes, one process per GPU.
 
 Every rank holds both datasets and runs the same join with
-``shard_index = rank, shard_count = world`` (``pierce_join_opts``): the edge
-rays of each direction are split into contiguous ranges of the join's ray
-list and the parity rays into ranges of source objects, so the union of the
+``shard_index = rank, shard_count = world`` (``pierce_join_opts``): each edge
+ray belongs to one rank by a hash of its segment's endpoints (rays from the
+kept triangles) or by its range of edge indices (the dataset's edges), never
+by its position in a ray list, whose order differs from run to run; the
+parity rays are split into ranges of source objects.  The union of the
 ranks' pair sets is the join's pair set; containment is split by B object,
 which makes the ranks' pair sets disjoint.  The one exchange is at the end:
 an all-gather of each rank's pairs (variable counts, padded to the largest)
