@@ -519,50 +519,87 @@ __global__ void k_single_box(const float4* __restrict__ soup, int64_t n, float* 
 
 // ---- per-object data: first vertex, bounding box ------------------------
 
-// Per object: lowest triangle index and bounding box.  Triangles of one
-// object are usually contiguous, so a warp whose lanes all belong to one
-// object reduces in registers and issues 7 atomics instead of 224.
-__global__ void k_first_tri(const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj, int32_t* first_tri,
-                            uint32_t* obj_box_o, const float* __restrict__ verts, const uint32_t* __restrict__ idx) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
-        const int64_t t = base + threadIdx.x;
+// Triangle chunk boxes (the box of every 32 consecutive triangles) and, per
+// object, its lowest and highest triangle index, triangle count and box, in
+// one pass over the triangles.  Each warp reads a contiguous range of chunks
+// and carries the running aggregate of the object whose triangles it is
+// reading (a chunk whose 32 triangles all belong to one object contributes
+// its chunk box); the aggregate goes to memory with atomics only when the
+// object changes and at the end of the range, so an object of many
+// consecutive triangles costs a few atomics per warp that reads it instead
+// of a handful per 32 triangles (thousands of warps adding to one counter
+// serialise in L2).  Chunks that mix objects, or hold invalid object ids,
+// update per triangle.  chunk_box may be null.
+__global__ void __launch_bounds__(256) k_prepare_tris(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                                      const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj,
+                                                      float* __restrict__ chunk_box, int32_t* first_tri,
+                                                      int32_t* last, int32_t* count, uint32_t* obj_box_o) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t chunks = (nt + 31) / 32;
+    const int64_t c0 = chunks * w / nwarps, c1 = chunks * (w + 1) / nwarps;
+    // the carried aggregate (the same in every lane)
+    int32_t cur = -1, cfirst = 0, clast = 0, ccount = 0;
+    float cmn[3] = {0, 0, 0}, cmx[3] = {0, 0, 0};
+    auto flush = [&]() {
+        if (cur >= 0 && lane == 0) {
+            atomicMin(first_tri + cur, cfirst);
+            atomicMax(last + cur, clast);
+            atomicAdd(count + cur, ccount);
+            uint32_t* bx = obj_box_o + 6 * (size_t)cur;
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(bx + k, f2o(cmn[k]));
+                atomicMax(bx + 3 + k, f2o(cmx[k]));
+            }
+        }
+        cur = -1;
+    };
+    for (int64_t c = c0; c < c1; ++c) {
+        const int64_t t = c * 32 + lane;
         const bool valid = t < nt;
-        int32_t o = valid ? t2o[t] : -1;
+        int32_t o = valid ? __ldg(t2o + t) : -1;
         if (o >= nobj) o = -1;
         float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-        if (o >= 0) {
-            const float3 a = load_vertex(verts, __ldg(idx + 3 * t));
-            const float3 b = load_vertex(verts, __ldg(idx + 3 * t + 1));
-            const float3 c = load_vertex(verts, __ldg(idx + 3 * t + 2));
-            mn[0] = fminf(a.x, fminf(b.x, c.x));
-            mn[1] = fminf(a.y, fminf(b.y, c.y));
-            mn[2] = fminf(a.z, fminf(b.z, c.z));
-            mx[0] = fmaxf(a.x, fmaxf(b.x, c.x));
-            mx[1] = fmaxf(a.y, fmaxf(b.y, c.y));
-            mx[2] = fmaxf(a.z, fmaxf(b.z, c.z));
+        if (valid) {
+            for (int v = 0; v < 3; ++v) {
+                const float3 p = load_vertex(verts, __ldg(idx + 3 * t + v));
+                mn[0] = fminf(mn[0], p.x); mn[1] = fminf(mn[1], p.y); mn[2] = fminf(mn[2], p.z);
+                mx[0] = fmaxf(mx[0], p.x); mx[1] = fmaxf(mx[1], p.y); mx[2] = fmaxf(mx[2], p.z);
+            }
         }
-        const int32_t o0 = __shfl_sync(0xFFFFFFFFu, o, 0);
-        const bool uniform = __all_sync(0xFFFFFFFFu, o == o0) && o0 >= 0;
-        if (uniform) {
-            int32_t tmin = (int32_t)t;
+        float lo[3] = {mn[0], mn[1], mn[2]}, hi[3] = {mx[0], mx[1], mx[2]};
+        for (int k = 0; k < 3; ++k)
             for (int off = 16; off > 0; off >>= 1) {
-                tmin = min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, off));
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], off));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], off));
+            }
+        if (chunk_box && lane < 6) chunk_box[6 * c + lane] = lane < 3 ? lo[lane] : hi[lane - 3];
+        const int32_t o0 = __shfl_sync(0xFFFFFFFFu, o, 0);
+        if (__all_sync(0xFFFFFFFFu, o == o0) && o0 >= 0) {
+            // every triangle of the chunk belongs to o0: the chunk box is its share
+            if (o0 != cur) {
+                flush();
+                cur = o0;
+                cfirst = (int32_t)(c * 32);
+                clast = (int32_t)(c * 32 + 31);
+                ccount = 0;
                 for (int k = 0; k < 3; ++k) {
-                    mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
-                    mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
+                    cmn[k] = lo[k];
+                    cmx[k] = hi[k];
                 }
             }
-            if ((threadIdx.x & 31) == 0) {
-                atomicMin(first_tri + o0, tmin);
-                uint32_t* bx = obj_box_o + 6 * (size_t)o0;
-                for (int k = 0; k < 3; ++k) {
-                    atomicMin(bx + k, f2o(mn[k]));
-                    atomicMax(bx + 3 + k, f2o(mx[k]));
-                }
+            cfirst = min(cfirst, (int32_t)(c * 32));
+            clast = max(clast, (int32_t)(c * 32 + 31));
+            ccount += 32;
+            for (int k = 0; k < 3; ++k) {
+                cmn[k] = fminf(cmn[k], lo[k]);
+                cmx[k] = fmaxf(cmx[k], hi[k]);
             }
         } else if (o >= 0) {
             atomicMin(first_tri + o, (int32_t)t);
+            atomicMax(last + o, (int32_t)t);
+            atomicAdd(count + o, 1);
             uint32_t* bx = obj_box_o + 6 * (size_t)o;
             for (int k = 0; k < 3; ++k) {
                 atomicMin(bx + k, f2o(mn[k]));
@@ -570,30 +607,7 @@ __global__ void k_first_tri(const int32_t* __restrict__ t2o, int64_t nt, int32_t
             }
         }
     }
-}
-
-// Per object: number of triangles and highest triangle index (warps whose
-// lanes share one object aggregate first).
-__global__ void k_obj_count_last(const int32_t* __restrict__ t2o, int64_t nt, int32_t nobj, int32_t* count,
-                                 int32_t* last) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nt; base += stride) {
-        const int64_t t = base + threadIdx.x;
-        int32_t o = t < nt ? t2o[t] : -1;
-        if (o >= nobj) o = -1;
-        const int32_t o0 = __shfl_sync(0xFFFFFFFFu, o, 0);
-        const unsigned valid = __ballot_sync(0xFFFFFFFFu, o >= 0);
-        if (__all_sync(0xFFFFFFFFu, o == o0 || o < 0) && o0 >= 0) {
-            const int hi = 31 - __clz(valid);
-            if ((threadIdx.x & 31) == 0) {  // t is this warp's first triangle here
-                atomicAdd(count + o0, __popc(valid));
-                atomicMax(last + o0, (int32_t)(t + hi));
-            }
-        } else if (o >= 0) {
-            atomicAdd(count + o, 1);
-            atomicMax(last + o, (int32_t)t);
-        }
-    }
+    flush();
 }
 
 __global__ void k_obj_finish(const int32_t* __restrict__ first_tri, const int32_t* __restrict__ count,
@@ -676,11 +690,7 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready
     const int32_t nobj = ds->num_objects;
     {
         cudaStream_t st = ctx->stream;
-        const int64_t tc = (int64_t)(ds->nt + 31) / 32, ec = (int64_t)(ds->ne + 31) / 32;
-        if (tc > 0 && ds->d_tri_chunk_box)
-            k_chunk_boxes<false><<<grid_for(ctx, 32 * tc, 256), 256, 0, st>>>(ds->d_vertices, ds->d_indices, nullptr,
-                                                                              (int64_t)ds->nt, ds->d_tri_chunk_box);
-        ctx->launches += (tc > 0);
+        const int64_t ec = (int64_t)(ds->ne + 31) / 32;
         if (!edges_ready && ec > 0 && ds->d_edge_chunk_box) {
             k_chunk_boxes<true><<<grid_for(ctx, 32 * ec, 256), 256, 0, st>>>(nullptr, nullptr, ds->d_edges,
                                                                              (int64_t)ds->ne, ds->d_edge_chunk_box);
@@ -688,6 +698,13 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready
         }
     }
     if (nobj <= 0) {
+        // no objects: the triangle chunk boxes alone
+        const int64_t tc = (int64_t)(ds->nt + 31) / 32;
+        if (tc > 0 && ds->d_tri_chunk_box) {
+            k_chunk_boxes<false><<<grid_for(ctx, 32 * tc, 256), 256, 0, ctx->stream>>>(
+                ds->d_vertices, ds->d_indices, nullptr, (int64_t)ds->nt, ds->d_tri_chunk_box);
+            ctx->launches += 1;
+        }
         if (edges_ready) return check_cuda(cudaStreamWaitEvent(ctx->stream, edges_ready, 0), "upload wait");
         return PIERCE_OK;
     }
@@ -709,17 +726,18 @@ int prepare_objects(pierce_ctx* ctx, pierce_dataset* ds, cudaEvent_t edges_ready
         ctx->launches += 1;
     }
     k_obj_box_init<<<grid_for(ctx, 6 * (int64_t)nobj, 256), 256, 0, st>>>(box_o, nobj);
-    if (ds->nt > 0)
-        k_first_tri<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt, nobj,
-                                                                          first_tri, box_o, ds->d_vertices,
-                                                                          ds->d_indices);
-    if (ds->nt > 0)
-        k_obj_count_last<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, st>>>(ds->d_tri_to_object, (int64_t)ds->nt,
-                                                                               nobj, count, last);
+    if (ds->nt > 0) {
+        // one warp per range of chunks: a multiple of the SMs' warp slots
+        const int64_t tc = (int64_t)(ds->nt + 31) / 32;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((tc + 7) / 8, (int64_t)ctx->sm_count * 8));
+        k_prepare_tris<<<(unsigned)blocks, 256, 0, st>>>(ds->d_vertices, ds->d_indices, ds->d_tri_to_object,
+                                                         (int64_t)ds->nt, nobj, ds->d_tri_chunk_box, first_tri, last,
+                                                         count, box_o);
+    }
     k_obj_finish<<<grid_for(ctx, nobj, 256), 256, 0, st>>>(first_tri, count, last, nobj, (int64_t)ds->nv,
                                                             ds->d_vertices, ds->d_indices, ds->d_first_vertex, box_o,
                                                             ds->d_obj_range, flag);
-    ctx->launches += 6 + (ds->nt > 0 ? 2 : 0);
+    ctx->launches += 5 + (ds->nt > 0 ? 1 : 0);
     if (int s = check_cuda(cudaGetLastError(), "prepare_objects")) return s;
     // the edge side (uploaded on the copy stream) must have arrived
     if (edges_ready)
