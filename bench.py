@@ -609,6 +609,16 @@ def main_tubes(args):
     resident = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1 if args.only_tuned else 0)
     da = J.Dataset.from_geometry(ctx, A, resident)
     db = J.Dataset.from_geometry(ctx, B, resident)
+    # the library's autotuner picks leaf size, rays per fetch, stack depth,
+    # hash load factor and traversal form for this join (untimed)
+    autotuned, n_trials = None, 0
+    if not args.no_autotune:
+        ta = time.perf_counter()
+        autotuned, trials = J.autotune(ctx, da, db, tuned_o, repeats=2)
+        n_trials = len(trials)
+        tuned_o = J.tuned_opts(tuned_o, autotuned)
+        ctx.release_scratch()
+        log(f"autotuned in {time.perf_counter() - ta:.1f} s over {n_trials} trials: {autotuned}")
     for _ in range(max(args.warmup, 3)):
         r = J.run_join(ctx, da, db, tuned_o, download=False)
     torch.cuda.synchronize()
@@ -633,6 +643,7 @@ def main_tubes(args):
     if args.only_tuned:
         print(json.dumps({"metric": METRIC, "value": 1000.0 / tuned_ms, "unit": UNIT, "ms_per_step": tuned_ms,
                           "partial": "only the tuned device-resident joins", "config": tubes_config(args.scale),
+                          "autotuned": autotuned,
                           "stats": {k2: st[k2] for k2 in ("ms_total", "ms_build", "ms_edge_rays", "ms_dedup",
                                                           "ms_sizing", "rays", "tri_tests", "node_visits",
                                                           "raw_hits", "active_triangles", "launches")},
@@ -708,7 +719,8 @@ def main_tubes(args):
         "warmup": max(args.warmup, 3), "ms_per_step": tuned_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic", "config": cfg,
         "settings": {"leaf_size": args.leaf_size, "plain_leaf_size": args.plain_leaf_size, "sizing": "learned",
-                     "precision": "exact (fp32 filter, fp64, expansions)", "parallelism": "single GPU"},
+                     "precision": "exact (fp32 filter, fp64, expansions)", "parallelism": "single GPU",
+                     "autotuned": autotuned, "autotune_trials": n_trials},
         "sizes": {"tube_triangles": A.num_triangles, "tube_edges": A.num_edges,
                   "ellipsoid_triangles": B.num_triangles, "ellipsoid_edges": B.num_edges},
         "ray_tri_tests_per_s": st["tri_tests"] / (st["ms_total"] / 1000.0) if st["ms_total"] > 0 else None,
@@ -830,6 +842,7 @@ def main():
                          "intersection + containment of 2 x 50,000 ellipsoids; batched: 4,096 overlap queries; "
                          "preprocess: edge extraction of the .pre producer on the host cores")
     ap.add_argument("--cpu-sample-tubes", type=int, default=10)
+    ap.add_argument("--no-autotune", action="store_true", help="tubes: keep the default tuning values")
     ap.add_argument("--only-tuned", action="store_true",
                     help="tubes: only the device-resident tuned joins (profiling runs; prints a partial line)")
     ap.add_argument("--wave-tris", type=float, default=1.0e9, help="batched: triangles per wave (both sides)")

@@ -144,8 +144,10 @@ struct EdgeRayParams {
 // The segment of ray e and its source object: packed dataset edge e, or --
 // with a ray soup -- edge k = e & 3 of soup triangle t = e >> 2: (v0, v1),
 // (v1, v2) or (v2, v0), v0 carrying the object id.
+// SOUP: 1 rays from a soup, 0 dataset edges, -1 decided by P.ray_soup at run time.
+template <int SOUP = -1>
 __device__ __forceinline__ void load_ray(const EdgeRayParams& P, int64_t e, float3& p, float3& q, int32_t& obj) {
-    if (P.ray_soup) {
+    if (SOUP == 1 || (SOUP < 0 && P.ray_soup)) {
         const float4* tri = P.ray_soup + 3 * (e >> 2);
         const int k = (int)(e & 3);
         const float4 v0 = __ldg(tri);
@@ -305,13 +307,13 @@ __device__ __forceinline__ void leaf_tests(const EdgeRayParams& P, int64_t e, in
 
 // Ray e; `slot` indexes the per-ray counts and offsets of the two-pass
 // method (the ray's position in the launch's ray list, or e without one).
-template <int MODE, int PREC, bool WIDE = true>
+template <int MODE, int PREC, bool WIDE = true, int SOUP = -1>
 __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, int64_t slot, int* sstack, int* lstack,
                                            RayCounters& rc, PredCounters& pc, int depth) {
     const int tid = threadIdx.x;
     float3 p, q;
     int32_t src_obj;
-    load_ray(P, e, p, q, src_obj);
+    load_ray<SOUP>(P, e, p, q, src_obj);
     const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
     const float3 hi = make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z));
     int64_t out = (MODE == MODE_WRITE) ? P.offsets[slot] : 0;
@@ -433,7 +435,7 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
 // hits of each ray equal those of the one-ray-per-thread traversal.  When
 // the lanes start in different subtrees (partitions) each lane falls back
 // to the one-ray traversal with a local stack.
-template <int MODE, int PREC>
+template <int MODE, int PREC, int SOUP = -1>
 __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, int64_t slot, int2* wstack,
                                              int* lstack, RayCounters& rc, PredCounters& pc) {
     const int lane = threadIdx.x & 31;
@@ -442,7 +444,7 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
     if (!vmask) return;
     float3 p = make_float3(0, 0, 0), q = make_float3(0, 0, 0);
     int32_t src_obj = 0;
-    if (valid) load_ray(P, e, p, q, src_obj);
+    if (valid) load_ray<SOUP>(P, e, p, q, src_obj);
     int lf = 0, lc = 0;
     const int node0 = valid ? traversal_start(P.src, P.tgt, src_obj, lf, lc) : 0;
     const int leader = __ffs(vmask) - 1;
@@ -450,7 +452,7 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
     const int lf0 = __shfl_sync(0xFFFFFFFFu, lf, leader), lc0 = __shfl_sync(0xFFFFFFFFu, lc, leader);
     const bool same = __all_sync(0xFFFFFFFFu, !valid || (node0 == n0 && (n0 >= 0 || (lf == lf0 && lc == lc0))));
     if (!same) {
-        if (valid) trace_edge<MODE, PREC>(P, e, slot, nullptr, lstack, rc, pc, 0);
+        if (valid) trace_edge<MODE, PREC, true, SOUP>(P, e, slot, nullptr, lstack, rc, pc, 0);
         return;
     }
     const float3 lo = make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z));
@@ -520,7 +522,9 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
 // walk); FORM 2: the culled ray list in warp packets; FORM 0: one thread per
 // edge over a binary hierarchy (the unculled plain form).  Each form is its
 // own kernel, so none carries the registers of another's code.
-template <int MODE, int PREC, int FORM>
+// SOUP (listed forms): 1 rays from the source side's per-join soup, 0 the
+// dataset's edges, each its own instantiation (no registers for the other).
+template <int MODE, int PREC, int FORM, int SOUP>
 __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries
     int lstack[FORM ? kStackSize4 : kStackSize];
@@ -550,10 +554,10 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
                 const int64_t e = i < n ? (int64_t)P.ray_list[i] : -1;
                 const bool mine = e >= 0 && (!by_edge || (e >= elo && e < ehi));
                 if (FORM == 2) {
-                    trace_packet<MODE, PREC>(P, mine ? e : -1, (int64_t)i, wstack, lstack, rc, pc);
+                    trace_packet<MODE, PREC, SOUP>(P, mine ? e : -1, (int64_t)i, wstack, lstack, rc, pc);
                     rays += mine ? 1u : 0u;
                 } else if (mine) {
-                    trace_edge<MODE, PREC>(P, e, (int64_t)i, sstack, lstack, rc, pc, P.short_stack);
+                    trace_edge<MODE, PREC, true, SOUP>(P, e, (int64_t)i, sstack, lstack, rc, pc, P.short_stack);
                     ++rays;
                 }
             }
@@ -563,7 +567,7 @@ __global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
         const int64_t lo = P.src.num_edges * P.shard_index / P.shard_count;
         const int64_t hi = P.src.num_edges * (P.shard_index + 1) / P.shard_count;
         if (e >= lo && e < hi) {
-            trace_edge<MODE, PREC, false>(P, e, e, sstack, lstack, rc, pc, P.short_stack);
+            trace_edge<MODE, PREC, false, 0>(P, e, e, sstack, lstack, rc, pc, P.short_stack);
             ++rays;
         }
     }
@@ -1118,9 +1122,11 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     cudaStream_t st = ctx->stream;
 #define PG_LAUNCH(M, PR)                                    \
     do {                                                    \
-        if (P.ray_list && P.packets) k_edge_rays<M, PR, 2><<<g, B, smem, st>>>(P); \
-        else if (P.ray_list) k_edge_rays<M, PR, 1><<<g, B, smem, st>>>(P);          \
-        else k_edge_rays<M, PR, 0><<<g, B, smem, st>>>(P);                          \
+        if (P.ray_list && P.packets && P.ray_soup) k_edge_rays<M, PR, 2, 1><<<g, B, smem, st>>>(P); \
+        else if (P.ray_list && P.packets) k_edge_rays<M, PR, 2, 0><<<g, B, smem, st>>>(P);         \
+        else if (P.ray_list && P.ray_soup) k_edge_rays<M, PR, 1, 1><<<g, B, smem, st>>>(P);        \
+        else if (P.ray_list) k_edge_rays<M, PR, 1, 0><<<g, B, smem, st>>>(P);                      \
+        else k_edge_rays<M, PR, 0, 0><<<g, B, smem, st>>>(P);                                      \
     } while (0)
 #define PG_MODES(PR)                                  \
     do {                                              \

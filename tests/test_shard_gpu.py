@@ -35,14 +35,20 @@ def test_shard_union_equals_join(ctx, pair, predicate, world, sizing):
             "containment": lambda: O.containment_keys(A, B)}[predicate]()
     da, db = datasets(ctx, A, B)
     base = J.make_opts(predicate=predicate, sizing=sizing)
-    whole = J.pairs_to_keys(J.run_join(ctx, da, db, base).pairs)
+    whole_run = J.run_join(ctx, da, db, base)
+    whole = J.pairs_to_keys(whole_run.pairs)
     assert np.array_equal(whole, want)
-    parts = [J.pairs_to_keys(J.run_join(ctx, da, db, SH.shard_opts(base, k, world)).pairs) for k in range(world)]
+    runs = [J.run_join(ctx, da, db, SH.shard_opts(base, k, world)) for k in range(world)]
+    parts = [J.pairs_to_keys(r.pairs) for r in runs]
     union = np.unique(np.concatenate(parts))
     assert np.array_equal(union, want), (predicate, world)
-    assert all(len(p) < len(want) for p in parts)
     if predicate == "containment":
         assert sum(len(p) for p in parts) == len(want)  # disjoint by B object
+    else:
+        # every ray and every parity ray is traced by exactly one shard
+        for key in ("rays", "parity_rays"):
+            assert sum(r.stats[key] for r in runs) == whole_run.stats[key], key
+        assert all(0 < r.stats["rays"] < whole_run.stats["rays"] for r in runs)
 
 
 def test_shard_merge_on_device(ctx, pair):
