@@ -34,7 +34,7 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
-                     int shard_count);
+                     int shard_count, uint16_t* masks);
 int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                                   uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
 int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
@@ -106,6 +106,8 @@ enum : int {
     SLOT_NODES4_OBJ_A = 32,  // ... of the object hierarchies (culling)
     SLOT_NODES4_OBJ_B = 33,
     SLOT_CONT_PARITY = 35,    // containment: parity table of B's first vertices in A
+    SLOT_MASKS_AB = 36,       // group rays: segment masks of the listed groups, A->B
+    SLOT_MASKS_BA = 37,
 };
 }  // namespace
 
@@ -900,6 +902,10 @@ struct Join {
     // (list entries name its triangles' edges) and the list's capacity
     const float4* ray_soup[2] = {nullptr, nullptr};
     int64_t ray_bound[2] = {-1, -1};
+    // group rays: the list names groups of ray_group[d] soup triangles, with
+    // the segments to trace in ray_masks[d] (one walk per group)
+    uint16_t* ray_masks[2] = {nullptr, nullptr};
+    int ray_group[2] = {0, 0};
     // rays the launches of direction d index (list capacity or edge count)
     int64_t rays_of(int d) const { return ray_soup[d] ? ray_bound[d] : (int64_t)(d ? B->ne : A->ne); }
     // whether side d takes its rays from its kept triangles
@@ -914,25 +920,37 @@ struct Join {
     // by group; a side's groups are filtered against the other side's
     // per-join hierarchy unless `prefiltered[d]` (a culling round already
     // kept only the groups that meet it).
-    int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2]) {
+    // Group rays (one walk per group of at most 4 triangles with the box of
+    // its segments) serve the four-wide walk (traversal 0) when groups never
+    // span partitions (groups_ok); otherwise every segment walks alone.
+    int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2], bool groups_ok) {
         const DevDataset* v[2] = {&va, &vb};
-        const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA};
+        const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA}, mslot[2] = {SLOT_MASKS_AB, SLOT_MASKS_BA};
         for (int d = 0; d < 2; ++d) {
             if (!use[d]) continue;
             const DevDataset& src = *v[d];
             const DevDataset& other = *v[1 - d];
             const int64_t n = src.soup ? src.num_tris : 0;
+            const bool groups = groups_ok && o.traversal == 0 && G[d] <= 4 && other.nodes4 != nullptr;
             void* p = nullptr;
             if (int s = scratch(ctx, slot[d], 4 * (3 * (size_t)n + 64), &p)) return s;
             list[d] = static_cast<uint32_t*>(p);
+            ray_masks[d] = nullptr;
+            ray_group[d] = 0;
+            if (groups) {
+                void* pm = nullptr;
+                if (int s = scratch(ctx, mslot[d], 2 * ((size_t)n + 64), &pm)) return s;
+                ray_masks[d] = static_cast<uint16_t*>(pm);
+                ray_group[d] = G[d];
+            }
             // a split join lists its shard's segments only (containment is
             // split by B object instead: every candidate's rays are traced)
             const int si = rays_by_candidates ? 0 : shard_i(), sn = rays_by_candidates ? 1 : shard_n();
             if (int s = launch_soup_rays(ctx, src.soup, n, G[d], prefiltered[d] ? nullptr : &other,
-                                         (d ? B : A)->d_obj_part, list[d], words + d, si, sn))
+                                         (d ? B : A)->d_obj_part, list[d], words + d, si, sn, ray_masks[d]))
                 return s;
             ray_soup[d] = src.soup;
-            ray_bound[d] = 3 * n;
+            ray_bound[d] = groups ? (n + G[d] - 1) / G[d] : 3 * n;
             listed[d] = true;
         }
         return PIERCE_OK;
@@ -1249,7 +1267,7 @@ struct Join {
             const int G[2] = {group_size(leaf_a), group_size(leaf_b)};
             // rays: A's groups against B's kept triangles; B's groups met A's already
             const bool pre[2] = {false, filtered[1]};
-            if (int s = soup_ray_lists(use, G, pre)) return s;
+            if (int s = soup_ray_lists(use, G, pre, true)) return s;
             if (!use[0])
                 if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
                                               words + 0, nullptr, chunk_list, words + 8))
@@ -1342,7 +1360,8 @@ struct Join {
             // side's groups of 4 soup triangles against the other side's
             const int G[2] = {4, 4};
             const bool pre[2] = {false, false};
-            if (int s = soup_ray_lists(use_tri, G, pre)) return s;
+            // groups of soup triangles here may span partitions
+            if (int s = soup_ray_lists(use_tri, G, pre, A->num_parts == 0)) return s;
         }
         st.active_triangles[0] = (uint64_t)na;
         st.active_triangles[1] = (uint64_t)nb;
@@ -1451,6 +1470,8 @@ struct Join {
                 ro.cursor = words + 2;
                 ro.soup = ray_soup[d];
                 ro.bound = rays_of(d);
+                ro.masks = ray_masks[d];
+                ro.group_size = ray_group[d];
                 if (!rays_by_candidates) {
                     ro.shard_index = shard_i();
                     ro.shard_count = shard_n();
