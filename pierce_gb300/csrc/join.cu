@@ -683,8 +683,10 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
 // own kernel, so none carries the registers of another's code.
 // SOUP (listed forms): 1 rays from the source side's per-join soup, 0 the
 // dataset's edges, each its own instantiation (no registers for the other).
+// Group rays (FORM 3) keep 6 blocks per SM resident (80 registers, no
+// spills; 7 blocks would spill).
 template <int MODE, int PREC, int FORM, int SOUP>
-__global__ void __launch_bounds__(128) k_edge_rays(EdgeRayParams P) {
+__global__ void __launch_bounds__(128, FORM == 3 ? 6 : 1) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries (then per-form data)
     int lstack[FORM ? kStackSize4 : kStackSize];
     RayCounters rc;
