@@ -1085,17 +1085,20 @@ struct Join {
 
     // Column grids of both sides' object boxes (scratch slots meta/entries):
     // both counting passes, then the two sizes read back together.
-    int column_grids() {
+    int column_grids(bool side_a = true, bool side_b = true) {
         const DevDataset* v[2] = {&va, &vb};
         const int meta_slot[2] = {SLOT_GRID_A, SLOT_GRID_B}, entries_slot[2] = {SLOT_GRID_A_ENTRIES, SLOT_GRID_B_ENTRIES};
         ColumnGrid* g[2] = {&gridA_, &gridB_};
+        const bool want[2] = {side_a, side_b};
         void* pm[2] = {nullptr, nullptr};
         const int32_t* total[2] = {nullptr, nullptr};
         for (int sd = 0; sd < 2; ++sd) {
+            if (!want[sd]) continue;
             if (int s = scratch(ctx, meta_slot[sd], column_grid_bytes(v[sd]->num_objects), &pm[sd])) return s;
             if (int s = column_grid_count(ctx, *v[sd], pm[sd], &total[sd])) return s;
         }
         for (int sd = 0; sd < 2; ++sd) {
+            if (!want[sd]) continue;
             int64_t n = 0;
             if (int s = host_value(ctx, total[sd], 4, &n, "column grid size")) return s;
             void* pe = nullptr;
@@ -1170,32 +1173,42 @@ struct Join {
     // datasets' own triangles, or keeps every triangle (see below).
     int prepare_active_bvh() {
         const int b0 = timer.record();
-        DevDataset objA, objB;
-        if (int s = object_bvh(A, SLOT_OBJ_A, SLOT_NODES4_OBJ_A, &objA)) return s;
-        if (int s = object_bvh(B, SLOT_OBJ_B, SLOT_NODES4_OBJ_B, &objB)) return s;
-        objA_ = objA;
-        objB_ = objB;
         object_parity = A->contiguous && B->contiguous;
-        if (object_parity && o.predicate != PIERCE_OVERLAP)
-            if (int s = column_grids()) return s;
-        uint8_t* act_a = active;
-        uint8_t* act_b = active + std::max(A->num_objects, 1);
-        if (int s = launch_object_active(ctx, va, objB, act_a)) return s;
-        if (int s = launch_object_active(ctx, vb, objA, act_b)) return s;
         if (o.predicate == PIERCE_CONTAINMENT && !o.include_overlap_pairs && object_parity) {
-            // containment = parity(B in A) \ overlap: only the objects of odd
-            // parity pairs need their overlaps, so culling keeps just those
+            // containment = parity(B in A) \ overlap: the odd-parity pairs
+            // are tested directly (containment_by_pairs), which needs only
+            // A's object hierarchy and column grid for the parity; the rest
+            // is built only if some pair is too large for that
+            if (int s = object_bvh(A, SLOT_OBJ_A, SLOT_NODES4_OBJ_A, &objA_)) return s;
+            if (int s = column_grids(true, false)) return s;
             if (int s = containment_parity()) return s;
-            if (int s = launch_containment_candidates(ctx, cont_ptable, cont_par, cont_pslots, act_a, A->num_objects,
-                                                      act_b, B->num_objects))
-                return s;
             rays_by_candidates = true;
-            // the candidate pairs are tested directly; the hierarchies are
-            // built only if some pair is too large for that
             pairs_pending = true;
             timer.span(b0, timer.record(), &st.ms_build);
             return PIERCE_OK;
         }
+        if (int s = object_bvh(A, SLOT_OBJ_A, SLOT_NODES4_OBJ_A, &objA_)) return s;
+        if (int s = object_bvh(B, SLOT_OBJ_B, SLOT_NODES4_OBJ_B, &objB_)) return s;
+        if (object_parity && o.predicate != PIERCE_OVERLAP)
+            if (int s = column_grids()) return s;
+        if (int s = launch_object_active(ctx, va, objB_, active)) return s;
+        if (int s = launch_object_active(ctx, vb, objA_, active + std::max(A->num_objects, 1))) return s;
+        return build_hierarchies(b0);
+    }
+
+    // Containment whose candidate pairs were too large to test directly:
+    // B's object hierarchy, the object flags restricted to the candidates'
+    // objects, then the culling pipeline.
+    int containment_fallback() {
+        const int b0 = timer.record();
+        uint8_t* act_a = active;
+        uint8_t* act_b = active + std::max(A->num_objects, 1);
+        if (int s = object_bvh(B, SLOT_OBJ_B, SLOT_NODES4_OBJ_B, &objB_)) return s;
+        if (int s = launch_object_active(ctx, va, objB_, act_a)) return s;
+        if (int s = launch_object_active(ctx, vb, objA_, act_b)) return s;
+        if (int s = launch_containment_candidates(ctx, cont_ptable, cont_par, cont_pslots, act_a, A->num_objects, act_b,
+                                                  B->num_objects))
+            return s;
         return build_hierarchies(b0);
     }
 
@@ -1922,7 +1935,7 @@ struct Join {
             if (int s = containment_by_pairs(out, &fallback)) return s;
             if (!fallback) return PIERCE_OK;
             pairs_pending = false;
-            if (int s = build_hierarchies(timer.record())) return s;
+            if (int s = containment_fallback()) return s;
         }
         // Overlap set of A vs B (both directions as in the reference), then
         // parity of B's first vertices against A, filtered by the overlap set.
