@@ -37,6 +37,8 @@ int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G,
                      int shard_count, uint16_t* masks);
 int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                                   uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
+int launch_group_incidences(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, int step,
+                            const DevDataset& tgt, unsigned long long* count);
 int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                              const DevDataset& a, const DevDataset& b, uint64_t* out, unsigned long long* count,
                              uint64_t cap, unsigned long long* fallback);
@@ -976,6 +978,27 @@ struct Join {
     // containment: the parity table of B's first vertices in A (odd entries
     // are the candidate pairs), computed once per join
     uint64_t min_table_slots = 0;  // pair table size floor after a table that proved too small
+    int groups_a_ = 0;  // A's per-join soup: triangles per group (0: not a grouped build)
+
+    // LEARNED sizing of an overlap join, once its hierarchies exist: the
+    // network's prediction is capped by 4 x the sampled incidence bound
+    // (k_group_incidences: 1/64 of A's kept groups against B's kept
+    // triangles) + 4096.  Objects far longer than their neighbours (tubes)
+    // have boxes that meet nearly everything, which the network's features
+    // cannot see; their kept groups are small.  A cap below the true count
+    // costs only the two-pass rerun.
+    int cap_learned_size() {
+        void* pc = nullptr;
+        if (int s = scratch(ctx, SLOT_AUX, 64, &pc)) return s;
+        unsigned long long* d_count = static_cast<unsigned long long*>(pc) + 2;
+        constexpr int kStep = 64;
+        if (int s = launch_group_incidences(ctx, va.soup, va.num_tris, groups_a_, kStep, vb, d_count)) return s;
+        int64_t n = 0;
+        if (int s = host_value(ctx, d_count, 8, &n, "sampled incidences")) return s;
+        const uint64_t cap = 4 * (uint64_t)n * kStep + 4096;
+        if (cap < o.expected_pairs) o.expected_pairs = cap;
+        return PIERCE_OK;
+    }
     bool pairs_pending = false;    // containment: candidate pairs to test before any hierarchy is built
 
     // Containment from the candidate pairs directly (k_containment_pairs):
@@ -1272,6 +1295,7 @@ struct Join {
                 return s;
             bool filtered[2] = {false, false};
             if (int s = grouped_side(0, tchunk_a, (uint32_t*)ta, leaf_a, &objB_, &filtered[0])) return s;
+            groups_a_ = group_size(leaf_a);
             if (int s = launch_chunk_cull(ctx, false, B->d_vertices, B->d_indices, B->d_tri_to_object, vb, act_b, va,
                                           tchunk_b, (uint32_t*)tb, words + 6, nullptr, chunk_list, words + 8))
                 return s;
@@ -1829,6 +1853,8 @@ struct Join {
         }
         s = prepare();
         if (s) return s;
+        if (strict_capacity && o.predicate == PIERCE_OVERLAP && groups_a_ > 0 && A->num_parts == 0)
+            if ((s = cap_learned_size())) return s;
         s = run_predicate(out);
         if (strict_capacity && (s == PIERCE_ERR_HASH_FULL || s == PIERCE_ERR_OUTPUT_OVERFLOW)) {
             // the prediction was too small: the two-pass method sizes exactly

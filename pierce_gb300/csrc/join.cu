@@ -1653,6 +1653,61 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
     }
 }
 
+// Pair-count bound for output sizing: every step-th group of G source soup
+// triangles against the target's four-wide per-join hierarchy, counting the
+// target triangles whose box meets the group's box (a run of one target
+// object counts once).  Every overlap pair has a kept source group whose box
+// meets a kept target triangle of the pair's target object, so step x this
+// count estimates an upper bound on the join's pairs.
+__global__ void __launch_bounds__(256) k_group_incidences(const float4* __restrict__ soup, int64_t n_tris, int G,
+                                                          int step, DevDataset tgt, unsigned long long* count) {
+    const int64_t n_groups = (n_tris + G - 1) / G;
+    unsigned long long local = 0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s * step < n_groups;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t first = s * step * G, last = min(first + (int64_t)G, n_tris);
+        float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+        for (int64_t t = first; t < last; ++t)
+            for (int v = 0; v < 3; ++v) {
+                const float4 a = __ldg(soup + 3 * t + v);
+                lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+                hi.x = fmaxf(hi.x, a.x); hi.y = fmaxf(hi.y, a.y); hi.z = fmaxf(hi.z, a.z);
+            }
+        int32_t last_obj = -1;
+        auto visit = [&](int lfirst, int lcount) {
+            for (int k = 0; k < lcount; ++k) {
+                const int64_t t = (int64_t)lfirst + k;
+                const float4 a4 = __ldg(tgt.soup + 3 * t), b4 = __ldg(tgt.soup + 3 * t + 1),
+                             c4 = __ldg(tgt.soup + 3 * t + 2);
+                const int32_t obj = __float_as_int(a4.w);
+                if (obj == last_obj) continue;
+                if (box_overlap(fminf(a4.x, fminf(b4.x, c4.x)), fmaxf(a4.x, fmaxf(b4.x, c4.x)),
+                                fminf(a4.y, fminf(b4.y, c4.y)), fmaxf(a4.y, fmaxf(b4.y, c4.y)),
+                                fminf(a4.z, fminf(b4.z, c4.z)), fmaxf(a4.z, fmaxf(b4.z, c4.z)), lo, hi)) {
+                    last_obj = obj;
+                    ++local;
+                }
+            }
+            return false;  // visit every leaf the box meets
+        };
+        if (tgt.root_is_leaf) visit(0, tgt.root_leaf_count);
+        else if (tgt.nodes4) any_hit4(tgt.nodes4, 0, lo, hi, visit);
+    }
+    flush_counter(count, local);
+}
+
+int launch_group_incidences(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, int step,
+                            const DevDataset& tgt, unsigned long long* count) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
+    if (n_tris <= 0 || tgt.num_tris <= 0 || (!tgt.root_is_leaf && !tgt.nodes4)) return PIERCE_OK;
+    const int64_t samples = ((n_tris + G - 1) / G + step - 1) / step;
+    const int64_t blocks = std::min<int64_t>((samples + 255) / 256, (int64_t)ctx->sm_count * 8);
+    k_group_incidences<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(soup, n_tris, G, step, tgt,
+                                                                                          count);
+    ctx->launches += 1;
+    return check_cuda(cudaGetLastError(), "group incidences");
+}
+
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
                      int shard_count, uint16_t* masks) {
