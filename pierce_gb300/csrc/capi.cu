@@ -910,6 +910,9 @@ struct Join {
     int ray_group[2] = {0, 0};
     // rays the launches of direction d index (list capacity or edge count)
     int64_t rays_of(int d) const { return ray_soup[d] ? ray_bound[d] : (int64_t)(d ? B->ne : A->ne); }
+    // the walks over four-wide copies: one segment per thread (0) or one
+    // group of kept triangles per thread (3)
+    bool four_wide() const { return o.traversal == 0 || o.traversal == 3; }
     // whether side d takes its rays from its kept triangles
     bool triangle_rays(int d, bool grouped) const {
         const pierce_dataset* ds = d ? B : A;
@@ -922,9 +925,9 @@ struct Join {
     // by group; a side's groups are filtered against the other side's
     // per-join hierarchy unless `prefiltered[d]` (a culling round already
     // kept only the groups that meet it).
-    // Group rays (one walk per group of at most 4 triangles with the box of
-    // its segments) serve the four-wide walk (traversal 0) when groups never
-    // span partitions (groups_ok); otherwise every segment walks alone.
+    // Group rays (traversal 3: one walk per group of at most 4 triangles
+    // with the box of its segments) serve joins whose groups never span
+    // partitions (groups_ok); otherwise every segment walks alone.
     int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2], bool groups_ok) {
         const DevDataset* v[2] = {&va, &vb};
         const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA}, mslot[2] = {SLOT_MASKS_AB, SLOT_MASKS_BA};
@@ -933,7 +936,7 @@ struct Join {
             const DevDataset& src = *v[d];
             const DevDataset& other = *v[1 - d];
             const int64_t n = src.soup ? src.num_tris : 0;
-            const bool groups = groups_ok && o.traversal == 0 && G[d] <= 4 && other.nodes4 != nullptr;
+            const bool groups = groups_ok && o.traversal == 3 && G[d] <= 4 && other.nodes4 != nullptr;
             void* p = nullptr;
             if (int s = scratch(ctx, slot[d], 4 * (3 * (size_t)n + 64), &p)) return s;
             list[d] = static_cast<uint32_t*>(p);
@@ -1407,11 +1410,11 @@ struct Join {
     }
 
     // Four-wide copy of a hierarchy: per-join hierarchies for the
-    // one-ray-per-thread walk (traversal 0; the other traversals walk the
-    // binary nodes) and, always, the hierarchies that culling walks.
+    // one-ray-per-thread and group walks (traversals 0 and 3; the others
+    // walk the binary nodes) and, always, the hierarchies that culling walks.
     int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot, bool always = false) {
         v.nodes4 = nullptr;
-        if ((o.traversal != 0 && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
+        if ((!four_wide() && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
         void* p = nullptr;
         if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) {
             // short of memory: the binary nodes serve every walk (slower)
@@ -1490,9 +1493,9 @@ struct Join {
         for (int d = 0; d < 2; ++d) {
             if (!dirs[d]) continue;
             const DevDataset& src = d ? vb : va;
-            // the four-wide copies also serve culling; only traversal 0 walks them
+            // the four-wide copies also serve culling; traversals 0 and 3 walk them
             DevDataset tgt = d ? va : vb;
-            if (o.traversal != 0) tgt.nodes4 = nullptr;
+            if (!four_wide()) tgt.nodes4 = nullptr;
             int32_t* counts = d ? counts_ba : counts_ab;
             const int64_t* offs = d ? off_ba : off_ab;
             const int b = timer.record();
@@ -1628,6 +1631,9 @@ struct Join {
         uint64_t n_extra = 0;
         for (;;) {
             cudaMemsetAsync(words + 4, 0, 8, ctx->stream);
+            // one zero count past the end: the scan's last offset is the total
+            // (the last listed ray differs from run to run, the total does not)
+            cudaMemsetAsync(counts + n_all, 0, 4, ctx->stream);
             const size_t span0 = timer.spans.size();
             if (int s = edge_rays(0, counts, counts + na, nullptr, nullptr, nullptr, nullptr, 0, extra, amb_cap))
                 return s;
@@ -1638,8 +1644,7 @@ struct Join {
                 timer.span(timer.spans[i].first, timer.spans[i].second, target);
             }
             int tb = timer.record();
-            if (n_all > 0)
-                if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all)) return s;
+            if (int s = exclusive_scan_i32_to_i64(ctx, counts, offs, n_all + 1)) return s;
             timer.span(tb, timer.record(), &st.ms_dedup);
             uint32_t bits = 0;
             if (int s = read_device_error(ctx, &bits)) return s;
@@ -1651,14 +1656,10 @@ struct Join {
             }
             // total = last offset + last count; B->A offsets continue after the A total
             total = 0;
-            int64_t last_off = 0, last_count = 0, off_b = 0, extra_n = 0;
-            if (n_all > 0) {
-                if (int s = host_value(ctx, offs + n_all - 1, 8, &last_off, "scan total")) return s;
-                if (int s = host_value(ctx, counts + n_all - 1, 4, &last_count, "scan total")) return s;
-                if (na > 0 && nb > 0)
-                    if (int s = host_value(ctx, offs + na, 8, &off_b, "scan split")) return s;
-                total = last_off + last_count;
-            }
+            int64_t off_b = 0, extra_n = 0;
+            if (int s = host_value(ctx, offs + n_all, 8, &total, "scan total")) return s;
+            if (na > 0 && nb > 0)
+                if (int s = host_value(ctx, offs + na, 8, &off_b, "scan split")) return s;
             if (int s = host_value(ctx, words + 4, 8, &extra_n, "resolved keys")) return s;
             total_ab = (na > 0 && nb > 0) ? off_b : (na > 0 ? total : 0);
             n_extra = (uint64_t)extra_n;
@@ -2072,7 +2073,7 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
     if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
-        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 2)
+        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 3)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
     if (o.edge_source < 0 || o.edge_source > 2)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: edge_source out of range");
@@ -2153,7 +2154,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     const std::vector<int> rays = {32, 64, 128}, stacks = {8, 16, 32};
     const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
                                              : std::vector<double>{cur.hash_load_factor};
-    const std::vector<int> traversals = {0, 1, 2};
+    const std::vector<int> traversals = {0, 1, 2, 3};
     // coordinate descent: one parameter at a time, keeping the best so far
     for (int param = 0; param < 5; ++param) {
         const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()
