@@ -178,9 +178,7 @@ typedef struct pierce_join_opts {
                                      rays, 32 otherwise) */
     int32_t traversal;            /* culled rays: 0 one ray per thread over four-wide copies of the per-join
                                      hierarchies, 1 a warp traverses its 32 rays together, 2 one ray per thread
-                                     over the binary nodes, 3 one walk per thread for a group of at most 4 kept
-                                     triangles (their unique segments share the walk over the four-wide
-                                     copies; rays from the kept triangles only, else as 0) */
+                                     over the binary nodes */
     int32_t edge_source;          /* pierce_edge_source.  Exact predicates give the same pairs from either
                                      source when the dataset's edges are its triangles' edges (as
                                      pierce_preprocess extracts them): a segment's hits do not depend on
@@ -315,7 +313,7 @@ void pierce_result_destroy(pierce_result* r);
  * warp {32, 64, 128}, stack depth {8, 16, 32}, hash load factor
  * {0.25, 0.5, 0.75} when the sizing uses a hash set, traversal {one ray per
  * thread over four-wide nodes, warp packets, one ray per thread over binary
- * nodes, one walk per group of kept triangles}), each trial the best
+ * nodes}), each trial the best
  * of `repeats` timed runs after one untimed run.  *best receives the
  * fastest values; trials[0 .. *num_trials) every trial (max_trials slots,
  * may be NULL). */

@@ -34,7 +34,7 @@ int launch_chunk_cull(pierce_ctx* ctx, bool edges, const float* verts, const uin
 int launch_flag_list(pierce_ctx* ctx, const uint8_t* flags, int64_t n, uint32_t* list, unsigned long long* count);
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
-                     int shard_count, uint16_t* masks);
+                     int shard_count, const Node4* entry_nodes4, int32_t* entries);
 int launch_containment_candidates(pierce_ctx* ctx, const uint64_t* ptable, const uint32_t* parity, uint64_t pslots,
                                   uint8_t* act_a, int64_t na, uint8_t* act_b, int64_t nb);
 int launch_group_incidences(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, int step,
@@ -108,8 +108,8 @@ enum : int {
     SLOT_NODES4_OBJ_A = 32,  // ... of the object hierarchies (culling)
     SLOT_NODES4_OBJ_B = 33,
     SLOT_CONT_PARITY = 35,    // containment: parity table of B's first vertices in A
-    SLOT_MASKS_AB = 36,       // group rays: segment masks of the listed groups, A->B
-    SLOT_MASKS_BA = 37,
+    SLOT_ENTRY_AB = 38,       // rays from triangles: entry nodes of the listed groups, A->B
+    SLOT_ENTRY_BA = 39,
 };
 }  // namespace
 
@@ -904,15 +904,12 @@ struct Join {
     // (list entries name its triangles' edges) and the list's capacity
     const float4* ray_soup[2] = {nullptr, nullptr};
     int64_t ray_bound[2] = {-1, -1};
-    // group rays: the list names groups of ray_group[d] soup triangles, with
-    // the segments to trace in ray_masks[d] (one walk per group)
-    uint16_t* ray_masks[2] = {nullptr, nullptr};
-    int ray_group[2] = {0, 0};
+    // rays from triangles: per group of ray_entry_group[d] soup triangles,
+    // the four-wide target node its walks start at (group_entry)
+    int32_t* ray_entry[2] = {nullptr, nullptr};
+    int ray_entry_group[2] = {1, 1};
     // rays the launches of direction d index (list capacity or edge count)
     int64_t rays_of(int d) const { return ray_soup[d] ? ray_bound[d] : (int64_t)(d ? B->ne : A->ne); }
-    // the walks over four-wide copies: one segment per thread (0) or one
-    // group of kept triangles per thread (3)
-    bool four_wide() const { return o.traversal == 0 || o.traversal == 3; }
     // whether side d takes its rays from its kept triangles
     bool triangle_rays(int d, bool grouped) const {
         const pierce_dataset* ds = d ? B : A;
@@ -925,37 +922,37 @@ struct Join {
     // by group; a side's groups are filtered against the other side's
     // per-join hierarchy unless `prefiltered[d]` (a culling round already
     // kept only the groups that meet it).
-    // Group rays (traversal 3: one walk per group of at most 4 triangles
-    // with the box of its segments) serve joins whose groups never span
-    // partitions (groups_ok); otherwise every segment walks alone.
-    int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2], bool groups_ok) {
+    // Each listed group's segments start their walks at the group's entry
+    // node in the other side's four-wide hierarchy (group_entry), when that
+    // hierarchy is not partitioned.
+    int soup_ray_lists(const bool use[2], const int G[2], const bool prefiltered[2]) {
         const DevDataset* v[2] = {&va, &vb};
-        const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA}, mslot[2] = {SLOT_MASKS_AB, SLOT_MASKS_BA};
+        const int slot[2] = {SLOT_LIST_AB, SLOT_LIST_BA}, eslot[2] = {SLOT_ENTRY_AB, SLOT_ENTRY_BA};
         for (int d = 0; d < 2; ++d) {
             if (!use[d]) continue;
             const DevDataset& src = *v[d];
             const DevDataset& other = *v[1 - d];
             const int64_t n = src.soup ? src.num_tris : 0;
-            const bool groups = groups_ok && o.traversal == 3 && G[d] <= 4 && other.nodes4 != nullptr;
             void* p = nullptr;
             if (int s = scratch(ctx, slot[d], 4 * (3 * (size_t)n + 64), &p)) return s;
             list[d] = static_cast<uint32_t*>(p);
-            ray_masks[d] = nullptr;
-            ray_group[d] = 0;
-            if (groups) {
-                void* pm = nullptr;
-                if (int s = scratch(ctx, mslot[d], 2 * ((size_t)n + 64), &pm)) return s;
-                ray_masks[d] = static_cast<uint16_t*>(pm);
-                ray_group[d] = G[d];
+            ray_entry[d] = nullptr;
+            ray_entry_group[d] = std::max(G[d], 1);
+            const bool entries = o.traversal == 0 && other.nodes4 && !other.part_roots && !other.root_is_leaf;
+            if (entries) {
+                void* pe = nullptr;
+                if (int s = scratch(ctx, eslot[d], 4 * ((size_t)n / ray_entry_group[d] + 64), &pe)) return s;
+                ray_entry[d] = static_cast<int32_t*>(pe);
             }
             // a split join lists its shard's segments only (containment is
             // split by B object instead: every candidate's rays are traced)
             const int si = rays_by_candidates ? 0 : shard_i(), sn = rays_by_candidates ? 1 : shard_n();
             if (int s = launch_soup_rays(ctx, src.soup, n, G[d], prefiltered[d] ? nullptr : &other,
-                                         (d ? B : A)->d_obj_part, list[d], words + d, si, sn, ray_masks[d]))
+                                         (d ? B : A)->d_obj_part, list[d], words + d, si, sn,
+                                         entries ? other.nodes4 : nullptr, ray_entry[d]))
                 return s;
             ray_soup[d] = src.soup;
-            ray_bound[d] = groups ? (n + G[d] - 1) / G[d] : 3 * n;
+            ray_bound[d] = 3 * n;
             listed[d] = true;
         }
         return PIERCE_OK;
@@ -1307,7 +1304,7 @@ struct Join {
             const int G[2] = {group_size(leaf_a), group_size(leaf_b)};
             // rays: A's groups against B's kept triangles; B's groups met A's already
             const bool pre[2] = {false, filtered[1]};
-            if (int s = soup_ray_lists(use, G, pre, true)) return s;
+            if (int s = soup_ray_lists(use, G, pre)) return s;
             if (!use[0])
                 if (int s = launch_chunk_cull(ctx, true, nullptr, nullptr, nullptr, va, act_a, vb, echunk_a, list[0],
                                               words + 0, nullptr, chunk_list, words + 8))
@@ -1401,7 +1398,7 @@ struct Join {
             const int G[2] = {4, 4};
             const bool pre[2] = {false, false};
             // groups of soup triangles here may span partitions
-            if (int s = soup_ray_lists(use_tri, G, pre, A->num_parts == 0)) return s;
+            if (int s = soup_ray_lists(use_tri, G, pre)) return s;
         }
         st.active_triangles[0] = (uint64_t)na;
         st.active_triangles[1] = (uint64_t)nb;
@@ -1410,11 +1407,11 @@ struct Join {
     }
 
     // Four-wide copy of a hierarchy: per-join hierarchies for the
-    // one-ray-per-thread and group walks (traversals 0 and 3; the others
-    // walk the binary nodes) and, always, the hierarchies that culling walks.
+    // one-ray-per-thread walk (traversal 0; the other traversals walk the
+    // binary nodes) and, always, the hierarchies that culling walks.
     int wide_nodes(DevDataset& v, uint64_t num_nodes, int slot, bool always = false) {
         v.nodes4 = nullptr;
-        if ((!four_wide() && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
+        if ((o.traversal != 0 && !always) || num_nodes == 0 || v.root_is_leaf) return PIERCE_OK;
         void* p = nullptr;
         if (int s = scratch(ctx, slot, sizeof(Node4) * (size_t)num_nodes + 128, &p)) {
             // short of memory: the binary nodes serve every walk (slower)
@@ -1493,9 +1490,9 @@ struct Join {
         for (int d = 0; d < 2; ++d) {
             if (!dirs[d]) continue;
             const DevDataset& src = d ? vb : va;
-            // the four-wide copies also serve culling; traversals 0 and 3 walk them
+            // the four-wide copies also serve culling; only traversal 0 walks them
             DevDataset tgt = d ? va : vb;
-            if (!four_wide()) tgt.nodes4 = nullptr;
+            if (o.traversal != 0) tgt.nodes4 = nullptr;
             int32_t* counts = d ? counts_ba : counts_ab;
             const int64_t* offs = d ? off_ba : off_ab;
             const int b = timer.record();
@@ -1510,8 +1507,8 @@ struct Join {
                 ro.cursor = words + 2;
                 ro.soup = ray_soup[d];
                 ro.bound = rays_of(d);
-                ro.masks = ray_masks[d];
-                ro.group_size = ray_group[d];
+                ro.entries = ray_entry[d];
+                ro.entry_group = ray_entry_group[d];
                 if (!rays_by_candidates) {
                     ro.shard_index = shard_i();
                     ro.shard_count = shard_n();
@@ -2073,7 +2070,7 @@ static int validate_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     if (!(o.hash_load_factor > 0.0 && o.hash_load_factor <= 1.0))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: hash_load_factor must be in (0, 1]");
     if (o.leaf_size < 0 || o.leaf_size > 16 || o.rays_per_warp < 0 || o.rays_per_warp % 32 != 0 ||
-        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 3)
+        o.rays_per_warp > 1024 || o.stack_depth < 0 || o.stack_depth > 32 || o.traversal < 0 || o.traversal > 2)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: tuning value out of range");
     if (o.edge_source < 0 || o.edge_source > 2)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "join: edge_source out of range");
@@ -2154,7 +2151,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     const std::vector<int> rays = {32, 64, 128}, stacks = {8, 16, 32};
     const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
                                              : std::vector<double>{cur.hash_load_factor};
-    const std::vector<int> traversals = {0, 1, 2, 3};
+    const std::vector<int> traversals = {0, 1, 2};
     // coordinate descent: one parameter at a time, keeping the best so far
     for (int param = 0; param < 5; ++param) {
         const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()

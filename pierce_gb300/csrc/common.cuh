@@ -116,10 +116,10 @@ struct RayOpts {
     int64_t bound = -1;       // listed rays at most (-1: the source's edge count)
     int shard_index = 0;      // trace shard shard_index of shard_count of the rays
     int shard_count = 1;
-    // group rays: the list names groups of group_size soup triangles and
-    // masks[i] the segments of list entry i to trace (one walk per group)
-    const uint16_t* masks = nullptr;
-    int group_size = 0;
+    // rays from a soup: entries[t / entry_group] is the four-wide target
+    // node the walks of soup triangle t's edges start at (null: the root)
+    const int32_t* entries = nullptr;
+    int entry_group = 1;
 };
 
 constexpr int kScratchSlots = 40;

@@ -135,10 +135,11 @@ struct EdgeRayParams {
     // packed dataset edge
     const float4* ray_soup;
     int64_t ray_bound;  // ray indices of a listed launch lie below this
-    // group rays (FORM 3): list entry i is a group of group_size source soup
-    // triangles and ray_masks[i] the unique segments of its edges to trace
-    const uint16_t* ray_masks;
-    int group_size;
+    // entry nodes of rays from a soup: ray_entry[t / entry_group] is the
+    // four-wide target node every walk of soup triangle t's edges starts at
+    // (group_entry); null: the root
+    const int32_t* ray_entry;
+    int entry_group;
     // shard k of n: dataset-edge rays with edge index in [E k / n,
     // E (k + 1) / n) of the source's E edges (ray lists from triangles hold
     // only the shard's rays already: k_soup_rays)
@@ -331,6 +332,7 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
     if (node < 0) {
         if (leaf_count > 0) leaf(leaf_first, leaf_count);
     } else if (WIDE && P.tgt.nodes4) {
+        if (SOUP == 1 && P.ray_entry) node = __ldg(P.ray_entry + (uint32_t)(e >> 2) / (uint32_t)P.entry_group);
         // four-wide walk: a Node4 visit tests the four grandchildren of a
         // binary node, enters the first internal hit and pushes the others.
         // Reached leaves are queued (8 per thread) and tested when the queue
@@ -424,161 +426,6 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
                 node = sp < depth ? sstack[sp * 128 + tid] : lstack[sp - depth];
             }
         }
-    }
-    if (MODE == MODE_COUNT) P.counts[slot] = nhit;
-    rc.hits += (uint32_t)nhit;
-}
-
-// Group rays: the unique segments of one group of source soup triangles
-// (mask bit 3 t + k: edge k, as in load_ray, of triangle first + t) walk the
-// target's four-wide hierarchy once, with the box of those segments, instead
-// of once per segment; at a reached leaf every target triangle whose box
-// meets the group's box is tested against each segment whose box meets it.
-// The exact tests are those of the segments' own walks; the walk is shared.
-// The group's vertices sit in shared memory, column tid of sv (3 * GMAX rows
-// of blockDim.x float4).  A group of one source object skips, as a single
-// ray does, the triangles of the target object it hit last; hits of a group
-// that spans objects are all emitted.  Groups never span partitions.
-template <int MODE, int PREC, int GMAX>
-__device__ __forceinline__ void trace_group(const EdgeRayParams& P, int64_t g, uint32_t mask, int64_t slot,
-                                            float4* sv, int* sstack, int* lstack, RayCounters& rc, PredCounters& pc,
-                                            int depth) {
-    const int tid = threadIdx.x;
-    const int B = blockDim.x;
-    const int64_t first = g * P.group_size;
-    const int nt = (int)min((int64_t)P.group_size, P.src.num_tris - first);
-#pragma unroll
-    for (int i = 0; i < 3 * GMAX; ++i)
-        if (i < 3 * nt) sv[i * B + tid] = __ldg(P.ray_soup + 3 * first + i);
-    const int32_t obj0 = __float_as_int(sv[tid].w);
-    bool one_obj = true;
-    for (int t = 1; t < nt; ++t) one_obj = one_obj && __float_as_int(sv[3 * t * B + tid].w) == obj0;
-    float3 lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-    for (uint32_t m = mask; m; m &= m - 1) {
-        const int e = __ffs(m) - 1, t = e / 3, k = e % 3;
-        const float4 a = sv[(3 * t + k) * B + tid], b = sv[(3 * t + (k == 2 ? 0 : k + 1)) * B + tid];
-        lo.x = fminf(lo.x, fminf(a.x, b.x)); lo.y = fminf(lo.y, fminf(a.y, b.y)); lo.z = fminf(lo.z, fminf(a.z, b.z));
-        hi.x = fmaxf(hi.x, fmaxf(a.x, b.x)); hi.y = fmaxf(hi.y, fmaxf(a.y, b.y)); hi.z = fmaxf(hi.z, fmaxf(a.z, b.z));
-    }
-    int64_t out = (MODE == MODE_WRITE) ? P.offsets[slot] : 0;
-    int32_t last_obj = -1;
-    int nhit = 0;
-    auto leaf = [&](int lfirst, int count) {
-        for (int j = 0; j < count; ++j) {
-            const int64_t t = (int64_t)lfirst + j;
-            const float4 a4 = __ldg(P.tgt.soup + 3 * t);
-            const int32_t obj = __float_as_int(a4.w);
-            if (one_obj && obj == last_obj) continue;
-            const float4 b4 = __ldg(P.tgt.soup + 3 * t + 1);
-            const float4 c4 = __ldg(P.tgt.soup + 3 * t + 2);
-            const float tlx = fminf(a4.x, fminf(b4.x, c4.x)), thx = fmaxf(a4.x, fmaxf(b4.x, c4.x));
-            const float tly = fminf(a4.y, fminf(b4.y, c4.y)), thy = fmaxf(a4.y, fmaxf(b4.y, c4.y));
-            const float tlz = fminf(a4.z, fminf(b4.z, c4.z)), thz = fmaxf(a4.z, fmaxf(b4.z, c4.z));
-            if (!box_overlap(tlx, thx, tly, thy, tlz, thz, lo, hi)) continue;
-            const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
-                         c = make_float3(c4.x, c4.y, c4.z);
-            for (uint32_t m = mask; m; m &= m - 1) {
-                const int e = __ffs(m) - 1, st = e / 3, k = e % 3;
-                const float4 p4 = sv[(3 * st + k) * B + tid], q4 = sv[(3 * st + (k == 2 ? 0 : k + 1)) * B + tid];
-                const float3 p = make_float3(p4.x, p4.y, p4.z), q = make_float3(q4.x, q4.y, q4.z);
-                if (!box_overlap(tlx, thx, tly, thy, tlz, thz, make_float3(fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z)),
-                                 make_float3(fmaxf(p.x, q.x), fmaxf(p.y, q.y), fmaxf(p.z, q.z))))
-                    continue;
-                ++rc.tests;
-                bool hit;
-                if (PREC == PREC_EXACT) {
-                    hit = seg_tri_exact(p, q, a, b, c, pc);
-                } else if (PREC == PREC_FP32) {
-                    hit = seg_tri_mt_fp32(p, q, a, b, c);
-                } else {
-                    const int cls = seg_tri_fp32_class(p, q, a, b, c);
-                    if (cls == SEG_AMBIGUOUS) {
-                        ++pc.fp32_ambiguous;
-                        if (MODE != MODE_WRITE) {
-                            const uint64_t ray = ((uint64_t)(first + st) << 2) | (uint64_t)k;
-                            const unsigned long long q_slot = atomicAdd(P.amb_count, 1ull);
-                            if (q_slot < P.amb_cap) P.amb_queue[q_slot] = (ray << 32) | (uint32_t)t;
-                            else atomicOr(P.err, ERR_AMBIGUOUS_OVERFLOW);
-                        }
-                        continue;
-                    }
-                    hit = cls == SEG_HIT;
-                }
-                if (!hit) continue;
-                ++nhit;
-                const int32_t src_obj = __float_as_int(sv[3 * st * B + tid].w);
-                if (MODE != MODE_COUNT) {
-                    const uint64_t key = P.swap ? pack_key(obj, src_obj) : pack_key(src_obj, obj);
-                    if (MODE == MODE_WRITE) {
-                        P.keys[out++] = key;
-                    } else {
-                        ++rc.inserts;
-                        hash_insert(P.table, P.mask, key, P.err, rc.probes);
-                    }
-                }
-                if (one_obj) {
-                    last_obj = obj;
-                    break;  // the pair is found: the other segments add nothing for this triangle
-                }
-            }
-        }
-    };
-    int leaf_first, leaf_count;
-    int node = traversal_start(P.src, P.tgt, obj0, leaf_first, leaf_count);
-    if (node < 0) {
-        if (leaf_count > 0) leaf(leaf_first, leaf_count);
-    } else {
-        constexpr int kPend = 8;
-        uint64_t pend[kPend];
-        int np = 0;
-        auto flush = [&]() {
-            for (int k = 0; k < np; ++k) leaf((int)(pend[k] >> 8), (int)(pend[k] & 0xFF));
-            np = 0;
-        };
-        int sp = 0;
-        for (;;) {
-            ++rc.nodes;
-            const Node4* nd = P.tgt.nodes4 + node;
-            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
-            const int4 ch = __ldg(&nd->ch);
-            const int cnt = __ldg(&nd->meta.x);
-            const bool h[4] = {box_overlap(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, lo, hi),
-                               box_overlap(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, lo, hi),
-                               box_overlap(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, lo, hi),
-                               box_overlap(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, lo, hi)};
-            const int c[4] = {ch.x, ch.y, ch.z, ch.w};
-            int next = -1;
-            bool overflow = false;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (!h[j]) continue;
-                if (c[j] < 0) {
-                    if (np == kPend) flush();
-                    pend[np++] = ((uint64_t)(uint32_t)(~c[j]) << 8) | (uint64_t)((cnt >> (8 * j)) & 0xFF);
-                } else if (next < 0) {
-                    next = c[j];
-                } else if (sp >= kStackSize4) {
-                    overflow = true;
-                } else {
-                    if (sp < depth) sstack[sp * 128 + tid] = c[j];
-                    else lstack[sp - depth] = c[j];
-                    ++sp;
-                }
-            }
-            if (overflow) {
-                atomicOr(P.err, ERR_STACK_OVERFLOW);
-                break;
-            }
-            if (next >= 0) {
-                node = next;
-            } else {
-                if (sp == 0) break;
-                --sp;
-                node = sp < depth ? sstack[sp * 128 + tid] : lstack[sp - depth];
-            }
-        }
-        flush();
     }
     if (MODE == MODE_COUNT) P.counts[slot] = nhit;
     rc.hits += (uint32_t)nhit;
@@ -683,38 +530,16 @@ __device__ __forceinline__ void trace_packet(const EdgeRayParams& P, int64_t e, 
 // own kernel, so none carries the registers of another's code.
 // SOUP (listed forms): 1 rays from the source side's per-join soup, 0 the
 // dataset's edges, each its own instantiation (no registers for the other).
-// Group rays (FORM 3) keep 6 blocks per SM resident (80 registers, no
-// spills; 7 blocks would spill).
+// The one-ray-per-thread walk over a list (FORM 1) with the FP32 filter
+// keeps 8 blocks of 128 per SM resident (64 registers).
 template <int MODE, int PREC, int FORM, int SOUP>
-__global__ void __launch_bounds__(128, FORM == 3 ? 6 : 1) k_edge_rays(EdgeRayParams P) {
+__global__ void __launch_bounds__(128, (FORM == 1 && PREC != PREC_EXACT) ? 8 : 1) k_edge_rays(EdgeRayParams P) {
     extern __shared__ int sstack[];  // short_stack x 128 entries (then per-form data)
     int lstack[FORM ? kStackSize4 : kStackSize];
     RayCounters rc;
     PredCounters pc{0, 0};
     uint32_t rays = 0;
-    if constexpr (FORM == 3) {
-        // group rays: the list holds groups, each with the mask of its
-        // segments (rays split across processes were split when listed)
-        const unsigned long long n = *P.ray_count;
-        const int lane = threadIdx.x & 31;
-        const unsigned long long per = (unsigned long long)P.rays_per_fetch;
-        float4* sv = reinterpret_cast<float4*>(sstack + P.short_stack * 128);
-        for (;;) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(P.ray_cursor, per);
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (base >= n) break;
-            for (unsigned long long r = lane; r < per; r += 32) {
-                const unsigned long long i = base + r;
-                if (i < n) {
-                    const uint32_t mask = __ldg(P.ray_masks + i);
-                    trace_group<MODE, PREC, 4>(P, (int64_t)P.ray_list[i], mask, (int64_t)i, sv, sstack, lstack, rc,
-                                               pc, P.short_stack);
-                    rays += (uint32_t)__popc(mask);
-                }
-            }
-        }
-    } else if (FORM) {
+    if (FORM) {
         // Compacted ray list, persistent blocks: each warp takes the next
         // rays_per_fetch rays from a global cursor (the work queue), so uneven
         // ray costs balance out.
@@ -1286,20 +1111,17 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     P.ray_bound = n_rays;
     P.shard_count = (ro && ro->shard_count > 1) ? ro->shard_count : 1;
     P.shard_index = (ro && ro->shard_count > 1) ? ro->shard_index : 0;
-    const bool groups = ro && ro->list && ro->soup && ro->masks && tgt.nodes4 && !P.packets;
-    P.ray_masks = groups ? ro->masks : nullptr;
-    P.group_size = groups ? ro->group_size : 0;
-    if (groups && (ro->group_size < 1 || ro->group_size > 4))
-        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "group rays: group size must be 1..4");
-    if (ro && ro->masks && !groups)
-        return set_error(PIERCE_ERR_INVALID_ARGUMENT, "group rays need a listed soup and a four-wide target");
+    // entry nodes hold for the unpartitioned four-wide hierarchy they were found in
+    const bool entries = ro && ro->list && ro->soup && ro->entries && tgt.nodes4 && !tgt.part_roots &&
+                         !tgt.root_is_leaf && !P.packets;
+    P.ray_entry = entries ? ro->entries : nullptr;
+    P.entry_group = entries ? std::max(ro->entry_group, 1) : 1;
     if (P.rays_per_fetch % 32 != 0 || P.rays_per_fetch > 1024)
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "rays per warp must be a multiple of 32, at most 1024");
     if (precision == PREC_DEFER && !P.amb_queue) precision = PREC_EXACT;
     const int B = 128;
     // per-thread short stacks, then (packets) one (node, mask) stack per warp
-    const size_t smem = sizeof(int) * 128 * (size_t)P.short_stack + (P.packets ? sizeof(int2) * 4 * kStackSize : 0) +
-                        (groups ? sizeof(float4) * 128 * 3 * 4 : 0);
+    const size_t smem = sizeof(int) * 128 * (size_t)P.short_stack + (P.packets ? sizeof(int2) * 4 * kStackSize : 0);
     dim3 g;
     if (P.ray_list) {
         cudaMemsetAsync(P.ray_cursor, 0, sizeof(unsigned long long), ctx->stream);
@@ -1313,8 +1135,7 @@ int launch_edge_rays(pierce_ctx* ctx, const DevDataset& src, const DevDataset& t
     cudaStream_t st = ctx->stream;
 #define PG_LAUNCH(M, PR)                                    \
     do {                                                    \
-        if (groups) k_edge_rays<M, PR, 3, 1><<<g, B, smem, st>>>(P);                                \
-        else if (P.ray_list && P.packets && P.ray_soup) k_edge_rays<M, PR, 2, 1><<<g, B, smem, st>>>(P); \
+        if (P.ray_list && P.packets && P.ray_soup) k_edge_rays<M, PR, 2, 1><<<g, B, smem, st>>>(P); \
         else if (P.ray_list && P.packets) k_edge_rays<M, PR, 2, 0><<<g, B, smem, st>>>(P);         \
         else if (P.ray_list && P.ray_soup) k_edge_rays<M, PR, 1, 1><<<g, B, smem, st>>>(P);        \
         else if (P.ray_list) k_edge_rays<M, PR, 1, 0><<<g, B, smem, st>>>(P);                      \
@@ -1559,6 +1380,38 @@ __device__ __forceinline__ uint32_t group_unique_edges(const float4* __restrict_
     return mask;
 }
 
+// Entry node of a group's walks in the four-wide hierarchy `tgt` (not
+// partitioned, root not a leaf): from the root, descend while exactly one
+// child box meets the group's box [lo, hi] and that child is internal.
+// Every leaf whose box meets the group's box lies under the node returned,
+// so a walk of any segment inside that box that starts there reaches the
+// same leaves, in the same order, as one that starts at the root.
+__device__ __forceinline__ int32_t group_entry(const Node4* __restrict__ nodes4, const float3& lo, const float3& hi) {
+    if (!(lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z)) return 0;  // NaN coordinates: the root
+    int32_t node = 0;
+    for (int depth = 0; depth < 64; ++depth) {
+        const Node4* nd = nodes4 + node;
+        const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+        const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+        const int4 ch = __ldg(&nd->ch);
+        const bool h[4] = {box_overlap(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, lo, hi),
+                           box_overlap(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, lo, hi),
+                           box_overlap(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, lo, hi),
+                           box_overlap(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, lo, hi)};
+        const int c[4] = {ch.x, ch.y, ch.z, ch.w};
+        int hits = 0, only = -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (h[j]) {
+                ++hits;
+                only = c[j];
+            }
+        if (hits != 1 || only < 0) return node;
+        node = only;
+    }
+    return node;
+}
+
 // One thread per group; whole blocks step through the groups together so
 // that a warp reserves its list range with one atomicAdd.  GMAX: the group
 // size the kernel keeps in registers (G <= GMAX); larger groups take the
@@ -1568,10 +1421,9 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
                                                    DevDataset filter, int use_filter,
                                                    const int32_t* __restrict__ obj_part, uint32_t* __restrict__ list,
                                                    unsigned long long* __restrict__ count, int shard_index,
-                                                   int shard_count, uint16_t* __restrict__ masks) {
+                                                   int shard_count, const Node4* __restrict__ entry_nodes4,
+                                                   int32_t* __restrict__ entries) {
     const int64_t n_groups = (n_tris + G - 1) / G;
-    // masks (GMAX > 0 only): list the groups instead of their segments, with
-    // the mask of the segments to trace
     // a split join lists only the segments of its shard (seg_shard)
     auto mine = [&](const float4& p, const float4& q) {
         return shard_count <= 1 || seg_shard(p, q, shard_count) == shard_index;
@@ -1609,10 +1461,12 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
             }
             keep = !one_part || group_meets(filter, obj_part, obj0, lo, hi);
         }
+        // the walks of a listed group's segments start at its entry node
+        if (keep && entries) entries[g] = group_entry(entry_nodes4, lo, hi);
         int n = 0;
         if (keep) {
             if constexpr (GMAX > 0) {
-                n = masks ? (mask ? 1 : 0) : __popc(mask);
+                n = __popc(mask);
             } else {
                 for (int64_t t = first; t < last; ++t)
                     for (int k = 0; k < 3; ++k) {
@@ -1633,10 +1487,6 @@ __global__ void __launch_bounds__(256) k_soup_rays(const float4* __restrict__ so
         unsigned long long pos = wbase + (unsigned long long)(incl - n);
         if (n) {
             if constexpr (GMAX > 0) {
-                if (masks) {
-                    list[pos] = (uint32_t)g;
-                    masks[pos] = (uint16_t)mask;
-                } else
                 for (uint32_t m = mask; m; m &= m - 1) {
                     const int e = __ffs(m) - 1;
                     list[pos++] = (uint32_t)(((first + e / 3) << 2) | (e % 3));
@@ -1710,8 +1560,8 @@ int launch_group_incidences(pierce_ctx* ctx, const float4* soup, int64_t n_tris,
 
 int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G, const DevDataset* filter,
                      const int32_t* obj_part, uint32_t* list, unsigned long long* count, int shard_index,
-                     int shard_count, uint16_t* masks) {
-    if (masks && G > 4) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "group rays: group size must be 1..4");
+                     int shard_count, const Node4* entry_nodes4, int32_t* entries) {
+    if (!entry_nodes4) entries = nullptr;
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream);
     if (n_tris <= 0) return check_cuda(cudaGetLastError(), "rays from triangles");
     if (n_tris >= (int64_t(1) << 30))
@@ -1722,16 +1572,16 @@ int launch_soup_rays(pierce_ctx* ctx, const float4* soup, int64_t n_tris, int G,
     const DevDataset f = filter ? *filter : DevDataset{};
     if (G <= 1)
         k_soup_rays<1><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
-                                                             shard_index, shard_count, masks);
+                                                             shard_index, shard_count, entry_nodes4, entries);
     else if (G <= 2)
         k_soup_rays<2><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
-                                                             shard_index, shard_count, masks);
+                                                             shard_index, shard_count, entry_nodes4, entries);
     else if (G <= 4)
         k_soup_rays<4><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
-                                                             shard_index, shard_count, masks);
+                                                             shard_index, shard_count, entry_nodes4, entries);
     else
         k_soup_rays<0><<<grid, 256, 0, ctx->stream>>>(soup, n_tris, G, f, filter ? 1 : 0, obj_part, list, count,
-                                                             shard_index, shard_count, nullptr);
+                                                             shard_index, shard_count, entry_nodes4, entries);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "rays from triangles");
 }

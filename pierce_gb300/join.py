@@ -244,7 +244,7 @@ def make_opts(predicate="overlap", direction="both", sizing="hash", precision="e
     o.active_bvh = 1 if active_bvh else 0
     o.sizing_model = sizing_model.handle if sizing_model is not None else None
     o.leaf_size, o.rays_per_warp, o.stack_depth = int(leaf_size), int(rays_per_warp), int(stack_depth)
-    o.traversal = ({"per_ray": 0, "packets": 1, "per_ray_binary": 2, "groups": 3}[traversal] if isinstance(traversal, str)
+    o.traversal = ({"per_ray": 0, "packets": 1, "per_ray_binary": 2}[traversal] if isinstance(traversal, str)
                    else int(traversal))
     o.edge_source = ({"auto": 0, "dataset": 1, "triangles": 2}[edge_source] if isinstance(edge_source, str)
                      else int(edge_source))

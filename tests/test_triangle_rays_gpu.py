@@ -78,7 +78,7 @@ def test_triangle_rays_without_chunk_culling(ctx, case):
 def test_triangle_rays_traversal_forms(ctx, case):
     name, A, B = case
     want, _ = O.overlap_keys(A, B)
-    for form in ("per_ray", "packets", "per_ray_binary", "groups"):
+    for form in ("per_ray", "packets", "per_ray_binary"):
         got = J.overlap_join(ctx, edgeless(ctx, A), edgeless(ctx, B), traversal=form)
         assert np.array_equal(J.pairs_to_keys(got.pairs), want), (name, form)
 
