@@ -929,7 +929,9 @@ def main_ellipsoids(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_step,
                               "partial": "only the tuned device-resident joins", "config": cfg,
-                              "intersection_ms": ri.stats["ms_total"], "containment": containment_phases,
+                              "intersection": {"total": ri.stats["ms_total"], "builds": ri.stats["ms_build"],
+                                               "edge_rays": sum(ri.stats["ms_edge_rays"])},
+                              "containment": containment_phases,
                               "gpu_launches": int(launches)}))
         return 0
 

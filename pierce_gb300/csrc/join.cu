@@ -310,6 +310,19 @@ __device__ __forceinline__ void leaf_tests(const EdgeRayParams& P, int64_t e, in
     }
 }
 
+// Prefetch of what a four-wide walk reads later: the triangles of a leaf
+// it queues (tested when the queue is flushed) and the nodes it pushes
+// (visited when popped), so that their loads overlap the walk instead of
+// waiting behind it.  0: none, 1: into L1, 2: into L2.
+constexpr int kPrefetchLeaves = 1;
+constexpr int kPrefetchNodes = 1;
+
+template <int LEVEL>
+__device__ __forceinline__ void prefetch_line(const void* p) {
+    if constexpr (LEVEL == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    else if constexpr (LEVEL == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Ray e; `slot` indexes the per-ray counts and offsets of the two-pass
 // method (the ray's position in the launch's ray list, or e without one).
 template <int MODE, int PREC, bool WIDE = true, int SOUP = -1>
@@ -366,12 +379,18 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
                 if (!h[j]) continue;
                 if (c[j] < 0) {
                     if (np == kPend) flush();
-                    pend[np++] = ((uint64_t)(uint32_t)(~c[j]) << 8) | (uint64_t)((cnt >> (8 * j)) & 0xFF);
+                    const int lf = ~c[j], lc = (cnt >> (8 * j)) & 0xFF;
+                    if (kPrefetchLeaves != 0 && lc > 0) {  // the lines the leaf's tests read
+                        prefetch_line<kPrefetchLeaves>(P.tgt.soup + 3 * (int64_t)lf);
+                        prefetch_line<kPrefetchLeaves>(P.tgt.soup + 3 * ((int64_t)lf + lc) - 1);
+                    }
+                    pend[np++] = ((uint64_t)(uint32_t)lf << 8) | (uint64_t)lc;
                 } else if (next < 0) {
                     next = c[j];
                 } else if (sp >= kStackSize4) {
                     overflow = true;
                 } else {
+                    if constexpr (kPrefetchNodes != 0) prefetch_line<kPrefetchNodes>(P.tgt.nodes4 + c[j]);
                     if (sp < depth) sstack[sp * 128 + tid] = c[j];
                     else lstack[sp - depth] = c[j];
                     ++sp;
