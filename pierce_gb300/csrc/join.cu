@@ -310,19 +310,6 @@ __device__ __forceinline__ void leaf_tests(const EdgeRayParams& P, int64_t e, in
     }
 }
 
-// Prefetch of what a four-wide walk reads later: the triangles of a leaf
-// it queues (tested when the queue is flushed) and the nodes it pushes
-// (visited when popped), so that their loads overlap the walk instead of
-// waiting behind it.  0: none, 1: into L1, 2: into L2.
-constexpr int kPrefetchLeaves = 1;
-constexpr int kPrefetchNodes = 1;
-
-template <int LEVEL>
-__device__ __forceinline__ void prefetch_line(const void* p) {
-    if constexpr (LEVEL == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-    else if constexpr (LEVEL == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 // Ray e; `slot` indexes the per-ray counts and offsets of the two-pass
 // method (the ray's position in the launch's ray list, or e without one).
 template <int MODE, int PREC, bool WIDE = true, int SOUP = -1>
@@ -379,18 +366,12 @@ __device__ __forceinline__ void trace_edge(const EdgeRayParams& P, int64_t e, in
                 if (!h[j]) continue;
                 if (c[j] < 0) {
                     if (np == kPend) flush();
-                    const int lf = ~c[j], lc = (cnt >> (8 * j)) & 0xFF;
-                    if (kPrefetchLeaves != 0 && lc > 0) {  // the lines the leaf's tests read
-                        prefetch_line<kPrefetchLeaves>(P.tgt.soup + 3 * (int64_t)lf);
-                        prefetch_line<kPrefetchLeaves>(P.tgt.soup + 3 * ((int64_t)lf + lc) - 1);
-                    }
-                    pend[np++] = ((uint64_t)(uint32_t)lf << 8) | (uint64_t)lc;
+                    pend[np++] = ((uint64_t)(uint32_t)(~c[j]) << 8) | (uint64_t)((cnt >> (8 * j)) & 0xFF);
                 } else if (next < 0) {
                     next = c[j];
                 } else if (sp >= kStackSize4) {
                     overflow = true;
                 } else {
-                    if constexpr (kPrefetchNodes != 0) prefetch_line<kPrefetchNodes>(P.tgt.nodes4 + c[j]);
                     if (sp < depth) sstack[sp * 128 + tid] = c[j];
                     else lstack[sp - depth] = c[j];
                     ++sp;
@@ -916,15 +897,18 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // ---- containment by candidate pairs -------------------------------------------
 // Containment is parity(B in A) \ overlap (pierce_containment_main.cpp:
 // 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
-// warp takes one such pair: the triangles of a, then of b, whose boxes meet
-// the intersection of the two object boxes are listed in shared memory, and
-// every listed pair of triangles whose boxes meet is tested with the exact
-// closed triangle-triangle predicate (an edge of one meets the other: six
-// segment tests, the edge definition for the edges of triangles).  The pair
-// is a containment pair when none meets.  A pair whose objects hold more than
-// kPairScanMax triangles together, or whose lists outgrow kPairList, is
+// warp takes one such pair: the triangles of a whose boxes meet the
+// intersection of the two object boxes are listed in shared memory (a patch
+// of a's surface), the box shrinks to that patch's box, and b's triangles
+// stream past in runs of 32 (one per lane), each tested against the listed
+// triangles whose boxes meet its own with the exact closed
+// triangle-triangle predicate (an edge of one meets the other: six segment
+// tests, the edge definition for the edges of triangles).  The pair is a
+// containment pair when none meets; a b deep inside a lists nothing and
+// costs one pass over a's triangles.  A pair whose objects hold more than
+// kPairScanMax triangles together, or whose patch outgrows kPairList, is
 // counted in *fallback and the join takes the culling pipeline instead.
-constexpr int kPairList = 384;
+constexpr int kPairList = 1024;
 constexpr int kPairScanMax = 1 << 16;
 constexpr int kPairWarps = 4;
 
@@ -974,7 +958,7 @@ __device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const fl
 }
 
 __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
-    __shared__ uint32_t s_list[kPairWarps][2][kPairList];
+    __shared__ uint32_t s_list[kPairWarps][kPairList];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     PredCounters pc{0, 0};
     uint32_t tests = 0;
@@ -985,46 +969,66 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
         const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
         const float* ba = P.a.obj_box + 6 * (size_t)a;
         const float* bb = P.b.obj_box + 6 * (size_t)b;
-        const float3 lo = make_float3(fmaxf(__ldg(ba), __ldg(bb)), fmaxf(__ldg(ba + 1), __ldg(bb + 1)),
-                                      fmaxf(__ldg(ba + 2), __ldg(bb + 2)));
-        const float3 hi = make_float3(fminf(__ldg(ba + 3), __ldg(bb + 3)), fminf(__ldg(ba + 4), __ldg(bb + 4)),
-                                      fminf(__ldg(ba + 5), __ldg(bb + 5)));
+        float3 lo = make_float3(fmaxf(__ldg(ba), __ldg(bb)), fmaxf(__ldg(ba + 1), __ldg(bb + 1)),
+                                fmaxf(__ldg(ba + 2), __ldg(bb + 2)));
+        float3 hi = make_float3(fminf(__ldg(ba + 3), __ldg(bb + 3)), fminf(__ldg(ba + 4), __ldg(bb + 4)),
+                                fminf(__ldg(ba + 5), __ldg(bb + 5)));
         bool meets = false, undecided = false;
         if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
             const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
             if ((int64_t)ra.y + rb.y > kPairScanMax) {
                 undecided = true;
             } else {
-                const int na = list_near(P.a, ra, lo, hi, s_list[w][0], lane);
-                const int nb = na > 0 ? list_near(P.b, rb, lo, hi, s_list[w][1], lane) : 0;
-                if (na < 0 || nb < 0) {
+                const int na = list_near(P.a, ra, lo, hi, s_list[w], lane);
+                if (na < 0) {
                     undecided = true;
-                } else {
-                    const int total = na * nb;
-                    for (int base = 0; base < total; base += 32) {
+                } else if (na > 0) {
+                    // the patch's box, within the objects' common box
+                    float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+                    for (int k = lane; k < na; k += 32) {
+                        const uint32_t t = s_list[w][k];
+                        for (int v = 0; v < 3; ++v) {
+                            const float3 x = tri_vertex(P.a, t, v);
+                            plo.x = fminf(plo.x, x.x); plo.y = fminf(plo.y, x.y); plo.z = fminf(plo.z, x.z);
+                            phi.x = fmaxf(phi.x, x.x); phi.y = fmaxf(phi.y, x.y); phi.z = fmaxf(phi.z, x.z);
+                        }
+                    }
+                    for (int off = 16; off; off >>= 1) {
+                        plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
+                        plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
+                        plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
+                        phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
+                        phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
+                        phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
+                    }
+                    lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
+                    hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
+                    // b's triangles, one per lane, against the patch
+                    for (int base = 0; base < rb.y && !meets; base += 32) {
                         const int k = base + lane;
                         bool hit = false;
-                        if (k < total) {
-                            const uint32_t ta = s_list[w][0][k / nb], tb = s_list[w][1][k % nb];
-                            const float3 a0 = tri_vertex(P.a, ta, 0), a1 = tri_vertex(P.a, ta, 1),
-                                         a2 = tri_vertex(P.a, ta, 2);
+                        if (k < rb.y) {
+                            const uint32_t tb = (uint32_t)(rb.x + k);
                             const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
                                          b2 = tri_vertex(P.b, tb, 2);
                             const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
                                                            fminf(b0.z, fminf(b1.z, b2.z)));
                             const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
                                                            fmaxf(b0.z, fmaxf(b1.z, b2.z)));
-                            if (tri_box_meets(a0, a1, a2, blo, bhi)) {
-                                ++tests;
-                                hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
-                                      seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
-                                      seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                            if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
+                                for (int j = 0; j < na && !hit; ++j) {
+                                    const uint32_t ta = s_list[w][j];
+                                    const float3 a0 = tri_vertex(P.a, ta, 0), a1 = tri_vertex(P.a, ta, 1),
+                                                 a2 = tri_vertex(P.a, ta, 2);
+                                    if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
+                                    ++tests;
+                                    hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
+                                          seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
+                                          seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                                }
                             }
                         }
-                        if (__any_sync(0xFFFFFFFFu, hit)) {
-                            meets = true;
-                            break;
-                        }
+                        meets = __any_sync(0xFFFFFFFFu, hit);
                     }
                 }
             }
