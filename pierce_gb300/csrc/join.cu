@@ -905,11 +905,14 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // triangle-triangle predicate (an edge of one meets the other: six segment
 // tests, the edge definition for the edges of triangles).  The pair is a
 // containment pair when none meets; a b deep inside a lists nothing and
-// costs one pass over a's triangles.  A pair whose objects hold more than
-// kPairScanMax triangles together, or whose patch outgrows kPairList, is
-// counted in *fallback and the join takes the culling pipeline instead.
+// costs one pass over a's triangles.  A patch larger than kPairList is read
+// from a's range in place.  A pair whose objects hold more than
+// kPairScanMax triangles together, or whose unlisted patch would cost more
+// than kPairStreamMax triangle pairs, is counted in *fallback and the join
+// takes the culling pipeline instead.
 constexpr int kPairList = 1024;
 constexpr int kPairScanMax = 1 << 16;
+constexpr int64_t kPairStreamMax = 1 << 22;  // triangle pairs a warp scans for a patch past kPairList
 constexpr int kPairWarps = 4;
 
 struct PairParams {
@@ -937,24 +940,43 @@ __device__ __forceinline__ bool tri_box_meets(const float3& p, const float3& q, 
 }
 
 // The warp lists the triangles of range r (first, count) of d whose box
-// meets [lo, hi]; returns their number, or -1 when they exceed kPairList.
-__device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const float3& hi, uint32_t* list, int lane) {
+// meets [lo, hi] (the first kPairList of them) and returns their number;
+// [plo, phi] receives the box of those triangles (on every lane).
+__device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const float3& hi, uint32_t* list, int lane,
+                         float3& plo, float3& phi) {
     int n = 0;
+    plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
+    phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
     for (int base = 0; base < r.y; base += 32) {
         const int k = base + lane;
         bool meet = false;
         uint32_t t = 0;
         if (k < r.y) {
             t = (uint32_t)(r.x + k);
-            meet = tri_box_meets(tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2), lo, hi);
+            const float3 v0 = tri_vertex(d, t, 0), v1 = tri_vertex(d, t, 1), v2 = tri_vertex(d, t, 2);
+            meet = tri_box_meets(v0, v1, v2, lo, hi);
+            if (meet) {
+                plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))), fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
+                                  fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
+                phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))), fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
+                                  fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
+            }
         }
         const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
         const int pos = n + __popc(m & ((1u << lane) - 1u));
         if (meet && pos < kPairList) list[pos] = t;
         n += __popc(m);
     }
+    for (int off = 16; off; off >>= 1) {
+        plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
+        plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
+        plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
+        phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
+        phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
+        phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
+    }
     __syncwarp();
-    return n > kPairList ? -1 : n;
+    return n;
 }
 
 __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
@@ -979,28 +1001,15 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
             if ((int64_t)ra.y + rb.y > kPairScanMax) {
                 undecided = true;
             } else {
-                const int na = list_near(P.a, ra, lo, hi, s_list[w], lane);
-                if (na < 0) {
+                float3 plo, phi;
+                const int na = list_near(P.a, ra, lo, hi, s_list[w], lane, plo, phi);
+                // a patch larger than the list is read from a's range directly
+                // (the same triangle on every lane: one load per warp)
+                const bool listed = na <= kPairList;
+                if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
                     undecided = true;
                 } else if (na > 0) {
                     // the patch's box, within the objects' common box
-                    float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-                    for (int k = lane; k < na; k += 32) {
-                        const uint32_t t = s_list[w][k];
-                        for (int v = 0; v < 3; ++v) {
-                            const float3 x = tri_vertex(P.a, t, v);
-                            plo.x = fminf(plo.x, x.x); plo.y = fminf(plo.y, x.y); plo.z = fminf(plo.z, x.z);
-                            phi.x = fmaxf(phi.x, x.x); phi.y = fmaxf(phi.y, x.y); phi.z = fmaxf(phi.z, x.z);
-                        }
-                    }
-                    for (int off = 16; off; off >>= 1) {
-                        plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
-                        plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
-                        plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
-                        phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
-                        phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
-                        phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
-                    }
                     lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
                     hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
                     // b's triangles, one per lane, against the patch
@@ -1016,8 +1025,9 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
                             const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
                                                            fmaxf(b0.z, fmaxf(b1.z, b2.z)));
                             if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
-                                for (int j = 0; j < na && !hit; ++j) {
-                                    const uint32_t ta = s_list[w][j];
+                                const int nj = listed ? na : ra.y;
+                                for (int j = 0; j < nj && !hit; ++j) {
+                                    const uint32_t ta = listed ? s_list[w][j] : (uint32_t)(ra.x + j);
                                     const float3 a0 = tri_vertex(P.a, ta, 0), a1 = tri_vertex(P.a, ta, 1),
                                                  a2 = tri_vertex(P.a, ta, 2);
                                     if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;

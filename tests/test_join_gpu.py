@@ -315,18 +315,25 @@ def test_nested_containers_enlarge_and_rerun(ctx):
 
 @pytest.mark.parametrize("sizing", ["hash", "two_pass"])
 def test_containment_pairs_and_their_fallback(ctx, sizing):
-    """Containment tests its odd-parity candidate pairs directly; a pair too
-    large for that (a 327,680-triangle container, or a container whose
-    triangles nearly all lie in the box of the object inside) sends the join
-    through the culling pipeline.  Both must give the oracle's pairs."""
+    """Containment tests its odd-parity candidate pairs directly.  A
+    container patch larger than the shared-memory list (5,120 triangles
+    around a 320-triangle sphere inside) is read in place; a pair too large
+    for either (a 327,680-triangle container, or a 5,120-triangle container
+    whose triangles nearly all lie in the box of a 5,120-triangle sphere
+    inside) sends the join through the culling pipeline.  All must give the
+    oracle's pairs."""
     small = pg.ellipsoid_pair(1, 2, 300, 300, 2, lo=0, hi=70, frac_contact=0.1)
     big = (pg.icospheres(51, 1, 7, ln_mu=float(np.log(20.0)), sigma=0.0, lo=0.0, hi=0.0),
            pg.icospheres(52, 30, 2, ln_mu=0.0, sigma=0.2, lo=-10.0, hi=10.0))
     tight = (pg.icospheres(53, 1, 4, ln_mu=float(np.log(10.0)), sigma=0.0, lo=0.0, hi=0.0),
              pg.icospheres(54, 1, 4, ln_mu=float(np.log(9.9)), sigma=0.0, lo=0.0, hi=0.0))
-    for name, (A, B) in (("pairs", small), ("large container", big), ("dense container", tight)):
+    patch = (pg.icospheres(55, 1, 4, ln_mu=float(np.log(10.0)), sigma=0.0, lo=0.0, hi=0.0),
+             pg.icospheres(56, 1, 2, ln_mu=float(np.log(9.9)), sigma=0.0, lo=0.0, hi=0.0))
+    by_pairs = {"pairs": 1, "large patch": 1, "large container": 0, "dense container": 0}
+    for name, (A, B) in (("pairs", small), ("large patch", patch), ("large container", big),
+                         ("dense container", tight)):
         want = O.containment_keys(A, B)
         got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
         assert np.array_equal(keys(got), want), name
-        assert got.stats["containment_by_pairs"] == (1 if name == "pairs" else 0), name
+        assert got.stats["containment_by_pairs"] == by_pairs[name], name
     assert len(O.containment_keys(*big)) > 5 and len(O.containment_keys(*tight)) == 1
