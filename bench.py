@@ -150,11 +150,11 @@ def edge_ray_bytes(src, tgt, raw_hits):
     return 28 * E + 16 * F + 12 * V + 32 * (2 * F - 1) + 8 * raw_hits
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced edge
-# of k_edge_rays, from one ncu capture of the edge-ray launches of this
-# build on a reduced case of the same workload (the traffic per traced edge
-# is then scaled by the traced edges of the full join).
-EDGE_RAY_DRAM_BYTES_PER_RAY = {"tubes": 45.72, "ellipsoids": 45.72}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced
+# segment of the two edge-ray launches of one join, from one full-size ncu
+# capture of this build (one pass per launch): the tube join's 3.876 GB over
+# 67,917,789 segments, the ellipsoid intersection join's launches likewise.
+EDGE_RAY_DRAM_BYTES_PER_RAY = {"tubes": 57.06, "ellipsoids": 45.72}
 
 
 def traffic_estimate(rays, workload="tubes"):
@@ -930,7 +930,7 @@ def main_ellipsoids(args):
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_step,
                               "partial": "only the tuned device-resident joins", "config": cfg,
                               "intersection": {"total": ri.stats["ms_total"], "builds": ri.stats["ms_build"],
-                                               "edge_rays": sum(ri.stats["ms_edge_rays"])},
+                                               "edge_rays": sum(ri.stats["ms_edge_rays"]), "rays": ri.stats["rays"]},
                               "containment": containment_phases,
                               "gpu_launches": int(launches)}))
         return 0

@@ -899,7 +899,8 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
 // warp takes one such pair: the triangles of a whose boxes meet the
 // intersection of the two object boxes are listed in shared memory (a patch
-// of a's surface), the box shrinks to that patch's box, and b's triangles
+// of a's surface; the vertices of up to kPairVerts of them are kept in
+// shared memory), the box shrinks to that patch's box, and b's triangles
 // stream past in runs of 32 (one per lane), each tested against the listed
 // triangles whose boxes meet its own with the exact closed
 // triangle-triangle predicate (an edge of one meets the other: six segment
@@ -910,7 +911,8 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // kPairScanMax triangles together, or whose unlisted patch would cost more
 // than kPairStreamMax triangle pairs, is counted in *fallback and the join
 // takes the culling pipeline instead.
-constexpr int kPairList = 1024;
+constexpr int kPairList = 768;
+constexpr int kPairVerts = 192;  // listed triangles whose vertices a warp keeps in shared memory
 constexpr int kPairScanMax = 1 << 16;
 constexpr int64_t kPairStreamMax = 1 << 22;  // triangle pairs a warp scans for a patch past kPairList
 constexpr int kPairWarps = 4;
@@ -981,6 +983,7 @@ __device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const fl
 
 __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
     __shared__ uint32_t s_list[kPairWarps][kPairList];
+    __shared__ float4 s_tri[kPairWarps][kPairVerts][3];  // 48 KB per block with the lists
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     PredCounters pc{0, 0};
     uint32_t tests = 0;
@@ -1006,6 +1009,19 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
                 // a patch larger than the list is read from a's range directly
                 // (the same triangle on every lane: one load per warp)
                 const bool listed = na <= kPairList;
+                // a small patch's vertices go to shared memory: the lanes
+                // then read each listed triangle together (one broadcast)
+                const bool cached = na <= kPairVerts;
+                if (cached) {
+                    for (int k = lane; k < na; k += 32) {
+                        const uint32_t t = s_list[w][k];
+                        for (int v = 0; v < 3; ++v) {
+                            const float3 x = tri_vertex(P.a, t, v);
+                            s_tri[w][k][v] = make_float4(x.x, x.y, x.z, 0.0f);
+                        }
+                    }
+                    __syncwarp();
+                }
                 if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
                     undecided = true;
                 } else if (na > 0) {
@@ -1027,9 +1043,18 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
                             if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
                                 const int nj = listed ? na : ra.y;
                                 for (int j = 0; j < nj && !hit; ++j) {
-                                    const uint32_t ta = listed ? s_list[w][j] : (uint32_t)(ra.x + j);
-                                    const float3 a0 = tri_vertex(P.a, ta, 0), a1 = tri_vertex(P.a, ta, 1),
-                                                 a2 = tri_vertex(P.a, ta, 2);
+                                    float3 a0, a1, a2;
+                                    if (cached) {
+                                        const float4 x0 = s_tri[w][j][0], x1 = s_tri[w][j][1], x2 = s_tri[w][j][2];
+                                        a0 = make_float3(x0.x, x0.y, x0.z);
+                                        a1 = make_float3(x1.x, x1.y, x1.z);
+                                        a2 = make_float3(x2.x, x2.y, x2.z);
+                                    } else {
+                                        const uint32_t ta = listed ? s_list[w][j] : (uint32_t)(ra.x + j);
+                                        a0 = tri_vertex(P.a, ta, 0);
+                                        a1 = tri_vertex(P.a, ta, 1);
+                                        a2 = tri_vertex(P.a, ta, 2);
+                                    }
                                     if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
                                     ++tests;
                                     hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
