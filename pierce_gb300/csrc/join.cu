@@ -897,24 +897,21 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // ---- containment by candidate pairs -------------------------------------------
 // Containment is parity(B in A) \ overlap (pierce_containment_main.cpp:
 // 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
-// warp takes one such pair: the triangles of a whose boxes meet the
-// intersection of the two object boxes are listed in shared memory (a patch
-// of a's surface; the vertices of up to kPairVerts of them are kept in
-// shared memory), the box shrinks to that patch's box, and b's triangles
-// stream past in runs of 32 (one per lane), each tested against the listed
-// triangles whose boxes meet its own with the exact closed
-// triangle-triangle predicate (an edge of one meets the other: six segment
-// tests, the edge definition for the edges of triangles).  The pair is a
-// containment pair when none meets; a b deep inside a lists nothing and
-// costs one pass over a's triangles.  A patch larger than kPairList is read
-// from a's range in place.  A pair whose objects hold more than
-// kPairScanMax triangles together, or whose unlisted patch would cost more
-// than kPairStreamMax triangle pairs, is counted in *fallback and the join
-// takes the culling pipeline instead.
-constexpr int kPairList = 768;
-constexpr int kPairVerts = 192;  // listed triangles whose vertices a warp keeps in shared memory
+// warp takes one such pair.  It lists the 32-triangle chunks of a (the
+// dataset's own chunks, clipped to a's range) whose boxes meet the
+// intersection of the two object boxes, with their boxes, in shared memory;
+// the box shrinks to the union of those chunks.  b's triangles then pass one
+// per lane (whole chunks of b that miss the box are skipped), each against
+// the listed chunks whose boxes meet its own and, in those, the triangles
+// whose boxes do, with the exact closed triangle-triangle predicate (an edge
+// of one meets the other: six segment tests, the edge definition for the
+// edges of triangles).  The pair is a containment pair when none meets; a b
+// deep inside a lists nothing and costs one pass over a's chunk boxes.  A
+// pair whose objects hold more than kPairScanMax triangles together, or
+// with more than kPairChunks listed chunks, is counted in *fallback and the
+// join takes the culling pipeline instead.
+constexpr int kPairChunks = 256;
 constexpr int kPairScanMax = 1 << 16;
-constexpr int64_t kPairStreamMax = 1 << 22;  // triangle pairs a warp scans for a patch past kPairList
 constexpr int kPairWarps = 4;
 
 struct PairParams {
@@ -941,49 +938,13 @@ __device__ __forceinline__ bool tri_box_meets(const float3& p, const float3& q, 
                        fmaxf(p.y, fmaxf(q.y, r.y)), fminf(p.z, fminf(q.z, r.z)), fmaxf(p.z, fmaxf(q.z, r.z)), lo, hi);
 }
 
-// The warp lists the triangles of range r (first, count) of d whose box
-// meets [lo, hi] (the first kPairList of them) and returns their number;
-// [plo, phi] receives the box of those triangles (on every lane).
-__device__ int list_near(const DevDataset& d, int2 r, const float3& lo, const float3& hi, uint32_t* list, int lane,
-                         float3& plo, float3& phi) {
-    int n = 0;
-    plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
-    phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-    for (int base = 0; base < r.y; base += 32) {
-        const int k = base + lane;
-        bool meet = false;
-        uint32_t t = 0;
-        if (k < r.y) {
-            t = (uint32_t)(r.x + k);
-            const float3 v0 = tri_vertex(d, t, 0), v1 = tri_vertex(d, t, 1), v2 = tri_vertex(d, t, 2);
-            meet = tri_box_meets(v0, v1, v2, lo, hi);
-            if (meet) {
-                plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))), fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
-                                  fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
-                phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))), fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
-                                  fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
-            }
-        }
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
-        const int pos = n + __popc(m & ((1u << lane) - 1u));
-        if (meet && pos < kPairList) list[pos] = t;
-        n += __popc(m);
-    }
-    for (int off = 16; off; off >>= 1) {
-        plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
-        plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
-        plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
-        phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
-        phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
-        phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
-    }
-    __syncwarp();
-    return n;
+__device__ __forceinline__ bool boxes_meet(const float* b, const float3& lo, const float3& hi) {
+    return box_overlap(b[0], b[3], b[1], b[4], b[2], b[5], lo, hi);
 }
 
 __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
-    __shared__ uint32_t s_list[kPairWarps][kPairList];
-    __shared__ float4 s_tri[kPairWarps][kPairVerts][3];  // 48 KB per block with the lists
+    __shared__ uint32_t s_chunk[kPairWarps][kPairChunks];
+    __shared__ float s_cbox[kPairWarps][kPairChunks][6];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     PredCounters pc{0, 0};
     uint32_t tests = 0;
@@ -1001,65 +962,82 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
         bool meets = false, undecided = false;
         if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
             const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
-            if ((int64_t)ra.y + rb.y > kPairScanMax) {
+            if ((int64_t)ra.y + rb.y > kPairScanMax || !P.a.tri_chunk_box || !P.b.tri_chunk_box) {
                 undecided = true;
             } else {
-                float3 plo, phi;
-                const int na = list_near(P.a, ra, lo, hi, s_list[w], lane, plo, phi);
-                // a patch larger than the list is read from a's range directly
-                // (the same triangle on every lane: one load per warp)
-                const bool listed = na <= kPairList;
-                // a small patch's vertices go to shared memory: the lanes
-                // then read each listed triangle together (one broadcast)
-                const bool cached = na <= kPairVerts;
-                if (cached) {
-                    for (int k = lane; k < na; k += 32) {
-                        const uint32_t t = s_list[w][k];
-                        for (int v = 0; v < 3; ++v) {
-                            const float3 x = tri_vertex(P.a, t, v);
-                            s_tri[w][k][v] = make_float4(x.x, x.y, x.z, 0.0f);
+                // a's chunks that meet the common box, with the union of their boxes
+                const int c0 = ra.x >> 5, c1 = (ra.x + ra.y - 1) >> 5;
+                int nc = 0;
+                float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+                for (int base = c0; base <= c1; base += 32) {
+                    const int c = base + lane;
+                    float cb[6];
+                    bool meet = false;
+                    if (c <= c1) {
+                        for (int k = 0; k < 6; ++k) cb[k] = __ldg(P.a.tri_chunk_box + 6 * (size_t)c + k);
+                        meet = boxes_meet(cb, lo, hi);
+                    }
+                    const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
+                    const int pos = nc + __popc(m & ((1u << lane) - 1u));
+                    if (meet) {
+                        plo = make_float3(fminf(plo.x, cb[0]), fminf(plo.y, cb[1]), fminf(plo.z, cb[2]));
+                        phi = make_float3(fmaxf(phi.x, cb[3]), fmaxf(phi.y, cb[4]), fmaxf(phi.z, cb[5]));
+                        if (pos < kPairChunks) {
+                            s_chunk[w][pos] = (uint32_t)c;
+                            for (int k = 0; k < 6; ++k) s_cbox[w][pos][k] = cb[k];
                         }
                     }
-                    __syncwarp();
+                    nc += __popc(m);
                 }
-                if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
+                for (int off = 16; off; off >>= 1) {
+                    plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
+                    plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
+                    plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
+                    phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
+                    phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
+                    phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
+                }
+                __syncwarp();
+                if (nc > kPairChunks) {
                     undecided = true;
-                } else if (na > 0) {
-                    // the patch's box, within the objects' common box
+                } else if (nc > 0) {
                     lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
                     hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
-                    // b's triangles, one per lane, against the patch
+                    const int a_end = ra.x + ra.y;
+                    // b's triangles, one per lane, against the listed chunks
                     for (int base = 0; base < rb.y && !meets; base += 32) {
                         const int k = base + lane;
                         bool hit = false;
                         if (k < rb.y) {
                             const uint32_t tb = (uint32_t)(rb.x + k);
-                            const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
-                                         b2 = tri_vertex(P.b, tb, 2);
-                            const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
-                                                           fminf(b0.z, fminf(b1.z, b2.z)));
-                            const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
-                                                           fmaxf(b0.z, fmaxf(b1.z, b2.z)));
-                            if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
-                                const int nj = listed ? na : ra.y;
-                                for (int j = 0; j < nj && !hit; ++j) {
-                                    float3 a0, a1, a2;
-                                    if (cached) {
-                                        const float4 x0 = s_tri[w][j][0], x1 = s_tri[w][j][1], x2 = s_tri[w][j][2];
-                                        a0 = make_float3(x0.x, x0.y, x0.z);
-                                        a1 = make_float3(x1.x, x1.y, x1.z);
-                                        a2 = make_float3(x2.x, x2.y, x2.z);
-                                    } else {
-                                        const uint32_t ta = listed ? s_list[w][j] : (uint32_t)(ra.x + j);
-                                        a0 = tri_vertex(P.a, ta, 0);
-                                        a1 = tri_vertex(P.a, ta, 1);
-                                        a2 = tri_vertex(P.a, ta, 2);
+                            float bcb[6];
+                            for (int q = 0; q < 6; ++q) bcb[q] = __ldg(P.b.tri_chunk_box + 6 * (size_t)(tb >> 5) + q);
+                            if (boxes_meet(bcb, lo, hi)) {
+                                const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
+                                             b2 = tri_vertex(P.b, tb, 2);
+                                const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
+                                                               fminf(b0.z, fminf(b1.z, b2.z)));
+                                const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
+                                                               fmaxf(b0.z, fmaxf(b1.z, b2.z)));
+                                if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
+                                    for (int j = 0; j < nc && !hit; ++j) {
+                                        if (!boxes_meet(s_cbox[w][j], blo, bhi)) continue;
+                                        const int c = (int)s_chunk[w][j];
+                                        const int t0 = max(c << 5, ra.x), t1 = min((c << 5) + 32, a_end);
+                                        for (int t = t0; t < t1 && !hit; ++t) {
+                                            const float3 a0 = tri_vertex(P.a, (uint32_t)t, 0),
+                                                         a1 = tri_vertex(P.a, (uint32_t)t, 1),
+                                                         a2 = tri_vertex(P.a, (uint32_t)t, 2);
+                                            if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
+                                            ++tests;
+                                            hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) ||
+                                                  seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
+                                                  seg_tri_exact(a2, a0, b0, b1, b2, pc) ||
+                                                  seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
+                                                  seg_tri_exact(b1, b2, a0, a1, a2, pc) ||
+                                                  seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                                        }
                                     }
-                                    if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
-                                    ++tests;
-                                    hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
-                                          seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
-                                          seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
                                 }
                             }
                         }
