@@ -897,22 +897,25 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // ---- containment by candidate pairs -------------------------------------------
 // Containment is parity(B in A) \ overlap (pierce_containment_main.cpp:
 // 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
-// warp takes one such pair.  It lists the 32-triangle chunks of a (the
-// dataset's own chunks, clipped to a's range) whose boxes meet the
-// intersection of the two object boxes, with their boxes, in shared memory;
-// the box shrinks to the union of those chunks.  b's triangles then pass one
-// per lane (whole chunks of b that miss the box are skipped), each against
-// the listed chunks whose boxes meet its own and, in those, the triangles
-// whose boxes do, with the exact closed triangle-triangle predicate (an edge
-// of one meets the other: six segment tests, the edge definition for the
-// edges of triangles).  The pair is a containment pair when none meets; a b
-// deep inside a lists nothing and costs one pass over a's chunk boxes.  A
-// pair whose objects hold more than kPairScanMax triangles together, or
-// with more than kPairChunks listed chunks, is counted in *fallback and the
-// join takes the culling pipeline instead.
-constexpr int kPairChunks = 256;
+// block of kPairThreads takes one such pair, so that one large pair does
+// not hold a lone warp for the whole launch: it lists the triangles of a
+// whose boxes meet the intersection of the two object boxes (a patch of a's
+// surface; the vertices of up to kPairVerts of them are kept in shared
+// memory), shrinks the box to that patch's box, and streams b's triangles
+// past them, one per thread, each tested against the listed triangles whose
+// boxes meet its own with the exact closed triangle-triangle predicate (an
+// edge of one meets the other: six segment tests, the edge definition for
+// the edges of triangles).  The pair is a containment pair when none meets;
+// a b deep inside a lists nothing and costs one pass over a's triangles.  A
+// patch larger than kPairList is read from a's range in place.  A pair whose
+// objects hold more than kPairScanMax triangles together, or whose unlisted
+// patch would cost more than kPairStreamMax triangle pairs, is counted in
+// *fallback and the join takes the culling pipeline instead.
+constexpr int kPairThreads = 256;
+constexpr int kPairList = 1024;
+constexpr int kPairVerts = 512;
 constexpr int kPairScanMax = 1 << 16;
-constexpr int kPairWarps = 4;
+constexpr int64_t kPairStreamMax = 1 << 22;
 
 struct PairParams {
     const uint64_t* ptable;
@@ -938,20 +941,28 @@ __device__ __forceinline__ bool tri_box_meets(const float3& p, const float3& q, 
                        fmaxf(p.y, fmaxf(q.y, r.y)), fminf(p.z, fminf(q.z, r.z)), fmaxf(p.z, fmaxf(q.z, r.z)), lo, hi);
 }
 
-__device__ __forceinline__ bool boxes_meet(const float* b, const float3& lo, const float3& hi) {
-    return box_overlap(b[0], b[3], b[1], b[4], b[2], b[5], lo, hi);
+__device__ __forceinline__ float block_min(float v, float* red) {
+    for (int off = 16; off; off >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float r = red[0];
+    for (int k = 1; k < kPairThreads / 32; ++k) r = fminf(r, red[k]);
+    __syncthreads();
+    return r;
 }
+__device__ __forceinline__ float block_max(float v, float* red) { return -block_min(-v, red); }
 
-__global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
-    __shared__ uint32_t s_chunk[kPairWarps][kPairChunks];
-    __shared__ float s_cbox[kPairWarps][kPairChunks][6];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(kPairThreads) k_containment_pairs(PairParams P) {
+    __shared__ uint32_t s_list[kPairList];
+    __shared__ float4 s_tri[kPairVerts][3];
+    __shared__ int s_warp[kPairThreads / 32];
+    __shared__ float s_red[kPairThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     PredCounters pc{0, 0};
     uint32_t tests = 0;
-    const int64_t warps = (int64_t)gridDim.x * kPairWarps;
-    for (int64_t i = blockIdx.x * (int64_t)kPairWarps + w; i < (int64_t)P.pslots; i += warps) {
+    for (int64_t i = blockIdx.x; i < (int64_t)P.pslots; i += gridDim.x) {
         const uint64_t key = P.ptable[i];
-        if (key == kEmptyKey || !(P.parity[i] & 1u)) continue;  // warp-uniform
+        if (key == kEmptyKey || !(P.parity[i] & 1u)) continue;  // block-uniform
         const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
         const float* ba = P.a.obj_box + 6 * (size_t)a;
         const float* bb = P.b.obj_box + 6 * (size_t)b;
@@ -962,91 +973,102 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
         bool meets = false, undecided = false;
         if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
             const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
-            if ((int64_t)ra.y + rb.y > kPairScanMax || !P.a.tri_chunk_box || !P.b.tri_chunk_box) {
+            if ((int64_t)ra.y + rb.y > kPairScanMax) {
                 undecided = true;
             } else {
-                // a's chunks that meet the common box, with the union of their boxes
-                const int c0 = ra.x >> 5, c1 = (ra.x + ra.y - 1) >> 5;
-                int nc = 0;
+                // a's triangles near the common box: list (block-wide compaction) and patch box
+                int na = 0;
                 float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-                for (int base = c0; base <= c1; base += 32) {
-                    const int c = base + lane;
-                    float cb[6];
+                for (int base = 0; base < ra.y; base += kPairThreads) {
+                    const int k = base + tid;
                     bool meet = false;
-                    if (c <= c1) {
-                        for (int k = 0; k < 6; ++k) cb[k] = __ldg(P.a.tri_chunk_box + 6 * (size_t)c + k);
-                        meet = boxes_meet(cb, lo, hi);
-                    }
-                    const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
-                    const int pos = nc + __popc(m & ((1u << lane) - 1u));
-                    if (meet) {
-                        plo = make_float3(fminf(plo.x, cb[0]), fminf(plo.y, cb[1]), fminf(plo.z, cb[2]));
-                        phi = make_float3(fmaxf(phi.x, cb[3]), fmaxf(phi.y, cb[4]), fmaxf(phi.z, cb[5]));
-                        if (pos < kPairChunks) {
-                            s_chunk[w][pos] = (uint32_t)c;
-                            for (int k = 0; k < 6; ++k) s_cbox[w][pos][k] = cb[k];
+                    uint32_t t = 0;
+                    if (k < ra.y) {
+                        t = (uint32_t)(ra.x + k);
+                        const float3 v0 = tri_vertex(P.a, t, 0), v1 = tri_vertex(P.a, t, 1), v2 = tri_vertex(P.a, t, 2);
+                        meet = tri_box_meets(v0, v1, v2, lo, hi);
+                        if (meet) {
+                            plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))),
+                                              fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
+                                              fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
+                            phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))),
+                                              fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
+                                              fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
                         }
                     }
-                    nc += __popc(m);
+                    const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
+                    if (lane == 0) s_warp[w] = __popc(m);
+                    __syncthreads();
+                    int before = na, total = 0;
+                    for (int q = 0; q < kPairThreads / 32; ++q) {
+                        if (q < w) before += s_warp[q];
+                        total += s_warp[q];
+                    }
+                    const int pos = before + __popc(m & ((1u << lane) - 1u));
+                    if (meet && pos < kPairList) s_list[pos] = t;
+                    na += total;
+                    __syncthreads();
                 }
-                for (int off = 16; off; off >>= 1) {
-                    plo.x = fminf(plo.x, __shfl_xor_sync(0xFFFFFFFFu, plo.x, off));
-                    plo.y = fminf(plo.y, __shfl_xor_sync(0xFFFFFFFFu, plo.y, off));
-                    plo.z = fminf(plo.z, __shfl_xor_sync(0xFFFFFFFFu, plo.z, off));
-                    phi.x = fmaxf(phi.x, __shfl_xor_sync(0xFFFFFFFFu, phi.x, off));
-                    phi.y = fmaxf(phi.y, __shfl_xor_sync(0xFFFFFFFFu, phi.y, off));
-                    phi.z = fmaxf(phi.z, __shfl_xor_sync(0xFFFFFFFFu, phi.z, off));
+                plo = make_float3(block_min(plo.x, s_red), block_min(plo.y, s_red), block_min(plo.z, s_red));
+                phi = make_float3(block_max(phi.x, s_red), block_max(phi.y, s_red), block_max(phi.z, s_red));
+                const bool listed = na <= kPairList;
+                const bool cached = na <= kPairVerts;
+                if (cached) {
+                    for (int k = tid; k < na; k += kPairThreads) {
+                        const uint32_t t = s_list[k];
+                        for (int v = 0; v < 3; ++v) {
+                            const float3 x = tri_vertex(P.a, t, v);
+                            s_tri[k][v] = make_float4(x.x, x.y, x.z, 0.0f);
+                        }
+                    }
+                    __syncthreads();
                 }
-                __syncwarp();
-                if (nc > kPairChunks) {
+                if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
                     undecided = true;
-                } else if (nc > 0) {
+                } else if (na > 0) {
                     lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
                     hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
-                    const int a_end = ra.x + ra.y;
-                    // b's triangles, one per lane, against the listed chunks
-                    for (int base = 0; base < rb.y && !meets; base += 32) {
-                        const int k = base + lane;
+                    const int nj = listed ? na : ra.y;
+                    // b's triangles, one per thread, against the patch
+                    for (int base = 0; base < rb.y && !meets; base += kPairThreads) {
+                        const int k = base + tid;
                         bool hit = false;
                         if (k < rb.y) {
                             const uint32_t tb = (uint32_t)(rb.x + k);
-                            float bcb[6];
-                            for (int q = 0; q < 6; ++q) bcb[q] = __ldg(P.b.tri_chunk_box + 6 * (size_t)(tb >> 5) + q);
-                            if (boxes_meet(bcb, lo, hi)) {
-                                const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
-                                             b2 = tri_vertex(P.b, tb, 2);
-                                const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
-                                                               fminf(b0.z, fminf(b1.z, b2.z)));
-                                const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
-                                                               fmaxf(b0.z, fmaxf(b1.z, b2.z)));
-                                if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
-                                    for (int j = 0; j < nc && !hit; ++j) {
-                                        if (!boxes_meet(s_cbox[w][j], blo, bhi)) continue;
-                                        const int c = (int)s_chunk[w][j];
-                                        const int t0 = max(c << 5, ra.x), t1 = min((c << 5) + 32, a_end);
-                                        for (int t = t0; t < t1 && !hit; ++t) {
-                                            const float3 a0 = tri_vertex(P.a, (uint32_t)t, 0),
-                                                         a1 = tri_vertex(P.a, (uint32_t)t, 1),
-                                                         a2 = tri_vertex(P.a, (uint32_t)t, 2);
-                                            if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
-                                            ++tests;
-                                            hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) ||
-                                                  seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
-                                                  seg_tri_exact(a2, a0, b0, b1, b2, pc) ||
-                                                  seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
-                                                  seg_tri_exact(b1, b2, a0, a1, a2, pc) ||
-                                                  seg_tri_exact(b2, b0, a0, a1, a2, pc);
-                                        }
+                            const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
+                                         b2 = tri_vertex(P.b, tb, 2);
+                            const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
+                                                           fminf(b0.z, fminf(b1.z, b2.z)));
+                            const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
+                                                           fmaxf(b0.z, fmaxf(b1.z, b2.z)));
+                            if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
+                                for (int j = 0; j < nj && !hit; ++j) {
+                                    float3 a0, a1, a2;
+                                    if (cached) {
+                                        const float4 x0 = s_tri[j][0], x1 = s_tri[j][1], x2 = s_tri[j][2];
+                                        a0 = make_float3(x0.x, x0.y, x0.z);
+                                        a1 = make_float3(x1.x, x1.y, x1.z);
+                                        a2 = make_float3(x2.x, x2.y, x2.z);
+                                    } else {
+                                        const uint32_t ta = listed ? s_list[j] : (uint32_t)(ra.x + j);
+                                        a0 = tri_vertex(P.a, ta, 0);
+                                        a1 = tri_vertex(P.a, ta, 1);
+                                        a2 = tri_vertex(P.a, ta, 2);
                                     }
+                                    if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
+                                    ++tests;
+                                    hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
+                                          seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
+                                          seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
                                 }
                             }
                         }
-                        meets = __any_sync(0xFFFFFFFFu, hit);
+                        meets = __syncthreads_or(hit) != 0;
                     }
                 }
             }
         }
-        if (lane == 0) {
+        if (tid == 0) {
             if (undecided) {
                 atomicAdd(P.fallback, 1ull);
             } else if (!meets) {
@@ -1054,7 +1076,7 @@ __global__ void __launch_bounds__(128) k_containment_pairs(PairParams P) {
                 if (pos < P.cap) P.out[pos] = key;
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
     flush_counter(&P.ctr->tri_tests, tests);
     flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
@@ -2339,8 +2361,8 @@ int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint
     P.cap = cap;
     P.fallback = fallback;
     P.ctr = ctx->d_counters;
-    const int64_t blocks = std::min<int64_t>(((int64_t)pslots + kPairWarps - 1) / kPairWarps, (int64_t)ctx->sm_count * 16);
-    k_containment_pairs<<<(unsigned)std::max<int64_t>(blocks, 1), 32 * kPairWarps, 0, ctx->stream>>>(P);
+    const int64_t blocks = std::min<int64_t>((int64_t)pslots, (int64_t)ctx->sm_count * 8);
+    k_containment_pairs<<<(unsigned)std::max<int64_t>(blocks, 1), kPairThreads, 0, ctx->stream>>>(P);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "containment by pairs");
 }
