@@ -315,14 +315,13 @@ def test_nested_containers_enlarge_and_rerun(ctx):
 
 @pytest.mark.parametrize("sizing", ["hash", "two_pass"])
 def test_containment_pairs_and_their_fallback(ctx, sizing):
-    """Containment tests its odd-parity candidate pairs directly over the
-    container's 32-triangle chunks that meet the pair: a 320-triangle sphere
-    inside a 5,120-triangle one (a large patch), two nested 5,120-triangle
-    spheres (every chunk of the container listed).  A pair too large for
-    that -- a 327,680-triangle container (past 65,536 triangles together),
-    or nested 20,480-triangle spheres (more than 256 listed chunks) -- sends
-    the join through the culling pipeline.  All must give the oracle's
-    pairs."""
+    """Containment tests its odd-parity candidate pairs directly, a block
+    per pair: a 320-triangle sphere inside a 5,120-triangle one has a
+    container patch larger than the shared-memory list, read in place.  A
+    pair too large for that -- a 327,680-triangle container (past 65,536
+    triangles together), or nested spheres of 5,120 or 20,480 triangles each
+    (an unlisted patch past 4 M triangle pairs) -- sends the join through
+    the culling pipeline.  All must give the oracle's pairs."""
     small = pg.ellipsoid_pair(1, 2, 300, 300, 2, lo=0, hi=70, frac_contact=0.1)
     big = (pg.icospheres(51, 1, 7, ln_mu=float(np.log(20.0)), sigma=0.0, lo=0.0, hi=0.0),
            pg.icospheres(52, 30, 2, ln_mu=0.0, sigma=0.2, lo=-10.0, hi=10.0))
@@ -332,9 +331,9 @@ def test_containment_pairs_and_their_fallback(ctx, sizing):
              pg.icospheres(56, 1, 2, ln_mu=float(np.log(9.9)), sigma=0.0, lo=0.0, hi=0.0))
     many = (pg.icospheres(57, 1, 5, ln_mu=float(np.log(10.0)), sigma=0.0, lo=0.0, hi=0.0),
             pg.icospheres(58, 1, 5, ln_mu=float(np.log(9.9)), sigma=0.0, lo=0.0, hi=0.0))
-    by_pairs = {"pairs": 1, "large patch": 1, "dense container": 1, "large container": 0, "many chunks": 0}
+    by_pairs = {"pairs": 1, "large patch": 1, "dense container": 0, "large container": 0, "nested 20,480": 0}
     for name, (A, B) in (("pairs", small), ("large patch", patch), ("dense container", tight),
-                         ("large container", big), ("many chunks", many)):
+                         ("large container", big), ("nested 20,480", many)):
         want = O.containment_keys(A, B)
         got = J.containment_join(ctx, ds(ctx, A), ds(ctx, B), sizing=sizing)
         assert np.array_equal(keys(got), want), name
