@@ -554,6 +554,7 @@ def main_tubes(args):
     plain GPU form, the edge-ray roofline and the CPU oracle on a sample."""
     import torch
     import pierce_gb300 as pg
+    from pierce_gb300 import capi
     from pierce_gb300 import join as J
     from pierce_gb300 import sizing as S
     from oracle import pyoracle as O
@@ -700,9 +701,13 @@ def main_tubes(args):
         ctx.release_scratch()
         return dt
 
-    _, keys_e, d2h = e2e.step(tuned_o, upload_tri, want_keys=True)
+    # datasets uploaded without edges trace the kept triangles' edges
+    tri_o = capi.JoinOpts.from_buffer_copy(tuned_o)
+    if tri_o.edge_source == capi.EDGES_DATASET:
+        tri_o.edge_source = capi.EDGES_AUTO
+    _, keys_e, d2h = e2e.step(tri_o, upload_tri, want_keys=True)
     e2e_identical = bool(np.array_equal(keys_e, keys_t))
-    e2e_s = timed(tuned_o, upload_tri, None, max(1, min(args.steps, 5)))
+    e2e_s = timed(tri_o, upload_tri, None, max(1, min(args.steps, 5)))
     e2e_edges_s = timed(tuned_o, upload, None, max(1, min(args.steps, 2)))
     plain_e2e_s = timed(plain_o, upload, plain_build, max(1, min(args.steps, 2)))
     log(f"e2e tuned {1000 * e2e_s:.1f} ms ({1000 * e2e_edges_s:.1f} ms uploading the edges too), "

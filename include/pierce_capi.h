@@ -313,7 +313,8 @@ void pierce_result_destroy(pierce_result* r);
  * warp {32, 64, 128}, stack depth {8, 16, 32}, hash load factor
  * {0.25, 0.5, 0.75} when the sizing uses a hash set, traversal {one ray per
  * thread over four-wide nodes, warp packets, one ray per thread over binary
- * nodes}), each trial the best
+ * nodes}, and the rays' source {as in base, the datasets' edges} when both
+ * datasets hold edges), each trial the best
  * of `repeats` timed runs after one untimed run.  *best receives the
  * fastest values; trials[0 .. *num_trials) every trial (max_trials slots,
  * may be NULL). */
@@ -322,6 +323,8 @@ typedef struct pierce_tuned {
     int32_t rays_per_warp;
     int32_t stack_depth;
     int32_t traversal;
+    int32_t edge_source;          /* pierce_edge_source */
+    int32_t reserved;
     double hash_load_factor;
     double ms;                    /* best GPU time of the join with these values */
 } pierce_tuned;

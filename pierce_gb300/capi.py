@@ -108,7 +108,7 @@ class MlpTrainOpts(C.Structure):
 
 class Tuned(C.Structure):
     _fields_ = [("leaf_size", I32), ("rays_per_warp", I32), ("stack_depth", I32), ("traversal", I32),
-                ("hash_load_factor", D), ("ms", D)]
+                ("edge_source", I32), ("reserved", I32), ("hash_load_factor", D), ("ms", D)]
 
 
 class DatasetInfo(C.Structure):

@@ -2125,6 +2125,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     cur.stack_depth = o.stack_depth > 0 ? o.stack_depth : 8;
     cur.hash_load_factor = o.hash_load_factor;
     cur.traversal = o.traversal;
+    cur.edge_source = o.edge_source;
     cur.ms = 1e300;
     // time one setting: one untimed run, then the best of `repeats`
     auto trial = [&](pierce_tuned& t) -> int {
@@ -2134,6 +2135,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
         q.stack_depth = t.stack_depth;
         q.hash_load_factor = t.hash_load_factor;
         q.traversal = t.traversal;
+        q.edge_source = t.edge_source;
         t.ms = 1e300;
         for (int r = 0; r <= repeats; ++r) {
             pierce_result* res = nullptr;
@@ -2152,10 +2154,14 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
     const std::vector<double> loads = hashed ? std::vector<double>{0.25, 0.5, 0.75}
                                              : std::vector<double>{cur.hash_load_factor};
     const std::vector<int> traversals = {0, 1, 2};
+    // the rays' source: as given, or the datasets' edges when both hold them
+    // (either gives the same pairs; which is faster depends on the meshes)
+    std::vector<int> sources = {o.edge_source};
+    if (o.edge_source != PIERCE_EDGES_DATASET && a->ne > 0 && b->ne > 0) sources.push_back(PIERCE_EDGES_DATASET);
     // coordinate descent: one parameter at a time, keeping the best so far
-    for (int param = 0; param < 5; ++param) {
+    for (int param = 0; param < 6; ++param) {
         const size_t n = param == 0 ? leaves.size() : param == 1 ? rays.size() : param == 2 ? stacks.size()
-                         : param == 3 ? loads.size() : traversals.size();
+                         : param == 3 ? loads.size() : param == 4 ? traversals.size() : sources.size();
         pierce_tuned winner = cur;
         for (size_t i = 0; i < n; ++i) {
             pierce_tuned t = cur;
@@ -2164,6 +2170,7 @@ int pierce_autotune_join(pierce_ctx* ctx, pierce_dataset* a, pierce_dataset* b, 
             if (param == 2) t.stack_depth = stacks[i];
             if (param == 3) t.hash_load_factor = loads[i];
             if (param == 4) t.traversal = traversals[i];
+            if (param == 5) t.edge_source = sources[i];
             if (int s = trial(t)) return s;
             if (t.ms < winner.ms) winner = t;
         }

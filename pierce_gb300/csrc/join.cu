@@ -899,10 +899,12 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 // 385-550), so only the odd-parity pairs (a, b) need an overlap answer.  A
 // block of kPairThreads takes one such pair, so that one large pair does
 // not hold a lone warp for the whole launch: it lists the triangles of a
-// whose boxes meet the intersection of the two object boxes (a patch of a's
+// (those of a's 32-triangle chunks whose boxes meet, read first) whose boxes
+// meet the intersection of the two object boxes (a patch of a's
 // surface; the vertices of up to kPairVerts of them are kept in shared
 // memory), shrinks the box to that patch's box, and streams b's triangles
-// past them, one per thread, each tested against the listed triangles whose
+// past them, one per thread (a triangle whose 32-triangle chunk box misses
+// the patch is skipped unread), each tested against the listed triangles whose
 // boxes meet its own with the exact closed triangle-triangle predicate (an
 // edge of one meets the other: six segment tests, the edge definition for
 // the edges of triangles).  The pair is a containment pair when none meets;
@@ -914,6 +916,7 @@ __global__ void k_keep_candidates(uint8_t* flags, int64_t n) {
 constexpr int kPairThreads = 256;
 constexpr int kPairList = 1024;
 constexpr int kPairVerts = 512;
+constexpr int kPairChunkList = 512;  // listed chunks of the container (more: its whole range)
 constexpr int kPairScanMax = 1 << 16;
 constexpr int64_t kPairStreamMax = 1 << 22;
 
@@ -952,8 +955,26 @@ __device__ __forceinline__ float block_min(float v, float* red) {
 }
 __device__ __forceinline__ float block_max(float v, float* red) { return -block_min(-v, red); }
 
+// Position of this thread's flag among the block's set flags, after `base`
+// (warp ballots; per-warp counts in s_warp), and the block's total.
+__device__ __forceinline__ int block_compact(bool flag, int base, int* s_warp) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, flag);
+    if (lane == 0) s_warp[w] = __popc(m);
+    __syncthreads();
+    int before = base;
+    for (int q = 0; q < w; ++q) before += s_warp[q];
+    return before + __popc(m & ((1u << lane) - 1u));
+}
+__device__ __forceinline__ int block_total(const int* s_warp) {
+    int total = 0;
+    for (int q = 0; q < kPairThreads / 32; ++q) total += s_warp[q];
+    return total;
+}
+
 __global__ void __launch_bounds__(kPairThreads) k_containment_pairs(PairParams P) {
     __shared__ uint32_t s_list[kPairList];
+    __shared__ uint32_t s_chunk[kPairChunkList];
     __shared__ float4 s_tri[kPairVerts][3];
     __shared__ int s_warp[kPairThreads / 32];
     __shared__ float s_red[kPairThreads / 32];
@@ -976,37 +997,53 @@ __global__ void __launch_bounds__(kPairThreads) k_containment_pairs(PairParams P
             if ((int64_t)ra.y + rb.y > kPairScanMax) {
                 undecided = true;
             } else {
-                // a's triangles near the common box: list (block-wide compaction) and patch box
+                // a's 32-triangle chunks whose boxes meet the common box, then
+                // the triangles of those chunks that do: the list (block-wide
+                // compaction) and the patch box
+                const int c0 = ra.x >> 5, c1 = (ra.x + ra.y - 1) >> 5;
+                int nmc = 0;
+                for (int base = c0; base <= c1; base += kPairThreads) {
+                    const int c = base + tid;
+                    bool meet = true;  // no chunk boxes: every chunk
+                    if (c > c1) meet = false;
+                    else if (P.a.tri_chunk_box) {
+                        const float* cb = P.a.tri_chunk_box + 6 * (size_t)c;
+                        meet = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
+                                           __ldg(cb + 5), lo, hi);
+                    }
+                    const int pos = block_compact(meet, nmc, s_warp);
+                    if (meet && pos < kPairChunkList) s_chunk[pos] = (uint32_t)c;
+                    nmc += block_total(s_warp);
+                    __syncthreads();
+                }
                 int na = 0;
                 float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-                for (int base = 0; base < ra.y; base += kPairThreads) {
+                const bool by_chunks = nmc <= kPairChunkList;
+                const int slots = by_chunks ? 32 * nmc : ra.y;
+                for (int base = 0; base < slots; base += kPairThreads) {
                     const int k = base + tid;
                     bool meet = false;
                     uint32_t t = 0;
-                    if (k < ra.y) {
-                        t = (uint32_t)(ra.x + k);
-                        const float3 v0 = tri_vertex(P.a, t, 0), v1 = tri_vertex(P.a, t, 1), v2 = tri_vertex(P.a, t, 2);
-                        meet = tri_box_meets(v0, v1, v2, lo, hi);
-                        if (meet) {
-                            plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))),
-                                              fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
-                                              fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
-                            phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))),
-                                              fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
-                                              fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
+                    if (k < slots) {
+                        const int tt = by_chunks ? (int)(s_chunk[k >> 5] << 5) + (k & 31) : ra.x + k;
+                        if (tt >= ra.x && tt < ra.x + ra.y) {
+                            t = (uint32_t)tt;
+                            const float3 v0 = tri_vertex(P.a, t, 0), v1 = tri_vertex(P.a, t, 1),
+                                         v2 = tri_vertex(P.a, t, 2);
+                            meet = tri_box_meets(v0, v1, v2, lo, hi);
+                            if (meet) {
+                                plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))),
+                                                  fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
+                                                  fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
+                                phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))),
+                                                  fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
+                                                  fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
+                            }
                         }
                     }
-                    const unsigned m = __ballot_sync(0xFFFFFFFFu, meet);
-                    if (lane == 0) s_warp[w] = __popc(m);
-                    __syncthreads();
-                    int before = na, total = 0;
-                    for (int q = 0; q < kPairThreads / 32; ++q) {
-                        if (q < w) before += s_warp[q];
-                        total += s_warp[q];
-                    }
-                    const int pos = before + __popc(m & ((1u << lane) - 1u));
+                    const int pos = block_compact(meet, na, s_warp);
                     if (meet && pos < kPairList) s_list[pos] = t;
-                    na += total;
+                    na += block_total(s_warp);
                     __syncthreads();
                 }
                 plo = make_float3(block_min(plo.x, s_red), block_min(plo.y, s_red), block_min(plo.z, s_red));
@@ -1033,7 +1070,13 @@ __global__ void __launch_bounds__(kPairThreads) k_containment_pairs(PairParams P
                     for (int base = 0; base < rb.y && !meets; base += kPairThreads) {
                         const int k = base + tid;
                         bool hit = false;
-                        if (k < rb.y) {
+                        bool near = k < rb.y;
+                        if (near && P.b.tri_chunk_box) {  // the triangle's chunk box first
+                            const float* cb = P.b.tri_chunk_box + 6 * (size_t)((rb.x + k) >> 5);
+                            near = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
+                                               __ldg(cb + 5), lo, hi);
+                        }
+                        if (near) {
                             const uint32_t tb = (uint32_t)(rb.x + k);
                             const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
                                          b2 = tri_vertex(P.b, tb, 2);

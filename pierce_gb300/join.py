@@ -268,6 +268,7 @@ def tuned_opts(opts: capi.JoinOpts, best: dict) -> capi.JoinOpts:
     o.leaf_size, o.rays_per_warp = int(best["leaf_size"]), int(best["rays_per_warp"])
     o.stack_depth, o.hash_load_factor = int(best["stack_depth"]), float(best["hash_load_factor"])
     o.traversal = int(best.get("traversal", 0))
+    o.edge_source = int(best.get("edge_source", o.edge_source))
     return o
 
 

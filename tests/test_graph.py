@@ -94,11 +94,11 @@ def test_autotuner_returns_a_tried_setting_with_identical_pairs(ctx, datasets):
     A, B = datasets
     base = J.make_opts(predicate="overlap", expected_pairs=2000)
     best, trials = J.autotune(ctx, A, B, base, repeats=1)
-    assert len(trials) == 4 + 3 + 3 + 3 + 3
+    assert len(trials) == 4 + 3 + 3 + 3 + 3 + 2  # the last two: the rays' source
     assert best["ms"] == min(t["ms"] for t in trials)
     assert best["leaf_size"] in (1, 2, 4, 8) and best["rays_per_warp"] in (32, 64, 128)
     assert best["stack_depth"] in (8, 16, 32) and best["hash_load_factor"] in (0.25, 0.5, 0.75)
-    assert best["traversal"] in (0, 1, 2)
+    assert best["traversal"] in (0, 1, 2) and best["edge_source"] in (0, 1)
     ref = J.run_join(ctx, A, B, base)
     for t in trials[::3]:
         r = J.run_join(ctx, A, B, J.tuned_opts(base, t))
