@@ -978,148 +978,163 @@ __global__ void __launch_bounds__(kPairThreads) k_containment_pairs(PairParams P
     __shared__ float4 s_tri[kPairVerts][3];
     __shared__ int s_warp[kPairThreads / 32];
     __shared__ float s_red[kPairThreads / 32];
+    __shared__ uint64_t s_pairs[kPairThreads];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     PredCounters pc{0, 0};
     uint32_t tests = 0;
-    for (int64_t i = blockIdx.x; i < (int64_t)P.pslots; i += gridDim.x) {
-        const uint64_t key = P.ptable[i];
-        if (key == kEmptyKey || !(P.parity[i] & 1u)) continue;  // block-uniform
-        const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
-        const float* ba = P.a.obj_box + 6 * (size_t)a;
-        const float* bb = P.b.obj_box + 6 * (size_t)b;
-        float3 lo = make_float3(fmaxf(__ldg(ba), __ldg(bb)), fmaxf(__ldg(ba + 1), __ldg(bb + 1)),
-                                fmaxf(__ldg(ba + 2), __ldg(bb + 2)));
-        float3 hi = make_float3(fminf(__ldg(ba + 3), __ldg(bb + 3)), fminf(__ldg(ba + 4), __ldg(bb + 4)),
-                                fminf(__ldg(ba + 5), __ldg(bb + 5)));
-        bool meets = false, undecided = false;
-        if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
-            const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
-            if ((int64_t)ra.y + rb.y > kPairScanMax) {
-                undecided = true;
-            } else {
-                // a's 32-triangle chunks whose boxes meet the common box, then
-                // the triangles of those chunks that do: the list (block-wide
-                // compaction) and the patch box
-                const int c0 = ra.x >> 5, c1 = (ra.x + ra.y - 1) >> 5;
-                int nmc = 0;
-                for (int base = c0; base <= c1; base += kPairThreads) {
-                    const int c = base + tid;
-                    bool meet = true;  // no chunk boxes: every chunk
-                    if (c > c1) meet = false;
-                    else if (P.a.tri_chunk_box) {
-                        const float* cb = P.a.tri_chunk_box + 6 * (size_t)c;
-                        meet = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
-                                           __ldg(cb + 5), lo, hi);
-                    }
-                    const int pos = block_compact(meet, nmc, s_warp);
-                    if (meet && pos < kPairChunkList) s_chunk[pos] = (uint32_t)c;
-                    nmc += block_total(s_warp);
-                    __syncthreads();
-                }
-                int na = 0;
-                float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-                const bool by_chunks = nmc <= kPairChunkList;
-                const int slots = by_chunks ? 32 * nmc : ra.y;
-                for (int base = 0; base < slots; base += kPairThreads) {
-                    const int k = base + tid;
-                    bool meet = false;
-                    uint32_t t = 0;
-                    if (k < slots) {
-                        const int tt = by_chunks ? (int)(s_chunk[k >> 5] << 5) + (k & 31) : ra.x + k;
-                        if (tt >= ra.x && tt < ra.x + ra.y) {
-                            t = (uint32_t)tt;
-                            const float3 v0 = tri_vertex(P.a, t, 0), v1 = tri_vertex(P.a, t, 1),
-                                         v2 = tri_vertex(P.a, t, 2);
-                            meet = tri_box_meets(v0, v1, v2, lo, hi);
-                            if (meet) {
-                                plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))),
-                                                  fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
-                                                  fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
-                                phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))),
-                                                  fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
-                                                  fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
-                            }
-                        }
-                    }
-                    const int pos = block_compact(meet, na, s_warp);
-                    if (meet && pos < kPairList) s_list[pos] = t;
-                    na += block_total(s_warp);
-                    __syncthreads();
-                }
-                plo = make_float3(block_min(plo.x, s_red), block_min(plo.y, s_red), block_min(plo.z, s_red));
-                phi = make_float3(block_max(phi.x, s_red), block_max(phi.y, s_red), block_max(phi.z, s_red));
-                const bool listed = na <= kPairList;
-                const bool cached = na <= kPairVerts;
-                if (cached) {
-                    for (int k = tid; k < na; k += kPairThreads) {
-                        const uint32_t t = s_list[k];
-                        for (int v = 0; v < 3; ++v) {
-                            const float3 x = tri_vertex(P.a, t, v);
-                            s_tri[k][v] = make_float4(x.x, x.y, x.z, 0.0f);
-                        }
-                    }
-                    __syncthreads();
-                }
-                if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
+    // windows of kPairThreads slots of the parity table: every thread reads
+    // one slot, the block compacts the odd pairs, then takes them in turn
+    for (int64_t wbase = (int64_t)blockIdx.x * kPairThreads; wbase < (int64_t)P.pslots;
+         wbase += (int64_t)gridDim.x * kPairThreads) {
+        uint64_t slot_key = kEmptyKey;
+        bool odd = false;
+        if (wbase + tid < (int64_t)P.pslots) {
+            slot_key = P.ptable[wbase + tid];
+            odd = slot_key != kEmptyKey && (P.parity[wbase + tid] & 1u);
+        }
+        const int odd_pos = block_compact(odd, 0, s_warp);
+        const int n_odd = block_total(s_warp);
+        if (odd) s_pairs[odd_pos] = slot_key;
+        __syncthreads();
+        for (int q = 0; q < n_odd; ++q) {
+            const uint64_t key = s_pairs[q];
+            const uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+            const float* ba = P.a.obj_box + 6 * (size_t)a;
+            const float* bb = P.b.obj_box + 6 * (size_t)b;
+            float3 lo = make_float3(fmaxf(__ldg(ba), __ldg(bb)), fmaxf(__ldg(ba + 1), __ldg(bb + 1)),
+                                    fmaxf(__ldg(ba + 2), __ldg(bb + 2)));
+            float3 hi = make_float3(fminf(__ldg(ba + 3), __ldg(bb + 3)), fminf(__ldg(ba + 4), __ldg(bb + 4)),
+                                    fminf(__ldg(ba + 5), __ldg(bb + 5)));
+            bool meets = false, undecided = false;
+            if (lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z) {
+                const int2 ra = __ldg(P.a.obj_range + a), rb = __ldg(P.b.obj_range + b);
+                if ((int64_t)ra.y + rb.y > kPairScanMax) {
                     undecided = true;
-                } else if (na > 0) {
-                    lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
-                    hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
-                    const int nj = listed ? na : ra.y;
-                    // b's triangles, one per thread, against the patch
-                    for (int base = 0; base < rb.y && !meets; base += kPairThreads) {
-                        const int k = base + tid;
-                        bool hit = false;
-                        bool near = k < rb.y;
-                        if (near && P.b.tri_chunk_box) {  // the triangle's chunk box first
-                            const float* cb = P.b.tri_chunk_box + 6 * (size_t)((rb.x + k) >> 5);
-                            near = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
+                } else {
+                    // a's 32-triangle chunks whose boxes meet the common box, then
+                    // the triangles of those chunks that do: the list (block-wide
+                    // compaction) and the patch box
+                    const int c0 = ra.x >> 5, c1 = (ra.x + ra.y - 1) >> 5;
+                    int nmc = 0;
+                    for (int base = c0; base <= c1; base += kPairThreads) {
+                        const int c = base + tid;
+                        bool meet = true;  // no chunk boxes: every chunk
+                        if (c > c1) meet = false;
+                        else if (P.a.tri_chunk_box) {
+                            const float* cb = P.a.tri_chunk_box + 6 * (size_t)c;
+                            meet = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
                                                __ldg(cb + 5), lo, hi);
                         }
-                        if (near) {
-                            const uint32_t tb = (uint32_t)(rb.x + k);
-                            const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
-                                         b2 = tri_vertex(P.b, tb, 2);
-                            const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
-                                                           fminf(b0.z, fminf(b1.z, b2.z)));
-                            const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
-                                                           fmaxf(b0.z, fmaxf(b1.z, b2.z)));
-                            if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
-                                for (int j = 0; j < nj && !hit; ++j) {
-                                    float3 a0, a1, a2;
-                                    if (cached) {
-                                        const float4 x0 = s_tri[j][0], x1 = s_tri[j][1], x2 = s_tri[j][2];
-                                        a0 = make_float3(x0.x, x0.y, x0.z);
-                                        a1 = make_float3(x1.x, x1.y, x1.z);
-                                        a2 = make_float3(x2.x, x2.y, x2.z);
-                                    } else {
-                                        const uint32_t ta = listed ? s_list[j] : (uint32_t)(ra.x + j);
-                                        a0 = tri_vertex(P.a, ta, 0);
-                                        a1 = tri_vertex(P.a, ta, 1);
-                                        a2 = tri_vertex(P.a, ta, 2);
-                                    }
-                                    if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
-                                    ++tests;
-                                    hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
-                                          seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
-                                          seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                        const int pos = block_compact(meet, nmc, s_warp);
+                        if (meet && pos < kPairChunkList) s_chunk[pos] = (uint32_t)c;
+                        nmc += block_total(s_warp);
+                        __syncthreads();
+                    }
+                    int na = 0;
+                    float3 plo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), phi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+                    const bool by_chunks = nmc <= kPairChunkList;
+                    const int slots = by_chunks ? 32 * nmc : ra.y;
+                    for (int base = 0; base < slots; base += kPairThreads) {
+                        const int k = base + tid;
+                        bool meet = false;
+                        uint32_t t = 0;
+                        if (k < slots) {
+                            const int tt = by_chunks ? (int)(s_chunk[k >> 5] << 5) + (k & 31) : ra.x + k;
+                            if (tt >= ra.x && tt < ra.x + ra.y) {
+                                t = (uint32_t)tt;
+                                const float3 v0 = tri_vertex(P.a, t, 0), v1 = tri_vertex(P.a, t, 1),
+                                             v2 = tri_vertex(P.a, t, 2);
+                                meet = tri_box_meets(v0, v1, v2, lo, hi);
+                                if (meet) {
+                                    plo = make_float3(fminf(plo.x, fminf(v0.x, fminf(v1.x, v2.x))),
+                                                      fminf(plo.y, fminf(v0.y, fminf(v1.y, v2.y))),
+                                                      fminf(plo.z, fminf(v0.z, fminf(v1.z, v2.z))));
+                                    phi = make_float3(fmaxf(phi.x, fmaxf(v0.x, fmaxf(v1.x, v2.x))),
+                                                      fmaxf(phi.y, fmaxf(v0.y, fmaxf(v1.y, v2.y))),
+                                                      fmaxf(phi.z, fmaxf(v0.z, fmaxf(v1.z, v2.z))));
                                 }
                             }
                         }
-                        meets = __syncthreads_or(hit) != 0;
+                        const int pos = block_compact(meet, na, s_warp);
+                        if (meet && pos < kPairList) s_list[pos] = t;
+                        na += block_total(s_warp);
+                        __syncthreads();
+                    }
+                    plo = make_float3(block_min(plo.x, s_red), block_min(plo.y, s_red), block_min(plo.z, s_red));
+                    phi = make_float3(block_max(phi.x, s_red), block_max(phi.y, s_red), block_max(phi.z, s_red));
+                    const bool listed = na <= kPairList;
+                    const bool cached = na <= kPairVerts;
+                    if (cached) {
+                        for (int k = tid; k < na; k += kPairThreads) {
+                            const uint32_t t = s_list[k];
+                            for (int v = 0; v < 3; ++v) {
+                                const float3 x = tri_vertex(P.a, t, v);
+                                s_tri[k][v] = make_float4(x.x, x.y, x.z, 0.0f);
+                            }
+                        }
+                        __syncthreads();
+                    }
+                    if (!listed && (int64_t)ra.y * rb.y > kPairStreamMax) {
+                        undecided = true;
+                    } else if (na > 0) {
+                        lo = make_float3(fmaxf(lo.x, plo.x), fmaxf(lo.y, plo.y), fmaxf(lo.z, plo.z));
+                        hi = make_float3(fminf(hi.x, phi.x), fminf(hi.y, phi.y), fminf(hi.z, phi.z));
+                        const int nj = listed ? na : ra.y;
+                        // b's triangles, one per thread, against the patch
+                        for (int base = 0; base < rb.y && !meets; base += kPairThreads) {
+                            const int k = base + tid;
+                            bool hit = false;
+                            bool near = k < rb.y;
+                            if (near && P.b.tri_chunk_box) {  // the triangle's chunk box first
+                                const float* cb = P.b.tri_chunk_box + 6 * (size_t)((rb.x + k) >> 5);
+                                near = box_overlap(__ldg(cb), __ldg(cb + 3), __ldg(cb + 1), __ldg(cb + 4), __ldg(cb + 2),
+                                                   __ldg(cb + 5), lo, hi);
+                            }
+                            if (near) {
+                                const uint32_t tb = (uint32_t)(rb.x + k);
+                                const float3 b0 = tri_vertex(P.b, tb, 0), b1 = tri_vertex(P.b, tb, 1),
+                                             b2 = tri_vertex(P.b, tb, 2);
+                                const float3 blo = make_float3(fminf(b0.x, fminf(b1.x, b2.x)), fminf(b0.y, fminf(b1.y, b2.y)),
+                                                               fminf(b0.z, fminf(b1.z, b2.z)));
+                                const float3 bhi = make_float3(fmaxf(b0.x, fmaxf(b1.x, b2.x)), fmaxf(b0.y, fmaxf(b1.y, b2.y)),
+                                                               fmaxf(b0.z, fmaxf(b1.z, b2.z)));
+                                if (box_overlap(blo.x, bhi.x, blo.y, bhi.y, blo.z, bhi.z, lo, hi)) {
+                                    for (int j = 0; j < nj && !hit; ++j) {
+                                        float3 a0, a1, a2;
+                                        if (cached) {
+                                            const float4 x0 = s_tri[j][0], x1 = s_tri[j][1], x2 = s_tri[j][2];
+                                            a0 = make_float3(x0.x, x0.y, x0.z);
+                                            a1 = make_float3(x1.x, x1.y, x1.z);
+                                            a2 = make_float3(x2.x, x2.y, x2.z);
+                                        } else {
+                                            const uint32_t ta = listed ? s_list[j] : (uint32_t)(ra.x + j);
+                                            a0 = tri_vertex(P.a, ta, 0);
+                                            a1 = tri_vertex(P.a, ta, 1);
+                                            a2 = tri_vertex(P.a, ta, 2);
+                                        }
+                                        if (!tri_box_meets(a0, a1, a2, blo, bhi)) continue;
+                                        ++tests;
+                                        hit = seg_tri_exact(a0, a1, b0, b1, b2, pc) || seg_tri_exact(a1, a2, b0, b1, b2, pc) ||
+                                              seg_tri_exact(a2, a0, b0, b1, b2, pc) || seg_tri_exact(b0, b1, a0, a1, a2, pc) ||
+                                              seg_tri_exact(b1, b2, a0, a1, a2, pc) || seg_tri_exact(b2, b0, a0, a1, a2, pc);
+                                    }
+                                }
+                            }
+                            meets = __syncthreads_or(hit) != 0;
+                        }
                     }
                 }
             }
-        }
-        if (tid == 0) {
-            if (undecided) {
-                atomicAdd(P.fallback, 1ull);
-            } else if (!meets) {
-                const unsigned long long pos = atomicAdd(P.count, 1ull);
-                if (pos < P.cap) P.out[pos] = key;
+            if (tid == 0) {
+                if (undecided) {
+                    atomicAdd(P.fallback, 1ull);
+                } else if (!meets) {
+                    const unsigned long long pos = atomicAdd(P.count, 1ull);
+                    if (pos < P.cap) P.out[pos] = key;
+                }
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
     flush_counter(&P.ctr->tri_tests, tests);
     flush_counter(&P.ctr->fp32_ambiguous, pc.fp32_ambiguous);
@@ -2404,7 +2419,7 @@ int launch_containment_pairs(pierce_ctx* ctx, const uint64_t* ptable, const uint
     P.cap = cap;
     P.fallback = fallback;
     P.ctr = ctx->d_counters;
-    const int64_t blocks = std::min<int64_t>((int64_t)pslots, (int64_t)ctx->sm_count * 8);
+    const int64_t blocks = std::min<int64_t>(((int64_t)pslots + kPairThreads - 1) / kPairThreads, (int64_t)ctx->sm_count * 8);
     k_containment_pairs<<<(unsigned)std::max<int64_t>(blocks, 1), kPairThreads, 0, ctx->stream>>>(P);
     ctx->launches += 1;
     return check_cuda(cudaGetLastError(), "containment by pairs");
