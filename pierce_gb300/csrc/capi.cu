@@ -603,7 +603,8 @@ void pierce_dataset_destroy(pierce_dataset* ds) {
     cudaDeviceSynchronize();
     void* ptrs[] = {ds->d_vertices, ds->d_indices,  ds->d_tri_to_object, ds->d_edges,  ds->d_edge_src,
                     ds->d_soup,     ds->d_nodes,    ds->d_first_vertex,  ds->d_obj_box, ds->d_obj_part,
-                    ds->d_part_roots, ds->d_obj_range, ds->d_tri_chunk_box, ds->d_edge_chunk_box};
+                    ds->d_part_roots, ds->d_obj_range, ds->d_tri_chunk_box, ds->d_edge_chunk_box,
+                    ds->d_obj_hier, ds->d_grid, ds->d_grid_entries};
     for (void* p : ptrs) dataset_free(p);
     // the frees complete now, so the next dataset of the context reuses the memory
     cudaStreamSynchronize(0);
@@ -623,8 +624,16 @@ int pierce_dataset_set_partitions(pierce_ctx* ctx, pierce_dataset* ds, const int
     cudaDeviceSynchronize();  // dataset_free needs an idle device
     dataset_free(ds->d_obj_part);
     dataset_free(ds->d_part_roots);
+    dataset_free(ds->d_obj_hier);  // the object hierarchy follows the partitions
+    dataset_free(ds->d_grid);
+    dataset_free(ds->d_grid_entries);
     ds->d_obj_part = nullptr;
     ds->d_part_roots = nullptr;
+    ds->d_obj_hier = nullptr;
+    ds->obj_hier_ready = 0;
+    ds->d_grid = nullptr;
+    ds->d_grid_entries = nullptr;
+    ds->grid_ready = 0;
     ds->num_parts = 0;
     const bool was_built = ds->built != 0;
     ds->built = 0;
@@ -1108,16 +1117,34 @@ struct Join {
 
     // Column grids of both sides' object boxes (scratch slots meta/entries):
     // both counting passes, then the two sizes read back together.
+    // Column grids of the sides that are parity targets.  A grid depends
+    // only on its dataset's object boxes: the first eager join builds it into
+    // memory the dataset keeps; a join graph (whose plan fixes every host
+    // read) and a join short of memory use the context's scratch instead.
     int column_grids(bool side_a = true, bool side_b = true) {
         const DevDataset* v[2] = {&va, &vb};
+        pierce_dataset* ds[2] = {A, B};
         const int meta_slot[2] = {SLOT_GRID_A, SLOT_GRID_B}, entries_slot[2] = {SLOT_GRID_A_ENTRIES, SLOT_GRID_B_ENTRIES};
         ColumnGrid* g[2] = {&gridA_, &gridB_};
-        const bool want[2] = {side_a, side_b};
+        bool want[2] = {side_a, side_b};
+        for (int sd = 0; sd < 2; ++sd)
+            if (want[sd] && ds[sd]->grid_ready) {
+                *g[sd] = ds[sd]->grid;
+                want[sd] = false;
+            }
+        if (A == B && want[0] && want[1]) want[1] = false;  // one dataset on both sides: one grid
         void* pm[2] = {nullptr, nullptr};
+        bool keep[2] = {false, false};
         const int32_t* total[2] = {nullptr, nullptr};
         for (int sd = 0; sd < 2; ++sd) {
             if (!want[sd]) continue;
-            if (int s = scratch(ctx, meta_slot[sd], column_grid_bytes(v[sd]->num_objects), &pm[sd])) return s;
+            const size_t mb = column_grid_bytes(v[sd]->num_objects);
+            if (!ctx->plan) {
+                if (cudaMallocFromPoolAsync(&pm[sd], mb, ctx->pool, ctx->stream) == cudaSuccess) keep[sd] = true;
+                else cudaGetLastError();
+            }
+            if (!keep[sd])
+                if (int s = scratch(ctx, meta_slot[sd], mb, &pm[sd])) return s;
             if (int s = column_grid_count(ctx, *v[sd], pm[sd], &total[sd])) return s;
         }
         for (int sd = 0; sd < 2; ++sd) {
@@ -1125,9 +1152,35 @@ struct Join {
             int64_t n = 0;
             if (int s = host_value(ctx, total[sd], 4, &n, "column grid size")) return s;
             void* pe = nullptr;
-            if (int s = scratch(ctx, entries_slot[sd], 4 * (size_t)std::max<int64_t>(n, 1), &pe)) return s;
+            const size_t eb = 4 * (size_t)std::max<int64_t>(n, 1);
+            if (keep[sd] && cudaMallocFromPoolAsync(&pe, eb, ctx->pool, ctx->stream) != cudaSuccess) {
+                cudaGetLastError();
+                pe = nullptr;
+            }
+            if (!pe) {
+                // the grid stays with this join: copy its meta to scratch too
+                if (keep[sd]) {
+                    void* pm2 = nullptr;
+                    const size_t mb = column_grid_bytes(v[sd]->num_objects);
+                    if (int s = scratch(ctx, meta_slot[sd], mb, &pm2)) return s;
+                    cudaMemcpyAsync(pm2, pm[sd], mb, cudaMemcpyDeviceToDevice, ctx->stream);
+                    cudaFreeAsync(pm[sd], ctx->stream);
+                    pm[sd] = pm2;
+                    keep[sd] = false;
+                }
+                if (int s = scratch(ctx, entries_slot[sd], eb, &pe)) return s;
+            }
             if (int s = column_grid_fill(ctx, *v[sd], pm[sd], (int32_t*)pe, g[sd])) return s;
+            if (keep[sd]) {
+                if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "column grid")) return s;
+                ds[sd]->d_grid = pm[sd];
+                ds[sd]->d_grid_entries = pe;
+                ds[sd]->device_bytes += column_grid_bytes(v[sd]->num_objects) + eb;
+                ds[sd]->grid = *g[sd];
+                ds[sd]->grid_ready = 1;
+            }
         }
+        if (A == B && side_a && side_b) gridB_ = gridA_;
         return PIERCE_OK;
     }
 
@@ -1159,19 +1212,35 @@ struct Join {
     }
 
     // BVH of one dataset's object boxes (degenerate triangles lo, hi, hi).
+    // The hierarchy over ds's object boxes (degenerate triangles lo, hi, hi),
+    // with its four-wide copy.  It depends only on the dataset, so the first
+    // join builds it into memory the dataset keeps (freed with the dataset)
+    // and later joins reuse it; where that memory cannot be had (or a graph
+    // is being captured) it goes to the context's scratch for this join.
     int object_bvh(pierce_dataset* ds, int slot, int slot4, DevDataset* out) {
+        if (ds->obj_hier_ready) {
+            *out = ds->obj_hier;
+            return PIERCE_OK;
+        }
         const int64_t n = ds->num_objects;
+        const size_t m = (size_t)std::max<int64_t>(n, 1);
+        const size_t bytes = 16 * m + (48 + 64) * m + 256 + 8 * (size_t)ds->num_parts;
+        const size_t bytes4 = sizeof(Node4) * m + 256;
         void* p = nullptr;
-        const size_t bytes = 16 * (size_t)std::max<int64_t>(n, 1) + (48 + 64) * (size_t)std::max<int64_t>(n, 1) + 256 +
-                             8 * (size_t)ds->num_parts;
-        if (int s = scratch(ctx, slot, bytes, &p)) return s;
+        bool keep = false;
+        if (!capturing(ctx)) {
+            if (cudaMallocFromPoolAsync(&p, bytes + bytes4, ctx->pool, ctx->stream) == cudaSuccess) keep = true;
+            else cudaGetLastError();
+        }
+        if (!keep)
+            if (int s = scratch(ctx, slot, bytes, &p)) return s;
         uint32_t* idx = static_cast<uint32_t*>(p);
-        int32_t* t2o = reinterpret_cast<int32_t*>(idx + 3 * std::max<int64_t>(n, 1));
-        char* q = reinterpret_cast<char*>(t2o + std::max<int64_t>(n, 1));
+        int32_t* t2o = reinterpret_cast<int32_t*>(idx + 3 * m);
+        char* q = reinterpret_cast<char*>(t2o + m);
         q += (256 - ((uintptr_t)q & 255)) & 255;
         float4* soup = reinterpret_cast<float4*>(q);
-        Node* nodes = reinterpret_cast<Node*>(soup + 3 * std::max<int64_t>(n, 1));
-        int2* roots = ds->num_parts ? reinterpret_cast<int2*>(nodes + std::max<int64_t>(n, 1)) : nullptr;
+        Node* nodes = reinterpret_cast<Node*>(soup + 3 * m);
+        int2* roots = ds->num_parts ? reinterpret_cast<int2*>(nodes + m) : nullptr;
         if (int s = launch_object_pseudo_tris(ctx, (int32_t)n, idx, t2o)) return s;
         BvhShape shape;
         if (int s = build_lbvh(ctx, ds->d_obj_box, idx, t2o, nullptr, n, 1, soup, nodes, &shape, nullptr,
@@ -1186,7 +1255,21 @@ struct Join {
         out->obj_part = ds->d_obj_part;
         out->part_roots = roots;
         out->soup_boxes = 1;
-        return wide_nodes(*out, shape.num_nodes, slot4, true);
+        if (!keep) return wide_nodes(*out, shape.num_nodes, slot4, true);
+        if (shape.num_nodes > 0 && !shape.root_is_leaf) {
+            char* q4 = static_cast<char*>(p) + bytes;
+            q4 += (256 - ((uintptr_t)q4 & 255)) & 255;
+            Node4* n4 = reinterpret_cast<Node4*>(q4);
+            if (int s = collapse4(ctx, nodes, (int64_t)shape.num_nodes, n4)) return s;
+            out->nodes4 = n4;
+        }
+        // complete before another stream of another context reads it
+        if (int s = check_cuda(cudaStreamSynchronize(ctx->stream), "object hierarchy")) return s;
+        ds->d_obj_hier = p;
+        ds->obj_hier = *out;
+        ds->obj_hier_ready = 1;
+        ds->device_bytes += bytes + bytes4;
+        return PIERCE_OK;
     }
 
     // Per-join BVHs over the triangles that can take part in an overlap pair

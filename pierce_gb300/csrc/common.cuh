@@ -229,6 +229,18 @@ struct pierce_dataset {
     float* d_tri_chunk_box = nullptr;
     float* d_edge_chunk_box = nullptr;
     int edges_grouped = 0;  // edge sources non-decreasing (edges grouped by object)
+    // hierarchy over the object boxes (with its four-wide copy), which the
+    // per-join path culls against: built by the first join that needs it
+    // and kept, since it depends only on the objects and their partitions
+    void* d_obj_hier = nullptr;
+    pgpu::DevDataset obj_hier{};
+    int obj_hier_ready = 0;
+    // xy column grid over the object boxes (parity candidates when this
+    // dataset is the target), kept the same way
+    void* d_grid = nullptr;          // bounds, counts and offsets
+    void* d_grid_entries = nullptr;  // object ids per cell
+    pgpu::ColumnGrid grid{};
+    int grid_ready = 0;
 
     pgpu::DevDataset view() const {
         pgpu::DevDataset v;
