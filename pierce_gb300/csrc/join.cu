@@ -1461,36 +1461,40 @@ __device__ __forceinline__ int seg_shard(const float4& p, const float4& q, int n
 template <int GMAX>
 __device__ __forceinline__ uint32_t group_unique_edges(const float4* __restrict__ soup, int64_t first, int64_t last,
                                                        float3& lo, float3& hi, int shard_index, int shard_count) {
-    constexpr int NV = 3 * GMAX;
+    static_assert(3 * GMAX <= 16, "vertex ids are packed in 4 bits");
     const int nv = 3 * (int)(last - first);
-    float4 v[NV];
-    int cid[NV];
+    const float4* v = soup + 3 * first;
     lo = make_float3(3.4e38f, 3.4e38f, 3.4e38f);
     hi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        cid[i] = i;
-        if (i < nv) {
-            v[i] = __ldg(soup + 3 * first + i);
-            lo.x = fminf(lo.x, v[i].x); lo.y = fminf(lo.y, v[i].y); lo.z = fminf(lo.z, v[i].z);
-            hi.x = fmaxf(hi.x, v[i].x); hi.y = fmaxf(hi.y, v[i].y); hi.z = fmaxf(hi.z, v[i].z);
-#pragma unroll
-            for (int j = 0; j < i; ++j)
-                if (cid[i] == i && same_point(v[j], v[i])) cid[i] = cid[j];
-        }
+    // vertex i's id: the first vertex of the group with its coordinates
+    // (4 bits each; the vertices are read again rather than kept)
+    uint64_t ids = 0;
+    for (int i = 0; i < nv; ++i) {
+        const float4 a = __ldg(v + i);
+        lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+        hi.x = fmaxf(hi.x, a.x); hi.y = fmaxf(hi.y, a.y); hi.z = fmaxf(hi.z, a.z);
+        uint64_t c = (uint64_t)i;
+        for (int j = 0; j < i; ++j)
+            if (same_point(__ldg(v + j), a)) {
+                c = (ids >> (4 * j)) & 15u;
+                break;
+            }
+        ids |= c << (4 * i);
     }
-    int key[NV];
+    // edge e = 3 t + k joins vertices 3 t + k and 3 t + (k + 1) % 3; its key is
+    // the unordered id pair (8 bits each, packed in two words)
+    uint64_t keys[2] = {0, 0};
     uint32_t mask = 0;
-#pragma unroll
-    for (int e = 0; e < NV; ++e) {
-        const int t = e / 3, k = e % 3;
-        const int a = cid[3 * t + k], b = cid[3 * t + (k == 2 ? 0 : k + 1)];
-        key[e] = a < b ? a * 64 + b : b * 64 + a;
-        bool dup = e >= nv;
-#pragma unroll
-        for (int f = 0; f < e; ++f) dup = dup || key[f] == key[e];
-        if (!dup && shard_count > 1)
-            dup = seg_shard(v[3 * t + k], v[3 * t + (k == 2 ? 0 : k + 1)], shard_count) != shard_index;
+    for (int e = 0; e < nv; ++e) {
+        const int t = e / 3, k = e - 3 * t;
+        const int ia = 3 * t + k, ib = 3 * t + (k == 2 ? 0 : k + 1);
+        const uint32_t a = (uint32_t)(ids >> (4 * ia)) & 15u, b = (uint32_t)(ids >> (4 * ib)) & 15u;
+        const uint64_t key = a < b ? a * 16 + b : b * 16 + a;
+        bool dup = false;
+        for (int f = 0; f < e && !dup; ++f) dup = ((keys[f >> 3] >> (8 * (f & 7))) & 255u) == key;
+        if (e < 8) keys[0] |= key << (8 * e);
+        else keys[1] |= key << (8 * (e - 8));
+        if (!dup && shard_count > 1) dup = seg_shard(__ldg(v + ia), __ldg(v + ib), shard_count) != shard_index;
         if (!dup) mask |= 1u << e;
     }
     return mask;
