@@ -152,10 +152,10 @@ def edge_ray_bytes(src, tgt, raw_hits):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced
 # segment of the two edge-ray launches of one join, from one full-size ncu
-# capture of this build (one pass per launch): the tube join's 3.876 GB over
-# 67,917,789 segments, the ellipsoid intersection join's 250.2 MB over
+# capture of this build (one pass per launch): the tube join's 3.896 GB over
+# 67,917,789 segments, the ellipsoid intersection join's 250.3 MB over
 # 4,148,442 segments.
-EDGE_RAY_DRAM_BYTES_PER_RAY = {"tubes": 57.06, "ellipsoids": 60.32}
+EDGE_RAY_DRAM_BYTES_PER_RAY = {"tubes": 57.37, "ellipsoids": 60.34}
 
 
 def traffic_estimate(rays, workload="tubes"):
