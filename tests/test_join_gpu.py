@@ -339,3 +339,19 @@ def test_containment_pairs_and_their_fallback(ctx, sizing):
         assert np.array_equal(keys(got), want), name
         assert got.stats["containment_by_pairs"] == by_pairs[name], name
     assert len(O.containment_keys(*big)) > 5 and len(O.containment_keys(*tight)) == 1
+
+
+def test_object_hierarchy_and_grid_kept_per_dataset(ctx):
+    """A dataset's object hierarchy and column grid are built by its first
+    join and kept: the next join on the same datasets launches fewer
+    kernels and returns the same pairs; fresh datasets build them again."""
+    A, B = pg.icospheres(71, 200, 2, hi=40.0), pg.icospheres(72, 200, 2, hi=40.0)
+    want = O.intersection_keys(A, B)
+    da, db = ds(ctx, A), ds(ctx, B)
+    r1 = J.intersection_join(ctx, da, db)
+    r2 = J.intersection_join(ctx, da, db)
+    assert np.array_equal(keys(r1), want) and np.array_equal(keys(r2), want)
+    assert r2.stats["launches"] < r1.stats["launches"]
+    r3 = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B))
+    assert np.array_equal(keys(r3), want)
+    assert r3.stats["launches"] == r1.stats["launches"]
