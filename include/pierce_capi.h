@@ -148,8 +148,9 @@ typedef struct pierce_tuning {
 
 /* Where a join's edge rays come from (pierce_join_opts.edge_source). */
 enum pierce_edge_source {
-    PIERCE_EDGES_AUTO = 0,       /* triangles wherever the join builds grouped per-join hierarchies, else the
-                                    dataset's edges (triangles when the dataset has none) */
+    PIERCE_EDGES_AUTO = 0,       /* per side: the kept triangles' edges where the join builds grouped
+                                    per-join hierarchies and the side keeps fewer than half of its
+                                    triangles, else the dataset's edges (triangles when it has none) */
     PIERCE_EDGES_DATASET = 1,    /* the dataset's edge list (the `.pre` edges) */
     PIERCE_EDGES_TRIANGLES = 2   /* the edges of the triangles kept for the join's per-join hierarchies, each
                                     segment of a leaf group once (needs active_bvh) */

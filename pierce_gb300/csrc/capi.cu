@@ -919,12 +919,23 @@ struct Join {
     int ray_entry_group[2] = {1, 1};
     // rays the launches of direction d index (list capacity or edge count)
     int64_t rays_of(int d) const { return ray_soup[d] ? ray_bound[d] : (int64_t)(d ? B->ne : A->ne); }
-    // whether side d takes its rays from its kept triangles
+    // Whether side d takes its rays from its kept triangles.  Automatically:
+    // always without dataset edges; after grouped culling, when the side
+    // keeps fewer than half of its triangles.  A side that keeps most of them
+    // (a dense join) traces its own edge list instead: the kept triangles'
+    // edges repeat every edge two triangles of different groups share, and
+    // in dense joins those repeats cost more raw hits than the finer culling
+    // saves (measured on 40 sweep joins: 6.46 against 4.60 s on the densest,
+    // with 965 M against 644 M raw hits; the tube and ellipsoid joins keep
+    // 1.5-17 % per side and run faster on the kept triangles).
     bool triangle_rays(int d, bool grouped) const {
         const pierce_dataset* ds = d ? B : A;
         if (o.edge_source == PIERCE_EDGES_TRIANGLES) return true;
         if (o.edge_source == PIERCE_EDGES_DATASET) return false;
-        return grouped || (ds->ne == 0 && ds->nt > 0);
+        if (ds->ne == 0) return ds->nt > 0;
+        if (!grouped) return false;
+        const int64_t kept = (d ? vb : va).num_tris;
+        return 2 * kept < (int64_t)ds->nt;
     }
     // Ray lists of the sides that trace their kept triangles' edges: the
     // edges of the side's per-join soup, G triangles per group, listed group
