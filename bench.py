@@ -483,14 +483,18 @@ def main_batched(args):
 TRIANGLE_FIELDS = ("vertices", "indices", "tri_to_object")
 
 
-def pinned_view(G, keep: list):
+def pinned_view(G, keep: list, edges: bool = True):
     """A pierce_mesh_view over pinned host copies of G's arrays (the copies
-    are appended to keep).  Returns (view, bytes of the triangle arrays,
+    are appended to keep; without `edges`, the edge arrays are left out and
+    the view holds none).  Returns (view, bytes of the triangle arrays,
     bytes of the edge arrays)."""
     import torch
     from pierce_gb300 import capi
     ptr, nbytes = {}, {}
     for field in ("vertices", "indices", "tri_to_object", "edge_starts", "edge_ends", "edge_src"):
+        if not edges and field not in TRIANGLE_FIELDS:
+            ptr[field], nbytes[field] = 0, 0
+            continue
         src = np.ascontiguousarray(getattr(G, field))
         pin = torch.empty(max(src.nbytes, 1), dtype=torch.uint8, pin_memory=True)
         pin.numpy()[:src.nbytes] = src.view(np.uint8).reshape(-1)
@@ -502,7 +506,7 @@ def pinned_view(G, keep: list):
     v.indices, v.num_triangles = ptr["indices"], G.num_triangles
     v.tri_to_object = ptr["tri_to_object"]
     v.edge_starts, v.edge_ends, v.edge_src = ptr["edge_starts"], ptr["edge_ends"], ptr["edge_src"]
-    v.num_edges, v.num_objects = G.num_edges, G.num_objects
+    v.num_edges, v.num_objects = (G.num_edges if edges else 0), G.num_objects
     tri = sum(nbytes[f] for f in TRIANGLE_FIELDS)
     return v, tri, sum(nbytes.values()) - tri
 
@@ -548,11 +552,69 @@ class E2E:
         return st.as_dict(), keys, 8 * cap
 
 
+def tubes_replica_tail(args, ctx, da, db, A, B, tuned_o, tuned_ms, keys_t, launches, clocks, rank, world,
+                       local_rank, dist):
+    """The tube line under torchrun: every rank has timed its replica of the
+    device-resident join; each now times the end-to-end join from pinned
+    host buffers without edges (the tuned form's upload), the times are
+    maxed over ranks, and rank 0 prints the line."""
+    import torch
+    from pierce_gb300 import capi
+    from pierce_gb300 import join as J
+    da.close()
+    db.close()
+    ctx.release_scratch()
+    keep = []
+    va, a_tri, _ = pinned_view(A, keep, edges=False)
+    vb, b_tri, _ = pinned_view(B, keep, edges=False)
+    e2e = E2E(ctx, (va, vb), out_pairs=max(1 << 22, 2 * len(keys_t)))
+    upload_tri = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
+    tri_o = capi.JoinOpts.from_buffer_copy(tuned_o)
+    if tri_o.edge_source == capi.EDGES_DATASET:
+        tri_o.edge_source = capi.EDGES_AUTO
+    _, keys_e, d2h = e2e.step(tri_o, upload_tri, want_keys=True)
+    ctx.synchronize()
+    dist.barrier()
+    n = max(1, min(args.steps, 5))
+    t1 = time.perf_counter()
+    for _ in range(n):
+        e2e.step(tri_o, upload_tri, None)
+    e2e_s = max_over_ranks((time.perf_counter() - t1) / n, dist)
+    identical = bool(np.array_equal(keys_e, keys_t))
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": world * 1000.0 / tuned_ms, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": tuned_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (exact predicates)", "data": "synthetic",
+            "config": tubes_config(args.scale),
+            "settings": {"parallelism": f"replicas x{world}", "sizing": "learned",
+                         "precision": "exact (fp32 filter, fp64, expansions)"},
+            "pairs": len(keys_t), "identical_e2e": identical,
+            "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(world * (a_tri + b_tri)),
+                    "d2h_bytes_per_step": int(world * d2h), "ms_per_step": 1000.0 * e2e_s, "edges_uploaded": False},
+            "gpu_launches": int(launches) * world, "clocks": clocks.summary(local_rank),
+        }
+        print(json.dumps(line))
+    dist.destroy_process_group()
+    return 0
+
+
 def main_tubes(args):
     """Large tube-mesh overlap join (the default line): the tuned form with
     inputs resident in HBM (value), end to end through the C ABI (e2e), the
-    plain GPU form, the edge-ray roofline and the CPU oracle on a sample."""
+    plain GPU form, the edge-ray roofline and the CPU oracle on a sample.
+    Under torchrun every rank runs a replica of the join on its own GPU
+    (weak scaling, max time over ranks); rank 0 alone adds the plain form,
+    the CPU sample and the upload with edges, and prints the line."""
     import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
     import pierce_gb300 as pg
     from pierce_gb300 import capi
     from pierce_gb300 import join as J
@@ -572,7 +634,7 @@ def main_tubes(args):
     # CPU oracle on a sample: the first k tubes against every ellipsoid near them
     cpu, cpu_touch, sample_keys, ref_sem = None, None, None, None
     k = max(1, min(n_tubes, args.cpu_sample_tubes))
-    if not (args.no_cpu_baseline or args.only_tuned):
+    if not (args.no_cpu_baseline or args.only_tuned or rank != 0):
         tb = time.perf_counter()
         As, Bs, near = tube_sample(k, args.scale, inst_b, boxes=mesh_boxes(B))
         prep_s = time.perf_counter() - tb
@@ -597,14 +659,14 @@ def main_tubes(args):
         log(f"cpu sample: {k} tubes vs {len(near)} ellipsoids: {cpu_s:.2f} s ({prep_s:.1f} s set-up), "
             f"{len(sample_keys)} pairs; TOUCH {touch_s:.2f} s; reference semantics {ref_sem}")
 
-    ctx = J.Context(0)
+    ctx = J.Context(local_rank)
     upload = J.default_tuning(leaf_size=args.leaf_size, defer_build=1)
     model = S.SizingModel.load(ctx, S.TRAINED_MODEL)
     tuned_o = J.make_opts(predicate="overlap", sizing="learned", sizing_model=model)
     plain_o = J.make_opts(predicate="overlap", sizing="two_pass", precision="fp32", cull_objects=False,
                           defer_exact=False, active_bvh=False)
     plain_build = J.default_tuning(leaf_size=args.plain_leaf_size)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local_rank))
 
     # device-resident legs: inputs already in HBM (profiling runs skip the
     # edge arrays, which only the plain form reads)
@@ -623,8 +685,10 @@ def main_tubes(args):
         log(f"autotuned in {time.perf_counter() - ta:.1f} s over {n_trials} trials: {autotuned}")
     for _ in range(max(args.warmup, 3)):
         r = J.run_join(ctx, da, db, tuned_o, download=False)
+    if dist:
+        dist.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(clocks_path("clocks_tubes.csv"))
+    clocks = Clocks(clocks_path(f"clocks_tubes_rank{rank}.csv" if world > 1 else "clocks_tubes.csv"))
     l0 = ctx.kernel_launches
     stats = []
     with clocks:
@@ -640,9 +704,9 @@ def main_tubes(args):
         if args.only_tuned:
             torch.cuda.nvtx.range_pop()
     launches = ctx.kernel_launches - l0
-    tuned_ms = e0.elapsed_time(e1) / args.steps
+    tuned_ms = max_over_ranks(e0.elapsed_time(e1), dist) / args.steps
     st = stats[-1]
-    if args.only_tuned:
+    if args.only_tuned and world == 1:
         print(json.dumps({"metric": METRIC, "value": 1000.0 / tuned_ms, "unit": UNIT, "ms_per_step": tuned_ms,
                           "partial": "only the tuned device-resident joins", "config": tubes_config(args.scale),
                           "autotuned": autotuned,
@@ -654,6 +718,9 @@ def main_tubes(args):
     tuned = J.run_join(ctx, da, db, tuned_o)
     keys_t = J.pairs_to_keys(tuned.pairs)
     ctx.release_scratch()
+    if world > 1:
+        return tubes_replica_tail(args, ctx, da, db, A, B, tuned_o, tuned_ms, keys_t, launches, clocks, rank,
+                                  world, local_rank, dist)
 
     # plain form on the same resident data: dataset hierarchies + two-pass join
     def plain_dev():
