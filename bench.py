@@ -483,16 +483,19 @@ def main_batched(args):
 TRIANGLE_FIELDS = ("vertices", "indices", "tri_to_object")
 
 
-def pinned_view(G, keep: list, edges: bool = True):
+def pinned_view(G, keep: list, edges: bool = True, ranges: bool = False):
     """A pierce_mesh_view over pinned host copies of G's arrays (the copies
     are appended to keep; without `edges`, the edge arrays are left out and
-    the view holds none).  Returns (view, bytes of the triangle arrays,
-    bytes of the edge arrays)."""
+    the view holds none; with `ranges` and a mesh stored object by object,
+    the objects go as triangle offsets instead of per-triangle ids).
+    Returns (view, bytes of the triangle arrays, bytes of the edge arrays)."""
     import torch
     from pierce_gb300 import capi
+    from pierce_gb300 import join as J
+    off = J.object_offsets(G.tri_to_object, G.num_objects) if ranges else None
     ptr, nbytes = {}, {}
     for field in ("vertices", "indices", "tri_to_object", "edge_starts", "edge_ends", "edge_src"):
-        if not edges and field not in TRIANGLE_FIELDS:
+        if (not edges and field not in TRIANGLE_FIELDS) or (field == "tri_to_object" and off is not None):
             ptr[field], nbytes[field] = 0, 0
             continue
         src = np.ascontiguousarray(getattr(G, field))
@@ -508,7 +511,30 @@ def pinned_view(G, keep: list, edges: bool = True):
     v.edge_starts, v.edge_ends, v.edge_src = ptr["edge_starts"], ptr["edge_ends"], ptr["edge_src"]
     v.num_edges, v.num_objects = (G.num_edges if edges else 0), G.num_objects
     tri = sum(nbytes[f] for f in TRIANGLE_FIELDS)
-    return v, tri, sum(nbytes.values()) - tri
+    if off is not None:
+        keep.append(off)
+        v.object_offsets = off.ctypes.data
+        tri += off.nbytes
+    return v, tri, sum(nbytes.values()) - tri + (off.nbytes if off is not None else 0)
+
+
+def range_view(v, G, keep: list):
+    """A copy of view v (over the same pinned arrays) without edges and, when
+    G is stored object by object, with its objects as triangle offsets
+    instead of per-triangle ids.  Returns (view, bytes it uploads)."""
+    from pierce_gb300 import capi
+    from pierce_gb300 import join as J
+    r = capi.MeshView.from_buffer_copy(v)
+    r.edge_starts = r.edge_ends = r.edge_src = None
+    r.num_edges = 0
+    nbytes = 12 * G.vertices.shape[0] + 12 * G.num_triangles
+    off = J.object_offsets(G.tri_to_object, G.num_objects)
+    if off is None:
+        return r, nbytes + 4 * G.num_triangles
+    keep.append(off)
+    r.tri_to_object = None
+    r.object_offsets = off.ctypes.data
+    return r, nbytes + off.nbytes
 
 
 class E2E:
@@ -565,8 +591,8 @@ def tubes_replica_tail(args, ctx, da, db, A, B, tuned_o, tuned_ms, keys_t, launc
     db.close()
     ctx.release_scratch()
     keep = []
-    va, a_tri, _ = pinned_view(A, keep, edges=False)
-    vb, b_tri, _ = pinned_view(B, keep, edges=False)
+    va, a_tri, _ = pinned_view(A, keep, edges=False, ranges=True)
+    vb, b_tri, _ = pinned_view(B, keep, edges=False, ranges=True)
     e2e = E2E(ctx, (va, vb), out_pairs=max(1 << 22, 2 * len(keys_t)))
     upload_tri = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
     tri_o = capi.JoinOpts.from_buffer_copy(tuned_o)
@@ -757,13 +783,18 @@ def main_tubes(args):
     vb, b_tri, b_edge = pinned_view(B, keep)
     e2e = E2E(ctx, (va, vb), out_pairs=max(1 << 22, 2 * len(keys_t)))
     upload_tri = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
+    # the tuned form's upload: the same pinned arrays, no edges, and the
+    # objects as triangle offsets (both meshes are stored object by object)
+    ra, ra_tri = range_view(va, A, keep)
+    rb, rb_tri = range_view(vb, B, keep)
+    e2e_tri = E2E(ctx, (ra, rb), out_pairs=max(1 << 22, 2 * len(keys_t)))
 
-    def timed(opts, up, build, n):
-        e2e.step(opts, up, build)
+    def timed(opts, up, build, n, runner=e2e):
+        runner.step(opts, up, build)
         ctx.synchronize()
         t1 = time.perf_counter()
         for _ in range(n):
-            e2e.step(opts, up, build)
+            runner.step(opts, up, build)
         dt = (time.perf_counter() - t1) / n
         ctx.release_scratch()
         return dt
@@ -772,9 +803,9 @@ def main_tubes(args):
     tri_o = capi.JoinOpts.from_buffer_copy(tuned_o)
     if tri_o.edge_source == capi.EDGES_DATASET:
         tri_o.edge_source = capi.EDGES_AUTO
-    _, keys_e, d2h = e2e.step(tri_o, upload_tri, want_keys=True)
+    _, keys_e, d2h = e2e_tri.step(tri_o, upload_tri, want_keys=True)
     e2e_identical = bool(np.array_equal(keys_e, keys_t))
-    e2e_s = timed(tri_o, upload_tri, None, max(1, min(args.steps, 5)))
+    e2e_s = timed(tri_o, upload_tri, None, max(1, min(args.steps, 5)), e2e_tri)
     e2e_edges_s = timed(tuned_o, upload, None, max(1, min(args.steps, 2)))
     plain_e2e_s = timed(plain_o, upload, plain_build, max(1, min(args.steps, 2)))
     log(f"e2e tuned {1000 * e2e_s:.1f} ms ({1000 * e2e_edges_s:.1f} ms uploading the edges too), "
@@ -815,9 +846,9 @@ def main_tubes(args):
                   "e2e": {"value": 1.0 / plain_e2e_s, "ms_per_step": 1000.0 * plain_e2e_s,
                           "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)},
                   "e2e_speedup_tuned": plain_e2e_s / e2e_s},
-        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(a_tri + b_tri),
+        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(ra_tri + rb_tri),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s,
-                "edges_uploaded": False,
+                "edges_uploaded": False, "objects_as_ranges": True,
                 "with_edge_upload": {"value": 1.0 / e2e_edges_s, "ms_per_step": 1000.0 * e2e_edges_s,
                                      "h2d_bytes_per_step": int(a_tri + b_tri + a_edge + b_edge)}},
         "reference_semantics_diff": ref_sem,
@@ -1076,7 +1107,12 @@ def main_ellipsoids(args):
             v.num_objects = G.num_objects
             return v
 
-        va, vb = view_of("A", A), view_of("B", B)
+        # both meshes are stored object by object: the objects go as
+        # triangle offsets (the library writes the per-triangle ids)
+        keep_off = []
+        va, ha_bytes = range_view(view_of("A", A), A, keep_off)
+        vb, hb_bytes = range_view(view_of("B", B), B, keep_off)
+        h2d = ha_bytes + hb_bytes
         upload_only = J.default_tuning(leaf_size=args.leaf_size, defer_build=1, skip_edges=1)
         out_pairs = torch.empty(8 * (1 << 22), dtype=torch.uint8, pin_memory=True)
 
@@ -1110,7 +1146,7 @@ def main_ellipsoids(args):
         e2e_s = (time.perf_counter() - t0) / e2e_steps
         e2e = {"value": 2.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h_total // e2e_steps), "ms_per_step": 1000.0 * e2e_s,
-               "edges_uploaded": False}
+               "edges_uploaded": False, "objects_as_ranges": len(keep_off) == 2}
 
     cpu, ref_sem = None, None
     if rank == 0 and not args.no_cpu_baseline:

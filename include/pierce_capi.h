@@ -107,6 +107,14 @@ typedef struct pierce_mesh_view {
     const int32_t* edge_src;      /* num_edges source object ids */
     uint64_t num_edges;
     int32_t num_objects;          /* max object id + 1; < 0: computed by the library */
+    /* Optional, for meshes stored object by object (as `.pre` files are):
+       object o holds triangles [object_offsets[o], object_offsets[o + 1]),
+       num_objects + 1 non-decreasing entries from 0 to num_triangles, always
+       in host memory.  When given (num_objects >= 0), tri_to_object may be
+       NULL and is not read: the library writes the per-triangle object ids
+       on the device, so the upload moves 8 bytes per object instead of 4 per
+       triangle. */
+    const int64_t* object_offsets;
 } pierce_mesh_view;
 
 enum pierce_memory { PIERCE_HOST_MEMORY = 0, PIERCE_DEVICE_MEMORY = 1 };

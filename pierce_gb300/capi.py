@@ -49,7 +49,7 @@ NOALLOC_MAX_PAIRS = 1 << 21
 class MeshView(C.Structure):
     _fields_ = [("vertices", V), ("num_vertices", U64), ("indices", V), ("num_triangles", U64),
                 ("tri_to_object", V), ("edge_starts", V), ("edge_ends", V), ("edge_src", V),
-                ("num_edges", U64), ("num_objects", I32)]
+                ("num_edges", U64), ("num_objects", I32), ("object_offsets", V)]
 
 
 # pierce_mesh_instance (pierce_instance.h), as a numpy record type.

@@ -326,6 +326,20 @@ __global__ void k_pack_edges(const float* __restrict__ s, const float* __restric
     }
 }
 
+// Per-triangle object ids from object ranges: triangle t belongs to the
+// object o with off[o] <= t < off[o + 1] (binary search; empty objects skipped).
+__global__ void k_fill_t2o(const int64_t* __restrict__ off, int32_t nobj, int64_t nt, int32_t* __restrict__ t2o) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        int32_t lo = 0, hi = nobj;  // off[lo] <= t < off[hi]
+        while (hi - lo > 1) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (__ldg(off + mid) <= t) lo = mid;
+            else hi = mid;
+        }
+        t2o[t] = lo;
+    }
+}
+
 __global__ void k_max_i32(const int32_t* __restrict__ v, int64_t n, int32_t* out) {
     int32_t m = -1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -662,6 +676,25 @@ int pierce_dataset_build(pierce_ctx* ctx, pierce_dataset* ds, const pierce_tunin
     return build_bvh(ctx, ds, t.leaf_size);
 }
 
+// The per-triangle object ids of a new dataset on `stream`: copied from the
+// view, or written from its object ranges (the offsets go over in one copy).
+static int upload_object_ids(pierce_ctx* ctx, pierce_dataset* ds, const pierce_mesh_view* v, cudaMemcpyKind kind,
+                             cudaStream_t stream) {
+    if (!v->object_offsets)
+        return check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, 4 * ds->nt, kind, stream), "copy t2o");
+    const size_t bytes = 8 * ((size_t)ds->num_objects + 1);
+    void* d_off = nullptr;
+    if (int s = check_cuda(cudaMallocFromPoolAsync(&d_off, bytes, ctx->pool, stream), "object offsets")) return s;
+    if (int s = check_cuda(cudaMemcpyAsync(d_off, v->object_offsets, bytes, cudaMemcpyHostToDevice, stream),
+                           "copy object offsets"))
+        return s;
+    k_fill_t2o<<<grid_for(ctx, (int64_t)ds->nt, 256), 256, 0, stream>>>((const int64_t*)d_off, ds->num_objects,
+                                                                        (int64_t)ds->nt, ds->d_tri_to_object);
+    ctx->launches += 1;
+    if (int s = check_cuda(cudaGetLastError(), "object ids from ranges")) return s;
+    return check_cuda(cudaFreeAsync(d_off, stream), "object offsets");
+}
+
 int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory, const pierce_tuning* tuning,
                           pierce_dataset** out) {
     if (!ctx || !v || !out) return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: null argument");
@@ -670,9 +703,22 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
     // take their rays from the triangles)
     const bool skip_edges = tuning && tuning->skip_edges;
     const uint64_t num_edges = skip_edges ? 0 : v->num_edges;
-    if ((v->num_vertices && !v->vertices) || (v->num_triangles && (!v->indices || !v->tri_to_object)) ||
+    const bool ranges = v->object_offsets != nullptr;
+    if ((v->num_vertices && !v->vertices) || (v->num_triangles && (!v->indices || (!v->tri_to_object && !ranges))) ||
         (num_edges && (!v->edge_starts || !v->edge_ends || !v->edge_src)))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: missing array");
+    if (ranges) {
+        // object ranges: a count is given, the offsets run from 0 to the
+        // triangle count without decreasing
+        if (v->num_objects < 0)
+            return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: object ranges need num_objects");
+        const int64_t* off = v->object_offsets;
+        bool ok = off[0] == 0 && off[v->num_objects] == (int64_t)v->num_triangles;
+        for (int32_t o = 0; ok && o < v->num_objects; ++o) ok = off[o] <= off[o + 1];
+        if (!ok)
+            return set_error(PIERCE_ERR_INVALID_ARGUMENT,
+                             "dataset_create: object offsets must rise from 0 to the triangle count");
+    }
     if (v->num_triangles >= (1ull << 31) || num_edges >= (1ull << 40) || v->num_vertices >= (1ull << 32))
         return set_error(PIERCE_ERR_INVALID_ARGUMENT, "dataset_create: dataset too large for 32-bit ids");
     cudaSetDevice(ctx->device);
@@ -731,9 +777,7 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
                 break;
             if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, cs), "copy indices")))
                 break;
-            if (ob &&
-                (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, cs), "copy t2o")))
-                break;
+            if (ob && (s = upload_object_ids(ctx, ds, v, kind, cs))) break;
             if ((s = check_cuda(cudaEventRecord(ctx->ev_tris, cs), "upload event"))) break;
             if ((s = check_cuda(cudaMemsetAsync(ctx->d_upload_flag, 1, sizeof(int32_t), cs), "upload flag"))) break;
             if (ds->ne) {
@@ -756,8 +800,7 @@ int pierce_dataset_create(pierce_ctx* ctx, const pierce_mesh_view* v, int memory
         const size_t vb = 12 * ds->nv, ib = 12 * ds->nt, ob = 4 * ds->nt;
         if (vb && (s = check_cuda(cudaMemcpyAsync(ds->d_vertices, v->vertices, vb, kind, st), "copy vertices"))) break;
         if (ib && (s = check_cuda(cudaMemcpyAsync(ds->d_indices, v->indices, ib, kind, st), "copy indices"))) break;
-        if (ob && (s = check_cuda(cudaMemcpyAsync(ds->d_tri_to_object, v->tri_to_object, ob, kind, st), "copy t2o")))
-            break;
+        if (ob && (s = upload_object_ids(ctx, ds, v, kind, st))) break;
         if (ds->ne) {
             void *ps = nullptr, *pe = nullptr;
             void* po = ds->d_edge_src;

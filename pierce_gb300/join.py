@@ -101,17 +101,26 @@ class Dataset:
 
     @classmethod
     def from_arrays(cls, ctx: Context, vertices, indices, tri_to_object, edge_starts, edge_ends, edge_src,
-                    num_objects: int = -1, tuning: capi.Tuning | None = None) -> "Dataset":
+                    num_objects: int = -1, tuning: capi.Tuning | None = None,
+                    object_offsets=None) -> "Dataset":
+        """A dataset from host arrays.  With `object_offsets` (num_objects + 1
+        triangle offsets of a mesh stored object by object) the per-triangle
+        object ids are written on the device and `tri_to_object` may be None."""
+        t2o = np.zeros(0, np.int32) if tri_to_object is None else tri_to_object
         arrs = [np.ascontiguousarray(vertices, np.float32), np.ascontiguousarray(indices, np.uint32),
-                np.ascontiguousarray(tri_to_object, np.int32), np.ascontiguousarray(edge_starts, np.float32),
+                np.ascontiguousarray(t2o, np.int32), np.ascontiguousarray(edge_starts, np.float32),
                 np.ascontiguousarray(edge_ends, np.float32), np.ascontiguousarray(edge_src, np.int32)]
         v = capi.MeshView()
         v.vertices, v.num_vertices = arrs[0].ctypes.data, arrs[0].size // 3
         v.indices, v.num_triangles = arrs[1].ctypes.data, arrs[1].size // 3
-        v.tri_to_object = arrs[2].ctypes.data
+        v.tri_to_object = arrs[2].ctypes.data if tri_to_object is not None else None
         v.edge_starts, v.edge_ends, v.edge_src = arrs[3].ctypes.data, arrs[4].ctypes.data, arrs[5].ctypes.data
         v.num_edges = arrs[5].size
         v.num_objects = num_objects
+        if object_offsets is not None:
+            off = np.ascontiguousarray(object_offsets, np.int64)
+            arrs.append(off)
+            v.object_offsets = off.ctypes.data
         h = C.c_void_p()
         t = tuning if tuning is not None else default_tuning()
         check(capi.lib().pierce_dataset_create(ctx.handle, C.byref(v), capi.HOST_MEMORY, C.byref(t), C.byref(h)),
@@ -220,6 +229,17 @@ class JoinResult:
     pairs: np.ndarray          # (n, 2) int32, sorted by (a, b)
     stats: dict
     containment_count: int = 0
+
+
+def object_offsets(tri_to_object, num_objects: int):
+    """Triangle offsets (num_objects + 1, int64) of a mesh stored object by
+    object (object ids non-decreasing over the triangles), or None."""
+    t2o = np.asarray(tri_to_object)
+    if len(t2o) and (np.any(np.diff(t2o) < 0) or t2o[0] < 0 or t2o[-1] >= num_objects):
+        return None
+    off = np.zeros(num_objects + 1, np.int64)
+    np.cumsum(np.bincount(t2o, minlength=num_objects), out=off[1:])
+    return off
 
 
 def make_opts(predicate="overlap", direction="both", sizing="hash", precision="exact", expected_pairs=0,

@@ -355,3 +355,25 @@ def test_object_hierarchy_and_grid_kept_per_dataset(ctx):
     r3 = J.intersection_join(ctx, ds(ctx, A), ds(ctx, B))
     assert np.array_equal(keys(r3), want)
     assert r3.stats["launches"] == r1.stats["launches"]
+
+
+def test_objects_as_triangle_ranges(ctx):
+    """A mesh stored object by object may give its objects as triangle
+    offsets instead of per-triangle ids: the library writes the ids on the
+    device, and the joins are those of the per-triangle form.  Offsets that
+    do not rise from 0 to the triangle count are rejected."""
+    A, B = pg.icospheres(81, 150, 2, hi=35.0), pg.icospheres(82, 150, 2, hi=35.0)
+    def ranged(G):
+        off = J.object_offsets(G.tri_to_object, G.num_objects)
+        assert off is not None
+        return J.Dataset.from_arrays(ctx, G.vertices, G.indices, None, G.edge_starts, G.edge_ends, G.edge_src,
+                                     G.num_objects, object_offsets=off)
+    da, db = ranged(A), ranged(B)
+    assert np.array_equal(da.download()["tri_to_object"], A.tri_to_object)
+    assert np.array_equal(keys(J.intersection_join(ctx, da, db)), O.intersection_keys(A, B))
+    bad = J.object_offsets(A.tri_to_object, A.num_objects).copy()
+    bad[1], bad[2] = bad[2], bad[1]
+    if bad[1] != bad[2]:
+        with pytest.raises(Exception):
+            J.Dataset.from_arrays(ctx, A.vertices, A.indices, None, A.edge_starts, A.edge_ends, A.edge_src,
+                                  A.num_objects, object_offsets=bad)
