@@ -51,7 +51,10 @@
  * Conventions: plain C types only; every call returns a pierce_status and
  * never exits the process; a failed call leaves a message for
  * pierce_last_error() (per host thread).  All device work of a context runs
- * on that context's own CUDA stream; one context per host thread.
+ * on that context's own CUDA stream; one context per host thread.  A dataset
+ * keeps indexes built by its first join (the hierarchy and column grid of
+ * its object boxes), so two host threads must not start the first joins of
+ * one dataset at the same time.
  * Out-of-capacity conditions inside kernels (hash table full, traversal
  * stack overflow, output buffer overflow) come back as status codes.
  * A pair is (object id in dataset A, object id in dataset B), 8 bytes,
