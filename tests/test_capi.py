@@ -112,3 +112,16 @@ def test_python_mirrors_match_the_c_struct_layouts(tmp_path):
         layout = _c_layout(header, {s: _names(t) for s, t in types.items()}, tmp_path)
         for s, t in types.items():
             assert _py_layout(t) == layout[s], s
+
+
+def test_object_offsets_of_meshes_stored_object_by_object():
+    """Triangle offsets for pierce_mesh_view.object_offsets: only for object
+    ids that never decrease over the triangles; empty objects give equal
+    offsets."""
+    from pierce_gb300 import join as J
+    off = J.object_offsets(np.array([0, 0, 1, 1, 1, 3], np.int32), 4)
+    assert off.dtype == np.int64 and off.tolist() == [0, 2, 5, 5, 6]
+    assert J.object_offsets(np.array([0, 1, 0], np.int32), 2) is None
+    assert J.object_offsets(np.array([0, 2], np.int32), 2) is None  # id past the object count
+    assert J.object_offsets(np.zeros(0, np.int32), 3).tolist() == [0, 0, 0, 0]
+
